@@ -1,0 +1,299 @@
+"""Benchmark of the trace-and-accumulate path on GB300.
+
+Workload (one step = one frame of the mid-size scene): 64 objects (rect / circle / flat
+mirror / curved mirror, seed 2), 8 lights x 2^18 primary rays, 16 bounces, 1920x1080
+canvas, int64 fixed-point accumulation, resolve to RGBA16F.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``value``: traced segments per second over the whole job (all ranks), device time of the
+captured graph (trace + bin + raster + resolve) from CUDA events on the library's stream,
+L2 flushed between steps.  ``e2e``: the same metric through the public C ABI with host
+buffers (scene tables uploaded from the host and the RGBA16F image read back every step).
+``--impl reference`` times the CPU restatement of the reference tracer (the reference is
+Rust and cannot be built here) on all host cores over a bounded sample of primaries.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "traced segments/s + accumulated px/s on 1 GB300; p50/p99 scene latency vs plain"
+WORKLOAD = ("mid_scene: 64 objects (rect/circle/mirror/curved mirror, seed 2), 8 lights x 2^18 rays, "
+            "16 bounces, 1920x1080, int64 Q31.32 accumulation, RGBA16F resolve")
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(ws, v: float, device) -> float:
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(stride: int):
+    """Oracle (CPU restatement of tracer.rs) on a bounded sample: trace + raster."""
+    from light_garden_gb300 import workloads as W
+    from oracle import oracle as O
+    pk = W.mid_scene().packed()
+    t0 = time.perf_counter()
+    segs, _, _, st = O.trace(pk, ray_stride=stride, threads=0)
+    t1 = time.perf_counter()
+    _, px = O.raster(segs, pk.params, threads=0)
+    t2 = time.perf_counter()
+    return len(segs), px, t1 - t0, t2 - t1, int(st.primary_rays)
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    stride = args.cpu_stride
+    cores = os.cpu_count()
+    for _ in range(args.warmup):
+        cpu_sample(stride)
+    times, nseg, npx, nprim = [], 0, 0, 0
+    for _ in range(args.steps):
+        n, px, tt, tr, prim = cpu_sample(stride)
+        times.append(tt + tr)
+        nseg, npx, nprim = n, px, prim
+    step_s = statistics.mean(times)
+    value = nseg / step_s
+    sample = (f"every {stride}th primary ray of each light ({nprim} of {8 << 18} primaries) traced and "
+              f"rasterised per step: {nseg} segments, {npx} pixel updates")
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "segments/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample": sample},
+        "px_per_s": npx / step_s,
+        "cpu_baseline": {"value": value, "unit": "segments/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "segments/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference is Rust (no toolchain) and its geometry crate is not vendored; this is the C "
+                "restatement of tracer.rs timed on the host cores",
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args, ws, rank, local):
+    import ctypes as C
+
+    import torch
+
+    from light_garden_gb300 import abi, workloads as W
+    from light_garden_gb300.runtime import Context
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = W.mid_scene()
+    pk = w.packed()
+    Wd, Hd = pk.params.width, pk.params.height
+    ctx = Context(device=local)
+    ctx.upload(pk)
+    out_dev = torch.empty((Hd, Wd * 4), dtype=torch.int16, device=dev)
+    out_host = torch.empty((Hd, Wd * 4), dtype=torch.int16, pin_memory=True)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    pitch = Wd * 8
+    for _ in range(max(3, args.warmup)):
+        st = ctx.render_into(out_dev.data_ptr(), pitch, True)
+    torch.cuda.synchronize()
+    launches_per_step = 1 + pk.params.max_bounce + 1 + 7
+
+    barrier(ws)
+    torch.cuda.synchronize()
+    stage = {k: 0.0 for k in ("trace_ms", "bin_ms", "raster_ms", "resolve_ms", "total_ms")}
+    segs = pixels = refs = visits = solves = 0
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()  # write 512 MB > L2 between steps (not timed)
+            torch.cuda.synchronize()
+            st = ctx.render_into(out_dev.data_ptr(), pitch, True)
+            for k in stage:
+                stage[k] += st[k]
+            segs, pixels, refs, visits, solves = (st["segments"], st["pixels"], st["tile_refs"], st["ray_visits"],
+                                                  st["fp64_solves"])
+    torch.cuda.synchronize()
+    barrier(ws)
+    ms = stage["total_ms"] / args.steps
+    ms_max = allmax(ws, ms, dev)
+    value = ws * segs / (ms_max * 1e-3)
+    px_per_s = ws * pixels / (ms_max * 1e-3)
+    avg = {k: v / args.steps for k, v in stage.items()}
+
+    # end to end through the C ABI: scene tables from the host, image back to pinned host memory
+    h2d = C.sizeof(abi.lg_geo) * pk.n_geo + C.sizeof(abi.lg_object) * pk.n_objects + \
+        C.sizeof(abi.lg_light) * pk.n_lights + C.sizeof(abi.lg_params)
+    d2h = Hd * Wd * 8
+    ctx.upload(pk)
+    ctx.render_into(out_host.data_ptr(), pitch, False)
+    barrier(ws)
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.upload(pk)
+        st = ctx.render_into(out_host.data_ptr(), pitch, False)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = allmax(ws, statistics.mean(e2e_times), dev)
+    e2e_value = ws * st["segments"] / e2e_s
+
+    # roofline of the dominant stage
+    hbm, peak_kind = peaks()
+    dom = max(("trace_ms", "bin_ms", "raster_ms"), key=lambda k: avg[k])
+    if dom == "raster_ms":
+        alg = 64.0 * pixels  # int64 RGBA read-modify-write per accumulated pixel
+        kern = "k_raster<true> (tile accumulation)"
+    elif dom == "bin_ms":
+        alg = 2 * 32.0 * segs + 8.0 * refs
+        kern = "k_bin_count + k_bin_scatter"
+    else:
+        alg = 80.0 * visits + 80.0 * visits + 32.0 * segs
+        kern = "k_trace_gen (all generations)"
+    achieved = alg / (avg[dom] * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "traffic": None, "peak_source": peak_kind}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        n, px, tt, tr, prim = cpu_sample(args.cpu_stride)
+        cpu = {"value": n / (tt + tr), "unit": "segments/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"every {args.cpu_stride}th primary of each light ({prim} primaries): {n} segments "
+                         f"traced in {tt:.2f} s and rasterised ({px} px) in {tr:.2f} s",
+               "trace_segments_per_s": n / tt, "raster_px_per_s": px / tr}
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": "segments/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp64+fp32 trace, int64 accumulate", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "l2": "flushed between steps (512 MB write); working set > L2",
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+            "px_per_s": px_per_s,
+            "segments_per_step": segs, "pixels_per_step": pixels, "tile_refs_per_step": refs,
+            "ray_visits_per_step": visits, "fp64_solves_per_step": solves,
+            "stage_ms": avg,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "segments/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": e2e_s * 1e3},
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(out), flush=True)
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-stride", type=int, default=64)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_ours(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,273 @@
+/*
+ * lg.h — C ABI of the GB300 trace-and-accumulate library (liblightgarden_cuda.so).
+ *
+ * This is the drop-in boundary for light_garden's per-frame hot path:
+ *
+ *   Tracer::trace_all            src/light_garden/tracer.rs:276-358   -> lg_trace
+ *   Tracer::trace                src/light_garden/tracer.rs:360-493   -> (inside lg_trace)
+ *   {Point,Spot,Directional}Light::set_num_rays
+ *                                src/light_garden/light.rs:103-115,163-174,225-249 -> (inside lg_trace)
+ *   StringMod::draw              src/light_garden/string_mod.rs:33-158 -> lg_params.string_mod overlay
+ *   SubRenderPass::update_vertex_buffer
+ *                                src/sub_render_pass.rs:188-203       -> segments stay on the device
+ *   Renderer::render_to_texture  src/renderer.rs:164-188 (LineList, blend src/light_garden/mod.rs:57-73)
+ *                                                                      -> lg_accumulate
+ *   Renderer::render_texture     src/renderer.rs:330-418, src/render_to_texture.wgsl:17-28
+ *                                                                      -> lg_resolve_f16
+ *   Tracer::{push_object, push_light, clear, ...} src/light_garden/tracer.rs:48-116,
+ *   pub fields max_bounce / cutoff_color       src/light_garden/tracer.rs:9-11
+ *                                                                      -> lg_scene_upload
+ *
+ * The reference has no FFI; its Rust `Tracer` owns Vec<Object>/Vec<Light> and returns a
+ * Vec<(P2, Color)>.  Here the caller owns the scene description (flat arrays of the
+ * structs below), the library copies it to the device, owns every device buffer, and the
+ * caller owns every output buffer.  A context is used by one host thread at a time;
+ * several contexts may share a device.  Every entry point returns an lg_status and never
+ * aborts the process; lg_last_error() describes the last failure of a context.
+ *
+ * World coordinates follow the reference: the canvas is the rectangle
+ * [-aspect, aspect] x [-1, 1] with aspect = width / height (src/sub_render_pass.rs:146-158).
+ * Geometry is FP64 (collision2d's Float = f64), colours are FP32 RGBA (light.rs:7).
+ */
+#ifndef LIGHT_GARDEN_GB300_LG_H
+#define LIGHT_GARDEN_GB300_LG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LG_ABI_VERSION 1
+
+typedef enum lg_status {
+  LG_OK = 0,
+  LG_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad index, out-of-range parameter */
+  LG_ERR_UNSUPPORTED = 2,      /* a shape kind, blend mode or option this path does not implement */
+  LG_ERR_OUT_OF_MEMORY = 3,    /* device or pinned-host allocation failed */
+  LG_ERR_CUDA = 4,             /* a CUDA runtime call failed (message in lg_last_error) */
+  LG_ERR_NO_SCENE = 5,         /* lg_trace/lg_render before lg_scene_upload */
+  LG_ERR_TRUNCATED = 6,        /* caller buffer too small; *n_out holds the size needed */
+  LG_ERR_TIMEOUT = 7,          /* a bounded device-side wait expired (no hang, no trap) */
+  LG_ERR_BUDGET = 8,           /* admission refused: request does not fit the HBM budget */
+  LG_ERR_NOT_READY = 9,        /* serving: result not finished yet */
+  LG_ERR_NOT_FOUND = 10        /* serving: unknown request id */
+} lg_status;
+
+/* ---- geometry nodes: the collision2d `Geo` variants on the path ----------------------- */
+enum lg_geo_kind {
+  LG_GEO_CIRCLE = 0,  /* GeoCircle  { origin, radius }                              */
+  LG_GEO_RECT = 1,    /* GeoRect    { origin (centre), rotation, width, height }    */
+  LG_GEO_SEGMENT = 2, /* GeoLineSegment a -> b (straight mirror)                    */
+  LG_GEO_CUBIC = 3,   /* GeoCubicBezier P0..P3 (curved mirror)                      */
+  LG_GEO_LOGIC = 4    /* GeoLogic   { op, a, b, origin, rotation } (CSG)            */
+};
+
+/* Logic / LogicOp (src/light_garden/mod.rs:366-372: geo_a & geo_b, |, and_not) */
+enum lg_logic_op { LG_OP_AND = 0, LG_OP_OR = 1, LG_OP_AND_NOT = 2 };
+
+/* One node of a geometry tree.  Trees are stored as a flat array; LOGIC nodes name their
+ * two children by index into the same array.  LOGIC children are expressed in the
+ * node's local frame: world = origin + R(rot) * local, R = [[c, -s], [s, c]]. */
+typedef struct lg_geo {
+  int32_t kind;     /* enum lg_geo_kind */
+  int32_t op;       /* LOGIC: enum lg_logic_op */
+  int32_t a, b;     /* LOGIC: child node indices */
+  double origin[2]; /* CIRCLE centre | RECT centre | LOGIC origin */
+  double rot[2];    /* RECT / LOGIC rotation as (cos, sin); (1, 0) = identity */
+  double v[8];      /* CIRCLE: v[0] = radius
+                       RECT:   v[0] = width, v[1] = height
+                       SEGMENT: (v[0], v[1]) -> (v[2], v[3])
+                       CUBIC:  P0 = (v[0], v[1]) ... P3 = (v[6], v[7]) */
+} lg_geo;
+
+/* ---- objects: ObjectE + Option<Material> (src/light_garden/object.rs:7-16,51-55) ------ */
+enum lg_object_kind {
+  LG_OBJ_STRAIGHT_MIRROR = 0, /* root must be a SEGMENT */
+  LG_OBJ_CURVED_MIRROR = 1,   /* root must be a CUBIC   */
+  LG_OBJ_CIRCLE = 2,
+  LG_OBJ_RECT = 3,
+  LG_OBJ_LENS = 4,            /* Logic(And, circle, circle), object.rs:387-415 */
+  LG_OBJ_CONVEX_POLYGON = 5,  /* not on this path: lg_scene_upload returns LG_ERR_UNSUPPORTED */
+  LG_OBJ_ELLIPSE = 6,         /* not on this path: lg_scene_upload returns LG_ERR_UNSUPPORTED */
+  LG_OBJ_GEO = 7              /* any geometry tree (CSG results, object.rs:107-113) */
+};
+
+typedef struct lg_object {
+  int32_t kind;            /* enum lg_object_kind */
+  int32_t geo;             /* index of the root node in the geo array */
+  int32_t has_material;    /* 0: material_opt = None -> perfect mirror (tracer.rs:473-481) */
+  int32_t _pad;
+  double refractive_index; /* Material::refractive_index; default 1.2 (object.rs:441-447) */
+} lg_object;
+
+/* ---- lights (src/light_garden/light.rs:10-14) ----------------------------------------- */
+enum lg_light_kind { LG_LIGHT_POINT = 0, LG_LIGHT_DIRECTIONAL = 1, LG_LIGHT_SPOT = 2 };
+
+typedef struct lg_light {
+  int32_t kind;      /* enum lg_light_kind */
+  uint32_t num_rays; /* rays generated per frame (set_num_rays) */
+  float color[4];    /* RGBA of every primary ray */
+  double origin[2];  /* POINT/SPOT: position.  DIRECTIONAL: segment start a */
+  double v[2];       /* SPOT: spot_direction.   DIRECTIONAL: segment end b  */
+  double spot_angle; /* SPOT: full opening angle in radians */
+} lg_light;
+
+/* ---- blend state (wgpu::BlendComponent, src/light_garden/mod.rs:57-73) --------------- *
+ * Only order-independent blends are accepted (dst_factor One with Add / ReverseSubtract,
+ * or Min / Max); anything that reads the destination is order-dependent under
+ * concurrent accumulation and is rejected with LG_ERR_UNSUPPORTED. */
+enum lg_blend_factor {
+  LG_BF_ZERO = 0, LG_BF_ONE = 1, LG_BF_SRC = 2, LG_BF_ONE_MINUS_SRC = 3,
+  LG_BF_SRC_ALPHA = 4, LG_BF_ONE_MINUS_SRC_ALPHA = 5, LG_BF_DST = 6,
+  LG_BF_ONE_MINUS_DST = 7, LG_BF_DST_ALPHA = 8, LG_BF_ONE_MINUS_DST_ALPHA = 9,
+  LG_BF_SRC_ALPHA_SATURATED = 10, LG_BF_CONSTANT = 11, LG_BF_ONE_MINUS_CONSTANT = 12
+};
+enum lg_blend_op { LG_BO_ADD = 0, LG_BO_SUBTRACT = 1, LG_BO_REVERSE_SUBTRACT = 2, LG_BO_MIN = 3, LG_BO_MAX = 4 };
+
+typedef struct lg_blend_component {
+  int32_t src_factor, dst_factor, op;
+} lg_blend_component;
+
+enum lg_accum_mode {
+  LG_ACCUM_FIXED64 = 0, /* signed Q31.32 fixed point in int64: order-independent, bit-reproducible */
+  LG_ACCUM_F32 = 1      /* FP32 atomics: faster to reason about, not bit-reproducible */
+};
+
+/* ---- string-mod overlay (src/light_garden/string_mod.rs) ------------------------------- */
+enum lg_string_mod_mode { LG_SM_ADD = 0, LG_SM_MUL = 1, LG_SM_POW = 2, LG_SM_BASE = 3 };
+
+typedef struct lg_string_mod {
+  uint64_t modulo;  /* number of points m; 0 disables the overlay */
+  uint64_t num;
+  uint64_t turns;
+  uint32_t mode;    /* enum lg_string_mod_mode */
+  uint32_t curve;   /* 0 = Curve::Circle (the only curve on this path) */
+  float color[4];
+} lg_string_mod;
+
+/* ---- per-scene parameters ------------------------------------------------------------- */
+typedef struct lg_params {
+  uint32_t max_bounce;          /* Tracer::max_bounce (default 5, GUI 1..=20); here 1..=64 */
+  uint32_t width, height;       /* accumulation canvas in pixels */
+  float cutoff_color[4];        /* Tracer::cutoff_color (default 0.001) */
+  float clear_color[4];         /* render-texture clear; wgpu::Color::BLACK = (0,0,0,1) */
+  float blend_constant[4];      /* for LG_BF_CONSTANT */
+  lg_blend_component color_blend; /* default One / One / Add */
+  lg_blend_component alpha_blend; /* default SrcAlpha / One / Add */
+  int32_t accum;                /* enum lg_accum_mode */
+  int32_t emit_control_lines;   /* append curved-mirror control polygons (tracer.rs:341-346) */
+  int32_t record_paths;         /* also write one lg_path_record per segment (parity tooling) */
+  int32_t _pad;
+  lg_string_mod string_mod;     /* overlay segments, drawn with the same raster */
+} lg_params;
+
+/* Fills *p with the reference defaults (tracer.rs:37-39, mod.rs:57-73). */
+void lg_params_default(lg_params* p);
+
+/* ---- outputs -------------------------------------------------------------------------- */
+/* One emitted line segment: two (P2, Color) vertices of the reference's line list,
+ * positions narrowed to f32 exactly like update_vertex_buffer (sub_render_pass.rs:188-203). */
+typedef struct lg_segment {
+  float x0, y0, x1, y1;
+  float color[4];
+} lg_segment;
+
+enum lg_path_flags {
+  LG_PATH_NEAR_DEGENERATE = 1, /* a decision on this path fell inside the FP64 epsilon band */
+  LG_PATH_TIR = 2,             /* this segment ends in total internal reflection */
+  LG_PATH_FALLBACK = 4         /* candidate list overflowed: every object re-solved in FP64 */
+};
+enum lg_path_source { LG_SRC_TRACE = 0, LG_SRC_CONTROL_LINE = 1, LG_SRC_STRING_MOD = 2 };
+
+/* Identity of a segment in the ray tree, for parity checks against a CPU trace. */
+typedef struct lg_path_record {
+  uint64_t path;    /* bit k = branch taken at generation k+1: 0 reflected/mirror, 1 refracted */
+  uint32_t primary; /* primary ray index within its light */
+  uint16_t light;   /* light index */
+  uint8_t gen;      /* generation (0 = primary ray) */
+  uint8_t flags;    /* enum lg_path_flags, inherited by descendants */
+  int32_t hit;      /* object index hit, -1 = canvas exit */
+  uint32_t source;  /* enum lg_path_source */
+} lg_path_record;
+
+typedef struct lg_trace_stats {
+  uint64_t primary_rays;   /* rays generated by all lights */
+  uint64_t ray_visits;     /* queue entries traced (after the cutoff) */
+  uint64_t segments;       /* segments written (traced + overlays) */
+  uint64_t fp64_solves;    /* object intersections re-solved in FP64 */
+  uint64_t fp64_fallbacks; /* rays whose FP32 candidate list overflowed */
+  uint64_t near_degenerate;/* segments carrying LG_PATH_NEAR_DEGENERATE */
+  uint64_t pixels;         /* pixel updates made by lg_accumulate */
+  uint64_t tile_refs;      /* (segment, tile) pairs binned by lg_accumulate */
+  uint32_t retries;        /* re-launches after a ring/queue overflow */
+  uint32_t _pad;
+  /* device time from CUDA events on the library's stream; lg_render splits accumulate
+     into bin (count, scan, scatter) and raster (tile accumulation) */
+  float trace_ms, accumulate_ms, resolve_ms, total_ms, bin_ms, raster_ms;
+} lg_trace_stats;
+
+typedef struct lg_device_opts {
+  int32_t device;             /* CUDA device ordinal */
+  uint32_t _pad;
+  uint64_t segment_capacity;  /* initial segment ring size (0 = automatic); grows on overflow */
+  uint64_t queue_capacity;    /* initial per-generation ray queue size (0 = automatic) */
+} lg_device_opts;
+
+typedef struct lg_ctx lg_ctx;
+
+/* ---- context --------------------------------------------------------------------------- */
+lg_status lg_create(lg_ctx** out, const lg_device_opts* opts_or_null);
+lg_status lg_destroy(lg_ctx* ctx);
+const char* lg_last_error(const lg_ctx* ctx_or_null);
+uint32_t lg_abi_version(void);
+
+/* ---- one scene ------------------------------------------------------------------------ */
+/* Copies a scene (geometry trees, objects, lights, parameters) to the device.  Replaces
+ * the whole object/light list, like Tracer::clear + push_object/push_light
+ * (tracer.rs:54-94) followed by Light::set_num_rays (light.rs:45-51). */
+lg_status lg_scene_upload(lg_ctx* ctx, const lg_geo* geos, uint32_t n_geo,
+                          const lg_object* objects, uint32_t n_objects,
+                          const lg_light* lights, uint32_t n_lights, const lg_params* params);
+
+/* Traces every light (Tracer::trace_all, tracer.rs:276-358) into the device segment ring.
+ * If the ring or a generation queue overflows, the library grows it and traces again
+ * (stats->retries counts this). */
+lg_status lg_trace(lg_ctx* ctx, lg_trace_stats* stats_or_null);
+
+/* Clears the accumulation image to params.clear_color and rasterises every segment in the
+ * ring into it: aliased 1-px lines, one sample per pixel column (x-major) or row
+ * (y-major) at the pixel centre, half-open at the far end, blended per lg_params. */
+lg_status lg_accumulate(lg_ctx* ctx, lg_trace_stats* stats_or_null);
+
+/* Rasterises caller-provided segments (host memory) into the accumulation image after
+ * clearing it.  Same raster rule and blend as lg_accumulate. */
+lg_status lg_accumulate_segments(lg_ctx* ctx, const lg_segment* segments, uint64_t n,
+                                 lg_trace_stats* stats_or_null);
+
+/* Converts the accumulation image to RGBA16F (IEEE binary16, round to nearest even),
+ * row 0 = top of the canvas.  dst is host memory unless dst_is_device != 0.
+ * pitch_bytes >= width * 8. */
+lg_status lg_resolve_f16(lg_ctx* ctx, uint16_t* dst, size_t pitch_bytes, int32_t dst_is_device);
+
+/* Optional export tonemap (renderer.rs:313-328): u8 = sat(f^(1/2.2) * 255), truncating
+ * like Rust `as u8`; RGBA8, pitch_bytes >= width * 4. */
+lg_status lg_resolve_rgba8(lg_ctx* ctx, uint8_t* dst, size_t pitch_bytes, int32_t dst_is_device);
+
+/* trace + accumulate + resolve_f16 as one captured CUDA graph launch. */
+lg_status lg_render(lg_ctx* ctx, uint16_t* dst, size_t pitch_bytes, int32_t dst_is_device,
+                    lg_trace_stats* stats_or_null);
+
+/* Copies segments (and optionally their path records) out of the ring.  If cap is too
+ * small, returns LG_ERR_TRUNCATED with *n_out = segments available. */
+lg_status lg_segments_download(lg_ctx* ctx, lg_segment* out, lg_path_record* paths_or_null,
+                               uint64_t cap, uint64_t* n_out);
+
+/* Copies the raw accumulation image: width*height*4 values, int64 (FIXED64) or float (F32). */
+lg_status lg_accum_download(lg_ctx* ctx, void* out, uint64_t cap_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LIGHT_GARDEN_GB300_LG_H */

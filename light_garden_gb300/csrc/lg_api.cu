@@ -1,0 +1,871 @@
+// lg_api.cu — host side of the C ABI declared in include/lg.h.
+//
+// Owns the device buffers of one context and drives the kernels:
+//   lg_scene_upload  validates and flattens the scene (tracer.rs:48-116 object/light lists)
+//   lg_trace         light setup + one wavefront kernel per generation + overlays
+//                    (tracer.rs:276-358), growing the ring / queues on overflow
+//   lg_accumulate    bin -> scan -> units -> scatter -> tile raster (renderer.rs:164-188)
+//   lg_resolve_f16   Q31.32 -> binary16 (renderer.rs:330-418)
+//   lg_render        the three above as one captured CUDA graph launch
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "lg_kernels.cuh"
+
+using namespace lgd;
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+constexpr uint32_t UNIT_REFS = 2048;
+constexpr size_t OBJ_SMEM_MAX = 96 * 1024;
+
+}  // namespace
+
+struct lg_ctx {
+  int device = 0;
+  int n_sm = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // scene
+  DevBuf d_scan, d_info, d_leaves, d_prog, d_lights, d_cubics;
+  uint32_t n_obj = 0, n_leaves = 0, n_prog = 0, n_lights = 0, n_cubic = 0;
+  uint64_t n_primary = 0;
+  lg_params prm{};
+  bool has_scene = false;
+  double aspect = 1.0;
+  // trace
+  DevBuf d_queue[2];
+  uint64_t queue_cap = 0;
+  DevBuf d_segs, d_paths;
+  uint64_t seg_cap = 0;
+  DevBuf d_ctr;
+  Counters* h_ctr = nullptr;
+  uint64_t seg_cap_hint = 0, queue_cap_hint = 0;
+  // raster
+  DevBuf d_tile_count, d_tile_off, d_tile_cursor, d_unit_off, d_refs, d_units, d_accum, d_stage;
+  uint64_t refs_cap = 0, units_cap = 0;
+  uint32_t n_tiles = 0, ntx = 0, nty = 0;
+  // launch shapes
+  int trace_grid = 0, raster_grid = 0, bin_grid = 0;
+  size_t obj_smem = 0;
+  int smem_fits = 0;
+  // graph
+  cudaGraphExec_t gexec = nullptr;
+  bool graph_valid = false;
+  cudaEvent_t ev[6] = {};
+};
+
+namespace {
+
+lg_status fail(lg_ctx* c, lg_status st, const std::string& msg) {
+  if (c) c->err = msg;
+  return st;
+}
+
+lg_status cuda_fail(lg_ctx* c, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+  (void)cudaGetLastError();
+  return fail(c, e == cudaErrorMemoryAllocation ? LG_ERR_OUT_OF_MEMORY : LG_ERR_CUDA, m);
+}
+
+#define CK(call, what)                              \
+  do {                                              \
+    cudaError_t e_ = (call);                        \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
+  } while (0)
+
+lg_status ensure(lg_ctx* c, DevBuf& b, size_t bytes, const char* what) {
+  if (bytes <= b.bytes && b.p) return LG_OK;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(&b.p, bytes);
+  if (e != cudaSuccess) {
+    b.p = nullptr;
+    return cuda_fail(c, e, what);
+  }
+  b.bytes = bytes;
+  c->graph_valid = false;
+  return LG_OK;
+}
+
+void release(DevBuf& b) {
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+}
+
+// ---------------------------------------------------------------- scene flattening
+struct Xf {
+  double ox, oy, c, s;  // world = (ox, oy) + R(c, s) * local
+  void apply(double x, double y, double& wx, double& wy) const {
+    wx = ox + c * x - s * y;
+    wy = oy + s * x + c * y;
+  }
+};
+
+struct Flat {
+  std::vector<ObjScan> scan;
+  std::vector<ObjInfo> info;
+  std::vector<Leaf64> leaves;
+  std::vector<uint8_t> prog;
+  std::vector<LightDev> lights;
+  std::vector<uint32_t> cubics;
+};
+
+lg_status flatten_node(lg_ctx* c, const lg_geo* G, uint32_t n_geo, int32_t gi, const Xf& T, int depth, Flat& F,
+                       uint32_t leaf0, std::vector<uint8_t>& prog) {
+  if (gi < 0 || (uint32_t)gi >= n_geo) return fail(c, LG_ERR_INVALID_ARGUMENT, "geometry index out of range");
+  if (depth > 32) return fail(c, LG_ERR_INVALID_ARGUMENT, "geometry tree deeper than 32 (cycle?)");
+  const lg_geo& g = G[gi];
+  if (g.kind == LG_GEO_LOGIC) {
+    if (g.op < 0 || g.op > 2) return fail(c, LG_ERR_INVALID_ARGUMENT, "unknown logic op");
+    Xf T2;
+    T.apply(g.origin[0], g.origin[1], T2.ox, T2.oy);
+    T2.c = T.c * g.rot[0] - T.s * g.rot[1];
+    T2.s = T.s * g.rot[0] + T.c * g.rot[1];
+    lg_status st = flatten_node(c, G, n_geo, g.a, T2, depth + 1, F, leaf0, prog);
+    if (st) return st;
+    st = flatten_node(c, G, n_geo, g.b, T2, depth + 1, F, leaf0, prog);
+    if (st) return st;
+    prog.push_back(g.op == LG_OP_AND ? PROG_AND : g.op == LG_OP_OR ? PROG_OR : PROG_AND_NOT);
+    return LG_OK;
+  }
+  Leaf64 L;
+  std::memset(&L, 0, sizeof L);
+  switch (g.kind) {
+    case LG_GEO_CIRCLE:
+      L.kind = LEAF_CIRCLE;
+      T.apply(g.origin[0], g.origin[1], L.p[0], L.p[1]);
+      L.p[2] = g.v[0];
+      break;
+    case LG_GEO_RECT:
+      L.kind = LEAF_RECT;
+      T.apply(g.origin[0], g.origin[1], L.p[0], L.p[1]);
+      L.p[2] = T.c * g.rot[0] - T.s * g.rot[1];
+      L.p[3] = T.s * g.rot[0] + T.c * g.rot[1];
+      L.p[4] = 0.5 * g.v[0];
+      L.p[5] = 0.5 * g.v[1];
+      break;
+    case LG_GEO_SEGMENT:
+      L.kind = LEAF_SEGMENT;
+      T.apply(g.v[0], g.v[1], L.p[0], L.p[1]);
+      T.apply(g.v[2], g.v[3], L.p[2], L.p[3]);
+      break;
+    case LG_GEO_CUBIC:
+      L.kind = LEAF_CUBIC;
+      for (int k = 0; k < 4; ++k) T.apply(g.v[2 * k], g.v[2 * k + 1], L.p[2 * k], L.p[2 * k + 1]);
+      break;
+    default:
+      return fail(c, LG_ERR_UNSUPPORTED, "unsupported geometry kind " + std::to_string(g.kind));
+  }
+  const uint32_t li = (uint32_t)F.leaves.size() - leaf0;
+  if (li >= (uint32_t)MAX_LEAVES - 1) return fail(c, LG_ERR_UNSUPPORTED, "more than 63 leaves in one object");
+  F.leaves.push_back(L);
+  prog.push_back((uint8_t)li);
+  return LG_OK;
+}
+
+// bounding circle of one leaf about a centre: returns the max distance
+double leaf_extent(const Leaf64& L, double cx, double cy) {
+  auto d = [&](double x, double y) { return std::hypot(x - cx, y - cy); };
+  switch (L.kind) {
+    case LEAF_CIRCLE: return d(L.p[0], L.p[1]) + std::fabs(L.p[2]);
+    case LEAF_RECT: return d(L.p[0], L.p[1]) + std::hypot(L.p[4], L.p[5]);
+    case LEAF_SEGMENT: return std::max(d(L.p[0], L.p[1]), d(L.p[2], L.p[3]));
+    default: {
+      double m = 0;
+      for (int k = 0; k < 4; ++k) m = std::max(m, d(L.p[2 * k], L.p[2 * k + 1]));
+      return m;
+    }
+  }
+}
+
+void leaf_box(const Leaf64& L, double& x0, double& y0, double& x1, double& y1) {
+  auto add = [&](double x, double y) {
+    x0 = std::min(x0, x); y0 = std::min(y0, y); x1 = std::max(x1, x); y1 = std::max(y1, y);
+  };
+  switch (L.kind) {
+    case LEAF_CIRCLE: {
+      const double r = std::fabs(L.p[2]);
+      add(L.p[0] - r, L.p[1] - r);
+      add(L.p[0] + r, L.p[1] + r);
+      break;
+    }
+    case LEAF_RECT: {
+      const double ex = std::fabs(L.p[2]) * L.p[4] + std::fabs(L.p[3]) * L.p[5];
+      const double ey = std::fabs(L.p[3]) * L.p[4] + std::fabs(L.p[2]) * L.p[5];
+      add(L.p[0] - ex, L.p[1] - ey);
+      add(L.p[0] + ex, L.p[1] + ey);
+      break;
+    }
+    case LEAF_SEGMENT:
+      add(L.p[0], L.p[1]);
+      add(L.p[2], L.p[3]);
+      break;
+    default:
+      for (int k = 0; k < 4; ++k) add(L.p[2 * k], L.p[2 * k + 1]);
+  }
+}
+
+void leaf_f32(const Leaf64& L, float* a) {
+  if (L.kind == LEAF_CIRCLE) {
+    a[0] = (float)L.p[0]; a[1] = (float)L.p[1]; a[2] = (float)L.p[2];
+  } else if (L.kind == LEAF_RECT) {
+    for (int k = 0; k < 6; ++k) a[k] = (float)L.p[k];
+  } else {
+    a[0] = (float)L.p[0]; a[1] = (float)L.p[1];
+    a[2] = (float)(L.p[2] - L.p[0]); a[3] = (float)(L.p[3] - L.p[1]);
+  }
+}
+
+bool blend_supported(const lg_blend_component& b) {
+  if (b.op == LG_BO_MIN || b.op == LG_BO_MAX) return b.src_factor == LG_BF_ONE && b.dst_factor == LG_BF_ONE;
+  if (b.op != LG_BO_ADD && b.op != LG_BO_REVERSE_SUBTRACT) return false;
+  if (b.dst_factor != LG_BF_ONE) return false;
+  switch (b.src_factor) {
+    case LG_BF_ZERO: case LG_BF_ONE: case LG_BF_SRC: case LG_BF_ONE_MINUS_SRC: case LG_BF_SRC_ALPHA:
+    case LG_BF_ONE_MINUS_SRC_ALPHA: case LG_BF_CONSTANT: case LG_BF_ONE_MINUS_CONSTANT: return true;
+    default: return false;
+  }
+}
+
+lg_status flatten_scene(lg_ctx* c, const lg_geo* G, uint32_t n_geo, const lg_object* O, uint32_t n_obj,
+                        const lg_light* Ls, uint32_t n_lights, Flat& F) {
+  for (uint32_t k = 0; k < n_obj; ++k) {
+    const lg_object& o = O[k];
+    if (o.kind == LG_OBJ_CONVEX_POLYGON || o.kind == LG_OBJ_ELLIPSE)
+      return fail(c, LG_ERR_UNSUPPORTED, "object " + std::to_string(k) + ": ConvexPolygon / Ellipse are not on this path");
+    if (o.kind < 0 || o.kind > LG_OBJ_GEO) return fail(c, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": unknown kind");
+    if (o.geo < 0 || (uint32_t)o.geo >= n_geo) return fail(c, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": geometry index out of range");
+    const int rk = G[o.geo].kind;
+    const bool ok = (o.kind == LG_OBJ_STRAIGHT_MIRROR && rk == LG_GEO_SEGMENT) ||
+                    (o.kind == LG_OBJ_CURVED_MIRROR && rk == LG_GEO_CUBIC) ||
+                    (o.kind == LG_OBJ_CIRCLE && rk == LG_GEO_CIRCLE) || (o.kind == LG_OBJ_RECT && rk == LG_GEO_RECT) ||
+                    (o.kind == LG_OBJ_LENS && rk == LG_GEO_LOGIC) || o.kind == LG_OBJ_GEO;
+    if (!ok) return fail(c, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": kind does not match its geometry");
+    if (o.has_material && !(o.refractive_index > 0.0))
+      return fail(c, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": refractive index must be > 0");
+    const uint32_t leaf0 = (uint32_t)F.leaves.size();
+    std::vector<uint8_t> prog;
+    Xf T{0.0, 0.0, 1.0, 0.0};
+    lg_status st = flatten_node(c, G, n_geo, o.geo, T, 0, F, leaf0, prog);
+    if (st) return st;
+    ObjInfo oi;
+    std::memset(&oi, 0, sizeof oi);
+    oi.leaf_begin = leaf0;
+    oi.n_leaves = (uint16_t)(F.leaves.size() - leaf0);
+    oi.prog_begin = (uint32_t)F.prog.size();
+    oi.prog_len = (uint16_t)prog.size();
+    oi.flags = (o.has_material ? INFO_MATERIAL : 0u) |
+               ((o.kind == LG_OBJ_STRAIGHT_MIRROR || o.kind == LG_OBJ_CURVED_MIRROR) ? INFO_NO_CONTAINS : 0u);
+    oi.n = o.has_material ? o.refractive_index : 1.0;
+    F.prog.insert(F.prog.end(), prog.begin(), prog.end());
+    F.info.push_back(oi);
+    if (o.kind == LG_OBJ_CURVED_MIRROR) F.cubics.push_back(k);
+    // FP32 scan record
+    ObjScan s;
+    std::memset(&s, 0, sizeof s);
+    double x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
+    for (uint32_t i = leaf0; i < F.leaves.size(); ++i) leaf_box(F.leaves[i], x0, y0, x1, y1);
+    const double cx = 0.5 * (x0 + x1), cy = 0.5 * (y0 + y1);
+    double R = 0.0;
+    for (uint32_t i = leaf0; i < F.leaves.size(); ++i) R = std::max(R, leaf_extent(F.leaves[i], cx, cy));
+    if (!std::isfinite(cx) || !std::isfinite(cy) || !std::isfinite(R))
+      return fail(c, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": non-finite geometry");
+    s.cx = (float)cx;
+    s.cy = (float)cy;
+    s.R = (float)(R * (1.0 + 1e-6) + 1e-6 * (1.0 + std::fabs(cx) + std::fabs(cy)));
+    const uint32_t nl = oi.n_leaves;
+    bool simple = nl <= 2;
+    for (uint32_t i = leaf0; i < F.leaves.size(); ++i) simple = simple && F.leaves[i].kind != LEAF_CUBIC;
+    uint32_t info = SCAN_BOUND;
+    if (simple && nl == 1) {
+      info = SCAN_ONE | (F.leaves[leaf0].kind << 4);
+      leaf_f32(F.leaves[leaf0], s.a);
+    } else if (simple && nl == 2) {
+      const uint8_t op = prog.back();
+      info = SCAN_TWO | (F.leaves[leaf0].kind << 4) | (F.leaves[leaf0 + 1].kind << 6) |
+             ((uint32_t)(op == PROG_AND ? LG_OP_AND : op == PROG_OR ? LG_OP_OR : LG_OP_AND_NOT) << 8);
+      leaf_f32(F.leaves[leaf0], s.a);
+      leaf_f32(F.leaves[leaf0 + 1], s.b);
+    }
+    s.info = info | oi.flags;
+    F.scan.push_back(s);
+  }
+  uint64_t first = 0;
+  for (uint32_t l = 0; l < n_lights; ++l) {
+    const lg_light& L = Ls[l];
+    if (L.kind < 0 || L.kind > LG_LIGHT_SPOT) return fail(c, LG_ERR_INVALID_ARGUMENT, "light " + std::to_string(l) + ": unknown kind");
+    LightDev d;
+    std::memset(&d, 0, sizeof d);
+    d.ox = L.origin[0]; d.oy = L.origin[1]; d.vx = L.v[0]; d.vy = L.v[1];
+    d.spot_angle = L.spot_angle;
+    d.n0 = 1.0;
+    for (int i = 0; i < 4; ++i) d.color[i] = L.color[i];
+    d.kind = (uint32_t)L.kind;
+    d.num_rays = L.num_rays;
+    d.first = first;
+    first += L.num_rays;
+    F.lights.push_back(d);
+  }
+  return LG_OK;
+}
+
+SceneDev scene_dev(lg_ctx* c) {
+  SceneDev S;
+  S.scan = (const ObjScan*)c->d_scan.p;
+  S.info = (const ObjInfo*)c->d_info.p;
+  S.leaves = (const Leaf64*)c->d_leaves.p;
+  S.prog = (const uint8_t*)c->d_prog.p;
+  S.lights = (LightDev*)c->d_lights.p;
+  S.n_obj = c->n_obj;
+  S.n_lights = c->n_lights;
+  S.n_primary = c->n_primary;
+  S.aspect = c->aspect;
+  for (int i = 0; i < 4; ++i) S.cutoff[i] = c->prm.cutoff_color[i];
+  S.max_bounce = c->prm.max_bounce;
+  S.record_paths = c->prm.record_paths ? 1u : 0u;
+  return S;
+}
+
+TraceBufs trace_bufs(lg_ctx* c) {
+  TraceBufs B;
+  B.queue[0] = (RayRec*)c->d_queue[0].p;
+  B.queue[1] = (RayRec*)c->d_queue[1].p;
+  B.queue_cap = c->queue_cap;
+  B.segs = (lg_segment*)c->d_segs.p;
+  B.paths = (lg_path_record*)c->d_paths.p;
+  B.seg_cap = c->seg_cap;
+  B.ctr = (Counters*)c->d_ctr.p;
+  return B;
+}
+
+RasterArgs raster_args(lg_ctx* c) {
+  RasterArgs A;
+  std::memset(&A, 0, sizeof A);
+  A.segs = (const lg_segment*)c->d_segs.p;
+  A.seg_cap = c->seg_cap;
+  A.W = c->prm.width;
+  A.H = c->prm.height;
+  A.ntx = c->ntx;
+  A.nty = c->nty;
+  A.n_tiles = c->n_tiles;
+  A.unit_refs = UNIT_REFS;
+  for (int ch = 0; ch < 4; ++ch) {
+    const lg_blend_component& b = ch < 3 ? c->prm.color_blend : c->prm.alpha_blend;
+    A.blend.src[ch] = b.src_factor;
+    A.blend.op[ch] = b.op;
+    A.blend.constant[ch] = c->prm.blend_constant[ch];
+    A.blend.clear[ch] = c->prm.clear_color[ch];
+  }
+  A.tile_count = (uint32_t*)c->d_tile_count.p;
+  A.tile_off = (uint64_t*)c->d_tile_off.p;
+  A.tile_cursor = (unsigned long long*)c->d_tile_cursor.p;
+  A.unit_off = (uint64_t*)c->d_unit_off.p;
+  A.refs = (uint32_t*)c->d_refs.p;
+  A.refs_cap = c->refs_cap;
+  A.units = (Unit*)c->d_units.p;
+  A.units_cap = c->units_cap;
+  A.accum = c->d_accum.p;
+  A.ctr = (Counters*)c->d_ctr.p;
+  return A;
+}
+
+lg_status ensure_trace_buffers(lg_ctx* c) {
+  lg_status st;
+  if ((st = ensure(c, c->d_queue[0], c->queue_cap * sizeof(RayRec), "ray queue"))) return st;
+  if ((st = ensure(c, c->d_queue[1], c->queue_cap * sizeof(RayRec), "ray queue"))) return st;
+  if ((st = ensure(c, c->d_segs, c->seg_cap * sizeof(lg_segment), "segment ring"))) return st;
+  if (c->prm.record_paths && (st = ensure(c, c->d_paths, c->seg_cap * sizeof(lg_path_record), "path records")))
+    return st;
+  return LG_OK;
+}
+
+lg_status ensure_raster_buffers(lg_ctx* c) {
+  lg_status st;
+  const uint64_t px = (uint64_t)c->prm.width * c->prm.height;
+  const size_t elem = c->prm.accum == LG_ACCUM_F32 ? 4 : 8;
+  if ((st = ensure(c, c->d_accum, px * 4 * elem, "accumulation image"))) return st;
+  if ((st = ensure(c, c->d_tile_count, (size_t)c->n_tiles * 4, "tile counts"))) return st;
+  if ((st = ensure(c, c->d_tile_off, (size_t)c->n_tiles * 8, "tile offsets"))) return st;
+  if ((st = ensure(c, c->d_tile_cursor, (size_t)c->n_tiles * 8, "tile cursors"))) return st;
+  if ((st = ensure(c, c->d_unit_off, (size_t)c->n_tiles * 8, "unit offsets"))) return st;
+  if ((st = ensure(c, c->d_refs, c->refs_cap * 4, "tile refs"))) return st;
+  c->units_cap = c->n_tiles + c->refs_cap / UNIT_REFS + 1;
+  if ((st = ensure(c, c->d_units, c->units_cap * sizeof(Unit), "raster units"))) return st;
+  return LG_OK;
+}
+
+lg_status enqueue_trace(lg_ctx* c) {
+  const SceneDev S = scene_dev(c);
+  const TraceBufs B = trace_bufs(c);
+  CK(cudaMemsetAsync(c->d_ctr.p, 0, sizeof(Counters), c->stream), "memset counters");
+  if (c->n_lights) k_light_setup<<<1, 256, 0, c->stream>>>(S);
+  for (uint32_t g = 0; g < c->prm.max_bounce; ++g)
+    k_trace_gen<<<c->trace_grid, 256, c->smem_fits ? c->obj_smem : 0, c->stream>>>(S, B, g, c->smem_fits);
+  const uint64_t n_ov = 3ull * c->n_cubic * (c->prm.emit_control_lines ? 1 : 0) + c->prm.string_mod.modulo;
+  if (n_ov) {
+    const int blocks = (int)std::min<uint64_t>((n_ov + 255) / 256, 4096);
+    k_overlay<<<blocks, 256, 0, c->stream>>>(S, B, (const uint32_t*)c->d_cubics.p,
+                                             c->prm.emit_control_lines ? c->n_cubic : 0, c->prm.string_mod);
+  }
+  CK(cudaGetLastError(), "trace launch");
+  return LG_OK;
+}
+
+lg_status stage_event(lg_ctx* c, int i) {
+  CK(cudaEventRecordWithFlags(c->ev[i], c->stream, cudaEventRecordExternal), "stage event");
+  return LG_OK;
+}
+
+// binned_event >= 0 records that stage event between binning and the tile raster
+lg_status enqueue_accumulate(lg_ctx* c, int binned_event = -1) {
+  const RasterArgs A = raster_args(c);
+  const int fixed = c->prm.accum == LG_ACCUM_FIXED64;
+  k_clear_accum<<<c->n_sm * 8, 256, 0, c->stream>>>(A, fixed);
+  CK(cudaMemsetAsync(c->d_tile_count.p, 0, (size_t)c->n_tiles * 4, c->stream), "memset tile counts");
+  CK(cudaMemsetAsync(&((Counters*)c->d_ctr.p)->pixels, 0, sizeof(unsigned long long), c->stream), "memset pixels");
+  k_bin_count<<<c->bin_grid, 256, 0, c->stream>>>(A);
+  k_scan_tiles<<<1, 1024, 0, c->stream>>>(A);
+  k_build_units<<<std::max(1u, (c->n_tiles + 255) / 256), 256, 0, c->stream>>>(A);
+  k_bin_scatter<<<c->bin_grid, 256, 0, c->stream>>>(A);
+  if (binned_event >= 0) {
+    lg_status st = stage_event(c, binned_event);
+    if (st) return st;
+  }
+  if (fixed)
+    k_raster<true><<<c->raster_grid, 256, 4 * TILE * TILE_PAD * 8, c->stream>>>(A);
+  else
+    k_raster<false><<<c->raster_grid, 256, 4 * TILE * TILE_PAD * 4, c->stream>>>(A);
+  CK(cudaGetLastError(), "accumulate launch");
+  return LG_OK;
+}
+
+lg_status enqueue_resolve(lg_ctx* c, uint16_t* dst, size_t pitch) {
+  const int fixed = c->prm.accum == LG_ACCUM_FIXED64;
+  k_resolve_f16<<<c->n_sm * 8, 256, 0, c->stream>>>(c->d_accum.p, fixed, c->prm.width, c->prm.height, dst, pitch);
+  CK(cudaGetLastError(), "resolve launch");
+  return LG_OK;
+}
+
+lg_status sync_counters(lg_ctx* c) {
+  CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream), "read counters");
+  CK(cudaStreamSynchronize(c->stream), "synchronize");
+  if (c->h_ctr->error_flags & ERR_TMA_TIMEOUT)
+    return fail(c, LG_ERR_TIMEOUT, "object-table bulk copy did not complete within its wait limit");
+  return LG_OK;
+}
+
+bool trace_overflowed(lg_ctx* c, uint64_t& need_seg, uint64_t& need_q) {
+  need_seg = c->h_ctr->seg_count;
+  need_q = 0;
+  for (int g = 0; g <= MAX_GEN; ++g) need_q = std::max<uint64_t>(need_q, c->h_ctr->queue_count[g]);
+  return need_seg > c->seg_cap || need_q > c->queue_cap;
+}
+
+lg_status grow_trace(lg_ctx* c, uint64_t need_seg, uint64_t need_q) {
+  c->graph_valid = false;  // capacities are baked into the captured launches
+  if (need_seg > c->seg_cap) c->seg_cap = need_seg + need_seg / 4 + 1024;
+  if (need_q > c->queue_cap) c->queue_cap = need_q + need_q / 2 + 1024;
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  const double want = (double)c->seg_cap * (sizeof(lg_segment) + (c->prm.record_paths ? sizeof(lg_path_record) : 0)) +
+                      2.0 * c->queue_cap * sizeof(RayRec);
+  if (want > (double)total_b * 0.9)
+    return fail(c, LG_ERR_OUT_OF_MEMORY, "trace needs " + std::to_string(want / 1e9) + " GB of segment ring and ray queues");
+  return ensure_trace_buffers(c);
+}
+
+void fill_stats(lg_ctx* c, lg_trace_stats* s) {
+  if (!s) return;
+  const Counters& k = *c->h_ctr;
+  s->primary_rays = c->n_primary;
+  s->ray_visits = k.visits;
+  s->segments = std::min<uint64_t>(k.seg_count, c->seg_cap);
+  s->fp64_solves = k.fp64_solves;
+  s->fp64_fallbacks = k.fallbacks;
+  s->near_degenerate = k.near;
+  s->pixels = k.pixels;
+  s->tile_refs = k.tile_refs;
+}
+
+lg_status run_trace(lg_ctx* c, uint32_t& retries) {
+  for (int attempt = 0; attempt < 8; ++attempt) {
+    lg_status st = enqueue_trace(c);
+    if (st) return st;
+    if ((st = sync_counters(c))) return st;
+    uint64_t ns, nq;
+    if (!trace_overflowed(c, ns, nq)) return LG_OK;
+    ++retries;
+    if ((st = grow_trace(c, ns, nq))) return st;
+  }
+  return fail(c, LG_ERR_OUT_OF_MEMORY, "segment ring / ray queue kept overflowing");
+}
+
+lg_status run_accumulate(lg_ctx* c, uint32_t& retries) {
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    lg_status st = enqueue_accumulate(c);
+    if (st) return st;
+    if ((st = sync_counters(c))) return st;
+    if (c->h_ctr->tile_refs <= c->refs_cap) return LG_OK;
+    ++retries;
+    c->refs_cap = c->h_ctr->tile_refs + c->h_ctr->tile_refs / 8 + 4096;
+    c->graph_valid = false;
+    if ((st = ensure_raster_buffers(c))) return st;
+  }
+  return fail(c, LG_ERR_OUT_OF_MEMORY, "tile reference list kept overflowing");
+}
+
+lg_status need_scene(lg_ctx* c) {
+  if (!c) return LG_ERR_INVALID_ARGUMENT;
+  if (!c->has_scene) return fail(c, LG_ERR_NO_SCENE, "no scene uploaded");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  return LG_OK;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+}  // namespace
+
+// =============================================================================== C ABI
+extern "C" {
+
+uint32_t lg_abi_version(void) { return LG_ABI_VERSION; }
+
+void lg_params_default(lg_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof *p);
+  p->max_bounce = 5;  // tracer.rs:37
+  p->width = 512;
+  p->height = 512;
+  for (int i = 0; i < 4; ++i) p->cutoff_color[i] = 0.001f;  // tracer.rs:38
+  p->clear_color[3] = 1.0f;                                 // wgpu::Color::BLACK
+  p->color_blend = {LG_BF_ONE, LG_BF_ONE, LG_BO_ADD};       // mod.rs:67-71
+  p->alpha_blend = {LG_BF_SRC_ALPHA, LG_BF_ONE, LG_BO_ADD}; // mod.rs:62-66
+  p->accum = LG_ACCUM_FIXED64;
+  p->emit_control_lines = 1;
+}
+
+const char* lg_last_error(const lg_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+lg_status lg_create(lg_ctx** out, const lg_device_opts* opts) {
+  if (!out) return LG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  lg_ctx* c = new (std::nothrow) lg_ctx();
+  if (!c) return LG_ERR_OUT_OF_MEMORY;
+  c->device = opts ? opts->device : 0;
+  c->seg_cap_hint = opts ? opts->segment_capacity : 0;
+  c->queue_cap_hint = opts ? opts->queue_capacity : 0;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, c->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_ctr, sizeof(Counters));
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_ctr.p, sizeof(Counters));
+  for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
+  if (e != cudaSuccess) {
+    lg_status st = e == cudaErrorMemoryAllocation ? LG_ERR_OUT_OF_MEMORY : LG_ERR_CUDA;
+    (void)cudaGetLastError();
+    lg_destroy(c);
+    return st;
+  }
+  c->d_ctr.bytes = sizeof(Counters);
+  std::memset(c->h_ctr, 0, sizeof(Counters));
+  lg_params_default(&c->prm);
+  *out = c;
+  return LG_OK;
+}
+
+lg_status lg_destroy(lg_ctx* c) {
+  if (!c) return LG_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  DevBuf* bufs[] = {&c->d_scan, &c->d_info, &c->d_leaves, &c->d_prog, &c->d_lights, &c->d_cubics, &c->d_queue[0],
+                    &c->d_queue[1], &c->d_segs, &c->d_paths, &c->d_ctr, &c->d_tile_count, &c->d_tile_off,
+                    &c->d_tile_cursor, &c->d_unit_off, &c->d_refs, &c->d_units, &c->d_accum, &c->d_stage};
+  for (DevBuf* b : bufs) release(*b);
+  if (c->h_ctr) cudaFreeHost(c->h_ctr);
+  for (int i = 0; i < 6; ++i)
+    if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return LG_OK;
+}
+
+lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const lg_object* objects, uint32_t n_objects,
+                          const lg_light* lights, uint32_t n_lights, const lg_params* params) {
+  if (!c || !params || (n_geo && !geos) || (n_objects && !objects) || (n_lights && !lights))
+    return c ? fail(c, LG_ERR_INVALID_ARGUMENT, "null pointer") : LG_ERR_INVALID_ARGUMENT;
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  const lg_params& p = *params;
+  if (p.max_bounce > (uint32_t)MAX_GEN) return fail(c, LG_ERR_INVALID_ARGUMENT, "max_bounce must be <= 64");
+  if (p.width == 0 || p.height == 0 || p.width > 32768 || p.height > 32768)
+    return fail(c, LG_ERR_INVALID_ARGUMENT, "canvas must be 1..32768 pixels per side");
+  if (p.accum != LG_ACCUM_FIXED64 && p.accum != LG_ACCUM_F32) return fail(c, LG_ERR_INVALID_ARGUMENT, "unknown accum mode");
+  if (!blend_supported(p.color_blend) || !blend_supported(p.alpha_blend))
+    return fail(c, LG_ERR_UNSUPPORTED, "blend state reads the destination (order-dependent): not supported");
+  if (p.string_mod.modulo && (p.string_mod.curve != 0 || p.string_mod.mode > LG_SM_BASE))
+    return fail(c, LG_ERR_UNSUPPORTED, "string mod: only Curve::Circle with Add/Mul/Pow/Base");
+  if (p.string_mod.modulo > (1ull << 30)) return fail(c, LG_ERR_INVALID_ARGUMENT, "string mod modulo too large");
+  if (n_lights > 65535) return fail(c, LG_ERR_INVALID_ARGUMENT, "at most 65535 lights");
+  Flat F;
+  lg_status st = flatten_scene(c, geos, n_geo, objects, n_objects, lights, n_lights, F);
+  if (st) return st;
+  CK(cudaStreamSynchronize(c->stream), "synchronize");
+  const bool same_shape = c->has_scene && c->n_obj == n_objects && c->n_leaves == F.leaves.size() &&
+                          c->n_prog == F.prog.size() && c->n_lights == n_lights && c->n_cubic == F.cubics.size() &&
+                          std::memcmp(&c->prm, &p, sizeof p) == 0;
+  if ((st = ensure(c, c->d_scan, F.scan.size() * sizeof(ObjScan), "scene"))) return st;
+  if ((st = ensure(c, c->d_info, F.info.size() * sizeof(ObjInfo), "scene"))) return st;
+  if ((st = ensure(c, c->d_leaves, F.leaves.size() * sizeof(Leaf64), "scene"))) return st;
+  if ((st = ensure(c, c->d_prog, F.prog.size() + 16, "scene"))) return st;
+  if ((st = ensure(c, c->d_lights, F.lights.size() * sizeof(LightDev), "scene"))) return st;
+  if ((st = ensure(c, c->d_cubics, F.cubics.size() * 4, "scene"))) return st;
+  if (!F.scan.empty()) CK(cudaMemcpyAsync(c->d_scan.p, F.scan.data(), F.scan.size() * sizeof(ObjScan), cudaMemcpyHostToDevice, c->stream), "upload");
+  if (!F.info.empty()) CK(cudaMemcpyAsync(c->d_info.p, F.info.data(), F.info.size() * sizeof(ObjInfo), cudaMemcpyHostToDevice, c->stream), "upload");
+  if (!F.leaves.empty()) CK(cudaMemcpyAsync(c->d_leaves.p, F.leaves.data(), F.leaves.size() * sizeof(Leaf64), cudaMemcpyHostToDevice, c->stream), "upload");
+  if (!F.prog.empty()) CK(cudaMemcpyAsync(c->d_prog.p, F.prog.data(), F.prog.size(), cudaMemcpyHostToDevice, c->stream), "upload");
+  if (!F.lights.empty()) CK(cudaMemcpyAsync(c->d_lights.p, F.lights.data(), F.lights.size() * sizeof(LightDev), cudaMemcpyHostToDevice, c->stream), "upload");
+  if (!F.cubics.empty()) CK(cudaMemcpyAsync(c->d_cubics.p, F.cubics.data(), F.cubics.size() * 4, cudaMemcpyHostToDevice, c->stream), "upload");
+  CK(cudaStreamSynchronize(c->stream), "upload");
+  c->n_obj = n_objects;
+  c->n_leaves = (uint32_t)F.leaves.size();
+  c->n_prog = (uint32_t)F.prog.size();
+  c->n_lights = n_lights;
+  c->n_cubic = (uint32_t)F.cubics.size();
+  c->n_primary = 0;
+  for (uint32_t l = 0; l < n_lights; ++l) c->n_primary += lights[l].num_rays;
+  c->prm = p;
+  c->aspect = (double)((float)p.width / (float)p.height);
+  c->ntx = (p.width + TILE - 1) / TILE;
+  c->nty = (p.height + TILE - 1) / TILE;
+  c->n_tiles = c->ntx * c->nty;
+  // launch shapes
+  c->obj_smem = (size_t)n_objects * sizeof(ObjScan);
+  c->smem_fits = c->obj_smem <= OBJ_SMEM_MAX ? 1 : 0;
+  int occ = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace_gen, 256, c->smem_fits ? c->obj_smem : 0), "occupancy");
+  c->trace_grid = c->n_sm * std::max(1, occ);
+  const size_t rsm = 4 * TILE * TILE_PAD * (p.accum == LG_ACCUM_F32 ? 4 : 8);
+  if (p.accum == LG_ACCUM_F32) {
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_raster<false>, 256, rsm), "occupancy");
+  } else {
+    CK(cudaFuncSetAttribute(k_raster<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm), "smem attr");
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_raster<true>, 256, rsm), "occupancy");
+  }
+  c->raster_grid = c->n_sm * std::max(1, occ);
+  c->bin_grid = c->n_sm * 8;
+  // capacities: first guesses, grown on overflow
+  const uint64_t overlays = 3ull * F.cubics.size() + p.string_mod.modulo;
+  // an explicit capacity from lg_device_opts is honoured as given (it still grows on overflow)
+  const uint64_t want_seg = c->seg_cap_hint ? c->seg_cap_hint : 8 * c->n_primary + overlays + 1024;
+  const uint64_t want_q = c->queue_cap_hint ? c->queue_cap_hint : 2 * c->n_primary + 1024;
+  c->seg_cap = std::max(c->seg_cap, want_seg);
+  c->queue_cap = std::max(c->queue_cap, want_q);
+  if ((st = ensure_trace_buffers(c))) return st;
+  c->refs_cap = std::max<uint64_t>(c->refs_cap, 1u << 20);
+  if ((st = ensure_raster_buffers(c))) return st;
+  if ((st = ensure(c, c->d_stage, (size_t)p.width * p.height * 8, "resolve staging"))) return st;
+  if (!same_shape) c->graph_valid = false;
+  c->has_scene = true;
+  return LG_OK;
+}
+
+lg_status lg_trace(lg_ctx* c, lg_trace_stats* stats) {
+  lg_status st = need_scene(c);
+  if (st) return st;
+  uint32_t retries = 0;
+  CK(cudaEventRecord(c->ev[0], c->stream), "event");
+  if ((st = run_trace(c, retries))) return st;
+  CK(cudaEventRecord(c->ev[1], c->stream), "event");
+  CK(cudaEventSynchronize(c->ev[1]), "event");
+  if (stats) {
+    std::memset(stats, 0, sizeof *stats);
+    fill_stats(c, stats);
+    stats->retries = retries;
+    stats->trace_ms = elapsed(c->ev[0], c->ev[1]);
+    stats->total_ms = stats->trace_ms;
+  }
+  return LG_OK;
+}
+
+lg_status lg_accumulate(lg_ctx* c, lg_trace_stats* stats) {
+  lg_status st = need_scene(c);
+  if (st) return st;
+  uint32_t retries = 0;
+  CK(cudaEventRecord(c->ev[0], c->stream), "event");
+  if ((st = run_accumulate(c, retries))) return st;
+  CK(cudaEventRecord(c->ev[1], c->stream), "event");
+  CK(cudaEventSynchronize(c->ev[1]), "event");
+  if (stats) {
+    std::memset(stats, 0, sizeof *stats);
+    fill_stats(c, stats);
+    stats->retries = retries;
+    stats->accumulate_ms = elapsed(c->ev[0], c->ev[1]);
+    stats->total_ms = stats->accumulate_ms;
+  }
+  return LG_OK;
+}
+
+lg_status lg_accumulate_segments(lg_ctx* c, const lg_segment* segs, uint64_t n, lg_trace_stats* stats) {
+  lg_status st = need_scene(c);
+  if (st) return st;
+  if (n && !segs) return fail(c, LG_ERR_INVALID_ARGUMENT, "null segments");
+  if (n > c->seg_cap) {
+    c->seg_cap = n;
+    if ((st = ensure_trace_buffers(c))) return st;
+  }
+  if (n) CK(cudaMemcpyAsync(c->d_segs.p, segs, n * sizeof(lg_segment), cudaMemcpyHostToDevice, c->stream), "upload segments");
+  Counters* d = (Counters*)c->d_ctr.p;
+  CK(cudaMemsetAsync(d, 0, sizeof(Counters), c->stream), "memset counters");
+  unsigned long long nn = n;
+  CK(cudaMemcpyAsync(&d->seg_count, &nn, sizeof nn, cudaMemcpyHostToDevice, c->stream), "segment count");
+  CK(cudaStreamSynchronize(c->stream), "synchronize");
+  c->graph_valid = false;  // the ring no longer holds a trace
+  return lg_accumulate(c, stats);
+}
+
+lg_status lg_resolve_f16(lg_ctx* c, uint16_t* dst, size_t pitch, int32_t dst_is_device) {
+  lg_status st = need_scene(c);
+  if (st) return st;
+  const size_t row = (size_t)c->prm.width * 8;
+  if (!dst || pitch < row) return fail(c, LG_ERR_INVALID_ARGUMENT, "destination null or pitch < width * 8");
+  if (dst_is_device) {
+    if ((st = enqueue_resolve(c, dst, pitch))) return st;
+  } else {
+    if ((st = enqueue_resolve(c, (uint16_t*)c->d_stage.p, row))) return st;
+    CK(cudaMemcpy2DAsync(dst, pitch, c->d_stage.p, row, row, c->prm.height, cudaMemcpyDeviceToHost, c->stream), "download image");
+  }
+  CK(cudaStreamSynchronize(c->stream), "synchronize");
+  return LG_OK;
+}
+
+lg_status lg_resolve_rgba8(lg_ctx* c, uint8_t* dst, size_t pitch, int32_t dst_is_device) {
+  lg_status st = need_scene(c);
+  if (st) return st;
+  const size_t row = (size_t)c->prm.width * 4;
+  if (!dst || pitch < row) return fail(c, LG_ERR_INVALID_ARGUMENT, "destination null or pitch < width * 4");
+  const int fixed = c->prm.accum == LG_ACCUM_FIXED64;
+  uint8_t* out = dst_is_device ? dst : (uint8_t*)c->d_stage.p;
+  k_resolve_rgba8<<<c->n_sm * 8, 256, 0, c->stream>>>(c->d_accum.p, fixed, c->prm.width, c->prm.height, out,
+                                                       dst_is_device ? pitch : row);
+  CK(cudaGetLastError(), "resolve launch");
+  if (!dst_is_device)
+    CK(cudaMemcpy2DAsync(dst, pitch, c->d_stage.p, row, row, c->prm.height, cudaMemcpyDeviceToHost, c->stream), "download image");
+  CK(cudaStreamSynchronize(c->stream), "synchronize");
+  return LG_OK;
+}
+
+lg_status lg_render(lg_ctx* c, uint16_t* dst, size_t pitch, int32_t dst_is_device, lg_trace_stats* stats) {
+  lg_status st = need_scene(c);
+  if (st) return st;
+  const size_t row = (size_t)c->prm.width * 8;
+  if (!dst || pitch < row) return fail(c, LG_ERR_INVALID_ARGUMENT, "destination null or pitch < width * 8");
+  uint32_t retries = 0;
+  for (int attempt = 0; attempt < 8; ++attempt) {
+    if (!c->graph_valid) {
+      if (c->gexec) cudaGraphExecDestroy(c->gexec);
+      c->gexec = nullptr;
+      cudaGraph_t g = nullptr;
+      CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+      // timing events recorded as graph nodes: start, traced, binned, rasterised, resolved
+      lg_status s1 = stage_event(c, 0);
+      if (!s1) s1 = enqueue_trace(c);
+      if (!s1) s1 = stage_event(c, 1);
+      if (!s1) s1 = enqueue_accumulate(c, 2);
+      if (!s1) s1 = stage_event(c, 3);
+      if (!s1) s1 = enqueue_resolve(c, (uint16_t*)c->d_stage.p, row);
+      if (!s1) s1 = stage_event(c, 4);
+      cudaError_t e = cudaMemcpyAsync(c->h_ctr, c->d_ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream);
+      cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+      if (s1) { if (g) cudaGraphDestroy(g); return s1; }
+      if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(c, e, "capture counters"); }
+      if (e2 != cudaSuccess) return cuda_fail(c, e2, "end capture");
+      e = cudaGraphInstantiate(&c->gexec, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return cuda_fail(c, e, "graph instantiate");
+      c->graph_valid = true;
+    }
+    CK(cudaGraphLaunch(c->gexec, c->stream), "graph launch");
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    if (c->h_ctr->error_flags & ERR_TMA_TIMEOUT)
+      return fail(c, LG_ERR_TIMEOUT, "object-table bulk copy did not complete within its wait limit");
+    uint64_t ns, nq;
+    if (trace_overflowed(c, ns, nq)) {
+      ++retries;
+      if ((st = grow_trace(c, ns, nq))) return st;
+      continue;
+    }
+    if (c->h_ctr->tile_refs > c->refs_cap) {
+      ++retries;
+      c->refs_cap = c->h_ctr->tile_refs + c->h_ctr->tile_refs / 8 + 4096;
+      if ((st = ensure_raster_buffers(c))) return st;
+      c->graph_valid = false;
+      continue;
+    }
+    if (dst_is_device) {
+      CK(cudaMemcpy2DAsync(dst, pitch, c->d_stage.p, row, row, c->prm.height, cudaMemcpyDeviceToDevice, c->stream), "copy image");
+    } else {
+      CK(cudaMemcpy2DAsync(dst, pitch, c->d_stage.p, row, row, c->prm.height, cudaMemcpyDeviceToHost, c->stream), "download image");
+    }
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    if (stats) {
+      std::memset(stats, 0, sizeof *stats);
+      fill_stats(c, stats);
+      stats->retries = retries;
+      stats->trace_ms = elapsed(c->ev[0], c->ev[1]);
+      stats->bin_ms = elapsed(c->ev[1], c->ev[2]);
+      stats->raster_ms = elapsed(c->ev[2], c->ev[3]);
+      stats->accumulate_ms = elapsed(c->ev[1], c->ev[3]);
+      stats->resolve_ms = elapsed(c->ev[3], c->ev[4]);
+      stats->total_ms = elapsed(c->ev[0], c->ev[4]);
+    }
+    return LG_OK;
+  }
+  return fail(c, LG_ERR_OUT_OF_MEMORY, "render buffers kept overflowing");
+}
+
+lg_status lg_segments_download(lg_ctx* c, lg_segment* out, lg_path_record* paths, uint64_t cap, uint64_t* n_out) {
+  lg_status st = need_scene(c);
+  if (st) return st;
+  if (!n_out) return fail(c, LG_ERR_INVALID_ARGUMENT, "null n_out");
+  CK(cudaMemcpyAsync(c->h_ctr, c->d_ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream), "read counters");
+  CK(cudaStreamSynchronize(c->stream), "synchronize");
+  const uint64_t n = std::min<uint64_t>(c->h_ctr->seg_count, c->seg_cap);
+  *n_out = n;
+  if (cap < n) return fail(c, LG_ERR_TRUNCATED, "buffer holds fewer segments than the ring");
+  if (paths && !c->prm.record_paths) return fail(c, LG_ERR_INVALID_ARGUMENT, "path records need params.record_paths");
+  if (n && out) CK(cudaMemcpyAsync(out, c->d_segs.p, n * sizeof(lg_segment), cudaMemcpyDeviceToHost, c->stream), "download segments");
+  if (n && paths) CK(cudaMemcpyAsync(paths, c->d_paths.p, n * sizeof(lg_path_record), cudaMemcpyDeviceToHost, c->stream), "download paths");
+  CK(cudaStreamSynchronize(c->stream), "synchronize");
+  return LG_OK;
+}
+
+lg_status lg_accum_download(lg_ctx* c, void* out, uint64_t cap_bytes) {
+  lg_status st = need_scene(c);
+  if (st) return st;
+  const uint64_t bytes = (uint64_t)c->prm.width * c->prm.height * 4 * (c->prm.accum == LG_ACCUM_F32 ? 4 : 8);
+  if (!out) return fail(c, LG_ERR_INVALID_ARGUMENT, "null output");
+  if (cap_bytes < bytes) return fail(c, LG_ERR_TRUNCATED, "output smaller than the accumulation image");
+  CK(cudaMemcpyAsync(out, c->d_accum.p, bytes, cudaMemcpyDeviceToHost, c->stream), "download accumulation image");
+  CK(cudaStreamSynchronize(c->stream), "synchronize");
+  return LG_OK;
+}
+
+}  // extern "C"

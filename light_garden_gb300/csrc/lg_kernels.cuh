@@ -1,0 +1,53 @@
+// lg_kernels.cuh — kernel entry points shared between the .cu translation units.
+#pragma once
+#include "lg_device.cuh"
+
+namespace lgd {
+
+struct Unit {              // one raster work unit: a chunk of one tile's segment list
+  uint32_t tile;
+  uint32_t n;              // refs in this unit
+  uint64_t begin;          // first ref
+};
+
+struct BlendDev {
+  int32_t src[4];          // source factor per channel (lg_blend_factor)
+  int32_t op[4];           // op per channel (lg_blend_op)
+  float constant[4];
+  float clear[4];
+};
+
+struct RasterArgs {
+  const lg_segment* segs;
+  uint64_t seg_cap;
+  uint32_t W, H, ntx, nty;
+  uint32_t n_tiles;
+  uint32_t unit_refs;      // refs per work unit
+  BlendDev blend;
+  uint32_t* tile_count;    // refs per tile
+  uint64_t* tile_off;      // exclusive prefix of tile_count
+  unsigned long long* tile_cursor;
+  uint64_t* unit_off;      // exclusive prefix of units per tile
+  uint32_t* refs;          // segment index per (tile, segment) pair, grouped by tile
+  uint64_t refs_cap;
+  Unit* units;
+  uint64_t units_cap;
+  void* accum;             // H * W * 4 of int64 (FIXED64) or float (F32)
+  Counters* ctr;
+};
+
+__global__ void k_light_setup(SceneDev S);
+__global__ void k_trace_gen(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
+__global__ void k_overlay(SceneDev S, TraceBufs B, const uint32_t* cubic_objs, uint32_t n_cubic, lg_string_mod sm);
+
+__global__ void k_clear_accum(RasterArgs A, int fixed);
+__global__ void k_bin_count(RasterArgs A);
+__global__ void k_scan_tiles(RasterArgs A);
+__global__ void k_build_units(RasterArgs A);
+__global__ void k_bin_scatter(RasterArgs A);
+template <bool FIXED>
+__global__ void k_raster(RasterArgs A);
+__global__ void k_resolve_f16(const void* accum, int fixed, uint32_t W, uint32_t H, uint16_t* dst, size_t pitch);
+__global__ void k_resolve_rgba8(const void* accum, int fixed, uint32_t W, uint32_t H, uint8_t* dst, size_t pitch);
+
+}  // namespace lgd

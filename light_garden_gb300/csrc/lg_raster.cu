@@ -1,0 +1,351 @@
+// lg_raster.cu — line accumulation and resolve (sm_103a).
+//
+// The reference draws its segment list as a 1-px LineList with additive blending into an
+// Rgba16Float texture (src/sub_render_pass.rs:43-101, src/light_garden/mod.rs:57-73,
+// src/texture_renderer.rs:5) and resolves it with a textured quad
+// (src/render_to_texture.wgsl:17-28).  Here:
+//   1. k_bin_count / k_scan_tiles / k_build_units / k_bin_scatter sort (segment, tile)
+//      pairs into per-tile lists (32 x 32 px tiles) and cut each list into work units;
+//   2. k_raster: persistent CTAs take units from a device counter, accumulate the unit's
+//      segments into a shared-memory tile with shared atomics (one warp per segment, one
+//      lane per major-axis pixel), then flush the tile with one global atomic per pixel
+//      channel.  Fixed-point (int64 Q31.32) sums make the image independent of the order
+//      in which units and segments are processed, so it is bit-reproducible;
+//   3. k_resolve_f16: Q31.32 -> f32 -> binary16 (RNE), 8 B per pixel.
+#include <cuda_fp16.h>
+
+#include <type_traits>
+
+#include "lg_kernels.cuh"
+
+namespace lgd {
+
+// ------------------------------------------------------------------ blend helpers
+__device__ __forceinline__ float blend_factor(int f, int ch, const float* src, const float* k) {
+  switch (f) {
+    case LG_BF_ZERO: return 0.0f;
+    case LG_BF_ONE: return 1.0f;
+    case LG_BF_SRC: return src[ch];
+    case LG_BF_ONE_MINUS_SRC: return __fsub_rn(1.0f, src[ch]);
+    case LG_BF_SRC_ALPHA: return src[3];
+    case LG_BF_ONE_MINUS_SRC_ALPHA: return __fsub_rn(1.0f, src[3]);
+    case LG_BF_CONSTANT: return k[ch];
+    default: return __fsub_rn(1.0f, k[ch]);
+  }
+}
+
+__device__ __forceinline__ float contribution(const BlendDev& B, int ch, const float* src) {
+  if (B.op[ch] == LG_BO_MIN || B.op[ch] == LG_BO_MAX) return src[ch];
+  return __fmul_rn(src[ch], blend_factor(B.src[ch], ch, src, B.constant));
+}
+
+__device__ __forceinline__ long long ident64(int op) {
+  return op == LG_BO_MIN ? 0x7fffffffffffffffll : (op == LG_BO_MAX ? (long long)0x8000000000000000ull : 0ll);
+}
+__device__ __forceinline__ float ident32(int op) {
+  return op == LG_BO_MIN ? INFINITY : (op == LG_BO_MAX ? -INFINITY : 0.0f);
+}
+
+// ------------------------------------------------------------------ clear
+__global__ void k_clear_accum(RasterArgs A, int fixed) {
+  const uint64_t n = (uint64_t)A.W * A.H;
+  if (fixed) {
+    longlong4_32a c;
+    c.x = to_fixed(A.blend.clear[0]);
+    c.y = to_fixed(A.blend.clear[1]);
+    c.z = to_fixed(A.blend.clear[2]);
+    c.w = to_fixed(A.blend.clear[3]);
+    longlong4_32a* p = reinterpret_cast<longlong4_32a*>(A.accum);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+      p[i] = c;
+  } else {
+    const float4 c = make_float4(A.blend.clear[0], A.blend.clear[1], A.blend.clear[2], A.blend.clear[3]);
+    float4* p = reinterpret_cast<float4*>(A.accum);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+      p[i] = c;
+  }
+}
+
+// ------------------------------------------------------------------ binning
+// Visits every tile that holds at least one pixel of the segment: per tile column
+// (x-major) the minor range is bounded by the samples at both ends, since v(i) is
+// monotone in i.
+template <class F>
+__device__ __forceinline__ void for_each_tile(const RSetup& R, const RasterArgs& A, F&& f) {
+  const int nmin = (int)(R.xmajor ? A.H : A.W);
+  const int tlo = R.lo / TILE, thi = (R.hi - 1) / TILE;
+  for (int tm = tlo; tm <= thi; ++tm) {
+    const int a = max(R.lo, tm * TILE), b = min(R.hi, tm * TILE + TILE) - 1;
+    const int ja = raster_minor(R, a), jb = raster_minor(R, b);
+    int jlo = min(ja, jb), jhi = max(ja, jb);
+    if (jhi < 0 || jlo >= nmin) continue;
+    jlo = max(jlo, 0);
+    jhi = min(jhi, nmin - 1);
+    for (int tn = jlo / TILE; tn <= jhi / TILE; ++tn) {
+      const uint32_t tile = R.xmajor ? (uint32_t)tn * A.ntx + (uint32_t)tm : (uint32_t)tm * A.ntx + (uint32_t)tn;
+      f(tile);
+    }
+  }
+}
+
+__device__ __forceinline__ uint64_t n_segments(const RasterArgs& A) {
+  const unsigned long long n = A.ctr->seg_count;
+  return n < A.seg_cap ? n : A.seg_cap;
+}
+
+__global__ void __launch_bounds__(256) k_bin_count(RasterArgs A) {
+  const uint64_t n = n_segments(A);
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    RSetup R;
+    if (!raster_setup(A.segs[i], A.W, A.H, R)) continue;
+    for_each_tile(R, A, [&](uint32_t tile) {
+      // lanes of a warp usually share tiles (neighbouring rays): one atomic per group
+      const unsigned act = __activemask();
+      const unsigned grp = __match_any_sync(act, tile);
+      const int leader = __ffs(grp) - 1;
+      if ((int)lane_id() == leader) atomicAdd(&A.tile_count[tile], (unsigned)__popc(grp));
+    });
+  }
+}
+
+// single-CTA exclusive scan of refs and units per tile
+__global__ void __launch_bounds__(1024) k_scan_tiles(RasterArgs A) {
+  __shared__ unsigned long long wsum_r[32], wsum_u[32];
+  __shared__ unsigned long long carry_r, carry_u;
+  if (threadIdx.x == 0) { carry_r = 0; carry_u = 0; }
+  __syncthreads();
+  const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+  for (uint32_t base = 0; base < A.n_tiles; base += blockDim.x) {
+    const uint32_t t = base + threadIdx.x;
+    const unsigned long long c = t < A.n_tiles ? A.tile_count[t] : 0ull;
+    const unsigned long long u = (c + A.unit_refs - 1) / A.unit_refs;
+    unsigned long long ir = c, iu = u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long yr = __shfl_up_sync(0xffffffffu, ir, o), yu = __shfl_up_sync(0xffffffffu, iu, o);
+      if ((int)lane >= o) { ir += yr; iu += yu; }
+    }
+    if (lane == 31) { wsum_r[wid] = ir; wsum_u[wid] = iu; }
+    __syncthreads();
+    if (wid == 0) {
+      unsigned long long sr = lane < (blockDim.x >> 5) ? wsum_r[lane] : 0ull;
+      unsigned long long su = lane < (blockDim.x >> 5) ? wsum_u[lane] : 0ull;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long yr = __shfl_up_sync(0xffffffffu, sr, o), yu = __shfl_up_sync(0xffffffffu, su, o);
+        if ((int)lane >= o) { sr += yr; su += yu; }
+      }
+      wsum_r[lane] = sr;
+      wsum_u[lane] = su;
+    }
+    __syncthreads();
+    const unsigned long long pr = (wid ? wsum_r[wid - 1] : 0ull) + ir - c + carry_r;
+    const unsigned long long pu = (wid ? wsum_u[wid - 1] : 0ull) + iu - u + carry_u;
+    if (t < A.n_tiles) {
+      A.tile_off[t] = pr;
+      A.tile_cursor[t] = pr;
+      A.unit_off[t] = pu;
+    }
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) {
+      carry_r = pr + c;
+      carry_u = pu + u;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    A.ctr->tile_refs = carry_r;
+    A.ctr->units = carry_u;
+    A.ctr->unit_cursor = 0;
+  }
+}
+
+__global__ void k_build_units(RasterArgs A) {
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < A.n_tiles; t += gridDim.x * blockDim.x) {
+    const uint64_t c = A.tile_count[t], off = A.tile_off[t];
+    uint64_t u = A.unit_off[t];
+    for (uint64_t b = 0; b < c; b += A.unit_refs, ++u) {
+      if (u >= A.units_cap) return;
+      Unit U;
+      U.tile = t;
+      U.begin = off + b;
+      U.n = (uint32_t)(c - b < A.unit_refs ? c - b : A.unit_refs);
+      A.units[u] = U;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_bin_scatter(RasterArgs A) {
+  const uint64_t n = n_segments(A);
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    RSetup R;
+    if (!raster_setup(A.segs[i], A.W, A.H, R)) continue;
+    for_each_tile(R, A, [&](uint32_t tile) {
+      const unsigned act = __activemask();
+      const unsigned grp = __match_any_sync(act, tile);
+      const int leader = __ffs(grp) - 1;
+      unsigned long long base = 0;
+      if ((int)lane_id() == leader) base = atomicAdd(&A.tile_cursor[tile], (unsigned long long)__popc(grp));
+      base = __shfl_sync(grp, base, leader);
+      const unsigned long long slot = base + __popc(grp & lanemask_lt());
+      if (slot < A.refs_cap) A.refs[slot] = (uint32_t)i;
+    });
+  }
+}
+
+// ------------------------------------------------------------------ tile raster
+constexpr int TILE_WORDS = TILE * TILE_PAD;  // per channel
+
+template <bool FIXED>
+__global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  using acc_t = typename std::conditional<FIXED, long long, float>::type;
+  acc_t* acc = reinterpret_cast<acc_t*>(smem_raw);
+  __shared__ unsigned long long s_unit, s_pixels;
+  if (threadIdx.x == 0) s_pixels = 0;
+  const unsigned lane = lane_id(), warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const BlendDev& B = A.blend;
+  unsigned long long my_pixels = 0;
+  unsigned long long n_units = A.ctr->units;
+  if (n_units > A.units_cap) n_units = A.units_cap;
+  for (;;) {
+    if (threadIdx.x == 0) s_unit = atomicAdd(&A.ctr->unit_cursor, 1ull);
+    __syncthreads();
+    const unsigned long long u = s_unit;
+    if (u >= n_units) break;
+    const Unit U = A.units[u];
+    const uint32_t tx = U.tile % A.ntx, ty = U.tile / A.ntx;
+    for (int k = threadIdx.x; k < 4 * TILE_WORDS; k += blockDim.x) {
+      const int op = B.op[k / TILE_WORDS];
+      if (FIXED) acc[k] = (acc_t)ident64(op); else acc[k] = (acc_t)ident32(op);
+    }
+    __syncthreads();
+    const uint64_t end = U.begin + U.n;
+    for (uint64_t r = U.begin + warp; r < end; r += nwarps) {
+      if (r >= A.refs_cap) break;
+      const uint32_t si = A.refs[r];
+      const float4* sp = reinterpret_cast<const float4*>(A.segs + si);
+      const float4 g = __ldg(sp), cc = __ldg(sp + 1);
+      lg_segment s;
+      s.x0 = g.x; s.y0 = g.y; s.x1 = g.z; s.y1 = g.w;
+      s.color[0] = cc.x; s.color[1] = cc.y; s.color[2] = cc.z; s.color[3] = cc.w;
+      RSetup R;
+      if (!raster_setup(s, A.W, A.H, R)) continue;
+      const int tm = R.xmajor ? (int)tx : (int)ty, tn = R.xmajor ? (int)ty : (int)tx;
+      const int i = tm * TILE + (int)lane;
+      if (i < R.lo || i >= R.hi) continue;
+      const int j = raster_minor(R, i);
+      const int jl = j - tn * TILE;
+      const int nmin = (int)(R.xmajor ? A.H : A.W);
+      if (jl < 0 || jl >= TILE || j >= nmin) continue;
+      const int row = R.xmajor ? jl : (int)lane, col = R.xmajor ? (int)lane : jl;
+      const int cell = row * TILE_PAD + col;
+#pragma unroll
+      for (int ch = 0; ch < 4; ++ch) {
+        const float v = contribution(B, ch, s.color);
+        const int op = B.op[ch];
+        acc_t* p = acc + ch * TILE_WORDS + cell;
+        if (FIXED) {
+          const long long q = to_fixed(v);
+          if (op == LG_BO_ADD) atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)q);
+          else if (op == LG_BO_REVERSE_SUBTRACT) atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)(-q));
+          else if (op == LG_BO_MIN) atomicMin(reinterpret_cast<long long*>(p), q);
+          else atomicMax(reinterpret_cast<long long*>(p), q);
+        } else {
+          float* pf = reinterpret_cast<float*>(p);
+          if (op == LG_BO_ADD) atomicAdd(pf, v);
+          else if (op == LG_BO_REVERSE_SUBTRACT) atomicAdd(pf, -v);
+          else if (op == LG_BO_MIN) { float o = *pf; while (v < o) { const float w = __int_as_float(atomicCAS(reinterpret_cast<int*>(pf), __float_as_int(o), __float_as_int(v))); if (w == o) break; o = w; } }
+          else { float o = *pf; while (v > o) { const float w = __int_as_float(atomicCAS(reinterpret_cast<int*>(pf), __float_as_int(o), __float_as_int(v))); if (w == o) break; o = w; } }
+        }
+      }
+      ++my_pixels;
+    }
+    __syncthreads();
+    // flush: one global atomic per touched pixel channel
+    for (int k = threadIdx.x; k < TILE * TILE; k += blockDim.x) {
+      const int row = k / TILE, col = k % TILE;
+      const uint32_t x = tx * TILE + col, y = ty * TILE + row;
+      if (x >= A.W || y >= A.H) continue;
+      const uint64_t px = ((uint64_t)y * A.W + x) * 4;
+#pragma unroll
+      for (int ch = 0; ch < 4; ++ch) {
+        const acc_t v = acc[ch * TILE_WORDS + row * TILE_PAD + col];
+        const int op = B.op[ch];
+        if (FIXED) {
+          if ((long long)v == ident64(op)) continue;
+          long long* g = reinterpret_cast<long long*>(A.accum) + px + ch;
+          if (op == LG_BO_MIN) atomicMin(g, (long long)v);
+          else if (op == LG_BO_MAX) atomicMax(g, (long long)v);
+          else atomicAdd(reinterpret_cast<unsigned long long*>(g), (unsigned long long)(long long)v);
+        } else {
+          if ((float)v == ident32(op)) continue;
+          float* g = reinterpret_cast<float*>(A.accum) + px + ch;
+          if (op == LG_BO_MIN || op == LG_BO_MAX) {
+            float o = *g;
+            const float fv = (float)v;
+            while (op == LG_BO_MIN ? fv < o : fv > o) {
+              const float w = __int_as_float(atomicCAS(reinterpret_cast<int*>(g), __float_as_int(o), __float_as_int(fv)));
+              if (w == o) break;
+              o = w;
+            }
+          } else {
+            atomicAdd(g, (float)v);
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  atomicAdd(&s_pixels, my_pixels);
+  __syncthreads();
+  if (threadIdx.x == 0) atomicAdd(&A.ctr->pixels, s_pixels);
+}
+
+template __global__ void k_raster<true>(RasterArgs A);
+template __global__ void k_raster<false>(RasterArgs A);
+
+// ------------------------------------------------------------------ resolve
+__device__ __forceinline__ float4 load_px(const void* acc, int fixed, uint64_t i) {
+  if (fixed) {
+    const longlong4_32a v = reinterpret_cast<const longlong4_32a*>(acc)[i];
+    const float s = 2.3283064365386963e-10f;  // 2^-32
+    return make_float4(__fmul_rn(__ll2float_rn(v.x), s), __fmul_rn(__ll2float_rn(v.y), s),
+                       __fmul_rn(__ll2float_rn(v.z), s), __fmul_rn(__ll2float_rn(v.w), s));
+  }
+  return reinterpret_cast<const float4*>(acc)[i];
+}
+
+__global__ void k_resolve_f16(const void* acc, int fixed, uint32_t W, uint32_t H, uint16_t* dst, size_t pitch) {
+  const uint64_t n = (uint64_t)W * H;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const float4 f = load_px(acc, fixed, i);
+    const uint32_t y = (uint32_t)(i / W), x = (uint32_t)(i % W);
+    ushort4 h;
+    h.x = __half_as_ushort(__float2half_rn(f.x));
+    h.y = __half_as_ushort(__float2half_rn(f.y));
+    h.z = __half_as_ushort(__float2half_rn(f.z));
+    h.w = __half_as_ushort(__float2half_rn(f.w));
+    *reinterpret_cast<ushort4*>(reinterpret_cast<char*>(dst) + y * pitch + (uint64_t)x * 8) = h;
+  }
+}
+
+// renderer.rs:313-328: u8 = (f16 value ^ (1 / 2.2) * 255) as u8 (saturating, truncating)
+__global__ void k_resolve_rgba8(const void* acc, int fixed, uint32_t W, uint32_t H, uint8_t* dst, size_t pitch) {
+  const uint64_t n = (uint64_t)W * H;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const float4 f = load_px(acc, fixed, i);
+    const uint32_t y = (uint32_t)(i / W), x = (uint32_t)(i % W);
+    const float c[4] = {f.x, f.y, f.z, f.w};
+    uchar4 o;
+    unsigned char* po = &o.x;
+    for (int k = 0; k < 4; ++k) {
+      const float h = __half2float(__float2half_rn(c[k]));
+      const float g = __fmul_rn(powf(h, __fdiv_rn(1.0f, 2.2f)), 255.0f);
+      po[k] = (g != g || g <= 0.0f) ? 0 : (g >= 255.0f ? 255 : (unsigned char)g);
+    }
+    *reinterpret_cast<uchar4*>(dst + y * pitch + (uint64_t)x * 4) = o;
+  }
+}
+
+}  // namespace lgd

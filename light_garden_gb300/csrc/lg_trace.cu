@@ -1,0 +1,457 @@
+// lg_trace.cu — ray generation and the per-generation trace kernel (sm_103a).
+//
+// Tracer::trace (src/light_garden/tracer.rs:360-493) walks a breadth-first ray tree per
+// primary ray.  Here every generation is one persistent kernel over a device queue of
+// all live rays of all lights (the wavefront), so warps stay full no matter how the
+// trees branch:
+//   gen 0 reads a virtual queue (light, ray index) and generates the primary ray
+//   (light.rs:103-115, 163-174, 225-249); gen g > 0 reads the queue written by gen g-1.
+//   For each ray: cutoff (tracer.rs:378-384), nearest hit (412-424), medium (428-442),
+//   refract / reflect with colour split (444-481) or canvas exit (482-488).
+//   Segments are appended to the ring and children to the next queue with one atomic
+//   per warp (ballot + popc compaction).
+#include "lg_kernels.cuh"
+
+namespace lgd {
+
+// ------------------------------------------------------------- bulk copy to shared memory
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+  unsigned ok;
+  asm volatile(
+      "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(d),
+      "l"(src), "r"(bytes), "r"(b)
+      : "memory");
+}
+
+// Stages the ObjScan table into shared memory.  Returns the table to scan: shared memory
+// on success, the global table if it does not fit or the bounded wait expired (in which
+// case ERR_TMA_TIMEOUT is raised and the caller returns).
+__device__ const ObjScan* stage_objects(const SceneDev& S, ObjScan* sobj, uint64_t* bar, bool fits,
+                                        Counters* ctr, bool& failed) {
+  failed = false;
+  if (!fits || S.n_obj == 0) return S.scan;
+  const unsigned bytes = S.n_obj * (unsigned)sizeof(ObjScan);
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    mbar_expect_tx(bar, bytes);
+    const unsigned chunk = 32768u;
+    for (unsigned off = 0; off < bytes; off += chunk) {
+      const unsigned n = bytes - off < chunk ? bytes - off : chunk;
+      bulk_g2s(reinterpret_cast<char*>(sobj) + off, reinterpret_cast<const char*>(S.scan) + off, n, bar);
+    }
+  }
+  __syncthreads();  // barrier initialised before anyone waits on it
+  bool done = false;
+  for (int it = 0; it < (1 << 22) && !done; ++it) {
+    done = mbar_try_wait(bar, 0);
+    if (!done && it > 64) __nanosleep(64);
+  }
+  if (!done) {
+    atomicOr(&ctr->error_flags, ERR_TMA_TIMEOUT);
+    // give the copy a last bounded chance to land before this CTA's shared memory is released
+    for (int it = 0; it < (1 << 20) && !mbar_try_wait(bar, 0); ++it) __nanosleep(256);
+    failed = true;
+  }
+  __syncthreads();
+  return sobj;
+}
+
+// ------------------------------------------------------------------- primary rays
+__device__ inline void primary_ray(const LightDev& L, uint64_t i, double& ox, double& oy, double& dx, double& dy) {
+  const double n = (double)L.num_rays;
+  if (L.kind == LG_LIGHT_POINT) {  // light.rs:168-172
+    const double f = (double)i * 3.141592653589793 * 2.0 / n;
+    double s, c;
+    sincos(f, &s, &c);
+    ox = L.ox; oy = L.oy; dx = c; dy = s;
+  } else if (L.kind == LG_LIGHT_SPOT) {  // light.rs:230-247
+    const double sx = L.vx, sy = L.vy;
+    const double dir_angle =
+        fabs(sx) < SPOT_EPSILON ? (sy >= 0.0 ? 3.141592653589793 * 0.5 : -3.141592653589793 * 0.5) : atan(sy / sx);
+    const double min_angle = dir_angle - 0.5 * L.spot_angle;
+    const double ang = min_angle + ((double)(i + 1) / n) * L.spot_angle;
+    double s, c;
+    sincos(ang, &s, &c);
+    const double sign = signbit(sx) ? -1.0 : 1.0;
+    ox = L.ox; oy = L.oy; dx = sign * c; dy = sign * s;
+  } else {  // directional: origins along a -> b, unit left normal
+    const double ex = L.vx - L.ox, ey = L.vy - L.oy;
+    const double r = (double)i / n;
+    ox = L.ox + ex * r;
+    oy = L.oy + ey * r;
+    const double l = sqrt(ey * ey + ex * ex);
+    dx = l > 0.0 ? -ey / l : -ey;
+    dy = l > 0.0 ? ex / l : ex;
+  }
+}
+
+__global__ void k_light_setup(SceneDev S) {
+  for (uint32_t l = threadIdx.x; l < S.n_lights; l += blockDim.x) {
+    LightDev& L = S.lights[l];
+    double n = 1.0;  // tracer.rs:280-287: the last containing object wins
+    for (uint32_t k = 0; k < S.n_obj; ++k) {
+      bool near = false;
+      if ((S.info[k].flags & INFO_MATERIAL) && obj_contains64(S, k, L.ox, L.oy, near)) n = S.info[k].n;
+    }
+    L.n0 = n;
+  }
+}
+
+// ------------------------------------------------------------------- one generation
+struct Visit {
+  bool emit;
+  float x0, y0, x1, y1;
+  int hit;
+  uint8_t flags;
+  int nchild;
+  RayRec child[2];
+};
+
+__device__ __forceinline__ bool below_cutoff(const float* c, const float* k) {
+  return (c[0] < k[0] && c[1] < k[1] && c[2] < k[2]) || c[3] < k[3];
+}
+__device__ __forceinline__ bool near_cutoff(const float* c, const float* k) {
+  bool n = false;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) n |= fabsf(c[i] - k[i]) <= 1e-6f * k[i];
+  return n;
+}
+
+__device__ void visit(const SceneDev& S, const ObjScan* objs, const RayRec& r, uint32_t gen, Visit& v,
+                      unsigned long long& n_solves) {
+  v.emit = false;
+  v.nchild = 0;
+  uint8_t fl = r.flags;
+  if (near_cutoff(r.c, S.cutoff)) fl |= LG_PATH_NEAR_DEGENERATE;
+  const double ox = r.ox, oy = r.oy, dx = r.dx, dy = r.dy;
+  const float ox32 = (float)ox, oy32 = (float)oy, dx32 = (float)dx, dy32 = (float)dy;
+
+  // pass 1 (FP32): the nearest certain hit bounds the search
+  float thr = INFINITY;
+  for (uint32_t j = 0; j < S.n_obj; ++j) {
+    const float4 h = *reinterpret_cast<const float4*>(&objs[j]);
+    const float ocx = h.x - ox32, ocy = h.y - oy32;
+    const float b = ocx * dx32 + ocy * dy32, perp = ocx * dy32 - ocy * dx32;
+    const float btol = 2e-6f * (fabsf(b) + fabsf(perp) + h.z) + 1e-6f;
+    if (fabsf(perp) > h.z + btol || b + h.z + btol < -TAU32) continue;
+    const float lb = b - h.z - btol;
+    if (lb > thr) continue;
+    const Class32 c = classify32(objs[j], ox32, oy32, dx32, dy32, lb);
+    if (c.ub < INFINITY) thr = fminf(thr, c.ub * (1.0f + 1e-4f) + 1e-4f);
+  }
+  // pass 2 (FP64): re-solve every object that may hold the nearest hit, in object order
+  double best_d2 = INFINITY, ev = INFINITY, second = INFINITY;
+  int best = -1;
+  Hit64 bh;
+  for (uint32_t j = 0; j < S.n_obj; ++j) {
+    const float4 h = *reinterpret_cast<const float4*>(&objs[j]);
+    const float ocx = h.x - ox32, ocy = h.y - oy32;
+    const float b = ocx * dx32 + ocy * dy32, perp = ocx * dy32 - ocy * dx32;
+    const float btol = 2e-6f * (fabsf(b) + fabsf(perp) + h.z) + 1e-6f;
+    if (fabsf(perp) > h.z + btol || b + h.z + btol < -TAU32) continue;
+    const float lb = b - h.z - btol;
+    if (lb > thr) continue;
+    const Class32 c = classify32(objs[j], ox32, oy32, dx32, dy32, lb);
+    if (!(c.key <= thr)) continue;
+    Hit64 hh;
+    double d2;
+    ++n_solves;
+    if (obj_solve64(S, j, ox, oy, dx, dy, hh, d2, ev)) {
+      if (d2 < best_d2) {
+        second = best_d2;
+        best_d2 = d2;
+        best = (int)j;
+        bh = hh;
+      } else if (d2 < second) {
+        second = d2;
+      }
+    }
+  }
+  if (best >= 0 && second < INFINITY && second - best_d2 <= BAND * best_d2) fl |= LG_PATH_NEAR_DEGENERATE;
+  if (best >= 0 ? ev <= bh.t * (1.0 + 1e-6) + 1e-12 : ev < INFINITY) fl |= LG_PATH_NEAR_DEGENERATE;
+
+  if (best >= 0) {
+    const ObjInfo oi = S.info[best];
+    v.emit = true;
+    v.x0 = (float)ox; v.y0 = (float)oy; v.x1 = (float)bh.px; v.y1 = (float)bh.py;
+    v.hit = best;
+    if (oi.flags & INFO_MATERIAL) {
+      // medium on the far side (tracer.rs:428-442); "origin inside obj" at the midpoint
+      double n2 = 1.0;
+      bool near = false;
+      if (obj_contains64(S, (uint32_t)best, 0.5 * (ox + bh.px), 0.5 * (oy + bh.py), near)) {
+        const float px32 = (float)bh.px, py32 = (float)bh.py;
+        for (uint32_t k = 0; k < S.n_obj; ++k) {
+          if ((int)k == best) continue;
+          const float4 h = *reinterpret_cast<const float4*>(&objs[k]);
+          if (!(__float_as_uint(h.w) & INFO_MATERIAL)) continue;
+          const float ex = px32 - h.x, ey = py32 - h.y;
+          const float tol = 2e-6f * (fabsf(px32) + fabsf(py32) + fabsf(h.x) + fabsf(h.y) + h.z) + 1e-6f;
+          if (ex * ex + ey * ey > (h.z + tol) * (h.z + tol)) continue;
+          if (obj_contains64(S, k, bh.px, bh.py, near)) {
+            n2 = S.info[k].n;
+            break;
+          }
+        }
+      } else {
+        n2 = oi.n;
+      }
+      if (near) fl |= LG_PATH_NEAR_DEGENERATE;
+      // Ray::refract: Snell + unpolarised Fresnel, TIR -> reflectance 1
+      double nx = bh.nx, ny = bh.ny;
+      double ci = -(dx * nx + dy * ny);
+      if (ci < 0.0) { ci = -ci; nx = -nx; ny = -ny; }
+      const double n1 = r.n;
+      const double eta = n1 / n2;
+      const double k = 1.0 - eta * eta * (1.0 - ci * ci);
+      if (fabs(k) <= BAND) fl |= LG_PATH_NEAR_DEGENERATE;
+      double R = 1.0;
+      bool refr = false;
+      double tx = 0.0, ty = 0.0;
+      if (k >= 0.0) {
+        const double ct = sqrt(k);
+        tx = eta * dx + (eta * ci - ct) * nx;
+        ty = eta * dy + (eta * ci - ct) * ny;
+        refr = true;
+        const double ds = n1 * ci + n2 * ct, dp = n1 * ct + n2 * ci;
+        if (ds != 0.0 && dp != 0.0) {
+          const double rs = (n1 * ci - n2 * ct) / ds, rp = (n1 * ct - n2 * ci) / dp;
+          R = 0.5 * (rs * rs + rp * rp);
+        }
+      }
+      v.flags = fl | (refr ? 0 : LG_PATH_TIR);
+      const float refl = (float)R;
+      const float om = 1.0f - refl;
+      RayRec& a = v.child[0];
+      a.ox = bh.px; a.oy = bh.py; a.dx = dx + 2.0 * ci * nx; a.dy = dy + 2.0 * ci * ny;
+      a.n = n1;
+      a.c[0] = __fmul_rn(r.c[0], refl); a.c[1] = __fmul_rn(r.c[1], refl); a.c[2] = __fmul_rn(r.c[2], refl);
+      a.c[3] = r.c[3];
+      a.path = r.path;
+      a.flags = fl;
+      v.nchild = 1;
+      if (refr) {
+        RayRec& t = v.child[1];
+        t.ox = bh.px; t.oy = bh.py; t.dx = tx; t.dy = ty;
+        t.n = n2;
+        t.c[0] = __fmul_rn(r.c[0], om); t.c[1] = __fmul_rn(r.c[1], om); t.c[2] = __fmul_rn(r.c[2], om);
+        t.c[3] = r.c[3];
+        t.path = r.path | (1ull << gen);
+        t.flags = fl;
+        v.nchild = 2;
+      }
+    } else {
+      v.flags = fl;
+      const double dn = dx * bh.nx + dy * bh.ny;  // Ray::reflect
+      RayRec& a = v.child[0];
+      a.ox = bh.px; a.oy = bh.py; a.dx = dx - 2.0 * dn * bh.nx; a.dy = dy - 2.0 * dn * bh.ny;
+      a.n = r.n;
+      a.c[0] = r.c[0]; a.c[1] = r.c[1]; a.c[2] = r.c[2]; a.c[3] = r.c[3];
+      a.path = r.path;
+      a.flags = fl;
+      v.nchild = 1;
+    }
+  } else {
+    // canvas exit: nearest hit with the canvas rectangle (tracer.rs:482-488)
+    Leaf64 canvas;
+    canvas.kind = LEAF_RECT;
+    canvas.p[0] = 0.0; canvas.p[1] = 0.0; canvas.p[2] = 1.0; canvas.p[3] = 0.0;
+    canvas.p[4] = S.aspect; canvas.p[5] = 1.0;
+    Hit64 ch[3];
+    double cev = INFINITY;
+    const int nh = leaf_hits64(canvas, ox, oy, dx, dy, ch, cev);
+    if (nh > 0) {
+      int bi = 0;
+      for (int q = 1; q < nh; ++q)
+        if (ch[q].t < ch[bi].t) bi = q;
+      v.emit = true;
+      v.x0 = (float)ox; v.y0 = (float)oy; v.x1 = (float)ch[bi].px; v.y1 = (float)ch[bi].py;
+      v.hit = -1;
+      v.flags = fl | (cev < INFINITY ? LG_PATH_NEAR_DEGENERATE : 0);
+    }
+  }
+  // children: the next generation skips colours below the cutoff (tracer.rs:378-384)
+  int w = 0;
+  for (int q = 0; q < v.nchild; ++q) {
+    RayRec c = v.child[q];
+    if (gen + 1 >= S.max_bounce || below_cutoff(c.c, S.cutoff)) continue;
+    c.gen = (uint8_t)(gen + 1);
+    c.prim = r.prim;
+    c.light = r.light;
+    if (near_cutoff(c.c, S.cutoff)) c.flags |= LG_PATH_NEAR_DEGENERATE;
+    v.child[w++] = c;
+  }
+  v.nchild = w;
+}
+
+__global__ void __launch_bounds__(256) k_trace_gen(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ unsigned long long blk_visits, blk_solves, blk_near;
+  if (threadIdx.x == 0) { blk_visits = 0; blk_solves = 0; blk_near = 0; }
+  bool failed;
+  const ObjScan* objs = stage_objects(S, reinterpret_cast<ObjScan*>(smem_raw), &bar, smem_fits != 0, B.ctr, failed);
+  if (failed) return;
+
+  unsigned long long n_in;
+  if (gen == 0) {
+    n_in = S.n_primary;
+  } else {
+    n_in = B.ctr->queue_count[gen];
+    if (n_in > B.queue_cap) n_in = B.queue_cap;
+  }
+  const RayRec* qin = B.queue[gen & 1];
+  RayRec* qout = B.queue[(gen + 1) & 1];
+  const unsigned lane = lane_id();
+  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+  unsigned long long my_visits = 0, my_solves = 0, my_near = 0;
+
+  for (uint64_t base = warp * 32; base < n_in; base += nwarps * 32) {
+    const uint64_t idx = base + lane;
+    Visit v;
+    v.emit = false;
+    v.nchild = 0;
+    RayRec r;
+    bool live = idx < n_in;
+    if (live) {
+      if (gen == 0) {
+        uint32_t l = 0;
+        while (l + 1 < S.n_lights && S.lights[l + 1].first <= idx) ++l;
+        const LightDev& L = S.lights[l];
+        const uint64_t i = idx - L.first;
+        primary_ray(L, i, r.ox, r.oy, r.dx, r.dy);
+        r.n = L.n0;
+        r.c[0] = L.color[0]; r.c[1] = L.color[1]; r.c[2] = L.color[2]; r.c[3] = L.color[3];
+        r.path = 0;
+        r.prim = (uint32_t)i;
+        r.light = (uint16_t)l;
+        r.gen = 0;
+        r.flags = 0;
+      } else {
+        r = qin[idx];
+      }
+      if (below_cutoff(r.c, S.cutoff)) live = false;
+    }
+    if (live) {
+      ++my_visits;
+      visit(S, objs, r, gen, v, my_solves);
+    }
+    // segments: one atomic per warp
+    const unsigned emask = __ballot_sync(0xffffffffu, v.emit);
+    if (emask) {
+      unsigned long long sbase = 0;
+      const int leader = __ffs(emask) - 1;
+      if ((int)lane == leader) sbase = atomicAdd(&B.ctr->seg_count, (unsigned long long)__popc(emask));
+      sbase = __shfl_sync(0xffffffffu, sbase, leader);
+      if (v.emit) {
+        const unsigned long long slot = sbase + __popc(emask & lanemask_lt());
+        if (v.flags & LG_PATH_NEAR_DEGENERATE) ++my_near;
+        if (slot < B.seg_cap) {
+          float4* dst = reinterpret_cast<float4*>(B.segs + slot);
+          dst[0] = make_float4(v.x0, v.y0, v.x1, v.y1);
+          dst[1] = make_float4(r.c[0], r.c[1], r.c[2], r.c[3]);
+          if (S.record_paths) {
+            lg_path_record pr;
+            pr.path = r.path; pr.primary = r.prim; pr.light = r.light; pr.gen = (uint8_t)gen;
+            pr.flags = v.flags; pr.hit = v.hit; pr.source = LG_SRC_TRACE;
+            B.paths[slot] = pr;
+          }
+        }
+      }
+    }
+    // children: warp prefix sum of 0..2 per lane, one atomic per warp
+    int incl = v.nchild;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if ((int)lane >= o) incl += y;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total > 0 && gen + 1 < S.max_bounce) {
+      unsigned long long qbase = 0;
+      if (lane == 31) qbase = atomicAdd(&B.ctr->queue_count[gen + 1], (unsigned long long)total);
+      qbase = __shfl_sync(0xffffffffu, qbase, 31);
+      const unsigned long long first = qbase + (unsigned long long)(incl - v.nchild);
+      for (int q = 0; q < v.nchild; ++q)
+        if (first + q < B.queue_cap) qout[first + q] = v.child[q];
+    }
+  }
+  atomicAdd(&blk_visits, my_visits);
+  atomicAdd(&blk_solves, my_solves);
+  atomicAdd(&blk_near, my_near);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    atomicAdd(&B.ctr->visits, blk_visits);
+    atomicAdd(&B.ctr->fp64_solves, blk_solves);
+    atomicAdd(&B.ctr->near, blk_near);
+  }
+}
+
+// ------------------------------------------------------------------- overlays
+// Curved-mirror control lines (tracer.rs:341-346) and the string-mod chords
+// (string_mod.rs:45-55, 104-122) appended after the traced segments.
+__global__ void k_overlay(SceneDev S, TraceBufs B, const uint32_t* cubic_objs, uint32_t n_cubic,
+                          lg_string_mod sm) {
+  const uint64_t n_ctrl = 3ull * n_cubic;
+  const uint64_t total = n_ctrl + sm.modulo;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+    lg_segment s;
+    lg_path_record pr;
+    pr.path = 0; pr.light = 0xffff; pr.flags = 0; pr.hit = -1;
+    if (i < n_ctrl) {
+      const uint32_t k = cubic_objs[i / 3];
+      const int q = (int)(i % 3);
+      const Leaf64& L = S.leaves[S.info[k].leaf_begin];
+      s.x0 = (float)L.p[2 * q]; s.y0 = (float)L.p[2 * q + 1];
+      s.x1 = (float)L.p[2 * q + 2]; s.y1 = (float)L.p[2 * q + 3];
+      s.color[0] = 1.f; s.color[1] = 0.f; s.color[2] = 0.f; s.color[3] = 1.f;
+      pr.primary = k; pr.gen = (uint8_t)q; pr.source = LG_SRC_CONTROL_LINE;
+    } else {
+      const uint64_t m = sm.modulo, iix = i - n_ctrl;
+      uint64_t ix;
+      if (sm.mode == LG_SM_ADD) ix = (iix + sm.num) % m;
+      else if (sm.mode == LG_SM_MUL) ix = (iix * sm.num) % m;
+      else {
+        uint64_t b = sm.mode == LG_SM_POW ? iix : sm.num, e = sm.mode == LG_SM_POW ? (uint32_t)sm.num : (uint32_t)iix, p = 1;
+        while (e) { if (e & 1) p *= b; b *= b; e >>= 1; }
+        ix = p % m;
+      }
+      const double aa = (double)(sm.turns * (iix % m)) * (2.0 * 3.141592653589793) / (double)m;
+      const double ab = (double)(sm.turns * (ix % m)) * (2.0 * 3.141592653589793) / (double)m;
+      double sa, ca, sb, cb;
+      sincos(aa, &sa, &ca);
+      sincos(ab, &sb, &cb);
+      s.x0 = (float)ca; s.y0 = (float)sa; s.x1 = (float)cb; s.y1 = (float)sb;
+      s.color[0] = sm.color[0]; s.color[1] = sm.color[1]; s.color[2] = sm.color[2]; s.color[3] = sm.color[3];
+      pr.primary = (uint32_t)iix; pr.gen = 0; pr.source = LG_SRC_STRING_MOD;
+    }
+    const unsigned long long slot = atomicAdd(&B.ctr->seg_count, 1ull);
+    if (slot < B.seg_cap) {
+      B.segs[slot] = s;
+      if (S.record_paths) B.paths[slot] = pr;
+    }
+  }
+}
+
+}  // namespace lgd

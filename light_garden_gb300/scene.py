@@ -1,0 +1,273 @@
+"""Scene model with the reference's names, packed into the C ABI tables of ``lg.h``.
+
+Mirrors light_garden's scene types:
+
+* geometry  (collision2d ``Geo``): :class:`Circle`, :class:`Rect`, :class:`LineSegment`,
+  :class:`CubicBezier`, :class:`Logic` (with ``&``, ``|`` and :meth:`Geo.and_not`, as
+  used by ``LightGarden::mouse_clicked``, src/light_garden/mod.rs:366-372);
+* objects   (``Object``/``ObjectE``, src/light_garden/object.rs:7-16,51-113):
+  :class:`Object` with the constructors ``new_mirror``, ``new_curved_mirror``,
+  ``new_circle``, ``new_rect``, ``new_lens``, ``new_geo`` and ``material_opt``;
+* lights    (``Light``, src/light_garden/light.rs:10-14): :class:`PointLight`,
+  :class:`SpotLight`, :class:`DirectionalLight`.
+
+:func:`pack` flattens a list of objects and lights into ``lg_geo``/``lg_object``/
+``lg_light`` arrays: one node array holding every geometry tree, objects naming their
+root node.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence, Tuple
+
+from . import abi
+
+P2 = Tuple[float, float]
+Color = Tuple[float, float, float, float]
+
+
+def _rot(angle: float) -> Tuple[float, float]:
+    return (math.cos(angle), math.sin(angle))
+
+
+class Geo:
+    """Base class of geometry nodes (collision2d ``Geo``)."""
+
+    def __and__(self, other: "Geo") -> "Logic":
+        return Logic(abi.LG_OP_AND, self, other)
+
+    def __or__(self, other: "Geo") -> "Logic":
+        return Logic(abi.LG_OP_OR, self, other)
+
+    def and_not(self, other: "Geo") -> "Logic":
+        return Logic(abi.LG_OP_AND_NOT, self, other)
+
+
+@dataclass
+class Circle(Geo):
+    origin: P2
+    radius: float
+
+
+@dataclass
+class Rect(Geo):
+    """Rect { origin (centre), rotation, width, height }; ``rotation`` is (cos, sin)."""
+    origin: P2
+    width: float
+    height: float
+    rotation: Tuple[float, float] = (1.0, 0.0)
+
+    @staticmethod
+    def from_tlbr(top: float, left: float, bottom: float, right: float) -> "Rect":
+        return Rect(((left + right) * 0.5, (top + bottom) * 0.5), right - left, top - bottom)
+
+
+@dataclass
+class LineSegment(Geo):
+    a: P2
+    b: P2
+
+    @staticmethod
+    def from_ab(a: P2, b: P2) -> "LineSegment":
+        return LineSegment(a, b)
+
+
+@dataclass
+class CubicBezier(Geo):
+    points: Tuple[P2, P2, P2, P2]
+
+    def get_control_lines(self) -> List[Tuple[P2, Color]]:
+        """CurvedMirror::get_control_lines (object.rs:355-365): red control polygon."""
+        red = (1.0, 0.0, 0.0, 1.0)
+        p = self.points
+        return [(p[0], red), (p[1], red), (p[1], red), (p[2], red), (p[2], red), (p[3], red)]
+
+
+@dataclass
+class Logic(Geo):
+    """Logic { op, a, b, origin, rotation }: children live in the node's local frame."""
+    op: int
+    a: Geo
+    b: Geo
+    origin: P2 = (0.0, 0.0)
+    rotation: Tuple[float, float] = (1.0, 0.0)
+
+
+@dataclass
+class Material:
+    refractive_index: float = 1.2  # Material::default, object.rs:441-447
+
+
+@dataclass
+class Object:
+    kind: int
+    geo: Geo
+    material_opt: Optional[Material]
+
+    @staticmethod
+    def new_mirror(a: P2, b: P2) -> "Object":
+        return Object(abi.LG_OBJ_STRAIGHT_MIRROR, LineSegment(a, b), None)
+
+    @staticmethod
+    def new_curved_mirror(cubic: CubicBezier) -> "Object":
+        return Object(abi.LG_OBJ_CURVED_MIRROR, cubic, None)
+
+    @staticmethod
+    def new_circle(origin: P2, radius: float) -> "Object":
+        return Object(abi.LG_OBJ_CIRCLE, Circle(origin, radius), Material())
+
+    @staticmethod
+    def new_rect(origin: P2, width: float, height: float) -> "Object":
+        return Object(abi.LG_OBJ_RECT, Rect(origin, width, height), Material())
+
+    @staticmethod
+    def new_lens(origin: P2, radius: float, distance: float) -> "Object":
+        # Lens::new, object.rs:393-411: And of two circles at (+-distance/2, 0)
+        lg = Logic(abi.LG_OP_AND, Circle((distance * 0.5, 0.0), radius),
+                   Circle((-distance * 0.5, 0.0), radius), origin)
+        return Object(abi.LG_OBJ_LENS, lg, Material())
+
+    @staticmethod
+    def new_geo(geo: Geo) -> "Object":
+        return Object(abi.LG_OBJ_GEO, geo, Material())
+
+    def get_material(self) -> Optional[Material]:
+        return self.material_opt
+
+
+@dataclass
+class PointLight:
+    position: P2
+    num_rays: int
+    color: Color
+
+    def set_num_rays(self, n: Optional[int]) -> None:
+        if n is not None:
+            self.num_rays = n
+
+
+@dataclass
+class SpotLight:
+    position: P2
+    spot_angle: float
+    spot_direction: P2
+    num_rays: int
+    color: Color
+
+    def set_num_rays(self, n: Optional[int]) -> None:
+        if n is not None:
+            self.num_rays = n
+
+
+@dataclass
+class DirectionalLight:
+    color: Color
+    num_rays: int
+    start: LineSegment
+
+    def set_num_rays(self, n: Optional[int]) -> None:
+        if n is not None:
+            self.num_rays = n
+
+
+Light = object  # PointLight | SpotLight | DirectionalLight
+
+
+# ---- packing --------------------------------------------------------------------------------
+def _emit_geo(g: Geo, nodes: list) -> int:
+    idx = len(nodes)
+    rec = abi.lg_geo()
+    rec.rot[0], rec.rot[1] = 1.0, 0.0
+    nodes.append(rec)
+    if isinstance(g, Circle):
+        rec.kind = abi.LG_GEO_CIRCLE
+        rec.origin[:] = g.origin
+        rec.v[0] = g.radius
+    elif isinstance(g, Rect):
+        rec.kind = abi.LG_GEO_RECT
+        rec.origin[:] = g.origin
+        rec.rot[:] = g.rotation
+        rec.v[0], rec.v[1] = g.width, g.height
+    elif isinstance(g, LineSegment):
+        rec.kind = abi.LG_GEO_SEGMENT
+        rec.v[0], rec.v[1] = g.a
+        rec.v[2], rec.v[3] = g.b
+    elif isinstance(g, CubicBezier):
+        rec.kind = abi.LG_GEO_CUBIC
+        for k, p in enumerate(g.points):
+            rec.v[2 * k], rec.v[2 * k + 1] = p
+    elif isinstance(g, Logic):
+        rec.kind = abi.LG_GEO_LOGIC
+        rec.op = g.op
+        rec.origin[:] = g.origin
+        rec.rot[:] = g.rotation
+        a = _emit_geo(g.a, nodes)
+        b = _emit_geo(g.b, nodes)
+        nodes[idx].a, nodes[idx].b = a, b
+    else:
+        raise TypeError(f"unsupported geometry {type(g).__name__}")
+    return idx
+
+
+def pack_light(light) -> abi.lg_light:
+    rec = abi.lg_light()
+    rec.num_rays = int(light.num_rays)
+    rec.color[:] = tuple(float(c) for c in light.color)
+    if isinstance(light, PointLight):
+        rec.kind = abi.LG_LIGHT_POINT
+        rec.origin[:] = light.position
+    elif isinstance(light, SpotLight):
+        rec.kind = abi.LG_LIGHT_SPOT
+        rec.origin[:] = light.position
+        rec.v[:] = light.spot_direction
+        rec.spot_angle = light.spot_angle
+    elif isinstance(light, DirectionalLight):
+        rec.kind = abi.LG_LIGHT_DIRECTIONAL
+        rec.origin[:] = light.start.a
+        rec.v[:] = light.start.b
+    else:
+        raise TypeError(f"unsupported light {type(light).__name__}")
+    return rec
+
+
+@dataclass
+class PackedScene:
+    geos: object
+    n_geo: int
+    objects: object
+    n_objects: int
+    lights: object
+    n_lights: int
+    params: abi.lg_params = field(default_factory=abi.params_default)
+
+    def args(self):
+        """Positional arguments of lg_scene_upload / lgo_trace after the context."""
+        return (self.geos, self.n_geo, self.objects, self.n_objects, self.lights, self.n_lights)
+
+
+def pack(objects: Sequence[Object], lights: Sequence, params: Optional[abi.lg_params] = None) -> PackedScene:
+    nodes: list = []
+    objs = (abi.lg_object * max(1, len(objects)))()
+    for k, ob in enumerate(objects):
+        root = _emit_geo(ob.geo, nodes)
+        objs[k].kind = ob.kind
+        objs[k].geo = root
+        objs[k].has_material = 1 if ob.material_opt is not None else 0
+        objs[k].refractive_index = ob.material_opt.refractive_index if ob.material_opt else 1.0
+    geos = (abi.lg_geo * max(1, len(nodes)))(*nodes)
+    lts = (abi.lg_light * max(1, len(lights)))(*[pack_light(l) for l in lights])
+    return PackedScene(geos, len(nodes), objs, len(objects), lts, len(lights),
+                       params if params is not None else abi.params_default())
+
+
+def canvas_bounds(width: int, height: int) -> Rect:
+    """Rect::from_tlbr(1, -aspect, -1, aspect) with the f32 aspect of sub_render_pass.rs:146-156."""
+    import numpy as np
+    aspect = float(np.float32(width) / np.float32(height))
+    return Rect.from_tlbr(1.0, -aspect, -1.0, aspect)
+
+
+def rotation(angle: float) -> Tuple[float, float]:
+    """A Rot2 as (cos, sin)."""
+    return _rot(angle)

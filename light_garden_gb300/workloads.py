@@ -1,0 +1,176 @@
+"""Seeded synthetic scenes with the shapes, sizes and value distributions of the five
+benchmark configurations of the trace-and-accumulate path.
+
+The reference publishes no benchmark scenes; its only scene file is ``default.ron``.  These
+generators stand in for the configurations:
+
+* :func:`plain_small`   1 point light (4096 rays) + circle (r 0.2, n 1.5) + flat mirror,
+                        8 bounces, 512x512, FP32 accumulation;
+* :func:`mid_scene`     64 objects (rect / circle / mirror / curved mirror), 8 lights x 2^18
+                        rays, 16 bounces, 1920x1080, 64-bit fixed point;
+* :func:`csg_scene`     256 CSG objects (circle op rect), 2^22 rays, 32 bounces, 4096x4096,
+                        string-mod overlay (m = 4096, chords i -> 7 i mod m);
+* :func:`batch_scenes`  mixed sizes: objects log-uniform [4, 1024], rays log-uniform
+                        [2^12, 2^20], bounces U{4..32}, canvases {256, 512, 1024, 2048}^2.
+
+Choices the configurations leave open (spot angle U[10, 90] degrees, directional segment
+length U[0.1, 0.5], the curved-mirror template, the CSG child placement) are made here
+and fixed by the seed.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+from typing import List, Optional
+
+import numpy as np
+
+from . import abi
+from .scene import (Circle, CubicBezier, DirectionalLight, LineSegment, Logic, Material, Object,
+                    PackedScene, PointLight, Rect, SpotLight, pack)
+
+# control polygon of a curved mirror in its local frame (an arch), scaled by the object size
+_CUBIC_TEMPLATE = np.array([[-1.0, -0.5], [-0.35, 0.6], [0.35, 0.6], [1.0, -0.5]])
+
+
+@dataclass
+class Workload:
+    name: str
+    objects: List[Object]
+    lights: list
+    params: abi.lg_params
+
+    def packed(self) -> PackedScene:
+        return pack(self.objects, self.lights, self.params)
+
+    @property
+    def primary_rays(self) -> int:
+        return int(sum(l.num_rays for l in self.lights))
+
+
+def _params(max_bounce: int, width: int, height: int, accum: int) -> abi.lg_params:
+    p = abi.params_default()
+    p.max_bounce = max_bounce
+    p.width, p.height = width, height
+    p.accum = accum
+    return p
+
+
+def plain_small(accum: int = abi.LG_ACCUM_F32, num_rays: int = 4096) -> Workload:
+    objects = [
+        Object(abi.LG_OBJ_CIRCLE, Circle((0.0, 0.0), 0.2), Material(1.5)),
+        Object.new_mirror((0.6, -0.5), (0.6, 0.5)),
+    ]
+    lights = [PointLight((-0.8, 0.0), num_rays, (1.0, 1.0, 1.0, 1.0))]
+    return Workload("plain_small", objects, lights, _params(8, 512, 512, accum))
+
+
+def _rand_rot(rng) -> tuple:
+    a = rng.uniform(0.0, 2.0 * math.pi)
+    return (math.cos(a), math.sin(a))
+
+
+def _rand_object(rng, kind: str) -> Object:
+    c = tuple(rng.uniform(-1.0, 1.0, 2))
+    size = rng.uniform(0.02, 0.15)
+    cs = _rand_rot(rng)
+    n = rng.uniform(1.3, 1.8)
+    if kind == "circle":
+        return Object(abi.LG_OBJ_CIRCLE, Circle(c, size), Material(n))
+    if kind == "rect":
+        hh = rng.uniform(0.02, 0.15)
+        return Object(abi.LG_OBJ_RECT, Rect(c, 2.0 * size, 2.0 * hh, cs), Material(n))
+    if kind == "mirror":
+        d = np.array(cs) * size
+        return Object.new_mirror((c[0] - d[0], c[1] - d[1]), (c[0] + d[0], c[1] + d[1]))
+    # curved mirror
+    R = np.array([[cs[0], -cs[1]], [cs[1], cs[0]]])
+    pts = (_CUBIC_TEMPLATE * size) @ R.T + np.array(c)
+    return Object.new_curved_mirror(CubicBezier(tuple(tuple(p) for p in pts)))
+
+
+def _rand_light(rng, kind: str, num_rays: int):
+    pos = tuple(rng.uniform(-1.0, 1.0, 2))
+    color = (float(rng.uniform()), float(rng.uniform()), float(rng.uniform()), 1.0)
+    if kind == "point":
+        return PointLight(pos, num_rays, color)
+    if kind == "spot":
+        a = rng.uniform(0.0, 2.0 * math.pi)
+        ang = math.radians(rng.uniform(10.0, 90.0))
+        return SpotLight(pos, ang, (math.cos(a), math.sin(a)), num_rays, color)
+    half = 0.5 * rng.uniform(0.1, 0.5)
+    cs = _rand_rot(rng)
+    a = (pos[0] - half * cs[0], pos[1] - half * cs[1])
+    b = (pos[0] + half * cs[0], pos[1] + half * cs[1])
+    return DirectionalLight(color, num_rays, LineSegment(a, b))
+
+
+def mid_scene(seed: int = 2, accum: int = abi.LG_ACCUM_FIXED64, rays_per_light: int = 1 << 18,
+              n_objects: int = 64, n_lights: int = 8) -> Workload:
+    rng = np.random.default_rng(seed)
+    kinds = ["rect", "circle", "mirror", "curved"]
+    objects = [_rand_object(rng, kinds[rng.integers(0, 4)]) for _ in range(n_objects)]
+    lkinds = ["point", "directional", "spot"]
+    lights = [_rand_light(rng, lkinds[rng.integers(0, 3)], rays_per_light) for _ in range(n_lights)]
+    return Workload("mid_scene", objects, lights, _params(16, 1920, 1080, accum))
+
+
+def _csg_object(rng) -> Object:
+    op = int(rng.integers(0, 3))
+    c = tuple(rng.uniform(-1.0, 1.0, 2))
+    circle = Circle(tuple(rng.uniform(-0.05, 0.05, 2)), rng.uniform(0.02, 0.15))
+    rect = Rect((0.0, 0.0), 2.0 * rng.uniform(0.02, 0.15), 2.0 * rng.uniform(0.02, 0.15), _rand_rot(rng))
+    return Object(abi.LG_OBJ_GEO, Logic(op, circle, rect, c, _rand_rot(rng)), Material(rng.uniform(1.3, 1.8)))
+
+
+def csg_scene(seed: int = 3, total_rays: int = 1 << 22, n_objects: int = 256, n_lights: int = 8,
+              width: int = 4096, height: int = 4096, string_mod: bool = True) -> Workload:
+    rng = np.random.default_rng(seed)
+    objects = [_csg_object(rng) for _ in range(n_objects)]
+    lkinds = ["point", "directional", "spot"]
+    per = total_rays // n_lights
+    lights = [_rand_light(rng, lkinds[rng.integers(0, 3)], per) for _ in range(n_lights)]
+    p = _params(32, width, height, abi.LG_ACCUM_FIXED64)
+    if string_mod:
+        p.string_mod.modulo = 4096
+        p.string_mod.num = 7
+        p.string_mod.turns = 1
+        p.string_mod.mode = abi.LG_SM_MUL
+        p.string_mod.curve = 0
+        p.string_mod.color[:] = (0.25, 0.25, 0.25, 1.0)
+    return Workload("csg_scene", objects, lights, p)
+
+
+def _log_uniform_int(rng, lo: float, hi: float) -> int:
+    return int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+
+
+def batch_scene(rng) -> Workload:
+    n_obj = _log_uniform_int(rng, 4, 1024)
+    rays = _log_uniform_int(rng, 1 << 12, 1 << 20)
+    bounces = int(rng.integers(4, 33))
+    side = int(rng.choice([256, 512, 1024, 2048]))
+    kinds = ["rect", "circle", "mirror", "curved", "csg"]
+    objects = []
+    for _ in range(n_obj):
+        k = kinds[rng.integers(0, 5)]
+        objects.append(_csg_object(rng) if k == "csg" else _rand_object(rng, k))
+    n_lights = int(rng.integers(1, 9))
+    per = max(1, rays // n_lights)
+    lkinds = ["point", "directional", "spot"]
+    lights = [_rand_light(rng, lkinds[rng.integers(0, 3)], per) for _ in range(n_lights)]
+    return Workload("batch_scene", objects, lights, _params(bounces, side, side, abi.LG_ACCUM_FIXED64))
+
+
+def batch_scenes(seed: int = 4, count: int = 512) -> List[Workload]:
+    rng = np.random.default_rng(seed)
+    return [batch_scene(rng) for _ in range(count)]
+
+
+def scale_rays(w: Workload, factor: float) -> Workload:
+    """The same scene with every light's ray count scaled (for bounded CPU samples)."""
+    import copy
+    w2 = copy.deepcopy(w)
+    for l in w2.lights:
+        l.num_rays = max(1, int(round(l.num_rays * factor)))
+    return w2

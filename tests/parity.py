@@ -1,0 +1,81 @@
+"""Path-keyed comparison of a GPU trace against the CPU oracle's trace.
+
+Both sides key every segment by (source, light, primary, generation, path bits).  The
+tolerances are the spec ones: hit-object ids and the set of segments match exactly
+outside the near-degenerate set (segments flagged LG_PATH_NEAR_DEGENERATE on either side,
+which includes every descendant of a flagged decision), and endpoints match within
+ENDPOINT_TOL relative to max(1, |p|).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+ENDPOINT_TOL = 1e-5
+NEAR = 1
+
+
+def _keys(paths: np.ndarray) -> np.ndarray:
+    return (paths["source"].astype(np.uint64) << np.uint64(60)) ^ (paths["light"].astype(np.uint64) << np.uint64(44)) \
+        ^ (paths["primary"].astype(np.uint64) << np.uint64(8)) ^ paths["gen"].astype(np.uint64)
+
+
+@dataclass
+class ParityReport:
+    matched: int
+    gpu_only: int
+    oracle_only: int
+    gpu_only_unflagged: int
+    oracle_only_unflagged: int
+    hit_mismatch_unflagged: int
+    color_mismatch_unflagged: int
+    max_endpoint_err: float
+    flagged: int
+
+    def ok(self) -> bool:
+        return (self.gpu_only_unflagged == 0 and self.oracle_only_unflagged == 0 and
+                self.hit_mismatch_unflagged == 0 and self.color_mismatch_unflagged == 0 and
+                self.max_endpoint_err <= ENDPOINT_TOL)
+
+
+def compare(g_segs, g_paths, o_segs, o_paths, o_s64, primary_filter=None) -> ParityReport:
+    if primary_filter is not None:
+        keep = (g_paths["source"] != 0) | primary_filter(g_paths["primary"])
+        g_segs, g_paths = g_segs[keep], g_paths[keep]
+    gi = {}
+    for i, (k, p) in enumerate(zip(_keys(g_paths).tolist(), g_paths["path"].tolist())):
+        gi[(k, p)] = i
+    oi = {}
+    for i, (k, p) in enumerate(zip(_keys(o_paths).tolist(), o_paths["path"].tolist())):
+        oi[(k, p)] = i
+    common = gi.keys() & oi.keys()
+    g_only = gi.keys() - oi.keys()
+    o_only = oi.keys() - gi.keys()
+    gflag = (g_paths["flags"] & NEAR) != 0
+    oflag = (o_paths["flags"] & NEAR) != 0
+    ig = np.array([gi[k] for k in common], dtype=np.int64)
+    io = np.array([oi[k] for k in common], dtype=np.int64)
+    flagged = gflag[ig] | oflag[io] if len(ig) else np.zeros(0, bool)
+    clean_g, clean_o = ig[~flagged], io[~flagged]
+    hit_mm = int((g_paths["hit"][clean_g] != o_paths["hit"][clean_o]).sum())
+    col_mm = int((g_segs["color"][clean_g] != o_segs["color"][clean_o]).any(axis=1).sum())
+    if len(clean_g):
+        gp = np.stack([g_segs["x0"][clean_g], g_segs["y0"][clean_g], g_segs["x1"][clean_g], g_segs["y1"][clean_g]], 1)
+        op = o_s64[clean_o]
+        err = np.abs(gp.astype(np.float64) - op) / np.maximum(1.0, np.abs(op))
+        max_err = float(err.max())
+    else:
+        max_err = 0.0
+    g_only_unf = sum(1 for k in g_only if not gflag[gi[k]])
+    o_only_unf = sum(1 for k in o_only if not oflag[oi[k]])
+    return ParityReport(len(common), len(g_only), len(o_only), g_only_unf, o_only_unf, hit_mm, col_mm, max_err,
+                        int(flagged.sum()) + len(g_only) + len(o_only) - g_only_unf - o_only_unf)
+
+
+def rel_l2(a: np.ndarray, b: np.ndarray) -> float:
+    a = a.astype(np.float64)
+    b = b.astype(np.float64)
+    d = np.linalg.norm((a - b).ravel())
+    n = np.linalg.norm(b.ravel())
+    return float(d / n) if n > 0 else float(d)
