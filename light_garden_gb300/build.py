@@ -38,14 +38,18 @@ def _stale(target: Path, deps) -> bool:
     return any(Path(d).stat().st_mtime > t for d in deps)
 
 
-def build(verbose: bool = False, force: bool = False, extra_flags=()) -> Path:
-    LIB_DIR.mkdir(exist_ok=True)
-    OBJ_DIR.mkdir(exist_ok=True)
+def build(verbose: bool = False, force: bool = False, extra_flags=(), lib_dir: Path = LIB_DIR,
+          obj_dir: Path = OBJ_DIR) -> Path:
+    """Compile (only what changed) and link the library into ``lib_dir``.  Experiment
+    builds pass ``extra_flags`` with their own ``lib_dir`` / ``obj_dir``."""
+    lib_dir, obj_dir = Path(lib_dir), Path(obj_dir)
+    lib_dir.mkdir(parents=True, exist_ok=True)
+    obj_dir.mkdir(parents=True, exist_ok=True)
     headers = [CSRC / h for h in HEADERS] + [PKG.parent / "include" / "lg.h"]
     cc = nvcc()
 
     def compile_one(src: str) -> Path:
-        obj = OBJ_DIR / (Path(src).stem + ".o")
+        obj = obj_dir / (Path(src).stem + ".o")
         if force or _stale(obj, [CSRC / src] + headers):
             cmd = [cc, *ARCH, *NVCC_FLAGS, *extra_flags, "-dc", "-o", str(obj), str(CSRC / src)]
             if verbose:
@@ -59,7 +63,7 @@ def build(verbose: bool = False, force: bool = False, extra_flags=()) -> Path:
 
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
-    lib = LIB_DIR / "liblightgarden_cuda.so"
+    lib = lib_dir / "liblightgarden_cuda.so"
     if force or _stale(lib, objs):
         cmd = [cc, *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-cudart", "static"]
         if verbose:

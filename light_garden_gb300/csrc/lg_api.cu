@@ -25,7 +25,7 @@ struct DevBuf {
   size_t bytes = 0;
 };
 
-constexpr uint32_t UNIT_REFS = 2048;
+constexpr uint32_t UNIT_REFS = 1024;  // keeps the split shared-memory sums below 2^31
 constexpr size_t OBJ_SMEM_MAX = 96 * 1024;
 
 }  // namespace
@@ -43,7 +43,7 @@ struct lg_ctx {
   bool has_scene = false;
   double aspect = 1.0;
   // trace
-  DevBuf d_queue[2];
+  DevBuf d_queue[2], d_scanrec, d_hitrec, d_list[N_LISTS];
   uint64_t queue_cap = 0;
   DevBuf d_segs, d_paths;
   uint64_t seg_cap = 0;
@@ -55,7 +55,7 @@ struct lg_ctx {
   uint64_t refs_cap = 0, units_cap = 0;
   uint32_t n_tiles = 0, ntx = 0, nty = 0;
   // launch shapes
-  int trace_grid = 0, raster_grid = 0, bin_grid = 0;
+  int trace_grid[4] = {0, 0, 0, 0}, raster_grid = 0, bin_grid = 0;  // scan, refine, full, bounce
   size_t obj_smem = 0;
   int smem_fits = 0;
   // graph
@@ -114,10 +114,16 @@ struct Xf {
   }
 };
 
+// host FP64 leaf; converted to the device's double-float Leaf64 at upload
+struct LeafH {
+  uint32_t kind;
+  double p[8];
+};
+
 struct Flat {
   std::vector<ObjScan> scan;
   std::vector<ObjInfo> info;
-  std::vector<Leaf64> leaves;
+  std::vector<LeafH> leaves;
   std::vector<uint8_t> prog;
   std::vector<LightDev> lights;
   std::vector<uint32_t> cubics;
@@ -141,13 +147,14 @@ lg_status flatten_node(lg_ctx* c, const lg_geo* G, uint32_t n_geo, int32_t gi, c
     prog.push_back(g.op == LG_OP_AND ? PROG_AND : g.op == LG_OP_OR ? PROG_OR : PROG_AND_NOT);
     return LG_OK;
   }
-  Leaf64 L;
+  LeafH L;
   std::memset(&L, 0, sizeof L);
   switch (g.kind) {
     case LG_GEO_CIRCLE:
       L.kind = LEAF_CIRCLE;
       T.apply(g.origin[0], g.origin[1], L.p[0], L.p[1]);
       L.p[2] = g.v[0];
+      L.p[3] = g.v[0] != 0.0 ? 1.0 / g.v[0] : 0.0;  // normal = (p - c) / r
       break;
     case LG_GEO_RECT:
       L.kind = LEAF_RECT;
@@ -157,11 +164,15 @@ lg_status flatten_node(lg_ctx* c, const lg_geo* G, uint32_t n_geo, int32_t gi, c
       L.p[4] = 0.5 * g.v[0];
       L.p[5] = 0.5 * g.v[1];
       break;
-    case LG_GEO_SEGMENT:
+    case LG_GEO_SEGMENT: {
       L.kind = LEAF_SEGMENT;
       T.apply(g.v[0], g.v[1], L.p[0], L.p[1]);
       T.apply(g.v[2], g.v[3], L.p[2], L.p[3]);
+      const double ex = L.p[2] - L.p[0], ey = L.p[3] - L.p[1], l = std::sqrt(ex * ex + ey * ey);
+      L.p[4] = l > 0.0 ? -ey / l : 0.0;  // unit left normal
+      L.p[5] = l > 0.0 ? ex / l : 0.0;
       break;
+    }
     case LG_GEO_CUBIC:
       L.kind = LEAF_CUBIC;
       for (int k = 0; k < 4; ++k) T.apply(g.v[2 * k], g.v[2 * k + 1], L.p[2 * k], L.p[2 * k + 1]);
@@ -177,7 +188,7 @@ lg_status flatten_node(lg_ctx* c, const lg_geo* G, uint32_t n_geo, int32_t gi, c
 }
 
 // bounding circle of one leaf about a centre: returns the max distance
-double leaf_extent(const Leaf64& L, double cx, double cy) {
+double leaf_extent(const LeafH& L, double cx, double cy) {
   auto d = [&](double x, double y) { return std::hypot(x - cx, y - cy); };
   switch (L.kind) {
     case LEAF_CIRCLE: return d(L.p[0], L.p[1]) + std::fabs(L.p[2]);
@@ -191,7 +202,7 @@ double leaf_extent(const Leaf64& L, double cx, double cy) {
   }
 }
 
-void leaf_box(const Leaf64& L, double& x0, double& y0, double& x1, double& y1) {
+void leaf_box(const LeafH& L, double& x0, double& y0, double& x1, double& y1) {
   auto add = [&](double x, double y) {
     x0 = std::min(x0, x); y0 = std::min(y0, y); x1 = std::max(x1, x); y1 = std::max(y1, y);
   };
@@ -218,7 +229,7 @@ void leaf_box(const Leaf64& L, double& x0, double& y0, double& x1, double& y1) {
   }
 }
 
-void leaf_f32(const Leaf64& L, float* a) {
+void leaf_f32(const LeafH& L, float* a) {
   if (L.kind == LEAF_CIRCLE) {
     a[0] = (float)L.p[0]; a[1] = (float)L.p[1]; a[2] = (float)L.p[2];
   } else if (L.kind == LEAF_RECT) {
@@ -269,7 +280,7 @@ lg_status flatten_scene(lg_ctx* c, const lg_geo* G, uint32_t n_geo, const lg_obj
     oi.prog_len = (uint16_t)prog.size();
     oi.flags = (o.has_material ? INFO_MATERIAL : 0u) |
                ((o.kind == LG_OBJ_STRAIGHT_MIRROR || o.kind == LG_OBJ_CURVED_MIRROR) ? INFO_NO_CONTAINS : 0u);
-    oi.n = o.has_material ? o.refractive_index : 1.0;
+    oi.n = DF(o.has_material ? o.refractive_index : 1.0);
     F.prog.insert(F.prog.end(), prog.begin(), prog.end());
     F.info.push_back(oi);
     if (o.kind == LG_OBJ_CURVED_MIRROR) F.cubics.push_back(k);
@@ -311,7 +322,7 @@ lg_status flatten_scene(lg_ctx* c, const lg_geo* G, uint32_t n_geo, const lg_obj
     std::memset(&d, 0, sizeof d);
     d.ox = L.origin[0]; d.oy = L.origin[1]; d.vx = L.v[0]; d.vy = L.v[1];
     d.spot_angle = L.spot_angle;
-    d.n0 = 1.0;
+    d.n0 = DF(1.0);
     for (int i = 0; i < 4; ++i) d.color[i] = L.color[i];
     d.kind = (uint32_t)L.kind;
     d.num_rays = L.num_rays;
@@ -332,7 +343,7 @@ SceneDev scene_dev(lg_ctx* c) {
   S.n_obj = c->n_obj;
   S.n_lights = c->n_lights;
   S.n_primary = c->n_primary;
-  S.aspect = c->aspect;
+  S.aspect = DF(c->aspect);
   for (int i = 0; i < 4; ++i) S.cutoff[i] = c->prm.cutoff_color[i];
   S.max_bounce = c->prm.max_bounce;
   S.record_paths = c->prm.record_paths ? 1u : 0u;
@@ -344,6 +355,9 @@ TraceBufs trace_bufs(lg_ctx* c) {
   B.queue[0] = (RayRec*)c->d_queue[0].p;
   B.queue[1] = (RayRec*)c->d_queue[1].p;
   B.queue_cap = c->queue_cap;
+  B.scan = (ScanRec*)c->d_scanrec.p;
+  B.hit = (HitRec*)c->d_hitrec.p;
+  for (int i = 0; i < N_LISTS; ++i) B.list[i] = (uint32_t*)c->d_list[i].p;
   B.segs = (lg_segment*)c->d_segs.p;
   B.paths = (lg_path_record*)c->d_paths.p;
   B.seg_cap = c->seg_cap;
@@ -360,7 +374,7 @@ RasterArgs raster_args(lg_ctx* c) {
   A.H = c->prm.height;
   A.ntx = c->ntx;
   A.nty = c->nty;
-  A.n_tiles = c->n_tiles;
+  A.n_tiles = 2 * c->n_tiles;  // bins: x-major and y-major segments of each tile
   A.unit_refs = UNIT_REFS;
   for (int ch = 0; ch < 4; ++ch) {
     const lg_blend_component& b = ch < 3 ? c->prm.color_blend : c->prm.alpha_blend;
@@ -386,6 +400,10 @@ lg_status ensure_trace_buffers(lg_ctx* c) {
   lg_status st;
   if ((st = ensure(c, c->d_queue[0], c->queue_cap * sizeof(RayRec), "ray queue"))) return st;
   if ((st = ensure(c, c->d_queue[1], c->queue_cap * sizeof(RayRec), "ray queue"))) return st;
+  if ((st = ensure(c, c->d_scanrec, c->queue_cap * sizeof(ScanRec), "scan records"))) return st;
+  if ((st = ensure(c, c->d_hitrec, c->queue_cap * sizeof(HitRec), "hit records"))) return st;
+  for (int i = 0; i < N_LISTS; ++i)
+    if ((st = ensure(c, c->d_list[i], c->queue_cap * 4, "work lists"))) return st;
   if ((st = ensure(c, c->d_segs, c->seg_cap * sizeof(lg_segment), "segment ring"))) return st;
   if (c->prm.record_paths && (st = ensure(c, c->d_paths, c->seg_cap * sizeof(lg_path_record), "path records")))
     return st;
@@ -397,12 +415,13 @@ lg_status ensure_raster_buffers(lg_ctx* c) {
   const uint64_t px = (uint64_t)c->prm.width * c->prm.height;
   const size_t elem = c->prm.accum == LG_ACCUM_F32 ? 4 : 8;
   if ((st = ensure(c, c->d_accum, px * 4 * elem, "accumulation image"))) return st;
-  if ((st = ensure(c, c->d_tile_count, (size_t)c->n_tiles * 4, "tile counts"))) return st;
-  if ((st = ensure(c, c->d_tile_off, (size_t)c->n_tiles * 8, "tile offsets"))) return st;
-  if ((st = ensure(c, c->d_tile_cursor, (size_t)c->n_tiles * 8, "tile cursors"))) return st;
-  if ((st = ensure(c, c->d_unit_off, (size_t)c->n_tiles * 8, "unit offsets"))) return st;
+  const size_t bins = 2 * (size_t)c->n_tiles;
+  if ((st = ensure(c, c->d_tile_count, bins * 4, "tile counts"))) return st;
+  if ((st = ensure(c, c->d_tile_off, bins * 8, "tile offsets"))) return st;
+  if ((st = ensure(c, c->d_tile_cursor, bins * 8, "tile cursors"))) return st;
+  if ((st = ensure(c, c->d_unit_off, bins * 8, "unit offsets"))) return st;
   if ((st = ensure(c, c->d_refs, c->refs_cap * 4, "tile refs"))) return st;
-  c->units_cap = c->n_tiles + c->refs_cap / UNIT_REFS + 1;
+  c->units_cap = bins + c->refs_cap / UNIT_REFS + 1;
   if ((st = ensure(c, c->d_units, c->units_cap * sizeof(Unit), "raster units"))) return st;
   return LG_OK;
 }
@@ -412,8 +431,14 @@ lg_status enqueue_trace(lg_ctx* c) {
   const TraceBufs B = trace_bufs(c);
   CK(cudaMemsetAsync(c->d_ctr.p, 0, sizeof(Counters), c->stream), "memset counters");
   if (c->n_lights) k_light_setup<<<1, 256, 0, c->stream>>>(S);
-  for (uint32_t g = 0; g < c->prm.max_bounce; ++g)
-    k_trace_gen<<<c->trace_grid, 256, c->smem_fits ? c->obj_smem : 0, c->stream>>>(S, B, g, c->smem_fits);
+  const size_t tsm = c->smem_fits ? c->obj_smem : 0;
+  for (uint32_t g = 0; g < c->prm.max_bounce; ++g) {
+    k_scan<<<c->trace_grid[0], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
+    for (int l = LIST_REFINE_CIRCLE; l <= LIST_REFINE_SEGMENT; ++l)
+      k_refine<<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g, l);
+    k_full<<<c->trace_grid[2], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
+    k_bounce<<<c->trace_grid[3], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
+  }
   const uint64_t n_ov = 3ull * c->n_cubic * (c->prm.emit_control_lines ? 1 : 0) + c->prm.string_mod.modulo;
   if (n_ov) {
     const int blocks = (int)std::min<uint64_t>((n_ov + 255) / 256, 4096);
@@ -422,6 +447,14 @@ lg_status enqueue_trace(lg_ctx* c) {
   }
   CK(cudaGetLastError(), "trace launch");
   return LG_OK;
+}
+
+int raster_mode(const lg_params& p) {
+  if (p.accum == LG_ACCUM_F32) return RM_F32_;
+  const lg_blend_component* b[2] = {&p.color_blend, &p.alpha_blend};
+  for (const lg_blend_component* x : b)
+    if (x->op == LG_BO_MIN || x->op == LG_BO_MAX) return RM_FIXED_MINMAX_;
+  return RM_FIXED_SPLIT_;
 }
 
 lg_status stage_event(lg_ctx* c, int i) {
@@ -434,20 +467,27 @@ lg_status enqueue_accumulate(lg_ctx* c, int binned_event = -1) {
   const RasterArgs A = raster_args(c);
   const int fixed = c->prm.accum == LG_ACCUM_FIXED64;
   k_clear_accum<<<c->n_sm * 8, 256, 0, c->stream>>>(A, fixed);
-  CK(cudaMemsetAsync(c->d_tile_count.p, 0, (size_t)c->n_tiles * 4, c->stream), "memset tile counts");
+  CK(cudaMemsetAsync(c->d_tile_count.p, 0, (size_t)c->n_tiles * 8, c->stream), "memset tile counts");
   CK(cudaMemsetAsync(&((Counters*)c->d_ctr.p)->pixels, 0, sizeof(unsigned long long), c->stream), "memset pixels");
-  k_bin_count<<<c->bin_grid, 256, 0, c->stream>>>(A);
+  const uint32_t bins = 2 * c->n_tiles;
+  const int smem_tiles = bins <= MAX_SMEM_TILES ? 1 : 0;
+  const size_t bsm = smem_tiles ? (size_t)bins * 4 : 0;
+  k_bin_count<<<c->bin_grid, 256, bsm, c->stream>>>(A, smem_tiles);
   k_scan_tiles<<<1, 1024, 0, c->stream>>>(A);
-  k_build_units<<<std::max(1u, (c->n_tiles + 255) / 256), 256, 0, c->stream>>>(A);
-  k_bin_scatter<<<c->bin_grid, 256, 0, c->stream>>>(A);
+  k_build_units<<<std::max(1u, (2 * c->n_tiles + 255) / 256), 256, 0, c->stream>>>(A);
+  k_bin_scatter<<<c->bin_grid, 256, bsm, c->stream>>>(A, smem_tiles);
   if (binned_event >= 0) {
     lg_status st = stage_event(c, binned_event);
     if (st) return st;
   }
-  if (fixed)
-    k_raster<true><<<c->raster_grid, 256, 4 * TILE * TILE_PAD * 8, c->stream>>>(A);
+  const int mode = raster_mode(c->prm);
+  const size_t rsm = (size_t)raster_smem_bytes(mode);
+  if (mode == RM_FIXED_SPLIT_)
+    k_raster<RM_FIXED_SPLIT_><<<c->raster_grid, 256, rsm, c->stream>>>(A);
+  else if (mode == RM_FIXED_MINMAX_)
+    k_raster<RM_FIXED_MINMAX_><<<c->raster_grid, 256, rsm, c->stream>>>(A);
   else
-    k_raster<false><<<c->raster_grid, 256, 4 * TILE * TILE_PAD * 4, c->stream>>>(A);
+    k_raster<RM_F32_><<<c->raster_grid, 256, rsm, c->stream>>>(A);
   CK(cudaGetLastError(), "accumulate launch");
   return LG_OK;
 }
@@ -481,10 +521,16 @@ lg_status grow_trace(lg_ctx* c, uint64_t need_seg, uint64_t need_q) {
   size_t free_b = 0, total_b = 0;
   cudaMemGetInfo(&free_b, &total_b);
   const double want = (double)c->seg_cap * (sizeof(lg_segment) + (c->prm.record_paths ? sizeof(lg_path_record) : 0)) +
-                      2.0 * c->queue_cap * sizeof(RayRec);
+                      (double)c->queue_cap * (2 * sizeof(RayRec) + sizeof(ScanRec) + sizeof(HitRec) + 4 * N_LISTS);
   if (want > (double)total_b * 0.9)
     return fail(c, LG_ERR_OUT_OF_MEMORY, "trace needs " + std::to_string(want / 1e9) + " GB of segment ring and ray queues");
   return ensure_trace_buffers(c);
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
 }
 
 void fill_stats(lg_ctx* c, lg_trace_stats* s) {
@@ -500,7 +546,11 @@ void fill_stats(lg_ctx* c, lg_trace_stats* s) {
   s->tile_refs = k.tile_refs;
 }
 
-lg_status run_trace(lg_ctx* c, uint32_t& retries) {
+lg_status run_trace_once(lg_ctx* c, uint32_t& retries);
+
+lg_status run_trace(lg_ctx* c, uint32_t& retries) { return run_trace_once(c, retries); }
+
+lg_status run_trace_once(lg_ctx* c, uint32_t& retries) {
   for (int attempt = 0; attempt < 8; ++attempt) {
     lg_status st = enqueue_trace(c);
     if (st) return st;
@@ -521,6 +571,7 @@ lg_status run_accumulate(lg_ctx* c, uint32_t& retries) {
     if (c->h_ctr->tile_refs <= c->refs_cap) return LG_OK;
     ++retries;
     c->refs_cap = c->h_ctr->tile_refs + c->h_ctr->tile_refs / 8 + 4096;
+    if (c->refs_cap >= 0xffffffffull) return fail(c, LG_ERR_UNSUPPORTED, "more than 2^32 (segment, tile) pairs in one frame");
     c->graph_valid = false;
     if ((st = ensure_raster_buffers(c))) return st;
   }
@@ -534,11 +585,6 @@ lg_status need_scene(lg_ctx* c) {
   return LG_OK;
 }
 
-float elapsed(cudaEvent_t a, cudaEvent_t b) {
-  float ms = 0.f;
-  cudaEventElapsedTime(&ms, a, b);
-  return ms;
-}
 
 }  // namespace
 
@@ -577,7 +623,13 @@ lg_status lg_create(lg_ctx** out, const lg_device_opts* opts) {
   if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_ctr, sizeof(Counters));
   if (e == cudaSuccess) e = cudaMalloc(&c->d_ctr.p, sizeof(Counters));
   for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_gen, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_full, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bounce, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_bin_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(MAX_SMEM_TILES * 4));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_bin_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(MAX_SMEM_TILES * 4));
   if (e != cudaSuccess) {
     lg_status st = e == cudaErrorMemoryAllocation ? LG_ERR_OUT_OF_MEMORY : LG_ERR_CUDA;
     (void)cudaGetLastError();
@@ -597,7 +649,8 @@ lg_status lg_destroy(lg_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   DevBuf* bufs[] = {&c->d_scan, &c->d_info, &c->d_leaves, &c->d_prog, &c->d_lights, &c->d_cubics, &c->d_queue[0],
-                    &c->d_queue[1], &c->d_segs, &c->d_paths, &c->d_ctr, &c->d_tile_count, &c->d_tile_off,
+                    &c->d_queue[1], &c->d_scanrec, &c->d_hitrec, &c->d_list[0], &c->d_list[1], &c->d_list[2],
+                    &c->d_list[3], &c->d_segs, &c->d_paths, &c->d_ctr, &c->d_tile_count, &c->d_tile_off,
                     &c->d_tile_cursor, &c->d_unit_off, &c->d_refs, &c->d_units, &c->d_accum, &c->d_stage};
   for (DevBuf* b : bufs) release(*b);
   if (c->h_ctr) cudaFreeHost(c->h_ctr);
@@ -624,6 +677,7 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
     return fail(c, LG_ERR_UNSUPPORTED, "string mod: only Curve::Circle with Add/Mul/Pow/Base");
   if (p.string_mod.modulo > (1ull << 30)) return fail(c, LG_ERR_INVALID_ARGUMENT, "string mod modulo too large");
   if (n_lights > 65535) return fail(c, LG_ERR_INVALID_ARGUMENT, "at most 65535 lights");
+  if (n_objects > 65535) return fail(c, LG_ERR_UNSUPPORTED, "at most 65535 objects");
   Flat F;
   lg_status st = flatten_scene(c, geos, n_geo, objects, n_objects, lights, n_lights, F);
   if (st) return st;
@@ -633,13 +687,19 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
                           std::memcmp(&c->prm, &p, sizeof p) == 0;
   if ((st = ensure(c, c->d_scan, F.scan.size() * sizeof(ObjScan), "scene"))) return st;
   if ((st = ensure(c, c->d_info, F.info.size() * sizeof(ObjInfo), "scene"))) return st;
+  std::vector<Leaf64> dleaves(F.leaves.size());
+  for (size_t i = 0; i < F.leaves.size(); ++i) {
+    std::memset(&dleaves[i], 0, sizeof(Leaf64));
+    dleaves[i].kind = F.leaves[i].kind;
+    for (int k = 0; k < 8; ++k) dleaves[i].p[k] = DF(F.leaves[i].p[k]);
+  }
   if ((st = ensure(c, c->d_leaves, F.leaves.size() * sizeof(Leaf64), "scene"))) return st;
   if ((st = ensure(c, c->d_prog, F.prog.size() + 16, "scene"))) return st;
   if ((st = ensure(c, c->d_lights, F.lights.size() * sizeof(LightDev), "scene"))) return st;
   if ((st = ensure(c, c->d_cubics, F.cubics.size() * 4, "scene"))) return st;
   if (!F.scan.empty()) CK(cudaMemcpyAsync(c->d_scan.p, F.scan.data(), F.scan.size() * sizeof(ObjScan), cudaMemcpyHostToDevice, c->stream), "upload");
   if (!F.info.empty()) CK(cudaMemcpyAsync(c->d_info.p, F.info.data(), F.info.size() * sizeof(ObjInfo), cudaMemcpyHostToDevice, c->stream), "upload");
-  if (!F.leaves.empty()) CK(cudaMemcpyAsync(c->d_leaves.p, F.leaves.data(), F.leaves.size() * sizeof(Leaf64), cudaMemcpyHostToDevice, c->stream), "upload");
+  if (!dleaves.empty()) CK(cudaMemcpyAsync(c->d_leaves.p, dleaves.data(), dleaves.size() * sizeof(Leaf64), cudaMemcpyHostToDevice, c->stream), "upload");
   if (!F.prog.empty()) CK(cudaMemcpyAsync(c->d_prog.p, F.prog.data(), F.prog.size(), cudaMemcpyHostToDevice, c->stream), "upload");
   if (!F.lights.empty()) CK(cudaMemcpyAsync(c->d_lights.p, F.lights.data(), F.lights.size() * sizeof(LightDev), cudaMemcpyHostToDevice, c->stream), "upload");
   if (!F.cubics.empty()) CK(cudaMemcpyAsync(c->d_cubics.p, F.cubics.data(), F.cubics.size() * 4, cudaMemcpyHostToDevice, c->stream), "upload");
@@ -660,14 +720,25 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
   c->obj_smem = (size_t)n_objects * sizeof(ObjScan);
   c->smem_fits = c->obj_smem <= OBJ_SMEM_MAX ? 1 : 0;
   int occ = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trace_gen, 256, c->smem_fits ? c->obj_smem : 0), "occupancy");
-  c->trace_grid = c->n_sm * std::max(1, occ);
-  const size_t rsm = 4 * TILE * TILE_PAD * (p.accum == LG_ACCUM_F32 ? 4 : 8);
-  if (p.accum == LG_ACCUM_F32) {
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_raster<false>, 256, rsm), "occupancy");
+  const size_t tsm = c->smem_fits ? c->obj_smem : 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_scan, 256, tsm), "occupancy");
+  c->trace_grid[0] = c->n_sm * std::max(1, occ);
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_refine, 256, 0), "occupancy");
+  c->trace_grid[1] = c->n_sm * std::max(1, occ);
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_full, 256, tsm), "occupancy");
+  c->trace_grid[2] = c->n_sm * std::max(1, occ);
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bounce, 256, tsm), "occupancy");
+  c->trace_grid[3] = c->n_sm * std::max(1, occ);
+  const int mode = raster_mode(p);
+  const int rsm = raster_smem_bytes(mode);
+  if (mode == RM_FIXED_SPLIT_) {
+    CK(cudaFuncSetAttribute(k_raster<RM_FIXED_SPLIT_>, cudaFuncAttributeMaxDynamicSharedMemorySize, rsm), "smem attr");
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_raster<RM_FIXED_SPLIT_>, 256, rsm), "occupancy");
+  } else if (mode == RM_FIXED_MINMAX_) {
+    CK(cudaFuncSetAttribute(k_raster<RM_FIXED_MINMAX_>, cudaFuncAttributeMaxDynamicSharedMemorySize, rsm), "smem attr");
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_raster<RM_FIXED_MINMAX_>, 256, rsm), "occupancy");
   } else {
-    CK(cudaFuncSetAttribute(k_raster<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm), "smem attr");
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_raster<true>, 256, rsm), "occupancy");
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_raster<RM_F32_>, 256, rsm), "occupancy");
   }
   c->raster_grid = c->n_sm * std::max(1, occ);
   c->bin_grid = c->n_sm * 8;
@@ -677,7 +748,7 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
   const uint64_t want_seg = c->seg_cap_hint ? c->seg_cap_hint : 8 * c->n_primary + overlays + 1024;
   const uint64_t want_q = c->queue_cap_hint ? c->queue_cap_hint : 2 * c->n_primary + 1024;
   c->seg_cap = std::max(c->seg_cap, want_seg);
-  c->queue_cap = std::max(c->queue_cap, want_q);
+  c->queue_cap = std::max(c->queue_cap, std::max<uint64_t>(want_q, c->n_primary));  // gen 0 stores every primary
   if ((st = ensure_trace_buffers(c))) return st;
   c->refs_cap = std::max<uint64_t>(c->refs_cap, 1u << 20);
   if ((st = ensure_raster_buffers(c))) return st;
@@ -815,6 +886,7 @@ lg_status lg_render(lg_ctx* c, uint16_t* dst, size_t pitch, int32_t dst_is_devic
     if (c->h_ctr->tile_refs > c->refs_cap) {
       ++retries;
       c->refs_cap = c->h_ctr->tile_refs + c->h_ctr->tile_refs / 8 + 4096;
+      if (c->refs_cap >= 0xffffffffull) return fail(c, LG_ERR_UNSUPPORTED, "more than 2^32 (segment, tile) pairs in one frame");
       if ((st = ensure_raster_buffers(c))) return st;
       c->graph_valid = false;
       continue;
@@ -867,5 +939,6 @@ lg_status lg_accum_download(lg_ctx* c, void* out, uint64_t cap_bytes) {
   CK(cudaStreamSynchronize(c->stream), "synchronize");
   return LG_OK;
 }
+
 
 }  // extern "C"

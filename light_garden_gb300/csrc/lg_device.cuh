@@ -5,21 +5,24 @@
 //                    inline.  This is the table every ray scans; each CTA stages it in
 //                    shared memory with one cp.async.bulk copy.
 //   ObjInfo[n_obj]   32 B per object: leaf range, membership program, material.
-//   Leaf64[n_leaf]   72 B per leaf, FP64 world-space primitive (CSG trees flattened).
+//   Leaf64[n_leaf]   72 B per leaf, double-float world-space primitive (CSG trees flattened).
 //   prog[]           membership programs (postfix over leaf membership bits).
 //
 // Precision split (tracer.rs:395-424 does one FP64 intersection per object per ray):
 //   * the O(objects) scan runs in FP32 and classifies each object as a certain miss, a
 //     certain hit at t32 (margins well above FP32 error), or uncertain;
 //   * every object that could be the nearest hit (certain hits within the FP32 error of
-//     the best, and every uncertain object in front of it) is re-solved in FP64, as are
-//     the bounce (reflect / refract), the medium test and the canvas exit.
-//   The FP64 work is O(1) per ray visit; the FP32 scan carries the object count.
+//     the best, and every uncertain object in front of it) is re-solved in double-float
+//     (lg_df.cuh, ~48-bit significand on the FP32 pipe), as are the bounce
+//     (reflect / refract), the medium test and the canvas exit.
+//   That work is O(1) per ray visit; the FP32 scan carries the object count.  Native
+//   FP64 (1/64 of the FP32 rate on GB300) is used only to generate primary rays.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
 
 #include "../../include/lg.h"
+#include "lg_df.cuh"
 
 namespace lgd {
 
@@ -42,6 +45,14 @@ __host__ __device__ inline uint32_t info_scan(uint32_t i) { return i & 0xfu; }
 __host__ __device__ inline uint32_t info_leaf_a(uint32_t i) { return (i >> 4) & 0x3u; }
 __host__ __device__ inline uint32_t info_leaf_b(uint32_t i) { return (i >> 6) & 0x3u; }
 __host__ __device__ inline uint32_t info_op(uint32_t i) { return (i >> 8) & 0x3u; }
+// solve class of an object (which precise-solve code path it takes): 0 circle, 1 rect,
+// 2 segment (single-leaf objects), 3 cubic or deep CSG (bounding circle only), 4 two-leaf CSG
+constexpr uint32_t N_SOLVE_CLASSES = 5;
+__host__ __device__ inline uint32_t solve_class(uint32_t info) {
+  const uint32_t sk = info & 0xfu;
+  if (sk == 1u) return (info >> 4) & 0x3u;
+  return sk == 2u ? 4u : 3u;
+}
 constexpr uint32_t INFO_MATERIAL = 1u << 10;
 constexpr uint32_t INFO_NO_CONTAINS = 1u << 11; // mirror objects enclose nothing (object.rs:243-244)
 
@@ -59,7 +70,7 @@ struct __align__(16) ObjInfo {
   uint16_t prog_len;
   uint32_t prog_begin;
   uint32_t flags;     // INFO_MATERIAL | INFO_NO_CONTAINS
-  double n;           // refractive index
+  df n;               // refractive index
   uint64_t _pad;
 };
 static_assert(sizeof(ObjInfo) == 32, "ObjInfo is 32 B");
@@ -67,7 +78,8 @@ static_assert(sizeof(ObjInfo) == 32, "ObjInfo is 32 B");
 struct __align__(8) Leaf64 {
   uint32_t kind;
   uint32_t _pad;
-  double p[8];  // circle cx,cy,r | rect cx,cy,cos,sin,hw,hh | segment ax,ay,bx,by | cubic P0..P3
+  df p[8];  // circle cx,cy,r,1/r | rect cx,cy,cos,sin,hw,hh | segment ax,ay,bx,by,nx,ny (unit
+            // left normal) | cubic P0..P3
 };
 static_assert(sizeof(Leaf64) == 72, "Leaf64 is 72 B");
 
@@ -76,27 +88,44 @@ enum : uint8_t { PROG_AND = 0x80, PROG_OR = 0x81, PROG_AND_NOT = 0x82 };  // < 0
 struct __align__(16) LightDev {
   double ox, oy, vx, vy;
   double spot_angle;
-  double n0;           // start medium (tracer.rs:280-287), filled on the device
+  df n0;               // start medium (tracer.rs:280-287), filled on the device
   float color[4];
   uint32_t kind, num_rays;
   uint64_t first;      // index of this light's first primary in the virtual gen-0 queue
 };
 
+// Medium a ray travels in: an object index (its refractive index), or
+constexpr uint16_t MEDIUM_AIR = 0xffff;    // 1.0
+constexpr uint16_t MEDIUM_LIGHT = 0xfffe;  // the light's start medium (tracer.rs:280-287)
+constexpr uint16_t SRC_NONE = 0xffff;
+
 struct __align__(16) RayRec {
-  double ox, oy, dx, dy;
-  double n;
+  df ox, oy, dx, dy;
   uint64_t path;
   float c[4];
   uint32_t prim;
   uint16_t light;
   uint8_t gen, flags;
-  uint32_t _pad[2];
+  // first-order bound of how far rounding may have moved this ray: lateral offset of the
+  // origin (world units) and direction (radians).  A path whose bound grows past
+  // ILL_COND is numerically ill-conditioned and is flagged near-degenerate.
+  float ex, ea;
+  uint16_t medium;   // see MEDIUM_*
+  uint16_t src_obj;  // object whose surface the ray starts on (SRC_NONE for primaries)
+  uint8_t src_leaf;  // leaf of src_obj that holds the start point
+  uint8_t _pad[3];
 };
 static_assert(sizeof(RayRec) == 80, "RayRec is 80 B");
+constexpr float ILL_COND = 1e-11f;
+constexpr float DF_ROUND = 2e-14f;  // double-float rounding per bounce, relative to the coordinates
+
+// work lists of one generation (k_scan appends, k_refine / k_full consume)
+enum : int { LIST_REFINE_CIRCLE = 0, LIST_REFINE_RECT = 1, LIST_REFINE_SEGMENT = 2, LIST_FULL = 3, N_LISTS = 4 };
 
 struct Counters {
   unsigned long long seg_count;               // ring cursor (= segments demanded)
   unsigned long long queue_count[MAX_GEN + 1]; // entries demanded per generation
+  unsigned long long list_count[MAX_GEN][N_LISTS];
   unsigned long long visits, fp64_solves, fallbacks, near;
   unsigned long long pixels, tile_refs, units;
   unsigned long long unit_cursor;
@@ -113,15 +142,43 @@ struct SceneDev {
   LightDev* lights;
   uint32_t n_obj, n_lights;
   uint64_t n_primary;
-  double aspect;          // canvas half width (height is 1)
+  df aspect;              // canvas half width (height is 1)
   float cutoff[4];
   uint32_t max_bounce;
   uint32_t record_paths;
 };
 
+// per-ray result of the FP32 scan
+struct __align__(16) ScanRec {
+  uint16_t cand[8];  // candidate objects, in object order
+  uint8_t nc;        // number of candidates; NC_DEAD: the ray is below the colour cutoff
+  uint8_t overflow;  // more than CAND candidates: the full solve re-scans every object
+  int8_t leaf, face; // refine path: the winner's leaf and rect face
+  float t32;         // refine path: the winner's FP32 root
+  float thr;         // FP32 bound on the nearest hit distance
+  uint32_t _pad;
+};
+static_assert(sizeof(ScanRec) == 32, "ScanRec is 32 B");
+constexpr uint8_t NC_DEAD = 0xff;
+
+// per-ray nearest hit (k_refine / k_full), consumed by k_bounce
+struct __align__(16) HitRec {
+  df t, px, py, nx, ny;
+  float k;           // curvature at the hit
+  float ev;          // nearest near-degenerate decision event (full solve)
+  uint16_t obj;      // HIT_NONE: no object hit
+  uint8_t leaf, flags;
+  uint32_t _pad;
+};
+static_assert(sizeof(HitRec) == 64, "HitRec is 64 B");
+constexpr uint16_t HIT_NONE = 0xffff;
+
 struct TraceBufs {
   RayRec* queue[2];
   uint64_t queue_cap;
+  ScanRec* scan;       // [queue_cap]
+  HitRec* hit;         // [queue_cap]
+  uint32_t* list[N_LISTS];  // [queue_cap] each
   lg_segment* segs;
   lg_path_record* paths;
   uint64_t seg_cap;
@@ -132,209 +189,255 @@ struct TraceBufs {
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 __device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }
 
-// ------------------------------------------------------------------- FP64 geometry
+// ------------------------------------------------------------------- double-float geometry
 struct Hit64 {
-  double t, px, py, nx, ny;
+  df t, px, py, nx, ny;
+  float k;       // curvature of the surface at the hit (1/r for circles, 0 for flat faces)
+  uint8_t leaf;  // leaf of the object that was hit
 };
 
-__device__ __forceinline__ void near_event(double& ev, double t) {
-  if (t < 0.0) t = 0.0;
+// Near-degenerate decision events: ev keeps the smallest ray parameter at which a
+// decision (hit or no hit) fell inside the relative band BAND.
+__device__ __forceinline__ void near_event(float& ev, float t) {
+  if (t < 0.0f) t = 0.0f;
   if (t < ev) ev = t;
 }
-__device__ __forceinline__ void tmin_band(double t, double& ev) {
-  if (t > 1e-2 * T_MIN && t < 1e2 * T_MIN) near_event(ev, t);
+__device__ __forceinline__ void tmin_band(df t, float& ev) {
+  if (t.hi > 1e-11f && t.hi < 1e-7f) near_event(ev, t.hi);
+}
+__device__ __forceinline__ bool past_tmin(df t) { return t.hi > 1e-9f || (t.hi == 1e-9f && t.lo > 0.0f); }
+
+// Roots of one leaf: up to 3 hits with t > T_MIN, in ascending order of the leaf's own
+// parametrisation (circle: t; rect: entry, exit; cubic: curve parameter).  Each kind is
+// one out-of-line function so the kernel keeps a single copy of it in the instruction
+// cache however many call sites a ray visit has.
+static __device__ __noinline__ int hits_circle(const Leaf64& L, df ox, df oy, df dx, df dy, Hit64* h, float& ev) {
+  int n = 0;
+  (void)n;
+  const df cx = L.p[0], cy = L.p[1], r = L.p[2];
+  const df ocx = ox - cx, ocy = oy - cy;
+  const df a = dx * dx + dy * dy, b = ocx * dx + ocy * dy, cc = ocx * ocx + ocy * ocy - r * r;
+  const df disc = b * b - a * cc;
+  const float tc = -b.hi / a.hi;
+  if (fabsf(disc.hi) <= 1e-10f * (b.hi * b.hi + fabsf(a.hi * cc.hi)) && tc > -1e-9f) near_event(ev, tc);
+  if (df_neg(disc)) return 0;
+  const df sq = dsqrt(disc);
+  const df q = -(b + (df_neg(b) ? -sq : sq));
+  df t1 = DF_ZERO, t2 = DF_ZERO;
+  if (q.hi != 0.0f) {
+    t1 = q / a;
+    t2 = cc / q;
+  }
+  if (t2 < t1) { const df x = t1; t1 = t2; t2 = x; }
+  const df ts[2] = {t1, t2};
+  const float rabs = fabsf(r.hi);
+  for (int k = 0; k < 2; ++k) {
+    tmin_band(ts[k], ev);
+    if (past_tmin(ts[k])) {
+      const df px = ox + dx * ts[k], py = oy + dy * ts[k];
+      const df rinv = DF_ONE / r;
+      h[n].t = ts[k]; h[n].px = px; h[n].py = py;
+      h[n].nx = (px - cx) * rinv; h[n].ny = (py - cy) * rinv;
+      h[n].k = 1.0f / rabs;
+      ++n;
+    }
+  }
+  return n;
+
 }
 
-// roots of a leaf: up to 3 hits with t > T_MIN, in ascending order of the leaf's own
-// parametrisation (circle: t; rect: entry, exit; cubic: curve parameter)
-__device__ inline int leaf_hits64(const Leaf64& L, double ox, double oy, double dx, double dy, Hit64* h,
-                                  double& ev) {
+static __device__ __noinline__ int hits_segment(const Leaf64& L, df ox, df oy, df dx, df dy, Hit64* h, float& ev) {
   int n = 0;
+  (void)n;
+  const df ax = L.p[0], ay = L.p[1], ex = L.p[2] - ax, ey = L.p[3] - ay;
+  const df den = dx * ey - dy * ex;
+  const float le = sqrtf(ex.hi * ex.hi + ey.hi * ey.hi), ld = sqrtf(dx.hi * dx.hi + dy.hi * dy.hi);
+  const df wx = ax - ox, wy = ay - oy;
+  const df cwe = wx * ey - wy * ex;
+  if (fabsf(den.hi) <= 1e-10f * le * ld) near_event(ev, den.hi != 0.0f ? cwe.hi / den.hi : 0.0f);
+  if (den.hi == 0.0f) return 0;
+  const df inv = DF_ONE / den;
+  const df t = cwe * inv;
+  const df u = (wx * dy - wy * dx) * inv;
+  if (fabsf(u.hi) <= 1e-10f || fabsf(u.hi - 1.0f) <= 1e-10f) near_event(ev, t.hi);
+  if (df_neg(u) || DF_ONE < u) return 0;
+  tmin_band(t, ev);
+  if (!past_tmin(t)) return 0;
+  h[0].t = t; h[0].px = ox + dx * t; h[0].py = oy + dy * t;
+  h[0].nx = L.p[4]; h[0].ny = L.p[5];
+  h[0].k = 0.0f;
+  return 1;
+
+}
+
+static __device__ __noinline__ int hits_rect(const Leaf64& L, df ox, df oy, df dx, df dy, Hit64* h, float& ev) {
+  int n = 0;
+  (void)n;
+  const df c = L.p[2], s = L.p[3];
+  const df rx = ox - L.p[0], ry = oy - L.p[1];
+  const df O[2] = {c * rx + s * ry, c * ry - s * rx};
+  const df D[2] = {c * dx + s * dy, c * dy - s * dx};
+  const df hh[2] = {L.p[4], L.p[5]};
+  df tn = -DF_INF, tf = DF_INF, tn_other = -DF_INF;
+  float sn = 0.0f, sf = 0.0f;
+  int an = -1, af = -1;
+  for (int ax = 0; ax < 2; ++ax) {
+    if (D[ax].hi == 0.0f) {
+      if (fabsf(fabsf(O[ax].hi) - hh[ax].hi) <= 1e-10f * hh[ax].hi) near_event(ev, 0.0f);
+      if (hh[ax] < dabs(O[ax])) return 0;
+      continue;
+    }
+    const df inv = DF_ONE / D[ax];
+    df t1 = (-hh[ax] - O[ax]) * inv, t2 = (hh[ax] - O[ax]) * inv;
+    float s1 = -1.0f, s2 = 1.0f;
+    if (t2 < t1) { const df x = t1; t1 = t2; t2 = x; s1 = 1.0f; s2 = -1.0f; }
+    if (tn < t1) { tn_other = tn; tn = t1; an = ax; sn = s1; } else if (tn_other < t1) tn_other = t1;
+    if (t2 < tf) { tf = t2; af = ax; sf = s2; }
+  }
+  if (an < 0 || af < 0) return 0;
+  const float scale = fabsf(tn.hi) + fabsf(tf.hi) + 1.0f;
+  if (fabsf(tf.hi - tn.hi) <= 1e-10f * scale) near_event(ev, tn.hi);
+  if (tn_other.hi > -INFINITY && fabsf(tn.hi - tn_other.hi) <= 1e-10f * scale) near_event(ev, tn.hi);
+  if (tf < tn) return 0;
+  tmin_band(tn, ev);
+  if (past_tmin(tn)) {
+    const float lx = an == 0 ? sn : 0.0f, ly = an == 0 ? 0.0f : sn;
+    h[n].t = tn; h[n].px = ox + dx * tn; h[n].py = oy + dy * tn;
+    h[n].nx = c * lx - s * ly; h[n].ny = s * lx + c * ly;
+    h[n].k = 0.0f;
+    ++n;
+  }
+  tmin_band(tf, ev);
+  if (past_tmin(tf)) {
+    const float lx = af == 0 ? sf : 0.0f, ly = af == 0 ? 0.0f : sf;
+    h[n].t = tf; h[n].px = ox + dx * tf; h[n].py = oy + dy * tf;
+    h[n].nx = c * lx - s * ly; h[n].ny = s * lx + c * ly;
+    h[n].k = 0.0f;
+    ++n;
+  }
+  return n;
+
+}
+
+static __device__ __noinline__ int hits_cubic(const Leaf64& L, df ox, df oy, df dx, df dy, Hit64* h, float& ev) {
+  int n = 0;
+  (void)n;
+  const df* v = L.p;
+  // power basis B(s) = C3 s^3 + C2 s^2 + C1 s + C0
+  const df c0x = v[0], c0y = v[1];
+  const df c1x = 3.0f * (v[2] - v[0]), c1y = 3.0f * (v[3] - v[1]);
+  const df c2x = 3.0f * (v[4] - 2.0f * v[2]) + 3.0f * v[0], c2y = 3.0f * (v[5] - 2.0f * v[3]) + 3.0f * v[1];
+  const df c3x = v[6] + 3.0f * (v[2] - v[4]) - v[0], c3y = v[7] + 3.0f * (v[3] - v[5]) - v[1];
+  const df a0 = dx * (c0y - oy) - dy * (c0x - ox);
+  const df a1 = dx * c1y - dy * c1x, a2 = dx * c2y - dy * c2x, a3 = dx * c3y - dy * c3x;
+  const float scale = fabsf(a0.hi) + fabsf(a1.hi) + fabsf(a2.hi) + fabsf(a3.hi) + 1e-30f;
+  const df dd = dx * dx + dy * dy;
+  auto f = [&](df s) { return ((a3 * s + a2) * s + a1) * s + a0; };
+  auto tof = [&](df s) {
+    const df bx = ((c3x * s + c2x) * s + c1x) * s + c0x, by = ((c3y * s + c2y) * s + c1y) * s + c0y;
+    return ((bx - ox) * dx + (by - oy) * dy) / dd;
+  };
+  df knots[4];
+  int nk = 0;
+  knots[nk++] = DF_ZERO;
+  const df qa = 3.0f * a3, qb = 2.0f * a2, qc = a1;
+  if (qa.hi != 0.0f) {
+    const df disc = qb * qb - 4.0f * qa * qc;
+    if (!df_neg(disc)) {
+      const df sq = dsqrt(disc);
+      const df q = -0.5f * (qb + (df_neg(qb) ? -sq : sq));
+      df r1 = q / qa, r2 = q.hi != 0.0f ? qc / q : r1;
+      if (r2 < r1) { const df x = r1; r1 = r2; r2 = x; }
+      if (DF_ZERO < r1 && r1 < DF_ONE) knots[nk++] = r1;
+      if (DF_ZERO < r2 && r2 < DF_ONE && (nk == 1 || r2 != knots[nk - 1])) knots[nk++] = r2;
+    }
+  } else if (qb.hi != 0.0f) {
+    const df r = -qc / qb;
+    if (DF_ZERO < r && r < DF_ONE) knots[nk++] = r;
+  }
+  knots[nk++] = DF_ONE;
+  df roots[3];
+  int nr = 0;
+  for (int i = 0; i + 1 < nk; ++i) {
+    const df lo0 = knots[i], hi0 = knots[i + 1];
+    df flo = f(lo0);
+    const df fhi = f(hi0);
+    if (i > 0 && fabsf(flo.hi) <= 1e-10f * scale) near_event(ev, tof(lo0).hi);
+    if (flo.hi == 0.0f) {
+      if (nr == 0 || roots[nr - 1] != lo0) roots[nr++] = lo0;
+      continue;
+    }
+    if (fhi.hi == 0.0f) {
+      if (i + 2 == nk) roots[nr++] = hi0;
+      continue;
+    }
+    if (df_neg(flo) == df_neg(fhi)) continue;
+    // safeguarded Newton on the monotone bracket
+    df lo = lo0, hi = hi0, sv = DF_HALF * (lo0 + hi0);
+    for (int it = 0; it < 64; ++it) {
+      const df fs = f(sv);
+      if (fs.hi == 0.0f) break;
+      if (df_neg(fs) == df_neg(flo)) { lo = sv; flo = fs; } else { hi = sv; }
+      const df dfs = (3.0f * a3 * sv + 2.0f * a2) * sv + a1;
+      df sn = dfs.hi != 0.0f ? sv - fs / dfs : DF_HALF * (lo + hi);
+      if (!(lo < sn && sn < hi)) sn = DF_HALF * (lo + hi);
+      if (sn == sv || (hi - lo).hi <= 1e-14f * (1.0f + fabsf(sv.hi))) { sv = sn; break; }
+      sv = sn;
+    }
+    roots[nr++] = sv;
+  }
+  if (fabsf(a0.hi) <= 1e-10f * scale) near_event(ev, tof(DF_ZERO).hi);
+  if (fabsf(f(DF_ONE).hi) <= 1e-10f * scale) near_event(ev, tof(DF_ONE).hi);
+  for (int i = 0; i < nr; ++i) {
+    const df sv = roots[i];
+    const df t = tof(sv);
+    tmin_band(t, ev);
+    if (!past_tmin(t)) continue;
+    const df bx = (3.0f * c3x * sv + 2.0f * c2x) * sv + c1x, by = (3.0f * c3y * sv + 2.0f * c2y) * sv + c1y;
+    const df l = dsqrt(bx * bx + by * by);
+    h[n].t = t; h[n].px = ox + dx * t; h[n].py = oy + dy * t;
+    if (l.hi > 0.0f) {
+      const df li = DF_ONE / l;
+      h[n].nx = -(by * li); h[n].ny = bx * li;
+    } else {
+      near_event(ev, t.hi);
+      const df li = DF_ONE / dsqrt(dd);
+      h[n].nx = -(dy * li); h[n].ny = dx * li;
+    }
+    // curvature |B' x B''| / |B'|^3
+    const float bbx = 6.0f * c3x.hi * sv.hi + 2.0f * c2x.hi, bby = 6.0f * c3y.hi * sv.hi + 2.0f * c2y.hi;
+    const float lf = l.hi;
+    h[n].k = lf > 0.0f ? fabsf(bx.hi * bby - by.hi * bbx) / (lf * lf * lf) : 1e30f;
+    ++n;
+  }
+  return n;
+
+}
+
+__device__ __forceinline__ int leaf_hits64(const Leaf64& L, df ox, df oy, df dx, df dy, Hit64* h, float& ev) {
   switch (L.kind) {
-    case LEAF_CIRCLE: {
-      const double cx = L.p[0], cy = L.p[1], r = L.p[2];
-      const double ocx = ox - cx, ocy = oy - cy;
-      const double a = dx * dx + dy * dy, b = ocx * dx + ocy * dy, cc = ocx * ocx + ocy * ocy - r * r;
-      const double disc = b * b - a * cc;
-      if (fabs(disc) <= BAND * (b * b + fabs(a * cc)) && -b / a > -T_MIN) near_event(ev, -b / a);
-      if (disc < 0.0) return 0;
-      const double sq = sqrt(disc);
-      const double q = -(b + (b >= 0.0 ? sq : -sq));
-      double t1 = 0.0, t2 = 0.0;
-      if (q != 0.0) {
-        t1 = q / a;
-        t2 = cc / q;
-      }
-      if (t1 > t2) { const double x = t1; t1 = t2; t2 = x; }
-      const double ts[2] = {t1, t2};
-      for (int k = 0; k < 2; ++k) {
-        tmin_band(ts[k], ev);
-        if (ts[k] > T_MIN) {
-          const double px = ox + dx * ts[k], py = oy + dy * ts[k];
-          h[n].t = ts[k]; h[n].px = px; h[n].py = py;
-          h[n].nx = (px - cx) / r; h[n].ny = (py - cy) / r;
-          ++n;
-        }
-      }
-      return n;
-    }
-    case LEAF_SEGMENT: {
-      const double ax = L.p[0], ay = L.p[1], ex = L.p[2] - ax, ey = L.p[3] - ay;
-      const double den = dx * ey - dy * ex;
-      const double le = sqrt(ex * ex + ey * ey), ld = sqrt(dx * dx + dy * dy);
-      const double wx = ax - ox, wy = ay - oy;
-      if (fabs(den) <= BAND * le * ld) near_event(ev, den != 0.0 ? (wx * ey - wy * ex) / den : 0.0);
-      if (den == 0.0) return 0;
-      const double t = (wx * ey - wy * ex) / den;
-      const double u = (wx * dy - wy * dx) / den;
-      if (fabs(u) <= BAND || fabs(u - 1.0) <= BAND) near_event(ev, t);
-      if (u < 0.0 || u > 1.0) return 0;
-      tmin_band(t, ev);
-      if (!(t > T_MIN)) return 0;
-      h[0].t = t; h[0].px = ox + dx * t; h[0].py = oy + dy * t;
-      if (le > 0.0) { h[0].nx = -ey / le; h[0].ny = ex / le; } else { h[0].nx = 0.0; h[0].ny = 0.0; }
-      return 1;
-    }
-    case LEAF_RECT: {
-      const double c = L.p[2], s = L.p[3];
-      const double rx = ox - L.p[0], ry = oy - L.p[1];
-      const double O[2] = {c * rx + s * ry, -s * rx + c * ry};
-      const double D[2] = {c * dx + s * dy, -s * dx + c * dy};
-      const double hh[2] = {L.p[4], L.p[5]};
-      double tn = -INFINITY, tf = INFINITY, tn_other = -INFINITY, sn = 0.0, sf = 0.0;
-      int an = -1, af = -1;
-      for (int ax = 0; ax < 2; ++ax) {
-        if (D[ax] == 0.0) {
-          if (fabs(fabs(O[ax]) - hh[ax]) <= BAND * hh[ax]) near_event(ev, 0.0);
-          if (fabs(O[ax]) > hh[ax]) return 0;
-          continue;
-        }
-        double t1 = (-hh[ax] - O[ax]) / D[ax], t2 = (hh[ax] - O[ax]) / D[ax];
-        double s1 = -1.0, s2 = 1.0;
-        if (t1 > t2) { const double x = t1; t1 = t2; t2 = x; s1 = 1.0; s2 = -1.0; }
-        if (t1 > tn) { tn_other = tn; tn = t1; an = ax; sn = s1; } else if (t1 > tn_other) tn_other = t1;
-        if (t2 < tf) { tf = t2; af = ax; sf = s2; }
-      }
-      if (an < 0 || af < 0) return 0;
-      const double scale = fabs(tn) + fabs(tf) + 1.0;
-      if (fabs(tf - tn) <= BAND * scale) near_event(ev, tn);
-      if (tn_other > -INFINITY && fabs(tn - tn_other) <= BAND * scale) near_event(ev, tn);
-      if (tn > tf) return 0;
-      tmin_band(tn, ev);
-      if (tn > T_MIN) {
-        const double lx = an == 0 ? sn : 0.0, ly = an == 0 ? 0.0 : sn;
-        h[n].t = tn; h[n].px = ox + dx * tn; h[n].py = oy + dy * tn;
-        h[n].nx = c * lx - s * ly; h[n].ny = s * lx + c * ly;
-        ++n;
-      }
-      tmin_band(tf, ev);
-      if (tf > T_MIN) {
-        const double lx = af == 0 ? sf : 0.0, ly = af == 0 ? 0.0 : sf;
-        h[n].t = tf; h[n].px = ox + dx * tf; h[n].py = oy + dy * tf;
-        h[n].nx = c * lx - s * ly; h[n].ny = s * lx + c * ly;
-        ++n;
-      }
-      return n;
-    }
-    default: {  // LEAF_CUBIC: f(s) = cross(d, B(s) - o), roots on [0, 1]
-      const double* v = L.p;
-      // power basis B(s) = C3 s^3 + C2 s^2 + C1 s + C0
-      const double c0x = v[0], c0y = v[1];
-      const double c1x = 3.0 * (v[2] - v[0]), c1y = 3.0 * (v[3] - v[1]);
-      const double c2x = 3.0 * (v[4] - 2.0 * v[2]) + 3.0 * v[0], c2y = 3.0 * (v[5] - 2.0 * v[3]) + 3.0 * v[1];
-      const double c3x = v[6] + 3.0 * (v[2] - v[4]) - v[0], c3y = v[7] + 3.0 * (v[3] - v[5]) - v[1];
-      const double a0 = dx * (c0y - oy) - dy * (c0x - ox);
-      const double a1 = dx * c1y - dy * c1x, a2 = dx * c2y - dy * c2x, a3 = dx * c3y - dy * c3x;
-      const double scale = fabs(a0) + fabs(a1) + fabs(a2) + fabs(a3) + 1e-300;
-      const double dd = dx * dx + dy * dy;
-      auto f = [&](double s) { return ((a3 * s + a2) * s + a1) * s + a0; };
-      auto tof = [&](double s) {
-        const double bx = ((c3x * s + c2x) * s + c1x) * s + c0x, by = ((c3y * s + c2y) * s + c1y) * s + c0y;
-        return ((bx - ox) * dx + (by - oy) * dy) / dd;
-      };
-      double knots[4];
-      int nk = 0;
-      knots[nk++] = 0.0;
-      const double qa = 3.0 * a3, qb = 2.0 * a2, qc = a1;
-      if (qa != 0.0) {
-        const double disc = qb * qb - 4.0 * qa * qc;
-        if (disc >= 0.0) {
-          const double sq = sqrt(disc);
-          const double q = -0.5 * (qb + (qb >= 0.0 ? sq : -sq));
-          double r1 = q / qa, r2 = q != 0.0 ? qc / q : r1;
-          if (r1 > r2) { const double x = r1; r1 = r2; r2 = x; }
-          if (r1 > 0.0 && r1 < 1.0) knots[nk++] = r1;
-          if (r2 > 0.0 && r2 < 1.0 && (nk == 1 || r2 != knots[nk - 1])) knots[nk++] = r2;
-        }
-      } else if (qb != 0.0) {
-        const double r = -qc / qb;
-        if (r > 0.0 && r < 1.0) knots[nk++] = r;
-      }
-      knots[nk++] = 1.0;
-      double roots[3];
-      int nr = 0;
-      for (int i = 0; i + 1 < nk; ++i) {
-        const double lo0 = knots[i], hi0 = knots[i + 1];
-        double flo = f(lo0);
-        const double fhi = f(hi0);
-        if (i > 0 && fabs(flo) <= BAND * scale) near_event(ev, tof(lo0));
-        if (flo == 0.0) {
-          if (nr == 0 || roots[nr - 1] != lo0) roots[nr++] = lo0;
-          continue;
-        }
-        if (fhi == 0.0) {
-          if (i + 2 == nk) roots[nr++] = hi0;
-          continue;
-        }
-        if ((flo < 0.0) == (fhi < 0.0)) continue;
-        // safeguarded Newton on the monotone bracket
-        double lo = lo0, hi = hi0, s = 0.5 * (lo0 + hi0);
-        for (int it = 0; it < 64; ++it) {
-          const double fs = f(s);
-          if (fs == 0.0) break;
-          if ((fs < 0.0) == (flo < 0.0)) { lo = s; flo = fs; } else { hi = s; }
-          const double dfs = (3.0 * a3 * s + 2.0 * a2) * s + a1;
-          double sn = dfs != 0.0 ? s - fs / dfs : 0.5 * (lo + hi);
-          if (!(sn > lo && sn < hi)) sn = 0.5 * (lo + hi);
-          if (sn == s || hi - lo <= 4e-16 * (1.0 + fabs(s))) { s = sn; break; }
-          s = sn;
-        }
-        roots[nr++] = s;
-      }
-      if (fabs(a0) <= BAND * scale) near_event(ev, tof(0.0));
-      if (fabs(f(1.0)) <= BAND * scale) near_event(ev, tof(1.0));
-      for (int i = 0; i < nr; ++i) {
-        const double s = roots[i];
-        const double t = tof(s);
-        tmin_band(t, ev);
-        if (!(t > T_MIN)) continue;
-        const double bx = (3.0 * c3x * s + 2.0 * c2x) * s + c1x, by = (3.0 * c3y * s + 2.0 * c2y) * s + c1y;
-        const double l = sqrt(bx * bx + by * by);
-        h[n].t = t; h[n].px = ox + dx * t; h[n].py = oy + dy * t;
-        if (l > 0.0) { h[n].nx = -by / l; h[n].ny = bx / l; }
-        else { near_event(ev, t); const double ld = sqrt(dd); h[n].nx = -dy / ld; h[n].ny = dx / ld; }
-        ++n;
-      }
-      return n;
-    }
+    case LEAF_CIRCLE: return hits_circle(L, ox, oy, dx, dy, h, ev);
+    case LEAF_SEGMENT: return hits_segment(L, ox, oy, dx, dy, h, ev);
+    case LEAF_RECT: return hits_rect(L, ox, oy, dx, dy, h, ev);
+    default: return hits_cubic(L, ox, oy, dx, dy, h, ev);
   }
 }
 
 // closed-set membership of a leaf, with a near-boundary flag
-__device__ __forceinline__ bool leaf_contains64(const Leaf64& L, double px, double py, bool& near) {
+__device__ __forceinline__ bool leaf_contains64(const Leaf64& L, df px, df py, bool& near) {
   if (L.kind == LEAF_CIRCLE) {
-    const double dx = px - L.p[0], dy = py - L.p[1], r = L.p[2];
-    const double m = dx * dx + dy * dy - r * r;
-    if (fabs(m) <= BAND * r * r) near = true;
-    return m <= 0.0;
+    const df dx = px - L.p[0], dy = py - L.p[1], r = L.p[2];
+    const df m = dx * dx + dy * dy - r * r;
+    if (fabsf(m.hi) <= 1e-10f * r.hi * r.hi) near = true;
+    return !(DF_ZERO < m);
   }
   if (L.kind == LEAF_RECT) {
-    const double c = L.p[2], s = L.p[3], rx = px - L.p[0], ry = py - L.p[1];
-    const double lx = c * rx + s * ry, ly = -s * rx + c * ry;
-    const double ex = fabs(lx) - L.p[4], ey = fabs(ly) - L.p[5];
-    const double sd = ex > ey ? ex : ey;
-    if (fabs(sd) <= BAND * (L.p[4] + L.p[5])) near = true;
-    return sd <= 0.0;
+    const df c = L.p[2], s = L.p[3], rx = px - L.p[0], ry = py - L.p[1];
+    const df lx = c * rx + s * ry, ly = c * ry - s * rx;
+    const df ex = dabs(lx) - L.p[4], ey = dabs(ly) - L.p[5];
+    const df sd = dmax(ex, ey);
+    if (fabsf(sd.hi) <= 1e-10f * (L.p[4].hi + L.p[5].hi)) near = true;
+    return !(DF_ZERO < sd);
   }
   return false;
 }
@@ -358,8 +461,8 @@ __device__ __forceinline__ bool prog_eval(const uint8_t* prog, int len, uint64_t
   return st & 1ull;
 }
 
-// Object::contains (object.rs:240-259) in FP64
-__device__ inline bool obj_contains64(const SceneDev& S, uint32_t k, double px, double py, bool& near) {
+// Object::contains (object.rs:240-259)
+static __device__ __noinline__ bool obj_contains64(const SceneDev& S, uint32_t k, df px, df py, bool& near) {
   const ObjInfo oi = S.info[k];
   if (oi.flags & INFO_NO_CONTAINS) return false;
   uint64_t mask = 0;
@@ -368,13 +471,13 @@ __device__ inline bool obj_contains64(const SceneDev& S, uint32_t k, double px, 
   return prog_eval(S.prog + oi.prog_begin, oi.prog_len, mask);
 }
 
-// nearest valid hit of one object (geometry intersect + CSG filter), FP64
-__device__ inline bool obj_solve64(const SceneDev& S, uint32_t k, double ox, double oy, double dx, double dy,
-                                   Hit64& best, double& best_d2, double& ev) {
+// nearest valid hit of one object (geometry intersect + CSG filter)
+static __device__ __noinline__ bool obj_solve64(const SceneDev& S, uint32_t k, df ox, df oy, df dx, df dy, Hit64& best,
+                                   df& best_d2, float& ev) {
   const ObjInfo oi = S.info[k];
   const uint8_t* prog = S.prog + oi.prog_begin;
   bool found = false;
-  best_d2 = INFINITY;
+  best_d2 = DF_INF;
   for (int li = 0; li < oi.n_leaves; ++li) {
     const Leaf64 L = S.leaves[oi.leaf_begin + li];
     Hit64 h[3];
@@ -386,16 +489,17 @@ __device__ inline bool obj_solve64(const SceneDev& S, uint32_t k, double ox, dou
         uint64_t mask = 0;
         for (int i = 0; i < oi.n_leaves; ++i)
           if (i != li && leaf_contains64(S.leaves[oi.leaf_begin + i], h[j].px, h[j].py, near)) mask |= 1ull << i;
-        if (near) near_event(ev, h[j].t);
+        if (near) near_event(ev, h[j].t.hi);
         const bool in1 = prog_eval(prog, oi.prog_len, mask | (1ull << li));
         const bool in0 = prog_eval(prog, oi.prog_len, mask & ~(1ull << li));
         if (in1 == in0) continue;
       }
-      const double vx = h[j].px - ox, vy = h[j].py - oy;
-      const double d2 = vx * vx + vy * vy;
+      const df vx = h[j].px - ox, vy = h[j].py - oy;
+      const df d2 = vx * vx + vy * vy;
       if (d2 < best_d2) {
         best_d2 = d2;
         best = h[j];
+        best.leaf = (uint8_t)li;
         found = true;
       }
     }
@@ -408,12 +512,13 @@ __device__ inline bool obj_solve64(const SceneDev& S, uint32_t k, double ox, dou
 // ub = a certainly valid hit distance (INFINITY if none is certain).
 struct Class32 {
   float key, ub;
+  int leaf, face;  // leaf and face (rect: 2 * axis + (outward sign > 0)) of the root at ub
 };
 
-__device__ __forceinline__ void root32(float t, float tol, Class32& c, bool certain) {
+__device__ __forceinline__ void root32(float t, float tol, Class32& c, bool certain, int leaf, int face) {
   if (t < -TAU32) return;                     // certainly behind the origin
   if (certain && t > TAU32) {
-    c.ub = fminf(c.ub, t);
+    if (t < c.ub) { c.ub = t; c.leaf = leaf; c.face = face; }
     c.key = fminf(c.key, t);
   } else {
     c.key = fminf(c.key, fmaxf(t - tol, 0.0f));
@@ -442,8 +547,9 @@ __device__ __forceinline__ int leaf_member32(uint32_t kind, const float* L, floa
 
 // roots of one FP32 leaf: t values with a certainty flag each
 __device__ __forceinline__ int leaf_roots32(uint32_t kind, const float* L, float ox, float oy, float dx, float dy,
-                                            float* t, bool* cert, float& tol, bool& unknown) {
+                                            float* t, bool* cert, int* face, float& tol, bool& unknown) {
   unknown = false;
+  face[0] = face[1] = -1;
   if (kind == LEAF_CIRCLE) {
     const float ocx = ox - L[0], ocy = oy - L[1], r = L[2];
     const float b = ocx * dx + ocy * dy, perp = ocx * dy - ocy * dx;
@@ -484,7 +590,8 @@ __device__ __forceinline__ int leaf_roots32(uint32_t kind, const float* L, float
   const float D[2] = {L[2] * dx + L[3] * dy, -L[3] * dx + L[2] * dy};
   const float H[2] = {L[4], L[5]};
   const float scale = fabsf(rx) + fabsf(ry) + H[0] + H[1];
-  float tn = -INFINITY, tf = INFINITY;
+  float tn = -INFINITY, tf = INFINITY, tn2 = -INFINITY, tf2 = INFINITY;
+  int fn = -1, ff = -1;
   for (int ax = 0; ax < 2; ++ax) {
     const float band = 2e-6f * scale + 1e-6f;
     if (fabsf(D[ax]) < 1e-6f) {
@@ -493,9 +600,11 @@ __device__ __forceinline__ int leaf_roots32(uint32_t kind, const float* L, float
       continue;
     }
     float t1 = (-H[ax] - O[ax]) / D[ax], t2 = (H[ax] - O[ax]) / D[ax];
+    // entering through the -H face when D > 0 (outward normal -1), else the +H face
+    int f1 = 2 * ax + (D[ax] > 0.0f ? 0 : 1), f2 = 2 * ax + (D[ax] > 0.0f ? 1 : 0);
     if (t1 > t2) { const float x = t1; t1 = t2; t2 = x; }
-    tn = fmaxf(tn, t1);
-    tf = fminf(tf, t2);
+    if (t1 > tn) { tn2 = tn; tn = t1; fn = f1; } else { tn2 = fmaxf(tn2, t1); }
+    if (t2 < tf) { tf2 = tf; tf = t2; ff = f2; } else { tf2 = fminf(tf2, t2); }
   }
   tol = 4e-6f * (scale + fabsf(tn) + fabsf(tf)) + 1e-6f;
   if (tn > tf + tol) return 0;
@@ -504,8 +613,9 @@ __device__ __forceinline__ int leaf_roots32(uint32_t kind, const float* L, float
     cert[0] = false;
     return 1;
   }
-  t[0] = tn; cert[0] = true;
-  t[1] = tf; cert[1] = true;
+  // a root whose face is ambiguous (the ray meets a corner) stays uncertain
+  t[0] = tn; cert[0] = !(tn - tn2 <= tol); face[0] = fn;
+  t[1] = tf; cert[1] = !(tf2 - tf <= tol); face[1] = ff;
   return 2;
 }
 
@@ -515,10 +625,16 @@ __device__ __forceinline__ bool op_keep(uint32_t op, bool side_a, bool in_other)
   return side_a ? !in_other : in_other;
 }
 
-__device__ inline Class32 classify32(const ObjScan& r, float ox, float oy, float dx, float dy, float lb) {
+static // src_leaf: leaf of this object that holds the ray origin (-1: none).  On that leaf the
+// root nearest t = 0 is the surface the ray leaves; it is excluded as certain unless the
+// leaf's other root is also near 0 (grazing ray or a corner), which stays uncertain.
+__device__ __noinline__ Class32 classify32(const ObjScan& r, float ox, float oy, float dx, float dy, float lb,
+                                           int src_leaf) {
   Class32 c;
   c.key = INFINITY;
   c.ub = INFINITY;
+  c.leaf = -1;
+  c.face = -1;
   const uint32_t sk = info_scan(r.info);
   if (sk == SCAN_BOUND) {
     c.key = fmaxf(lb, 0.0f);
@@ -530,12 +646,21 @@ __device__ inline Class32 classify32(const ObjScan& r, float ox, float oy, float
     const uint32_t kind = side == 0 ? info_leaf_a(r.info) : info_leaf_b(r.info);
     float t[2];
     bool cert[2];
+    int face[2];
     float tol = 1e-5f;
     bool unknown = false;
-    const int n = leaf_roots32(kind, L, ox, oy, dx, dy, t, cert, tol, unknown);
-    if (unknown) {  // near-parallel: defer the whole object to FP64
+    int n = leaf_roots32(kind, L, ox, oy, dx, dy, t, cert, face, tol, unknown);
+    if (unknown) {  // near-parallel: defer the whole object to the precise solve
       c.key = fminf(c.key, fmaxf(lb, 0.0f));
       continue;
+    }
+    if (side == src_leaf && n > 0) {
+      const int ks = (n == 2 && fabsf(t[1]) < fabsf(t[0])) ? 1 : 0;
+      const bool other_near = n == 2 && fabsf(t[1 - ks]) < 4.0f * TAU32;
+      if (fabsf(t[ks]) < TAU32 && cert[ks] && !other_near) {
+        if (n == 2 && ks == 0) { t[0] = t[1]; cert[0] = cert[1]; face[0] = face[1]; }
+        n -= 1;
+      }
     }
     for (int k = 0; k < n; ++k) {
       bool certain = cert[k];
@@ -549,10 +674,67 @@ __device__ inline Class32 classify32(const ObjScan& r, float ox, float oy, float
         if (m < 0) certain = false;
         else if (!op_keep(info_op(r.info), side == 0, m == 1)) continue;
       }
-      root32(t[k], tol, c, certain);
+      root32(t[k], tol, c, certain, side, face[k]);
     }
   }
   return c;
+}
+
+// ------------------------------------------------------------------- winner refinement
+// The FP32 scan proved that the nearest hit is root `t32` of leaf `leaf` (rect: face
+// `face`) with margins far above FP32 error; recompute that one root in double-float
+// instead of solving the whole object: two Newton steps on |o + t d - c|^2 = r^2 for a
+// circle, the face plane of a rect, the 2x2 solve of a mirror segment.
+static __device__ __noinline__ bool refine_root(const SceneDev& S, uint32_t j, int leaf, int face, float t32, df ox,
+                                                df oy, df dx, df dy, Hit64& h) {
+  const ObjInfo oi = S.info[j];
+  const Leaf64 L = S.leaves[oi.leaf_begin + leaf];
+  df t;
+  if (L.kind == LEAF_CIRCLE) {
+    t = df{t32, 0.0f};
+    for (int it = 0; it < 2; ++it) {
+      const df vx = ox + dx * t - L.p[0], vy = oy + dy * t - L.p[1];
+      const df f = vx * vx + vy * vy - L.p[2] * L.p[2];
+      const float fp = 2.0f * (vx.hi * dx.hi + vy.hi * dy.hi);
+      if (fp == 0.0f) return false;
+      t = t - df{__fdiv_rn(f.hi, fp), 0.0f};
+    }
+    h.px = ox + dx * t;
+    h.py = oy + dy * t;
+    h.nx = (h.px - L.p[0]) * L.p[3];
+    h.ny = (h.py - L.p[1]) * L.p[3];
+    h.k = 1.0f / fabsf(L.p[2].hi);
+  } else if (L.kind == LEAF_SEGMENT) {
+    const df ex = L.p[2] - L.p[0], ey = L.p[3] - L.p[1], wx = L.p[0] - ox, wy = L.p[1] - oy;
+    const df den = dx * ey - dy * ex;
+    if (den.hi == 0.0f) return false;
+    t = (wx * ey - wy * ex) / den;
+    h.px = ox + dx * t;
+    h.py = oy + dy * t;
+    h.nx = L.p[4];
+    h.ny = L.p[5];
+    h.k = 0.0f;
+  } else if (L.kind == LEAF_RECT) {
+    if (face < 0) return false;
+    const int ax = face >> 1;
+    const float sg = (face & 1) ? 1.0f : -1.0f;
+    const df c = L.p[2], s = L.p[3];
+    const df nx = ax == 0 ? c * sg : -(s * sg), ny = ax == 0 ? s * sg : c * sg;  // outward face normal
+    const df den = nx * dx + ny * dy;
+    if (den.hi == 0.0f) return false;
+    const df off = nx * (ox - L.p[0]) + ny * (oy - L.p[1]);
+    t = (L.p[4 + ax] - off) / den;
+    h.px = ox + dx * t;
+    h.py = oy + dy * t;
+    h.nx = nx;
+    h.ny = ny;
+    h.k = 0.0f;
+  } else {
+    return false;
+  }
+  h.t = t;
+  h.leaf = (uint8_t)leaf;
+  return true;
 }
 
 // ------------------------------------------------------------------- raster rule

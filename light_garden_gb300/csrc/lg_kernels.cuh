@@ -37,16 +37,22 @@ struct RasterArgs {
 };
 
 __global__ void k_light_setup(SceneDev S);
-__global__ void k_trace_gen(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
+__global__ void k_scan(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
+__global__ void k_refine(SceneDev S, TraceBufs B, uint32_t gen, int list);
+__global__ void k_full(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
+__global__ void k_bounce(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
 __global__ void k_overlay(SceneDev S, TraceBufs B, const uint32_t* cubic_objs, uint32_t n_cubic, lg_string_mod sm);
 
 __global__ void k_clear_accum(RasterArgs A, int fixed);
-__global__ void k_bin_count(RasterArgs A);
+__global__ void k_bin_count(RasterArgs A, int smem_tiles);
 __global__ void k_scan_tiles(RasterArgs A);
 __global__ void k_build_units(RasterArgs A);
-__global__ void k_bin_scatter(RasterArgs A);
-template <bool FIXED>
+__global__ void k_bin_scatter(RasterArgs A, int smem_tiles);
+template <int MODE>
 __global__ void k_raster(RasterArgs A);
+int raster_smem_bytes(int mode);
+constexpr int RM_FIXED_SPLIT_ = 0, RM_FIXED_MINMAX_ = 1, RM_F32_ = 2;
+constexpr uint32_t MAX_SMEM_TILES = 32768;  // tile bins (2 per tile) with 32-bit counters in 128 KB
 __global__ void k_resolve_f16(const void* accum, int fixed, uint32_t W, uint32_t H, uint16_t* dst, size_t pitch);
 __global__ void k_resolve_rgba8(const void* accum, int fixed, uint32_t W, uint32_t H, uint8_t* dst, size_t pitch);
 

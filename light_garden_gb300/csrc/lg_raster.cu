@@ -82,8 +82,10 @@ __device__ __forceinline__ void for_each_tile(const RSetup& R, const RasterArgs&
     jlo = max(jlo, 0);
     jhi = min(jhi, nmin - 1);
     for (int tn = jlo / TILE; tn <= jhi / TILE; ++tn) {
+      // bin id = 2 * tile + orientation: x-major and y-major segments of a tile are
+      // rasterised in separate units, each with a bank-conflict-free layout
       const uint32_t tile = R.xmajor ? (uint32_t)tn * A.ntx + (uint32_t)tm : (uint32_t)tm * A.ntx + (uint32_t)tn;
-      f(tile);
+      f(2u * tile + (R.xmajor ? 0u : 1u));
     }
   }
 }
@@ -93,18 +95,34 @@ __device__ __forceinline__ uint64_t n_segments(const RasterArgs& A) {
   return n < A.seg_cap ? n : A.seg_cap;
 }
 
-__global__ void __launch_bounds__(256) k_bin_count(RasterArgs A) {
+// Per-CTA tile histogram in shared memory (native 32-bit shared atomics), one global
+// atomic per touched tile per CTA.  Falls back to warp-aggregated global atomics when the
+// tile count does not fit (smem_tiles == 0).
+__global__ void __launch_bounds__(256) k_bin_count(RasterArgs A, int smem_tiles) {
+  extern __shared__ unsigned hist[];
   const uint64_t n = n_segments(A);
+  if (smem_tiles) {
+    for (uint32_t t = threadIdx.x; t < A.n_tiles; t += blockDim.x) hist[t] = 0;
+    __syncthreads();
+  }
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
     RSetup R;
     if (!raster_setup(A.segs[i], A.W, A.H, R)) continue;
     for_each_tile(R, A, [&](uint32_t tile) {
-      // lanes of a warp usually share tiles (neighbouring rays): one atomic per group
-      const unsigned act = __activemask();
-      const unsigned grp = __match_any_sync(act, tile);
-      const int leader = __ffs(grp) - 1;
-      if ((int)lane_id() == leader) atomicAdd(&A.tile_count[tile], (unsigned)__popc(grp));
+      if (smem_tiles) {
+        atomicAdd(&hist[tile], 1u);
+      } else {
+        const unsigned act = __activemask();
+        const unsigned grp = __match_any_sync(act, tile);
+        const int leader = __ffs(grp) - 1;
+        if ((int)lane_id() == leader) atomicAdd(&A.tile_count[tile], (unsigned)__popc(grp));
+      }
     });
+  }
+  if (smem_tiles) {
+    __syncthreads();
+    for (uint32_t t = threadIdx.x; t < A.n_tiles; t += blockDim.x)
+      if (hist[t]) atomicAdd(&A.tile_count[t], hist[t]);
   }
 }
 
@@ -175,8 +193,36 @@ __global__ void k_build_units(RasterArgs A) {
   }
 }
 
-__global__ void __launch_bounds__(256) k_bin_scatter(RasterArgs A) {
+// Scatter of segment ids into the per-tile lists.  With shared-memory tiles a CTA counts
+// its own segments per tile, reserves one range per touched tile with a single global
+// atomic, and fills the ranges through shared-memory cursors.
+__global__ void __launch_bounds__(256) k_bin_scatter(RasterArgs A, int smem_tiles) {
+  extern __shared__ unsigned cur[];  // slots are < refs_cap < 2^32
   const uint64_t n = n_segments(A);
+  if (smem_tiles) {
+    for (uint32_t t = threadIdx.x; t < A.n_tiles; t += blockDim.x) cur[t] = 0;
+    __syncthreads();
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+      RSetup R;
+      if (!raster_setup(A.segs[i], A.W, A.H, R)) continue;
+      for_each_tile(R, A, [&](uint32_t tile) { atomicAdd(&cur[tile], 1u); });
+    }
+    __syncthreads();
+    for (uint32_t t = threadIdx.x; t < A.n_tiles; t += blockDim.x) {
+      const unsigned c = cur[t];
+      cur[t] = c ? (unsigned)atomicAdd(&A.tile_cursor[t], (unsigned long long)c) : 0u;
+    }
+    __syncthreads();
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+      RSetup R;
+      if (!raster_setup(A.segs[i], A.W, A.H, R)) continue;
+      for_each_tile(R, A, [&](uint32_t tile) {
+        const unsigned slot = atomicAdd(&cur[tile], 1u);
+        if (slot < A.refs_cap) A.refs[slot] = (uint32_t)i;
+      });
+    }
+    return;
+  }
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
     RSetup R;
     if (!raster_setup(A.segs[i], A.W, A.H, R)) continue;
@@ -194,16 +240,43 @@ __global__ void __launch_bounds__(256) k_bin_scatter(RasterArgs A) {
 }
 
 // ------------------------------------------------------------------ tile raster
-constexpr int TILE_WORDS = TILE * TILE_PAD;  // per channel
+constexpr int TILE_PX = TILE * TILE;  // cells per channel plane
 
-template <bool FIXED>
+// Layout of a unit's shared-memory tile: x-major units index cells [row][col] and their
+// 32 lanes own 32 columns; y-major units index [col][row] and their lanes own 32 rows.
+// Either way one warp's 32 accesses fall in 32 distinct banks.
+//
+// Fixed-point sums use exact split accumulation in native 32-bit shared atomics: a
+// contribution q (|q| <= 2^52) is split as q = a * 2^42 + b * 2^21 + c with 21-bit b, c
+// and signed a.  A unit holds at most 1024 segments and a segment adds at most once to a
+// pixel, so each plane sum stays below 2^31 and A * 2^42 + B * 2^21 + C is exact.
+enum RasterMode { RM_FIXED_SPLIT = 0, RM_FIXED_MINMAX = 1, RM_F32 = 2 };
+
+template <int MODE>
+struct RasterSmem {
+  static constexpr int acc_words = MODE == RM_FIXED_SPLIT ? 12 * TILE_PX : MODE == RM_FIXED_MINMAX ? 8 * TILE_PX : 4 * TILE_PX;
+  static constexpr int stage_words = 8 * 32 * 16;  // 8 warps x 32 staged segments x 64 B
+  static constexpr int bytes = (acc_words + stage_words) * 4;
+};
+
+// one staged segment: raster setup and per-channel source terms, 64 B
+struct __align__(16) Staged {
+  float ua, va, slope;
+  int lohi;             // lo | hi << 16 (major-axis pixel range); -1: nothing to draw
+  unsigned q[12];       // FIXED_SPLIT: (c, b, a) per channel; otherwise q[0..7] = 4 x int64 or 4 x float
+};
+
+template <int MODE>
 __global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  using acc_t = typename std::conditional<FIXED, long long, float>::type;
-  acc_t* acc = reinterpret_cast<acc_t*>(smem_raw);
+  unsigned* acc32 = reinterpret_cast<unsigned*>(smem_raw);
+  long long* acc64 = reinterpret_cast<long long*>(smem_raw);
+  float* accf = reinterpret_cast<float*>(smem_raw);
+  Staged* stage_all = reinterpret_cast<Staged*>(smem_raw + RasterSmem<MODE>::acc_words * 4);
   __shared__ unsigned long long s_unit, s_pixels;
   if (threadIdx.x == 0) s_pixels = 0;
   const unsigned lane = lane_id(), warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  Staged* stage = stage_all + warp * 32;
   const BlendDev& B = A.blend;
   unsigned long long my_pixels = 0;
   unsigned long long n_units = A.ctr->units;
@@ -214,83 +287,148 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
     const unsigned long long u = s_unit;
     if (u >= n_units) break;
     const Unit U = A.units[u];
-    const uint32_t tx = U.tile % A.ntx, ty = U.tile / A.ntx;
-    for (int k = threadIdx.x; k < 4 * TILE_WORDS; k += blockDim.x) {
-      const int op = B.op[k / TILE_WORDS];
-      if (FIXED) acc[k] = (acc_t)ident64(op); else acc[k] = (acc_t)ident32(op);
+    const uint32_t tile = U.tile >> 1;
+    const bool xmajor = (U.tile & 1u) == 0;
+    const uint32_t tx = tile % A.ntx, ty = tile / A.ntx;
+    const int tm = xmajor ? (int)tx : (int)ty, tn = xmajor ? (int)ty : (int)tx;
+    const int nmin = (int)(xmajor ? A.H : A.W);
+    if (MODE == RM_FIXED_SPLIT) {
+      uint4* z = reinterpret_cast<uint4*>(acc32);
+      for (int k = threadIdx.x; k < RasterSmem<MODE>::acc_words / 4; k += blockDim.x) z[k] = make_uint4(0, 0, 0, 0);
+    } else if (MODE == RM_FIXED_MINMAX) {
+      for (int k = threadIdx.x; k < 4 * TILE_PX; k += blockDim.x) acc64[k] = ident64(B.op[k / TILE_PX]);
+    } else {
+      for (int k = threadIdx.x; k < 4 * TILE_PX; k += blockDim.x) accf[k] = ident32(B.op[k / TILE_PX]);
     }
     __syncthreads();
-    const uint64_t end = U.begin + U.n;
-    for (uint64_t r = U.begin + warp; r < end; r += nwarps) {
-      if (r >= A.refs_cap) break;
-      const uint32_t si = A.refs[r];
-      const float4* sp = reinterpret_cast<const float4*>(A.segs + si);
-      const float4 g = __ldg(sp), cc = __ldg(sp + 1);
-      lg_segment s;
-      s.x0 = g.x; s.y0 = g.y; s.x1 = g.z; s.y1 = g.w;
-      s.color[0] = cc.x; s.color[1] = cc.y; s.color[2] = cc.z; s.color[3] = cc.w;
-      RSetup R;
-      if (!raster_setup(s, A.W, A.H, R)) continue;
-      const int tm = R.xmajor ? (int)tx : (int)ty, tn = R.xmajor ? (int)ty : (int)tx;
-      const int i = tm * TILE + (int)lane;
-      if (i < R.lo || i >= R.hi) continue;
-      const int j = raster_minor(R, i);
-      const int jl = j - tn * TILE;
-      const int nmin = (int)(R.xmajor ? A.H : A.W);
-      if (jl < 0 || jl >= TILE || j >= nmin) continue;
-      const int row = R.xmajor ? jl : (int)lane, col = R.xmajor ? (int)lane : jl;
-      const int cell = row * TILE_PAD + col;
+    const uint64_t end = min(U.begin + U.n, A.refs_cap);
+    for (uint64_t base = U.begin + (uint64_t)warp * 32; base < end; base += (uint64_t)nwarps * 32) {
+      // lane-parallel: fetch 32 segments and set them up
+      const uint64_t r = base + lane;
+      Staged st;
+      st.lohi = -1;
+      if (r < end) {
+        const uint32_t si = A.refs[r];
+        const float4* sp = reinterpret_cast<const float4*>(A.segs + si);
+        const float4 g = __ldg(sp), cc = __ldg(sp + 1);
+        lg_segment sg;
+        sg.x0 = g.x; sg.y0 = g.y; sg.x1 = g.z; sg.y1 = g.w;
+        sg.color[0] = cc.x; sg.color[1] = cc.y; sg.color[2] = cc.z; sg.color[3] = cc.w;
+        RSetup R;
+        if (raster_setup(sg, A.W, A.H, R)) {
+          st.ua = R.ua; st.va = R.va; st.slope = R.slope;
+          st.lohi = R.lo | (R.hi << 16);
 #pragma unroll
-      for (int ch = 0; ch < 4; ++ch) {
-        const float v = contribution(B, ch, s.color);
-        const int op = B.op[ch];
-        acc_t* p = acc + ch * TILE_WORDS + cell;
-        if (FIXED) {
-          const long long q = to_fixed(v);
-          if (op == LG_BO_ADD) atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)q);
-          else if (op == LG_BO_REVERSE_SUBTRACT) atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)(-q));
-          else if (op == LG_BO_MIN) atomicMin(reinterpret_cast<long long*>(p), q);
-          else atomicMax(reinterpret_cast<long long*>(p), q);
-        } else {
-          float* pf = reinterpret_cast<float*>(p);
-          if (op == LG_BO_ADD) atomicAdd(pf, v);
-          else if (op == LG_BO_REVERSE_SUBTRACT) atomicAdd(pf, -v);
-          else if (op == LG_BO_MIN) { float o = *pf; while (v < o) { const float w = __int_as_float(atomicCAS(reinterpret_cast<int*>(pf), __float_as_int(o), __float_as_int(v))); if (w == o) break; o = w; } }
-          else { float o = *pf; while (v > o) { const float w = __int_as_float(atomicCAS(reinterpret_cast<int*>(pf), __float_as_int(o), __float_as_int(v))); if (w == o) break; o = w; } }
+          for (int ch = 0; ch < 4; ++ch) {
+            const float v = contribution(B, ch, sg.color);
+            if (MODE == RM_FIXED_SPLIT) {
+              long long q = to_fixed(v);
+              if (B.op[ch] == LG_BO_REVERSE_SUBTRACT) q = -q;
+              st.q[3 * ch] = (unsigned)(q & 0x1fffffll);
+              st.q[3 * ch + 1] = (unsigned)((q >> 21) & 0x1fffffll);
+              st.q[3 * ch + 2] = (unsigned)(int)(q >> 42);
+            } else if (MODE == RM_FIXED_MINMAX) {
+              long long q = to_fixed(v);
+              if (B.op[ch] == LG_BO_REVERSE_SUBTRACT) q = -q;
+              st.q[2 * ch] = (unsigned)(q & 0xffffffffll);
+              st.q[2 * ch + 1] = (unsigned)(q >> 32);
+            } else {
+              st.q[ch] = __float_as_uint(B.op[ch] == LG_BO_REVERSE_SUBTRACT ? -v : v);
+            }
+          }
         }
       }
-      ++my_pixels;
+      stage[lane] = st;
+      __syncwarp();
+      const int n = (int)min((uint64_t)32, end - base);
+      const int i = tm * TILE + (int)lane;
+      for (int k = 0; k < n; ++k) {
+        const int lohi = stage[k].lohi;
+        if (lohi < 0) continue;
+        const int lo = lohi & 0xffff, hi = lohi >> 16;
+        if (i < lo || i >= hi) continue;
+        RSetup R;
+        R.ua = stage[k].ua; R.va = stage[k].va; R.slope = stage[k].slope;
+        const int j = raster_minor(R, i);
+        const int jl = j - tn * TILE;
+        if (jl < 0 || jl >= TILE || j >= nmin) continue;
+        const int cell = jl * TILE + (int)lane;  // [row][col] for x-major, [col][row] for y-major
+        if (MODE == RM_FIXED_SPLIT) {
+          const uint4 q0 = *reinterpret_cast<const uint4*>(&stage[k].q[0]);
+          const uint4 q1 = *reinterpret_cast<const uint4*>(&stage[k].q[4]);
+          const uint4 q2 = *reinterpret_cast<const uint4*>(&stage[k].q[8]);
+          const unsigned qs[12] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
+#pragma unroll
+          for (int w = 0; w < 12; ++w)
+            if (qs[w]) atomicAdd(acc32 + w * TILE_PX + cell, qs[w]);
+        } else if (MODE == RM_FIXED_MINMAX) {
+#pragma unroll
+          for (int ch = 0; ch < 4; ++ch) {
+            const long long q = (long long)(((unsigned long long)stage[k].q[2 * ch + 1] << 32) | stage[k].q[2 * ch]);
+            long long* p = acc64 + ch * TILE_PX + cell;
+            const int op = B.op[ch];
+            if (op == LG_BO_MIN) atomicMin(p, q);
+            else if (op == LG_BO_MAX) atomicMax(p, q);
+            else atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)q);
+          }
+        } else {
+#pragma unroll
+          for (int ch = 0; ch < 4; ++ch) {
+            const float v = __uint_as_float(stage[k].q[ch]);
+            float* pf = accf + ch * TILE_PX + cell;
+            const int op = B.op[ch];
+            if (op == LG_BO_ADD || op == LG_BO_REVERSE_SUBTRACT) atomicAdd(pf, v);
+            else {
+              float o = *pf;
+              while (op == LG_BO_MIN ? v < o : v > o) {
+                const float w = __int_as_float(atomicCAS(reinterpret_cast<int*>(pf), __float_as_int(o), __float_as_int(v)));
+                if (w == o) break;
+                o = w;
+              }
+            }
+          }
+        }
+        ++my_pixels;
+      }
+      __syncwarp();
     }
     __syncthreads();
     // flush: one global atomic per touched pixel channel
-    for (int k = threadIdx.x; k < TILE * TILE; k += blockDim.x) {
+    for (int k = threadIdx.x; k < TILE_PX; k += blockDim.x) {
       const int row = k / TILE, col = k % TILE;
       const uint32_t x = tx * TILE + col, y = ty * TILE + row;
       if (x >= A.W || y >= A.H) continue;
       const uint64_t px = ((uint64_t)y * A.W + x) * 4;
+      const int cell = xmajor ? row * TILE + col : col * TILE + row;
 #pragma unroll
       for (int ch = 0; ch < 4; ++ch) {
-        const acc_t v = acc[ch * TILE_WORDS + row * TILE_PAD + col];
         const int op = B.op[ch];
-        if (FIXED) {
-          if ((long long)v == ident64(op)) continue;
+        if (MODE == RM_FIXED_SPLIT) {
+          const unsigned* base = acc32 + 3 * ch * TILE_PX + cell;
+          const long long q = (long long)(int)base[2 * TILE_PX] * (1ll << 42) + (long long)base[TILE_PX] * (1ll << 21) +
+                              (long long)base[0];
+          if (q == 0) continue;
+          atomicAdd(reinterpret_cast<unsigned long long*>(A.accum) + px + ch, (unsigned long long)q);
+        } else if (MODE == RM_FIXED_MINMAX) {
+          const long long v = acc64[ch * TILE_PX + cell];
+          if (v == ident64(op)) continue;
           long long* g = reinterpret_cast<long long*>(A.accum) + px + ch;
-          if (op == LG_BO_MIN) atomicMin(g, (long long)v);
-          else if (op == LG_BO_MAX) atomicMax(g, (long long)v);
-          else atomicAdd(reinterpret_cast<unsigned long long*>(g), (unsigned long long)(long long)v);
+          if (op == LG_BO_MIN) atomicMin(g, v);
+          else if (op == LG_BO_MAX) atomicMax(g, v);
+          else atomicAdd(reinterpret_cast<unsigned long long*>(g), (unsigned long long)v);
         } else {
-          if ((float)v == ident32(op)) continue;
+          const float v = accf[ch * TILE_PX + cell];
+          if (v == ident32(op)) continue;
           float* g = reinterpret_cast<float*>(A.accum) + px + ch;
           if (op == LG_BO_MIN || op == LG_BO_MAX) {
             float o = *g;
-            const float fv = (float)v;
-            while (op == LG_BO_MIN ? fv < o : fv > o) {
-              const float w = __int_as_float(atomicCAS(reinterpret_cast<int*>(g), __float_as_int(o), __float_as_int(fv)));
+            while (op == LG_BO_MIN ? v < o : v > o) {
+              const float w = __int_as_float(atomicCAS(reinterpret_cast<int*>(g), __float_as_int(o), __float_as_int(v)));
               if (w == o) break;
               o = w;
             }
           } else {
-            atomicAdd(g, (float)v);
+            atomicAdd(g, v);
           }
         }
       }
@@ -302,8 +440,14 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
   if (threadIdx.x == 0) atomicAdd(&A.ctr->pixels, s_pixels);
 }
 
-template __global__ void k_raster<true>(RasterArgs A);
-template __global__ void k_raster<false>(RasterArgs A);
+template __global__ void k_raster<RM_FIXED_SPLIT>(RasterArgs A);
+template __global__ void k_raster<RM_FIXED_MINMAX>(RasterArgs A);
+template __global__ void k_raster<RM_F32>(RasterArgs A);
+
+int raster_smem_bytes(int mode) {
+  return mode == RM_FIXED_SPLIT ? RasterSmem<RM_FIXED_SPLIT>::bytes
+                                : mode == RM_FIXED_MINMAX ? RasterSmem<RM_FIXED_MINMAX>::bytes : RasterSmem<RM_F32>::bytes;
+}
 
 // ------------------------------------------------------------------ resolve
 __device__ __forceinline__ float4 load_px(const void* acc, int fixed, uint64_t i) {

@@ -77,6 +77,7 @@ __device__ const ObjScan* stage_objects(const SceneDev& S, ObjScan* sobj, uint64
 }
 
 // ------------------------------------------------------------------- primary rays
+// native FP64 (only here): the reference's f64 sin_cos / atan per primary ray
 __device__ inline void primary_ray(const LightDev& L, uint64_t i, double& ox, double& oy, double& dx, double& dy) {
   const double n = (double)L.num_rays;
   if (L.kind == LG_LIGHT_POINT) {  // light.rs:168-172
@@ -108,25 +109,27 @@ __device__ inline void primary_ray(const LightDev& L, uint64_t i, double& ox, do
 __global__ void k_light_setup(SceneDev S) {
   for (uint32_t l = threadIdx.x; l < S.n_lights; l += blockDim.x) {
     LightDev& L = S.lights[l];
-    double n = 1.0;  // tracer.rs:280-287: the last containing object wins
+    df n = DF_ONE;  // tracer.rs:280-287: the last containing object wins
+    const df px = df_from_double(L.ox), py = df_from_double(L.oy);
     for (uint32_t k = 0; k < S.n_obj; ++k) {
       bool near = false;
-      if ((S.info[k].flags & INFO_MATERIAL) && obj_contains64(S, k, L.ox, L.oy, near)) n = S.info[k].n;
+      if ((S.info[k].flags & INFO_MATERIAL) && obj_contains64(S, k, px, py, near)) n = S.info[k].n;
     }
     L.n0 = n;
   }
 }
 
 // ------------------------------------------------------------------- one generation
-struct Visit {
-  bool emit;
-  float x0, y0, x1, y1;
-  int hit;
-  uint8_t flags;
-  int nchild;
-  RayRec child[2];
-};
-
+// Each generation runs as four kernels over the generation's queue (a wavefront), so that
+// every kernel executes one compact code path on coherent work:
+//   k_scan     FP32: nearest-hit search bound and candidate list per ray; sorts the rays
+//              into work lists (refine circle / rect / segment, full solve)
+//   k_refine   double-float refinement of a winner the FP32 scan proved (one leaf kind
+//              per launch)
+//   k_full     double-float solve of every candidate (near ties, uncertain roots, cubic
+//              and deep CSG objects), grouped by solve class
+//   k_bounce   medium (tracer.rs:428-442), refract / reflect with colour split
+//              (444-481) or canvas exit (482-488); appends segments and children
 __device__ __forceinline__ bool below_cutoff(const float* c, const float* k) {
   return (c[0] < k[0] && c[1] < k[1] && c[2] < k[2]) || c[3] < k[3];
 }
@@ -137,70 +140,279 @@ __device__ __forceinline__ bool near_cutoff(const float* c, const float* k) {
   return n;
 }
 
-__device__ void visit(const SceneDev& S, const ObjScan* objs, const RayRec& r, uint32_t gen, Visit& v,
-                      unsigned long long& n_solves) {
+// FP32 bounding-circle test shared by both scan passes: false if the object cannot hold a
+// hit at a ray parameter <= thr; lb receives a lower bound of its hit distances.
+__device__ __forceinline__ bool bound_test(const float4& h, float ox, float oy, float dx, float dy, float thr,
+                                           float& lb) {
+  const float ocx = h.x - ox, ocy = h.y - oy;
+  const float b = ocx * dx + ocy * dy, perp = ocx * dy - ocy * dx;
+  const float btol = 2e-6f * (fabsf(b) + fabsf(perp) + h.z) + 1e-6f;
+  if (fabsf(perp) > h.z + btol || b + h.z + btol < -TAU32) return false;
+  lb = b - h.z - btol;
+  return lb <= thr;
+}
+
+__device__ __forceinline__ uint64_t n_in_of(const SceneDev& S, const TraceBufs& B, uint32_t gen) {
+  if (gen == 0) return S.n_primary;
+  const unsigned long long n = B.ctr->queue_count[gen];
+  return n < B.queue_cap ? n : B.queue_cap;
+}
+
+__device__ __forceinline__ int leaf_kind_of(uint32_t info, int leaf) {
+  return (int)(leaf == 0 ? info_leaf_a(info) : info_leaf_b(info));
+}
+
+// appends idx to work list `list` (-1: none) with one atomic per (warp, list)
+__device__ __forceinline__ void list_append(const TraceBufs& B, uint32_t gen, int list, uint32_t idx) {
+  const unsigned act = __activemask();
+  const unsigned grp = __match_any_sync(act, list);
+  if (list < 0) return;
+  const int leader = __ffs(grp) - 1;
+  unsigned long long base = 0;
+  if ((int)lane_id() == leader) base = atomicAdd(&B.ctr->list_count[gen][list], (unsigned long long)__popc(grp));
+  base = __shfl_sync(grp, base, leader);
+  const unsigned long long slot = base + __popc(grp & lanemask_lt());
+  if (slot < B.queue_cap) B.list[list][slot] = idx;
+}
+
+__global__ void __launch_bounds__(256) k_scan(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar;
+  bool failed;
+  const ObjScan* objs = stage_objects(S, reinterpret_cast<ObjScan*>(smem_raw), &bar, smem_fits != 0, B.ctr, failed);
+  if (failed) return;
+  const uint64_t n_in = n_in_of(S, B, gen);
+  RayRec* q = B.queue[gen & 1];
+  for (uint64_t idx = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; idx < n_in;
+       idx += (uint64_t)gridDim.x * blockDim.x) {
+    RayRec r;
+    if (gen == 0) {
+      uint32_t l = 0;
+      while (l + 1 < S.n_lights && S.lights[l + 1].first <= idx) ++l;
+      const LightDev& L = S.lights[l];
+      const uint64_t i = idx - L.first;
+      double pox, poy, pdx, pdy;
+      primary_ray(L, i, pox, poy, pdx, pdy);
+      r.ox = df_from_double(pox); r.oy = df_from_double(poy);
+      r.dx = df_from_double(pdx); r.dy = df_from_double(pdy);
+      r.medium = MEDIUM_LIGHT;
+      r.src_obj = SRC_NONE;
+      r.src_leaf = 0;
+      r.c[0] = L.color[0]; r.c[1] = L.color[1]; r.c[2] = L.color[2]; r.c[3] = L.color[3];
+      r.path = 0;
+      r.prim = (uint32_t)i;
+      r.light = (uint16_t)l;
+      r.gen = 0;
+      r.flags = 0;
+      // rounding of the light's ray generator (sin/cos/atan) and the double-float split
+      r.ex = DF_ROUND * (1.0f + fabsf(r.ox.hi) + fabsf(r.oy.hi));
+      r.ea = DF_ROUND;
+      if (idx < B.queue_cap) q[idx] = r;
+    } else {
+      r = q[idx];
+    }
+    ScanRec sc;
+    sc.nc = 0;
+    sc.overflow = 0;
+    sc.leaf = -1;
+    sc.face = -1;
+    sc.t32 = 0.0f;
+    sc.thr = INFINITY;
+    int list = -1;
+    if (below_cutoff(r.c, S.cutoff)) {
+      sc.nc = NC_DEAD;
+    } else {
+      const float ox = r.ox.hi, oy = r.oy.hi, dx = r.dx.hi, dy = r.dy.hi;
+      // pass 1: the nearest certain hit bounds the search
+      float thr = INFINITY;
+      for (uint32_t j = 0; j < S.n_obj; ++j) {
+        const float4 h = *reinterpret_cast<const float4*>(&objs[j]);
+        float lb;
+        if (!bound_test(h, ox, oy, dx, dy, thr, lb)) continue;
+        const Class32 c = classify32(objs[j], ox, oy, dx, dy, lb, j == r.src_obj ? (int)r.src_leaf : -1);
+        if (c.ub < INFINITY) thr = fminf(thr, c.ub * (1.0f + 1e-4f) + 1e-4f);
+      }
+      // pass 2: every object that may hold the nearest hit, in object order
+      Class32 first;
+      first.key = INFINITY;
+      int nc = 0;
+      for (uint32_t j = 0; j < S.n_obj; ++j) {
+        const float4 h = *reinterpret_cast<const float4*>(&objs[j]);
+        float lb;
+        if (!bound_test(h, ox, oy, dx, dy, thr, lb)) continue;
+        const Class32 c = classify32(objs[j], ox, oy, dx, dy, lb, j == r.src_obj ? (int)r.src_leaf : -1);
+        if (!(c.key <= thr)) continue;
+        if (nc == 0) first = c;
+        if (nc < CAND) sc.cand[nc] = (uint16_t)j;
+        else sc.overflow = 1;
+        ++nc;
+      }
+      sc.nc = (uint8_t)(nc < CAND ? nc : CAND);
+      sc.thr = thr;
+      if (nc == 1 && first.key == first.ub && first.leaf >= 0) {
+        // a single candidate whose nearest root is certain: only that root is refined
+        const uint32_t oinfo = reinterpret_cast<const uint32_t*>(&objs[sc.cand[0]])[3];
+        const int kind = leaf_kind_of(oinfo, first.leaf);
+        sc.leaf = (int8_t)first.leaf;
+        sc.face = (int8_t)first.face;
+        sc.t32 = first.ub;
+        list = kind == LEAF_CIRCLE ? LIST_REFINE_CIRCLE : kind == LEAF_RECT ? LIST_REFINE_RECT
+             : kind == LEAF_SEGMENT ? LIST_REFINE_SEGMENT : LIST_FULL;
+      } else if (nc > 0) {
+        list = LIST_FULL;
+      }
+    }
+    B.scan[idx] = sc;
+    list_append(B, gen, list, (uint32_t)idx);
+  }
+}
+
+__device__ __forceinline__ void store_hit(HitRec& o, int obj, const Hit64& h, float ev, uint8_t flags) {
+  o.obj = obj < 0 ? HIT_NONE : (uint16_t)obj;
+  o.t = h.t; o.px = h.px; o.py = h.py; o.nx = h.nx; o.ny = h.ny;
+  o.k = h.k;
+  o.leaf = h.leaf;
+  o.ev = ev;
+  o.flags = flags;
+}
+
+__global__ void __launch_bounds__(256) k_refine(SceneDev S, TraceBufs B, uint32_t gen, int list) {
+  unsigned long long n = B.ctr->list_count[gen][list];
+  if (n > B.queue_cap) n = B.queue_cap;
+  const RayRec* q = B.queue[gen & 1];
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t idx = B.list[list][i];
+    const RayRec r = q[idx];
+    const ScanRec sc = B.scan[idx];
+    Hit64 h;
+    if (refine_root(S, sc.cand[0], sc.leaf, sc.face, sc.t32, r.ox, r.oy, r.dx, r.dy, h)) {
+      store_hit(B.hit[idx], sc.cand[0], h, INFINITY, 0);
+    } else {  // cannot refine (degenerate): solve it fully after this kernel
+      const unsigned long long slot = atomicAdd(&B.ctr->list_count[gen][LIST_FULL], 1ull);
+      if (slot < B.queue_cap) B.list[LIST_FULL][slot] = idx;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_full(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ unsigned long long blk_solves;
+  if (threadIdx.x == 0) blk_solves = 0;
+  bool failed;
+  const ObjScan* objs = stage_objects(S, reinterpret_cast<ObjScan*>(smem_raw), &bar, smem_fits != 0, B.ctr, failed);
+  if (failed) return;
+  unsigned long long n = B.ctr->list_count[gen][LIST_FULL];
+  if (n > B.queue_cap) n = B.queue_cap;
+  const RayRec* q = B.queue[gen & 1];
+  unsigned long long my_solves = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t idx = B.list[LIST_FULL][i];
+    const RayRec r = q[idx];
+    const ScanRec sc = B.scan[idx];
+    df best_d2 = DF_INF, second = DF_INF;
+    float ev = INFINITY;
+    int best = -1;
+    Hit64 bh;
+    bh.leaf = 0;
+    // the nearest hit is the minimum of (d2, object index): candidates may be solved in
+    // any order, so the warp runs one solve class at a time
+    auto consider = [&](uint32_t j) {
+      Hit64 hh;
+      df d2;
+      ++my_solves;
+      if (obj_solve64(S, j, r.ox, r.oy, r.dx, r.dy, hh, d2, ev)) {
+        if (d2 < best_d2 || (d2 == best_d2 && (int)j < best)) {
+          second = best_d2;
+          best_d2 = d2;
+          best = (int)j;
+          bh = hh;
+        } else if (d2 < second) {
+          second = d2;
+        }
+      }
+    };
+    if (!sc.overflow) {
+      uint32_t pending = (1u << sc.nc) - 1u;
+      uint32_t cls[CAND];
+      for (int k = 0; k < CAND; ++k)
+        cls[k] = k < sc.nc ? solve_class(reinterpret_cast<const uint32_t*>(&objs[sc.cand[k]])[3]) : 7u;
+      const unsigned am = __activemask();
+      for (uint32_t c = 0; c < N_SOLVE_CLASSES; ++c) {
+        for (;;) {
+          int k = -1;
+          for (int kk = 0; kk < sc.nc; ++kk)
+            if (k < 0 && ((pending >> kk) & 1u) && cls[kk] == c) k = kk;
+          if (!__any_sync(am, k >= 0)) break;
+          if (k >= 0) {
+            pending &= ~(1u << k);
+            consider(sc.cand[k]);
+          }
+        }
+      }
+    } else {  // list overflow (rare): every object that passes the FP32 filters, in order
+      const float ox = r.ox.hi, oy = r.oy.hi, dx = r.dx.hi, dy = r.dy.hi;
+      for (uint32_t j = 0; j < S.n_obj; ++j) {
+        const float4 h = *reinterpret_cast<const float4*>(&objs[j]);
+        float lb;
+        if (!bound_test(h, ox, oy, dx, dy, sc.thr, lb)) continue;
+        if (!(classify32(objs[j], ox, oy, dx, dy, lb, j == r.src_obj ? (int)r.src_leaf : -1).key <= sc.thr)) continue;
+        consider(j);
+      }
+    }
+    uint8_t fl = sc.overflow ? LG_PATH_FALLBACK : 0;
+    if (best >= 0 && second.hi < INFINITY && (second - best_d2).hi <= 1e-10f * best_d2.hi) fl |= LG_PATH_NEAR_DEGENERATE;
+    store_hit(B.hit[idx], best, bh, ev, fl);
+  }
+  atomicAdd(&blk_solves, my_solves);
+  __syncthreads();
+  if (threadIdx.x == 0) atomicAdd(&B.ctr->fp64_solves, blk_solves);
+}
+
+struct Bounce {
+  bool emit;
+  float x1, y1;
+  int hit;
+  uint8_t flags;
+  int nchild;
+  RayRec child[2];
+};
+
+__device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, const RayRec& r, const ScanRec& sc,
+                                       const HitRec* hrec, uint32_t gen, Bounce& v) {
   v.emit = false;
   v.nchild = 0;
   uint8_t fl = r.flags;
   if (near_cutoff(r.c, S.cutoff)) fl |= LG_PATH_NEAR_DEGENERATE;
-  const double ox = r.ox, oy = r.oy, dx = r.dx, dy = r.dy;
-  const float ox32 = (float)ox, oy32 = (float)oy, dx32 = (float)dx, dy32 = (float)dy;
-
-  // pass 1 (FP32): the nearest certain hit bounds the search
-  float thr = INFINITY;
-  for (uint32_t j = 0; j < S.n_obj; ++j) {
-    const float4 h = *reinterpret_cast<const float4*>(&objs[j]);
-    const float ocx = h.x - ox32, ocy = h.y - oy32;
-    const float b = ocx * dx32 + ocy * dy32, perp = ocx * dy32 - ocy * dx32;
-    const float btol = 2e-6f * (fabsf(b) + fabsf(perp) + h.z) + 1e-6f;
-    if (fabsf(perp) > h.z + btol || b + h.z + btol < -TAU32) continue;
-    const float lb = b - h.z - btol;
-    if (lb > thr) continue;
-    const Class32 c = classify32(objs[j], ox32, oy32, dx32, dy32, lb);
-    if (c.ub < INFINITY) thr = fminf(thr, c.ub * (1.0f + 1e-4f) + 1e-4f);
-  }
-  // pass 2 (FP64): re-solve every object that may hold the nearest hit, in object order
-  double best_d2 = INFINITY, ev = INFINITY, second = INFINITY;
-  int best = -1;
-  Hit64 bh;
-  for (uint32_t j = 0; j < S.n_obj; ++j) {
-    const float4 h = *reinterpret_cast<const float4*>(&objs[j]);
-    const float ocx = h.x - ox32, ocy = h.y - oy32;
-    const float b = ocx * dx32 + ocy * dy32, perp = ocx * dy32 - ocy * dx32;
-    const float btol = 2e-6f * (fabsf(b) + fabsf(perp) + h.z) + 1e-6f;
-    if (fabsf(perp) > h.z + btol || b + h.z + btol < -TAU32) continue;
-    const float lb = b - h.z - btol;
-    if (lb > thr) continue;
-    const Class32 c = classify32(objs[j], ox32, oy32, dx32, dy32, lb);
-    if (!(c.key <= thr)) continue;
-    Hit64 hh;
-    double d2;
-    ++n_solves;
-    if (obj_solve64(S, j, ox, oy, dx, dy, hh, d2, ev)) {
-      if (d2 < best_d2) {
-        second = best_d2;
-        best_d2 = d2;
-        best = (int)j;
-        bh = hh;
-      } else if (d2 < second) {
-        second = d2;
-      }
-    }
-  }
-  if (best >= 0 && second < INFINITY && second - best_d2 <= BAND * best_d2) fl |= LG_PATH_NEAR_DEGENERATE;
-  if (best >= 0 ? ev <= bh.t * (1.0 + 1e-6) + 1e-12 : ev < INFINITY) fl |= LG_PATH_NEAR_DEGENERATE;
+  const df ox = r.ox, oy = r.oy, dx = r.dx, dy = r.dy;
+  HitRec bh;
+  bh.obj = HIT_NONE;
+  bh.flags = 0;
+  bh.ev = INFINITY;
+  if (sc.nc > 0) bh = *hrec;
+  fl |= bh.flags;
+  const int best = bh.obj == HIT_NONE ? -1 : (int)bh.obj;
+  if (best >= 0 ? bh.ev <= bh.t.hi * (1.0f + 1e-6f) + 1e-12f : bh.ev < INFINITY) fl |= LG_PATH_NEAR_DEGENERATE;
 
   if (best >= 0) {
     const ObjInfo oi = S.info[best];
     v.emit = true;
-    v.x0 = (float)ox; v.y0 = (float)oy; v.x1 = (float)bh.px; v.y1 = (float)bh.py;
+    v.x1 = bh.px.hi; v.y1 = bh.py.hi;
     v.hit = best;
+    // first-order error at the hit: lateral offset L, offset along the surface ds
+    const df ddn = dx * bh.nx + dy * bh.ny;
+    const float ci_abs = fabsf(ddn.hi);
+    const float L = r.ex + bh.t.hi * r.ea + DF_ROUND * (1.0f + fabsf(bh.px.hi) + fabsf(bh.py.hi));
+    const float ds = L / fmaxf(ci_abs, 1e-6f);
+    const float kap = fminf(bh.k, 1e30f);
+    if (L > ILL_COND) fl |= LG_PATH_NEAR_DEGENERATE;
     if (oi.flags & INFO_MATERIAL) {
       // medium on the far side (tracer.rs:428-442); "origin inside obj" at the midpoint
-      double n2 = 1.0;
+      df n2 = DF_ONE;
+      uint16_t m2 = MEDIUM_AIR;
       bool near = false;
-      if (obj_contains64(S, (uint32_t)best, 0.5 * (ox + bh.px), 0.5 * (oy + bh.py), near)) {
-        const float px32 = (float)bh.px, py32 = (float)bh.py;
+      if (obj_contains64(S, (uint32_t)best, DF_HALF * (ox + bh.px), DF_HALF * (oy + bh.py), near)) {
+        const float px32 = bh.px.hi, py32 = bh.py.hi;
         for (uint32_t k = 0; k < S.n_obj; ++k) {
           if ((int)k == best) continue;
           const float4 h = *reinterpret_cast<const float4*>(&objs[k]);
@@ -210,84 +422,103 @@ __device__ void visit(const SceneDev& S, const ObjScan* objs, const RayRec& r, u
           if (ex * ex + ey * ey > (h.z + tol) * (h.z + tol)) continue;
           if (obj_contains64(S, k, bh.px, bh.py, near)) {
             n2 = S.info[k].n;
+            m2 = (uint16_t)k;
             break;
           }
         }
       } else {
         n2 = oi.n;
+        m2 = (uint16_t)best;
       }
       if (near) fl |= LG_PATH_NEAR_DEGENERATE;
       // Ray::refract: Snell + unpolarised Fresnel, TIR -> reflectance 1
-      double nx = bh.nx, ny = bh.ny;
-      double ci = -(dx * nx + dy * ny);
-      if (ci < 0.0) { ci = -ci; nx = -nx; ny = -ny; }
-      const double n1 = r.n;
-      const double eta = n1 / n2;
-      const double k = 1.0 - eta * eta * (1.0 - ci * ci);
-      if (fabs(k) <= BAND) fl |= LG_PATH_NEAR_DEGENERATE;
-      double R = 1.0;
+      df nx = bh.nx, ny = bh.ny;
+      df ci = -ddn;
+      if (df_neg(ci)) { ci = -ci; nx = -nx; ny = -ny; }
+      const df n1 = r.medium == MEDIUM_AIR ? DF_ONE
+                    : r.medium == MEDIUM_LIGHT ? S.lights[r.light].n0 : S.info[r.medium].n;
+      const df eta = n1 / n2;
+      const df k = DF_ONE - eta * eta * (DF_ONE - ci * ci);
+      if (fabsf(k.hi) <= 1e-10f) fl |= LG_PATH_NEAR_DEGENERATE;
+      float R = 1.0f;
       bool refr = false;
-      double tx = 0.0, ty = 0.0;
-      if (k >= 0.0) {
-        const double ct = sqrt(k);
-        tx = eta * dx + (eta * ci - ct) * nx;
-        ty = eta * dy + (eta * ci - ct) * ny;
+      df tx = DF_ZERO, ty = DF_ZERO, ct = DF_ZERO;
+      if (!df_neg(k)) {
+        ct = dsqrt(k);
+        const df m = eta * ci - ct;
+        tx = eta * dx + m * nx;
+        ty = eta * dy + m * ny;
         refr = true;
-        const double ds = n1 * ci + n2 * ct, dp = n1 * ct + n2 * ci;
-        if (ds != 0.0 && dp != 0.0) {
-          const double rs = (n1 * ci - n2 * ct) / ds, rp = (n1 * ct - n2 * ci) / dp;
-          R = 0.5 * (rs * rs + rp * rp);
+        const df dsn = n1 * ci + n2 * ct, dp = n1 * ct + n2 * ci;
+        if (dsn.hi != 0.0f && dp.hi != 0.0f) {
+          const df rs = (n1 * ci - n2 * ct) / dsn, rp = (n1 * ct - n2 * ci) / dp;
+          R = (DF_HALF * (rs * rs + rp * rp)).hi;
         }
       }
       v.flags = fl | (refr ? 0 : LG_PATH_TIR);
-      const float refl = (float)R;
+      const float refl = R;
       const float om = 1.0f - refl;
       RayRec& a = v.child[0];
-      a.ox = bh.px; a.oy = bh.py; a.dx = dx + 2.0 * ci * nx; a.dy = dy + 2.0 * ci * ny;
-      a.n = n1;
+      const df ci2 = ci * 2.0f;
+      a.ox = bh.px; a.oy = bh.py; a.dx = dx + ci2 * nx; a.dy = dy + ci2 * ny;
+      a.medium = r.medium;
+      a.src_obj = (uint16_t)best;
+      a.src_leaf = bh.leaf;
       a.c[0] = __fmul_rn(r.c[0], refl); a.c[1] = __fmul_rn(r.c[1], refl); a.c[2] = __fmul_rn(r.c[2], refl);
       a.c[3] = r.c[3];
       a.path = r.path;
       a.flags = fl;
+      a.ex = L;
+      a.ea = r.ea + 2.0f * kap * ds;
       v.nchild = 1;
       if (refr) {
         RayRec& t = v.child[1];
         t.ox = bh.px; t.oy = bh.py; t.dx = tx; t.dy = ty;
-        t.n = n2;
+        t.medium = m2;
+        t.src_obj = (uint16_t)best;
+        t.src_leaf = bh.leaf;
         t.c[0] = __fmul_rn(r.c[0], om); t.c[1] = __fmul_rn(r.c[1], om); t.c[2] = __fmul_rn(r.c[2], om);
         t.c[3] = r.c[3];
         t.path = r.path | (1ull << gen);
         t.flags = fl;
+        const float gain = eta.hi * ci.hi / fmaxf(ct.hi, 1e-6f);
+        t.ex = ds * ct.hi + L;
+        t.ea = gain * (r.ea + kap * ds) + kap * ds;
         v.nchild = 2;
       }
     } else {
       v.flags = fl;
-      const double dn = dx * bh.nx + dy * bh.ny;  // Ray::reflect
+      const df dn2 = ddn * 2.0f;  // Ray::reflect
       RayRec& a = v.child[0];
-      a.ox = bh.px; a.oy = bh.py; a.dx = dx - 2.0 * dn * bh.nx; a.dy = dy - 2.0 * dn * bh.ny;
-      a.n = r.n;
+      a.ox = bh.px; a.oy = bh.py; a.dx = dx - dn2 * bh.nx; a.dy = dy - dn2 * bh.ny;
+      a.medium = r.medium;
+      a.src_obj = (uint16_t)best;
+      a.src_leaf = bh.leaf;
       a.c[0] = r.c[0]; a.c[1] = r.c[1]; a.c[2] = r.c[2]; a.c[3] = r.c[3];
       a.path = r.path;
       a.flags = fl;
+      a.ex = L;
+      a.ea = r.ea + 2.0f * kap * ds;
       v.nchild = 1;
     }
   } else {
     // canvas exit: nearest hit with the canvas rectangle (tracer.rs:482-488)
     Leaf64 canvas;
     canvas.kind = LEAF_RECT;
-    canvas.p[0] = 0.0; canvas.p[1] = 0.0; canvas.p[2] = 1.0; canvas.p[3] = 0.0;
-    canvas.p[4] = S.aspect; canvas.p[5] = 1.0;
+    canvas.p[0] = DF_ZERO; canvas.p[1] = DF_ZERO; canvas.p[2] = DF_ONE; canvas.p[3] = DF_ZERO;
+    canvas.p[4] = S.aspect; canvas.p[5] = DF_ONE;
     Hit64 ch[3];
-    double cev = INFINITY;
+    float cev = INFINITY;
     const int nh = leaf_hits64(canvas, ox, oy, dx, dy, ch, cev);
     if (nh > 0) {
       int bi = 0;
       for (int q = 1; q < nh; ++q)
         if (ch[q].t < ch[bi].t) bi = q;
       v.emit = true;
-      v.x0 = (float)ox; v.y0 = (float)oy; v.x1 = (float)ch[bi].px; v.y1 = (float)ch[bi].py;
+      v.x1 = ch[bi].px.hi; v.y1 = ch[bi].py.hi;
       v.hit = -1;
-      v.flags = fl | (cev < INFINITY ? LG_PATH_NEAR_DEGENERATE : 0);
+      const float L = r.ex + ch[bi].t.hi * r.ea;
+      v.flags = fl | (cev < INFINITY || L > ILL_COND ? LG_PATH_NEAR_DEGENERATE : 0);
     }
   }
   // children: the next generation skips colours below the cutoff (tracer.rs:378-384)
@@ -298,64 +529,40 @@ __device__ void visit(const SceneDev& S, const ObjScan* objs, const RayRec& r, u
     c.gen = (uint8_t)(gen + 1);
     c.prim = r.prim;
     c.light = r.light;
-    if (near_cutoff(c.c, S.cutoff)) c.flags |= LG_PATH_NEAR_DEGENERATE;
+    if (near_cutoff(c.c, S.cutoff) || !(c.ex <= ILL_COND && c.ea <= ILL_COND)) c.flags |= LG_PATH_NEAR_DEGENERATE;
     v.child[w++] = c;
   }
   v.nchild = w;
 }
 
-__global__ void __launch_bounds__(256) k_trace_gen(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
+__global__ void __launch_bounds__(256) k_bounce(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
-  __shared__ unsigned long long blk_visits, blk_solves, blk_near;
-  if (threadIdx.x == 0) { blk_visits = 0; blk_solves = 0; blk_near = 0; }
+  __shared__ unsigned long long blk_visits, blk_near;
+  if (threadIdx.x == 0) { blk_visits = 0; blk_near = 0; }
   bool failed;
   const ObjScan* objs = stage_objects(S, reinterpret_cast<ObjScan*>(smem_raw), &bar, smem_fits != 0, B.ctr, failed);
   if (failed) return;
-
-  unsigned long long n_in;
-  if (gen == 0) {
-    n_in = S.n_primary;
-  } else {
-    n_in = B.ctr->queue_count[gen];
-    if (n_in > B.queue_cap) n_in = B.queue_cap;
-  }
+  const uint64_t n_in = n_in_of(S, B, gen) < B.queue_cap ? n_in_of(S, B, gen) : B.queue_cap;
   const RayRec* qin = B.queue[gen & 1];
   RayRec* qout = B.queue[(gen + 1) & 1];
   const unsigned lane = lane_id();
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
-  unsigned long long my_visits = 0, my_solves = 0, my_near = 0;
-
+  unsigned long long my_visits = 0, my_near = 0;
   for (uint64_t base = warp * 32; base < n_in; base += nwarps * 32) {
     const uint64_t idx = base + lane;
-    Visit v;
+    Bounce v;
     v.emit = false;
     v.nchild = 0;
     RayRec r;
-    bool live = idx < n_in;
-    if (live) {
-      if (gen == 0) {
-        uint32_t l = 0;
-        while (l + 1 < S.n_lights && S.lights[l + 1].first <= idx) ++l;
-        const LightDev& L = S.lights[l];
-        const uint64_t i = idx - L.first;
-        primary_ray(L, i, r.ox, r.oy, r.dx, r.dy);
-        r.n = L.n0;
-        r.c[0] = L.color[0]; r.c[1] = L.color[1]; r.c[2] = L.color[2]; r.c[3] = L.color[3];
-        r.path = 0;
-        r.prim = (uint32_t)i;
-        r.light = (uint16_t)l;
-        r.gen = 0;
-        r.flags = 0;
-      } else {
-        r = qin[idx];
+    if (idx < n_in) {
+      r = qin[idx];
+      const ScanRec sc = B.scan[idx];
+      if (sc.nc != NC_DEAD) {
+        ++my_visits;
+        bounce(S, objs, r, sc, &B.hit[idx], gen, v);
       }
-      if (below_cutoff(r.c, S.cutoff)) live = false;
-    }
-    if (live) {
-      ++my_visits;
-      visit(S, objs, r, gen, v, my_solves);
     }
     // segments: one atomic per warp
     const unsigned emask = __ballot_sync(0xffffffffu, v.emit);
@@ -369,7 +576,7 @@ __global__ void __launch_bounds__(256) k_trace_gen(SceneDev S, TraceBufs B, uint
         if (v.flags & LG_PATH_NEAR_DEGENERATE) ++my_near;
         if (slot < B.seg_cap) {
           float4* dst = reinterpret_cast<float4*>(B.segs + slot);
-          dst[0] = make_float4(v.x0, v.y0, v.x1, v.y1);
+          dst[0] = make_float4(r.ox.hi, r.oy.hi, v.x1, v.y1);
           dst[1] = make_float4(r.c[0], r.c[1], r.c[2], r.c[3]);
           if (S.record_paths) {
             lg_path_record pr;
@@ -398,12 +605,10 @@ __global__ void __launch_bounds__(256) k_trace_gen(SceneDev S, TraceBufs B, uint
     }
   }
   atomicAdd(&blk_visits, my_visits);
-  atomicAdd(&blk_solves, my_solves);
   atomicAdd(&blk_near, my_near);
   __syncthreads();
   if (threadIdx.x == 0) {
     atomicAdd(&B.ctr->visits, blk_visits);
-    atomicAdd(&B.ctr->fp64_solves, blk_solves);
     atomicAdd(&B.ctr->near, blk_near);
   }
 }
@@ -423,8 +628,8 @@ __global__ void k_overlay(SceneDev S, TraceBufs B, const uint32_t* cubic_objs, u
       const uint32_t k = cubic_objs[i / 3];
       const int q = (int)(i % 3);
       const Leaf64& L = S.leaves[S.info[k].leaf_begin];
-      s.x0 = (float)L.p[2 * q]; s.y0 = (float)L.p[2 * q + 1];
-      s.x1 = (float)L.p[2 * q + 2]; s.y1 = (float)L.p[2 * q + 3];
+      s.x0 = L.p[2 * q].hi; s.y0 = L.p[2 * q + 1].hi;
+      s.x1 = L.p[2 * q + 2].hi; s.y1 = L.p[2 * q + 3].hi;
       s.color[0] = 1.f; s.color[1] = 0.f; s.color[2] = 0.f; s.color[3] = 1.f;
       pr.primary = k; pr.gen = (uint8_t)q; pr.source = LG_SRC_CONTROL_LINE;
     } else {

@@ -13,6 +13,7 @@ from dataclasses import dataclass
 import numpy as np
 
 ENDPOINT_TOL = 1e-5
+COLOR_TOL = 1e-6   # relative: a few f32 ulps from the f64 -> f32 rounding of the reflectance
 NEAR = 1
 
 
@@ -59,7 +60,9 @@ def compare(g_segs, g_paths, o_segs, o_paths, o_s64, primary_filter=None) -> Par
     flagged = gflag[ig] | oflag[io] if len(ig) else np.zeros(0, bool)
     clean_g, clean_o = ig[~flagged], io[~flagged]
     hit_mm = int((g_paths["hit"][clean_g] != o_paths["hit"][clean_o]).sum())
-    col_mm = int((g_segs["color"][clean_g] != o_segs["color"][clean_o]).any(axis=1).sum())
+    gc = g_segs["color"][clean_g].astype(np.float64)
+    oc = o_segs["color"][clean_o].astype(np.float64)
+    col_mm = int((np.abs(gc - oc) > COLOR_TOL * np.maximum(np.abs(oc), 1e-30)).any(axis=1).sum())
     if len(clean_g):
         gp = np.stack([g_segs["x0"][clean_g], g_segs["y0"][clean_g], g_segs["x1"][clean_g], g_segs["y1"][clean_g]], 1)
         op = o_s64[clean_o]
@@ -67,8 +70,21 @@ def compare(g_segs, g_paths, o_segs, o_paths, o_s64, primary_filter=None) -> Par
         max_err = float(err.max())
     else:
         max_err = 0.0
-    g_only_unf = sum(1 for k in g_only if not gflag[gi[k]])
-    o_only_unf = sum(1 for k in o_only if not oflag[oi[k]])
+    def excused(key, own_flag, other_index, other_flag):
+        # flagged on its own side, or its parent is flagged on the other side (the trees
+        # diverged below a near-degenerate decision)
+        if own_flag:
+            return True
+        (k, path) = key
+        gen = k & 0xff
+        if gen == 0:
+            return False
+        parent = ((k & ~np.uint64(0xff).item()) | (gen - 1), path & ~(1 << (gen - 1)))
+        j = other_index.get(parent)
+        return j is not None and bool(other_flag[j])
+
+    g_only_unf = sum(1 for k in g_only if not excused(k, gflag[gi[k]], oi, oflag))
+    o_only_unf = sum(1 for k in o_only if not excused(k, oflag[oi[k]], gi, gflag))
     return ParityReport(len(common), len(g_only), len(o_only), g_only_unf, o_only_unf, hit_mm, col_mm, max_err,
                         int(flagged.sum()) + len(g_only) + len(o_only) - g_only_unf - o_only_unf)
 
