@@ -229,8 +229,12 @@ void leaf_box(const LeafH& L, double& x0, double& y0, double& x1, double& y1) {
   }
 }
 
-void leaf_f32(const LeafH& L, float* a) {
-  if (L.kind == LEAF_CIRCLE) {
+void leaf_f32(const LeafH& L, float* a, float* b) {
+  if (L.kind == LEAF_CUBIC) {
+    for (int k = 0; k < 6; ++k) a[k] = (float)L.p[k];
+    b[0] = (float)L.p[6];
+    b[1] = (float)L.p[7];
+  } else if (L.kind == LEAF_CIRCLE) {
     a[0] = (float)L.p[0]; a[1] = (float)L.p[1]; a[2] = (float)L.p[2];
   } else if (L.kind == LEAF_RECT) {
     for (int k = 0; k < 6; ++k) a[k] = (float)L.p[k];
@@ -298,18 +302,20 @@ lg_status flatten_scene(lg_ctx* c, const lg_geo* G, uint32_t n_geo, const lg_obj
     s.cy = (float)cy;
     s.R = (float)(R * (1.0 + 1e-6) + 1e-6 * (1.0 + std::fabs(cx) + std::fabs(cy)));
     const uint32_t nl = oi.n_leaves;
-    bool simple = nl <= 2;
-    for (uint32_t i = leaf0; i < F.leaves.size(); ++i) simple = simple && F.leaves[i].kind != LEAF_CUBIC;
+    // one leaf of any kind (a cubic takes both inline slots), or two non-cubic leaves
+    bool no_cubic = true;
+    for (uint32_t i = leaf0; i < F.leaves.size(); ++i) no_cubic = no_cubic && F.leaves[i].kind != LEAF_CUBIC;
     uint32_t info = SCAN_BOUND;
-    if (simple && nl == 1) {
+    float scratch[6];
+    if (nl == 1) {
       info = SCAN_ONE | (F.leaves[leaf0].kind << 4);
-      leaf_f32(F.leaves[leaf0], s.a);
-    } else if (simple && nl == 2) {
+      leaf_f32(F.leaves[leaf0], s.a, s.b);
+    } else if (nl == 2 && no_cubic) {
       const uint8_t op = prog.back();
       info = SCAN_TWO | (F.leaves[leaf0].kind << 4) | (F.leaves[leaf0 + 1].kind << 6) |
              ((uint32_t)(op == PROG_AND ? LG_OP_AND : op == PROG_OR ? LG_OP_OR : LG_OP_AND_NOT) << 8);
-      leaf_f32(F.leaves[leaf0], s.a);
-      leaf_f32(F.leaves[leaf0 + 1], s.b);
+      leaf_f32(F.leaves[leaf0], s.a, scratch);
+      leaf_f32(F.leaves[leaf0 + 1], s.b, scratch);
     }
     s.info = info | oi.flags;
     F.scan.push_back(s);
@@ -434,7 +440,7 @@ lg_status enqueue_trace(lg_ctx* c) {
   const size_t tsm = c->smem_fits ? c->obj_smem : 0;
   for (uint32_t g = 0; g < c->prm.max_bounce; ++g) {
     k_scan<<<c->trace_grid[0], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
-    for (int l = LIST_REFINE_CIRCLE; l <= LIST_REFINE_SEGMENT; ++l)
+    for (int l = LIST_REFINE_CIRCLE; l <= LIST_REFINE_CUBIC; ++l)
       k_refine<<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g, l);
     k_full<<<c->trace_grid[2], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
     k_bounce<<<c->trace_grid[3], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
@@ -650,7 +656,7 @@ lg_status lg_destroy(lg_ctx* c) {
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   DevBuf* bufs[] = {&c->d_scan, &c->d_info, &c->d_leaves, &c->d_prog, &c->d_lights, &c->d_cubics, &c->d_queue[0],
                     &c->d_queue[1], &c->d_scanrec, &c->d_hitrec, &c->d_list[0], &c->d_list[1], &c->d_list[2],
-                    &c->d_list[3], &c->d_segs, &c->d_paths, &c->d_ctr, &c->d_tile_count, &c->d_tile_off,
+                    &c->d_list[3], &c->d_list[4], &c->d_segs, &c->d_paths, &c->d_ctr, &c->d_tile_count, &c->d_tile_off,
                     &c->d_tile_cursor, &c->d_unit_off, &c->d_refs, &c->d_units, &c->d_accum, &c->d_stage};
   for (DevBuf* b : bufs) release(*b);
   if (c->h_ctr) cudaFreeHost(c->h_ctr);

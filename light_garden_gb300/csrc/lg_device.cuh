@@ -120,7 +120,9 @@ constexpr float ILL_COND = 1e-11f;
 constexpr float DF_ROUND = 2e-14f;  // double-float rounding per bounce, relative to the coordinates
 
 // work lists of one generation (k_scan appends, k_refine / k_full consume)
-enum : int { LIST_REFINE_CIRCLE = 0, LIST_REFINE_RECT = 1, LIST_REFINE_SEGMENT = 2, LIST_FULL = 3, N_LISTS = 4 };
+enum : int {
+  LIST_REFINE_CIRCLE = 0, LIST_REFINE_RECT = 1, LIST_REFINE_SEGMENT = 2, LIST_REFINE_CUBIC = 3, LIST_FULL = 4, N_LISTS = 5
+};
 
 struct Counters {
   unsigned long long seg_count;               // ring cursor (= segments demanded)
@@ -156,7 +158,7 @@ struct __align__(16) ScanRec {
   int8_t leaf, face; // refine path: the winner's leaf and rect face
   float t32;         // refine path: the winner's FP32 root
   float thr;         // FP32 bound on the nearest hit distance
-  uint32_t _pad;
+  float s32;         // refine path, cubic: the winner's FP32 curve parameter
 };
 static_assert(sizeof(ScanRec) == 32, "ScanRec is 32 B");
 constexpr uint8_t NC_DEAD = 0xff;
@@ -513,12 +515,13 @@ static __device__ __noinline__ bool obj_solve64(const SceneDev& S, uint32_t k, d
 struct Class32 {
   float key, ub;
   int leaf, face;  // leaf and face (rect: 2 * axis + (outward sign > 0)) of the root at ub
+  float s;         // cubic: curve parameter of the root at ub
 };
 
-__device__ __forceinline__ void root32(float t, float tol, Class32& c, bool certain, int leaf, int face) {
+__device__ __forceinline__ void root32(float t, float tol, Class32& c, bool certain, int leaf, int face, float sv) {
   if (t < -TAU32) return;                     // certainly behind the origin
   if (certain && t > TAU32) {
-    if (t < c.ub) { c.ub = t; c.leaf = leaf; c.face = face; }
+    if (t < c.ub) { c.ub = t; c.leaf = leaf; c.face = face; c.s = sv; }
     c.key = fminf(c.key, t);
   } else {
     c.key = fminf(c.key, fmaxf(t - tol, 0.0f));
@@ -545,11 +548,78 @@ __device__ __forceinline__ int leaf_member32(uint32_t kind, const float* L, floa
   return 0;  // segments enclose nothing
 }
 
+// Roots of a cubic Bezier leaf in FP32: f(s) = cross(d, B(s) - o) is monotone between the
+// roots of f', so each sign change between consecutive knots is one root, found by
+// bisection.  A knot where |f| is within the FP32 error (tangency, a curve end on the ray)
+// or a root where f' is small makes the whole leaf "unknown" (precise solve).
+__device__ __forceinline__ int cubic_roots32(const float* A, const float* Bp, float ox, float oy, float dx, float dy,
+                                             float* t, bool* cert, float* sv, float& tol, bool& unknown) {
+  const float c0x = A[0], c0y = A[1];
+  const float c1x = 3.0f * (A[2] - A[0]), c1y = 3.0f * (A[3] - A[1]);
+  const float c2x = 3.0f * (A[4] - 2.0f * A[2] + A[0]), c2y = 3.0f * (A[5] - 2.0f * A[3] + A[1]);
+  const float c3x = Bp[0] + 3.0f * (A[2] - A[4]) - A[0], c3y = Bp[1] + 3.0f * (A[3] - A[5]) - A[1];
+  const float a0 = dx * (c0y - oy) - dy * (c0x - ox);
+  const float a1 = dx * c1y - dy * c1x, a2 = dx * c2y - dy * c2x, a3 = dx * c3y - dy * c3x;
+  const float sc = fabsf(a0) + fabsf(a1) + fabsf(a2) + fabsf(a3) + 1e-30f;
+  const float err = 1e-4f * sc + 2e-6f * (fabsf(c0x) + fabsf(c0y) + fabsf(ox) + fabsf(oy));
+  auto f = [&](float u) { return ((a3 * u + a2) * u + a1) * u + a0; };
+  float knots[4];
+  int nk = 0;
+  knots[nk++] = 0.0f;
+  const float qa = 3.0f * a3, qb = 2.0f * a2, qc = a1;
+  if (fabsf(qa) > 1e-7f * sc) {
+    const float disc = qb * qb - 4.0f * qa * qc;
+    if (disc >= 0.0f) {
+      const float sq = sqrtf(disc);
+      const float q = -0.5f * (qb + (qb >= 0.0f ? sq : -sq));
+      float r1 = q / qa, r2 = q != 0.0f ? qc / q : r1;
+      if (r1 > r2) { const float x = r1; r1 = r2; r2 = x; }
+      if (r1 > 0.0f && r1 < 1.0f) knots[nk++] = r1;
+      if (r2 > 0.0f && r2 < 1.0f && r2 != knots[nk - 1]) knots[nk++] = r2;
+    }
+  } else if (fabsf(qb) > 1e-7f * sc) {
+    const float r = -qc / qb;
+    if (r > 0.0f && r < 1.0f) knots[nk++] = r;
+  }
+  knots[nk++] = 1.0f;
+  int n = 0;
+  tol = 1e-6f;
+  const float dd = dx * dx + dy * dy;
+  for (int i = 0; i + 1 < nk; ++i) {
+    float lo = knots[i], hi = knots[i + 1];
+    float flo = f(lo);
+    const float fhi = f(hi);
+    if (fabsf(flo) <= err || fabsf(fhi) <= err) { unknown = true; return 0; }
+    if ((flo < 0.0f) == (fhi < 0.0f)) continue;
+    for (int it = 0; it < 26; ++it) {
+      const float mid = 0.5f * (lo + hi);
+      const float fm = f(mid);
+      if ((fm < 0.0f) == (flo < 0.0f)) { lo = mid; flo = fm; } else { hi = mid; }
+    }
+    const float u = 0.5f * (lo + hi);
+    const float fp = (3.0f * a3 * u + 2.0f * a2) * u + a1;
+    if (fabsf(fp) < 1e-3f * sc) { unknown = true; return 0; }
+    const float bx = ((c3x * u + c2x) * u + c1x) * u + c0x, by = ((c3y * u + c2y) * u + c1y) * u + c0y;
+    const float dbx = (3.0f * c3x * u + 2.0f * c2x) * u + c1x, dby = (3.0f * c3y * u + 2.0f * c2y) * u + c1y;
+    t[n] = ((bx - ox) * dx + (by - oy) * dy) / dd;
+    sv[n] = u;
+    cert[n] = u > 1e-4f && u < 1.0f - 1e-4f;
+    const float tl = fabsf(dbx * dx + dby * dy) * (err / fabsf(fp) + 1e-6f) +
+                     2e-6f * (fabsf(bx) + fabsf(by) + fabsf(ox) + fabsf(oy)) + 1e-6f;
+    tol = fmaxf(tol, tl);
+    ++n;
+  }
+  return n;
+}
+
 // roots of one FP32 leaf: t values with a certainty flag each
-__device__ __forceinline__ int leaf_roots32(uint32_t kind, const float* L, float ox, float oy, float dx, float dy,
-                                            float* t, bool* cert, int* face, float& tol, bool& unknown) {
+__device__ __forceinline__ int leaf_roots32(uint32_t kind, const float* L, const float* L2, float ox, float oy,
+                                            float dx, float dy, float* t, bool* cert, int* face, float* sv, float& tol,
+                                            bool& unknown) {
   unknown = false;
-  face[0] = face[1] = -1;
+  face[0] = face[1] = face[2] = -1;
+  sv[0] = sv[1] = sv[2] = 0.0f;
+  if (kind == LEAF_CUBIC) return cubic_roots32(L, L2, ox, oy, dx, dy, t, cert, sv, tol, unknown);
   if (kind == LEAF_CIRCLE) {
     const float ocx = ox - L[0], ocy = oy - L[1], r = L[2];
     const float b = ocx * dx + ocy * dy, perp = ocx * dy - ocy * dx;
@@ -635,6 +705,7 @@ __device__ __noinline__ Class32 classify32(const ObjScan& r, float ox, float oy,
   c.ub = INFINITY;
   c.leaf = -1;
   c.face = -1;
+  c.s = 0.0f;
   const uint32_t sk = info_scan(r.info);
   if (sk == SCAN_BOUND) {
     c.key = fmaxf(lb, 0.0f);
@@ -644,21 +715,26 @@ __device__ __noinline__ Class32 classify32(const ObjScan& r, float ox, float oy,
   for (int side = 0; side < nleaf; ++side) {
     const float* L = side == 0 ? r.a : r.b;
     const uint32_t kind = side == 0 ? info_leaf_a(r.info) : info_leaf_b(r.info);
-    float t[2];
-    bool cert[2];
-    int face[2];
+    float t[3];
+    bool cert[3];
+    int face[3];
+    float sv[3];
     float tol = 1e-5f;
     bool unknown = false;
-    int n = leaf_roots32(kind, L, ox, oy, dx, dy, t, cert, face, tol, unknown);
+    int n = leaf_roots32(kind, L, r.b, ox, oy, dx, dy, t, cert, face, sv, tol, unknown);
     if (unknown) {  // near-parallel: defer the whole object to the precise solve
       c.key = fminf(c.key, fmaxf(lb, 0.0f));
       continue;
     }
     if (side == src_leaf && n > 0) {
-      const int ks = (n == 2 && fabsf(t[1]) < fabsf(t[0])) ? 1 : 0;
-      const bool other_near = n == 2 && fabsf(t[1 - ks]) < 4.0f * TAU32;
+      int ks = 0;
+      for (int k = 1; k < n; ++k)
+        if (fabsf(t[k]) < fabsf(t[ks])) ks = k;
+      bool other_near = false;
+      for (int k = 0; k < n; ++k)
+        if (k != ks && fabsf(t[k]) < 4.0f * TAU32) other_near = true;
       if (fabsf(t[ks]) < TAU32 && cert[ks] && !other_near) {
-        if (n == 2 && ks == 0) { t[0] = t[1]; cert[0] = cert[1]; face[0] = face[1]; }
+        for (int k = ks; k + 1 < n; ++k) { t[k] = t[k + 1]; cert[k] = cert[k + 1]; face[k] = face[k + 1]; sv[k] = sv[k + 1]; }
         n -= 1;
       }
     }
@@ -674,7 +750,7 @@ __device__ __noinline__ Class32 classify32(const ObjScan& r, float ox, float oy,
         if (m < 0) certain = false;
         else if (!op_keep(info_op(r.info), side == 0, m == 1)) continue;
       }
-      root32(t[k], tol, c, certain, side, face[k]);
+      root32(t[k], tol, c, certain, side, face[k], sv[k]);
     }
   }
   return c;
@@ -685,8 +761,8 @@ __device__ __noinline__ Class32 classify32(const ObjScan& r, float ox, float oy,
 // `face`) with margins far above FP32 error; recompute that one root in double-float
 // instead of solving the whole object: two Newton steps on |o + t d - c|^2 = r^2 for a
 // circle, the face plane of a rect, the 2x2 solve of a mirror segment.
-static __device__ __noinline__ bool refine_root(const SceneDev& S, uint32_t j, int leaf, int face, float t32, df ox,
-                                                df oy, df dx, df dy, Hit64& h) {
+static __device__ __noinline__ bool refine_root(const SceneDev& S, uint32_t j, int leaf, int face, float t32, float s32,
+                                                df ox, df oy, df dx, df dy, Hit64& h) {
   const ObjInfo oi = S.info[j];
   const Leaf64 L = S.leaves[oi.leaf_begin + leaf];
   df t;
@@ -715,6 +791,7 @@ static __device__ __noinline__ bool refine_root(const SceneDev& S, uint32_t j, i
     h.ny = L.p[5];
     h.k = 0.0f;
   } else if (L.kind == LEAF_RECT) {
+    (void)s32;
     if (face < 0) return false;
     const int ax = face >> 1;
     const float sg = (face & 1) ? 1.0f : -1.0f;
@@ -729,8 +806,33 @@ static __device__ __noinline__ bool refine_root(const SceneDev& S, uint32_t j, i
     h.nx = nx;
     h.ny = ny;
     h.k = 0.0f;
-  } else {
-    return false;
+  } else {  // cubic: Newton on f(s) = cross(d, B(s) - o) from the FP32 root
+    const df* v = L.p;
+    const df c0x = v[0], c0y = v[1];
+    const df c1x = 3.0f * (v[2] - v[0]), c1y = 3.0f * (v[3] - v[1]);
+    const df c2x = 3.0f * (v[4] - 2.0f * v[2]) + 3.0f * v[0], c2y = 3.0f * (v[5] - 2.0f * v[3]) + 3.0f * v[1];
+    const df c3x = v[6] + 3.0f * (v[2] - v[4]) - v[0], c3y = v[7] + 3.0f * (v[3] - v[5]) - v[1];
+    const df a0 = dx * (c0y - oy) - dy * (c0x - ox);
+    const df a1 = dx * c1y - dy * c1x, a2 = dx * c2y - dy * c2x, a3 = dx * c3y - dy * c3x;
+    df u{s32, 0.0f};
+    for (int it = 0; it < 2; ++it) {
+      const df fu = ((a3 * u + a2) * u + a1) * u + a0;
+      const float fp = (3.0f * a3.hi * u.hi + 2.0f * a2.hi) * u.hi + a1.hi;
+      if (fp == 0.0f) return false;
+      u = u - df{__fdiv_rn(fu.hi, fp), 0.0f};
+    }
+    const df bx = ((c3x * u + c2x) * u + c1x) * u + c0x, by = ((c3y * u + c2y) * u + c1y) * u + c0y;
+    t = ((bx - ox) * dx + (by - oy) * dy) / (dx * dx + dy * dy);
+    h.px = ox + dx * t;
+    h.py = oy + dy * t;
+    const df tx = (3.0f * c3x * u + 2.0f * c2x) * u + c1x, ty = (3.0f * c3y * u + 2.0f * c2y) * u + c1y;
+    const df l = dsqrt(tx * tx + ty * ty);
+    if (!(l.hi > 0.0f)) return false;
+    const df li = DF_ONE / l;
+    h.nx = -(ty * li);
+    h.ny = tx * li;
+    const float bbx = 6.0f * c3x.hi * u.hi + 2.0f * c2x.hi, bby = 6.0f * c3y.hi * u.hi + 2.0f * c2y.hi;
+    h.k = fabsf(tx.hi * bby - ty.hi * bbx) / (l.hi * l.hi * l.hi);
   }
   h.t = t;
   h.leaf = (uint8_t)leaf;

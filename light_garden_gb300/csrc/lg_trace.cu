@@ -217,6 +217,7 @@ __global__ void __launch_bounds__(256) k_scan(SceneDev S, TraceBufs B, uint32_t 
     sc.leaf = -1;
     sc.face = -1;
     sc.t32 = 0.0f;
+    sc.s32 = 0.0f;
     sc.thr = INFINITY;
     int list = -1;
     if (below_cutoff(r.c, S.cutoff)) {
@@ -256,8 +257,9 @@ __global__ void __launch_bounds__(256) k_scan(SceneDev S, TraceBufs B, uint32_t 
         sc.leaf = (int8_t)first.leaf;
         sc.face = (int8_t)first.face;
         sc.t32 = first.ub;
+        sc.s32 = first.s;
         list = kind == LEAF_CIRCLE ? LIST_REFINE_CIRCLE : kind == LEAF_RECT ? LIST_REFINE_RECT
-             : kind == LEAF_SEGMENT ? LIST_REFINE_SEGMENT : LIST_FULL;
+             : kind == LEAF_SEGMENT ? LIST_REFINE_SEGMENT : LIST_REFINE_CUBIC;
       } else if (nc > 0) {
         list = LIST_FULL;
       }
@@ -285,7 +287,7 @@ __global__ void __launch_bounds__(256) k_refine(SceneDev S, TraceBufs B, uint32_
     const RayRec r = q[idx];
     const ScanRec sc = B.scan[idx];
     Hit64 h;
-    if (refine_root(S, sc.cand[0], sc.leaf, sc.face, sc.t32, r.ox, r.oy, r.dx, r.dy, h)) {
+    if (refine_root(S, sc.cand[0], sc.leaf, sc.face, sc.t32, sc.s32, r.ox, r.oy, r.dx, r.dy, h)) {
       store_hit(B.hit[idx], sc.cand[0], h, INFINITY, 0);
     } else {  // cannot refine (degenerate): solve it fully after this kernel
       const unsigned long long slot = atomicAdd(&B.ctr->list_count[gen][LIST_FULL], 1ull);
