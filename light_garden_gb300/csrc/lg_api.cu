@@ -439,7 +439,7 @@ lg_status enqueue_trace(lg_ctx* c) {
   if (c->n_lights) k_light_setup<<<1, 256, 0, c->stream>>>(S);
   const size_t tsm = c->smem_fits ? c->obj_smem : 0;
   for (uint32_t g = 0; g < c->prm.max_bounce; ++g) {
-    k_scan<<<c->trace_grid[0], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
+    k_scan<<<c->trace_grid[0], SCAN_THREADS, (size_t)scan_smem_bytes() + tsm, c->stream>>>(S, B, g, c->smem_fits);
     for (int l = LIST_REFINE_CIRCLE; l <= LIST_REFINE_CUBIC; ++l)
       k_refine<<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g, l);
     k_full<<<c->trace_grid[2], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
@@ -629,7 +629,8 @@ lg_status lg_create(lg_ctx** out, const lg_device_opts* opts) {
   if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_ctr, sizeof(Counters));
   if (e == cudaSuccess) e = cudaMalloc(&c->d_ctr.p, sizeof(Counters));
   for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, scan_smem_bytes() + (int)OBJ_SMEM_MAX);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_full, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bounce, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
   if (e == cudaSuccess)
@@ -727,7 +728,7 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
   c->smem_fits = c->obj_smem <= OBJ_SMEM_MAX ? 1 : 0;
   int occ = 0;
   const size_t tsm = c->smem_fits ? c->obj_smem : 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_scan, 256, tsm), "occupancy");
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_scan, SCAN_THREADS, (size_t)scan_smem_bytes() + tsm), "occupancy");
   c->trace_grid[0] = c->n_sm * std::max(1, occ);
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_refine, 256, 0), "occupancy");
   c->trace_grid[1] = c->n_sm * std::max(1, occ);

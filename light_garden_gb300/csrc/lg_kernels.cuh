@@ -38,6 +38,8 @@ struct RasterArgs {
 
 __global__ void k_light_setup(SceneDev S);
 __global__ void k_scan(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
+int scan_smem_bytes();
+constexpr int SCAN_THREADS = 128;
 __global__ void k_refine(SceneDev S, TraceBufs B, uint32_t gen, int list);
 __global__ void k_full(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
 __global__ void k_bounce(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);

@@ -175,97 +175,186 @@ __device__ __forceinline__ void list_append(const TraceBufs& B, uint32_t gen, in
   if (slot < B.queue_cap) B.list[list][slot] = idx;
 }
 
-__global__ void __launch_bounds__(256) k_scan(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
+// Warp-cooperative FP32 scan.  Objects are taken in chunks of SCAN_CHUNK: every lane
+// bounding-tests its own ray against the chunk (pruned by its running bound thr) and
+// writes the passing (ray, object) pairs to the warp's shared buffer; then all 32 lanes
+// classify the warp's pairs side by side, so the exact FP32 tests run at full SIMD width
+// instead of only in the lanes whose ray happens to cross a given object.  Each lane then
+// folds its own results in object order: thr shrinks with every certain hit and the
+// candidates (key <= thr) keep object order for the tie rule of tracer.rs:404,417.
+constexpr int SCAN_WARPS = 4;
+constexpr int SCAN_CHUNK = 16;
+
+struct __align__(16) PairSlot {
+  float key, ub, s;
+  uint32_t m;  // object | (leaf + 1) << 16 | (face + 1) << 24; before classification key holds lb
+};
+
+struct ScanSmem {
+  PairSlot pairs[SCAN_WARPS][32][SCAN_CHUNK];
+  PairSlot cand[SCAN_WARPS][32][CAND];
+  float4 ray[SCAN_WARPS][32];
+  uint32_t src[SCAN_WARPS][32];
+  int off[SCAN_WARPS][33];
+};
+
+int scan_smem_bytes() { return (int)sizeof(ScanSmem); }
+
+__global__ void __launch_bounds__(SCAN_WARPS * 32) k_scan(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
+  ScanSmem& W = *reinterpret_cast<ScanSmem*>(smem_raw);
+  ObjScan* sobj = reinterpret_cast<ObjScan*>(smem_raw + sizeof(ScanSmem));
   bool failed;
-  const ObjScan* objs = stage_objects(S, reinterpret_cast<ObjScan*>(smem_raw), &bar, smem_fits != 0, B.ctr, failed);
+  const ObjScan* objs = stage_objects(S, sobj, &bar, smem_fits != 0, B.ctr, failed);
   if (failed) return;
   const uint64_t n_in = n_in_of(S, B, gen);
   RayRec* q = B.queue[gen & 1];
-  for (uint64_t idx = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; idx < n_in;
-       idx += (uint64_t)gridDim.x * blockDim.x) {
+  const unsigned lane = lane_id(), w = threadIdx.x >> 5;
+  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+  for (uint64_t base = warp * 32; base < n_in; base += nwarps * 32) {
+    const uint64_t idx = base + lane;
+    bool live = idx < n_in;
     RayRec r;
-    if (gen == 0) {
-      uint32_t l = 0;
-      while (l + 1 < S.n_lights && S.lights[l + 1].first <= idx) ++l;
-      const LightDev& L = S.lights[l];
-      const uint64_t i = idx - L.first;
-      double pox, poy, pdx, pdy;
-      primary_ray(L, i, pox, poy, pdx, pdy);
-      r.ox = df_from_double(pox); r.oy = df_from_double(poy);
-      r.dx = df_from_double(pdx); r.dy = df_from_double(pdy);
-      r.medium = MEDIUM_LIGHT;
-      r.src_obj = SRC_NONE;
-      r.src_leaf = 0;
-      r.c[0] = L.color[0]; r.c[1] = L.color[1]; r.c[2] = L.color[2]; r.c[3] = L.color[3];
-      r.path = 0;
-      r.prim = (uint32_t)i;
-      r.light = (uint16_t)l;
-      r.gen = 0;
-      r.flags = 0;
-      // rounding of the light's ray generator (sin/cos/atan) and the double-float split
-      r.ex = DF_ROUND * (1.0f + fabsf(r.ox.hi) + fabsf(r.oy.hi));
-      r.ea = DF_ROUND;
-      if (idx < B.queue_cap) q[idx] = r;
-    } else {
-      r = q[idx];
+    if (live) {
+      if (gen == 0) {
+        uint32_t l = 0;
+        while (l + 1 < S.n_lights && S.lights[l + 1].first <= idx) ++l;
+        const LightDev& L = S.lights[l];
+        const uint64_t i = idx - L.first;
+        double pox, poy, pdx, pdy;
+        primary_ray(L, i, pox, poy, pdx, pdy);
+        r.ox = df_from_double(pox); r.oy = df_from_double(poy);
+        r.dx = df_from_double(pdx); r.dy = df_from_double(pdy);
+        r.medium = MEDIUM_LIGHT;
+        r.src_obj = SRC_NONE;
+        r.src_leaf = 0;
+        r.c[0] = L.color[0]; r.c[1] = L.color[1]; r.c[2] = L.color[2]; r.c[3] = L.color[3];
+        r.path = 0;
+        r.prim = (uint32_t)i;
+        r.light = (uint16_t)l;
+        r.gen = 0;
+        r.flags = 0;
+        // rounding of the light's ray generator (sin/cos/atan) and the double-float split
+        r.ex = DF_ROUND * (1.0f + fabsf(r.ox.hi) + fabsf(r.oy.hi));
+        r.ea = DF_ROUND;
+        if (idx < B.queue_cap) q[idx] = r;
+      } else {
+        r = q[idx];
+      }
     }
-    ScanRec sc;
-    sc.nc = 0;
-    sc.overflow = 0;
-    sc.leaf = -1;
-    sc.face = -1;
-    sc.t32 = 0.0f;
-    sc.s32 = 0.0f;
-    sc.thr = INFINITY;
-    int list = -1;
-    if (below_cutoff(r.c, S.cutoff)) {
-      sc.nc = NC_DEAD;
-    } else {
-      const float ox = r.ox.hi, oy = r.oy.hi, dx = r.dx.hi, dy = r.dy.hi;
-      // pass 1: the nearest certain hit bounds the search
-      float thr = INFINITY;
-      for (uint32_t j = 0; j < S.n_obj; ++j) {
-        const float4 h = *reinterpret_cast<const float4*>(&objs[j]);
+    const bool dead = live && below_cutoff(r.c, S.cutoff);
+    live = live && !dead;
+    const float ox = r.ox.hi, oy = r.oy.hi, dx = r.dx.hi, dy = r.dy.hi;
+    W.ray[w][lane] = make_float4(ox, oy, dx, dy);
+    W.src[w][lane] = live ? ((uint32_t)r.src_obj << 8 | r.src_leaf) : 0xffffffffu;
+    float thr = INFINITY;
+    int nc = 0;
+    bool overflow = false;
+    for (uint32_t j0 = 0; j0 < S.n_obj; j0 += SCAN_CHUNK) {
+      const uint32_t jn = min((uint32_t)SCAN_CHUNK, S.n_obj - j0);
+      int cnt = 0;
+      for (uint32_t jj = 0; jj < jn; ++jj) {
+        const float4 h = *reinterpret_cast<const float4*>(&objs[j0 + jj]);
         float lb;
-        if (!bound_test(h, ox, oy, dx, dy, thr, lb)) continue;
-        const Class32 c = classify32(objs[j], ox, oy, dx, dy, lb, j == r.src_obj ? (int)r.src_leaf : -1);
-        if (c.ub < INFINITY) thr = fminf(thr, c.ub * (1.0f + 1e-4f) + 1e-4f);
+        if (live && bound_test(h, ox, oy, dx, dy, thr, lb)) {
+          PairSlot ps;
+          ps.key = lb;
+          ps.ub = 0.0f;
+          ps.s = 0.0f;
+          ps.m = j0 + jj;
+          W.pairs[w][lane][cnt++] = ps;
+        }
       }
-      // pass 2: every object that may hold the nearest hit, in object order
-      Class32 first;
-      first.key = INFINITY;
-      int nc = 0;
-      for (uint32_t j = 0; j < S.n_obj; ++j) {
-        const float4 h = *reinterpret_cast<const float4*>(&objs[j]);
-        float lb;
-        if (!bound_test(h, ox, oy, dx, dy, thr, lb)) continue;
-        const Class32 c = classify32(objs[j], ox, oy, dx, dy, lb, j == r.src_obj ? (int)r.src_leaf : -1);
-        if (!(c.key <= thr)) continue;
-        if (nc == 0) first = c;
-        if (nc < CAND) sc.cand[nc] = (uint16_t)j;
-        else sc.overflow = 1;
-        ++nc;
+      // flatten the warp's pairs: exclusive scan of the per-lane counts
+      int incl = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((int)lane >= o) incl += y;
       }
-      sc.nc = (uint8_t)(nc < CAND ? nc : CAND);
+      W.off[w][lane] = incl - cnt;
+      if (lane == 31) W.off[w][32] = incl;
+      __syncwarp();
+      const int total = W.off[w][32];
+      for (int p = (int)lane; p < total; p += 32) {
+        int lo = 0, hi = 32;  // owner: the last lane whose offset is <= p
+        while (hi - lo > 1) {
+          const int mid = (lo + hi) >> 1;
+          if (W.off[w][mid] <= p) lo = mid; else hi = mid;
+        }
+        const int k = p - W.off[w][lo];
+        PairSlot& ps = W.pairs[w][lo][k];
+        const uint32_t j = ps.m;
+        const float4 rr = W.ray[w][lo];
+        const uint32_t src = W.src[w][lo];
+        const Class32 c = classify32(objs[j], rr.x, rr.y, rr.z, rr.w, ps.key, (src >> 8) == j ? (int)(src & 0xffu) : -1);
+        PairSlot o;
+        o.key = c.key;
+        o.ub = c.ub;
+        o.s = c.s;
+        o.m = j | ((uint32_t)(c.leaf + 1) << 16) | ((uint32_t)(c.face + 1) << 24);
+        ps = o;
+      }
+      __syncwarp();
+      // fold this lane's results in object order
+      for (int k = 0; k < cnt; ++k) {
+        const PairSlot ps = W.pairs[w][lane][k];
+        if (ps.ub < INFINITY) thr = fminf(thr, ps.ub * (1.0f + 1e-4f) + 1e-4f);
+        if (!(ps.key <= thr)) continue;
+        if (nc == CAND) {  // full: drop candidates the bound has since excluded
+          int wr = 0;
+          for (int q2 = 0; q2 < CAND; ++q2)
+            if (W.cand[w][lane][q2].key <= thr) W.cand[w][lane][wr++] = W.cand[w][lane][q2];
+          nc = wr;
+        }
+        if (nc < CAND) W.cand[w][lane][nc++] = ps;
+        else overflow = true;
+      }
+      __syncwarp();
+    }
+    if (idx < n_in) {
+      ScanRec sc;
+      sc.nc = 0;
+      sc.overflow = overflow ? 1 : 0;
+      sc.leaf = -1;
+      sc.face = -1;
+      sc.t32 = 0.0f;
+      sc.s32 = 0.0f;
       sc.thr = thr;
-      if (nc == 1 && first.key == first.ub && first.leaf >= 0) {
-        // a single candidate whose nearest root is certain: only that root is refined
-        const uint32_t oinfo = reinterpret_cast<const uint32_t*>(&objs[sc.cand[0]])[3];
-        const int kind = leaf_kind_of(oinfo, first.leaf);
-        sc.leaf = (int8_t)first.leaf;
-        sc.face = (int8_t)first.face;
-        sc.t32 = first.ub;
-        sc.s32 = first.s;
-        list = kind == LEAF_CIRCLE ? LIST_REFINE_CIRCLE : kind == LEAF_RECT ? LIST_REFINE_RECT
-             : kind == LEAF_SEGMENT ? LIST_REFINE_SEGMENT : LIST_REFINE_CUBIC;
-      } else if (nc > 0) {
-        list = LIST_FULL;
+      int list = -1;
+      if (dead) {
+        sc.nc = NC_DEAD;
+      } else {
+        int m = 0;
+        PairSlot first;
+        first.key = INFINITY;
+        for (int k = 0; k < nc; ++k) {
+          const PairSlot ps = W.cand[w][lane][k];
+          if (!(ps.key <= thr)) continue;
+          if (m == 0) first = ps;
+          sc.cand[m++] = (uint16_t)(ps.m & 0xffffu);
+        }
+        sc.nc = (uint8_t)m;
+        const int leaf = (int)((first.m >> 16) & 0xffu) - 1, face = (int)(first.m >> 24) - 1;
+        if (!overflow && m == 1 && first.key == first.ub && leaf >= 0) {
+          // a single candidate whose nearest root is certain: only that root is refined
+          const uint32_t oinfo = reinterpret_cast<const uint32_t*>(&objs[sc.cand[0]])[3];
+          const int kind = leaf_kind_of(oinfo, leaf);
+          sc.leaf = (int8_t)leaf;
+          sc.face = (int8_t)face;
+          sc.t32 = first.ub;
+          sc.s32 = first.s;
+          list = kind == LEAF_CIRCLE ? LIST_REFINE_CIRCLE : kind == LEAF_RECT ? LIST_REFINE_RECT
+               : kind == LEAF_SEGMENT ? LIST_REFINE_SEGMENT : LIST_REFINE_CUBIC;
+        } else if (m > 0 || overflow) {
+          list = LIST_FULL;
+        }
       }
+      B.scan[idx] = sc;
+      list_append(B, gen, list, (uint32_t)idx);
     }
-    B.scan[idx] = sc;
-    list_append(B, gen, list, (uint32_t)idx);
   }
 }
 
