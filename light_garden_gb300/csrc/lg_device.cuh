@@ -121,8 +121,11 @@ constexpr float DF_ROUND = 2e-14f;  // double-float rounding per bounce, relativ
 
 // work lists of one generation (k_scan appends, k_refine / k_full consume)
 enum : int {
-  LIST_REFINE_CIRCLE = 0, LIST_REFINE_RECT = 1, LIST_REFINE_SEGMENT = 2, LIST_REFINE_CUBIC = 3, LIST_FULL = 4, N_LISTS = 5
+  LIST_REFINE_CIRCLE = 0, LIST_REFINE_RECT = 1, LIST_REFINE_SEGMENT = 2, LIST_REFINE_CUBIC = 3, LIST_FULL = 4,
+  LIST_EXIT = 5,  // no object hit and the canvas exit needs the precise path (origin outside, corner)
+  N_LISTS = 6
 };
+constexpr int8_t LEAF_REFINE_FAILED = -2;  // ScanRec::leaf after k_refine handed the ray to k_full
 
 struct Counters {
   unsigned long long seg_count;               // ring cursor (= segments demanded)

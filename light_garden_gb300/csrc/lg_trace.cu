@@ -175,6 +175,55 @@ __device__ __forceinline__ void list_append(const TraceBufs& B, uint32_t gen, in
   if (slot < B.queue_cap) B.list[list][slot] = idx;
 }
 
+// Canvas exit of a ray that hits no object, when its origin is clearly inside the canvas
+// and the exit is clearly not at a corner: the exit face is found in FP32, the exit point
+// computed in double-float.  Anything else takes the precise path in k_bounce.
+__device__ __forceinline__ bool fast_canvas_exit(const SceneDev& S, const RayRec& r, float& x1, float& y1, float& L) {
+  const float ax = S.aspect.hi, ox = r.ox.hi, oy = r.oy.hi, dx = r.dx.hi, dy = r.dy.hi;
+  if (!(fabsf(ox) < ax - 1e-4f && fabsf(oy) < 1.0f - 1e-4f)) return false;
+  const float tx = dx > 0.0f ? (ax - ox) / dx : dx < 0.0f ? (-ax - ox) / dx : INFINITY;
+  const float ty = dy > 0.0f ? (1.0f - oy) / dy : dy < 0.0f ? (-1.0f - oy) / dy : INFINITY;
+  if (!(fabsf(tx - ty) > 1e-4f * (fminf(tx, ty) + 1.0f))) return false;
+  df t;
+  if (tx < ty) {
+    const df bound = dx > 0.0f ? S.aspect : -S.aspect;
+    t = (bound - r.ox) / r.dx;
+  } else {
+    const df bound = dy > 0.0f ? DF_ONE : -DF_ONE;
+    t = (bound - r.oy) / r.dy;
+  }
+  x1 = (r.ox + r.dx * t).hi;
+  y1 = (r.oy + r.dy * t).hi;
+  L = r.ex + t.hi * r.ea;
+  return true;
+}
+
+// appends one segment per emitting lane with one atomic per warp (all lanes call)
+__device__ __forceinline__ void emit_segments(const SceneDev& S, const TraceBufs& B, bool emit, const RayRec& r,
+                                              float x1, float y1, uint8_t flags, int hit, uint32_t gen,
+                                              unsigned long long& my_near) {
+  const unsigned lane = lane_id();
+  const unsigned emask = __ballot_sync(0xffffffffu, emit);
+  if (!emask) return;
+  unsigned long long sbase = 0;
+  const int leader = __ffs(emask) - 1;
+  if ((int)lane == leader) sbase = atomicAdd(&B.ctr->seg_count, (unsigned long long)__popc(emask));
+  sbase = __shfl_sync(0xffffffffu, sbase, leader);
+  if (!emit) return;
+  const unsigned long long slot = sbase + __popc(emask & lanemask_lt());
+  if (flags & LG_PATH_NEAR_DEGENERATE) ++my_near;
+  if (slot >= B.seg_cap) return;
+  float4* dst = reinterpret_cast<float4*>(B.segs + slot);
+  dst[0] = make_float4(r.ox.hi, r.oy.hi, x1, y1);
+  dst[1] = make_float4(r.c[0], r.c[1], r.c[2], r.c[3]);
+  if (S.record_paths) {
+    lg_path_record pr;
+    pr.path = r.path; pr.primary = r.prim; pr.light = r.light; pr.gen = (uint8_t)gen;
+    pr.flags = flags; pr.hit = hit; pr.source = LG_SRC_TRACE;
+    B.paths[slot] = pr;
+  }
+}
+
 // Warp-cooperative FP32 scan.  Objects are taken in chunks of SCAN_CHUNK: every lane
 // bounding-tests its own ray against the chunk (pruned by its running bound thr) and
 // writes the passing (ray, object) pairs to the warp's shared buffer; then all 32 lanes
@@ -190,9 +239,9 @@ struct __align__(16) PairSlot {
   uint32_t m;  // object | (leaf + 1) << 16 | (face + 1) << 24; before classification key holds lb
 };
 
-struct ScanSmem {
-  PairSlot pairs[SCAN_WARPS][32][SCAN_CHUNK];
-  PairSlot cand[SCAN_WARPS][32][CAND];
+struct ScanSmem {  // [slot][lane]: a warp's 32 lanes touch 32 consecutive slots
+  PairSlot pairs[SCAN_WARPS][SCAN_CHUNK][32];
+  PairSlot cand[SCAN_WARPS][CAND][32];
   float4 ray[SCAN_WARPS][32];
   uint32_t src[SCAN_WARPS][32];
   int off[SCAN_WARPS][33];
@@ -200,11 +249,14 @@ struct ScanSmem {
 
 int scan_smem_bytes() { return (int)sizeof(ScanSmem); }
 
-__global__ void __launch_bounds__(SCAN_WARPS * 32) k_scan(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
+__global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
   ScanSmem& W = *reinterpret_cast<ScanSmem*>(smem_raw);
   ObjScan* sobj = reinterpret_cast<ObjScan*>(smem_raw + sizeof(ScanSmem));
+  __shared__ unsigned long long blk_visits, blk_near;
+  if (threadIdx.x == 0) { blk_visits = 0; blk_near = 0; }
+  unsigned long long my_visits = 0, my_near = 0;
   bool failed;
   const ObjScan* objs = stage_objects(S, sobj, &bar, smem_fits != 0, B.ctr, failed);
   if (failed) return;
@@ -264,7 +316,7 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32) k_scan(SceneDev S, TraceBufs 
           ps.ub = 0.0f;
           ps.s = 0.0f;
           ps.m = j0 + jj;
-          W.pairs[w][lane][cnt++] = ps;
+          W.pairs[w][cnt++][lane] = ps;
         }
       }
       // flatten the warp's pairs: exclusive scan of the per-lane counts
@@ -285,7 +337,7 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32) k_scan(SceneDev S, TraceBufs 
           if (W.off[w][mid] <= p) lo = mid; else hi = mid;
         }
         const int k = p - W.off[w][lo];
-        PairSlot& ps = W.pairs[w][lo][k];
+        PairSlot& ps = W.pairs[w][k][lo];
         const uint32_t j = ps.m;
         const float4 rr = W.ray[w][lo];
         const uint32_t src = W.src[w][lo];
@@ -300,20 +352,23 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32) k_scan(SceneDev S, TraceBufs 
       __syncwarp();
       // fold this lane's results in object order
       for (int k = 0; k < cnt; ++k) {
-        const PairSlot ps = W.pairs[w][lane][k];
+        const PairSlot ps = W.pairs[w][k][lane];
         if (ps.ub < INFINITY) thr = fminf(thr, ps.ub * (1.0f + 1e-4f) + 1e-4f);
         if (!(ps.key <= thr)) continue;
         if (nc == CAND) {  // full: drop candidates the bound has since excluded
           int wr = 0;
           for (int q2 = 0; q2 < CAND; ++q2)
-            if (W.cand[w][lane][q2].key <= thr) W.cand[w][lane][wr++] = W.cand[w][lane][q2];
+            if (W.cand[w][q2][lane].key <= thr) W.cand[w][wr++][lane] = W.cand[w][q2][lane];
           nc = wr;
         }
-        if (nc < CAND) W.cand[w][lane][nc++] = ps;
+        if (nc < CAND) W.cand[w][nc++][lane] = ps;
         else overflow = true;
       }
       __syncwarp();
     }
+    bool emit = false;
+    float x1 = 0.0f, y1 = 0.0f;
+    uint8_t eflags = 0;
     if (idx < n_in) {
       ScanRec sc;
       sc.nc = 0;
@@ -331,7 +386,7 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32) k_scan(SceneDev S, TraceBufs 
         PairSlot first;
         first.key = INFINITY;
         for (int k = 0; k < nc; ++k) {
-          const PairSlot ps = W.cand[w][lane][k];
+          const PairSlot ps = W.cand[w][k][lane];
           if (!(ps.key <= thr)) continue;
           if (m == 0) first = ps;
           sc.cand[m++] = (uint16_t)(ps.m & 0xffffu);
@@ -350,11 +405,29 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32) k_scan(SceneDev S, TraceBufs 
                : kind == LEAF_SEGMENT ? LIST_REFINE_SEGMENT : LIST_REFINE_CUBIC;
         } else if (m > 0 || overflow) {
           list = LIST_FULL;
+        } else {
+          // no object can be hit: leave through the canvas (tracer.rs:482-488)
+          float L;
+          if (fast_canvas_exit(S, r, x1, y1, L)) {
+            emit = true;
+            ++my_visits;
+            eflags = r.flags | (near_cutoff(r.c, S.cutoff) || L > ILL_COND ? LG_PATH_NEAR_DEGENERATE : 0);
+          } else {
+            list = LIST_EXIT;
+          }
         }
       }
       B.scan[idx] = sc;
       list_append(B, gen, list, (uint32_t)idx);
     }
+    emit_segments(S, B, emit, r, x1, y1, eflags, -1, gen, my_near);
+  }
+  atomicAdd(&blk_visits, my_visits);
+  atomicAdd(&blk_near, my_near);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    atomicAdd(&B.ctr->visits, blk_visits);
+    atomicAdd(&B.ctr->near, blk_near);
   }
 }
 
@@ -379,6 +452,7 @@ __global__ void __launch_bounds__(256) k_refine(SceneDev S, TraceBufs B, uint32_
     if (refine_root(S, sc.cand[0], sc.leaf, sc.face, sc.t32, sc.s32, r.ox, r.oy, r.dx, r.dy, h)) {
       store_hit(B.hit[idx], sc.cand[0], h, INFINITY, 0);
     } else {  // cannot refine (degenerate): solve it fully after this kernel
+      B.scan[idx].leaf = LEAF_REFINE_FAILED;
       const unsigned long long slot = atomicAdd(&B.ctr->list_count[gen][LIST_FULL], 1ull);
       if (slot < B.queue_cap) B.list[LIST_FULL][slot] = idx;
     }
@@ -634,50 +708,40 @@ __global__ void __launch_bounds__(256) k_bounce(SceneDev S, TraceBufs B, uint32_
   bool failed;
   const ObjScan* objs = stage_objects(S, reinterpret_cast<ObjScan*>(smem_raw), &bar, smem_fits != 0, B.ctr, failed);
   if (failed) return;
-  const uint64_t n_in = n_in_of(S, B, gen) < B.queue_cap ? n_in_of(S, B, gen) : B.queue_cap;
+  // the rays with work: every work list of this generation, one after the other
+  uint64_t off[N_LISTS + 1];
+  off[0] = 0;
+  for (int l = 0; l < N_LISTS; ++l) {
+    const unsigned long long c = B.ctr->list_count[gen][l];
+    off[l + 1] = off[l] + (c < B.queue_cap ? c : B.queue_cap);
+  }
+  const uint64_t total = off[N_LISTS];
   const RayRec* qin = B.queue[gen & 1];
   RayRec* qout = B.queue[(gen + 1) & 1];
   const unsigned lane = lane_id();
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
   unsigned long long my_visits = 0, my_near = 0;
-  for (uint64_t base = warp * 32; base < n_in; base += nwarps * 32) {
-    const uint64_t idx = base + lane;
+  for (uint64_t base = warp * 32; base < total; base += nwarps * 32) {
+    const uint64_t i = base + lane;
     Bounce v;
     v.emit = false;
     v.nchild = 0;
+    v.flags = 0;
+    v.hit = -1;
     RayRec r;
-    if (idx < n_in) {
-      r = qin[idx];
+    if (i < total) {
+      int l = 0;
+      while (i >= off[l + 1]) ++l;
+      const uint32_t idx = B.list[l][i - off[l]];
       const ScanRec sc = B.scan[idx];
-      if (sc.nc != NC_DEAD) {
+      if (!(l < LIST_FULL && sc.leaf == LEAF_REFINE_FAILED)) {  // those are in the full list too
+        r = qin[idx];
         ++my_visits;
         bounce(S, objs, r, sc, &B.hit[idx], gen, v);
       }
     }
-    // segments: one atomic per warp
-    const unsigned emask = __ballot_sync(0xffffffffu, v.emit);
-    if (emask) {
-      unsigned long long sbase = 0;
-      const int leader = __ffs(emask) - 1;
-      if ((int)lane == leader) sbase = atomicAdd(&B.ctr->seg_count, (unsigned long long)__popc(emask));
-      sbase = __shfl_sync(0xffffffffu, sbase, leader);
-      if (v.emit) {
-        const unsigned long long slot = sbase + __popc(emask & lanemask_lt());
-        if (v.flags & LG_PATH_NEAR_DEGENERATE) ++my_near;
-        if (slot < B.seg_cap) {
-          float4* dst = reinterpret_cast<float4*>(B.segs + slot);
-          dst[0] = make_float4(r.ox.hi, r.oy.hi, v.x1, v.y1);
-          dst[1] = make_float4(r.c[0], r.c[1], r.c[2], r.c[3]);
-          if (S.record_paths) {
-            lg_path_record pr;
-            pr.path = r.path; pr.primary = r.prim; pr.light = r.light; pr.gen = (uint8_t)gen;
-            pr.flags = v.flags; pr.hit = v.hit; pr.source = LG_SRC_TRACE;
-            B.paths[slot] = pr;
-          }
-        }
-      }
-    }
+    emit_segments(S, B, v.emit, r, v.x1, v.y1, v.flags, v.hit, gen, my_near);
     // children: warp prefix sum of 0..2 per lane, one atomic per warp
     int incl = v.nchild;
 #pragma unroll
@@ -685,10 +749,10 @@ __global__ void __launch_bounds__(256) k_bounce(SceneDev S, TraceBufs B, uint32_
       const int y = __shfl_up_sync(0xffffffffu, incl, o);
       if ((int)lane >= o) incl += y;
     }
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
-    if (total > 0 && gen + 1 < S.max_bounce) {
+    const int tot = __shfl_sync(0xffffffffu, incl, 31);
+    if (tot > 0 && gen + 1 < S.max_bounce) {
       unsigned long long qbase = 0;
-      if (lane == 31) qbase = atomicAdd(&B.ctr->queue_count[gen + 1], (unsigned long long)total);
+      if (lane == 31) qbase = atomicAdd(&B.ctr->queue_count[gen + 1], (unsigned long long)tot);
       qbase = __shfl_sync(0xffffffffu, qbase, 31);
       const unsigned long long first = qbase + (unsigned long long)(incl - v.nchild);
       for (int q = 0; q < v.nchild; ++q)
