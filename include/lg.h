@@ -210,7 +210,8 @@ typedef struct lg_trace_stats {
 
 typedef struct lg_device_opts {
   int32_t device;             /* CUDA device ordinal */
-  uint32_t _pad;
+  int32_t raster_variant;     /* 0: autotune on the first accumulation; 1: shared-atomic tile
+                                 raster; 2: warp-private tile raster (results are identical) */
   uint64_t segment_capacity;  /* initial segment ring size (0 = automatic); grows on overflow */
   uint64_t queue_capacity;    /* initial per-generation ray queue size (0 = automatic) */
 } lg_device_opts;

@@ -105,7 +105,7 @@ class lg_trace_stats(C.Structure):
 
 
 class lg_device_opts(C.Structure):
-    _fields_ = [("device", C.c_int32), ("_pad", C.c_uint32), ("segment_capacity", C.c_uint64),
+    _fields_ = [("device", C.c_int32), ("raster_variant", C.c_int32), ("segment_capacity", C.c_uint64),
                 ("queue_capacity", C.c_uint64)]
 
 

@@ -25,7 +25,8 @@ struct DevBuf {
   size_t bytes = 0;
 };
 
-constexpr uint32_t UNIT_REFS = 1024;  // keeps the split shared-memory sums below 2^31
+constexpr uint32_t UNIT_REFS = 1024;       // shared-atomic raster: keeps the split sums below 2^31
+constexpr uint32_t UNIT_REFS_WARP = 8192;  // warp-private raster: no bound, bigger units flush less
 constexpr size_t OBJ_SMEM_MAX = 96 * 1024;
 
 }  // namespace
@@ -56,6 +57,8 @@ struct lg_ctx {
   uint32_t n_tiles = 0, ntx = 0, nty = 0;
   // launch shapes
   int trace_grid[4] = {0, 0, 0, 0}, raster_grid = 0, bin_grid = 0;  // scan, refine, full, bounce
+  int raster_warp_grid = 0;
+  int raster_variant = 0;  // 1 shared-atomic tile raster, 2 warp-private tile raster; 0 = not tuned yet
   size_t obj_smem = 0;
   int smem_fits = 0;
   // graph
@@ -381,7 +384,7 @@ RasterArgs raster_args(lg_ctx* c) {
   A.ntx = c->ntx;
   A.nty = c->nty;
   A.n_tiles = 2 * c->n_tiles;  // bins: x-major and y-major segments of each tile
-  A.unit_refs = UNIT_REFS;
+  A.unit_refs = c->raster_variant == 2 ? UNIT_REFS_WARP : UNIT_REFS;
   for (int ch = 0; ch < 4; ++ch) {
     const lg_blend_component& b = ch < 3 ? c->prm.color_blend : c->prm.alpha_blend;
     A.blend.src[ch] = b.src_factor;
@@ -488,7 +491,12 @@ lg_status enqueue_accumulate(lg_ctx* c, int binned_event = -1) {
   }
   const int mode = raster_mode(c->prm);
   const size_t rsm = (size_t)raster_smem_bytes(mode);
-  if (mode == RM_FIXED_SPLIT_)
+  if (c->raster_variant == 2) {
+    if (mode == RM_F32_)
+      k_raster_warp<RM_F32_><<<c->raster_warp_grid, 32, raster_warp_smem_bytes(), c->stream>>>(A);
+    else
+      k_raster_warp<RM_FIXED_SPLIT_><<<c->raster_warp_grid, 32, raster_warp_smem_bytes(), c->stream>>>(A);
+  } else if (mode == RM_FIXED_SPLIT_)
     k_raster<RM_FIXED_SPLIT_><<<c->raster_grid, 256, rsm, c->stream>>>(A);
   else if (mode == RM_FIXED_MINMAX_)
     k_raster<RM_FIXED_MINMAX_><<<c->raster_grid, 256, rsm, c->stream>>>(A);
@@ -569,7 +577,37 @@ lg_status run_trace_once(lg_ctx* c, uint32_t& retries) {
   return fail(c, LG_ERR_OUT_OF_MEMORY, "segment ring / ray queue kept overflowing");
 }
 
+lg_status run_accumulate_once(lg_ctx* c, uint32_t& retries);
+
+// Autotuner: the first accumulation of a context runs both tile-raster kernels (each a
+// complete, identical accumulation) and keeps the faster for every later launch and graph.
+lg_status tune_raster(lg_ctx* c, uint32_t& retries) {
+  float best = INFINITY;
+  int pick = 1;
+  for (int v = 1; v <= 2; ++v) {
+    c->raster_variant = v;
+    CK(cudaEventRecord(c->ev[4], c->stream), "event");
+    lg_status st = run_accumulate_once(c, retries);
+    if (st) return st;
+    CK(cudaEventRecord(c->ev[5], c->stream), "event");
+    CK(cudaEventSynchronize(c->ev[5]), "event");
+    const float ms = elapsed(c->ev[4], c->ev[5]);
+    if (ms < best) { best = ms; pick = v; }
+  }
+  c->graph_valid = false;
+  if (c->raster_variant != pick) {
+    c->raster_variant = pick;
+    return run_accumulate_once(c, retries);
+  }
+  return LG_OK;
+}
+
 lg_status run_accumulate(lg_ctx* c, uint32_t& retries) {
+  if (c->raster_variant == 0) return tune_raster(c, retries);
+  return run_accumulate_once(c, retries);
+}
+
+lg_status run_accumulate_once(lg_ctx* c, uint32_t& retries) {
   for (int attempt = 0; attempt < 4; ++attempt) {
     lg_status st = enqueue_accumulate(c);
     if (st) return st;
@@ -622,6 +660,7 @@ lg_status lg_create(lg_ctx** out, const lg_device_opts* opts) {
   if (!c) return LG_ERR_OUT_OF_MEMORY;
   c->device = opts ? opts->device : 0;
   c->seg_cap_hint = opts ? opts->segment_capacity : 0;
+  c->raster_variant = opts && (opts->raster_variant == 1 || opts->raster_variant == 2) ? opts->raster_variant : 0;
   c->queue_cap_hint = opts ? opts->queue_capacity : 0;
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, c->device);
@@ -748,6 +787,10 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_raster<RM_F32_>, 256, rsm), "occupancy");
   }
   c->raster_grid = c->n_sm * std::max(1, occ);
+  CK(cudaFuncSetAttribute(k_raster_warp<RM_FIXED_SPLIT_>, cudaFuncAttributeMaxDynamicSharedMemorySize, raster_warp_smem_bytes()), "smem attr");
+  CK(cudaFuncSetAttribute(k_raster_warp<RM_F32_>, cudaFuncAttributeMaxDynamicSharedMemorySize, raster_warp_smem_bytes()), "smem attr");
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_raster_warp<RM_FIXED_SPLIT_>, 32, raster_warp_smem_bytes()), "occupancy");
+  c->raster_warp_grid = c->n_sm * std::max(1, occ);
   c->bin_grid = c->n_sm * 8;
   // capacities: first guesses, grown on overflow
   const uint64_t overlays = 3ull * F.cubics.size() + p.string_mod.modulo;
@@ -856,6 +899,10 @@ lg_status lg_render(lg_ctx* c, uint16_t* dst, size_t pitch, int32_t dst_is_devic
   const size_t row = (size_t)c->prm.width * 8;
   if (!dst || pitch < row) return fail(c, LG_ERR_INVALID_ARGUMENT, "destination null or pitch < width * 8");
   uint32_t retries = 0;
+  if (c->raster_variant == 0) {  // pick the raster kernel before it is baked into the graph
+    if ((st = run_trace(c, retries))) return st;
+    if ((st = tune_raster(c, retries))) return st;
+  }
   for (int attempt = 0; attempt < 8; ++attempt) {
     if (!c->graph_valid) {
       if (c->gexec) cudaGraphExecDestroy(c->gexec);

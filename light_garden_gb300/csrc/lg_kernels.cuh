@@ -53,6 +53,9 @@ __global__ void k_bin_scatter(RasterArgs A, int smem_tiles);
 template <int MODE>
 __global__ void k_raster(RasterArgs A);
 int raster_smem_bytes(int mode);
+template <int MODE>
+__global__ void k_raster_warp(RasterArgs A);
+int raster_warp_smem_bytes();
 constexpr int RM_FIXED_SPLIT_ = 0, RM_FIXED_MINMAX_ = 1, RM_F32_ = 2;
 constexpr uint32_t MAX_SMEM_TILES = 32768;  // tile bins (2 per tile) with 32-bit counters in 128 KB
 __global__ void k_resolve_f16(const void* accum, int fixed, uint32_t W, uint32_t H, uint16_t* dst, size_t pitch);

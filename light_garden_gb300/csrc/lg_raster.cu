@@ -256,13 +256,16 @@ template <int MODE>
 struct RasterSmem {
   static constexpr int acc_words = MODE == RM_FIXED_SPLIT ? 12 * TILE_PX : MODE == RM_FIXED_MINMAX ? 8 * TILE_PX : 4 * TILE_PX;
   static constexpr int stage_words = 8 * 32 * 16;  // 8 warps x 32 staged segments x 64 B
-  static constexpr int bytes = (acc_words + stage_words) * 4;
+  static constexpr int owner_words = 8 * 32 * 32 / 4;  // 8 warps x 1024 (segment, column) pairs, 1 B each
+  static constexpr int pref_words = 8 * 33;
+  static constexpr int bytes = (acc_words + stage_words + owner_words + pref_words) * 4;
 };
 
-// one staged segment: raster setup and per-channel source terms, 64 B
+// one staged segment: raster setup restricted to the unit's tile and the per-channel
+// source terms, 64 B
 struct __align__(16) Staged {
   float ua, va, slope;
-  int lohi;             // lo | hi << 16 (major-axis pixel range); -1: nothing to draw
+  int span;             // first tile-local major-axis pixel | count << 16
   unsigned q[12];       // FIXED_SPLIT: (c, b, a) per channel; otherwise q[0..7] = 4 x int64 or 4 x float
 };
 
@@ -273,10 +276,14 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
   long long* acc64 = reinterpret_cast<long long*>(smem_raw);
   float* accf = reinterpret_cast<float*>(smem_raw);
   Staged* stage_all = reinterpret_cast<Staged*>(smem_raw + RasterSmem<MODE>::acc_words * 4);
+  uint8_t* owner_all = reinterpret_cast<uint8_t*>(stage_all + 8 * 32);
+  int* pref_all = reinterpret_cast<int*>(owner_all + 8 * 1024);
   __shared__ unsigned long long s_unit, s_pixels;
   if (threadIdx.x == 0) s_pixels = 0;
   const unsigned lane = lane_id(), warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   Staged* stage = stage_all + warp * 32;
+  uint8_t* owner = owner_all + warp * 1024;
+  int* pref = pref_all + warp * 33;
   const BlendDev& B = A.blend;
   unsigned long long my_pixels = 0;
   unsigned long long n_units = A.ctr->units;
@@ -303,10 +310,10 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
     __syncthreads();
     const uint64_t end = min(U.begin + U.n, A.refs_cap);
     for (uint64_t base = U.begin + (uint64_t)warp * 32; base < end; base += (uint64_t)nwarps * 32) {
-      // lane-parallel: fetch 32 segments and set them up
+      // lane-parallel: fetch 32 segments, set them up and clip them to this tile
       const uint64_t r = base + lane;
       Staged st;
-      st.lohi = -1;
+      int cnt = 0;
       if (r < end) {
         const uint32_t si = A.refs[r];
         const float4* sp = reinterpret_cast<const float4*>(A.segs + si);
@@ -316,8 +323,10 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
         sg.color[0] = cc.x; sg.color[1] = cc.y; sg.color[2] = cc.z; sg.color[3] = cc.w;
         RSetup R;
         if (raster_setup(sg, A.W, A.H, R)) {
+          const int c0 = max(R.lo - tm * TILE, 0), c1 = min(R.hi - tm * TILE, TILE);
+          cnt = max(c1 - c0, 0);
           st.ua = R.ua; st.va = R.va; st.slope = R.slope;
-          st.lohi = R.lo | (R.hi << 16);
+          st.span = c0 | (cnt << 16);
 #pragma unroll
           for (int ch = 0; ch < 4; ++ch) {
             const float v = contribution(B, ch, sg.color);
@@ -339,24 +348,31 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
         }
       }
       stage[lane] = st;
+      // pack every (segment, pixel column) pair of the batch densely over the lanes
+      int incl = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((int)lane >= o) incl += y;
+      }
+      pref[lane] = incl - cnt;
+      for (int k = 0; k < cnt; ++k) owner[incl - cnt + k] = (uint8_t)lane;
+      const int total = __shfl_sync(0xffffffffu, incl, 31);
       __syncwarp();
-      const int n = (int)min((uint64_t)32, end - base);
-      const int i = tm * TILE + (int)lane;
-      for (int k = 0; k < n; ++k) {
-        const int lohi = stage[k].lohi;
-        if (lohi < 0) continue;
-        const int lo = lohi & 0xffff, hi = lohi >> 16;
-        if (i < lo || i >= hi) continue;
+      for (int pi = (int)lane; pi < total; pi += 32) {
+        const int k = owner[pi];
+        const Staged& sk = stage[k];
+        const int i = tm * TILE + (sk.span & 0xffff) + (pi - pref[k]);
         RSetup R;
-        R.ua = stage[k].ua; R.va = stage[k].va; R.slope = stage[k].slope;
+        R.ua = sk.ua; R.va = sk.va; R.slope = sk.slope;
         const int j = raster_minor(R, i);
         const int jl = j - tn * TILE;
         if (jl < 0 || jl >= TILE || j >= nmin) continue;
-        const int cell = jl * TILE + (int)lane;  // [row][col] for x-major, [col][row] for y-major
+        const int cell = jl * TILE + (i - tm * TILE);  // [row][col] for x-major, [col][row] for y-major
         if (MODE == RM_FIXED_SPLIT) {
-          const uint4 q0 = *reinterpret_cast<const uint4*>(&stage[k].q[0]);
-          const uint4 q1 = *reinterpret_cast<const uint4*>(&stage[k].q[4]);
-          const uint4 q2 = *reinterpret_cast<const uint4*>(&stage[k].q[8]);
+          const uint4 q0 = *reinterpret_cast<const uint4*>(&sk.q[0]);
+          const uint4 q1 = *reinterpret_cast<const uint4*>(&sk.q[4]);
+          const uint4 q2 = *reinterpret_cast<const uint4*>(&sk.q[8]);
           const unsigned qs[12] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
 #pragma unroll
           for (int w = 0; w < 12; ++w)
@@ -364,7 +380,7 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
         } else if (MODE == RM_FIXED_MINMAX) {
 #pragma unroll
           for (int ch = 0; ch < 4; ++ch) {
-            const long long q = (long long)(((unsigned long long)stage[k].q[2 * ch + 1] << 32) | stage[k].q[2 * ch]);
+            const long long q = (long long)(((unsigned long long)sk.q[2 * ch + 1] << 32) | sk.q[2 * ch]);
             long long* p = acc64 + ch * TILE_PX + cell;
             const int op = B.op[ch];
             if (op == LG_BO_MIN) atomicMin(p, q);
@@ -374,7 +390,7 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
         } else {
 #pragma unroll
           for (int ch = 0; ch < 4; ++ch) {
-            const float v = __uint_as_float(stage[k].q[ch]);
+            const float v = __uint_as_float(sk.q[ch]);
             float* pf = accf + ch * TILE_PX + cell;
             const int op = B.op[ch];
             if (op == LG_BO_ADD || op == LG_BO_REVERSE_SUBTRACT) atomicAdd(pf, v);
@@ -439,6 +455,144 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
   __syncthreads();
   if (threadIdx.x == 0) atomicAdd(&A.ctr->pixels, s_pixels);
 }
+
+// One warp per unit with a private tile: lane L owns pixel column L of the tile (x-major
+// units) or pixel row L (y-major units), and every segment of an x-major unit touches a
+// column at most once, so no two lanes or warps ever update the same accumulator and
+// plain 64-bit read-modify-write replaces atomics.  Units can therefore hold any number
+// of segments (fewer flushes); occupancy is bounded by the 32 KB tile per warp.
+template <int MODE>
+__global__ void __launch_bounds__(32) k_raster_warp(RasterArgs A) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  long long* acc64 = reinterpret_cast<long long*>(smem_raw);      // [ch][minor][lane]
+  float* accf = reinterpret_cast<float*>(smem_raw);
+  struct __align__(16) St {
+    float ua, va, slope;
+    int lohi;
+    long long q[4];
+  };
+  St* stage = reinterpret_cast<St*>(smem_raw + 4 * TILE_PX * 8);
+  const unsigned lane = lane_id();
+  const BlendDev& B = A.blend;
+  unsigned long long my_pixels = 0;
+  unsigned long long n_units = A.ctr->units;
+  if (n_units > A.units_cap) n_units = A.units_cap;
+  for (;;) {
+    unsigned long long u = 0;
+    if (lane == 0) u = atomicAdd(&A.ctr->unit_cursor, 1ull);
+    u = __shfl_sync(0xffffffffu, u, 0);
+    if (u >= n_units) break;
+    const Unit U = A.units[u];
+    const uint32_t tile = U.tile >> 1;
+    const bool xmajor = (U.tile & 1u) == 0;
+    const uint32_t tx = tile % A.ntx, ty = tile / A.ntx;
+    const int tm = xmajor ? (int)tx : (int)ty, tn = xmajor ? (int)ty : (int)tx;
+    const int nmin = (int)(xmajor ? A.H : A.W);
+    const int i = tm * TILE + (int)lane;
+    for (int k = (int)lane; k < 4 * TILE_PX; k += 32) {
+      if (MODE == RM_F32) accf[k] = ident32(B.op[k / TILE_PX]);
+      else acc64[k] = ident64(B.op[k / TILE_PX]);
+    }
+    __syncwarp();
+    const uint64_t end = min(U.begin + U.n, A.refs_cap);
+    for (uint64_t base = U.begin; base < end; base += 32) {
+      const uint64_t r = base + lane;
+      St st;
+      st.lohi = -1;
+      if (r < end) {
+        const uint32_t si = A.refs[r];
+        const float4* sp = reinterpret_cast<const float4*>(A.segs + si);
+        const float4 g = __ldg(sp), cc = __ldg(sp + 1);
+        lg_segment sg;
+        sg.x0 = g.x; sg.y0 = g.y; sg.x1 = g.z; sg.y1 = g.w;
+        sg.color[0] = cc.x; sg.color[1] = cc.y; sg.color[2] = cc.z; sg.color[3] = cc.w;
+        RSetup R;
+        if (raster_setup(sg, A.W, A.H, R)) {
+          st.ua = R.ua; st.va = R.va; st.slope = R.slope;
+          st.lohi = R.lo | (R.hi << 16);
+#pragma unroll
+          for (int ch = 0; ch < 4; ++ch) {
+            const float v = contribution(B, ch, sg.color);
+            if (MODE == RM_F32) {
+              st.q[ch] = (long long)__float_as_uint(B.op[ch] == LG_BO_REVERSE_SUBTRACT ? -v : v);
+            } else {
+              const long long q = to_fixed(v);
+              st.q[ch] = B.op[ch] == LG_BO_REVERSE_SUBTRACT ? -q : q;
+            }
+          }
+        }
+      }
+      stage[lane] = st;
+      __syncwarp();
+      const int n = (int)min((uint64_t)32, end - base);
+      for (int k = 0; k < n; ++k) {
+        const int lohi = stage[k].lohi;
+        if (lohi < 0 || i < (lohi & 0xffff) || i >= (lohi >> 16)) continue;
+        RSetup R;
+        R.ua = stage[k].ua; R.va = stage[k].va; R.slope = stage[k].slope;
+        const int j = raster_minor(R, i);
+        const int jl = j - tn * TILE;
+        if (jl < 0 || jl >= TILE || j >= nmin) continue;
+        const int cell = jl * TILE + (int)lane;
+#pragma unroll
+        for (int ch = 0; ch < 4; ++ch) {
+          const int op = B.op[ch];
+          const long long q = stage[k].q[ch];
+          if (MODE == RM_F32) {
+            float& a = accf[ch * TILE_PX + cell];
+            const float v = __uint_as_float((unsigned)q);
+            a = op == LG_BO_MIN ? fminf(a, v) : op == LG_BO_MAX ? fmaxf(a, v) : a + v;
+          } else {
+            long long& a = acc64[ch * TILE_PX + cell];
+            a = op == LG_BO_MIN ? min(a, q) : op == LG_BO_MAX ? max(a, q) : a + q;
+          }
+        }
+        ++my_pixels;
+      }
+      __syncwarp();
+    }
+    // flush the private tile: one global atomic per touched pixel channel
+    for (int k = (int)lane; k < TILE_PX; k += 32) {
+      const int jl = k / TILE, c = k % TILE;  // cell k = [minor][lane]
+      const uint32_t x = xmajor ? tx * TILE + c : tx * TILE + jl;
+      const uint32_t y = xmajor ? ty * TILE + jl : ty * TILE + c;
+      if (x >= A.W || y >= A.H) continue;
+      const uint64_t px = ((uint64_t)y * A.W + x) * 4;
+#pragma unroll
+      for (int ch = 0; ch < 4; ++ch) {
+        const int op = B.op[ch];
+        if (MODE == RM_F32) {
+          const float v = accf[ch * TILE_PX + k];
+          if (v == ident32(op)) continue;
+          float* g = reinterpret_cast<float*>(A.accum) + px + ch;
+          if (op == LG_BO_MIN || op == LG_BO_MAX) {
+            float o = *g;
+            while (op == LG_BO_MIN ? v < o : v > o) {
+              const float w = __int_as_float(atomicCAS(reinterpret_cast<int*>(g), __float_as_int(o), __float_as_int(v)));
+              if (w == o) break;
+              o = w;
+            }
+          } else {
+            atomicAdd(g, v);
+          }
+        } else {
+          const long long v = acc64[ch * TILE_PX + k];
+          if (v == ident64(op)) continue;
+          long long* g = reinterpret_cast<long long*>(A.accum) + px + ch;
+          if (op == LG_BO_MIN) atomicMin(g, v);
+          else if (op == LG_BO_MAX) atomicMax(g, v);
+          else atomicAdd(reinterpret_cast<unsigned long long*>(g), (unsigned long long)v);
+        }
+      }
+    }
+    __syncwarp();
+  }
+  if (my_pixels) atomicAdd(&A.ctr->pixels, my_pixels);
+}
+
+template __global__ void k_raster_warp<RM_FIXED_SPLIT>(RasterArgs A);
+template __global__ void k_raster_warp<RM_F32>(RasterArgs A);
+int raster_warp_smem_bytes() { return 4 * TILE_PX * 8 + 32 * 48; }
 
 template __global__ void k_raster<RM_FIXED_SPLIT>(RasterArgs A);
 template __global__ void k_raster<RM_FIXED_MINMAX>(RasterArgs A);

@@ -53,7 +53,10 @@ def test_csg_scene_trace_parity_subsampled(ctx, oracle):
     assert rep.matched > 0.99 * len(os_)
 
 
-def test_raster_bit_exact_on_same_segments(ctx, oracle):
+@pytest.mark.parametrize("variant", [1, 2])
+def test_raster_bit_exact_on_same_segments(gpu, oracle, variant):
+    from light_garden_gb300.runtime import Context
+    ctx = Context(raster_variant=variant)
     w = W.mid_scene(rays_per_light=1 << 12)
     pk = w.packed()
     ctx.upload(pk)
@@ -66,6 +69,7 @@ def test_raster_bit_exact_on_same_segments(ctx, oracle):
     assert np.array_equal(g_acc, o_acc)
     # resolve is bit-exact too
     assert np.array_equal(ctx.resolve_f16(), oracle.resolve_f16(o_acc))
+    ctx.close()
 
 
 def test_accumulate_segments_matches_oracle(ctx, oracle):
@@ -129,13 +133,16 @@ def test_ring_overflow_grows_and_retraces(gpu, oracle):
     assert compare(gs, gp, os_, op, o64).ok()
 
 
+@pytest.mark.parametrize("variant", [1, 2])
 @pytest.mark.parametrize("cb,ab", [
     ((abi.LG_BF_ONE, abi.LG_BF_ONE, abi.LG_BO_REVERSE_SUBTRACT), (abi.LG_BF_ONE, abi.LG_BF_ONE, abi.LG_BO_ADD)),
     ((abi.LG_BF_ONE, abi.LG_BF_ONE, abi.LG_BO_MAX), (abi.LG_BF_ONE, abi.LG_BF_ONE, abi.LG_BO_MIN)),
     ((abi.LG_BF_SRC_ALPHA, abi.LG_BF_ONE, abi.LG_BO_ADD), (abi.LG_BF_ONE_MINUS_SRC, abi.LG_BF_ONE, abi.LG_BO_ADD)),
     ((abi.LG_BF_CONSTANT, abi.LG_BF_ONE, abi.LG_BO_ADD), (abi.LG_BF_ONE_MINUS_CONSTANT, abi.LG_BF_ONE, abi.LG_BO_ADD)),
 ])
-def test_blend_modes_bit_exact(ctx, oracle, cb, ab):
+def test_blend_modes_bit_exact(gpu, oracle, cb, ab, variant):
+    from light_garden_gb300.runtime import Context
+    ctx = Context(raster_variant=variant)
     pk = W.plain_small(accum=abi.LG_ACCUM_FIXED64, num_rays=1024).packed()
     pk.params.color_blend = abi.lg_blend_component(*cb)
     pk.params.alpha_blend = abi.lg_blend_component(*ab)
@@ -146,6 +153,7 @@ def test_blend_modes_bit_exact(ctx, oracle, cb, ab):
     ctx.accumulate()
     o_acc, _ = oracle.raster(segs, pk.params)
     assert np.array_equal(ctx.accum(), o_acc)
+    ctx.close()
 
 
 def test_overlays_match_oracle(ctx, oracle):
