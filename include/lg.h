@@ -268,6 +268,23 @@ lg_status lg_segments_download(lg_ctx* ctx, lg_segment* out, lg_path_record* pat
 /* Copies the raw accumulation image: width*height*4 values, int64 (FIXED64) or float (F32). */
 lg_status lg_accum_download(lg_ctx* ctx, void* out, uint64_t cap_bytes);
 
+/* No counterpart in the reference.  For callers that may not allocate device memory
+ * (plug-ins whose host owns every allocation, real-time loops that must not take the
+ * allocator's locks or risk the implicit synchronisation of cudaMalloc / cudaFree, code
+ * under a fixed memory budget): clears `accum` to params->clear_color and rasterises the
+ * n segments into it exactly like lg_accumulate_segments, on the calling thread's current
+ * device and the given stream (NULL = default stream), without a context and without
+ * allocating.  `segments` and `accum` must be device-accessible (accum: width*height*4
+ * int64 for LG_ACCUM_FIXED64, float for LG_ACCUM_F32).  Binning scratch lives in one
+ * 32 MiB array per device, resident until the process exits; limits per call: at most
+ * 4096 tiles of 32x32 pixels (e.g. 2048x2048) and 8,000,000 (segment, tile) pairs, else
+ * LG_ERR_BUDGET (and the image is not valid).  The first call on a device sets the array
+ * up; make it before any stream capture.  Calls share the array, so calls that overlap on
+ * the GPU race: serialise them.  Returns after the work completed; *pixels_out (optional)
+ * receives the number of pixel updates. */
+lg_status lg_accumulate_segments_noalloc(const lg_segment* segments, uint64_t n, const lg_params* params,
+                                         void* accum, void* stream, uint64_t* pixels_out);
+
 #ifdef __cplusplus
 }
 #endif

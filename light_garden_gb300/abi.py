@@ -161,6 +161,8 @@ EXPORTS = [
     ("lg_segments_download", C.c_int, [C.c_void_p, C.POINTER(lg_segment), C.POINTER(lg_path_record),
                                        C.c_uint64, C.POINTER(C.c_uint64)]),
     ("lg_accum_download", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    ("lg_accumulate_segments_noalloc", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(lg_params), C.c_void_p,
+                                                 C.c_void_p, C.POINTER(C.c_uint64)]),
 ]
 
 
