@@ -29,6 +29,10 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "traced segments/s + accumulated px/s on 1 GB300; p50/p99 scene latency vs plain"
+# DRAM bytes (read + write) per accumulated pixel of k_raster, measured with ncu on the
+# quarter-size mid scene (profiles/k_raster_mid_scene.md)
+RASTER_DRAM_BYTES_PER_PIXEL = 2.63
+
 WORKLOAD = ("mid_scene: 64 objects (rect/circle/mirror/curved mirror, seed 2), 8 lights x 2^18 rays, "
             "16 bounces, 1920x1080, int64 Q31.32 accumulation, RGBA16F resolve")
 
@@ -123,6 +127,13 @@ def allmax(ws, v: float, device) -> float:
     return float(t.item())
 
 
+def aggregate(ws: int, units: int, ms: float, device) -> tuple:
+    """Whole-job throughput of ``ws`` replicas that each processed ``units`` in ``ms``:
+    the slowest rank's time bounds the job (max over ranks)."""
+    ms_max = allmax(ws, ms, device)
+    return ws * units / (ms_max * 1e-3), ms_max
+
+
 def cpu_sample(stride: int):
     """Oracle (CPU restatement of tracer.rs) on a bounded sample: trace + raster."""
     from light_garden_gb300 import workloads as W
@@ -208,8 +219,7 @@ def run_ours(args, ws, rank, local):
     torch.cuda.synchronize()
     barrier(ws)
     ms = stage["total_ms"] / args.steps
-    ms_max = allmax(ws, ms, dev)
-    value = ws * segs / (ms_max * 1e-3)
+    value, ms_max = aggregate(ws, segs, ms, dev)
     px_per_s = ws * pixels / (ms_max * 1e-3)
     avg = {k: v / args.steps for k, v in stage.items()}
 
@@ -228,24 +238,26 @@ def run_ours(args, ws, rank, local):
         ctx.upload(pk)
         st = ctx.render_into(out_host.data_ptr(), pitch, False)
         e2e_times.append(time.perf_counter() - t0)
-    e2e_s = allmax(ws, statistics.mean(e2e_times), dev)
-    e2e_value = ws * st["segments"] / e2e_s
+    e2e_value, e2e_ms = aggregate(ws, st["segments"], statistics.mean(e2e_times) * 1e3, dev)
+    e2e_s = e2e_ms * 1e-3
 
-    # roofline of the dominant stage
+    # Roofline of the dominant kernel.  k_raster (one launch per frame) is the longest
+    # single kernel; the trace is 7 kernels per generation.  Algorithmic bytes per
+    # accumulated pixel: an int64 RGBA read-modify-write, 32 B read + 32 B written.  The
+    # launch is timed live by CUDA events recorded in the captured graph around it.
+    # DRAM traffic per accumulated pixel comes from the ncu capture summarised in
+    # profiles/k_raster_mid_scene.md (a quarter-size case; traffic scales with pixels).
     hbm, peak_kind = peaks()
-    dom = max(("trace_ms", "bin_ms", "raster_ms"), key=lambda k: avg[k])
-    if dom == "raster_ms":
-        alg = 64.0 * pixels  # int64 RGBA read-modify-write per accumulated pixel
-        kern = "k_raster<true> (tile accumulation)"
-    elif dom == "bin_ms":
-        alg = 2 * 32.0 * segs + 8.0 * refs
-        kern = "k_bin_count + k_bin_scatter"
-    else:
-        alg = 80.0 * visits + 80.0 * visits + 32.0 * segs
-        kern = "k_trace_gen (all generations)"
-    achieved = alg / (avg[dom] * 1e-3) / 1e9
-    roof = {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": achieved / hbm, "traffic": None, "peak_source": peak_kind}
+    alg = 64.0 * pixels
+    achieved = alg / (avg["raster_ms"] * 1e-3) / 1e9
+    traffic = RASTER_DRAM_BYTES_PER_PIXEL * pixels
+    roof = {"bound": "hbm", "kernel": "k_raster<0> (tile accumulation, shared-memory atomics)",
+            "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
+            "peak_source": peak_kind, "algorithmic_bytes": alg,
+            "note": "the read-modify-write runs in shared memory; DRAM traffic is the segment and reference "
+                    "reads plus one flush per tile unit"}
+    trace_fp32 = {"kernel": "k_scan/k_refine/k_full/k_bounce (trace, all generations)", "ms": avg["trace_ms"],
+                  "ray_visits": visits, "ns_per_visit": avg["trace_ms"] * 1e6 / max(1, visits)}
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -266,6 +278,7 @@ def run_ours(args, ws, rank, local):
             "ray_visits_per_step": visits, "fp64_solves_per_step": solves,
             "stage_ms": avg,
             "roofline": roof,
+            "trace": trace_fp32,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "segments/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": e2e_s * 1e3},

@@ -211,6 +211,8 @@ def _emit_geo(g: Geo, nodes: list) -> int:
 
 
 def pack_light(light) -> abi.lg_light:
+    if not isinstance(light, (PointLight, SpotLight, DirectionalLight)):
+        raise TypeError(f"unsupported light {type(light).__name__}")
     rec = abi.lg_light()
     rec.num_rays = int(light.num_rays)
     rec.color[:] = tuple(float(c) for c in light.color)
@@ -226,8 +228,6 @@ def pack_light(light) -> abi.lg_light:
         rec.kind = abi.LG_LIGHT_DIRECTIONAL
         rec.origin[:] = light.start.a
         rec.v[:] = light.start.b
-    else:
-        raise TypeError(f"unsupported light {type(light).__name__}")
     return rec
 
 

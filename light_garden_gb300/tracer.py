@@ -36,8 +36,8 @@ class Tracer:
         self.color_blend = (abi.LG_BF_ONE, abi.LG_BF_ONE, abi.LG_BO_ADD)
         self.alpha_blend = (abi.LG_BF_SRC_ALPHA, abi.LG_BF_ONE, abi.LG_BO_ADD)
         self.trace_time_vd: List[float] = []
-        self._ctx = Context(device)
-        self._uploaded = None
+        self.device = device
+        self._ctx: Optional[Context] = None  # created by the first GPU call
 
     # -- object / light list (tracer.rs:48-129) ---------------------------------------------
     def clear_objects(self) -> None:
@@ -95,9 +95,14 @@ class Tracer:
         p.emit_control_lines = 1 if self.emit_control_lines else 0
         return p
 
+    def packed(self):
+        """The scene as the C ABI's tables (what ``lg_scene_upload`` receives)."""
+        return pack(self.objects, self.lights, self.params())
+
     def _sync(self) -> None:
-        packed = pack(self.objects, self.lights, self.params())
-        self._ctx.upload(packed)
+        if self._ctx is None:
+            self._ctx = Context(self.device)
+        self._ctx.upload(self.packed())
 
     def trace_all_array(self) -> np.ndarray:
         """All segments of one frame as a structured array (x0, y0, x1, y1, color[4])."""
@@ -126,4 +131,6 @@ class Tracer:
         return img
 
     def close(self) -> None:
-        self._ctx.close()
+        if self._ctx is not None:
+            self._ctx.close()
+            self._ctx = None

@@ -1,0 +1,156 @@
+"""The C ABI without a GPU: struct layouts against the C compiler, the exported symbols of
+liblightgarden_cuda.so against every function ``include/lg.h`` declares, and the calls whose
+behaviour is defined before any device work (argument checks, defaults, version)."""
+import ctypes as C
+import json
+import re
+import subprocess
+
+import pytest
+
+from light_garden_gb300 import abi
+
+HEADER = abi.LIB_DIR.parent.parent / "include" / "lg.h"
+
+STRUCTS = [abi.lg_geo, abi.lg_object, abi.lg_light, abi.lg_blend_component, abi.lg_string_mod, abi.lg_params,
+           abi.lg_segment, abi.lg_path_record, abi.lg_trace_stats, abi.lg_device_opts]
+
+
+def declared_functions():
+    """Names of the functions declared in lg.h (prototypes at file scope)."""
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\*?\s*(lg_[a-z0-9_]+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def c_layout(tmp_path_factory):
+    """sizeof / offsetof of every struct field as the C compiler lays it out."""
+    d = tmp_path_factory.mktemp("abi")
+    lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', 'int main(void) {',
+             'printf("{");']
+    first = True
+    for s in STRUCTS:
+        name = s.__name__
+        items = [f'"\\"{name}\\": %zu"', ] + [f'"\\"{name}.{f}\\": %zu"' for f, *_ in s._fields_]
+        args = [f"sizeof({name})"] + [f"offsetof({name}, {f})" for f, *_ in s._fields_]
+        for it, a in zip(items, args):
+            sep = "" if first else ", "
+            first = False
+            lines.append(f'printf("{sep}" {it}, {a});')
+    lines += ['printf("}\\n");', "return 0; }"]
+    src = d / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = d / "layout"
+    subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", "-o", str(exe), str(src)], check=True)
+    return json.loads(subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout)
+
+
+def test_header_compiles_as_c_and_cxx(tmp_path):
+    for cc, ext in (("gcc", "c"), ("g++", "cpp")):
+        src = tmp_path / f"h.{ext}"
+        src.write_text(f'#include "{HEADER}"\nint main(void) {{ return LG_ABI_VERSION == 1 ? 0 : 1; }}\n')
+        subprocess.run([cc, "-Wall", "-Werror", "-pedantic", "-o", str(tmp_path / f"h_{ext}"), str(src)],
+                       check=True)
+
+
+@pytest.mark.parametrize("struct", STRUCTS, ids=lambda s: s.__name__)
+def test_struct_layout_matches_c(struct, c_layout):
+    name = struct.__name__
+    assert C.sizeof(struct) == c_layout[name], f"sizeof({name})"
+    for f, *_ in struct._fields_:
+        assert getattr(struct, f).offset == c_layout[f"{name}.{f}"], f"offsetof({name}, {f})"
+
+
+def test_record_sizes_are_the_documented_ones():
+    # one segment = 4 f32 endpoints + RGBA f32 (the reference's vertex pair, sub_render_pass.rs:188-203)
+    assert C.sizeof(abi.lg_segment) == 32
+    assert C.sizeof(abi.lg_path_record) == 24
+    assert abi.segment_dtype().itemsize == 32 and abi.path_dtype().itemsize == 24
+
+
+def test_every_declared_function_is_exported(cuda_lib):
+    names = declared_functions()
+    assert len(names) >= 15, names
+    bound = {n for n, *_ in abi.EXPORTS}
+    assert set(names) == bound, f"header vs bindings: {set(names) ^ bound}"
+    out = subprocess.run(["nm", "-D", "--defined-only", str(abi.LIB_PATH)], check=True, capture_output=True,
+                         text=True).stdout
+    exported = {l.split()[-1] for l in out.splitlines() if l.strip()}
+    missing = [n for n in names if n not in exported]
+    assert not missing, missing
+    for n in names:
+        assert getattr(cuda_lib, n) is not None
+
+
+def test_library_exports_only_the_abi(cuda_lib):
+    """No stray C++ or CUDA runtime symbols leak into the dynamic symbol table as lg_*."""
+    out = subprocess.run(["nm", "-D", "--defined-only", str(abi.LIB_PATH)], check=True, capture_output=True,
+                         text=True).stdout
+    lg = sorted(l.split()[-1] for l in out.splitlines() if l.split()[-1].startswith("lg_"))
+    assert lg == declared_functions()
+
+
+def test_abi_version_and_defaults(cuda_lib):
+    assert cuda_lib.lg_abi_version() == 1
+    p = abi.lg_params()
+    cuda_lib.lg_params_default(C.byref(p))
+    assert p.max_bounce == 5  # Tracer::new, tracer.rs:37
+    assert list(p.cutoff_color) == pytest.approx([0.001] * 4)  # tracer.rs:38
+    assert (p.width, p.height) == (512, 512)
+    assert list(p.clear_color) == [0.0, 0.0, 0.0, 1.0]
+    assert (p.color_blend.src_factor, p.color_blend.dst_factor, p.color_blend.op) == (
+        abi.LG_BF_ONE, abi.LG_BF_ONE, abi.LG_BO_ADD)  # mod.rs:67-71
+    assert (p.alpha_blend.src_factor, p.alpha_blend.dst_factor, p.alpha_blend.op) == (
+        abi.LG_BF_SRC_ALPHA, abi.LG_BF_ONE, abi.LG_BO_ADD)
+    assert p.accum == abi.LG_ACCUM_FIXED64
+    # the Python mirror builds the same defaults
+    q = abi.params_default()
+    assert bytes(q) == bytes(p)
+    cuda_lib.lg_params_default(None)  # tolerated
+
+
+def test_null_context_is_an_argument_error(cuda_lib):
+    L = cuda_lib
+    s = abi.lg_trace_stats()
+    assert L.lg_create(None, None) == abi.LG_ERR_INVALID_ARGUMENT
+    assert L.lg_trace(None, C.byref(s)) == abi.LG_ERR_INVALID_ARGUMENT
+    assert L.lg_accumulate(None, C.byref(s)) == abi.LG_ERR_INVALID_ARGUMENT
+    assert L.lg_accumulate_segments(None, None, 0, None) == abi.LG_ERR_INVALID_ARGUMENT
+    assert L.lg_resolve_f16(None, None, 0, 0) == abi.LG_ERR_INVALID_ARGUMENT
+    assert L.lg_resolve_rgba8(None, None, 0, 0) == abi.LG_ERR_INVALID_ARGUMENT
+    assert L.lg_render(None, None, 0, 0, None) == abi.LG_ERR_INVALID_ARGUMENT
+    assert L.lg_segments_download(None, None, None, 0, None) == abi.LG_ERR_INVALID_ARGUMENT
+    assert L.lg_accum_download(None, None, 0) == abi.LG_ERR_INVALID_ARGUMENT
+    assert L.lg_scene_upload(None, None, 0, None, 0, None, 0, None) == abi.LG_ERR_INVALID_ARGUMENT
+    assert L.lg_last_error(None) == b"null context"
+    assert L.lg_destroy(None) in (abi.LG_OK, abi.LG_ERR_INVALID_ARGUMENT)
+
+
+def test_noalloc_argument_checks_precede_device_work(cuda_lib):
+    p = abi.params_default()
+    n = C.c_uint64(123)
+    assert cuda_lib.lg_accumulate_segments_noalloc(None, 5, C.byref(p), None, None, C.byref(n)) == \
+        abi.LG_ERR_INVALID_ARGUMENT
+    assert cuda_lib.lg_accumulate_segments_noalloc(None, 0, None, None, None, None) == abi.LG_ERR_INVALID_ARGUMENT
+
+
+def test_create_without_a_gpu_fails_cleanly(cuda_lib):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = C.c_void_p(1)
+    st = cuda_lib.lg_create(C.byref(h), None)
+    assert st == abi.LG_ERR_CUDA
+    assert not h.value
+
+
+def test_python_context_has_no_cpu_fallback(monkeypatch, tmp_path):
+    """Without the built library the product path raises instead of computing elsewhere."""
+    monkeypatch.setattr(abi, "LIB_PATH", tmp_path / "missing.so")
+    monkeypatch.setattr(abi, "_lib", None)
+    from light_garden_gb300.runtime import Context
+    with pytest.raises(RuntimeError, match="missing"):
+        Context()
