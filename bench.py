@@ -189,10 +189,10 @@ def run_ours(args, ws, rank, local):
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    w = W.mid_scene()
+    w = W.mid_scene(rays_per_light=args.rays_per_light)
     pk = w.packed()
     Wd, Hd = pk.params.width, pk.params.height
-    ctx = Context(device=local)
+    ctx = Context(device=local, raster_variant=args.raster_variant)
     ctx.upload(pk)
     out_dev = torch.empty((Hd, Wd * 4), dtype=torch.int16, device=dev)
     out_host = torch.empty((Hd, Wd * 4), dtype=torch.int16, pin_memory=True)
@@ -271,7 +271,9 @@ def run_ours(args, ws, rank, local):
             "metric": METRIC, "value": value, "unit": "segments/s", "n_gpus": ws, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp64+fp32 trace, int64 accumulate", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "l2": "flushed between steps (512 MB write); working set > L2",
+            "config": {"workload": WORKLOAD if args.rays_per_light == 1 << 18 else
+                       WORKLOAD.replace("2^18 rays", f"{args.rays_per_light} rays"),
+                       "l2": "flushed between steps (512 MB write); working set > L2",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
             "px_per_s": px_per_s,
             "segments_per_step": segs, "pixels_per_step": pixels, "tile_refs_per_step": refs,
@@ -295,8 +297,12 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-stride", type=int, default=64)
+    ap.add_argument("--cpu-stride", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    # smaller cases of the same workload for profiler captures (the reported line uses the defaults)
+    ap.add_argument("--rays-per-light", type=int, default=1 << 18)
+    ap.add_argument("--raster-variant", type=int, default=0, choices=[0, 1, 2],
+                    help="0: autotuned; 1: shared-memory tile atomics; 2: warp-private tiles")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":

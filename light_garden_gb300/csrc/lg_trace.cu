@@ -1,15 +1,17 @@
-// lg_trace.cu — ray generation and the per-generation trace kernel (sm_103a).
+// lg_trace.cu — ray generation and the per-generation trace kernels (sm_103a).
 //
 // Tracer::trace (src/light_garden/tracer.rs:360-493) walks a breadth-first ray tree per
-// primary ray.  Here every generation is one persistent kernel over a device queue of
-// all live rays of all lights (the wavefront), so warps stay full no matter how the
-// trees branch:
+// primary ray.  Here each generation of all trees of all lights is one device queue (a
+// wavefront), processed by a short chain of kernels so that warps stay full no matter how
+// the trees branch:
 //   gen 0 reads a virtual queue (light, ray index) and generates the primary ray
 //   (light.rs:103-115, 163-174, 225-249); gen g > 0 reads the queue written by gen g-1.
 //   For each ray: cutoff (tracer.rs:378-384), nearest hit (412-424), medium (428-442),
 //   refract / reflect with colour split (444-481) or canvas exit (482-488).
-//   Segments are appended to the ring and children to the next queue with one atomic
-//   per warp (ballot + popc compaction).
+//   Segments are appended to the segment ring and children to the next queue with one
+//   atomic per warp (ballot + popc compaction).
+// The chain per generation (k_scan, k_refine x 4 leaf kinds, k_full, k_bounce) is
+// described above k_scan below.
 #include "lg_kernels.cuh"
 
 namespace lgd {
