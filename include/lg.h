@@ -268,6 +268,36 @@ lg_status lg_segments_download(lg_ctx* ctx, lg_segment* out, lg_path_record* pat
 /* Copies the raw accumulation image: width*height*4 values, int64 (FIXED64) or float (F32). */
 lg_status lg_accum_download(lg_ctx* ctx, void* out, uint64_t cap_bytes);
 
+/* ---- batches: many scenes in one trace ----------------------------------------------- *
+ * No counterpart in the reference, which traces one scene per Tracer (tracer.rs:276-358).
+ * A batch concatenates the scenes' tables and traces all rays of all scenes together, one
+ * wavefront per generation, accumulating each generation into the scenes' own images. */
+typedef struct lg_scene_desc {
+  const lg_geo* geos;
+  const lg_object* objects;
+  const lg_light* lights;
+  const lg_params* params;
+  uint32_t n_geo, n_objects, n_lights, _pad;
+} lg_scene_desc;
+
+/* Uploads k scenes (replacing the context's scene or batch; lg_trace / lg_render then need
+ * lg_scene_upload again).  Scenes may differ in objects, lights, canvas size, max_bounce and
+ * cutoff; they must share the accum mode, blend state, blend constant and clear colour, and
+ * may not use the string-mod overlay (LG_ERR_UNSUPPORTED).  At most 65535 scenes, 65535
+ * objects per scene and 65535 lights in all. */
+lg_status lg_batch_upload(lg_ctx* ctx, const lg_scene_desc* scenes, uint32_t k);
+
+/* Traces, accumulates and resolves every scene of the batch (one captured CUDA graph).
+ * dst receives the RGBA16F images one after another in scene order, each width*height*4
+ * binary16 values with rows top-down and no padding; dst_bytes >= 8 * sum(width*height).
+ * Each image is bit-identical to lg_render of that scene alone.  The first call of a
+ * context also picks the faster tile-raster kernel for the batch (autotune). */
+lg_status lg_batch_render(lg_ctx* ctx, uint16_t* dst, uint64_t dst_bytes, int32_t dst_is_device,
+                          lg_trace_stats* stats_or_null);
+
+/* First pixel of scene `scene`'s image in lg_batch_render's output (in pixels, 4 values each). */
+lg_status lg_batch_image_offset(const lg_ctx* ctx, uint32_t scene, uint64_t* px_offset);
+
 /* No counterpart in the reference.  For callers that may not allocate device memory
  * (plug-ins whose host owns every allocation, real-time loops that must not take the
  * allocator's locks or risk the implicit synchronisation of cudaMalloc / cudaFree, code

@@ -139,6 +139,12 @@ def params_default() -> lg_params:
     return p
 
 
+class lg_scene_desc(C.Structure):
+    _fields_ = [("geos", C.POINTER(lg_geo)), ("objects", C.POINTER(lg_object)), ("lights", C.POINTER(lg_light)),
+                ("params", C.POINTER(lg_params)), ("n_geo", C.c_uint32), ("n_objects", C.c_uint32),
+                ("n_lights", C.c_uint32), ("_pad", C.c_uint32)]
+
+
 # ---- library loading --------------------------------------------------------------------
 _lib = None
 
@@ -161,6 +167,9 @@ EXPORTS = [
     ("lg_segments_download", C.c_int, [C.c_void_p, C.POINTER(lg_segment), C.POINTER(lg_path_record),
                                        C.c_uint64, C.POINTER(C.c_uint64)]),
     ("lg_accum_download", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    ("lg_batch_upload", C.c_int, [C.c_void_p, C.POINTER(lg_scene_desc), C.c_uint32]),
+    ("lg_batch_render", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_int32, C.POINTER(lg_trace_stats)]),
+    ("lg_batch_image_offset", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint64)]),
     ("lg_accumulate_segments_noalloc", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(lg_params), C.c_void_p,
                                                  C.c_void_p, C.POINTER(C.c_uint64)]),
 ]

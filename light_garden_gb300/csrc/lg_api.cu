@@ -14,100 +14,11 @@
 #include <string>
 #include <vector>
 
-#include "lg_kernels.cuh"
+#include "lg_ctx.hpp"
 
 using namespace lgd;
 
-namespace {
-
-struct DevBuf {
-  void* p = nullptr;
-  size_t bytes = 0;
-};
-
-constexpr uint32_t UNIT_REFS = 1024;       // shared-atomic raster: keeps the split sums below 2^31
-constexpr uint32_t UNIT_REFS_WARP = 8192;  // warp-private raster: no bound, bigger units flush less
-constexpr size_t OBJ_SMEM_MAX = 96 * 1024;
-
-}  // namespace
-
-struct lg_ctx {
-  int device = 0;
-  int n_sm = 0;
-  cudaStream_t stream = nullptr;
-  std::string err;
-  // scene
-  DevBuf d_scan, d_info, d_leaves, d_prog, d_lights, d_cubics;
-  uint32_t n_obj = 0, n_leaves = 0, n_prog = 0, n_lights = 0, n_cubic = 0;
-  uint64_t n_primary = 0;
-  lg_params prm{};
-  bool has_scene = false;
-  double aspect = 1.0;
-  // trace
-  DevBuf d_queue[2], d_scanrec, d_hitrec, d_list[N_LISTS];
-  uint64_t queue_cap = 0;
-  DevBuf d_segs, d_paths;
-  uint64_t seg_cap = 0;
-  DevBuf d_ctr;
-  Counters* h_ctr = nullptr;
-  uint64_t seg_cap_hint = 0, queue_cap_hint = 0;
-  // raster
-  DevBuf d_tile_count, d_tile_off, d_tile_cursor, d_unit_off, d_refs, d_units, d_accum, d_stage;
-  uint64_t refs_cap = 0, units_cap = 0;
-  uint32_t n_tiles = 0, ntx = 0, nty = 0;
-  // launch shapes
-  int trace_grid[4] = {0, 0, 0, 0}, raster_grid = 0, bin_grid = 0;  // scan, refine, full, bounce
-  int raster_warp_grid = 0;
-  int raster_variant = 0;  // 1 shared-atomic tile raster, 2 warp-private tile raster; 0 = not tuned yet
-  size_t obj_smem = 0;
-  int smem_fits = 0;
-  // graph
-  cudaGraphExec_t gexec = nullptr;
-  bool graph_valid = false;
-  cudaEvent_t ev[6] = {};
-};
-
-namespace {
-
-lg_status fail(lg_ctx* c, lg_status st, const std::string& msg) {
-  if (c) c->err = msg;
-  return st;
-}
-
-lg_status cuda_fail(lg_ctx* c, cudaError_t e, const char* what) {
-  std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
-  (void)cudaGetLastError();
-  return fail(c, e == cudaErrorMemoryAllocation ? LG_ERR_OUT_OF_MEMORY : LG_ERR_CUDA, m);
-}
-
-#define CK(call, what)                              \
-  do {                                              \
-    cudaError_t e_ = (call);                        \
-    if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
-  } while (0)
-
-lg_status ensure(lg_ctx* c, DevBuf& b, size_t bytes, const char* what) {
-  if (bytes <= b.bytes && b.p) return LG_OK;
-  if (b.p) cudaFree(b.p);
-  b.p = nullptr;
-  b.bytes = 0;
-  if (bytes == 0) bytes = 16;
-  cudaError_t e = cudaMalloc(&b.p, bytes);
-  if (e != cudaSuccess) {
-    b.p = nullptr;
-    return cuda_fail(c, e, what);
-  }
-  b.bytes = bytes;
-  c->graph_valid = false;
-  return LG_OK;
-}
-
-void release(DevBuf& b) {
-  if (b.p) cudaFree(b.p);
-  b.p = nullptr;
-  b.bytes = 0;
-}
-
+namespace lgh {
 // ---------------------------------------------------------------- scene flattening
 struct Xf {
   double ox, oy, c, s;  // world = (ox, oy) + R(c, s) * local
@@ -117,35 +28,20 @@ struct Xf {
   }
 };
 
-// host FP64 leaf; converted to the device's double-float Leaf64 at upload
-struct LeafH {
-  uint32_t kind;
-  double p[8];
-};
-
-struct Flat {
-  std::vector<ObjScan> scan;
-  std::vector<ObjInfo> info;
-  std::vector<LeafH> leaves;
-  std::vector<uint8_t> prog;
-  std::vector<LightDev> lights;
-  std::vector<uint32_t> cubics;
-};
-
-lg_status flatten_node(lg_ctx* c, const lg_geo* G, uint32_t n_geo, int32_t gi, const Xf& T, int depth, Flat& F,
+lg_status flatten_node(std::string& err, const lg_geo* G, uint32_t n_geo, int32_t gi, const Xf& T, int depth, Flat& F,
                        uint32_t leaf0, std::vector<uint8_t>& prog) {
-  if (gi < 0 || (uint32_t)gi >= n_geo) return fail(c, LG_ERR_INVALID_ARGUMENT, "geometry index out of range");
-  if (depth > 32) return fail(c, LG_ERR_INVALID_ARGUMENT, "geometry tree deeper than 32 (cycle?)");
+  if (gi < 0 || (uint32_t)gi >= n_geo) return set_err(err, LG_ERR_INVALID_ARGUMENT, "geometry index out of range");
+  if (depth > 32) return set_err(err, LG_ERR_INVALID_ARGUMENT, "geometry tree deeper than 32 (cycle?)");
   const lg_geo& g = G[gi];
   if (g.kind == LG_GEO_LOGIC) {
-    if (g.op < 0 || g.op > 2) return fail(c, LG_ERR_INVALID_ARGUMENT, "unknown logic op");
+    if (g.op < 0 || g.op > 2) return set_err(err, LG_ERR_INVALID_ARGUMENT, "unknown logic op");
     Xf T2;
     T.apply(g.origin[0], g.origin[1], T2.ox, T2.oy);
     T2.c = T.c * g.rot[0] - T.s * g.rot[1];
     T2.s = T.s * g.rot[0] + T.c * g.rot[1];
-    lg_status st = flatten_node(c, G, n_geo, g.a, T2, depth + 1, F, leaf0, prog);
+    lg_status st = flatten_node(err, G, n_geo, g.a, T2, depth + 1, F, leaf0, prog);
     if (st) return st;
-    st = flatten_node(c, G, n_geo, g.b, T2, depth + 1, F, leaf0, prog);
+    st = flatten_node(err, G, n_geo, g.b, T2, depth + 1, F, leaf0, prog);
     if (st) return st;
     prog.push_back(g.op == LG_OP_AND ? PROG_AND : g.op == LG_OP_OR ? PROG_OR : PROG_AND_NOT);
     return LG_OK;
@@ -181,10 +77,10 @@ lg_status flatten_node(lg_ctx* c, const lg_geo* G, uint32_t n_geo, int32_t gi, c
       for (int k = 0; k < 4; ++k) T.apply(g.v[2 * k], g.v[2 * k + 1], L.p[2 * k], L.p[2 * k + 1]);
       break;
     default:
-      return fail(c, LG_ERR_UNSUPPORTED, "unsupported geometry kind " + std::to_string(g.kind));
+      return set_err(err, LG_ERR_UNSUPPORTED, "unsupported geometry kind " + std::to_string(g.kind));
   }
   const uint32_t li = (uint32_t)F.leaves.size() - leaf0;
-  if (li >= (uint32_t)MAX_LEAVES - 1) return fail(c, LG_ERR_UNSUPPORTED, "more than 63 leaves in one object");
+  if (li >= (uint32_t)MAX_LEAVES - 1) return set_err(err, LG_ERR_UNSUPPORTED, "more than 63 leaves in one object");
   F.leaves.push_back(L);
   prog.push_back((uint8_t)li);
   return LG_OK;
@@ -258,26 +154,26 @@ bool blend_supported(const lg_blend_component& b) {
   }
 }
 
-lg_status flatten_scene(lg_ctx* c, const lg_geo* G, uint32_t n_geo, const lg_object* O, uint32_t n_obj,
+lg_status flatten_scene(std::string& err, const lg_geo* G, uint32_t n_geo, const lg_object* O, uint32_t n_obj,
                         const lg_light* Ls, uint32_t n_lights, Flat& F) {
   for (uint32_t k = 0; k < n_obj; ++k) {
     const lg_object& o = O[k];
     if (o.kind == LG_OBJ_CONVEX_POLYGON || o.kind == LG_OBJ_ELLIPSE)
-      return fail(c, LG_ERR_UNSUPPORTED, "object " + std::to_string(k) + ": ConvexPolygon / Ellipse are not on this path");
-    if (o.kind < 0 || o.kind > LG_OBJ_GEO) return fail(c, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": unknown kind");
-    if (o.geo < 0 || (uint32_t)o.geo >= n_geo) return fail(c, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": geometry index out of range");
+      return set_err(err, LG_ERR_UNSUPPORTED, "object " + std::to_string(k) + ": ConvexPolygon / Ellipse are not on this path");
+    if (o.kind < 0 || o.kind > LG_OBJ_GEO) return set_err(err, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": unknown kind");
+    if (o.geo < 0 || (uint32_t)o.geo >= n_geo) return set_err(err, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": geometry index out of range");
     const int rk = G[o.geo].kind;
     const bool ok = (o.kind == LG_OBJ_STRAIGHT_MIRROR && rk == LG_GEO_SEGMENT) ||
                     (o.kind == LG_OBJ_CURVED_MIRROR && rk == LG_GEO_CUBIC) ||
                     (o.kind == LG_OBJ_CIRCLE && rk == LG_GEO_CIRCLE) || (o.kind == LG_OBJ_RECT && rk == LG_GEO_RECT) ||
                     (o.kind == LG_OBJ_LENS && rk == LG_GEO_LOGIC) || o.kind == LG_OBJ_GEO;
-    if (!ok) return fail(c, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": kind does not match its geometry");
+    if (!ok) return set_err(err, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": kind does not match its geometry");
     if (o.has_material && !(o.refractive_index > 0.0))
-      return fail(c, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": refractive index must be > 0");
+      return set_err(err, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": refractive index must be > 0");
     const uint32_t leaf0 = (uint32_t)F.leaves.size();
     std::vector<uint8_t> prog;
     Xf T{0.0, 0.0, 1.0, 0.0};
-    lg_status st = flatten_node(c, G, n_geo, o.geo, T, 0, F, leaf0, prog);
+    lg_status st = flatten_node(err, G, n_geo, o.geo, T, 0, F, leaf0, prog);
     if (st) return st;
     ObjInfo oi;
     std::memset(&oi, 0, sizeof oi);
@@ -300,7 +196,7 @@ lg_status flatten_scene(lg_ctx* c, const lg_geo* G, uint32_t n_geo, const lg_obj
     double R = 0.0;
     for (uint32_t i = leaf0; i < F.leaves.size(); ++i) R = std::max(R, leaf_extent(F.leaves[i], cx, cy));
     if (!std::isfinite(cx) || !std::isfinite(cy) || !std::isfinite(R))
-      return fail(c, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": non-finite geometry");
+      return set_err(err, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": non-finite geometry");
     s.cx = (float)cx;
     s.cy = (float)cy;
     s.R = (float)(R * (1.0 + 1e-6) + 1e-6 * (1.0 + std::fabs(cx) + std::fabs(cy)));
@@ -326,7 +222,7 @@ lg_status flatten_scene(lg_ctx* c, const lg_geo* G, uint32_t n_geo, const lg_obj
   uint64_t first = 0;
   for (uint32_t l = 0; l < n_lights; ++l) {
     const lg_light& L = Ls[l];
-    if (L.kind < 0 || L.kind > LG_LIGHT_SPOT) return fail(c, LG_ERR_INVALID_ARGUMENT, "light " + std::to_string(l) + ": unknown kind");
+    if (L.kind < 0 || L.kind > LG_LIGHT_SPOT) return set_err(err, LG_ERR_INVALID_ARGUMENT, "light " + std::to_string(l) + ": unknown kind");
     LightDev d;
     std::memset(&d, 0, sizeof d);
     d.ox = L.origin[0]; d.oy = L.origin[1]; d.vx = L.v[0]; d.vy = L.v[1];
@@ -340,6 +236,77 @@ lg_status flatten_scene(lg_ctx* c, const lg_geo* G, uint32_t n_geo, const lg_obj
     F.lights.push_back(d);
   }
   return LG_OK;
+}
+
+
+lg_status validate_params(std::string& err, const lg_params& p) {
+  if (p.max_bounce > (uint32_t)MAX_GEN) return set_err(err, LG_ERR_INVALID_ARGUMENT, "max_bounce must be <= 64");
+  if (p.width == 0 || p.height == 0 || p.width > 32768 || p.height > 32768)
+    return set_err(err, LG_ERR_INVALID_ARGUMENT, "canvas must be 1..32768 pixels per side");
+  if (p.accum != LG_ACCUM_FIXED64 && p.accum != LG_ACCUM_F32)
+    return set_err(err, LG_ERR_INVALID_ARGUMENT, "unknown accum mode");
+  if (!blend_supported(p.color_blend) || !blend_supported(p.alpha_blend))
+    return set_err(err, LG_ERR_UNSUPPORTED, "blend state reads the destination (order-dependent): not supported");
+  if (p.string_mod.modulo && (p.string_mod.curve != 0 || p.string_mod.mode > LG_SM_BASE))
+    return set_err(err, LG_ERR_UNSUPPORTED, "string mod: only Curve::Circle with Add/Mul/Pow/Base");
+  if (p.string_mod.modulo > (1ull << 30)) return set_err(err, LG_ERR_INVALID_ARGUMENT, "string mod modulo too large");
+  return LG_OK;
+}
+
+int raster_mode(const lg_params& p) {
+  if (p.accum == LG_ACCUM_F32) return RM_F32_;
+  const lg_blend_component* b[2] = {&p.color_blend, &p.alpha_blend};
+  for (const lg_blend_component* x : b)
+    if (x->op == LG_BO_MIN || x->op == LG_BO_MAX) return RM_FIXED_MINMAX_;
+  return RM_FIXED_SPLIT_;
+}
+
+void to_device_leaves(const std::vector<LeafH>& in, std::vector<Leaf64>& out) {
+  out.resize(in.size());
+  for (size_t i = 0; i < in.size(); ++i) {
+    std::memset(&out[i], 0, sizeof(Leaf64));
+    out[i].kind = in[i].kind;
+    for (int k = 0; k < 8; ++k) out[i].p[k] = DF(in[i].p[k]);
+  }
+}
+
+}  // namespace lgh
+
+using namespace lgh;
+
+namespace lgh {
+
+lg_status fail(lg_ctx* c, lg_status st, const std::string& msg) {
+  if (c) c->err = msg;
+  return st;
+}
+
+lg_status cuda_fail(lg_ctx* c, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+  (void)cudaGetLastError();
+  return fail(c, e == cudaErrorMemoryAllocation ? LG_ERR_OUT_OF_MEMORY : LG_ERR_CUDA, m);
+}
+
+lg_status ensure(lg_ctx* c, DevBuf& b, size_t bytes, const char* what) {
+  if (bytes <= b.bytes && b.p) return LG_OK;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(&b.p, bytes);
+  if (e != cudaSuccess) {
+    b.p = nullptr;
+    return cuda_fail(c, e, what);
+  }
+  b.bytes = bytes;
+  c->graph_valid = false;
+  return LG_OK;
+}
+
+void release(DevBuf& b) {
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
 }
 
 SceneDev scene_dev(lg_ctx* c) {
@@ -356,6 +323,9 @@ SceneDev scene_dev(lg_ctx* c) {
   for (int i = 0; i < 4; ++i) S.cutoff[i] = c->prm.cutoff_color[i];
   S.max_bounce = c->prm.max_bounce;
   S.record_paths = c->prm.record_paths ? 1u : 0u;
+  S.scenes = nullptr;
+  S.n_scenes = 1;
+  S._pad = 0;
   return S;
 }
 
@@ -369,6 +339,7 @@ TraceBufs trace_bufs(lg_ctx* c) {
   for (int i = 0; i < N_LISTS; ++i) B.list[i] = (uint32_t*)c->d_list[i].p;
   B.segs = (lg_segment*)c->d_segs.p;
   B.paths = (lg_path_record*)c->d_paths.p;
+  B.seg_scene = nullptr;
   B.seg_cap = c->seg_cap;
   B.ctr = (Counters*)c->d_ctr.p;
   return B;
@@ -439,31 +410,24 @@ lg_status enqueue_trace(lg_ctx* c) {
   const SceneDev S = scene_dev(c);
   const TraceBufs B = trace_bufs(c);
   CK(cudaMemsetAsync(c->d_ctr.p, 0, sizeof(Counters), c->stream), "memset counters");
-  if (c->n_lights) k_light_setup<<<1, 256, 0, c->stream>>>(S);
+  if (c->n_lights) k_light_setup<false><<<1, 256, 0, c->stream>>>(S);
   const size_t tsm = c->smem_fits ? c->obj_smem : 0;
   for (uint32_t g = 0; g < c->prm.max_bounce; ++g) {
-    k_scan<<<c->trace_grid[0], SCAN_THREADS, (size_t)scan_smem_bytes() + tsm, c->stream>>>(S, B, g, c->smem_fits);
+    k_scan<false><<<c->trace_grid[0], SCAN_THREADS, (size_t)scan_smem_bytes() + tsm, c->stream>>>(S, B, g,
+                                                                                                  c->smem_fits);
     for (int l = LIST_REFINE_CIRCLE; l <= LIST_REFINE_CUBIC; ++l)
-      k_refine<<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g, l);
-    k_full<<<c->trace_grid[2], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
-    k_bounce<<<c->trace_grid[3], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
+      k_refine<false><<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g, l);
+    k_full<false><<<c->trace_grid[2], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
+    k_bounce<false><<<c->trace_grid[3], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
   }
   const uint64_t n_ov = 3ull * c->n_cubic * (c->prm.emit_control_lines ? 1 : 0) + c->prm.string_mod.modulo;
   if (n_ov) {
     const int blocks = (int)std::min<uint64_t>((n_ov + 255) / 256, 4096);
-    k_overlay<<<blocks, 256, 0, c->stream>>>(S, B, (const uint32_t*)c->d_cubics.p,
+    k_overlay<<<blocks, 256, 0, c->stream>>>(S, B, (const uint32_t*)c->d_cubics.p, nullptr,
                                              c->prm.emit_control_lines ? c->n_cubic : 0, c->prm.string_mod);
   }
   CK(cudaGetLastError(), "trace launch");
   return LG_OK;
-}
-
-int raster_mode(const lg_params& p) {
-  if (p.accum == LG_ACCUM_F32) return RM_F32_;
-  const lg_blend_component* b[2] = {&p.color_blend, &p.alpha_blend};
-  for (const lg_blend_component* x : b)
-    if (x->op == LG_BO_MIN || x->op == LG_BO_MAX) return RM_FIXED_MINMAX_;
-  return RM_FIXED_SPLIT_;
 }
 
 lg_status stage_event(lg_ctx* c, int i) {
@@ -630,7 +594,7 @@ lg_status need_scene(lg_ctx* c) {
 }
 
 
-}  // namespace
+}  // namespace lgh
 
 // =============================================================================== C ABI
 extern "C" {
@@ -669,9 +633,11 @@ lg_status lg_create(lg_ctx** out, const lg_device_opts* opts) {
   if (e == cudaSuccess) e = cudaMalloc(&c->d_ctr.p, sizeof(Counters));
   for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, scan_smem_bytes() + (int)OBJ_SMEM_MAX);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_full, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bounce, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
+    e = cudaFuncSetAttribute(k_scan<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, scan_smem_bytes() + (int)OBJ_SMEM_MAX);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_full<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bounce<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_scan<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, scan_smem_bytes());
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_bin_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(MAX_SMEM_TILES * 4));
   if (e == cudaSuccess)
@@ -697,11 +663,14 @@ lg_status lg_destroy(lg_ctx* c) {
   DevBuf* bufs[] = {&c->d_scan, &c->d_info, &c->d_leaves, &c->d_prog, &c->d_lights, &c->d_cubics, &c->d_queue[0],
                     &c->d_queue[1], &c->d_scanrec, &c->d_hitrec, &c->d_list[0], &c->d_list[1], &c->d_list[2],
                     &c->d_list[3], &c->d_list[4], &c->d_list[5], &c->d_segs, &c->d_paths, &c->d_ctr, &c->d_tile_count, &c->d_tile_off,
-                    &c->d_tile_cursor, &c->d_unit_off, &c->d_refs, &c->d_units, &c->d_accum, &c->d_stage};
+                    &c->d_tile_cursor, &c->d_unit_off, &c->d_refs, &c->d_units, &c->d_accum, &c->d_stage,
+                    &c->d_scenes, &c->d_canvases, &c->d_seg_scene, &c->d_cubic_scene, &c->d_part};
   for (DevBuf* b : bufs) release(*b);
   if (c->h_ctr) cudaFreeHost(c->h_ctr);
   for (int i = 0; i < 6; ++i)
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  for (cudaEvent_t e : c->bev)
+    if (e) cudaEventDestroy(e);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return LG_OK;
@@ -713,19 +682,12 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
     return c ? fail(c, LG_ERR_INVALID_ARGUMENT, "null pointer") : LG_ERR_INVALID_ARGUMENT;
   CK(cudaSetDevice(c->device), "cudaSetDevice");
   const lg_params& p = *params;
-  if (p.max_bounce > (uint32_t)MAX_GEN) return fail(c, LG_ERR_INVALID_ARGUMENT, "max_bounce must be <= 64");
-  if (p.width == 0 || p.height == 0 || p.width > 32768 || p.height > 32768)
-    return fail(c, LG_ERR_INVALID_ARGUMENT, "canvas must be 1..32768 pixels per side");
-  if (p.accum != LG_ACCUM_FIXED64 && p.accum != LG_ACCUM_F32) return fail(c, LG_ERR_INVALID_ARGUMENT, "unknown accum mode");
-  if (!blend_supported(p.color_blend) || !blend_supported(p.alpha_blend))
-    return fail(c, LG_ERR_UNSUPPORTED, "blend state reads the destination (order-dependent): not supported");
-  if (p.string_mod.modulo && (p.string_mod.curve != 0 || p.string_mod.mode > LG_SM_BASE))
-    return fail(c, LG_ERR_UNSUPPORTED, "string mod: only Curve::Circle with Add/Mul/Pow/Base");
-  if (p.string_mod.modulo > (1ull << 30)) return fail(c, LG_ERR_INVALID_ARGUMENT, "string mod modulo too large");
+  lg_status st = validate_params(c->err, p);
+  if (st) return st;
   if (n_lights > 65535) return fail(c, LG_ERR_INVALID_ARGUMENT, "at most 65535 lights");
   if (n_objects > 65535) return fail(c, LG_ERR_UNSUPPORTED, "at most 65535 objects");
   Flat F;
-  lg_status st = flatten_scene(c, geos, n_geo, objects, n_objects, lights, n_lights, F);
+  st = flatten_scene(c->err, geos, n_geo, objects, n_objects, lights, n_lights, F);
   if (st) return st;
   CK(cudaStreamSynchronize(c->stream), "synchronize");
   const bool same_shape = c->has_scene && c->n_obj == n_objects && c->n_leaves == F.leaves.size() &&
@@ -733,12 +695,8 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
                           std::memcmp(&c->prm, &p, sizeof p) == 0;
   if ((st = ensure(c, c->d_scan, F.scan.size() * sizeof(ObjScan), "scene"))) return st;
   if ((st = ensure(c, c->d_info, F.info.size() * sizeof(ObjInfo), "scene"))) return st;
-  std::vector<Leaf64> dleaves(F.leaves.size());
-  for (size_t i = 0; i < F.leaves.size(); ++i) {
-    std::memset(&dleaves[i], 0, sizeof(Leaf64));
-    dleaves[i].kind = F.leaves[i].kind;
-    for (int k = 0; k < 8; ++k) dleaves[i].p[k] = DF(F.leaves[i].p[k]);
-  }
+  std::vector<Leaf64> dleaves;
+  to_device_leaves(F.leaves, dleaves);
   if ((st = ensure(c, c->d_leaves, F.leaves.size() * sizeof(Leaf64), "scene"))) return st;
   if ((st = ensure(c, c->d_prog, F.prog.size() + 16, "scene"))) return st;
   if ((st = ensure(c, c->d_lights, F.lights.size() * sizeof(LightDev), "scene"))) return st;
@@ -750,6 +708,11 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
   if (!F.lights.empty()) CK(cudaMemcpyAsync(c->d_lights.p, F.lights.data(), F.lights.size() * sizeof(LightDev), cudaMemcpyHostToDevice, c->stream), "upload");
   if (!F.cubics.empty()) CK(cudaMemcpyAsync(c->d_cubics.p, F.cubics.data(), F.cubics.size() * 4, cudaMemcpyHostToDevice, c->stream), "upload");
   CK(cudaStreamSynchronize(c->stream), "upload");
+  if (c->multi) {  // leaving batch mode: every captured launch and launch shape is stale
+    c->multi = false;
+    c->graph_valid = false;
+    c->n_scenes = 0;
+  }
   c->n_obj = n_objects;
   c->n_leaves = (uint32_t)F.leaves.size();
   c->n_prog = (uint32_t)F.prog.size();
@@ -767,13 +730,13 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
   c->smem_fits = c->obj_smem <= OBJ_SMEM_MAX ? 1 : 0;
   int occ = 0;
   const size_t tsm = c->smem_fits ? c->obj_smem : 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_scan, SCAN_THREADS, (size_t)scan_smem_bytes() + tsm), "occupancy");
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_scan<false>, SCAN_THREADS, (size_t)scan_smem_bytes() + tsm), "occupancy");
   c->trace_grid[0] = c->n_sm * std::max(1, occ);
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_refine, 256, 0), "occupancy");
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_refine<false>, 256, 0), "occupancy");
   c->trace_grid[1] = c->n_sm * std::max(1, occ);
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_full, 256, tsm), "occupancy");
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_full<false>, 256, tsm), "occupancy");
   c->trace_grid[2] = c->n_sm * std::max(1, occ);
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bounce, 256, tsm), "occupancy");
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bounce<false>, 256, tsm), "occupancy");
   c->trace_grid[3] = c->n_sm * std::max(1, occ);
   const int mode = raster_mode(p);
   const int rsm = raster_smem_bytes(mode);

@@ -1,0 +1,95 @@
+// lg_ctx.hpp — the context behind lg_ctx* and the host helpers shared by lg_api.cu
+// (single scene) and lg_batch.cu (multi-scene batches and serving).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "lg_host.hpp"
+
+namespace lgh {
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+constexpr uint32_t UNIT_REFS = 1024;       // shared-atomic raster: keeps the split sums below 2^31
+constexpr uint32_t UNIT_REFS_WARP = 8192;  // warp-private raster: no bound, bigger units flush less
+constexpr size_t OBJ_SMEM_MAX = 96 * 1024;
+
+}  // namespace lgh
+
+using namespace lgh;
+
+struct lg_ctx {
+  int device = 0;
+  int n_sm = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // scene
+  DevBuf d_scan, d_info, d_leaves, d_prog, d_lights, d_cubics;
+  uint32_t n_obj = 0, n_leaves = 0, n_prog = 0, n_lights = 0, n_cubic = 0;
+  uint64_t n_primary = 0;
+  lg_params prm{};
+  bool has_scene = false;
+  double aspect = 1.0;
+  // trace
+  DevBuf d_queue[2], d_scanrec, d_hitrec, d_list[N_LISTS];
+  uint64_t queue_cap = 0;
+  DevBuf d_segs, d_paths;
+  uint64_t seg_cap = 0;
+  DevBuf d_ctr;
+  Counters* h_ctr = nullptr;
+  uint64_t seg_cap_hint = 0, queue_cap_hint = 0;
+  // raster
+  DevBuf d_tile_count, d_tile_off, d_tile_cursor, d_unit_off, d_refs, d_units, d_accum, d_stage;
+  uint64_t refs_cap = 0, units_cap = 0;
+  uint32_t n_tiles = 0, ntx = 0, nty = 0;
+  // launch shapes
+  int trace_grid[4] = {0, 0, 0, 0}, raster_grid = 0, bin_grid = 0;  // scan, refine, full, bounce
+  int raster_warp_grid = 0;
+  int raster_variant = 0;  // 1 shared-atomic tile raster, 2 warp-private tile raster; 0 = not tuned yet
+  size_t obj_smem = 0;
+  int smem_fits = 0;
+  // graph
+  cudaGraphExec_t gexec = nullptr;
+  bool graph_valid = false;
+  cudaEvent_t ev[6] = {};
+  // multi-scene mode (lg_batch_upload): the concatenated scenes replace the single scene
+  bool multi = false;
+  uint32_t n_scenes = 0;
+  std::vector<SceneRec> h_scenes;
+  std::vector<SceneCanvas> h_canvases;
+  std::vector<uint64_t> h_px_base;       // first pixel of each scene's image
+  DevBuf d_scenes, d_canvases, d_seg_scene, d_cubic_scene, d_part;
+  uint64_t total_px = 0;
+  uint32_t total_bins = 0;
+  uint32_t max_bounce_all = 0;
+  uint64_t n_overlay = 0;
+  int batch_grid_scan = 0;
+  std::vector<cudaEvent_t> bev;          // batch stage events (start, per generation x 2, resolved)
+};
+
+
+namespace lgh {
+
+lg_status fail(lg_ctx* c, lg_status st, const std::string& msg);
+lg_status cuda_fail(lg_ctx* c, cudaError_t e, const char* what);
+lg_status ensure(lg_ctx* c, DevBuf& b, size_t bytes, const char* what);
+void release(DevBuf& b);
+lg_status sync_counters(lg_ctx* c);
+float elapsed(cudaEvent_t a, cudaEvent_t b);
+lg_status ensure_trace_buffers(lg_ctx* c);
+SceneDev scene_dev(lg_ctx* c);
+TraceBufs trace_bufs(lg_ctx* c);
+RasterArgs raster_args(lg_ctx* c);
+void fill_stats(lg_ctx* c, lg_trace_stats* s);
+
+#define CK(call, what)                                      \
+  do {                                                      \
+    cudaError_t e_ = (call);                                \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, what);   \
+  } while (0)
+
+}  // namespace lgh

@@ -92,6 +92,8 @@ struct __align__(16) LightDev {
   float color[4];
   uint32_t kind, num_rays;
   uint64_t first;      // index of this light's first primary in the virtual gen-0 queue
+  uint32_t scene;      // scene of this light (multi-scene traces)
+  uint32_t _pad;
 };
 
 // Medium a ray travels in: an object index (its refractive index), or
@@ -113,7 +115,8 @@ struct __align__(16) RayRec {
   uint16_t medium;   // see MEDIUM_*
   uint16_t src_obj;  // object whose surface the ray starts on (SRC_NONE for primaries)
   uint8_t src_leaf;  // leaf of src_obj that holds the start point
-  uint8_t _pad[3];
+  uint8_t _pad;
+  uint16_t scene;    // scene of the ray (multi-scene traces); object indices are scene-local
 };
 static_assert(sizeof(RayRec) == 80, "RayRec is 80 B");
 constexpr float ILL_COND = 1e-11f;
@@ -134,10 +137,24 @@ struct Counters {
   unsigned long long visits, fp64_solves, fallbacks, near;
   unsigned long long pixels, tile_refs, units;
   unsigned long long unit_cursor;
+  // multi-scene streaming accumulation: the ring and the tile lists are reused every
+  // generation; these keep the totals and the largest per-generation demands
+  unsigned long long seg_total, seg_max, refs_total, refs_max;
   unsigned int error_flags;
   unsigned int _pad;
 };
 constexpr unsigned ERR_TMA_TIMEOUT = 1u;
+
+// One scene of a multi-scene trace: its objects are [obj_base, obj_base + n_obj) of the
+// concatenated tables (ray, scan and hit records hold indices relative to obj_base).
+struct __align__(16) SceneRec {
+  uint32_t obj_base, n_obj;
+  df aspect;              // canvas half width (height is 1)
+  float cutoff[4];
+  uint32_t max_bounce;
+  uint32_t _pad[3];
+};
+static_assert(sizeof(SceneRec) == 48, "SceneRec is 48 B");
 
 struct SceneDev {
   const ObjScan* scan;
@@ -149,9 +166,40 @@ struct SceneDev {
   uint64_t n_primary;
   df aspect;              // canvas half width (height is 1)
   float cutoff[4];
-  uint32_t max_bounce;
+  uint32_t max_bounce;    // multi-scene: the largest of the scenes
   uint32_t record_paths;
+  const SceneRec* scenes; // multi-scene traces only
+  uint32_t n_scenes;
+  uint32_t _pad;
 };
+
+// The scene a ray belongs to, as the kernels use it.  Single-scene kernels (MULTI false)
+// take everything from the kernel parameters; multi-scene kernels read the scene table.
+struct SceneLoc {
+  uint32_t base, n;
+  df aspect;
+  float cutoff[4];
+  uint32_t max_bounce;
+};
+template <bool MULTI>
+__device__ __forceinline__ SceneLoc scene_of(const SceneDev& S, uint32_t sid) {
+  SceneLoc L;
+  if (!MULTI) {
+    L.base = 0; L.n = S.n_obj; L.aspect = S.aspect; L.max_bounce = S.max_bounce;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) L.cutoff[i] = S.cutoff[i];
+  } else {
+    const SceneRec& R = S.scenes[sid];
+    L.base = R.obj_base; L.n = R.n_obj; L.aspect = R.aspect; L.max_bounce = R.max_bounce;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) L.cutoff[i] = R.cutoff[i];
+  }
+  return L;
+}
+template <bool MULTI>
+__device__ __forceinline__ uint32_t obj_base_of(const SceneDev& S, uint32_t sid) {
+  return MULTI ? S.scenes[sid].obj_base : 0u;
+}
 
 // per-ray result of the FP32 scan
 struct __align__(16) ScanRec {
@@ -186,6 +234,7 @@ struct TraceBufs {
   uint32_t* list[N_LISTS];  // [queue_cap] each
   lg_segment* segs;
   lg_path_record* paths;
+  uint16_t* seg_scene;      // multi-scene traces: the scene of every segment
   uint64_t seg_cap;
   Counters* ctr;
 };

@@ -17,8 +17,18 @@ struct BlendDev {
   float clear[4];
 };
 
+// One scene's canvas in a multi-scene accumulation: its bins (2 per tile) start at
+// bin_base and its pixels at px_base of the shared accumulation buffer.
+struct SceneCanvas {
+  uint32_t W, H, ntx, nty;
+  uint64_t bin_base, px_base;
+};
+
 struct RasterArgs {
   const lg_segment* segs;
+  const uint16_t* seg_scene;      // multi-scene: scene of each segment (nullptr: one scene)
+  const SceneCanvas* canvases;    // multi-scene: per-scene canvas, in bin order
+  uint32_t n_scenes;
   uint64_t seg_cap;
   uint32_t W, H, ntx, nty;
   uint32_t n_tiles;
@@ -36,14 +46,20 @@ struct RasterArgs {
   Counters* ctr;
 };
 
+template <bool MULTI>
 __global__ void k_light_setup(SceneDev S);
+template <bool MULTI>
 __global__ void k_scan(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
 int scan_smem_bytes();
 constexpr int SCAN_THREADS = 128;
+template <bool MULTI>
 __global__ void k_refine(SceneDev S, TraceBufs B, uint32_t gen, int list);
+template <bool MULTI>
 __global__ void k_full(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
+template <bool MULTI>
 __global__ void k_bounce(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
-__global__ void k_overlay(SceneDev S, TraceBufs B, const uint32_t* cubic_objs, uint32_t n_cubic, lg_string_mod sm);
+__global__ void k_overlay(SceneDev S, TraceBufs B, const uint32_t* cubic_objs, const uint16_t* cubic_scene,
+                          uint32_t n_cubic, lg_string_mod sm);
 
 __global__ void k_clear_accum(RasterArgs A, int fixed);
 __global__ void k_bin_count(RasterArgs A, int smem_tiles);
@@ -58,6 +74,12 @@ __global__ void k_raster_warp(RasterArgs A);
 int raster_warp_smem_bytes();
 constexpr int RM_FIXED_SPLIT_ = 0, RM_FIXED_MINMAX_ = 1, RM_F32_ = 2;
 constexpr uint32_t MAX_SMEM_TILES = 32768;  // tile bins (2 per tile) with 32-bit counters in 128 KB
+// multi-scene streaming accumulation
+__global__ void k_stream_rotate(Counters* ctr, uint64_t seg_cap);
+constexpr int TILE_SCAN_CHUNK = 4096;  // bins per CTA of the multi-block tile scan
+__global__ void k_tiles_partial(RasterArgs A, unsigned long long* part);
+__global__ void k_tiles_scan_partials(RasterArgs A, unsigned long long* part, uint32_t n_part);
+__global__ void k_tiles_apply(RasterArgs A, const unsigned long long* part);
 __global__ void k_resolve_f16(const void* accum, int fixed, uint32_t W, uint32_t H, uint16_t* dst, size_t pitch);
 __global__ void k_resolve_rgba8(const void* accum, int fixed, uint32_t W, uint32_t H, uint8_t* dst, size_t pitch);
 

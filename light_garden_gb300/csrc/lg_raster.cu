@@ -66,12 +66,43 @@ __global__ void k_clear_accum(RasterArgs A, int fixed) {
   }
 }
 
+// ------------------------------------------------------------------ canvases
+// The canvas a segment or a bin belongs to: the context's one canvas, or in a
+// multi-scene accumulation the scene's own.
+struct CanvasLoc {
+  uint32_t W, H, ntx;
+  uint64_t bin_base, px_base;
+};
+__device__ __forceinline__ CanvasLoc canvas_one(const RasterArgs& A) {
+  CanvasLoc C;
+  C.W = A.W; C.H = A.H; C.ntx = A.ntx; C.bin_base = 0; C.px_base = 0;
+  return C;
+}
+__device__ __forceinline__ CanvasLoc canvas_at(const RasterArgs& A, uint32_t s) {
+  const SceneCanvas& K = A.canvases[s];
+  CanvasLoc C;
+  C.W = K.W; C.H = K.H; C.ntx = K.ntx; C.bin_base = K.bin_base; C.px_base = K.px_base;
+  return C;
+}
+__device__ __forceinline__ CanvasLoc canvas_of_segment(const RasterArgs& A, uint64_t i) {
+  return A.seg_scene ? canvas_at(A, A.seg_scene[i]) : canvas_one(A);
+}
+__device__ __forceinline__ CanvasLoc canvas_of_bin(const RasterArgs& A, uint64_t bin) {
+  if (!A.seg_scene) return canvas_one(A);
+  uint32_t lo = 0, hi = A.n_scenes;  // the last scene whose first bin is <= bin
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (A.canvases[mid].bin_base <= bin) lo = mid; else hi = mid;
+  }
+  return canvas_at(A, lo);
+}
+
 // ------------------------------------------------------------------ binning
 // Visits every tile that holds at least one pixel of the segment: per tile column
 // (x-major) the minor range is bounded by the samples at both ends, since v(i) is
 // monotone in i.
 template <class F>
-__device__ __forceinline__ void for_each_tile(const RSetup& R, const RasterArgs& A, F&& f) {
+__device__ __forceinline__ void for_each_tile(const RSetup& R, const CanvasLoc& A, F&& f) {
   const int nmin = (int)(R.xmajor ? A.H : A.W);
   const int tlo = R.lo / TILE, thi = (R.hi - 1) / TILE;
   for (int tm = tlo; tm <= thi; ++tm) {
@@ -85,7 +116,7 @@ __device__ __forceinline__ void for_each_tile(const RSetup& R, const RasterArgs&
       // bin id = 2 * tile + orientation: x-major and y-major segments of a tile are
       // rasterised in separate units, each with a bank-conflict-free layout
       const uint32_t tile = R.xmajor ? (uint32_t)tn * A.ntx + (uint32_t)tm : (uint32_t)tm * A.ntx + (uint32_t)tn;
-      f(2u * tile + (R.xmajor ? 0u : 1u));
+      f((uint32_t)(A.bin_base + 2u * tile + (R.xmajor ? 0u : 1u)));
     }
   }
 }
@@ -107,8 +138,9 @@ __global__ void __launch_bounds__(256) k_bin_count(RasterArgs A, int smem_tiles)
   }
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
     RSetup R;
-    if (!raster_setup(A.segs[i], A.W, A.H, R)) continue;
-    for_each_tile(R, A, [&](uint32_t tile) {
+    const CanvasLoc C = canvas_of_segment(A, i);
+    if (!raster_setup(A.segs[i], C.W, C.H, R)) continue;
+    for_each_tile(R, C, [&](uint32_t tile) {
       if (smem_tiles) {
         atomicAdd(&hist[tile], 1u);
       } else {
@@ -178,6 +210,115 @@ __global__ void __launch_bounds__(1024) k_scan_tiles(RasterArgs A) {
   }
 }
 
+// Multi-block version of k_scan_tiles for the many bins of a multi-scene accumulation:
+// per-CTA sums of refs and units, one scan of the CTA sums, then each CTA scans its own
+// chunk from its offset.  part holds 2 values per CTA (refs, units).
+__device__ __forceinline__ void tile_counts(const RasterArgs& A, uint32_t t, unsigned long long& c,
+                                            unsigned long long& u) {
+  c = t < A.n_tiles ? A.tile_count[t] : 0ull;
+  u = (c + A.unit_refs - 1) / A.unit_refs;
+}
+
+// inclusive block scan of (r, u) over 1024 threads; returns the block totals in tr, tu
+__device__ __forceinline__ void block_scan2(unsigned long long& r, unsigned long long& u, unsigned long long& tr,
+                                            unsigned long long& tu) {
+  __shared__ unsigned long long wr[32], wu[32];
+  const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long yr = __shfl_up_sync(0xffffffffu, r, o), yu = __shfl_up_sync(0xffffffffu, u, o);
+    if ((int)lane >= o) { r += yr; u += yu; }
+  }
+  if (lane == 31) { wr[wid] = r; wu[wid] = u; }
+  __syncthreads();
+  if (wid == 0) {
+    unsigned long long sr = lane < (blockDim.x >> 5) ? wr[lane] : 0ull;
+    unsigned long long su = lane < (blockDim.x >> 5) ? wu[lane] : 0ull;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long yr = __shfl_up_sync(0xffffffffu, sr, o), yu = __shfl_up_sync(0xffffffffu, su, o);
+      if ((int)lane >= o) { sr += yr; su += yu; }
+    }
+    wr[lane] = sr;
+    wu[lane] = su;
+  }
+  __syncthreads();
+  if (wid) { r += wr[wid - 1]; u += wu[wid - 1]; }
+  tr = wr[(blockDim.x >> 5) - 1];
+  tu = wu[(blockDim.x >> 5) - 1];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(1024) k_tiles_partial(RasterArgs A, unsigned long long* part) {
+  const uint32_t b0 = blockIdx.x * (uint32_t)TILE_SCAN_CHUNK;
+  unsigned long long r = 0, u = 0;
+  for (uint32_t k = threadIdx.x; k < (uint32_t)TILE_SCAN_CHUNK; k += blockDim.x) {
+    unsigned long long c, v;
+    tile_counts(A, b0 + k, c, v);
+    r += c;
+    u += v;
+  }
+  unsigned long long tr, tu;
+  block_scan2(r, u, tr, tu);
+  if (threadIdx.x == 0) { part[2 * blockIdx.x] = tr; part[2 * blockIdx.x + 1] = tu; }
+}
+
+__global__ void __launch_bounds__(1024) k_tiles_scan_partials(RasterArgs A, unsigned long long* part, uint32_t n_part) {
+  __shared__ unsigned long long carry_r, carry_u;
+  if (threadIdx.x == 0) { carry_r = 0; carry_u = 0; }
+  __syncthreads();
+  for (uint32_t base = 0; base < n_part; base += blockDim.x) {
+    const uint32_t i = base + threadIdx.x;
+    const unsigned long long c = i < n_part ? part[2 * i] : 0ull, v = i < n_part ? part[2 * i + 1] : 0ull;
+    unsigned long long r = c, u = v, tr, tu;
+    block_scan2(r, u, tr, tu);
+    const unsigned long long cr = carry_r, cu = carry_u;
+    if (i < n_part) { part[2 * i] = cr + r - c; part[2 * i + 1] = cu + u - v; }
+    __syncthreads();
+    if (threadIdx.x == 0) { carry_r = cr + tr; carry_u = cu + tu; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    A.ctr->tile_refs = carry_r;
+    A.ctr->units = carry_u;
+    A.ctr->unit_cursor = 0;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_tiles_apply(RasterArgs A, const unsigned long long* part) {
+  __shared__ unsigned long long carry_r, carry_u;
+  if (threadIdx.x == 0) { carry_r = part[2 * blockIdx.x]; carry_u = part[2 * blockIdx.x + 1]; }
+  __syncthreads();
+  const uint32_t b0 = blockIdx.x * (uint32_t)TILE_SCAN_CHUNK;
+  for (uint32_t k = 0; k < (uint32_t)TILE_SCAN_CHUNK; k += blockDim.x) {
+    const uint32_t t = b0 + k + threadIdx.x;
+    unsigned long long c, v;
+    tile_counts(A, t, c, v);
+    unsigned long long r = c, u = v, tr, tu;
+    block_scan2(r, u, tr, tu);
+    const unsigned long long cr = carry_r, cu = carry_u;
+    if (t < A.n_tiles) {
+      A.tile_off[t] = cr + r - c;
+      A.tile_cursor[t] = cr + r - c;
+      A.unit_off[t] = cu + u - v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) { carry_r = cr + tr; carry_u = cu + tu; }
+    __syncthreads();
+  }
+}
+
+// End of one generation of a streaming accumulation: totals, largest demands, and the
+// segment ring emptied for the next generation.
+__global__ void k_stream_rotate(Counters* ctr, uint64_t seg_cap) {
+  const unsigned long long s = ctr->seg_count, r = ctr->tile_refs;
+  ctr->seg_total += s < seg_cap ? s : seg_cap;
+  if (s > ctr->seg_max) ctr->seg_max = s;
+  ctr->refs_total += r;
+  if (r > ctr->refs_max) ctr->refs_max = r;
+  ctr->seg_count = 0;
+}
+
 __global__ void k_build_units(RasterArgs A) {
   for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < A.n_tiles; t += gridDim.x * blockDim.x) {
     const uint64_t c = A.tile_count[t], off = A.tile_off[t];
@@ -204,8 +345,9 @@ __global__ void __launch_bounds__(256) k_bin_scatter(RasterArgs A, int smem_tile
     __syncthreads();
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
       RSetup R;
-      if (!raster_setup(A.segs[i], A.W, A.H, R)) continue;
-      for_each_tile(R, A, [&](uint32_t tile) { atomicAdd(&cur[tile], 1u); });
+      const CanvasLoc C = canvas_of_segment(A, i);
+      if (!raster_setup(A.segs[i], C.W, C.H, R)) continue;
+      for_each_tile(R, C, [&](uint32_t tile) { atomicAdd(&cur[tile], 1u); });
     }
     __syncthreads();
     for (uint32_t t = threadIdx.x; t < A.n_tiles; t += blockDim.x) {
@@ -215,8 +357,9 @@ __global__ void __launch_bounds__(256) k_bin_scatter(RasterArgs A, int smem_tile
     __syncthreads();
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
       RSetup R;
-      if (!raster_setup(A.segs[i], A.W, A.H, R)) continue;
-      for_each_tile(R, A, [&](uint32_t tile) {
+      const CanvasLoc C = canvas_of_segment(A, i);
+      if (!raster_setup(A.segs[i], C.W, C.H, R)) continue;
+      for_each_tile(R, C, [&](uint32_t tile) {
         const unsigned slot = atomicAdd(&cur[tile], 1u);
         if (slot < A.refs_cap) A.refs[slot] = (uint32_t)i;
       });
@@ -225,8 +368,9 @@ __global__ void __launch_bounds__(256) k_bin_scatter(RasterArgs A, int smem_tile
   }
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
     RSetup R;
-    if (!raster_setup(A.segs[i], A.W, A.H, R)) continue;
-    for_each_tile(R, A, [&](uint32_t tile) {
+    const CanvasLoc C = canvas_of_segment(A, i);
+    if (!raster_setup(A.segs[i], C.W, C.H, R)) continue;
+    for_each_tile(R, C, [&](uint32_t tile) {
       const unsigned act = __activemask();
       const unsigned grp = __match_any_sync(act, tile);
       const int leader = __ffs(grp) - 1;
@@ -294,11 +438,13 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
     const unsigned long long u = s_unit;
     if (u >= n_units) break;
     const Unit U = A.units[u];
-    const uint32_t tile = U.tile >> 1;
-    const bool xmajor = (U.tile & 1u) == 0;
-    const uint32_t tx = tile % A.ntx, ty = tile / A.ntx;
+    const CanvasLoc C = canvas_of_bin(A, U.tile);
+    const uint32_t lbin = (uint32_t)(U.tile - C.bin_base);
+    const uint32_t tile = lbin >> 1;
+    const bool xmajor = (lbin & 1u) == 0;
+    const uint32_t tx = tile % C.ntx, ty = tile / C.ntx;
     const int tm = xmajor ? (int)tx : (int)ty, tn = xmajor ? (int)ty : (int)tx;
-    const int nmin = (int)(xmajor ? A.H : A.W);
+    const int nmin = (int)(xmajor ? C.H : C.W);
     if (MODE == RM_FIXED_SPLIT) {
       uint4* z = reinterpret_cast<uint4*>(acc32);
       for (int k = threadIdx.x; k < RasterSmem<MODE>::acc_words / 4; k += blockDim.x) z[k] = make_uint4(0, 0, 0, 0);
@@ -322,7 +468,7 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
         sg.x0 = g.x; sg.y0 = g.y; sg.x1 = g.z; sg.y1 = g.w;
         sg.color[0] = cc.x; sg.color[1] = cc.y; sg.color[2] = cc.z; sg.color[3] = cc.w;
         RSetup R;
-        if (raster_setup(sg, A.W, A.H, R)) {
+        if (raster_setup(sg, C.W, C.H, R)) {
           const int c0 = max(R.lo - tm * TILE, 0), c1 = min(R.hi - tm * TILE, TILE);
           cnt = max(c1 - c0, 0);
           st.ua = R.ua; st.va = R.va; st.slope = R.slope;
@@ -413,8 +559,8 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
     for (int k = threadIdx.x; k < TILE_PX; k += blockDim.x) {
       const int row = k / TILE, col = k % TILE;
       const uint32_t x = tx * TILE + col, y = ty * TILE + row;
-      if (x >= A.W || y >= A.H) continue;
-      const uint64_t px = ((uint64_t)y * A.W + x) * 4;
+      if (x >= C.W || y >= C.H) continue;
+      const uint64_t px = (C.px_base + (uint64_t)y * C.W + x) * 4;
       const int cell = xmajor ? row * TILE + col : col * TILE + row;
 #pragma unroll
       for (int ch = 0; ch < 4; ++ch) {
@@ -483,11 +629,13 @@ __global__ void __launch_bounds__(32) k_raster_warp(RasterArgs A) {
     u = __shfl_sync(0xffffffffu, u, 0);
     if (u >= n_units) break;
     const Unit U = A.units[u];
-    const uint32_t tile = U.tile >> 1;
-    const bool xmajor = (U.tile & 1u) == 0;
-    const uint32_t tx = tile % A.ntx, ty = tile / A.ntx;
+    const CanvasLoc C = canvas_of_bin(A, U.tile);
+    const uint32_t lbin = (uint32_t)(U.tile - C.bin_base);
+    const uint32_t tile = lbin >> 1;
+    const bool xmajor = (lbin & 1u) == 0;
+    const uint32_t tx = tile % C.ntx, ty = tile / C.ntx;
     const int tm = xmajor ? (int)tx : (int)ty, tn = xmajor ? (int)ty : (int)tx;
-    const int nmin = (int)(xmajor ? A.H : A.W);
+    const int nmin = (int)(xmajor ? C.H : C.W);
     const int i = tm * TILE + (int)lane;
     for (int k = (int)lane; k < 4 * TILE_PX; k += 32) {
       if (MODE == RM_F32) accf[k] = ident32(B.op[k / TILE_PX]);
@@ -507,7 +655,7 @@ __global__ void __launch_bounds__(32) k_raster_warp(RasterArgs A) {
         sg.x0 = g.x; sg.y0 = g.y; sg.x1 = g.z; sg.y1 = g.w;
         sg.color[0] = cc.x; sg.color[1] = cc.y; sg.color[2] = cc.z; sg.color[3] = cc.w;
         RSetup R;
-        if (raster_setup(sg, A.W, A.H, R)) {
+        if (raster_setup(sg, C.W, C.H, R)) {
           st.ua = R.ua; st.va = R.va; st.slope = R.slope;
           st.lohi = R.lo | (R.hi << 16);
 #pragma unroll
@@ -556,8 +704,8 @@ __global__ void __launch_bounds__(32) k_raster_warp(RasterArgs A) {
       const int jl = k / TILE, c = k % TILE;  // cell k = [minor][lane]
       const uint32_t x = xmajor ? tx * TILE + c : tx * TILE + jl;
       const uint32_t y = xmajor ? ty * TILE + jl : ty * TILE + c;
-      if (x >= A.W || y >= A.H) continue;
-      const uint64_t px = ((uint64_t)y * A.W + x) * 4;
+      if (x >= C.W || y >= C.H) continue;
+      const uint64_t px = (C.px_base + (uint64_t)y * C.W + x) * 4;
 #pragma unroll
       for (int ch = 0; ch < 4; ++ch) {
         const int op = B.op[ch];

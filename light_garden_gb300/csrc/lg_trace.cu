@@ -108,18 +108,22 @@ __device__ inline void primary_ray(const LightDev& L, uint64_t i, double& ox, do
   }
 }
 
+template <bool MULTI>
 __global__ void k_light_setup(SceneDev S) {
-  for (uint32_t l = threadIdx.x; l < S.n_lights; l += blockDim.x) {
+  for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < S.n_lights; l += gridDim.x * blockDim.x) {
     LightDev& L = S.lights[l];
+    const SceneLoc sl = scene_of<MULTI>(S, L.scene);
     df n = DF_ONE;  // tracer.rs:280-287: the last containing object wins
     const df px = df_from_double(L.ox), py = df_from_double(L.oy);
-    for (uint32_t k = 0; k < S.n_obj; ++k) {
+    for (uint32_t k = sl.base; k < sl.base + sl.n; ++k) {
       bool near = false;
       if ((S.info[k].flags & INFO_MATERIAL) && obj_contains64(S, k, px, py, near)) n = S.info[k].n;
     }
     L.n0 = n;
   }
 }
+template __global__ void k_light_setup<false>(SceneDev);
+template __global__ void k_light_setup<true>(SceneDev);
 
 // ------------------------------------------------------------------- one generation
 // Each generation runs as four kernels over the generation's queue (a wavefront), so that
@@ -180,15 +184,15 @@ __device__ __forceinline__ void list_append(const TraceBufs& B, uint32_t gen, in
 // Canvas exit of a ray that hits no object, when its origin is clearly inside the canvas
 // and the exit is clearly not at a corner: the exit face is found in FP32, the exit point
 // computed in double-float.  Anything else takes the precise path in k_bounce.
-__device__ __forceinline__ bool fast_canvas_exit(const SceneDev& S, const RayRec& r, float& x1, float& y1, float& L) {
-  const float ax = S.aspect.hi, ox = r.ox.hi, oy = r.oy.hi, dx = r.dx.hi, dy = r.dy.hi;
+__device__ __forceinline__ bool fast_canvas_exit(const df aspect, const RayRec& r, float& x1, float& y1, float& L) {
+  const float ax = aspect.hi, ox = r.ox.hi, oy = r.oy.hi, dx = r.dx.hi, dy = r.dy.hi;
   if (!(fabsf(ox) < ax - 1e-4f && fabsf(oy) < 1.0f - 1e-4f)) return false;
   const float tx = dx > 0.0f ? (ax - ox) / dx : dx < 0.0f ? (-ax - ox) / dx : INFINITY;
   const float ty = dy > 0.0f ? (1.0f - oy) / dy : dy < 0.0f ? (-1.0f - oy) / dy : INFINITY;
   if (!(fabsf(tx - ty) > 1e-4f * (fminf(tx, ty) + 1.0f))) return false;
   df t;
   if (tx < ty) {
-    const df bound = dx > 0.0f ? S.aspect : -S.aspect;
+    const df bound = dx > 0.0f ? aspect : -aspect;
     t = (bound - r.ox) / r.dx;
   } else {
     const df bound = dy > 0.0f ? DF_ONE : -DF_ONE;
@@ -202,7 +206,7 @@ __device__ __forceinline__ bool fast_canvas_exit(const SceneDev& S, const RayRec
 
 // appends one segment per emitting lane with one atomic per warp (all lanes call)
 __device__ __forceinline__ void emit_segments(const SceneDev& S, const TraceBufs& B, bool emit, const RayRec& r,
-                                              float x1, float y1, uint8_t flags, int hit, uint32_t gen,
+                                              float x1, float y1, uint8_t flags, int hit,
                                               unsigned long long& my_near) {
   const unsigned lane = lane_id();
   const unsigned emask = __ballot_sync(0xffffffffu, emit);
@@ -218,9 +222,10 @@ __device__ __forceinline__ void emit_segments(const SceneDev& S, const TraceBufs
   float4* dst = reinterpret_cast<float4*>(B.segs + slot);
   dst[0] = make_float4(r.ox.hi, r.oy.hi, x1, y1);
   dst[1] = make_float4(r.c[0], r.c[1], r.c[2], r.c[3]);
+  if (B.seg_scene) B.seg_scene[slot] = r.scene;
   if (S.record_paths) {
     lg_path_record pr;
-    pr.path = r.path; pr.primary = r.prim; pr.light = r.light; pr.gen = (uint8_t)gen;
+    pr.path = r.path; pr.primary = r.prim; pr.light = r.light; pr.gen = r.gen;
     pr.flags = flags; pr.hit = hit; pr.source = LG_SRC_TRACE;
     B.paths[slot] = pr;
   }
@@ -246,11 +251,13 @@ struct ScanSmem {  // [slot][lane]: a warp's 32 lanes touch 32 consecutive slots
   PairSlot cand[SCAN_WARPS][CAND][32];
   float4 ray[SCAN_WARPS][32];
   uint32_t src[SCAN_WARPS][32];
+  uint32_t base[SCAN_WARPS][32];
   int off[SCAN_WARPS][33];
 };
 
 int scan_smem_bytes() { return (int)sizeof(ScanSmem); }
 
+template <bool MULTI>
 __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
@@ -260,7 +267,7 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
   if (threadIdx.x == 0) { blk_visits = 0; blk_near = 0; }
   unsigned long long my_visits = 0, my_near = 0;
   bool failed;
-  const ObjScan* objs = stage_objects(S, sobj, &bar, smem_fits != 0, B.ctr, failed);
+  const ObjScan* objs = stage_objects(S, sobj, &bar, !MULTI && smem_fits != 0, B.ctr, failed);
   if (failed) return;
   const uint64_t n_in = n_in_of(S, B, gen);
   RayRec* q = B.queue[gen & 1];
@@ -273,8 +280,11 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
     RayRec r;
     if (live) {
       if (gen == 0) {
-        uint32_t l = 0;
-        while (l + 1 < S.n_lights && S.lights[l + 1].first <= idx) ++l;
+        uint32_t l = 0, lhi = S.n_lights;  // the last light whose first primary is <= idx
+        while (lhi - l > 1) {
+          const uint32_t mid = (l + lhi) >> 1;
+          if (S.lights[mid].first <= idx) l = mid; else lhi = mid;
+        }
         const LightDev& L = S.lights[l];
         const uint64_t i = idx - L.first;
         double pox, poy, pdx, pdy;
@@ -290,6 +300,8 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
         r.light = (uint16_t)l;
         r.gen = 0;
         r.flags = 0;
+        r._pad = 0;
+        r.scene = MULTI ? (uint16_t)L.scene : (uint16_t)0;
         // rounding of the light's ray generator (sin/cos/atan) and the double-float split
         r.ex = DF_ROUND * (1.0f + fabsf(r.ox.hi) + fabsf(r.oy.hi));
         r.ea = DF_ROUND;
@@ -298,75 +310,103 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
         r = q[idx];
       }
     }
-    const bool dead = live && below_cutoff(r.c, S.cutoff);
+    const SceneLoc sl = scene_of<MULTI>(S, live ? r.scene : 0u);
+    const bool dead = live && below_cutoff(r.c, sl.cutoff);
     live = live && !dead;
     const float ox = r.ox.hi, oy = r.oy.hi, dx = r.dx.hi, dy = r.dy.hi;
     W.ray[w][lane] = make_float4(ox, oy, dx, dy);
     W.src[w][lane] = live ? ((uint32_t)r.src_obj << 8 | r.src_leaf) : 0xffffffffu;
+    W.base[w][lane] = sl.base;
     float thr = INFINITY;
     int nc = 0;
     bool overflow = false;
-    for (uint32_t j0 = 0; j0 < S.n_obj; j0 += SCAN_CHUNK) {
-      const uint32_t jn = min((uint32_t)SCAN_CHUNK, S.n_obj - j0);
-      int cnt = 0;
-      for (uint32_t jj = 0; jj < jn; ++jj) {
-        const float4 h = *reinterpret_cast<const float4*>(&objs[j0 + jj]);
-        float lb;
-        if (live && bound_test(h, ox, oy, dx, dy, thr, lb)) {
-          PairSlot ps;
-          ps.key = lb;
-          ps.ub = 0.0f;
-          ps.s = 0.0f;
-          ps.m = j0 + jj;
-          W.pairs[w][cnt++][lane] = ps;
+    // The warp scans one scene at a time: a multi-scene warp (rays of several scenes, at
+    // the seams of the queue) runs one pass per distinct scene with that scene's lanes;
+    // a single-scene warp runs exactly one pass.
+    const unsigned live_mask = __ballot_sync(0xffffffffu, live);
+    const uint32_t my_scene = live ? (uint32_t)r.scene : 0xffffffffu;
+    unsigned pending = MULTI ? live_mask : (live_mask ? 1u : 0u);
+    while (pending) {
+      bool mine;
+      uint32_t g_lo, g_hi;
+      if (MULTI) {
+        const int leader = __ffs(pending) - 1;
+        const uint32_t lead_scene = __shfl_sync(0xffffffffu, my_scene, leader);
+        const unsigned grp = __ballot_sync(0xffffffffu, my_scene == lead_scene);
+        pending &= ~grp;
+        mine = (grp >> lane) & 1u;
+        g_lo = __shfl_sync(0xffffffffu, sl.base, leader);
+        g_hi = g_lo + __shfl_sync(0xffffffffu, sl.n, leader);
+      } else {
+        pending = 0;
+        mine = live;
+        g_lo = 0;
+        g_hi = S.n_obj;
+      }
+      for (uint32_t j0 = g_lo; j0 < g_hi; j0 += SCAN_CHUNK) {
+        const uint32_t jn = min((uint32_t)SCAN_CHUNK, g_hi - j0);
+        int cnt = 0;
+        for (uint32_t jj = 0; jj < jn; ++jj) {
+          const uint32_t j = j0 + jj;
+          const float4 h = *reinterpret_cast<const float4*>(&objs[j]);
+          float lb;
+          if (mine && bound_test(h, ox, oy, dx, dy, thr, lb)) {
+            PairSlot ps;
+            ps.key = lb;
+            ps.ub = 0.0f;
+            ps.s = 0.0f;
+            ps.m = j - g_lo;  // scene-local object index
+            W.pairs[w][cnt++][lane] = ps;
+          }
         }
-      }
-      // flatten the warp's pairs: exclusive scan of the per-lane counts
-      int incl = cnt;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, incl, o);
-        if ((int)lane >= o) incl += y;
-      }
-      W.off[w][lane] = incl - cnt;
-      if (lane == 31) W.off[w][32] = incl;
-      __syncwarp();
-      const int total = W.off[w][32];
-      for (int p = (int)lane; p < total; p += 32) {
-        int lo = 0, hi = 32;  // owner: the last lane whose offset is <= p
-        while (hi - lo > 1) {
-          const int mid = (lo + hi) >> 1;
-          if (W.off[w][mid] <= p) lo = mid; else hi = mid;
+        // flatten the warp's pairs: exclusive scan of the per-lane counts
+        int incl = cnt;
+  #pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, incl, o);
+          if ((int)lane >= o) incl += y;
         }
-        const int k = p - W.off[w][lo];
-        PairSlot& ps = W.pairs[w][k][lo];
-        const uint32_t j = ps.m;
-        const float4 rr = W.ray[w][lo];
-        const uint32_t src = W.src[w][lo];
-        const Class32 c = classify32(objs[j], rr.x, rr.y, rr.z, rr.w, ps.key, (src >> 8) == j ? (int)(src & 0xffu) : -1);
-        PairSlot o;
-        o.key = c.key;
-        o.ub = c.ub;
-        o.s = c.s;
-        o.m = j | ((uint32_t)(c.leaf + 1) << 16) | ((uint32_t)(c.face + 1) << 24);
-        ps = o;
-      }
-      __syncwarp();
-      // fold this lane's results in object order
-      for (int k = 0; k < cnt; ++k) {
-        const PairSlot ps = W.pairs[w][k][lane];
-        if (ps.ub < INFINITY) thr = fminf(thr, ps.ub * (1.0f + 1e-4f) + 1e-4f);
-        if (!(ps.key <= thr)) continue;
-        if (nc == CAND) {  // full: drop candidates the bound has since excluded
-          int wr = 0;
-          for (int q2 = 0; q2 < CAND; ++q2)
-            if (W.cand[w][q2][lane].key <= thr) W.cand[w][wr++][lane] = W.cand[w][q2][lane];
-          nc = wr;
+        W.off[w][lane] = incl - cnt;
+        if (lane == 31) W.off[w][32] = incl;
+        __syncwarp();
+        const int total = W.off[w][32];
+        for (int p = (int)lane; p < total; p += 32) {
+          int lo = 0, hi = 32;  // owner: the last lane whose offset is <= p
+          while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (W.off[w][mid] <= p) lo = mid; else hi = mid;
+          }
+          const int k = p - W.off[w][lo];
+          PairSlot& ps = W.pairs[w][k][lo];
+          const uint32_t j = ps.m;
+          const float4 rr = W.ray[w][lo];
+          const uint32_t src = W.src[w][lo];
+          const Class32 c = classify32(objs[W.base[w][lo] + j], rr.x, rr.y, rr.z, rr.w, ps.key,
+                                       (src >> 8) == j ? (int)(src & 0xffu) : -1);
+          PairSlot o;
+          o.key = c.key;
+          o.ub = c.ub;
+          o.s = c.s;
+          o.m = j | ((uint32_t)(c.leaf + 1) << 16) | ((uint32_t)(c.face + 1) << 24);
+          ps = o;
         }
-        if (nc < CAND) W.cand[w][nc++][lane] = ps;
-        else overflow = true;
+        __syncwarp();
+        // fold this lane's results in object order
+        for (int k = 0; k < cnt; ++k) {
+          const PairSlot ps = W.pairs[w][k][lane];
+          if (ps.ub < INFINITY) thr = fminf(thr, ps.ub * (1.0f + 1e-4f) + 1e-4f);
+          if (!(ps.key <= thr)) continue;
+          if (nc == CAND) {  // full: drop candidates the bound has since excluded
+            int wr = 0;
+            for (int q2 = 0; q2 < CAND; ++q2)
+              if (W.cand[w][q2][lane].key <= thr) W.cand[w][wr++][lane] = W.cand[w][q2][lane];
+            nc = wr;
+          }
+          if (nc < CAND) W.cand[w][nc++][lane] = ps;
+          else overflow = true;
+        }
+        __syncwarp();
       }
-      __syncwarp();
     }
     bool emit = false;
     float x1 = 0.0f, y1 = 0.0f;
@@ -397,7 +437,7 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
         const int leaf = (int)((first.m >> 16) & 0xffu) - 1, face = (int)(first.m >> 24) - 1;
         if (!overflow && m == 1 && first.key == first.ub && leaf >= 0) {
           // a single candidate whose nearest root is certain: only that root is refined
-          const uint32_t oinfo = reinterpret_cast<const uint32_t*>(&objs[sc.cand[0]])[3];
+          const uint32_t oinfo = reinterpret_cast<const uint32_t*>(&objs[sl.base + sc.cand[0]])[3];
           const int kind = leaf_kind_of(oinfo, leaf);
           sc.leaf = (int8_t)leaf;
           sc.face = (int8_t)face;
@@ -410,10 +450,10 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
         } else {
           // no object can be hit: leave through the canvas (tracer.rs:482-488)
           float L;
-          if (fast_canvas_exit(S, r, x1, y1, L)) {
+          if (fast_canvas_exit(sl.aspect, r, x1, y1, L)) {
             emit = true;
             ++my_visits;
-            eflags = r.flags | (near_cutoff(r.c, S.cutoff) || L > ILL_COND ? LG_PATH_NEAR_DEGENERATE : 0);
+            eflags = r.flags | (near_cutoff(r.c, sl.cutoff) || L > ILL_COND ? LG_PATH_NEAR_DEGENERATE : 0);
           } else {
             list = LIST_EXIT;
           }
@@ -422,7 +462,7 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
       B.scan[idx] = sc;
       list_append(B, gen, list, (uint32_t)idx);
     }
-    emit_segments(S, B, emit, r, x1, y1, eflags, -1, gen, my_near);
+    emit_segments(S, B, emit, r, x1, y1, eflags, -1, my_near);
   }
   atomicAdd(&blk_visits, my_visits);
   atomicAdd(&blk_near, my_near);
@@ -433,6 +473,9 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
   }
 }
 
+template __global__ void k_scan<false>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<true>(SceneDev, TraceBufs, uint32_t, int);
+
 __device__ __forceinline__ void store_hit(HitRec& o, int obj, const Hit64& h, float ev, uint8_t flags) {
   o.obj = obj < 0 ? HIT_NONE : (uint16_t)obj;
   o.t = h.t; o.px = h.px; o.py = h.py; o.nx = h.nx; o.ny = h.ny;
@@ -442,6 +485,7 @@ __device__ __forceinline__ void store_hit(HitRec& o, int obj, const Hit64& h, fl
   o.flags = flags;
 }
 
+template <bool MULTI>
 __global__ void __launch_bounds__(256) k_refine(SceneDev S, TraceBufs B, uint32_t gen, int list) {
   unsigned long long n = B.ctr->list_count[gen][list];
   if (n > B.queue_cap) n = B.queue_cap;
@@ -451,7 +495,8 @@ __global__ void __launch_bounds__(256) k_refine(SceneDev S, TraceBufs B, uint32_
     const RayRec r = q[idx];
     const ScanRec sc = B.scan[idx];
     Hit64 h;
-    if (refine_root(S, sc.cand[0], sc.leaf, sc.face, sc.t32, sc.s32, r.ox, r.oy, r.dx, r.dy, h)) {
+    if (refine_root(S, obj_base_of<MULTI>(S, r.scene) + sc.cand[0], sc.leaf, sc.face, sc.t32, sc.s32, r.ox, r.oy,
+                    r.dx, r.dy, h)) {
       store_hit(B.hit[idx], sc.cand[0], h, INFINITY, 0);
     } else {  // cannot refine (degenerate): solve it fully after this kernel
       B.scan[idx].leaf = LEAF_REFINE_FAILED;
@@ -461,13 +506,18 @@ __global__ void __launch_bounds__(256) k_refine(SceneDev S, TraceBufs B, uint32_
   }
 }
 
+template __global__ void k_refine<false>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_refine<true>(SceneDev, TraceBufs, uint32_t, int);
+
+template <bool MULTI>
 __global__ void __launch_bounds__(256) k_full(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
   __shared__ unsigned long long blk_solves;
   if (threadIdx.x == 0) blk_solves = 0;
   bool failed;
-  const ObjScan* objs = stage_objects(S, reinterpret_cast<ObjScan*>(smem_raw), &bar, smem_fits != 0, B.ctr, failed);
+  const ObjScan* objs = stage_objects(S, reinterpret_cast<ObjScan*>(smem_raw), &bar, !MULTI && smem_fits != 0, B.ctr,
+                                      failed);
   if (failed) return;
   unsigned long long n = B.ctr->list_count[gen][LIST_FULL];
   if (n > B.queue_cap) n = B.queue_cap;
@@ -477,6 +527,8 @@ __global__ void __launch_bounds__(256) k_full(SceneDev S, TraceBufs B, uint32_t 
     const uint32_t idx = B.list[LIST_FULL][i];
     const RayRec r = q[idx];
     const ScanRec sc = B.scan[idx];
+    const SceneLoc sl = scene_of<MULTI>(S, r.scene);
+    const ObjScan* sobjs = objs + sl.base;
     df best_d2 = DF_INF, second = DF_INF;
     float ev = INFINITY;
     int best = -1;
@@ -488,7 +540,7 @@ __global__ void __launch_bounds__(256) k_full(SceneDev S, TraceBufs B, uint32_t 
       Hit64 hh;
       df d2;
       ++my_solves;
-      if (obj_solve64(S, j, r.ox, r.oy, r.dx, r.dy, hh, d2, ev)) {
+      if (obj_solve64(S, sl.base + j, r.ox, r.oy, r.dx, r.dy, hh, d2, ev)) {
         if (d2 < best_d2 || (d2 == best_d2 && (int)j < best)) {
           second = best_d2;
           best_d2 = d2;
@@ -503,7 +555,7 @@ __global__ void __launch_bounds__(256) k_full(SceneDev S, TraceBufs B, uint32_t 
       uint32_t pending = (1u << sc.nc) - 1u;
       uint32_t cls[CAND];
       for (int k = 0; k < CAND; ++k)
-        cls[k] = k < sc.nc ? solve_class(reinterpret_cast<const uint32_t*>(&objs[sc.cand[k]])[3]) : 7u;
+        cls[k] = k < sc.nc ? solve_class(reinterpret_cast<const uint32_t*>(&sobjs[sc.cand[k]])[3]) : 7u;
       const unsigned am = __activemask();
       for (uint32_t c = 0; c < N_SOLVE_CLASSES; ++c) {
         for (;;) {
@@ -519,11 +571,11 @@ __global__ void __launch_bounds__(256) k_full(SceneDev S, TraceBufs B, uint32_t 
       }
     } else {  // list overflow (rare): every object that passes the FP32 filters, in order
       const float ox = r.ox.hi, oy = r.oy.hi, dx = r.dx.hi, dy = r.dy.hi;
-      for (uint32_t j = 0; j < S.n_obj; ++j) {
-        const float4 h = *reinterpret_cast<const float4*>(&objs[j]);
+      for (uint32_t j = 0; j < sl.n; ++j) {
+        const float4 h = *reinterpret_cast<const float4*>(&sobjs[j]);
         float lb;
         if (!bound_test(h, ox, oy, dx, dy, sc.thr, lb)) continue;
-        if (!(classify32(objs[j], ox, oy, dx, dy, lb, j == r.src_obj ? (int)r.src_leaf : -1).key <= sc.thr)) continue;
+        if (!(classify32(sobjs[j], ox, oy, dx, dy, lb, j == r.src_obj ? (int)r.src_leaf : -1).key <= sc.thr)) continue;
         consider(j);
       }
     }
@@ -535,6 +587,8 @@ __global__ void __launch_bounds__(256) k_full(SceneDev S, TraceBufs B, uint32_t 
   __syncthreads();
   if (threadIdx.x == 0) atomicAdd(&B.ctr->fp64_solves, blk_solves);
 }
+template __global__ void k_full<false>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_full<true>(SceneDev, TraceBufs, uint32_t, int);
 
 struct Bounce {
   bool emit;
@@ -545,12 +599,14 @@ struct Bounce {
   RayRec child[2];
 };
 
+template <bool MULTI>
 __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, const RayRec& r, const ScanRec& sc,
-                                       const HitRec* hrec, uint32_t gen, Bounce& v) {
+                                       const HitRec* hrec, Bounce& v) {
   v.emit = false;
   v.nchild = 0;
+  const SceneLoc sl = scene_of<MULTI>(S, r.scene);
   uint8_t fl = r.flags;
-  if (near_cutoff(r.c, S.cutoff)) fl |= LG_PATH_NEAR_DEGENERATE;
+  if (near_cutoff(r.c, sl.cutoff)) fl |= LG_PATH_NEAR_DEGENERATE;
   const df ox = r.ox, oy = r.oy, dx = r.dx, dy = r.dy;
   HitRec bh;
   bh.obj = HIT_NONE;
@@ -562,7 +618,7 @@ __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, c
   if (best >= 0 ? bh.ev <= bh.t.hi * (1.0f + 1e-6f) + 1e-12f : bh.ev < INFINITY) fl |= LG_PATH_NEAR_DEGENERATE;
 
   if (best >= 0) {
-    const ObjInfo oi = S.info[best];
+    const ObjInfo oi = S.info[sl.base + best];
     v.emit = true;
     v.x1 = bh.px.hi; v.y1 = bh.py.hi;
     v.hit = best;
@@ -578,17 +634,17 @@ __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, c
       df n2 = DF_ONE;
       uint16_t m2 = MEDIUM_AIR;
       bool near = false;
-      if (obj_contains64(S, (uint32_t)best, DF_HALF * (ox + bh.px), DF_HALF * (oy + bh.py), near)) {
+      if (obj_contains64(S, sl.base + (uint32_t)best, DF_HALF * (ox + bh.px), DF_HALF * (oy + bh.py), near)) {
         const float px32 = bh.px.hi, py32 = bh.py.hi;
-        for (uint32_t k = 0; k < S.n_obj; ++k) {
+        for (uint32_t k = 0; k < sl.n; ++k) {
           if ((int)k == best) continue;
-          const float4 h = *reinterpret_cast<const float4*>(&objs[k]);
+          const float4 h = *reinterpret_cast<const float4*>(&objs[sl.base + k]);
           if (!(__float_as_uint(h.w) & INFO_MATERIAL)) continue;
           const float ex = px32 - h.x, ey = py32 - h.y;
           const float tol = 2e-6f * (fabsf(px32) + fabsf(py32) + fabsf(h.x) + fabsf(h.y) + h.z) + 1e-6f;
           if (ex * ex + ey * ey > (h.z + tol) * (h.z + tol)) continue;
-          if (obj_contains64(S, k, bh.px, bh.py, near)) {
-            n2 = S.info[k].n;
+          if (obj_contains64(S, sl.base + k, bh.px, bh.py, near)) {
+            n2 = S.info[sl.base + k].n;
             m2 = (uint16_t)k;
             break;
           }
@@ -603,7 +659,7 @@ __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, c
       df ci = -ddn;
       if (df_neg(ci)) { ci = -ci; nx = -nx; ny = -ny; }
       const df n1 = r.medium == MEDIUM_AIR ? DF_ONE
-                    : r.medium == MEDIUM_LIGHT ? S.lights[r.light].n0 : S.info[r.medium].n;
+                    : r.medium == MEDIUM_LIGHT ? S.lights[r.light].n0 : S.info[sl.base + r.medium].n;
       const df eta = n1 / n2;
       const df k = DF_ONE - eta * eta * (DF_ONE - ci * ci);
       if (fabsf(k.hi) <= 1e-10f) fl |= LG_PATH_NEAR_DEGENERATE;
@@ -646,7 +702,7 @@ __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, c
         t.src_leaf = bh.leaf;
         t.c[0] = __fmul_rn(r.c[0], om); t.c[1] = __fmul_rn(r.c[1], om); t.c[2] = __fmul_rn(r.c[2], om);
         t.c[3] = r.c[3];
-        t.path = r.path | (1ull << gen);
+        t.path = r.path | (1ull << r.gen);
         t.flags = fl;
         const float gain = eta.hi * ci.hi / fmaxf(ct.hi, 1e-6f);
         t.ex = ds * ct.hi + L;
@@ -673,7 +729,7 @@ __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, c
     Leaf64 canvas;
     canvas.kind = LEAF_RECT;
     canvas.p[0] = DF_ZERO; canvas.p[1] = DF_ZERO; canvas.p[2] = DF_ONE; canvas.p[3] = DF_ZERO;
-    canvas.p[4] = S.aspect; canvas.p[5] = DF_ONE;
+    canvas.p[4] = sl.aspect; canvas.p[5] = DF_ONE;
     Hit64 ch[3];
     float cev = INFINITY;
     const int nh = leaf_hits64(canvas, ox, oy, dx, dy, ch, cev);
@@ -692,23 +748,27 @@ __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, c
   int w = 0;
   for (int q = 0; q < v.nchild; ++q) {
     RayRec c = v.child[q];
-    if (gen + 1 >= S.max_bounce || below_cutoff(c.c, S.cutoff)) continue;
-    c.gen = (uint8_t)(gen + 1);
+    if ((uint32_t)r.gen + 1 >= sl.max_bounce || below_cutoff(c.c, sl.cutoff)) continue;
+    c.gen = (uint8_t)(r.gen + 1);
     c.prim = r.prim;
     c.light = r.light;
-    if (near_cutoff(c.c, S.cutoff) || !(c.ex <= ILL_COND && c.ea <= ILL_COND)) c.flags |= LG_PATH_NEAR_DEGENERATE;
+    c._pad = 0;
+    c.scene = r.scene;
+    if (near_cutoff(c.c, sl.cutoff) || !(c.ex <= ILL_COND && c.ea <= ILL_COND)) c.flags |= LG_PATH_NEAR_DEGENERATE;
     v.child[w++] = c;
   }
   v.nchild = w;
 }
 
+template <bool MULTI>
 __global__ void __launch_bounds__(256) k_bounce(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
   __shared__ unsigned long long blk_visits, blk_near;
   if (threadIdx.x == 0) { blk_visits = 0; blk_near = 0; }
   bool failed;
-  const ObjScan* objs = stage_objects(S, reinterpret_cast<ObjScan*>(smem_raw), &bar, smem_fits != 0, B.ctr, failed);
+  const ObjScan* objs = stage_objects(S, reinterpret_cast<ObjScan*>(smem_raw), &bar, !MULTI && smem_fits != 0, B.ctr,
+                                      failed);
   if (failed) return;
   // the rays with work: every work list of this generation, one after the other
   uint64_t off[N_LISTS + 1];
@@ -740,10 +800,10 @@ __global__ void __launch_bounds__(256) k_bounce(SceneDev S, TraceBufs B, uint32_
       if (!(l < LIST_FULL && sc.leaf == LEAF_REFINE_FAILED)) {  // those are in the full list too
         r = qin[idx];
         ++my_visits;
-        bounce(S, objs, r, sc, &B.hit[idx], gen, v);
+        bounce<MULTI>(S, objs, r, sc, &B.hit[idx], v);
       }
     }
-    emit_segments(S, B, v.emit, r, v.x1, v.y1, v.flags, v.hit, gen, my_near);
+    emit_segments(S, B, v.emit, r, v.x1, v.y1, v.flags, v.hit, my_near);
     // children: warp prefix sum of 0..2 per lane, one atomic per warp
     int incl = v.nchild;
 #pragma unroll
@@ -769,19 +829,23 @@ __global__ void __launch_bounds__(256) k_bounce(SceneDev S, TraceBufs B, uint32_
     atomicAdd(&B.ctr->near, blk_near);
   }
 }
+template __global__ void k_bounce<false>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_bounce<true>(SceneDev, TraceBufs, uint32_t, int);
 
 // ------------------------------------------------------------------- overlays
 // Curved-mirror control lines (tracer.rs:341-346) and the string-mod chords
 // (string_mod.rs:45-55, 104-122) appended after the traced segments.
-__global__ void k_overlay(SceneDev S, TraceBufs B, const uint32_t* cubic_objs, uint32_t n_cubic,
-                          lg_string_mod sm) {
+__global__ void k_overlay(SceneDev S, TraceBufs B, const uint32_t* cubic_objs, const uint16_t* cubic_scene,
+                          uint32_t n_cubic, lg_string_mod sm) {
   const uint64_t n_ctrl = 3ull * n_cubic;
   const uint64_t total = n_ctrl + sm.modulo;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
     lg_segment s;
     lg_path_record pr;
     pr.path = 0; pr.light = 0xffff; pr.flags = 0; pr.hit = -1;
+    uint16_t scene = 0;
     if (i < n_ctrl) {
+      if (cubic_scene) scene = cubic_scene[i / 3];
       const uint32_t k = cubic_objs[i / 3];
       const int q = (int)(i % 3);
       const Leaf64& L = S.leaves[S.info[k].leaf_begin];
@@ -811,6 +875,7 @@ __global__ void k_overlay(SceneDev S, TraceBufs B, const uint32_t* cubic_objs, u
     const unsigned long long slot = atomicAdd(&B.ctr->seg_count, 1ull);
     if (slot < B.seg_cap) {
       B.segs[slot] = s;
+      if (B.seg_scene) B.seg_scene[slot] = scene;
       if (S.record_paths) B.paths[slot] = pr;
     }
   }

@@ -117,6 +117,41 @@ class Context:
         self._check(st, "lg_segments_download")
         return (segs, recs) if paths else segs
 
+    # -- many scenes -------------------------------------------------------------------------
+    def batch_upload(self, scenes) -> None:
+        """Upload a batch of PackedScene (lg_batch_upload)."""
+        descs = (abi.lg_scene_desc * len(scenes))()
+        for d, sc in zip(descs, scenes):
+            d.geos = C.cast(sc.geos, C.POINTER(abi.lg_geo))
+            d.objects = C.cast(sc.objects, C.POINTER(abi.lg_object))
+            d.lights = C.cast(sc.lights, C.POINTER(abi.lg_light))
+            d.params = C.pointer(sc.params)
+            d.n_geo, d.n_objects, d.n_lights = sc.n_geo, sc.n_objects, sc.n_lights
+        self._check(self.lib.lg_batch_upload(self.h, descs, len(scenes)), "lg_batch_upload")
+        self.batch_shapes = [(sc.params.height, sc.params.width) for sc in scenes]
+        self.batch_offsets = []
+        for i in range(len(scenes)):
+            off = C.c_uint64(0)
+            self._check(self.lib.lg_batch_image_offset(self.h, i, C.byref(off)), "lg_batch_image_offset")
+            self.batch_offsets.append(int(off.value))
+        self.params = None
+
+    def batch_pixels(self) -> int:
+        return sum(h * w for h, w in self.batch_shapes)
+
+    def batch_render_into(self, ptr: int, nbytes: int, on_device: bool) -> dict:
+        s = abi.lg_trace_stats()
+        st = self.lib.lg_batch_render(self.h, C.c_void_p(ptr), nbytes, 1 if on_device else 0, C.byref(s))
+        self._check(st, "lg_batch_render")
+        return s.as_dict()
+
+    def batch_render(self):
+        """All images of the batch as a list of (height, width, 4) binary16 bit patterns."""
+        flat = np.zeros(self.batch_pixels() * 4, np.uint16)
+        stats = self.batch_render_into(flat.ctypes.data, flat.nbytes, False)
+        imgs = [flat[4 * o:4 * (o + h * w)].reshape(h, w, 4) for o, (h, w) in zip(self.batch_offsets, self.batch_shapes)]
+        return imgs, stats
+
     def accum(self) -> np.ndarray:
         h, w = self._shape()
         dt = np.float32 if self.params.accum == abi.LG_ACCUM_F32 else np.int64
