@@ -291,6 +291,90 @@ def run_ours(args, ws, rank, local):
     ctx.close()
 
 
+BATCH_WORKLOAD = ("batch: 512 seeded scenes (seed 4): objects log-uniform [4, 1024], rays log-uniform [2^12, 2^20], "
+                  "bounces U{4..32}, canvases {256, 512, 1024, 2048}^2, int64 accumulation")
+
+
+def run_batch(args, ws, rank, local):
+    """Mixed-size batch: all scenes in one multi-scene trace (lg_batch_render, one captured
+    graph) against the plain path rendering the same scenes one after another (lg_render)."""
+    import torch
+
+    from light_garden_gb300 import workloads as W
+    from light_garden_gb300.runtime import Context
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    ws_ = W.batch_scenes(count=args.batch_scenes)
+    if args.ray_scale != 1.0:
+        ws_ = [W.scale_rays(w, args.ray_scale) for w in ws_]
+    scenes = [w.packed() for w in ws_]
+    n = len(scenes)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    # batched path
+    ctx = Context(device=local, raster_variant=args.raster_variant)
+    ctx.batch_upload(scenes)
+    out = torch.empty(ctx.batch_pixels() * 4, dtype=torch.int16, device=dev)
+    for _ in range(max(1, args.warmup)):
+        st = ctx.batch_render_into(out.data_ptr(), out.numel() * 2, True)
+    torch.cuda.synchronize()
+    barrier(ws)
+    tot = 0.0
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            st = ctx.batch_render_into(out.data_ptr(), out.numel() * 2, True)
+            tot += st["total_ms"]
+    ms = tot / args.steps
+    value, ms_max = aggregate(ws, n, ms, dev)
+    # end to end: scene tables from the host, every image back to pinned host memory
+    host = torch.empty(out.numel(), dtype=torch.int16, pin_memory=True)
+    t0 = time.perf_counter()
+    ctx.batch_upload(scenes)
+    ctx.batch_render_into(host.data_ptr(), host.numel() * 2, False)
+    e2e_s = time.perf_counter() - t0
+    e2e_value, _ = aggregate(ws, n, e2e_s * 1e3, dev)
+    segs, pixels = st["segments"], st["pixels"]
+    ctx.close()
+    # plain path: the same scenes one by one through lg_render (device output)
+    plain = Context(device=local)
+    big = torch.empty(max(pk.params.width * pk.params.height for pk in scenes) * 4, dtype=torch.int16, device=dev)
+    lat = []
+    for pk in scenes[:4]:
+        plain.upload(pk)
+        plain.render_into(big.data_ptr(), pk.params.width * 8, True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for pk in scenes:
+        a = time.perf_counter()
+        plain.upload(pk)
+        plain.render_into(big.data_ptr(), pk.params.width * 8, True)
+        lat.append((time.perf_counter() - a) * 1e3)
+    plain_s = time.perf_counter() - t0
+    plain.close()
+    if rank == 0:
+        lat_sorted = sorted(lat)
+        pct = lambda q: lat_sorted[min(len(lat_sorted) - 1, int(q * len(lat_sorted)))]
+        out_line = {
+            "metric": "scenes/s, mixed-size batch (batched multi-scene trace vs plain one-scene path)",
+            "value": value, "unit": "scenes/s", "n_gpus": ws, "steps": args.steps, "warmup": max(1, args.warmup),
+            "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32 + double-float trace, int64 accumulate", "data": "synthetic",
+            "config": {"workload": BATCH_WORKLOAD + ("" if args.ray_scale == 1.0 else f", rays x {args.ray_scale}"),
+                       "scenes": n, "l2": "flushed between steps (512 MB write)"},
+            "segments_per_step": segs, "pixels_per_step": pixels,
+            "e2e": {"value": e2e_value, "unit": "scenes/s", "h2d_bytes_per_step": None,
+                    "d2h_bytes_per_step": host.numel() * 2, "ms_per_step": e2e_s * 1e3},
+            "plain": {"scenes_per_s": n / plain_s, "wall_s": plain_s, "p50_ms": pct(0.5), "p99_ms": pct(0.99)},
+            "batched_vs_plain": value / (n / plain_s),
+            "batch_latency_ms": ms_max,
+            "gpu_launches": None,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(out_line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -303,10 +387,16 @@ def main():
     ap.add_argument("--rays-per-light", type=int, default=1 << 18)
     ap.add_argument("--raster-variant", type=int, default=0, choices=[0, 1, 2],
                     help="0: autotuned; 1: shared-memory tile atomics; 2: warp-private tiles")
+    # the mixed-size batch configuration (not the default line)
+    ap.add_argument("--workload", default="mid", choices=["mid", "batch"])
+    ap.add_argument("--batch-scenes", type=int, default=512)
+    ap.add_argument("--ray-scale", type=float, default=1.0)
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, ws, rank)
+    elif args.workload == "batch":
+        run_batch(args, ws, rank, local)
     else:
         run_ours(args, ws, rank, local)
     if ws > 1:

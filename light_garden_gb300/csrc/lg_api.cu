@@ -324,6 +324,7 @@ SceneDev scene_dev(lg_ctx* c) {
   S.max_bounce = c->prm.max_bounce;
   S.record_paths = c->prm.record_paths ? 1u : 0u;
   S.scenes = nullptr;
+  S.bounds = nullptr;
   S.n_scenes = 1;
   S._pad = 0;
   return S;
@@ -340,6 +341,7 @@ TraceBufs trace_bufs(lg_ctx* c) {
   B.segs = (lg_segment*)c->d_segs.p;
   B.paths = (lg_path_record*)c->d_paths.p;
   B.seg_scene = nullptr;
+  B.order = nullptr;
   B.seg_cap = c->seg_cap;
   B.ctr = (Counters*)c->d_ctr.p;
   return B;
@@ -664,7 +666,8 @@ lg_status lg_destroy(lg_ctx* c) {
                     &c->d_queue[1], &c->d_scanrec, &c->d_hitrec, &c->d_list[0], &c->d_list[1], &c->d_list[2],
                     &c->d_list[3], &c->d_list[4], &c->d_list[5], &c->d_segs, &c->d_paths, &c->d_ctr, &c->d_tile_count, &c->d_tile_off,
                     &c->d_tile_cursor, &c->d_unit_off, &c->d_refs, &c->d_units, &c->d_accum, &c->d_stage,
-                    &c->d_scenes, &c->d_canvases, &c->d_seg_scene, &c->d_cubic_scene, &c->d_part};
+                    &c->d_scenes, &c->d_canvases, &c->d_seg_scene, &c->d_cubic_scene, &c->d_part,
+                    &c->d_bounds, &c->d_order, &c->d_scene_count, &c->d_scene_off};
   for (DevBuf* b : bufs) release(*b);
   if (c->h_ctr) cudaFreeHost(c->h_ctr);
   for (int i = 0; i < 6; ++i)

@@ -19,7 +19,8 @@ using namespace lgd;
 namespace lgh {
 namespace {
 
-constexpr uint32_t SMALL_BINS = 32768;  // up to this many bins the single-CTA tile scan is used
+constexpr uint32_t SMALL_BINS = 32768;          // up to this many bins the single-CTA tile scan is used
+constexpr uint64_t RING_SEGMENTS = 256ull << 20;  // segment ring of a batch (8.5 GB with scene ids)
 
 lg_status batch_buffers(lg_ctx* c) {
   lg_status st;
@@ -38,6 +39,7 @@ lg_status batch_buffers(lg_ctx* c) {
   if ((st = ensure(c, c->d_units, c->units_cap * sizeof(Unit), "raster units"))) return st;
   const size_t parts = (bins + TILE_SCAN_CHUNK - 1) / TILE_SCAN_CHUNK;
   if ((st = ensure(c, c->d_part, std::max<size_t>(parts, 1) * 16, "tile scan partials"))) return st;
+  if ((st = ensure(c, c->d_order, c->queue_cap * 4, "scene order"))) return st;
   return LG_OK;
 }
 
@@ -46,6 +48,7 @@ SceneDev batch_scene_dev(lg_ctx* c) {
   S.n_obj = c->n_obj;
   S.max_bounce = c->max_bounce_all;
   S.scenes = (const SceneRec*)c->d_scenes.p;
+  S.bounds = (const float4*)c->d_bounds.p;
   S.n_scenes = c->n_scenes;
   return S;
 }
@@ -70,10 +73,12 @@ lg_status enqueue_batch(lg_ctx* c, cudaEvent_t* ev) {
   const SceneDev S = batch_scene_dev(c);
   TraceBufs B = trace_bufs(c);
   B.seg_scene = (uint16_t*)c->d_seg_scene.p;
+  B.order = (const uint32_t*)c->d_order.p;
   const RasterArgs A = batch_raster_args(c);
   const int fixed = c->prm.accum == LG_ACCUM_FIXED64;
   CK(cudaEventRecordWithFlags(ev[0], c->stream, cudaEventRecordExternal), "stage event");
   CK(cudaMemsetAsync(c->d_ctr.p, 0, sizeof(Counters), c->stream), "memset counters");
+  CK(cudaMemsetAsync(c->d_scene_count.p, 0, (size_t)c->n_scenes * 4, c->stream), "memset scene counts");
   k_clear_accum<<<c->n_sm * 8, 256, 0, c->stream>>>(A, fixed);
   if (c->n_lights) k_light_setup<true><<<(c->n_lights + 127) / 128, 128, 0, c->stream>>>(S);
   const uint32_t bins = c->total_bins;
@@ -85,6 +90,13 @@ lg_status enqueue_batch(lg_ctx* c, cudaEvent_t* ev) {
   lg_string_mod no_sm;
   std::memset(&no_sm, 0, sizeof no_sm);
   for (uint32_t g = 0; g < c->max_bounce_all; ++g) {
+    if (g > 0) {  // visit this generation's queue in scene order
+      k_scene_hist<<<c->n_sm * 8, 256, 0, c->stream>>>(S, B, g, (unsigned*)c->d_scene_count.p);
+      k_scene_offsets<<<1, 1024, 0, c->stream>>>((unsigned*)c->d_scene_count.p, (unsigned*)c->d_scene_off.p,
+                                                  c->n_scenes);
+      k_scene_scatter<<<c->n_sm * 8, 256, 0, c->stream>>>(S, B, g, (unsigned*)c->d_scene_off.p,
+                                                          (uint32_t*)c->d_order.p);
+    }
     k_scan<true><<<c->batch_grid_scan, SCAN_THREADS, (size_t)scan_smem_bytes(), c->stream>>>(S, B, g, 0);
     for (int l = LIST_REFINE_CIRCLE; l <= LIST_REFINE_CUBIC; ++l)
       k_refine<true><<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g, l);
@@ -96,7 +108,10 @@ lg_status enqueue_batch(lg_ctx* c, cudaEvent_t* ev) {
                                                (const uint16_t*)c->d_cubic_scene.p, c->n_cubic, no_sm);
     }
     CK(cudaEventRecordWithFlags(ev[1 + 2 * g], c->stream, cudaEventRecordExternal), "stage event");
-    CK(cudaMemsetAsync(c->d_tile_count.p, 0, (size_t)bins * 4, c->stream), "memset tile counts");
+    // accumulate when the ring is full enough (every kernel below returns at once otherwise)
+    k_stream_decide<<<1, 1, 0, c->stream>>>((Counters*)c->d_ctr.p, g, c->seg_cap, c->queue_cap,
+                                             g + 1 == c->max_bounce_all ? 1 : 0);
+    k_clear_counts<<<c->n_sm * 4, 256, 0, c->stream>>>(A);
     k_bin_count<<<c->bin_grid, 256, bsm, c->stream>>>(A, smem_tiles);
     if (bins <= SMALL_BINS) {
       k_scan_tiles<<<1, 1024, 0, c->stream>>>(A);
@@ -278,6 +293,11 @@ lg_status lg_batch_upload(lg_ctx* c, const lg_scene_desc* scenes, uint32_t k) {
   if ((st = up(c->d_cubic_scene, cubic_scene.data(), cubic_scene.size() * 2, "scene"))) return st;
   if ((st = up(c->d_scenes, recs.data(), recs.size() * sizeof(SceneRec), "scene table"))) return st;
   if ((st = up(c->d_canvases, canv.data(), canv.size() * sizeof(SceneCanvas), "canvas table"))) return st;
+  std::vector<float4> bounds(F.scan.size());
+  for (size_t i = 0; i < F.scan.size(); ++i) std::memcpy(&bounds[i], &F.scan[i], sizeof(float4));
+  if ((st = up(c->d_bounds, bounds.data(), bounds.size() * sizeof(float4), "object bounds"))) return st;
+  if ((st = ensure(c, c->d_scene_count, (size_t)k * 4, "scene counts"))) return st;
+  if ((st = ensure(c, c->d_scene_off, (size_t)k * 4, "scene offsets"))) return st;
   CK(cudaStreamSynchronize(c->stream), "upload");
   c->n_scenes = k;
   c->h_scenes = recs;
@@ -297,10 +317,15 @@ lg_status lg_batch_upload(lg_ctx* c, const lg_scene_desc* scenes, uint32_t k) {
   c->total_px = total_px;
   c->total_bins = (uint32_t)total_bins;
   c->max_bounce_all = max_b;
-  // one generation at a time: the ring holds the widest generation (one segment per ray)
+  // The ring holds at least the widest generation (one segment per ray); beyond that it is
+  // sized so that several generations are accumulated in one pass (RING_SEGMENTS, or an
+  // eighth of free device memory).
   const uint64_t want_q = std::max<uint64_t>(c->queue_cap_hint, n_primary + n_primary / 2 + 1024);
   c->queue_cap = std::max(c->queue_cap, want_q);
-  c->seg_cap = std::max(c->seg_cap, c->queue_cap + c->n_overlay);
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  const uint64_t ring = std::min<uint64_t>(RING_SEGMENTS, free_b / 8 / (sizeof(lg_segment) + 2));
+  c->seg_cap = std::max(c->seg_cap, std::max(c->queue_cap + c->n_overlay, std::max<uint64_t>(ring, c->seg_cap_hint)));
   c->refs_cap = std::max<uint64_t>(c->refs_cap, std::min<uint64_t>(4 * c->seg_cap + 4096, 0xfffffff0ull));
   if ((st = batch_buffers(c))) return st;
   // launch shapes: the multi-scene kernels read the object tables from global memory

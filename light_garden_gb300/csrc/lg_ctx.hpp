@@ -63,6 +63,7 @@ struct lg_ctx {
   std::vector<SceneCanvas> h_canvases;
   std::vector<uint64_t> h_px_base;       // first pixel of each scene's image
   DevBuf d_scenes, d_canvases, d_seg_scene, d_cubic_scene, d_part;
+  DevBuf d_bounds, d_order, d_scene_count, d_scene_off;
   uint64_t total_px = 0;
   uint32_t total_bins = 0;
   uint32_t max_bounce_all = 0;

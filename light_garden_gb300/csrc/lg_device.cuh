@@ -141,7 +141,7 @@ struct Counters {
   // generation; these keep the totals and the largest per-generation demands
   unsigned long long seg_total, seg_max, refs_total, refs_max;
   unsigned int error_flags;
-  unsigned int _pad;
+  unsigned int skip_raster;  // streaming accumulation: this generation's accumulation is deferred
 };
 constexpr unsigned ERR_TMA_TIMEOUT = 1u;
 
@@ -169,6 +169,7 @@ struct SceneDev {
   uint32_t max_bounce;    // multi-scene: the largest of the scenes
   uint32_t record_paths;
   const SceneRec* scenes; // multi-scene traces only
+  const float4* bounds;   // multi-scene: bounding circle + info word of every object (ObjScan's first 16 B)
   uint32_t n_scenes;
   uint32_t _pad;
 };
@@ -235,6 +236,7 @@ struct TraceBufs {
   lg_segment* segs;
   lg_path_record* paths;
   uint16_t* seg_scene;      // multi-scene traces: the scene of every segment
+  const uint32_t* order;    // multi-scene traces, generations > 0: queue entries sorted by scene
   uint64_t seg_cap;
   Counters* ctr;
 };

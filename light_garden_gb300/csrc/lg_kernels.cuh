@@ -60,6 +60,9 @@ template <bool MULTI>
 __global__ void k_bounce(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
 __global__ void k_overlay(SceneDev S, TraceBufs B, const uint32_t* cubic_objs, const uint16_t* cubic_scene,
                           uint32_t n_cubic, lg_string_mod sm);
+__global__ void k_scene_hist(SceneDev S, TraceBufs B, uint32_t gen, unsigned* count);
+__global__ void k_scene_offsets(unsigned* count, unsigned* off, uint32_t n_scenes);
+__global__ void k_scene_scatter(SceneDev S, TraceBufs B, uint32_t gen, unsigned* off, uint32_t* order);
 
 __global__ void k_clear_accum(RasterArgs A, int fixed);
 __global__ void k_bin_count(RasterArgs A, int smem_tiles);
@@ -76,6 +79,8 @@ constexpr int RM_FIXED_SPLIT_ = 0, RM_FIXED_MINMAX_ = 1, RM_F32_ = 2;
 constexpr uint32_t MAX_SMEM_TILES = 32768;  // tile bins (2 per tile) with 32-bit counters in 128 KB
 // multi-scene streaming accumulation
 __global__ void k_stream_rotate(Counters* ctr, uint64_t seg_cap);
+__global__ void k_stream_decide(Counters* ctr, uint32_t gen, uint64_t seg_cap, uint64_t queue_cap, int last);
+__global__ void k_clear_counts(RasterArgs A);
 constexpr int TILE_SCAN_CHUNK = 4096;  // bins per CTA of the multi-block tile scan
 __global__ void k_tiles_partial(RasterArgs A, unsigned long long* part);
 __global__ void k_tiles_scan_partials(RasterArgs A, unsigned long long* part, uint32_t n_part);

@@ -130,6 +130,7 @@ __device__ __forceinline__ uint64_t n_segments(const RasterArgs& A) {
 // atomic per touched tile per CTA.  Falls back to warp-aggregated global atomics when the
 // tile count does not fit (smem_tiles == 0).
 __global__ void __launch_bounds__(256) k_bin_count(RasterArgs A, int smem_tiles) {
+  if (A.ctr->skip_raster) return;
   extern __shared__ unsigned hist[];
   const uint64_t n = n_segments(A);
   if (smem_tiles) {
@@ -160,6 +161,7 @@ __global__ void __launch_bounds__(256) k_bin_count(RasterArgs A, int smem_tiles)
 
 // single-CTA exclusive scan of refs and units per tile
 __global__ void __launch_bounds__(1024) k_scan_tiles(RasterArgs A) {
+  if (A.ctr->skip_raster) return;
   __shared__ unsigned long long wsum_r[32], wsum_u[32];
   __shared__ unsigned long long carry_r, carry_u;
   if (threadIdx.x == 0) { carry_r = 0; carry_u = 0; }
@@ -250,6 +252,7 @@ __device__ __forceinline__ void block_scan2(unsigned long long& r, unsigned long
 }
 
 __global__ void __launch_bounds__(1024) k_tiles_partial(RasterArgs A, unsigned long long* part) {
+  if (A.ctr->skip_raster) return;
   const uint32_t b0 = blockIdx.x * (uint32_t)TILE_SCAN_CHUNK;
   unsigned long long r = 0, u = 0;
   for (uint32_t k = threadIdx.x; k < (uint32_t)TILE_SCAN_CHUNK; k += blockDim.x) {
@@ -264,6 +267,7 @@ __global__ void __launch_bounds__(1024) k_tiles_partial(RasterArgs A, unsigned l
 }
 
 __global__ void __launch_bounds__(1024) k_tiles_scan_partials(RasterArgs A, unsigned long long* part, uint32_t n_part) {
+  if (A.ctr->skip_raster) return;
   __shared__ unsigned long long carry_r, carry_u;
   if (threadIdx.x == 0) { carry_r = 0; carry_u = 0; }
   __syncthreads();
@@ -286,6 +290,7 @@ __global__ void __launch_bounds__(1024) k_tiles_scan_partials(RasterArgs A, unsi
 }
 
 __global__ void __launch_bounds__(1024) k_tiles_apply(RasterArgs A, const unsigned long long* part) {
+  if (A.ctr->skip_raster) return;
   __shared__ unsigned long long carry_r, carry_u;
   if (threadIdx.x == 0) { carry_r = part[2 * blockIdx.x]; carry_u = part[2 * blockIdx.x + 1]; }
   __syncthreads();
@@ -308,9 +313,24 @@ __global__ void __launch_bounds__(1024) k_tiles_apply(RasterArgs A, const unsign
   }
 }
 
+// After each generation of a streaming accumulation: accumulate now only if the ring could
+// not take the next generation (one segment per queued ray at most), or nothing follows.
+__global__ void k_stream_decide(Counters* ctr, uint32_t gen, uint64_t seg_cap, uint64_t queue_cap, int last) {
+  const unsigned long long next = ctr->queue_count[gen + 1];
+  const unsigned long long nxt = next < queue_cap ? next : queue_cap;
+  const bool go = last || next == 0 || ctr->seg_count + nxt > seg_cap;
+  ctr->skip_raster = go ? 0u : 1u;
+}
+
+__global__ void k_clear_counts(RasterArgs A) {
+  if (A.ctr->skip_raster) return;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < A.n_tiles; t += gridDim.x * blockDim.x) A.tile_count[t] = 0u;
+}
+
 // End of one generation of a streaming accumulation: totals, largest demands, and the
 // segment ring emptied for the next generation.
 __global__ void k_stream_rotate(Counters* ctr, uint64_t seg_cap) {
+  if (ctr->skip_raster) return;
   const unsigned long long s = ctr->seg_count, r = ctr->tile_refs;
   ctr->seg_total += s < seg_cap ? s : seg_cap;
   if (s > ctr->seg_max) ctr->seg_max = s;
@@ -320,6 +340,7 @@ __global__ void k_stream_rotate(Counters* ctr, uint64_t seg_cap) {
 }
 
 __global__ void k_build_units(RasterArgs A) {
+  if (A.ctr->skip_raster) return;
   for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < A.n_tiles; t += gridDim.x * blockDim.x) {
     const uint64_t c = A.tile_count[t], off = A.tile_off[t];
     uint64_t u = A.unit_off[t];
@@ -338,6 +359,7 @@ __global__ void k_build_units(RasterArgs A) {
 // its own segments per tile, reserves one range per touched tile with a single global
 // atomic, and fills the ranges through shared-memory cursors.
 __global__ void __launch_bounds__(256) k_bin_scatter(RasterArgs A, int smem_tiles) {
+  if (A.ctr->skip_raster) return;
   extern __shared__ unsigned cur[];  // slots are < refs_cap < 2^32
   const uint64_t n = n_segments(A);
   if (smem_tiles) {
@@ -415,6 +437,7 @@ struct __align__(16) Staged {
 
 template <int MODE>
 __global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
+  if (A.ctr->skip_raster) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned* acc32 = reinterpret_cast<unsigned*>(smem_raw);
   long long* acc64 = reinterpret_cast<long long*>(smem_raw);
@@ -609,6 +632,7 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
 // of segments (fewer flushes); occupancy is bounded by the 32 KB tile per warp.
 template <int MODE>
 __global__ void __launch_bounds__(32) k_raster_warp(RasterArgs A) {
+  if (A.ctr->skip_raster) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   long long* acc64 = reinterpret_cast<long long*>(smem_raw);      // [ch][minor][lane]
   float* accf = reinterpret_cast<float*>(smem_raw);

@@ -275,8 +275,15 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
   for (uint64_t base = warp * 32; base < n_in; base += nwarps * 32) {
-    const uint64_t idx = base + lane;
-    bool live = idx < n_in;
+    // multi-scene generations > 0 visit the queue in scene order, so that a warp's rays
+    // (and a CTA's warps) share one scene
+    uint64_t idx = base + lane;
+    bool valid = idx < n_in;
+    if (MULTI && gen > 0 && valid) {
+      idx = B.order[idx];
+      valid = idx < n_in;
+    }
+    bool live = valid;
     RayRec r;
     if (live) {
       if (gen == 0) {
@@ -348,7 +355,7 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
         int cnt = 0;
         for (uint32_t jj = 0; jj < jn; ++jj) {
           const uint32_t j = j0 + jj;
-          const float4 h = *reinterpret_cast<const float4*>(&objs[j]);
+          const float4 h = MULTI ? __ldg(&S.bounds[j]) : *reinterpret_cast<const float4*>(&objs[j]);
           float lb;
           if (mine && bound_test(h, ox, oy, dx, dy, thr, lb)) {
             PairSlot ps;
@@ -411,7 +418,7 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
     bool emit = false;
     float x1 = 0.0f, y1 = 0.0f;
     uint8_t eflags = 0;
-    if (idx < n_in) {
+    if (valid) {
       ScanRec sc;
       sc.nc = 0;
       sc.overflow = overflow ? 1 : 0;
@@ -638,7 +645,7 @@ __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, c
         const float px32 = bh.px.hi, py32 = bh.py.hi;
         for (uint32_t k = 0; k < sl.n; ++k) {
           if ((int)k == best) continue;
-          const float4 h = *reinterpret_cast<const float4*>(&objs[sl.base + k]);
+          const float4 h = MULTI ? __ldg(&S.bounds[sl.base + k]) : *reinterpret_cast<const float4*>(&objs[sl.base + k]);
           if (!(__float_as_uint(h.w) & INFO_MATERIAL)) continue;
           const float ex = px32 - h.x, ey = py32 - h.y;
           const float tol = 2e-6f * (fabsf(px32) + fabsf(py32) + fabsf(h.x) + fabsf(h.y) + h.z) + 1e-6f;
@@ -831,6 +838,80 @@ __global__ void __launch_bounds__(256) k_bounce(SceneDev S, TraceBufs B, uint32_
 }
 template __global__ void k_bounce<false>(SceneDev, TraceBufs, uint32_t, int);
 template __global__ void k_bounce<true>(SceneDev, TraceBufs, uint32_t, int);
+
+// ------------------------------------------------------------------- scene order
+// Multi-scene generations > 0: a counting sort of the queue entries by scene (histogram,
+// exclusive scan, scatter of entry indices), so that k_scan's warps each see one scene.
+__device__ __forceinline__ unsigned long long warp_scene_atomic(unsigned* slot_base, uint32_t s, bool on) {
+  const unsigned act = __activemask();
+  const unsigned grp = __match_any_sync(act, on ? s : 0xffffffffu);
+  if (!on) return 0;
+  const int leader = __ffs(grp) - 1;
+  unsigned base = 0;
+  if ((int)lane_id() == leader) base = atomicAdd(&slot_base[s], (unsigned)__popc(grp));
+  base = __shfl_sync(grp, base, leader);
+  return base + __popc(grp & lanemask_lt());
+}
+
+__global__ void k_scene_hist(SceneDev S, TraceBufs B, uint32_t gen, unsigned* count) {
+  const uint64_t n = n_in_of(S, B, gen);
+  const RayRec* q = B.queue[gen & 1];
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t s = q[i].scene;
+    warp_scene_atomic(count, s, s < S.n_scenes);
+  }
+}
+
+// single CTA: off = exclusive scan of count; count is cleared for the next generation
+__global__ void __launch_bounds__(1024) k_scene_offsets(unsigned* count, unsigned* off, uint32_t n_scenes) {
+  __shared__ unsigned wsum[32];
+  __shared__ unsigned carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+  for (uint32_t base = 0; base < n_scenes; base += blockDim.x) {
+    const uint32_t i = base + threadIdx.x;
+    const unsigned c = i < n_scenes ? count[i] : 0u;
+    unsigned incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+      if ((int)lane >= o) incl += y;
+    }
+    if (lane == 31) wsum[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+      unsigned sw = lane < (blockDim.x >> 5) ? wsum[lane] : 0u;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, sw, o);
+        if ((int)lane >= o) sw += y;
+      }
+      wsum[lane] = sw;
+    }
+    __syncthreads();
+    const unsigned cr = carry;
+    const unsigned excl = cr + (wid ? wsum[wid - 1] : 0u) + incl - c;
+    if (i < n_scenes) {
+      off[i] = excl;
+      count[i] = 0u;
+    }
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = excl + c;
+    __syncthreads();
+  }
+}
+
+__global__ void k_scene_scatter(SceneDev S, TraceBufs B, uint32_t gen, unsigned* off, uint32_t* order) {
+  const uint64_t n = n_in_of(S, B, gen);
+  const RayRec* q = B.queue[gen & 1];
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t s = q[i].scene;
+    const bool on = s < S.n_scenes;
+    const unsigned long long pos = warp_scene_atomic(off, s, on);
+    if (on && pos < n) order[pos] = (uint32_t)i;
+  }
+}
 
 // ------------------------------------------------------------------- overlays
 // Curved-mirror control lines (tracer.rs:341-346) and the string-mod chords
