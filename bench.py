@@ -375,6 +375,96 @@ def run_batch(args, ws, rank, local):
         print(json.dumps(out_line), flush=True)
 
 
+def run_serve(args, ws, rank, local):
+    """Serving: requests from the mixed-size generator arrive as a Poisson stream; the server
+    (lg_serve_*, continuous batching under an HBM budget) against the plain path serving the
+    same arrivals one request at a time (lg_render, first come first served)."""
+    import numpy as np
+    import torch
+
+    from light_garden_gb300 import workloads as W
+    from light_garden_gb300.runtime import Context
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    ws_ = W.batch_scenes(seed=6, count=args.batch_scenes)
+    if args.ray_scale != 1.0:
+        ws_ = [W.scale_rays(w, args.ray_scale) for w in ws_]
+    scenes = [w.packed() for w in ws_]
+    n = len(scenes)
+    rng = np.random.default_rng(7)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n))
+    ctx = Context(device=local)
+    ctx.serve_begin(hbm_budget_bytes=int(args.budget_gb * (1 << 30)), max_slots=4096)
+    # warm up the kernels on two requests
+    for sc in scenes[:2]:
+        ctx.serve_submit(sc)
+    while ctx.serve_step()["in_flight"] or any(ctx.serve_poll(r) is None for r in list(ctx.serve_shapes)):
+        pass
+    done_at, arrive_of, ids = {}, {}, []
+    steps = restarts = 0
+    t0 = time.perf_counter()
+    nxt = 0
+    inflight = set()
+    while len(done_at) < n:
+        now = time.perf_counter() - t0
+        while nxt < n and arrivals[nxt] <= now:
+            rid = ctx.serve_submit(scenes[nxt])
+            arrive_of[rid] = arrivals[nxt]
+            inflight.add(rid)
+            nxt += 1
+        if not inflight:
+            time.sleep(max(0.0, arrivals[nxt] - now))
+            continue
+        st = ctx.serve_step()
+        steps += 1
+        restarts += st["restarted"]
+        if st["finished"] or st["in_flight"] == 0:
+            t = time.perf_counter() - t0
+            for rid in list(inflight):
+                if ctx.serve_poll(rid) is not None:
+                    done_at[rid] = t
+                    inflight.discard(rid)
+    makespan = time.perf_counter() - t0
+    lat = np.array([done_at[r] - arrive_of[r] for r in done_at]) * 1e3
+    ctx.serve_end()
+    ctx.close()
+    # plain path: one request at a time in arrival order
+    plain = Context(device=local)
+    big = torch.empty(max(pk.params.width * pk.params.height for pk in scenes) * 4, dtype=torch.int16, device=dev)
+    for pk in scenes[:2]:
+        plain.upload(pk)
+        plain.render_into(big.data_ptr(), pk.params.width * 8, True)
+    service = []
+    for pk in scenes:
+        a = time.perf_counter()
+        plain.upload(pk)
+        plain.render_into(big.data_ptr(), pk.params.width * 8, True)
+        service.append(time.perf_counter() - a)
+    plain.close()
+    end, plat = 0.0, []
+    for a, s in zip(arrivals, service):
+        end = max(end, a) + s
+        plat.append((end - a) * 1e3)
+    plat = np.array(plat)
+    if rank == 0:
+        line = {
+            "metric": "serving: scenes/s and p50/p99 scene latency (continuous batching vs plain one-scene path)",
+            "value": n / makespan, "unit": "scenes/s", "n_gpus": ws, "steps": steps, "warmup": 2,
+            "ms_per_step": makespan * 1e3 / max(1, steps), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32 + double-float trace, int64 accumulate", "data": "synthetic",
+            "config": {"workload": BATCH_WORKLOAD.replace("seed 4", "seed 6") +
+                       ("" if args.ray_scale == 1.0 else f", rays x {args.ray_scale}"),
+                       "requests": n, "arrivals": f"Poisson, {args.rate} requests/s",
+                       "hbm_budget_gb": args.budget_gb},
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "makespan_s": makespan, "restarts": restarts,
+            "plain": {"scenes_per_s": n / end, "p50_ms": float(np.percentile(plat, 50)),
+                      "p99_ms": float(np.percentile(plat, 99)), "makespan_s": end},
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -388,7 +478,9 @@ def main():
     ap.add_argument("--raster-variant", type=int, default=0, choices=[0, 1, 2],
                     help="0: autotuned; 1: shared-memory tile atomics; 2: warp-private tiles")
     # the mixed-size batch configuration (not the default line)
-    ap.add_argument("--workload", default="mid", choices=["mid", "batch"])
+    ap.add_argument("--workload", default="mid", choices=["mid", "batch", "serve"])
+    ap.add_argument("--rate", type=float, default=1000.0, help="serve: Poisson arrival rate (requests/s)")
+    ap.add_argument("--budget-gb", type=float, default=120.0, help="serve: HBM budget")
     ap.add_argument("--batch-scenes", type=int, default=512)
     ap.add_argument("--ray-scale", type=float, default=1.0)
     args = ap.parse_args()
@@ -397,6 +489,8 @@ def main():
         run_reference(args, ws, rank)
     elif args.workload == "batch":
         run_batch(args, ws, rank, local)
+    elif args.workload == "serve":
+        run_serve(args, ws, rank, local)
     else:
         run_ours(args, ws, rank, local)
     if ws > 1:

@@ -298,6 +298,41 @@ lg_status lg_batch_render(lg_ctx* ctx, uint16_t* dst, uint64_t dst_bytes, int32_
 /* First pixel of scene `scene`'s image in lg_batch_render's output (in pixels, 4 values each). */
 lg_status lg_batch_image_offset(const lg_ctx* ctx, uint32_t scene, uint64_t* px_offset);
 
+/* ---- serving: continuous batching of scene requests ---------------------------------- *
+ * No counterpart in the reference.  lg_serve_step runs one generation of the multi-scene
+ * wavefront over every request in flight and admits waiting requests at every step (their
+ * primaries join the same launch as the older requests' deeper generations).  Admission is
+ * bounded by the HBM budget (ray queues, segment ring, image pools); a finished request is
+ * resolved to RGBA16F and kept until lg_serve_poll copies it out (which frees its memory).
+ * Every image is bit-identical to lg_render of the scene alone.  Requests share blend state
+ * and clear colour, accumulate in LG_ACCUM_FIXED64 and may not use the string-mod overlay.
+ * While serving, lg_scene_upload and lg_batch_upload return LG_ERR_INVALID_ARGUMENT. */
+typedef struct lg_serve_opts {
+  uint64_t hbm_budget_bytes; /* device memory the server may hold (0: 80 % of free memory) */
+  uint32_t max_slots;        /* requests in flight at once, 1..65535 */
+  uint32_t _pad;
+} lg_serve_opts;
+
+typedef struct lg_serve_step_stats {
+  uint32_t admitted, finished, in_flight, pending;
+  uint32_t rasterised;      /* 1 if the step accumulated the segment ring */
+  uint32_t restarted;       /* 1 if the step overflowed its queue and restarted the requests in flight */
+  uint64_t live_rays;       /* rays queued for the next step */
+  uint64_t segments;        /* segments accumulated so far */
+  float step_ms;            /* host wall time of the step */
+  uint32_t _pad;
+} lg_serve_step_stats;
+
+lg_status lg_serve_begin(lg_ctx* ctx, const lg_serve_opts* opts);
+/* Validates and queues one scene; *id_out identifies it.  LG_ERR_BUDGET if the scene could
+ * never be admitted under the budget (too many primaries or too large a canvas). */
+lg_status lg_serve_submit(lg_ctx* ctx, const lg_scene_desc* scene, uint64_t* id_out);
+lg_status lg_serve_step(lg_ctx* ctx, lg_serve_step_stats* stats_or_null);
+/* LG_OK: the finished image (width*height*4 binary16, rows top-down) was copied to dst and
+ * the request forgotten; LG_ERR_NOT_READY: still queued or in flight; LG_ERR_NOT_FOUND. */
+lg_status lg_serve_poll(lg_ctx* ctx, uint64_t id, uint16_t* dst, uint64_t dst_bytes, int32_t dst_is_device);
+lg_status lg_serve_end(lg_ctx* ctx);
+
 /* No counterpart in the reference.  For callers that may not allocate device memory
  * (plug-ins whose host owns every allocation, real-time loops that must not take the
  * allocator's locks or risk the implicit synchronisation of cudaMalloc / cudaFree, code

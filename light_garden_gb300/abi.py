@@ -145,6 +145,19 @@ class lg_scene_desc(C.Structure):
                 ("n_lights", C.c_uint32), ("_pad", C.c_uint32)]
 
 
+class lg_serve_opts(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_slots", C.c_uint32), ("_pad", C.c_uint32)]
+
+
+class lg_serve_step_stats(C.Structure):
+    _fields_ = [("admitted", C.c_uint32), ("finished", C.c_uint32), ("in_flight", C.c_uint32),
+                ("pending", C.c_uint32), ("rasterised", C.c_uint32), ("restarted", C.c_uint32),
+                ("live_rays", C.c_uint64), ("segments", C.c_uint64), ("step_ms", C.c_float), ("_pad", C.c_uint32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if not f.startswith("_")}
+
+
 # ---- library loading --------------------------------------------------------------------
 _lib = None
 
@@ -170,6 +183,11 @@ EXPORTS = [
     ("lg_batch_upload", C.c_int, [C.c_void_p, C.POINTER(lg_scene_desc), C.c_uint32]),
     ("lg_batch_render", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_int32, C.POINTER(lg_trace_stats)]),
     ("lg_batch_image_offset", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint64)]),
+    ("lg_serve_begin", C.c_int, [C.c_void_p, C.POINTER(lg_serve_opts)]),
+    ("lg_serve_submit", C.c_int, [C.c_void_p, C.POINTER(lg_scene_desc), C.POINTER(C.c_uint64)]),
+    ("lg_serve_step", C.c_int, [C.c_void_p, C.POINTER(lg_serve_step_stats)]),
+    ("lg_serve_poll", C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.c_int32]),
+    ("lg_serve_end", C.c_int, [C.c_void_p]),
     ("lg_accumulate_segments_noalloc", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(lg_params), C.c_void_p,
                                                  C.c_void_p, C.POINTER(C.c_uint64)]),
 ]

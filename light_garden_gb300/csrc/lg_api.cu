@@ -326,7 +326,10 @@ SceneDev scene_dev(lg_ctx* c) {
   S.scenes = nullptr;
   S.bounds = nullptr;
   S.n_scenes = 1;
-  S._pad = 0;
+  S.serve = 0;
+  S.n_new = 0;
+  S.light_lo = 0;
+  S.light_hi = 0;
   return S;
 }
 
@@ -661,6 +664,7 @@ lg_status lg_destroy(lg_ctx* c) {
   if (!c) return LG_ERR_INVALID_ARGUMENT;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  serve_free(c);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   DevBuf* bufs[] = {&c->d_scan, &c->d_info, &c->d_leaves, &c->d_prog, &c->d_lights, &c->d_cubics, &c->d_queue[0],
                     &c->d_queue[1], &c->d_scanrec, &c->d_hitrec, &c->d_list[0], &c->d_list[1], &c->d_list[2],
@@ -683,6 +687,7 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
                           const lg_light* lights, uint32_t n_lights, const lg_params* params) {
   if (!c || !params || (n_geo && !geos) || (n_objects && !objects) || (n_lights && !lights))
     return c ? fail(c, LG_ERR_INVALID_ARGUMENT, "null pointer") : LG_ERR_INVALID_ARGUMENT;
+  if (c->serve) return fail(c, LG_ERR_INVALID_ARGUMENT, "serving in progress: lg_serve_end first");
   CK(cudaSetDevice(c->device), "cudaSetDevice");
   const lg_params& p = *params;
   lg_status st = validate_params(c->err, p);

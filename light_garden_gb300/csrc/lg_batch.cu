@@ -199,6 +199,7 @@ extern "C" {
 lg_status lg_batch_upload(lg_ctx* c, const lg_scene_desc* scenes, uint32_t k) {
   if (!c) return LG_ERR_INVALID_ARGUMENT;
   if (!scenes || k == 0) return fail(c, LG_ERR_INVALID_ARGUMENT, "no scenes");
+  if (c->serve) return fail(c, LG_ERR_INVALID_ARGUMENT, "serving in progress: lg_serve_end first");
   if (k > 65535) return fail(c, LG_ERR_INVALID_ARGUMENT, "at most 65535 scenes per batch");
   CK(cudaSetDevice(c->device), "cudaSetDevice");
   const lg_params* p0 = scenes[0].params;
@@ -242,6 +243,7 @@ lg_status lg_batch_upload(lg_ctx* c, const lg_scene_desc* scenes, uint32_t k) {
         F.cubics.push_back(obj0 + cu);
         cubic_scene.push_back((uint16_t)s);
       }
+    const uint32_t light0 = (uint32_t)F.lights.size();
     for (LightDev L : Fs.lights) {
       L.first += n_primary;
       L.scene = s;
@@ -255,6 +257,7 @@ lg_status lg_batch_upload(lg_ctx* c, const lg_scene_desc* scenes, uint32_t k) {
     R.aspect = DF((double)((float)p.width / (float)p.height));
     for (int i = 0; i < 4; ++i) R.cutoff[i] = p.cutoff_color[i];
     R.max_bounce = p.max_bounce;
+    R.light_base = light0;
     max_b = std::max(max_b, p.max_bounce);
     SceneCanvas& C = canv[s];
     C.W = p.width;

@@ -9,6 +9,8 @@
 #include "lg_host.hpp"
 
 namespace lgh {
+struct ServeState;  // lg_serve.cu
+
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
@@ -70,6 +72,7 @@ struct lg_ctx {
   uint64_t n_overlay = 0;
   int batch_grid_scan = 0;
   std::vector<cudaEvent_t> bev;          // batch stage events (start, per generation x 2, resolved)
+  ServeState* serve = nullptr;           // serving mode (lg_serve_begin .. lg_serve_end)
 };
 
 
@@ -86,6 +89,7 @@ SceneDev scene_dev(lg_ctx* c);
 TraceBufs trace_bufs(lg_ctx* c);
 RasterArgs raster_args(lg_ctx* c);
 void fill_stats(lg_ctx* c, lg_trace_stats* s);
+void serve_free(lg_ctx* c);
 
 #define CK(call, what)                                      \
   do {                                                      \

@@ -152,7 +152,8 @@ struct __align__(16) SceneRec {
   df aspect;              // canvas half width (height is 1)
   float cutoff[4];
   uint32_t max_bounce;
-  uint32_t _pad[3];
+  uint32_t light_base;    // the scene's first light (rays hold scene-local light indices)
+  uint32_t _pad[2];
 };
 static_assert(sizeof(SceneRec) == 48, "SceneRec is 48 B");
 
@@ -171,7 +172,12 @@ struct SceneDev {
   const SceneRec* scenes; // multi-scene traces only
   const float4* bounds;   // multi-scene: bounding circle + info word of every object (ObjScan's first 16 B)
   uint32_t n_scenes;
-  uint32_t _pad;
+  // Serving (continuous batching): every launch takes the queued rays of the previous
+  // step plus the primaries of the lights admitted now, [light_lo, light_hi), whose
+  // `first` indices count from 0 at this step.
+  uint32_t serve;
+  uint64_t n_new;
+  uint32_t light_lo, light_hi;
 };
 
 // The scene a ray belongs to, as the kernels use it.  Single-scene kernels (MULTI false)
@@ -181,17 +187,18 @@ struct SceneLoc {
   df aspect;
   float cutoff[4];
   uint32_t max_bounce;
+  uint32_t light_base;
 };
 template <bool MULTI>
 __device__ __forceinline__ SceneLoc scene_of(const SceneDev& S, uint32_t sid) {
   SceneLoc L;
   if (!MULTI) {
-    L.base = 0; L.n = S.n_obj; L.aspect = S.aspect; L.max_bounce = S.max_bounce;
+    L.base = 0; L.n = S.n_obj; L.aspect = S.aspect; L.max_bounce = S.max_bounce; L.light_base = 0;
 #pragma unroll
     for (int i = 0; i < 4; ++i) L.cutoff[i] = S.cutoff[i];
   } else {
     const SceneRec& R = S.scenes[sid];
-    L.base = R.obj_base; L.n = R.n_obj; L.aspect = R.aspect; L.max_bounce = R.max_bounce;
+    L.base = R.obj_base; L.n = R.n_obj; L.aspect = R.aspect; L.max_bounce = R.max_bounce; L.light_base = R.light_base;
 #pragma unroll
     for (int i = 0; i < 4; ++i) L.cutoff[i] = R.cutoff[i];
   }

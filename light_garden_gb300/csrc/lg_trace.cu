@@ -110,7 +110,8 @@ __device__ inline void primary_ray(const LightDev& L, uint64_t i, double& ox, do
 
 template <bool MULTI>
 __global__ void k_light_setup(SceneDev S) {
-  for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < S.n_lights; l += gridDim.x * blockDim.x) {
+  const uint32_t l0 = S.serve ? S.light_lo : 0u, l1 = S.serve ? S.light_hi : S.n_lights;
+  for (uint32_t l = l0 + blockIdx.x * blockDim.x + threadIdx.x; l < l1; l += gridDim.x * blockDim.x) {
     LightDev& L = S.lights[l];
     const SceneLoc sl = scene_of<MULTI>(S, L.scene);
     df n = DF_ONE;  // tracer.rs:280-287: the last containing object wins
@@ -158,9 +159,18 @@ __device__ __forceinline__ bool bound_test(const float4& h, float ox, float oy, 
   return lb <= thr;
 }
 
-__device__ __forceinline__ uint64_t n_in_of(const SceneDev& S, const TraceBufs& B, uint32_t gen) {
-  if (gen == 0) return S.n_primary;
+// Queued rays a launch takes (the children of the previous generation or step) ...
+__device__ __forceinline__ uint64_t n_real_of(const SceneDev& S, const TraceBufs& B, uint32_t gen) {
+  if (gen == 0 && !S.serve) return 0;
   const unsigned long long n = B.ctr->queue_count[gen];
+  return n < B.queue_cap ? n : B.queue_cap;
+}
+// ... and primaries it generates (virtual queue entries after the queued ones)
+__device__ __forceinline__ uint64_t n_new_of(const SceneDev& S, uint32_t gen) {
+  return S.serve ? S.n_new : (gen == 0 ? S.n_primary : 0);
+}
+__device__ __forceinline__ uint64_t n_in_of(const SceneDev& S, const TraceBufs& B, uint32_t gen) {
+  const uint64_t n = n_real_of(S, B, gen) + n_new_of(S, gen);
   return n < B.queue_cap ? n : B.queue_cap;
 }
 
@@ -269,31 +279,33 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
   bool failed;
   const ObjScan* objs = stage_objects(S, sobj, &bar, !MULTI && smem_fits != 0, B.ctr, failed);
   if (failed) return;
+  const uint64_t n_real = n_real_of(S, B, gen);
   const uint64_t n_in = n_in_of(S, B, gen);
   RayRec* q = B.queue[gen & 1];
   const unsigned lane = lane_id(), w = threadIdx.x >> 5;
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
   for (uint64_t base = warp * 32; base < n_in; base += nwarps * 32) {
-    // multi-scene generations > 0 visit the queue in scene order, so that a warp's rays
-    // (and a CTA's warps) share one scene
+    // multi-scene launches visit the queued rays in scene order, so that a warp's rays (and
+    // a CTA's warps) share one scene; new primaries follow, ordered by light
     uint64_t idx = base + lane;
     bool valid = idx < n_in;
-    if (MULTI && gen > 0 && valid) {
+    if (MULTI && valid && idx < n_real) {
       idx = B.order[idx];
-      valid = idx < n_in;
+      valid = idx < n_real;
     }
     bool live = valid;
     RayRec r;
     if (live) {
-      if (gen == 0) {
-        uint32_t l = 0, lhi = S.n_lights;  // the last light whose first primary is <= idx
-        while (lhi - l > 1) {
+      if (idx >= n_real) {
+        const uint64_t v = idx - n_real;  // primary number among this launch's new lights
+        uint32_t l = S.serve ? S.light_lo : 0u, lhi = S.serve ? S.light_hi : S.n_lights;
+        while (lhi - l > 1) {  // the last light whose first primary is <= v
           const uint32_t mid = (l + lhi) >> 1;
-          if (S.lights[mid].first <= idx) l = mid; else lhi = mid;
+          if (S.lights[mid].first <= v) l = mid; else lhi = mid;
         }
         const LightDev& L = S.lights[l];
-        const uint64_t i = idx - L.first;
+        const uint64_t i = v - L.first;
         double pox, poy, pdx, pdy;
         primary_ray(L, i, pox, poy, pdx, pdy);
         r.ox = df_from_double(pox); r.oy = df_from_double(poy);
@@ -304,7 +316,7 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
         r.c[0] = L.color[0]; r.c[1] = L.color[1]; r.c[2] = L.color[2]; r.c[3] = L.color[3];
         r.path = 0;
         r.prim = (uint32_t)i;
-        r.light = (uint16_t)l;
+        r.light = (uint16_t)(MULTI ? l - S.scenes[L.scene].light_base : l);
         r.gen = 0;
         r.flags = 0;
         r._pad = 0;
@@ -666,7 +678,7 @@ __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, c
       df ci = -ddn;
       if (df_neg(ci)) { ci = -ci; nx = -nx; ny = -ny; }
       const df n1 = r.medium == MEDIUM_AIR ? DF_ONE
-                    : r.medium == MEDIUM_LIGHT ? S.lights[r.light].n0 : S.info[sl.base + r.medium].n;
+                    : r.medium == MEDIUM_LIGHT ? S.lights[sl.light_base + r.light].n0 : S.info[sl.base + r.medium].n;
       const df eta = n1 / n2;
       const df k = DF_ONE - eta * eta * (DF_ONE - ci * ci);
       if (fabsf(k.hi) <= 1e-10f) fl |= LG_PATH_NEAR_DEGENERATE;
@@ -819,7 +831,7 @@ __global__ void __launch_bounds__(256) k_bounce(SceneDev S, TraceBufs B, uint32_
       if ((int)lane >= o) incl += y;
     }
     const int tot = __shfl_sync(0xffffffffu, incl, 31);
-    if (tot > 0 && gen + 1 < S.max_bounce) {
+    if (tot > 0 && (MULTI || gen + 1 < S.max_bounce)) {  // multi-scene: bounce() checks each ray's scene
       unsigned long long qbase = 0;
       if (lane == 31) qbase = atomicAdd(&B.ctr->queue_count[gen + 1], (unsigned long long)tot);
       qbase = __shfl_sync(0xffffffffu, qbase, 31);
@@ -854,7 +866,7 @@ __device__ __forceinline__ unsigned long long warp_scene_atomic(unsigned* slot_b
 }
 
 __global__ void k_scene_hist(SceneDev S, TraceBufs B, uint32_t gen, unsigned* count) {
-  const uint64_t n = n_in_of(S, B, gen);
+  const uint64_t n = n_real_of(S, B, gen);
   const RayRec* q = B.queue[gen & 1];
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t s = q[i].scene;
@@ -903,7 +915,7 @@ __global__ void __launch_bounds__(1024) k_scene_offsets(unsigned* count, unsigne
 }
 
 __global__ void k_scene_scatter(SceneDev S, TraceBufs B, uint32_t gen, unsigned* off, uint32_t* order) {
-  const uint64_t n = n_in_of(S, B, gen);
+  const uint64_t n = n_real_of(S, B, gen);
   const RayRec* q = B.queue[gen & 1];
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t s = q[i].scene;

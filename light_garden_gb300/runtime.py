@@ -118,15 +118,19 @@ class Context:
         return (segs, recs) if paths else segs
 
     # -- many scenes -------------------------------------------------------------------------
+    @staticmethod
+    def _desc(d, sc) -> None:
+        d.geos = C.cast(sc.geos, C.POINTER(abi.lg_geo))
+        d.objects = C.cast(sc.objects, C.POINTER(abi.lg_object))
+        d.lights = C.cast(sc.lights, C.POINTER(abi.lg_light))
+        d.params = C.pointer(sc.params)
+        d.n_geo, d.n_objects, d.n_lights = sc.n_geo, sc.n_objects, sc.n_lights
+
     def batch_upload(self, scenes) -> None:
         """Upload a batch of PackedScene (lg_batch_upload)."""
         descs = (abi.lg_scene_desc * len(scenes))()
         for d, sc in zip(descs, scenes):
-            d.geos = C.cast(sc.geos, C.POINTER(abi.lg_geo))
-            d.objects = C.cast(sc.objects, C.POINTER(abi.lg_object))
-            d.lights = C.cast(sc.lights, C.POINTER(abi.lg_light))
-            d.params = C.pointer(sc.params)
-            d.n_geo, d.n_objects, d.n_lights = sc.n_geo, sc.n_objects, sc.n_lights
+            self._desc(d, sc)
         self._check(self.lib.lg_batch_upload(self.h, descs, len(scenes)), "lg_batch_upload")
         self.batch_shapes = [(sc.params.height, sc.params.width) for sc in scenes]
         self.batch_offsets = []
@@ -151,6 +155,39 @@ class Context:
         stats = self.batch_render_into(flat.ctypes.data, flat.nbytes, False)
         imgs = [flat[4 * o:4 * (o + h * w)].reshape(h, w, 4) for o, (h, w) in zip(self.batch_offsets, self.batch_shapes)]
         return imgs, stats
+
+    # -- serving ------------------------------------------------------------------------------
+    def serve_begin(self, hbm_budget_bytes: int = 0, max_slots: int = 1024) -> None:
+        opts = abi.lg_serve_opts(hbm_budget_bytes, max_slots, 0)
+        self._check(self.lib.lg_serve_begin(self.h, C.byref(opts)), "lg_serve_begin")
+        self.serve_shapes = {}
+
+    def serve_submit(self, scene: PackedScene) -> int:
+        d = abi.lg_scene_desc()
+        self._desc(d, scene)
+        rid = C.c_uint64(0)
+        self._check(self.lib.lg_serve_submit(self.h, C.byref(d), C.byref(rid)), "lg_serve_submit")
+        self.serve_shapes[int(rid.value)] = (scene.params.height, scene.params.width)
+        return int(rid.value)
+
+    def serve_step(self) -> dict:
+        s = abi.lg_serve_step_stats()
+        self._check(self.lib.lg_serve_step(self.h, C.byref(s)), "lg_serve_step")
+        return s.as_dict()
+
+    def serve_poll(self, rid: int) -> Optional[np.ndarray]:
+        """The finished image of request rid, or None while it is queued or in flight."""
+        h, w = self.serve_shapes[rid]
+        out = np.zeros((h, w, 4), np.uint16)
+        st = self.lib.lg_serve_poll(self.h, rid, out.ctypes.data_as(C.c_void_p), out.nbytes, 0)
+        if st == abi.LG_ERR_NOT_READY:
+            return None
+        self._check(st, "lg_serve_poll")
+        del self.serve_shapes[rid]
+        return out
+
+    def serve_end(self) -> None:
+        self._check(self.lib.lg_serve_end(self.h), "lg_serve_end")
 
     def accum(self) -> np.ndarray:
         h, w = self._shape()

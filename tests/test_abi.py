@@ -13,7 +13,8 @@ from light_garden_gb300 import abi
 HEADER = abi.LIB_DIR.parent.parent / "include" / "lg.h"
 
 STRUCTS = [abi.lg_geo, abi.lg_object, abi.lg_light, abi.lg_blend_component, abi.lg_string_mod, abi.lg_params,
-           abi.lg_segment, abi.lg_path_record, abi.lg_trace_stats, abi.lg_device_opts, abi.lg_scene_desc]
+           abi.lg_segment, abi.lg_path_record, abi.lg_trace_stats, abi.lg_device_opts, abi.lg_scene_desc,
+           abi.lg_serve_opts, abi.lg_serve_step_stats]
 
 
 def declared_functions():
