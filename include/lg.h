@@ -214,6 +214,8 @@ typedef struct lg_device_opts {
                                  raster; 2: warp-private tile raster (results are identical) */
   uint64_t segment_capacity;  /* initial segment ring size (0 = automatic); grows on overflow */
   uint64_t queue_capacity;    /* initial per-generation ray queue size (0 = automatic) */
+  uint64_t stream_segments;   /* lg_render accumulates while tracing, with a ring of this many
+                                 segments, once a frame has more (0 = 2^28) */
 } lg_device_opts;
 
 typedef struct lg_ctx lg_ctx;

@@ -106,7 +106,7 @@ class lg_trace_stats(C.Structure):
 
 class lg_device_opts(C.Structure):
     _fields_ = [("device", C.c_int32), ("raster_variant", C.c_int32), ("segment_capacity", C.c_uint64),
-                ("queue_capacity", C.c_uint64)]
+                ("queue_capacity", C.c_uint64), ("stream_segments", C.c_uint64)]
 
 
 # numpy dtypes with the same layout, for bulk conversion of downloads

@@ -529,17 +529,21 @@ void fill_stats(lg_ctx* c, lg_trace_stats* s) {
   s->tile_refs = k.tile_refs;
 }
 
-lg_status run_trace_once(lg_ctx* c, uint32_t& retries);
+lg_status run_trace_once(lg_ctx* c, uint32_t& retries, uint64_t seg_limit = ~0ull);
 
-lg_status run_trace(lg_ctx* c, uint32_t& retries) { return run_trace_once(c, retries); }
+lg_status run_trace(lg_ctx* c, uint32_t& retries, uint64_t seg_limit = ~0ull) {
+  return run_trace_once(c, retries, seg_limit);
+}
 
-lg_status run_trace_once(lg_ctx* c, uint32_t& retries) {
+// seg_limit: return LG_ERR_TRUNCATED instead of growing the ring past it
+lg_status run_trace_once(lg_ctx* c, uint32_t& retries, uint64_t seg_limit) {
   for (int attempt = 0; attempt < 8; ++attempt) {
     lg_status st = enqueue_trace(c);
     if (st) return st;
     if ((st = sync_counters(c))) return st;
     uint64_t ns, nq;
     if (!trace_overflowed(c, ns, nq)) return LG_OK;
+    if (ns > seg_limit) return LG_ERR_TRUNCATED;
     ++retries;
     if ((st = grow_trace(c, ns, nq))) return st;
   }
@@ -631,6 +635,7 @@ lg_status lg_create(lg_ctx** out, const lg_device_opts* opts) {
   c->seg_cap_hint = opts ? opts->segment_capacity : 0;
   c->raster_variant = opts && (opts->raster_variant == 1 || opts->raster_variant == 2) ? opts->raster_variant : 0;
   c->queue_cap_hint = opts ? opts->queue_capacity : 0;
+  if (opts && opts->stream_segments) c->stream_ring = opts->stream_segments;
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, c->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
@@ -774,7 +779,10 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
   c->refs_cap = std::max<uint64_t>(c->refs_cap, 1u << 20);
   if ((st = ensure_raster_buffers(c))) return st;
   if ((st = ensure(c, c->d_stage, (size_t)p.width * p.height * 8, "resolve staging"))) return st;
-  if (!same_shape) c->graph_valid = false;
+  if (!same_shape) {
+    c->graph_valid = false;
+    c->streaming = false;  // a new scene starts with one accumulation pass per frame
+  }
   c->has_scene = true;
   return LG_OK;
 }
@@ -864,14 +872,173 @@ lg_status lg_resolve_rgba8(lg_ctx* c, uint8_t* dst, size_t pitch, int32_t dst_is
   return LG_OK;
 }
 
+// The whole frame with the accumulation interleaved: after each generation the segment ring
+// is accumulated if it could not take the next generation (k_stream_decide), so the ring
+// and the tile lists hold a bounded part of the frame.  ev: 2 * max_bounce + 2 events.
+static lg_status enqueue_stream_frame(lg_ctx* c, uint16_t* dst, size_t row, cudaEvent_t* ev) {
+  const SceneDev S = scene_dev(c);
+  const TraceBufs B = trace_bufs(c);
+  const RasterArgs A = raster_args(c);
+  const int fixed = c->prm.accum == LG_ACCUM_FIXED64;
+  CK(cudaEventRecordWithFlags(ev[0], c->stream, cudaEventRecordExternal), "stage event");
+  CK(cudaMemsetAsync(c->d_ctr.p, 0, sizeof(Counters), c->stream), "memset counters");
+  k_clear_accum<<<c->n_sm * 8, 256, 0, c->stream>>>(A, fixed);
+  if (c->n_lights) k_light_setup<false><<<1, 256, 0, c->stream>>>(S);
+  const size_t tsm = c->smem_fits ? c->obj_smem : 0;
+  const uint32_t bins = 2 * c->n_tiles;
+  const int smem_tiles = bins <= MAX_SMEM_TILES ? 1 : 0;
+  const size_t bsm = smem_tiles ? (size_t)bins * 4 : 0;
+  const uint32_t n_part = (bins + TILE_SCAN_CHUNK - 1) / TILE_SCAN_CHUNK;
+  const int mode = raster_mode(c->prm);
+  const size_t rsm = (size_t)raster_smem_bytes(mode);
+  const uint64_t n_ov = 3ull * c->n_cubic * (c->prm.emit_control_lines ? 1 : 0) + c->prm.string_mod.modulo;
+  const uint32_t G = c->prm.max_bounce;
+  for (uint32_t g = 0; g < G; ++g) {
+    k_scan<false><<<c->trace_grid[0], SCAN_THREADS, (size_t)scan_smem_bytes() + tsm, c->stream>>>(S, B, g,
+                                                                                                  c->smem_fits);
+    for (int l = LIST_REFINE_CIRCLE; l <= LIST_REFINE_CUBIC; ++l)
+      k_refine<false><<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g, l);
+    k_full<false><<<c->trace_grid[2], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
+    k_bounce<false><<<c->trace_grid[3], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
+    if (g == 0 && n_ov) {
+      const int blocks = (int)std::min<uint64_t>((n_ov + 255) / 256, 4096);
+      k_overlay<<<blocks, 256, 0, c->stream>>>(S, B, (const uint32_t*)c->d_cubics.p, nullptr,
+                                               c->prm.emit_control_lines ? c->n_cubic : 0, c->prm.string_mod);
+    }
+    CK(cudaEventRecordWithFlags(ev[1 + 2 * g], c->stream, cudaEventRecordExternal), "stage event");
+    k_stream_decide<<<1, 1, 0, c->stream>>>((Counters*)c->d_ctr.p, g, c->seg_cap, c->queue_cap, g + 1 == G ? 1 : 0);
+    k_clear_counts<<<c->n_sm * 4, 256, 0, c->stream>>>(A);
+    k_bin_count<<<c->bin_grid, 256, bsm, c->stream>>>(A, smem_tiles);
+    if (bins <= 32768) {
+      k_scan_tiles<<<1, 1024, 0, c->stream>>>(A);
+    } else {
+      k_tiles_partial<<<n_part, 1024, 0, c->stream>>>(A, (unsigned long long*)c->d_part.p);
+      k_tiles_scan_partials<<<1, 1024, 0, c->stream>>>(A, (unsigned long long*)c->d_part.p, n_part);
+      k_tiles_apply<<<n_part, 1024, 0, c->stream>>>(A, (const unsigned long long*)c->d_part.p);
+    }
+    k_build_units<<<std::max(1u, (bins + 255) / 256), 256, 0, c->stream>>>(A);
+    k_bin_scatter<<<c->bin_grid, 256, bsm, c->stream>>>(A, smem_tiles);
+    if (c->raster_variant == 2) {
+      if (mode == RM_F32_)
+        k_raster_warp<RM_F32_><<<c->raster_warp_grid, 32, raster_warp_smem_bytes(), c->stream>>>(A);
+      else
+        k_raster_warp<RM_FIXED_SPLIT_><<<c->raster_warp_grid, 32, raster_warp_smem_bytes(), c->stream>>>(A);
+    } else if (mode == RM_FIXED_SPLIT_) {
+      k_raster<RM_FIXED_SPLIT_><<<c->raster_grid, 256, rsm, c->stream>>>(A);
+    } else if (mode == RM_FIXED_MINMAX_) {
+      k_raster<RM_FIXED_MINMAX_><<<c->raster_grid, 256, rsm, c->stream>>>(A);
+    } else {
+      k_raster<RM_F32_><<<c->raster_grid, 256, rsm, c->stream>>>(A);
+    }
+    k_stream_rotate<<<1, 1, 0, c->stream>>>((Counters*)c->d_ctr.p, c->seg_cap);
+    CK(cudaEventRecordWithFlags(ev[2 + 2 * g], c->stream, cudaEventRecordExternal), "stage event");
+  }
+  k_resolve_f16<<<c->n_sm * 8, 256, 0, c->stream>>>(c->d_accum.p, fixed, c->prm.width, c->prm.height, dst, row);
+  CK(cudaEventRecordWithFlags(ev[1 + 2 * G], c->stream, cudaEventRecordExternal), "stage event");
+  CK(cudaGetLastError(), "stream frame launch");
+  return LG_OK;
+}
+
+// Switches a context to the streaming frame: a ring of stream_ring segments instead of one
+// that holds the whole frame.
+static lg_status start_streaming(lg_ctx* c) {
+  c->streaming = true;
+  c->graph_valid = false;
+  if (c->raster_variant == 0) c->raster_variant = 1;
+  const uint64_t n_ov = 3ull * c->n_cubic + c->prm.string_mod.modulo;
+  c->seg_cap = std::max<uint64_t>(c->stream_ring, c->queue_cap + n_ov + 1024);
+  c->refs_cap = std::min<uint64_t>(4 * c->seg_cap, 0xfffffff0ull);
+  if (c->bev.empty()) {
+    c->bev.assign(2 * MAX_GEN + 2, nullptr);
+    for (auto& e : c->bev) CK(cudaEventCreate(&e), "event");
+  }
+  lg_status st = ensure_trace_buffers(c);
+  if (st) return st;
+  if ((st = ensure_raster_buffers(c))) return st;
+  const size_t parts = (2 * (size_t)c->n_tiles + TILE_SCAN_CHUNK - 1) / TILE_SCAN_CHUNK;
+  return ensure(c, c->d_part, std::max<size_t>(parts, 1) * 16, "tile scan partials");
+}
+
+static lg_status render_streaming(lg_ctx* c, uint16_t* dst, size_t pitch, int32_t dst_is_device, lg_trace_stats* stats,
+                              uint32_t retries) {
+  const size_t row = (size_t)c->prm.width * 8;
+  std::vector<cudaEvent_t>& ev = c->bev;
+  const uint32_t G = c->prm.max_bounce;
+  for (int attempt = 0; attempt < 8; ++attempt) {
+    if (!c->graph_valid) {
+      if (c->gexec) cudaGraphExecDestroy(c->gexec);
+      c->gexec = nullptr;
+      cudaGraph_t g = nullptr;
+      CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+      lg_status s1 = enqueue_stream_frame(c, (uint16_t*)c->d_stage.p, row, ev.data());
+      cudaError_t e = cudaMemcpyAsync(c->h_ctr, c->d_ctr.p, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream);
+      cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+      if (s1) { if (g) cudaGraphDestroy(g); return s1; }
+      if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(c, e, "capture counters"); }
+      if (e2 != cudaSuccess) return cuda_fail(c, e2, "end capture");
+      e = cudaGraphInstantiate(&c->gexec, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return cuda_fail(c, e, "graph instantiate");
+      c->graph_valid = true;
+    }
+    CK(cudaGraphLaunch(c->gexec, c->stream), "graph launch");
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    const Counters& k = *c->h_ctr;
+    if (k.error_flags & ERR_TMA_TIMEOUT)
+      return fail(c, LG_ERR_TIMEOUT, "object-table bulk copy did not complete within its wait limit");
+    uint64_t nq = 0;
+    for (int g = 0; g <= MAX_GEN; ++g) nq = std::max<uint64_t>(nq, k.queue_count[g]);
+    if (nq > c->queue_cap || k.seg_max > c->seg_cap || k.refs_max > c->refs_cap) {
+      ++retries;
+      c->graph_valid = false;
+      if (nq > c->queue_cap) c->queue_cap = nq + nq / 2 + 1024;
+      c->seg_cap = std::max<uint64_t>(c->seg_cap, c->queue_cap + 3ull * c->n_cubic + c->prm.string_mod.modulo + 1024);
+      if (k.refs_max > c->refs_cap) c->refs_cap = k.refs_max + k.refs_max / 4 + 4096;
+      if (c->refs_cap >= 0xffffffffull) return fail(c, LG_ERR_UNSUPPORTED, "more than 2^32 (segment, tile) pairs in one pass");
+      lg_status st = ensure_trace_buffers(c);
+      if (st) return st;
+      if ((st = ensure_raster_buffers(c))) return st;
+      continue;
+    }
+    CK(cudaMemcpy2DAsync(dst, pitch, c->d_stage.p, row, row, c->prm.height,
+                         dst_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->stream), "copy image");
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    if (stats) {
+      std::memset(stats, 0, sizeof *stats);
+      fill_stats(c, stats);
+      stats->segments = k.seg_total;
+      stats->tile_refs = k.refs_total;
+      stats->retries = retries;
+      float tr = 0.f, ac = 0.f;
+      for (uint32_t g = 0; g < G; ++g) {
+        tr += elapsed(g == 0 ? ev[0] : ev[2 * g], ev[1 + 2 * g]);
+        ac += elapsed(ev[1 + 2 * g], ev[2 + 2 * g]);
+      }
+      stats->trace_ms = tr;
+      stats->accumulate_ms = ac;
+      stats->raster_ms = ac;
+      stats->resolve_ms = elapsed(ev[2 * G], ev[1 + 2 * G]);
+      stats->total_ms = elapsed(ev[0], ev[1 + 2 * G]);
+    }
+    return LG_OK;
+  }
+  return fail(c, LG_ERR_OUT_OF_MEMORY, "render buffers kept overflowing");
+}
+
 lg_status lg_render(lg_ctx* c, uint16_t* dst, size_t pitch, int32_t dst_is_device, lg_trace_stats* stats) {
   lg_status st = need_scene(c);
   if (st) return st;
   const size_t row = (size_t)c->prm.width * 8;
   if (!dst || pitch < row) return fail(c, LG_ERR_INVALID_ARGUMENT, "destination null or pitch < width * 8");
   uint32_t retries = 0;
+  if (c->streaming) return render_streaming(c, dst, pitch, dst_is_device, stats, retries);
   if (c->raster_variant == 0) {  // pick the raster kernel before it is baked into the graph
-    if ((st = run_trace(c, retries))) return st;
+    st = run_trace(c, retries, c->stream_ring);
+    if (st == LG_ERR_TRUNCATED) {  // more segments than one pass takes: stream the frame
+      if ((st = start_streaming(c))) return st;
+      return render_streaming(c, dst, pitch, dst_is_device, stats, retries);
+    }
+    if (st) return st;
     if ((st = tune_raster(c, retries))) return st;
   }
   for (int attempt = 0; attempt < 8; ++attempt) {
@@ -905,13 +1072,20 @@ lg_status lg_render(lg_ctx* c, uint16_t* dst, size_t pitch, int32_t dst_is_devic
     uint64_t ns, nq;
     if (trace_overflowed(c, ns, nq)) {
       ++retries;
+      if (ns > c->stream_ring) {
+        if ((st = start_streaming(c))) return st;
+        return render_streaming(c, dst, pitch, dst_is_device, stats, retries);
+      }
       if ((st = grow_trace(c, ns, nq))) return st;
       continue;
     }
     if (c->h_ctr->tile_refs > c->refs_cap) {
       ++retries;
       c->refs_cap = c->h_ctr->tile_refs + c->h_ctr->tile_refs / 8 + 4096;
-      if (c->refs_cap >= 0xffffffffull) return fail(c, LG_ERR_UNSUPPORTED, "more than 2^32 (segment, tile) pairs in one frame");
+      if (c->refs_cap >= 0xfffffff0ull) {
+        if ((st = start_streaming(c))) return st;
+        return render_streaming(c, dst, pitch, dst_is_device, stats, retries);
+      }
       if ((st = ensure_raster_buffers(c))) return st;
       c->graph_valid = false;
       continue;

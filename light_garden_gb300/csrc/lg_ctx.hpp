@@ -57,6 +57,8 @@ struct lg_ctx {
   // graph
   cudaGraphExec_t gexec = nullptr;
   bool graph_valid = false;
+  bool streaming = false;  // lg_render accumulates while tracing (the frame's segments exceed one pass)
+  uint64_t stream_ring = 256ull << 20;  // ... with a ring of this many segments
   cudaEvent_t ev[6] = {};
   // multi-scene mode (lg_batch_upload): the concatenated scenes replace the single scene
   bool multi = false;

@@ -110,7 +110,7 @@ struct __align__(16) RayRec {
   uint8_t gen, flags;
   // first-order bound of how far rounding may have moved this ray: lateral offset of the
   // origin (world units) and direction (radians).  A path whose bound grows past
-  // ILL_COND is numerically ill-conditioned and is flagged near-degenerate.
+  // ILL_COND is flagged near-degenerate; below it the bound widens the decision bands.
   float ex, ea;
   uint16_t medium;   // see MEDIUM_*
   uint16_t src_obj;  // object whose surface the ray starts on (SRC_NONE for primaries)
@@ -119,7 +119,12 @@ struct __align__(16) RayRec {
   uint16_t scene;    // scene of the ray (multi-scene traces); object indices are scene-local
 };
 static_assert(sizeof(RayRec) == 80, "RayRec is 80 B");
-constexpr float ILL_COND = 1e-11f;
+// A path whose error bound exceeds ILL_COND (world units / radians) is flagged: its
+// endpoints may then differ from an FP64 trace by more than a tenth of the 1e-5 endpoint
+// tolerance.  Below it, decisions are checked against the bound itself (Near).
+constexpr float ILL_COND = 1e-6f;
+constexpr float TOL_REACH = 5.0f;  // longest ray parameter inside a canvas (16:9 diagonal ~ 4.1)
+__device__ __forceinline__ float ray_tol(float ex, float ea) { return ex + TOL_REACH * ea; }
 constexpr float DF_ROUND = 2e-14f;  // double-float rounding per bounce, relative to the coordinates
 
 // work lists of one generation (k_scan appends, k_refine / k_full consume)
@@ -259,14 +264,21 @@ struct Hit64 {
   uint8_t leaf;  // leaf of the object that was hit
 };
 
-// Near-degenerate decision events: ev keeps the smallest ray parameter at which a
-// decision (hit or no hit) fell inside the relative band BAND.
-__device__ __forceinline__ void near_event(float& ev, float t) {
+// Near-degenerate decision events.  ev keeps the smallest ray parameter at which a
+// decision (hit or no hit, which side of a boundary) fell inside its band: the relative
+// band BAND of the arithmetic, widened to the ray's own error bound tol (world units: how
+// far rounding in earlier bounces may have moved the ray), since a decision whose margin is
+// below tol may come out either way in any finite precision.
+struct Near {
+  float ev;   // earliest near decision (ray parameter), INFINITY: none
+  float tol;  // position error bound of the ray
+};
+__device__ __forceinline__ void near_event(Near& n, float t) {
   if (t < 0.0f) t = 0.0f;
-  if (t < ev) ev = t;
+  if (t < n.ev) n.ev = t;
 }
-__device__ __forceinline__ void tmin_band(df t, float& ev) {
-  if (t.hi > 1e-11f && t.hi < 1e-7f) near_event(ev, t.hi);
+__device__ __forceinline__ void tmin_band(df t, Near& n) {
+  if (t.hi > 1e-11f && t.hi < fmaxf(1e-7f, 4.0f * n.tol)) near_event(n, t.hi);
 }
 __device__ __forceinline__ bool past_tmin(df t) { return t.hi > 1e-9f || (t.hi == 1e-9f && t.lo > 0.0f); }
 
@@ -274,7 +286,7 @@ __device__ __forceinline__ bool past_tmin(df t) { return t.hi > 1e-9f || (t.hi =
 // parametrisation (circle: t; rect: entry, exit; cubic: curve parameter).  Each kind is
 // one out-of-line function so the kernel keeps a single copy of it in the instruction
 // cache however many call sites a ray visit has.
-static __device__ __noinline__ int hits_circle(const Leaf64& L, df ox, df oy, df dx, df dy, Hit64* h, float& ev) {
+static __device__ __noinline__ int hits_circle(const Leaf64& L, df ox, df oy, df dx, df dy, Hit64* h, Near& ev) {
   int n = 0;
   (void)n;
   const df cx = L.p[0], cy = L.p[1], r = L.p[2];
@@ -282,7 +294,10 @@ static __device__ __noinline__ int hits_circle(const Leaf64& L, df ox, df oy, df
   const df a = dx * dx + dy * dy, b = ocx * dx + ocy * dy, cc = ocx * ocx + ocy * ocy - r * r;
   const df disc = b * b - a * cc;
   const float tc = -b.hi / a.hi;
-  if (fabsf(disc.hi) <= 1e-10f * (b.hi * b.hi + fabsf(a.hi * cc.hi)) && tc > -1e-9f) near_event(ev, tc);
+  // a lateral shift tol of the ray moves disc / a = r^2 - perp^2 by at most 2 r tol
+  if (fabsf(disc.hi) <= fmaxf(1e-10f * (b.hi * b.hi + fabsf(a.hi * cc.hi)), 2.0f * fabsf(r.hi) * ev.tol * a.hi) &&
+      tc > -1e-9f - ev.tol)
+    near_event(ev, tc);
   if (df_neg(disc)) return 0;
   const df sq = dsqrt(disc);
   const df q = -(b + (df_neg(b) ? -sq : sq));
@@ -309,7 +324,7 @@ static __device__ __noinline__ int hits_circle(const Leaf64& L, df ox, df oy, df
 
 }
 
-static __device__ __noinline__ int hits_segment(const Leaf64& L, df ox, df oy, df dx, df dy, Hit64* h, float& ev) {
+static __device__ __noinline__ int hits_segment(const Leaf64& L, df ox, df oy, df dx, df dy, Hit64* h, Near& ev) {
   int n = 0;
   (void)n;
   const df ax = L.p[0], ay = L.p[1], ex = L.p[2] - ax, ey = L.p[3] - ay;
@@ -322,7 +337,9 @@ static __device__ __noinline__ int hits_segment(const Leaf64& L, df ox, df oy, d
   const df inv = DF_ONE / den;
   const df t = cwe * inv;
   const df u = (wx * dy - wy * dx) * inv;
-  if (fabsf(u.hi) <= 1e-10f || fabsf(u.hi - 1.0f) <= 1e-10f) near_event(ev, t.hi);
+  // a lateral shift tol moves the crossing along the segment by tol / sin(angle): du = tol ld / |den|
+  const float ub = fmaxf(1e-10f, ev.tol * ld / fabsf(den.hi));
+  if (fabsf(u.hi) <= ub || fabsf(u.hi - 1.0f) <= ub) near_event(ev, t.hi);
   if (df_neg(u) || DF_ONE < u) return 0;
   tmin_band(t, ev);
   if (!past_tmin(t)) return 0;
@@ -333,7 +350,7 @@ static __device__ __noinline__ int hits_segment(const Leaf64& L, df ox, df oy, d
 
 }
 
-static __device__ __noinline__ int hits_rect(const Leaf64& L, df ox, df oy, df dx, df dy, Hit64* h, float& ev) {
+static __device__ __noinline__ int hits_rect(const Leaf64& L, df ox, df oy, df dx, df dy, Hit64* h, Near& ev) {
   int n = 0;
   (void)n;
   const df c = L.p[2], s = L.p[3];
@@ -346,7 +363,7 @@ static __device__ __noinline__ int hits_rect(const Leaf64& L, df ox, df oy, df d
   int an = -1, af = -1;
   for (int ax = 0; ax < 2; ++ax) {
     if (D[ax].hi == 0.0f) {
-      if (fabsf(fabsf(O[ax].hi) - hh[ax].hi) <= 1e-10f * hh[ax].hi) near_event(ev, 0.0f);
+      if (fabsf(fabsf(O[ax].hi) - hh[ax].hi) <= fmaxf(1e-10f * hh[ax].hi, ev.tol)) near_event(ev, 0.0f);
       if (hh[ax] < dabs(O[ax])) return 0;
       continue;
     }
@@ -359,8 +376,11 @@ static __device__ __noinline__ int hits_rect(const Leaf64& L, df ox, df oy, df d
   }
   if (an < 0 || af < 0) return 0;
   const float scale = fabsf(tn.hi) + fabsf(tf.hi) + 1.0f;
-  if (fabsf(tf.hi - tn.hi) <= 1e-10f * scale) near_event(ev, tn.hi);
-  if (tn_other.hi > -INFINITY && fabsf(tn.hi - tn_other.hi) <= 1e-10f * scale) near_event(ev, tn.hi);
+  // slab crossings: a lateral shift tol moves each crossing by up to tol / |D| along the ray
+  const float dmin = fmaxf(fminf(fabsf(D[0].hi), fabsf(D[1].hi)), 1e-3f);
+  const float tb = fmaxf(1e-10f * scale, 2.0f * ev.tol / dmin);
+  if (fabsf(tf.hi - tn.hi) <= tb) near_event(ev, tn.hi);
+  if (tn_other.hi > -INFINITY && fabsf(tn.hi - tn_other.hi) <= tb) near_event(ev, tn.hi);
   if (tf < tn) return 0;
   tmin_band(tn, ev);
   if (past_tmin(tn)) {
@@ -382,7 +402,7 @@ static __device__ __noinline__ int hits_rect(const Leaf64& L, df ox, df oy, df d
 
 }
 
-static __device__ __noinline__ int hits_cubic(const Leaf64& L, df ox, df oy, df dx, df dy, Hit64* h, float& ev) {
+static __device__ __noinline__ int hits_cubic(const Leaf64& L, df ox, df oy, df dx, df dy, Hit64* h, Near& ev) {
   int n = 0;
   (void)n;
   const df* v = L.p;
@@ -395,6 +415,8 @@ static __device__ __noinline__ int hits_cubic(const Leaf64& L, df ox, df oy, df 
   const df a1 = dx * c1y - dy * c1x, a2 = dx * c2y - dy * c2x, a3 = dx * c3y - dy * c3x;
   const float scale = fabsf(a0.hi) + fabsf(a1.hi) + fabsf(a2.hi) + fabsf(a3.hi) + 1e-30f;
   const df dd = dx * dx + dy * dy;
+  // f(s) = cross(d, B(s) - o) is |d| times a signed distance: a lateral shift tol moves it by tol |d|
+  const float fb = fmaxf(1e-10f * scale, ev.tol * sqrtf(dd.hi));
   auto f = [&](df s) { return ((a3 * s + a2) * s + a1) * s + a0; };
   auto tof = [&](df s) {
     const df bx = ((c3x * s + c2x) * s + c1x) * s + c0x, by = ((c3y * s + c2y) * s + c1y) * s + c0y;
@@ -425,7 +447,7 @@ static __device__ __noinline__ int hits_cubic(const Leaf64& L, df ox, df oy, df 
     const df lo0 = knots[i], hi0 = knots[i + 1];
     df flo = f(lo0);
     const df fhi = f(hi0);
-    if (i > 0 && fabsf(flo.hi) <= 1e-10f * scale) near_event(ev, tof(lo0).hi);
+    if (i > 0 && fabsf(flo.hi) <= fb) near_event(ev, tof(lo0).hi);
     if (flo.hi == 0.0f) {
       if (nr == 0 || roots[nr - 1] != lo0) roots[nr++] = lo0;
       continue;
@@ -449,8 +471,8 @@ static __device__ __noinline__ int hits_cubic(const Leaf64& L, df ox, df oy, df 
     }
     roots[nr++] = sv;
   }
-  if (fabsf(a0.hi) <= 1e-10f * scale) near_event(ev, tof(DF_ZERO).hi);
-  if (fabsf(f(DF_ONE).hi) <= 1e-10f * scale) near_event(ev, tof(DF_ONE).hi);
+  if (fabsf(a0.hi) <= fb) near_event(ev, tof(DF_ZERO).hi);
+  if (fabsf(f(DF_ONE).hi) <= fb) near_event(ev, tof(DF_ONE).hi);
   for (int i = 0; i < nr; ++i) {
     const df sv = roots[i];
     const df t = tof(sv);
@@ -477,7 +499,7 @@ static __device__ __noinline__ int hits_cubic(const Leaf64& L, df ox, df oy, df 
 
 }
 
-__device__ __forceinline__ int leaf_hits64(const Leaf64& L, df ox, df oy, df dx, df dy, Hit64* h, float& ev) {
+__device__ __forceinline__ int leaf_hits64(const Leaf64& L, df ox, df oy, df dx, df dy, Hit64* h, Near& ev) {
   switch (L.kind) {
     case LEAF_CIRCLE: return hits_circle(L, ox, oy, dx, dy, h, ev);
     case LEAF_SEGMENT: return hits_segment(L, ox, oy, dx, dy, h, ev);
@@ -486,12 +508,13 @@ __device__ __forceinline__ int leaf_hits64(const Leaf64& L, df ox, df oy, df dx,
   }
 }
 
-// closed-set membership of a leaf, with a near-boundary flag
-__device__ __forceinline__ bool leaf_contains64(const Leaf64& L, df px, df py, bool& near) {
+// closed-set membership of a leaf, with a near-boundary flag (within the relative band or
+// within tol, the point's own error bound, of the boundary)
+__device__ __forceinline__ bool leaf_contains64(const Leaf64& L, df px, df py, bool& near, float tol) {
   if (L.kind == LEAF_CIRCLE) {
     const df dx = px - L.p[0], dy = py - L.p[1], r = L.p[2];
     const df m = dx * dx + dy * dy - r * r;
-    if (fabsf(m.hi) <= 1e-10f * r.hi * r.hi) near = true;
+    if (fabsf(m.hi) <= fmaxf(1e-10f * r.hi * r.hi, 2.0f * fabsf(r.hi) * tol)) near = true;
     return !(DF_ZERO < m);
   }
   if (L.kind == LEAF_RECT) {
@@ -499,7 +522,7 @@ __device__ __forceinline__ bool leaf_contains64(const Leaf64& L, df px, df py, b
     const df lx = c * rx + s * ry, ly = c * ry - s * rx;
     const df ex = dabs(lx) - L.p[4], ey = dabs(ly) - L.p[5];
     const df sd = dmax(ex, ey);
-    if (fabsf(sd.hi) <= 1e-10f * (L.p[4].hi + L.p[5].hi)) near = true;
+    if (fabsf(sd.hi) <= fmaxf(1e-10f * (L.p[4].hi + L.p[5].hi), tol)) near = true;
     return !(DF_ZERO < sd);
   }
   return false;
@@ -525,18 +548,19 @@ __device__ __forceinline__ bool prog_eval(const uint8_t* prog, int len, uint64_t
 }
 
 // Object::contains (object.rs:240-259)
-static __device__ __noinline__ bool obj_contains64(const SceneDev& S, uint32_t k, df px, df py, bool& near) {
+static __device__ __noinline__ bool obj_contains64(const SceneDev& S, uint32_t k, df px, df py, bool& near,
+                                                   float tol) {
   const ObjInfo oi = S.info[k];
   if (oi.flags & INFO_NO_CONTAINS) return false;
   uint64_t mask = 0;
   for (int i = 0; i < oi.n_leaves; ++i)
-    if (leaf_contains64(S.leaves[oi.leaf_begin + i], px, py, near)) mask |= 1ull << i;
+    if (leaf_contains64(S.leaves[oi.leaf_begin + i], px, py, near, tol)) mask |= 1ull << i;
   return prog_eval(S.prog + oi.prog_begin, oi.prog_len, mask);
 }
 
 // nearest valid hit of one object (geometry intersect + CSG filter)
 static __device__ __noinline__ bool obj_solve64(const SceneDev& S, uint32_t k, df ox, df oy, df dx, df dy, Hit64& best,
-                                   df& best_d2, float& ev) {
+                                   df& best_d2, Near& ev) {
   const ObjInfo oi = S.info[k];
   const uint8_t* prog = S.prog + oi.prog_begin;
   bool found = false;
@@ -551,7 +575,7 @@ static __device__ __noinline__ bool obj_solve64(const SceneDev& S, uint32_t k, d
         bool near = false;
         uint64_t mask = 0;
         for (int i = 0; i < oi.n_leaves; ++i)
-          if (i != li && leaf_contains64(S.leaves[oi.leaf_begin + i], h[j].px, h[j].py, near)) mask |= 1ull << i;
+          if (i != li && leaf_contains64(S.leaves[oi.leaf_begin + i], h[j].px, h[j].py, near, ev.tol)) mask |= 1ull << i;
         if (near) near_event(ev, h[j].t.hi);
         const bool in1 = prog_eval(prog, oi.prog_len, mask | (1ull << li));
         const bool in0 = prog_eval(prog, oi.prog_len, mask & ~(1ull << li));

@@ -118,7 +118,7 @@ __global__ void k_light_setup(SceneDev S) {
     const df px = df_from_double(L.ox), py = df_from_double(L.oy);
     for (uint32_t k = sl.base; k < sl.base + sl.n; ++k) {
       bool near = false;
-      if ((S.info[k].flags & INFO_MATERIAL) && obj_contains64(S, k, px, py, near)) n = S.info[k].n;
+      if ((S.info[k].flags & INFO_MATERIAL) && obj_contains64(S, k, px, py, near, 0.0f)) n = S.info[k].n;
     }
     L.n0 = n;
   }
@@ -549,7 +549,7 @@ __global__ void __launch_bounds__(256) k_full(SceneDev S, TraceBufs B, uint32_t 
     const SceneLoc sl = scene_of<MULTI>(S, r.scene);
     const ObjScan* sobjs = objs + sl.base;
     df best_d2 = DF_INF, second = DF_INF;
-    float ev = INFINITY;
+    Near ev{INFINITY, ray_tol(r.ex, r.ea)};
     int best = -1;
     Hit64 bh;
     bh.leaf = 0;
@@ -599,8 +599,11 @@ __global__ void __launch_bounds__(256) k_full(SceneDev S, TraceBufs B, uint32_t 
       }
     }
     uint8_t fl = sc.overflow ? LG_PATH_FALLBACK : 0;
-    if (best >= 0 && second.hi < INFINITY && (second - best_d2).hi <= 1e-10f * best_d2.hi) fl |= LG_PATH_NEAR_DEGENERATE;
-    store_hit(B.hit[idx], best, bh, ev, fl);
+    // a tie between two objects, within the band or within what the ray's error bound moves d2
+    if (best >= 0 && second.hi < INFINITY &&
+        (second - best_d2).hi <= fmaxf(1e-10f * best_d2.hi, 4.0f * sqrtf(best_d2.hi) * ev.tol))
+      fl |= LG_PATH_NEAR_DEGENERATE;
+    store_hit(B.hit[idx], best, bh, ev.ev, fl);
   }
   atomicAdd(&blk_solves, my_solves);
   __syncthreads();
@@ -653,7 +656,7 @@ __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, c
       df n2 = DF_ONE;
       uint16_t m2 = MEDIUM_AIR;
       bool near = false;
-      if (obj_contains64(S, sl.base + (uint32_t)best, DF_HALF * (ox + bh.px), DF_HALF * (oy + bh.py), near)) {
+      if (obj_contains64(S, sl.base + (uint32_t)best, DF_HALF * (ox + bh.px), DF_HALF * (oy + bh.py), near, L)) {
         const float px32 = bh.px.hi, py32 = bh.py.hi;
         for (uint32_t k = 0; k < sl.n; ++k) {
           if ((int)k == best) continue;
@@ -662,7 +665,7 @@ __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, c
           const float ex = px32 - h.x, ey = py32 - h.y;
           const float tol = 2e-6f * (fabsf(px32) + fabsf(py32) + fabsf(h.x) + fabsf(h.y) + h.z) + 1e-6f;
           if (ex * ex + ey * ey > (h.z + tol) * (h.z + tol)) continue;
-          if (obj_contains64(S, sl.base + k, bh.px, bh.py, near)) {
+          if (obj_contains64(S, sl.base + k, bh.px, bh.py, near, L)) {
             n2 = S.info[sl.base + k].n;
             m2 = (uint16_t)k;
             break;
@@ -750,7 +753,7 @@ __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, c
     canvas.p[0] = DF_ZERO; canvas.p[1] = DF_ZERO; canvas.p[2] = DF_ONE; canvas.p[3] = DF_ZERO;
     canvas.p[4] = sl.aspect; canvas.p[5] = DF_ONE;
     Hit64 ch[3];
-    float cev = INFINITY;
+    Near cev{INFINITY, ray_tol(r.ex, r.ea)};
     const int nh = leaf_hits64(canvas, ox, oy, dx, dy, ch, cev);
     if (nh > 0) {
       int bi = 0;
@@ -760,7 +763,7 @@ __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, c
       v.x1 = ch[bi].px.hi; v.y1 = ch[bi].py.hi;
       v.hit = -1;
       const float L = r.ex + ch[bi].t.hi * r.ea;
-      v.flags = fl | (cev < INFINITY || L > ILL_COND ? LG_PATH_NEAR_DEGENERATE : 0);
+      v.flags = fl | (cev.ev < INFINITY || L > ILL_COND ? LG_PATH_NEAR_DEGENERATE : 0);
     }
   }
   // children: the next generation skips colours below the cutoff (tracer.rs:378-384)

@@ -33,6 +33,10 @@ class ParityReport:
     color_mismatch_unflagged: int
     max_endpoint_err: float
     flagged: int
+    # the flagged pairs present on both sides, compared anyway (informative, not a bar)
+    flagged_matched: int = 0
+    flagged_hit_mismatch: int = 0
+    flagged_max_endpoint_err: float = 0.0
 
     def ok(self) -> bool:
         return (self.gpu_only_unflagged == 0 and self.oracle_only_unflagged == 0 and
@@ -70,6 +74,14 @@ def compare(g_segs, g_paths, o_segs, o_paths, o_s64, primary_filter=None) -> Par
         max_err = float(err.max())
     else:
         max_err = 0.0
+    fg, fo = ig[flagged], io[flagged]
+    f_hit = int((g_paths["hit"][fg] != o_paths["hit"][fo]).sum())
+    if len(fg):
+        gpf = np.stack([g_segs["x0"][fg], g_segs["y0"][fg], g_segs["x1"][fg], g_segs["y1"][fg]], 1)
+        f_err = float((np.abs(gpf.astype(np.float64) - o_s64[fo]) / np.maximum(1.0, np.abs(o_s64[fo]))).max())
+    else:
+        f_err = 0.0
+
     def excused(key, own_flag, other_index, other_flag):
         # flagged on its own side, or its parent is flagged on the other side (the trees
         # diverged below a near-degenerate decision)
@@ -86,7 +98,8 @@ def compare(g_segs, g_paths, o_segs, o_paths, o_s64, primary_filter=None) -> Par
     g_only_unf = sum(1 for k in g_only if not excused(k, gflag[gi[k]], oi, oflag))
     o_only_unf = sum(1 for k in o_only if not excused(k, oflag[oi[k]], gi, gflag))
     return ParityReport(len(common), len(g_only), len(o_only), g_only_unf, o_only_unf, hit_mm, col_mm, max_err,
-                        int(flagged.sum()) + len(g_only) + len(o_only) - g_only_unf - o_only_unf)
+                        int(flagged.sum()) + len(g_only) + len(o_only) - g_only_unf - o_only_unf,
+                        int(len(fg)), f_hit, f_err)
 
 
 def rel_l2(a: np.ndarray, b: np.ndarray) -> float:

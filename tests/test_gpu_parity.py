@@ -249,3 +249,21 @@ def test_no_scene_and_truncation(gpu):
         buf = (abi.lg_segment * 4)()
         assert c.lib.lg_segments_download(c.h, buf, None, 4, C.byref(n)) == abi.LG_ERR_TRUNCATED
         assert n.value > 4
+
+
+def test_streaming_frame_matches_single_pass(gpu):
+    """A frame rendered with the accumulation interleaved between generations (the mode
+    lg_render switches to when a frame has more segments than its ring threshold) equals the
+    single-pass frame bit for bit, string-mod overlay included."""
+    from light_garden_gb300.runtime import Context
+    pk = W.csg_scene(total_rays=1 << 14, width=640, height=480).packed()
+    with Context() as a:
+        a.upload(pk)
+        ref, st_ref = a.render()
+    with Context(stream_segments=20000) as b:
+        b.upload(pk)
+        img, st = b.render()
+        img2, st2 = b.render()
+    assert st_ref["segments"] > 3 * 20000  # several accumulation passes
+    assert np.array_equal(img, ref) and np.array_equal(img2, ref)
+    assert st["segments"] == st_ref["segments"] and st["pixels"] == st_ref["pixels"]
