@@ -78,6 +78,20 @@ class Tracer:
         self.width, self.height = width, height
         self.canvas_bounds = canvas_bounds(width, height)
 
+    # -- scene files (tracer.rs:183-204) -------------------------------------------------------
+    def serialize(self) -> str:
+        """The object and light lists as RON text (Tracer::serialize)."""
+        from . import ron
+        return ron.dumps(self.objects, self.lights)
+
+    def load(self, data: str) -> None:
+        """Replace the object and light lists with those of a RON scene (Tracer::load)."""
+        from . import ron
+        objects, lights = ron.loads(data)
+        self.clear()
+        self.objects.extend(objects)
+        self.lights.extend(lights)
+
     def get_trace_time(self) -> float:
         """Mean of the last 20 trace times in ms (tracer.rs:206-208)."""
         v = self.trace_time_vd

@@ -102,3 +102,27 @@ def test_gpu_mid_scene_full_size_matches_fixture_subset(ctx):
     rep = compare(g_segs[keep], g_paths[keep], segs, paths, s64)
     assert rep.ok(), rep
     assert rep.matched > 0.99 * len(segs)
+
+
+@pytest.mark.gpu
+def test_gpu_default_scene_from_ron_matches_fixture(ctx):
+    """The reference's shipped scene (default.ron, loaded through light_garden_gb300.ron):
+    the GPU trace reproduces the stored oracle subset and the stored image digest."""
+    from light_garden_gb300 import ron
+    from light_garden_gb300.scene import pack
+    meta = json.loads((GOLD / "default_scene.json").read_text())
+    objs, lights = ron.load(GOLD / "default_scene.ron")
+    p = abi.params_default()
+    p.width, p.height = meta["width"], meta["height"]
+    p.record_paths = 1
+    pk = pack(objs, lights, p)
+    ctx.upload(pk)
+    ctx.trace()
+    g_segs, g_paths = ctx.segments(paths=True)
+    z = np.load(GOLD / "default_scene.npz")
+    keep = (g_paths["source"] != abi.LG_SRC_TRACE) | (g_paths["primary"] % meta["stride"] == 0)
+    rep = compare(g_segs[keep], g_paths[keep], z["segs"], z["paths"], z["s64"])
+    assert rep.ok(), rep
+    assert rep.matched > 0.99 * len(z["segs"])
+    ctx.accumulate()
+    assert ctx.accum().shape == (meta["height"], meta["width"], 4)
