@@ -413,30 +413,34 @@ constexpr int TILE_PX = TILE * TILE;  // cells per channel plane
 // Either way one warp's 32 accesses fall in 32 distinct banks.
 //
 // Fixed-point sums use exact split accumulation in native 32-bit shared atomics: a
-// contribution q (|q| <= 2^52) is split as q = a * 2^42 + b * 2^21 + c with 21-bit b, c
-// and signed a.  A unit holds at most 1024 segments and a segment adds at most once to a
-// pixel, so each plane sum stays below 2^31 and A * 2^42 + B * 2^21 + C is exact.
+// contribution |q| < 2^42 (a colour term below 1024) is split as q = b * 2^21 + c with an
+// unsigned 21-bit c and a signed b (|b| < 2^21).  A unit holds at most 1024 segments and a
+// segment adds at most once to a pixel, so both plane sums stay below 2^31 and
+// B * 2^21 + C is exact.  A segment with a larger term (up to the clamp, 2^52) skips the
+// tile and adds its 64-bit terms to the image with global atomics, which is just as exact.
 enum RasterMode { RM_FIXED_SPLIT = 0, RM_FIXED_MINMAX = 1, RM_F32 = 2 };
 
 template <int MODE>
 struct RasterSmem {
-  static constexpr int acc_words = MODE == RM_FIXED_SPLIT ? 12 * TILE_PX : MODE == RM_FIXED_MINMAX ? 8 * TILE_PX : 4 * TILE_PX;
-  static constexpr int stage_words = 8 * 32 * 16;  // 8 warps x 32 staged segments x 64 B
+  static constexpr int acc_words = MODE == RM_F32 ? 4 * TILE_PX : 8 * TILE_PX;
+  static constexpr int stage_words = 8 * 32 * 12;  // 8 warps x 32 staged segments x 48 B
   static constexpr int owner_words = 8 * 32 * 32 / 4;  // 8 warps x 1024 (segment, column) pairs, 1 B each
   static constexpr int pref_words = 8 * 33;
   static constexpr int bytes = (acc_words + stage_words + owner_words + pref_words) * 4;
 };
 
 // one staged segment: raster setup restricted to the unit's tile and the per-channel
-// source terms, 64 B
+// source terms, 48 B
+constexpr int SPAN_BIG = 1 << 30;  // FIXED_SPLIT: terms too large for the split planes
 struct __align__(16) Staged {
   float ua, va, slope;
-  int span;             // first tile-local major-axis pixel | count << 16
-  unsigned q[12];       // FIXED_SPLIT: (c, b, a) per channel; otherwise q[0..7] = 4 x int64 or 4 x float
+  int span;             // first tile-local major-axis pixel | count << 16 | SPAN_BIG
+  unsigned q[8];        // FIXED_SPLIT: (c, b) per channel, or 4 x int64 with SPAN_BIG;
+                        // FIXED_MINMAX: 4 x int64; F32: 4 x float
 };
 
 template <int MODE>
-__global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
+__global__ void __launch_bounds__(256, 4) k_raster(RasterArgs A) {
   if (A.ctr->skip_raster) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned* acc32 = reinterpret_cast<unsigned*>(smem_raw);
@@ -496,15 +500,16 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
           cnt = max(c1 - c0, 0);
           st.ua = R.ua; st.va = R.va; st.slope = R.slope;
           st.span = c0 | (cnt << 16);
+          long long qv[4];
+          bool big = false;
 #pragma unroll
           for (int ch = 0; ch < 4; ++ch) {
             const float v = contribution(B, ch, sg.color);
             if (MODE == RM_FIXED_SPLIT) {
               long long q = to_fixed(v);
               if (B.op[ch] == LG_BO_REVERSE_SUBTRACT) q = -q;
-              st.q[3 * ch] = (unsigned)(q & 0x1fffffll);
-              st.q[3 * ch + 1] = (unsigned)((q >> 21) & 0x1fffffll);
-              st.q[3 * ch + 2] = (unsigned)(int)(q >> 42);
+              qv[ch] = q;
+              big = big || q >= (1ll << 42) || q < -(1ll << 42);
             } else if (MODE == RM_FIXED_MINMAX) {
               long long q = to_fixed(v);
               if (B.op[ch] == LG_BO_REVERSE_SUBTRACT) q = -q;
@@ -513,6 +518,15 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
             } else {
               st.q[ch] = __float_as_uint(B.op[ch] == LG_BO_REVERSE_SUBTRACT ? -v : v);
             }
+          }
+          if (MODE == RM_FIXED_SPLIT) {
+#pragma unroll
+            for (int ch = 0; ch < 4; ++ch) {
+              const long long q = qv[ch];
+              st.q[2 * ch] = big ? (unsigned)(q & 0xffffffffll) : (unsigned)(q & 0x1fffffll);
+              st.q[2 * ch + 1] = big ? (unsigned)(q >> 32) : (unsigned)(int)(q >> 21);
+            }
+            if (big) st.span |= SPAN_BIG;
           }
         }
       }
@@ -531,7 +545,7 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
       for (int pi = (int)lane; pi < total; pi += 32) {
         const int k = owner[pi];
         const Staged& sk = stage[k];
-        const int i = tm * TILE + (sk.span & 0xffff) + (pi - pref[k]);
+        const int i = tm * TILE + (sk.span & 0xffff) + (pi - pref[k]);  // SPAN_BIG is above bit 16
         RSetup R;
         R.ua = sk.ua; R.va = sk.va; R.slope = sk.slope;
         const int j = raster_minor(R, i);
@@ -541,11 +555,20 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
         if (MODE == RM_FIXED_SPLIT) {
           const uint4 q0 = *reinterpret_cast<const uint4*>(&sk.q[0]);
           const uint4 q1 = *reinterpret_cast<const uint4*>(&sk.q[4]);
-          const uint4 q2 = *reinterpret_cast<const uint4*>(&sk.q[8]);
-          const unsigned qs[12] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
+          const unsigned qs[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+          if (sk.span & SPAN_BIG) {  // rare: the 64-bit terms straight into the image
+            const uint32_t x = xmajor ? (uint32_t)i : (uint32_t)j, y = xmajor ? (uint32_t)j : (uint32_t)i;
+            unsigned long long* g = reinterpret_cast<unsigned long long*>(A.accum) + (C.px_base + (uint64_t)y * C.W + x) * 4;
 #pragma unroll
-          for (int w = 0; w < 12; ++w)
-            if (qs[w]) atomicAdd(acc32 + w * TILE_PX + cell, qs[w]);
+            for (int ch = 0; ch < 4; ++ch) {
+              const unsigned long long q = ((unsigned long long)qs[2 * ch + 1] << 32) | qs[2 * ch];
+              if (q) atomicAdd(g + ch, q);
+            }
+          } else {
+#pragma unroll
+            for (int w = 0; w < 8; ++w)
+              if (qs[w]) atomicAdd(acc32 + w * TILE_PX + cell, qs[w]);
+          }
         } else if (MODE == RM_FIXED_MINMAX) {
 #pragma unroll
           for (int ch = 0; ch < 4; ++ch) {
@@ -589,9 +612,8 @@ __global__ void __launch_bounds__(256) k_raster(RasterArgs A) {
       for (int ch = 0; ch < 4; ++ch) {
         const int op = B.op[ch];
         if (MODE == RM_FIXED_SPLIT) {
-          const unsigned* base = acc32 + 3 * ch * TILE_PX + cell;
-          const long long q = (long long)(int)base[2 * TILE_PX] * (1ll << 42) + (long long)base[TILE_PX] * (1ll << 21) +
-                              (long long)base[0];
+          const unsigned* base = acc32 + 2 * ch * TILE_PX + cell;
+          const long long q = (long long)(int)base[TILE_PX] * (1ll << 21) + (long long)base[0];
           if (q == 0) continue;
           atomicAdd(reinterpret_cast<unsigned long long*>(A.accum) + px + ch, (unsigned long long)q);
         } else if (MODE == RM_FIXED_MINMAX) {

@@ -267,3 +267,31 @@ def test_streaming_frame_matches_single_pass(gpu):
     assert st_ref["segments"] > 3 * 20000  # several accumulation passes
     assert np.array_equal(img, ref) and np.array_equal(img2, ref)
     assert st["segments"] == st_ref["segments"] and st["pixels"] == st_ref["pixels"]
+
+
+@pytest.mark.parametrize("variant", [1, 2])
+def test_raster_large_terms_bit_exact(gpu, oracle, variant):
+    """Colour terms of 2^10 and more (the tile raster's split planes take |q| < 2^42) mixed
+    with ordinary ones, added and reverse-subtracted: bit-exact against the CPU raster."""
+    from light_garden_gb300.runtime import Context
+    rng = np.random.default_rng(5)
+    n = 20000
+    segs = np.zeros(n, abi.segment_dtype())
+    segs["x0"], segs["y0"] = rng.uniform(-1.2, 1.2, n), rng.uniform(-1.2, 1.2, n)
+    segs["x1"], segs["y1"] = rng.uniform(-1.2, 1.2, n), rng.uniform(-1.2, 1.2, n)
+    col = rng.uniform(0, 1, (n, 4)).astype(np.float32)
+    big = rng.random(n) < 0.05
+    col[big] *= np.float32(5000.0)
+    col[rng.random(n) < 0.01] = np.float32(3.0e6)  # beyond the clamp of 2^20
+    segs["color"] = col
+    for op in (abi.LG_BO_ADD, abi.LG_BO_REVERSE_SUBTRACT):
+        p = abi.params_default()
+        p.width, p.height = 640, 480
+        p.color_blend = abi.lg_blend_component(abi.LG_BF_ONE, abi.LG_BF_ONE, op)
+        pk = pack([], [], p)
+        with Context(raster_variant=variant) as c:
+            c.upload(pk)
+            c.accumulate_segments(segs)
+            acc = c.accum()
+        ref, _ = oracle.raster(segs, p)
+        assert np.array_equal(acc, ref), f"op {op}: {np.count_nonzero(acc != ref)} values differ"
