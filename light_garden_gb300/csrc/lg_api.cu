@@ -453,7 +453,7 @@ lg_status enqueue_accumulate(lg_ctx* c, int binned_event = -1) {
   k_bin_count<<<c->bin_grid, 256, bsm, c->stream>>>(A, smem_tiles);
   k_scan_tiles<<<1, 1024, 0, c->stream>>>(A);
   k_build_units<<<std::max(1u, (2 * c->n_tiles + 255) / 256), 256, 0, c->stream>>>(A);
-  k_bin_scatter<<<c->bin_grid, 256, bsm, c->stream>>>(A, smem_tiles);
+  k_bin_scatter<<<scatter_grid(c->n_sm, smem_tiles), SCATTER_THREADS, bsm, c->stream>>>(A, smem_tiles);
   if (binned_event >= 0) {
     lg_status st = stage_event(c, binned_event);
     if (st) return st;
@@ -917,7 +917,7 @@ static lg_status enqueue_stream_frame(lg_ctx* c, uint16_t* dst, size_t row, cuda
       k_tiles_apply<<<n_part, 1024, 0, c->stream>>>(A, (const unsigned long long*)c->d_part.p);
     }
     k_build_units<<<std::max(1u, (bins + 255) / 256), 256, 0, c->stream>>>(A);
-    k_bin_scatter<<<c->bin_grid, 256, bsm, c->stream>>>(A, smem_tiles);
+    k_bin_scatter<<<scatter_grid(c->n_sm, smem_tiles), SCATTER_THREADS, bsm, c->stream>>>(A, smem_tiles);
     if (c->raster_variant == 2) {
       if (mode == RM_F32_)
         k_raster_warp<RM_F32_><<<c->raster_warp_grid, 32, raster_warp_smem_bytes(), c->stream>>>(A);

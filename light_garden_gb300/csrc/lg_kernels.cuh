@@ -69,6 +69,12 @@ __global__ void k_bin_count(RasterArgs A, int smem_tiles);
 __global__ void k_scan_tiles(RasterArgs A);
 __global__ void k_build_units(RasterArgs A);
 __global__ void k_bin_scatter(RasterArgs A, int smem_tiles);
+// One CTA of 1024 threads per SM: each CTA fills its own range of every tile list, so the
+// partially written 32 B sectors still open are CTAs x tiles; with one CTA per SM they stay
+// in L2 and are written back whole (8 CTAs per SM overflowed L2 and turned every 4 B
+// reference into a DRAM read-modify-write).
+constexpr int SCATTER_THREADS = 1024;
+inline int scatter_grid(int n_sm, int smem_tiles) { return smem_tiles ? n_sm : 2 * n_sm; }
 template <int MODE>
 __global__ void k_raster(RasterArgs A);
 int raster_smem_bytes(int mode);

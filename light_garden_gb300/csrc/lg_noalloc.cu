@@ -183,7 +183,7 @@ extern "C" lg_status lg_accumulate_segments_noalloc(const lg_segment* segments, 
   k_bin_count<<<d->n_sm * 8, 256, bsm, s>>>(A, smem_tiles);
   k_scan_tiles<<<1, 1024, 0, s>>>(A);
   k_build_units<<<(bins + 255) / 256, 256, 0, s>>>(A);
-  k_bin_scatter<<<d->n_sm * 8, 256, bsm, s>>>(A, smem_tiles);
+  k_bin_scatter<<<scatter_grid(d->n_sm, smem_tiles), SCATTER_THREADS, bsm, s>>>(A, smem_tiles);
   if (mode == RM_FIXED_SPLIT_)
     k_raster<RM_FIXED_SPLIT_><<<d->raster_grid, 256, rsm, s>>>(A);
   else if (mode == RM_FIXED_MINMAX_)

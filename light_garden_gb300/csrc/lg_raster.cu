@@ -358,7 +358,7 @@ __global__ void k_build_units(RasterArgs A) {
 // Scatter of segment ids into the per-tile lists.  With shared-memory tiles a CTA counts
 // its own segments per tile, reserves one range per touched tile with a single global
 // atomic, and fills the ranges through shared-memory cursors.
-__global__ void __launch_bounds__(256) k_bin_scatter(RasterArgs A, int smem_tiles) {
+__global__ void __launch_bounds__(SCATTER_THREADS) k_bin_scatter(RasterArgs A, int smem_tiles) {
   if (A.ctr->skip_raster) return;
   extern __shared__ unsigned cur[];  // slots are < refs_cap < 2^32
   const uint64_t n = n_segments(A);

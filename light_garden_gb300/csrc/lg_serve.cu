@@ -301,7 +301,7 @@ lg_status serve_raster(lg_ctx* c, ServeState& V) {
     }
     if (bins) {
       k_build_units<<<std::max(1u, (bins + 255) / 256), 256, 0, c->stream>>>(A);
-      k_bin_scatter<<<c->n_sm * 8, 256, 0, c->stream>>>(A, 0);
+      k_bin_scatter<<<scatter_grid(c->n_sm, 0), SCATTER_THREADS, 0, c->stream>>>(A, 0);
       k_raster<RM_FIXED_SPLIT_><<<c->raster_grid, 256, (size_t)raster_smem_bytes(RM_FIXED_SPLIT_), c->stream>>>(A);
     }
     k_stream_rotate<<<1, 1, 0, c->stream>>>(dctr, c->seg_cap);

@@ -783,7 +783,7 @@ __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, c
 }
 
 template <bool MULTI>
-__global__ void __launch_bounds__(256) k_bounce(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
+__global__ void __launch_bounds__(256, 3) k_bounce(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
   __shared__ unsigned long long blk_visits, blk_near;
