@@ -61,7 +61,10 @@ enum lg_geo_kind {
   LG_GEO_RECT = 1,    /* GeoRect    { origin (centre), rotation, width, height }    */
   LG_GEO_SEGMENT = 2, /* GeoLineSegment a -> b (straight mirror)                    */
   LG_GEO_CUBIC = 3,   /* GeoCubicBezier P0..P3 (curved mirror)                      */
-  LG_GEO_LOGIC = 4    /* GeoLogic   { op, a, b, origin, rotation } (CSG)            */
+  LG_GEO_LOGIC = 4,   /* GeoLogic   { op, a, b, origin, rotation } (CSG)            */
+  LG_GEO_POLYGON = 5, /* convex polygon { points } (ConvexPolygon, object.rs:13,34-36) */
+  LG_GEO_ELLIPSE = 6, /* Ellipse { origin, a, b, rot } (object.rs:14,37-44)         */
+  LG_GEO_VERTICES = 7 /* continuation of a POLYGON's vertex list                   */
 };
 
 /* Logic / LogicOp (src/light_garden/mod.rs:366-372: geo_a & geo_b, |, and_not) */
@@ -73,13 +76,18 @@ enum lg_logic_op { LG_OP_AND = 0, LG_OP_OR = 1, LG_OP_AND_NOT = 2 };
 typedef struct lg_geo {
   int32_t kind;     /* enum lg_geo_kind */
   int32_t op;       /* LOGIC: enum lg_logic_op */
-  int32_t a, b;     /* LOGIC: child node indices */
-  double origin[2]; /* CIRCLE centre | RECT centre | LOGIC origin */
-  double rot[2];    /* RECT / LOGIC rotation as (cos, sin); (1, 0) = identity */
+  int32_t a, b;     /* LOGIC: child node indices.  POLYGON: a = vertex count (3..63),
+                       b = index of the VERTICES node holding vertices 4.. (-1: none);
+                       VERTICES: b = the next VERTICES node (-1: none) */
+  double origin[2]; /* CIRCLE centre | RECT centre | LOGIC / POLYGON origin | ELLIPSE centre */
+  double rot[2];    /* RECT / LOGIC / POLYGON / ELLIPSE rotation as (cos, sin); (1, 0) = identity */
   double v[8];      /* CIRCLE: v[0] = radius
                        RECT:   v[0] = width, v[1] = height
                        SEGMENT: (v[0], v[1]) -> (v[2], v[3])
-                       CUBIC:  P0 = (v[0], v[1]) ... P3 = (v[6], v[7]) */
+                       CUBIC:  P0 = (v[0], v[1]) ... P3 = (v[6], v[7])
+                       POLYGON / VERTICES: up to 4 vertices (x, y), in the node's frame, in
+                               order around a convex polygon (either orientation)
+                       ELLIPSE: v[0] = a (semi-axis along the rotated x), v[1] = b */
 } lg_geo;
 
 /* ---- objects: ObjectE + Option<Material> (src/light_garden/object.rs:7-16,51-55) ------ */
@@ -89,8 +97,8 @@ enum lg_object_kind {
   LG_OBJ_CIRCLE = 2,
   LG_OBJ_RECT = 3,
   LG_OBJ_LENS = 4,            /* Logic(And, circle, circle), object.rs:387-415 */
-  LG_OBJ_CONVEX_POLYGON = 5,  /* not on this path: lg_scene_upload returns LG_ERR_UNSUPPORTED */
-  LG_OBJ_ELLIPSE = 6,         /* not on this path: lg_scene_upload returns LG_ERR_UNSUPPORTED */
+  LG_OBJ_CONVEX_POLYGON = 5,  /* root must be a POLYGON */
+  LG_OBJ_ELLIPSE = 6,         /* root must be an ELLIPSE */
   LG_OBJ_GEO = 7              /* any geometry tree (CSG results, object.rs:107-113) */
 };
 

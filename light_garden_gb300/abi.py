@@ -33,7 +33,8 @@ STATUS_NAMES = {
     8: "LG_ERR_BUDGET", 9: "LG_ERR_NOT_READY", 10: "LG_ERR_NOT_FOUND",
 }
 
-LG_GEO_CIRCLE, LG_GEO_RECT, LG_GEO_SEGMENT, LG_GEO_CUBIC, LG_GEO_LOGIC = range(5)
+(LG_GEO_CIRCLE, LG_GEO_RECT, LG_GEO_SEGMENT, LG_GEO_CUBIC, LG_GEO_LOGIC, LG_GEO_POLYGON, LG_GEO_ELLIPSE,
+ LG_GEO_VERTICES) = range(8)
 LG_OP_AND, LG_OP_OR, LG_OP_AND_NOT = range(3)
 (LG_OBJ_STRAIGHT_MIRROR, LG_OBJ_CURVED_MIRROR, LG_OBJ_CIRCLE, LG_OBJ_RECT, LG_OBJ_LENS,
  LG_OBJ_CONVEX_POLYGON, LG_OBJ_ELLIPSE, LG_OBJ_GEO) = range(8)

@@ -46,9 +46,70 @@ lg_status flatten_node(std::string& err, const lg_geo* G, uint32_t n_geo, int32_
     prog.push_back(g.op == LG_OP_AND ? PROG_AND : g.op == LG_OP_OR ? PROG_OR : PROG_AND_NOT);
     return LG_OK;
   }
+  if (g.kind == LG_GEO_POLYGON) {
+    // a convex polygon is the And of its edges' half-planes
+    const int n = g.a;
+    if (n < 3 || n > 63) return set_err(err, LG_ERR_INVALID_ARGUMENT, "a polygon has 3..63 vertices");
+    std::vector<double> vx, vy;
+    const lg_geo* cur = &g;
+    for (int k = 0; k < n; ++k) {
+      if (k > 0 && k % 4 == 0) {
+        if (cur->b < 0 || (uint32_t)cur->b >= n_geo || G[cur->b].kind != LG_GEO_VERTICES)
+          return set_err(err, LG_ERR_INVALID_ARGUMENT, "polygon vertex chain broken");
+        cur = &G[cur->b];
+      }
+      vx.push_back(cur->v[2 * (k % 4)]);
+      vy.push_back(cur->v[2 * (k % 4) + 1]);
+    }
+    double area = 0.0;
+    for (int k = 0; k < n; ++k) area += vx[k] * vy[(k + 1) % n] - vy[k] * vx[(k + 1) % n];
+    if (area == 0.0) return set_err(err, LG_ERR_INVALID_ARGUMENT, "degenerate polygon");
+    const double sg = area > 0.0 ? 1.0 : -1.0;
+    Xf T2;
+    T.apply(g.origin[0], g.origin[1], T2.ox, T2.oy);
+    T2.c = T.c * g.rot[0] - T.s * g.rot[1];
+    T2.s = T.s * g.rot[0] + T.c * g.rot[1];
+    std::vector<double> wx(n), wy(n);
+    double box[4] = {INFINITY, INFINITY, -INFINITY, -INFINITY};
+    for (int k = 0; k < n; ++k) {
+      T2.apply(vx[k], vy[k], wx[k], wy[k]);
+      box[0] = std::min(box[0], wx[k]); box[1] = std::min(box[1], wy[k]);
+      box[2] = std::max(box[2], wx[k]); box[3] = std::max(box[3], wy[k]);
+    }
+    for (int k = 0; k < n; ++k) {
+      const double ex = wx[(k + 1) % n] - wx[k], ey = wy[(k + 1) % n] - wy[k], l = std::sqrt(ex * ex + ey * ey);
+      if (!(l > 0.0)) return set_err(err, LG_ERR_INVALID_ARGUMENT, "polygon with a zero-length edge");
+      LeafH H;
+      std::memset(&H, 0, sizeof H);
+      H.kind = LEAF_HALFPLANE;
+      H.p[0] = wx[k];
+      H.p[1] = wy[k];
+      H.p[2] = sg * ey / l;  // outward: right of a counter-clockwise edge
+      H.p[3] = -sg * ex / l;
+      for (int i = 0; i < 4; ++i) H.box[i] = box[i];
+      const uint32_t li = (uint32_t)F.leaves.size() - leaf0;
+      if (li >= (uint32_t)MAX_LEAVES - 1) return set_err(err, LG_ERR_UNSUPPORTED, "more than 63 leaves in one object");
+      F.leaves.push_back(H);
+      prog.push_back((uint8_t)li);
+      if (k > 0) prog.push_back(PROG_AND);
+    }
+    return LG_OK;
+  }
   LeafH L;
   std::memset(&L, 0, sizeof L);
   switch (g.kind) {
+    case LG_GEO_ELLIPSE: {
+      if (!(g.v[0] > 0.0) || !(g.v[1] > 0.0)) return set_err(err, LG_ERR_INVALID_ARGUMENT, "ellipse axes must be > 0");
+      L.kind = LEAF_ELLIPSE;
+      T.apply(g.origin[0], g.origin[1], L.p[0], L.p[1]);
+      L.p[2] = T.c * g.rot[0] - T.s * g.rot[1];
+      L.p[3] = T.s * g.rot[0] + T.c * g.rot[1];
+      L.p[4] = g.v[0];
+      L.p[5] = g.v[1];
+      L.p[6] = 1.0 / g.v[0];
+      L.p[7] = 1.0 / g.v[1];
+      break;
+    }
     case LG_GEO_CIRCLE:
       L.kind = LEAF_CIRCLE;
       T.apply(g.origin[0], g.origin[1], L.p[0], L.p[1]);
@@ -93,6 +154,10 @@ double leaf_extent(const LeafH& L, double cx, double cy) {
     case LEAF_CIRCLE: return d(L.p[0], L.p[1]) + std::fabs(L.p[2]);
     case LEAF_RECT: return d(L.p[0], L.p[1]) + std::hypot(L.p[4], L.p[5]);
     case LEAF_SEGMENT: return std::max(d(L.p[0], L.p[1]), d(L.p[2], L.p[3]));
+    case LEAF_ELLIPSE: return d(L.p[0], L.p[1]) + std::max(L.p[4], L.p[5]);
+    case LEAF_HALFPLANE:
+      return std::max(std::max(d(L.box[0], L.box[1]), d(L.box[2], L.box[3])),
+                      std::max(d(L.box[0], L.box[3]), d(L.box[2], L.box[1])));
     default: {
       double m = 0;
       for (int k = 0; k < 4; ++k) m = std::max(m, d(L.p[2 * k], L.p[2 * k + 1]));
@@ -122,6 +187,18 @@ void leaf_box(const LeafH& L, double& x0, double& y0, double& x1, double& y1) {
     case LEAF_SEGMENT:
       add(L.p[0], L.p[1]);
       add(L.p[2], L.p[3]);
+      break;
+    case LEAF_ELLIPSE: {
+      const double c = L.p[2], s = L.p[3];
+      const double ex = std::sqrt(L.p[4] * L.p[4] * c * c + L.p[5] * L.p[5] * s * s);
+      const double ey = std::sqrt(L.p[4] * L.p[4] * s * s + L.p[5] * L.p[5] * c * c);
+      add(L.p[0] - ex, L.p[1] - ey);
+      add(L.p[0] + ex, L.p[1] + ey);
+      break;
+    }
+    case LEAF_HALFPLANE:
+      add(L.box[0], L.box[1]);
+      add(L.box[2], L.box[3]);
       break;
     default:
       for (int k = 0; k < 4; ++k) add(L.p[2 * k], L.p[2 * k + 1]);
@@ -158,15 +235,15 @@ lg_status flatten_scene(std::string& err, const lg_geo* G, uint32_t n_geo, const
                         const lg_light* Ls, uint32_t n_lights, Flat& F) {
   for (uint32_t k = 0; k < n_obj; ++k) {
     const lg_object& o = O[k];
-    if (o.kind == LG_OBJ_CONVEX_POLYGON || o.kind == LG_OBJ_ELLIPSE)
-      return set_err(err, LG_ERR_UNSUPPORTED, "object " + std::to_string(k) + ": ConvexPolygon / Ellipse are not on this path");
     if (o.kind < 0 || o.kind > LG_OBJ_GEO) return set_err(err, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": unknown kind");
     if (o.geo < 0 || (uint32_t)o.geo >= n_geo) return set_err(err, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": geometry index out of range");
     const int rk = G[o.geo].kind;
     const bool ok = (o.kind == LG_OBJ_STRAIGHT_MIRROR && rk == LG_GEO_SEGMENT) ||
                     (o.kind == LG_OBJ_CURVED_MIRROR && rk == LG_GEO_CUBIC) ||
                     (o.kind == LG_OBJ_CIRCLE && rk == LG_GEO_CIRCLE) || (o.kind == LG_OBJ_RECT && rk == LG_GEO_RECT) ||
-                    (o.kind == LG_OBJ_LENS && rk == LG_GEO_LOGIC) || o.kind == LG_OBJ_GEO;
+                    (o.kind == LG_OBJ_LENS && rk == LG_GEO_LOGIC) ||
+                    (o.kind == LG_OBJ_CONVEX_POLYGON && rk == LG_GEO_POLYGON) ||
+                    (o.kind == LG_OBJ_ELLIPSE && rk == LG_GEO_ELLIPSE) || o.kind == LG_OBJ_GEO;
     if (!ok) return set_err(err, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": kind does not match its geometry");
     if (o.has_material && !(o.refractive_index > 0.0))
       return set_err(err, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": refractive index must be > 0");
@@ -201,12 +278,13 @@ lg_status flatten_scene(std::string& err, const lg_geo* G, uint32_t n_geo, const
     s.cy = (float)cy;
     s.R = (float)(R * (1.0 + 1e-6) + 1e-6 * (1.0 + std::fabs(cx) + std::fabs(cy)));
     const uint32_t nl = oi.n_leaves;
-    // one leaf of any kind (a cubic takes both inline slots), or two non-cubic leaves
+    // one leaf of a scanned kind (a cubic takes both inline slots), or two circle / rect /
+    // segment leaves; anything else (ellipses, polygons, deeper CSG) is bounded only
     bool no_cubic = true;
-    for (uint32_t i = leaf0; i < F.leaves.size(); ++i) no_cubic = no_cubic && F.leaves[i].kind != LEAF_CUBIC;
+    for (uint32_t i = leaf0; i < F.leaves.size(); ++i) no_cubic = no_cubic && F.leaves[i].kind < LEAF_CUBIC;
     uint32_t info = SCAN_BOUND;
     float scratch[6];
-    if (nl == 1) {
+    if (nl == 1 && F.leaves[leaf0].kind <= LEAF_CUBIC) {
       info = SCAN_ONE | (F.leaves[leaf0].kind << 4);
       leaf_f32(F.leaves[leaf0], s.a, s.b);
     } else if (nl == 2 && no_cubic) {

@@ -39,7 +39,9 @@ constexpr int TILE_PAD = 33;          // smem row stride (int64 words): no bank 
 // scan kinds (ObjScan::info bits 0..3)
 enum : uint32_t { SCAN_BOUND = 0, SCAN_ONE = 1, SCAN_TWO = 2 };
 // leaf kinds (Leaf64::kind and ObjScan leaf kinds)
-enum : uint32_t { LEAF_CIRCLE = 0, LEAF_RECT = 1, LEAF_SEGMENT = 2, LEAF_CUBIC = 3 };
+enum : uint32_t { LEAF_CIRCLE = 0, LEAF_RECT = 1, LEAF_SEGMENT = 2, LEAF_CUBIC = 3,
+                  // leaves the FP32 scan only bounds (their objects take the precise solve)
+                  LEAF_ELLIPSE = 4, LEAF_HALFPLANE = 5 };
 // ObjScan::info layout
 __host__ __device__ inline uint32_t info_scan(uint32_t i) { return i & 0xfu; }
 __host__ __device__ inline uint32_t info_leaf_a(uint32_t i) { return (i >> 4) & 0x3u; }
@@ -79,7 +81,9 @@ struct __align__(8) Leaf64 {
   uint32_t kind;
   uint32_t _pad;
   df p[8];  // circle cx,cy,r,1/r | rect cx,cy,cos,sin,hw,hh | segment ax,ay,bx,by,nx,ny (unit
-            // left normal) | cubic P0..P3
+            // left normal) | cubic P0..P3 | ellipse cx,cy,cos,sin,a,b,1/a,1/b | half-plane
+            // px,py,nx,ny: a point of the boundary line and the unit outward normal (a convex
+            // polygon is the And of its edges' half-planes)
 };
 static_assert(sizeof(Leaf64) == 72, "Leaf64 is 72 B");
 
@@ -499,11 +503,79 @@ static __device__ __noinline__ int hits_cubic(const Leaf64& L, df ox, df oy, df 
 
 }
 
+// Ellipse: the ray in the ellipse's frame scaled by (1/a, 1/b) meets the unit circle at the
+// same ray parameter; the normal is the normalised gradient (x/a^2, y/b^2).
+static __device__ __noinline__ int hits_ellipse(const Leaf64& L, df ox, df oy, df dx, df dy, Hit64* h, Near& ev) {
+  int n = 0;
+  const df c = L.p[2], s = L.p[3], ia = L.p[6], ib = L.p[7];
+  const df rx = ox - L.p[0], ry = oy - L.p[1];
+  const df lox = c * rx + s * ry, loy = c * ry - s * rx, ldx = c * dx + s * dy, ldy = c * dy - s * dx;
+  const df sox = lox * ia, soy = loy * ib, sdx = ldx * ia, sdy = ldy * ib;
+  const df a = sdx * sdx + sdy * sdy, b = sox * sdx + soy * sdy, cc = sox * sox + soy * soy - DF_ONE;
+  const df disc = b * b - a * cc;
+  const float tc = -b.hi / a.hi;
+  const float mn = fminf(L.p[4].hi, L.p[5].hi), mx = fmaxf(L.p[4].hi, L.p[5].hi);
+  // a lateral shift tol is at most tol / min(a, b) in the scaled frame
+  if (fabsf(disc.hi) <= fmaxf(1e-10f * (b.hi * b.hi + fabsf(a.hi * cc.hi)), 2.0f * ev.tol / mn * a.hi) &&
+      tc > -1e-9f - ev.tol)
+    near_event(ev, tc);
+  if (df_neg(disc)) return 0;
+  const df sq = dsqrt(disc);
+  const df q = -(b + (df_neg(b) ? -sq : sq));
+  df t1 = DF_ZERO, t2 = DF_ZERO;
+  if (q.hi != 0.0f) {
+    t1 = q / a;
+    t2 = cc / q;
+  }
+  if (t2 < t1) { const df x = t1; t1 = t2; t2 = x; }
+  const df ts[2] = {t1, t2};
+  for (int k = 0; k < 2; ++k) {
+    tmin_band(ts[k], ev);
+    if (!past_tmin(ts[k])) continue;
+    const df plx = lox + ldx * ts[k], ply = loy + ldy * ts[k];
+    const df gx = plx * ia * ia, gy = ply * ib * ib;
+    const df gl = dsqrt(gx * gx + gy * gy);
+    const df gi = gl.hi > 0.0f ? DF_ONE / gl : DF_ZERO;
+    const df nlx = gx * gi, nly = gy * gi;
+    h[n].t = ts[k];
+    h[n].px = ox + dx * ts[k];
+    h[n].py = oy + dy * ts[k];
+    h[n].nx = c * nlx - s * nly;
+    h[n].ny = s * nlx + c * nly;
+    h[n].k = mx / (mn * mn);  // the largest curvature of the ellipse
+    ++n;
+  }
+  return n;
+}
+
+// Half-plane (one edge of a convex polygon): the ray crossing its boundary line.
+static __device__ __noinline__ int hits_halfplane(const Leaf64& L, df ox, df oy, df dx, df dy, Hit64* h, Near& ev) {
+  const df nx = L.p[2], ny = L.p[3];
+  const df den = dx * nx + dy * ny;
+  const df dist = (L.p[0] - ox) * nx + (L.p[1] - oy) * ny;
+  const float ld = sqrtf(dx.hi * dx.hi + dy.hi * dy.hi);
+  const float scale = fabsf(L.p[0].hi) + fabsf(L.p[1].hi) + 1.0f;
+  if (fabsf(den.hi) <= 1e-10f * ld && fabsf(dist.hi) <= fmaxf(1e-10f * scale, ev.tol)) near_event(ev, 0.0f);
+  if (den.hi == 0.0f) return 0;
+  const df t = dist / den;
+  tmin_band(t, ev);
+  if (!past_tmin(t)) return 0;
+  h[0].t = t;
+  h[0].px = ox + dx * t;
+  h[0].py = oy + dy * t;
+  h[0].nx = nx;
+  h[0].ny = ny;
+  h[0].k = 0.0f;
+  return 1;
+}
+
 __device__ __forceinline__ int leaf_hits64(const Leaf64& L, df ox, df oy, df dx, df dy, Hit64* h, Near& ev) {
   switch (L.kind) {
     case LEAF_CIRCLE: return hits_circle(L, ox, oy, dx, dy, h, ev);
     case LEAF_SEGMENT: return hits_segment(L, ox, oy, dx, dy, h, ev);
     case LEAF_RECT: return hits_rect(L, ox, oy, dx, dy, h, ev);
+    case LEAF_ELLIPSE: return hits_ellipse(L, ox, oy, dx, dy, h, ev);
+    case LEAF_HALFPLANE: return hits_halfplane(L, ox, oy, dx, dy, h, ev);
     default: return hits_cubic(L, ox, oy, dx, dy, h, ev);
   }
 }
@@ -523,6 +595,18 @@ __device__ __forceinline__ bool leaf_contains64(const Leaf64& L, df px, df py, b
     const df ex = dabs(lx) - L.p[4], ey = dabs(ly) - L.p[5];
     const df sd = dmax(ex, ey);
     if (fabsf(sd.hi) <= fmaxf(1e-10f * (L.p[4].hi + L.p[5].hi), tol)) near = true;
+    return !(DF_ZERO < sd);
+  }
+  if (L.kind == LEAF_ELLIPSE) {
+    const df c = L.p[2], s = L.p[3], rx = px - L.p[0], ry = py - L.p[1];
+    const df u = (c * rx + s * ry) * L.p[6], w = (c * ry - s * rx) * L.p[7];
+    const df m = u * u + w * w - DF_ONE;
+    if (fabsf(m.hi) <= fmaxf(1e-10f, 2.0f * tol / fminf(L.p[4].hi, L.p[5].hi))) near = true;
+    return !(DF_ZERO < m);
+  }
+  if (L.kind == LEAF_HALFPLANE) {
+    const df sd = (px - L.p[0]) * L.p[2] + (py - L.p[1]) * L.p[3];  // > 0: outside
+    if (fabsf(sd.hi) <= fmaxf(1e-10f * (fabsf(L.p[0].hi) + fabsf(L.p[1].hi) + 1.0f), tol)) near = true;
     return !(DF_ZERO < sd);
   }
   return false;

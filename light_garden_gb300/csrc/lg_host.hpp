@@ -19,6 +19,7 @@ inline lg_status set_err(std::string& e, lg_status st, const std::string& m) {
 struct LeafH {
   uint32_t kind;
   double p[8];
+  double box[4];  // HALFPLANE: the world box of its polygon (the leaf itself is unbounded)
 };
 
 // One scene (or several, concatenated) in the layout of the device tables.

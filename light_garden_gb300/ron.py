@@ -11,7 +11,9 @@ refractive_index }``, ``Lens { l: Logic }``, ``CurvedMirror { cubic }``, ``Strai
 line_segment }`` and the ``Light`` variants (light.rs:10-14, 79-85, 139-145, 190-198).  The
 geometry types come from collision2d, which is not on disk; their layout here is the one
 default.ron shows (``GeoCircle { origin, radius }``, ``Rect { origin, rotation, width,
-height }``, ``Logic { op, a, b, origin, rotation }``, ``CubicBezier { points }``), with a
+height }``, ``Logic { op, a, b, origin, rotation }``, ``CubicBezier { points }``), the
+reference's own ``Ellipse { origin, a, b, rot }`` (object.rs:37-44) and a convex polygon as
+its list of points (``ConvexPolygon { points }``), with a
 rotation written as the four entries of nalgebra's column-major 2x2 matrix
 (cos, sin, -sin, cos), and a line segment as two points (fields ``a`` and ``b``, or any two
 point-valued fields in order).
@@ -23,8 +25,8 @@ import re
 from typing import Any, List, Tuple
 
 from . import abi
-from .scene import (Circle, CubicBezier, DirectionalLight, Geo, LineSegment, Logic, Material, Object, PointLight,
-                    Rect, SpotLight)
+from .scene import (Circle, ConvexPolygon, CubicBezier, DirectionalLight, Ellipse, Geo, LineSegment, Logic, Material,
+                    Object, PointLight, Rect, SpotLight)
 
 
 class RonError(ValueError):
@@ -219,7 +221,23 @@ def _geo(v) -> Geo:
         return _cubic(f)
     if n in ("GeoLogic", "Logic"):
         return _logic(f)
+    if n in ("GeoConvexPolygon", "ConvexPolygon"):
+        return _polygon(f)
+    if n in ("GeoEllipse", "Ellipse"):
+        return _ellipse(f)
     raise RonError(f"geometry {n} is not on this path")
+
+
+def _polygon(f) -> ConvexPolygon:
+    pts = f["points"] if isinstance(f, Struct) else f
+    pts = [_p2(p) for p in _unwrap(pts)] if not (isinstance(pts, list) and pts and _is_point(pts[0])) else [_p2(p) for p in pts]
+    if len(pts) < 3:
+        raise RonError("a convex polygon has at least 3 points")
+    return ConvexPolygon(tuple(pts))
+
+
+def _ellipse(f) -> Ellipse:
+    return Ellipse(_p2(f["origin"]), float(f["a"]), float(f["b"]), _rot(f.get("rot", f.get("rotation", [1, 0, 0, 1]))))
 
 
 def _cubic(f) -> CubicBezier:
@@ -267,9 +285,13 @@ def _object(v) -> Object:
                                             _rot(f.get("rotation", [1, 0, 0, 1]))), mat)
     if e.name == "Lens":
         return Object(abi.LG_OBJ_LENS, _logic(_unwrap(f["l"])), mat)
+    if e.name == "ConvexPolygon":
+        return Object(abi.LG_OBJ_CONVEX_POLYGON, _polygon(f), mat)
+    if e.name == "Ellipse":
+        return Object(abi.LG_OBJ_ELLIPSE, _ellipse(f), mat)
     if e.name == "Geo":
         return Object(abi.LG_OBJ_GEO, _geo(f if isinstance(f, Variant) else _unwrap(e.payload)), mat)
-    raise RonError(f"object {e.name} is not on this path (ConvexPolygon / Ellipse)")
+    raise RonError(f"object {e.name} is not on this path")
 
 
 def _color(c) -> Tuple[float, float, float, float]:
@@ -333,7 +355,24 @@ def _w_geo(g) -> str:
         return f"GeoCubicBezier((points: ({', '.join(_w_p2(p) for p in g.points)})))"
     if isinstance(g, Logic):
         return f"GeoLogic({_w_logic(g)})"
+    if isinstance(g, ConvexPolygon):
+        return f"GeoConvexPolygon({_w_polygon(g)})"
+    if isinstance(g, Ellipse):
+        return f"GeoEllipse({_w_ellipse(g)})"
     raise TypeError(type(g).__name__)
+
+
+def _w_polygon(g: ConvexPolygon) -> str:
+    if g.origin != (0.0, 0.0) or g.rotation != (1.0, 0.0):  # the file format holds world points
+        c, s = g.rotation
+        pts = [(g.origin[0] + c * x - s * y, g.origin[1] + s * x + c * y) for x, y in g.points]
+    else:
+        pts = list(g.points)
+    return f"(points: [{', '.join(_w_p2(p) for p in pts)}])"
+
+
+def _w_ellipse(g: Ellipse) -> str:
+    return f"(origin: {_w_p2(g.origin)}, a: {_f(g.a)}, b: {_f(g.b)}, rot: {_w_rot(g.rotation)})"
 
 
 def _w_logic(g: Logic) -> str:
@@ -355,6 +394,10 @@ def _w_object(o: Object) -> str:
              f"height: {_f(g.height)}))")
     elif o.kind == abi.LG_OBJ_LENS:
         e = f"Lens((l: {_w_logic(g)}))"
+    elif o.kind == abi.LG_OBJ_CONVEX_POLYGON:
+        e = f"ConvexPolygon({_w_polygon(g)})"
+    elif o.kind == abi.LG_OBJ_ELLIPSE:
+        e = f"Ellipse({_w_ellipse(g)})"
     else:
         e = f"Geo({_w_geo(g)})"
     m = "None" if o.material_opt is None else f"Some((refractive_index: {_f(o.material_opt.refractive_index)}))"
@@ -379,6 +422,6 @@ def _w_light(l) -> str:
 
 def dumps(objects, lights) -> str:
     """Text of a scene file (Tracer::serialize, tracer.rs:183-188; one item per line)."""
-    obj = ",\n    ".join(_w_object(o) for o in objects)
-    lts = ",\n    ".join(_w_light(l) for l in lights)
-    return f"([\n    {obj},\n], [\n    {lts},\n])\n" if objects or lights else "([], [])\n"
+    def block(items):
+        return "[\n" + "".join(f"    {x},\n" for x in items) + "]" if items else "[]"
+    return f"({block([_w_object(o) for o in objects])}, {block([_w_light(l) for l in lights])})\n"

@@ -84,6 +84,46 @@ class CubicBezier(Geo):
         return [(p[0], red), (p[1], red), (p[1], red), (p[2], red), (p[2], red), (p[3], red)]
 
 
+def convex_hull(points: Sequence[P2]) -> Tuple[P2, ...]:
+    """Counter-clockwise convex hull (Andrew's monotone chain), as ConvexPolygon::new_convex_hull
+    builds it (object.rs:34-36); collinear points are dropped."""
+    pts = sorted(set((float(x), float(y)) for x, y in points))
+    if len(pts) < 3:
+        return tuple(pts)
+
+    def turn(o, a, b):
+        return (a[0] - o[0]) * (b[1] - o[1]) - (a[1] - o[1]) * (b[0] - o[0])
+    lower: list = []
+    for p in pts:
+        while len(lower) >= 2 and turn(lower[-2], lower[-1], p) <= 0:
+            lower.pop()
+        lower.append(p)
+    upper: list = []
+    for p in reversed(pts):
+        while len(upper) >= 2 and turn(upper[-2], upper[-1], p) <= 0:
+            upper.pop()
+        upper.append(p)
+    return tuple(lower[:-1] + upper[:-1])
+
+
+@dataclass
+class ConvexPolygon(Geo):
+    """Convex polygon: vertices in order around it (either orientation), in the frame
+    (origin, rotation)."""
+    points: Tuple[P2, ...]
+    origin: P2 = (0.0, 0.0)
+    rotation: Tuple[float, float] = (1.0, 0.0)
+
+
+@dataclass
+class Ellipse(Geo):
+    """Ellipse { origin, a, b, rot } (object.rs:37-44): semi-axis a along the rotated x."""
+    origin: P2
+    a: float
+    b: float
+    rotation: Tuple[float, float] = (1.0, 0.0)
+
+
 @dataclass
 class Logic(Geo):
     """Logic { op, a, b, origin, rotation }: children live in the node's local frame."""
@@ -127,6 +167,16 @@ class Object:
         lg = Logic(abi.LG_OP_AND, Circle((distance * 0.5, 0.0), radius),
                    Circle((-distance * 0.5, 0.0), radius), origin)
         return Object(abi.LG_OBJ_LENS, lg, Material())
+
+    @staticmethod
+    def new_convex_polygon(points: Sequence[P2]) -> "Object":
+        # Object::new_convex_polygon (object.rs:92-98): the convex hull, default material
+        return Object(abi.LG_OBJ_CONVEX_POLYGON, ConvexPolygon(convex_hull(points)), Material())
+
+    @staticmethod
+    def new_ellipse(origin: P2, a: float, b: float) -> "Object":
+        # Object::new_ellipse (object.rs:99-105): unrotated, default material
+        return Object(abi.LG_OBJ_ELLIPSE, Ellipse(origin, a, b), Material())
 
     @staticmethod
     def new_geo(geo: Geo) -> "Object":
@@ -197,6 +247,32 @@ def _emit_geo(g: Geo, nodes: list) -> int:
         rec.kind = abi.LG_GEO_CUBIC
         for k, p in enumerate(g.points):
             rec.v[2 * k], rec.v[2 * k + 1] = p
+    elif isinstance(g, Ellipse):
+        rec.kind = abi.LG_GEO_ELLIPSE
+        rec.origin[:] = g.origin
+        rec.rot[:] = g.rotation
+        rec.v[0], rec.v[1] = g.a, g.b
+    elif isinstance(g, ConvexPolygon):
+        pts = list(g.points)
+        if not 3 <= len(pts) <= 63:
+            raise ValueError("a convex polygon has 3..63 vertices")
+        rec.kind = abi.LG_GEO_POLYGON
+        rec.origin[:] = g.origin
+        rec.rot[:] = g.rotation
+        rec.a, rec.b = len(pts), -1
+        for i, (x, y) in enumerate(pts[:4]):
+            rec.v[2 * i], rec.v[2 * i + 1] = x, y
+        prev = idx
+        for c0 in range(4, len(pts), 4):  # continuation records, 4 vertices each
+            cont = abi.lg_geo()
+            cont.kind = abi.LG_GEO_VERTICES
+            cont.b = -1
+            cont.rot[0] = 1.0
+            for i, (x, y) in enumerate(pts[c0:c0 + 4]):
+                cont.v[2 * i], cont.v[2 * i + 1] = x, y
+            nodes[prev].b = len(nodes)
+            prev = len(nodes)
+            nodes.append(cont)
     elif isinstance(g, Logic):
         rec.kind = abi.LG_GEO_LOGIC
         rec.op = g.op

@@ -26,8 +26,8 @@ from typing import List, Optional
 import numpy as np
 
 from . import abi
-from .scene import (Circle, CubicBezier, DirectionalLight, LineSegment, Logic, Material, Object,
-                    PackedScene, PointLight, Rect, SpotLight, pack)
+from .scene import (Circle, ConvexPolygon, CubicBezier, DirectionalLight, Ellipse, LineSegment, Logic, Material,
+                    Object, PackedScene, PointLight, Rect, SpotLight, convex_hull, pack)
 
 # control polygon of a curved mirror in its local frame (an arch), scaled by the object size
 _CUBIC_TEMPLATE = np.array([[-1.0, -0.5], [-0.35, 0.6], [0.35, 0.6], [1.0, -0.5]])
@@ -139,6 +139,35 @@ def csg_scene(seed: int = 3, total_rays: int = 1 << 22, n_objects: int = 256, n_
         p.string_mod.curve = 0
         p.string_mod.color[:] = (0.25, 0.25, 0.25, 1.0)
     return Workload("csg_scene", objects, lights, p)
+
+
+def _shape_object(rng, kind: str) -> Object:
+    c = tuple(rng.uniform(-1.0, 1.0, 2))
+    size = rng.uniform(0.04, 0.15)
+    if kind == "ellipse":
+        return Object(abi.LG_OBJ_ELLIPSE, Ellipse(c, size, size * rng.uniform(0.3, 1.0), _rand_rot(rng)),
+                      Material(rng.uniform(1.3, 1.8)))
+    if kind == "polygon":
+        k = int(rng.integers(3, 10))
+        ang = rng.uniform(0, 2 * math.pi, k)
+        rad = size * rng.uniform(0.6, 1.0, k)
+        pts = [(c[0] + r * math.cos(a), c[1] + r * math.sin(a)) for a, r in zip(ang, rad)]
+        hull = convex_hull(pts)
+        if len(hull) < 3:
+            hull = convex_hull(pts + [(c[0] + size, c[1]), (c[0], c[1] + size), (c[0] - size, c[1] - size)])
+        return Object(abi.LG_OBJ_CONVEX_POLYGON, ConvexPolygon(hull), Material(rng.uniform(1.3, 1.8)))
+    return _rand_object(rng, kind)
+
+
+def shapes_scene(seed: int = 8, rays_per_light: int = 1 << 14, n_objects: int = 48) -> Workload:
+    """Every shape of the scene model: ellipses and convex polygons (object.rs:13-14) beside
+    rects, circles, mirrors and curved mirrors; 4 lights, 12 bounces, 1024x768."""
+    rng = np.random.default_rng(seed)
+    kinds = ["ellipse", "polygon", "rect", "circle", "mirror", "curved"]
+    objects = [_shape_object(rng, kinds[rng.integers(0, len(kinds))]) for _ in range(n_objects)]
+    lkinds = ["point", "directional", "spot"]
+    lights = [_rand_light(rng, lkinds[rng.integers(0, 3)], rays_per_light) for _ in range(4)]
+    return Workload("shapes_scene", objects, lights, _params(12, 1024, 768, abi.LG_ACCUM_FIXED64))
 
 
 def _log_uniform_int(rng, lo: float, hi: float) -> int:

@@ -18,6 +18,10 @@
  *                membership makes the point a boundary of the combination:
  *                And: other inside; Or: other outside; AndNot: a-hits with b outside,
  *                b-hits with a inside.  contains() is closed (boundary points inside).
+ *   polygon      convex, vertices in the node's frame: every edge is a segment hit with the
+ *                outward normal; contains = on the inner side of every edge (closed).
+ *   ellipse      the ray in the ellipse frame scaled by (1/a, 1/b) meets the unit circle
+ *                (same ray parameter); normal = normalised gradient (x/a^2, y/b^2).
  *   hit point    o + t d on the ray.
  *   inside test  "obj.contains(ray origin)" (tracer.rs:431) is evaluated at the midpoint
  *                of origin -> hit; it equals the literal test whenever the origin is not
@@ -71,6 +75,25 @@ typedef struct {
   double aspect;
 } oscene;
 
+/* ------------------------------------------------------------------ polygons */
+#define MAX_POLY 63
+/* vertices of a POLYGON node (in its frame), following its VERTICES chain; returns the count */
+static int poly_vertices(const lg_geo* G, const lg_geo* g, v2* out) {
+  const int n = g->a;
+  int k = 0;
+  const lg_geo* cur = g;
+  while (k < n) {
+    for (int i = 0; i < 4 && k < n; ++i, ++k) out[k] = mk(cur->v[2 * i], cur->v[2 * i + 1]);
+    if (k < n) cur = &G[cur->b];
+  }
+  return n;
+}
+static double poly_orientation(const v2* P, int n) {
+  double a = 0.0;
+  for (int i = 0; i < n; ++i) a += cross(P[i], P[(i + 1) % n]);
+  return a >= 0.0 ? 1.0 : -1.0;
+}
+
 /* ------------------------------------------------------------------ geometry: contains */
 /* Membership with a near-boundary flag (closed sets). */
 static int geo_contains(const lg_geo* G, int gi, v2 p, uint32_t* fl) {
@@ -90,6 +113,28 @@ static int geo_contains(const lg_geo* G, int gi, v2 p, uint32_t* fl) {
       double sd = ex > ey ? ex : ey;
       if (fl && fabs(sd) <= BAND * (hw + hh)) *fl |= NEAR;
       return sd <= 0.0;
+    }
+    case LG_GEO_POLYGON: {
+      v2 P[MAX_POLY];
+      const int n = poly_vertices(G, g, P);
+      const double sgn = poly_orientation(P, n);
+      v2 l = irot(sub(p, mk(g->origin[0], g->origin[1])), g->rot[0], g->rot[1]);
+      int in = 1;
+      for (int i = 0; i < n; ++i) {
+        v2 e = sub(P[(i + 1) % n], P[i]);
+        double le = sqrt(dot(e, e));
+        double sd = -sgn * cross(e, sub(l, P[i])) / (le > 0 ? le : 1.0); /* > 0 outside this edge */
+        if (fl && fabs(sd) <= BAND * (le + 1e-300)) *fl |= NEAR;
+        if (sd > 0.0) in = 0;
+      }
+      return in;
+    }
+    case LG_GEO_ELLIPSE: {
+      v2 l = irot(sub(p, mk(g->origin[0], g->origin[1])), g->rot[0], g->rot[1]);
+      double u = l.x / g->v[0], w = l.y / g->v[1];
+      double m = u * u + w * w - 1.0;
+      if (fl && fabs(m) <= BAND) *fl |= NEAR;
+      return m <= 0.0;
     }
     case LG_GEO_LOGIC: {
       v2 l = irot(sub(p, mk(g->origin[0], g->origin[1])), g->rot[0], g->rot[1]);
@@ -299,9 +344,63 @@ static int hits_cubic(const lg_geo* g, v2 o, v2 d, ohit* out, int cap, double* e
   return n;
 }
 
+static int hits_polygon(const lg_geo* G, const lg_geo* g, v2 o, v2 d, ohit* out, int cap, double* ev) {
+  v2 P[MAX_POLY];
+  const int n = poly_vertices(G, g, P);
+  const double sgn = poly_orientation(P, n);
+  const double c = g->rot[0], s = g->rot[1];
+  v2 org = mk(g->origin[0], g->origin[1]);
+  v2 lo = irot(sub(o, org), c, s), ld = irot(d, c, s);
+  int m = 0;
+  for (int i = 0; i < n; ++i) {
+    ohit h[1];
+    if (hits_segment(P[i], P[(i + 1) % n], lo, ld, h, 1, ev) == 1 && m < cap) {
+      v2 e = sub(P[(i + 1) % n], P[i]);
+      v2 nrm = unit(scl(mk(e.y, -e.x), sgn)); /* outward */
+      out[m].t = h[0].t;
+      out[m].p = add(o, scl(d, h[0].t));
+      out[m].n = rot(nrm, c, s);
+      ++m;
+    }
+  }
+  return m;
+}
+
+static int hits_ellipse(const lg_geo* g, v2 o, v2 d, ohit* out, int cap, double* ev) {
+  const double c = g->rot[0], s = g->rot[1], A = g->v[0], Bb = g->v[1];
+  v2 org = mk(g->origin[0], g->origin[1]);
+  v2 lo = irot(sub(o, org), c, s), ld = irot(d, c, s);
+  v2 so = mk(lo.x / A, lo.y / Bb), sd = mk(ld.x / A, ld.y / Bb);
+  double a = dot(sd, sd), b = dot(so, sd), cc = dot(so, so) - 1.0;
+  double disc = b * b - a * cc;
+  if (fabs(disc) <= BAND * (b * b + fabs(a * cc)) && -b / a > -T_MIN) event(ev, -b / a);
+  if (disc < 0.0) return 0;
+  double sq = sqrt(disc);
+  double q = -(b + (b >= 0 ? sq : -sq));
+  double t1 = 0.0, t2 = 0.0;
+  if (q != 0.0) {
+    t1 = q / a;
+    t2 = cc / q;
+  }
+  if (t1 > t2) { double x = t1; t1 = t2; t2 = x; }
+  int n = 0;
+  double ts[2] = {t1, t2};
+  for (int k = 0; k < 2; ++k) {
+    tmin_band(ts[k], ev);
+    if (ts[k] > T_MIN) {
+      v2 pl = add(lo, scl(ld, ts[k]));
+      v2 gr = unit(mk(pl.x / (A * A), pl.y / (Bb * Bb)));
+      n = push_hit(out, n, cap, ts[k], o, d, rot(gr, c, s));
+    }
+  }
+  return n;
+}
+
 static int geo_hits(const lg_geo* G, int gi, v2 o, v2 d, ohit* out, int cap, double* ev, int depth) {
   const lg_geo* g = &G[gi];
   switch (g->kind) {
+    case LG_GEO_POLYGON: return hits_polygon(G, g, o, d, out, cap, ev);
+    case LG_GEO_ELLIPSE: return hits_ellipse(g, o, d, out, cap, ev);
     case LG_GEO_CIRCLE: return hits_circle(g, o, d, out, cap, ev);
     case LG_GEO_RECT: return hits_rect(g, o, d, out, cap, ev);
     case LG_GEO_SEGMENT: return hits_segment(mk(g->v[0], g->v[1]), mk(g->v[2], g->v[3]), o, d, out, cap, ev);
@@ -350,6 +449,18 @@ static int validate_geo(const lg_geo* G, uint32_t n_geo, int gi, int depth) {
   const lg_geo* g = &G[gi];
   switch (g->kind) {
     case LG_GEO_CIRCLE: case LG_GEO_RECT: case LG_GEO_SEGMENT: case LG_GEO_CUBIC: return LGO_OK;
+    case LG_GEO_ELLIPSE: return g->v[0] > 0.0 && g->v[1] > 0.0 ? LGO_OK : LGO_ERR_INVALID;
+    case LG_GEO_POLYGON: {
+      if (g->a < 3 || g->a > MAX_POLY) return LGO_ERR_INVALID;
+      int k = 4;
+      const lg_geo* cur = g;
+      while (k < g->a) {  /* the VERTICES chain */
+        if (cur->b < 0 || (uint32_t)cur->b >= n_geo || G[cur->b].kind != LG_GEO_VERTICES) return LGO_ERR_INVALID;
+        cur = &G[cur->b];
+        k += 4;
+      }
+      return LGO_OK;
+    }
     case LG_GEO_LOGIC: {
       if (g->op < 0 || g->op > 2) return LGO_ERR_INVALID;
       int r = validate_geo(G, n_geo, g->a, depth + 1);
@@ -363,7 +474,6 @@ static int validate_geo(const lg_geo* G, uint32_t n_geo, int gi, int depth) {
 static int validate_scene(const oscene* S) {
   for (uint32_t k = 0; k < S->n_obj; ++k) {
     const lg_object* ob = &S->o[k];
-    if (ob->kind == LG_OBJ_CONVEX_POLYGON || ob->kind == LG_OBJ_ELLIPSE) return LGO_ERR_UNSUPPORTED;
     if (ob->kind < 0 || ob->kind > LG_OBJ_GEO) return LGO_ERR_INVALID;
     int r = validate_geo(S->g, S->n_geo, ob->geo, 0);
     if (r) return r;
@@ -371,7 +481,8 @@ static int validate_scene(const oscene* S) {
     if ((ob->kind == LG_OBJ_STRAIGHT_MIRROR && rk != LG_GEO_SEGMENT) ||
         (ob->kind == LG_OBJ_CURVED_MIRROR && rk != LG_GEO_CUBIC) ||
         (ob->kind == LG_OBJ_CIRCLE && rk != LG_GEO_CIRCLE) ||
-        (ob->kind == LG_OBJ_RECT && rk != LG_GEO_RECT) || (ob->kind == LG_OBJ_LENS && rk != LG_GEO_LOGIC))
+        (ob->kind == LG_OBJ_RECT && rk != LG_GEO_RECT) || (ob->kind == LG_OBJ_LENS && rk != LG_GEO_LOGIC) ||
+        (ob->kind == LG_OBJ_CONVEX_POLYGON && rk != LG_GEO_POLYGON) || (ob->kind == LG_OBJ_ELLIPSE && rk != LG_GEO_ELLIPSE))
       return LGO_ERR_INVALID;
   }
   for (uint32_t k = 0; k < S->n_light; ++k)

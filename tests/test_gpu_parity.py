@@ -11,8 +11,8 @@ import numpy as np
 import pytest
 
 from light_garden_gb300 import abi, workloads as W
-from light_garden_gb300.scene import (Circle, CubicBezier, DirectionalLight, LineSegment, Logic, Material, Object,
-                                      PointLight, Rect, SpotLight, pack)
+from light_garden_gb300.scene import (Circle, ConvexPolygon, CubicBezier, DirectionalLight, LineSegment, Logic, Material,
+                                      Object, PointLight, Rect, SpotLight, pack)
 from parity import compare, rel_l2
 
 pytestmark = pytest.mark.gpu
@@ -221,10 +221,14 @@ def test_error_statuses(ctx):
         ctx.upload(pack(W.plain_small().objects, W.plain_small().lights, bad))
     assert e.value.status == abi.LG_ERR_UNSUPPORTED
     pk2 = W.plain_small().packed()
-    pk2.objects[0].kind = abi.LG_OBJ_CONVEX_POLYGON
+    pk2.objects[0].kind = abi.LG_OBJ_CONVEX_POLYGON  # a polygon object over a circle geometry
     with pytest.raises(abi.LgError) as e:
         ctx.upload(pk2)
-    assert e.value.status == abi.LG_ERR_UNSUPPORTED
+    assert e.value.status == abi.LG_ERR_INVALID_ARGUMENT
+    pk4 = pack([Object(abi.LG_OBJ_CONVEX_POLYGON, ConvexPolygon(((0, 0), (1, 0), (2, 0))), Material())], [])
+    with pytest.raises(abi.LgError) as e:  # collinear vertices: no interior
+        ctx.upload(pk4)
+    assert e.value.status == abi.LG_ERR_INVALID_ARGUMENT
     pk3 = W.plain_small().packed()
     pk3.objects[1].geo = 99
     with pytest.raises(abi.LgError) as e:
@@ -295,3 +299,19 @@ def test_raster_large_terms_bit_exact(gpu, oracle, variant):
             acc = c.accum()
         ref, _ = oracle.raster(segs, p)
         assert np.array_equal(acc, ref), f"op {op}: {np.count_nonzero(acc != ref)} values differ"
+
+
+def test_polygons_and_ellipses_parity(ctx, oracle):
+    """ConvexPolygon (the And of its edges' half-planes on the GPU, edge segments in the
+    oracle) and Ellipse objects among the other shapes: trace parity and image parity."""
+    pk = W.shapes_scene().packed()
+    st, rep, (gs, gp), (os_, op, o64) = _trace_both(ctx, oracle, pk, stride=11)
+    assert rep.ok(), rep
+    assert rep.matched > 0.99 * len(os_)
+    pk2 = W.shapes_scene().packed()
+    ctx.upload(pk2)
+    img, _ = ctx.render()
+    full, _, _, _ = oracle.trace(pk2)
+    ref_acc, _ = oracle.raster(full, pk2.params)
+    ref = oracle.resolve_f16(ref_acc)
+    assert rel_l2(img.view(np.float16).astype(np.float32), ref.view(np.float16).astype(np.float32)) < 1e-3

@@ -424,3 +424,49 @@ def test_resolve_images(oracle):
     # renderer.rs:325-328: u8 = sat(f^(1/2.2) · 255), truncated
     rgba = oracle.resolve_rgba8(acc)
     assert rgba[0, :, 0].tolist() == [0, 255, int(0.5 ** (1 / 2.2) * 255), 255, 0, int(0.25 ** (1 / 2.2) * 255)]
+
+
+def test_ellipse(oracle):
+    # x^2/4 + y^2 = 1: the x axis meets it at +-2, the y axis at +-1
+    e = S.Ellipse((0.0, 0.0), 2.0, 1.0)
+    h, _ = hits(oracle, e, (-3, 0), (1, 0))
+    assert_hit(h[0], 1.0, (-2.0, 0.0), (-1, 0))
+    assert_hit(h[1], 5.0, (2.0, 0.0), (1, 0))
+    # at (sqrt(2), 1/sqrt(2)) the gradient (x/4, y) points along (1, 2)/sqrt(5)
+    s2 = math.sqrt(2.0)
+    h, _ = hits(oracle, e, (s2, -3), (0, 1))
+    assert h[1][1] == pytest.approx((s2, 1 / s2), abs=1e-12)
+    assert h[1][2] == pytest.approx((1 / math.sqrt(5), 2 / math.sqrt(5)), abs=1e-12)
+    # rotated by 90 degrees: the long axis along y
+    h, _ = hits(oracle, S.Ellipse((0.0, 0.0), 2.0, 1.0, (0.0, 1.0)), (0, -3), (0, 1))
+    assert [x[0] for x in h] == pytest.approx([1.0, 5.0], abs=1e-12)
+    assert contains(oracle, e, (1.9, 0.0)) and not contains(oracle, e, (1.5, 0.7))
+
+
+def test_convex_polygon(oracle):
+    # a unit square written as a polygon hits like the rect of the same size
+    sq = S.ConvexPolygon(((-0.5, -0.5), (0.5, -0.5), (0.5, 0.5), (-0.5, 0.5)))
+    rect = S.Rect((0.0, 0.0), 1.0, 1.0)
+    for o, d in (((-2, 0.1), (1, 0)), ((0.3, -2), (0.2, 1)), ((-1, -0.9), (1, 1))):
+        hp, _ = hits(oracle, sq, o, d)
+        hr, _ = hits(oracle, rect, o, d)
+        assert [x[0] for x in hp] == pytest.approx([x[0] for x in hr], abs=1e-12)
+        for a, b in zip(hp, hr):
+            assert a[2] == pytest.approx(b[2], abs=1e-12)
+    # clockwise vertices give the same solid
+    cw = S.ConvexPolygon(tuple(reversed(sq.points)))
+    assert [x[0] for x in hits(oracle, cw, (-2, 0.1), (1, 0))[0]] == pytest.approx([1.5, 2.5])
+    # a regular heptagon (more vertices than one record holds), in a rotated frame
+    hept = S.ConvexPolygon(tuple((math.cos(2 * math.pi * k / 7), math.sin(2 * math.pi * k / 7)) for k in range(7)),
+                           (0.5, 0.25), (0.0, 1.0))
+    assert contains(oracle, hept, (0.5, 0.25)) and not contains(oracle, hept, (1.6, 0.25))
+    # vertex 0 maps to (0.5, 1.25): a vertical ray just beside it crosses two edges, the exit
+    # on the two edges meeting there
+    h, fl = hits(oracle, hept, (0.51, -3), (0, 1))
+    assert len(h) == 2 and fl == 0
+    top = h[1][1][1]
+    assert 1.2 < top < 1.25
+    # straight through the vertex both edges report it, and the decision is flagged
+    h, _ = hits(oracle, hept, (0.5, -3), (0, 1))
+    assert len(h) == 3 and h[1][0] == pytest.approx(h[2][0], abs=1e-12)
+    assert S.convex_hull([(0, 0), (1, 0), (0.5, 0.2), (1, 1), (0, 1), (0.5, 0.5)]) == ((0.0, 0.0), (1.0, 0.0), (1.0, 1.0), (0.0, 1.0))

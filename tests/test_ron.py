@@ -67,9 +67,21 @@ def test_round_trip():
     assert ron.loads(ron.dumps([], [])) == ([], [])
 
 
+def test_polygon_and_ellipse_objects():
+    objs, _ = ron.loads("""([
+        (object_enum: Ellipse((origin: [0.1, 0.2], a: 0.3, b: 0.2, rot: [0, 1, -1, 0])),
+         material_opt: Some((refractive_index: 1.4)), moved: false),
+        (object_enum: ConvexPolygon((points: [[0, 0], [1, 0], [1, 1], [0, 1]])), material_opt: None, moved: false),
+    ], [])""")
+    assert objs[0].kind == abi.LG_OBJ_ELLIPSE and objs[0].geo == S.Ellipse((0.1, 0.2), 0.3, 0.2, (0.0, 1.0))
+    assert objs[1].kind == abi.LG_OBJ_CONVEX_POLYGON and len(objs[1].geo.points) == 4
+    o2, _ = ron.loads(ron.dumps(objs, []))
+    assert o2 == objs
+
+
 def test_unsupported_objects_are_rejected():
     with pytest.raises(ron.RonError, match="not on this path"):
-        ron.loads("([(object_enum: Ellipse((origin: [0, 0], a: 1, b: 2, rot: 0)), material_opt: None, moved: false)], [])")
+        ron.loads("([(object_enum: Spline((points: [])), material_opt: None, moved: false)], [])")
     with pytest.raises(ron.RonError):
         ron.loads("([], [UnknownLight((position: [0, 0]))])")
 
