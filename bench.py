@@ -32,6 +32,7 @@ METRIC = "traced segments/s + accumulated px/s on 1 GB300; p50/p99 scene latency
 # DRAM bytes (read + write) per accumulated pixel of k_raster, measured with ncu on the
 # quarter-size mid scene (profiles/k_raster_mid_scene.md)
 RASTER_DRAM_BYTES_PER_PIXEL = 2.64
+CULL = {"auto": 0, "off": 1, "on": 2}  # lg_culling
 
 WORKLOAD = ("mid_scene: 64 objects (rect/circle/mirror/curved mirror, seed 2), 8 lights x 2^18 rays, "
             "16 bounces, 1920x1080, int64 Q31.32 accumulation, RGBA16F resolve")
@@ -192,7 +193,7 @@ def run_ours(args, ws, rank, local):
     w = W.mid_scene(rays_per_light=args.rays_per_light)
     pk = w.packed()
     Wd, Hd = pk.params.width, pk.params.height
-    ctx = Context(device=local, raster_variant=args.raster_variant)
+    ctx = Context(device=local, raster_variant=args.raster_variant, culling=CULL[args.culling], grid_density=args.grid_density)
     ctx.upload(pk)
     out_dev = torch.empty((Hd, Wd * 4), dtype=torch.int16, device=dev)
     out_host = torch.empty((Hd, Wd * 4), dtype=torch.int16, pin_memory=True)
@@ -257,7 +258,8 @@ def run_ours(args, ws, rank, local):
             "note": "the read-modify-write runs in shared memory; DRAM traffic is the segment and reference "
                     "reads plus one flush per tile unit"}
     trace_fp32 = {"kernel": "k_scan/k_refine/k_full/k_bounce (trace, all generations)", "ms": avg["trace_ms"],
-                  "ray_visits": visits, "ns_per_visit": avg["trace_ms"] * 1e6 / max(1, visits)}
+                  "ray_visits": visits, "ns_per_visit": avg["trace_ms"] * 1e6 / max(1, visits),
+                  "culling": args.culling, "bound_tests": st["bound_tests"], "object_tests": st["object_tests"]}
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -312,7 +314,7 @@ def run_batch(args, ws, rank, local):
     n = len(scenes)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
     # batched path
-    ctx = Context(device=local, raster_variant=args.raster_variant)
+    ctx = Context(device=local, raster_variant=args.raster_variant, culling=CULL[args.culling], grid_density=args.grid_density)
     ctx.batch_upload(scenes)
     out = torch.empty(ctx.batch_pixels() * 4, dtype=torch.int16, device=dev)
     for _ in range(max(1, args.warmup)):
@@ -338,7 +340,7 @@ def run_batch(args, ws, rank, local):
     segs, pixels = st["segments"], st["pixels"]
     ctx.close()
     # plain path: the same scenes one by one through lg_render (device output)
-    plain = Context(device=local)
+    plain = Context(device=local, culling=CULL[args.culling], grid_density=args.grid_density)
     big = torch.empty(max(pk.params.width * pk.params.height for pk in scenes) * 4, dtype=torch.int16, device=dev)
     lat = []
     for pk in scenes[:4]:
@@ -362,7 +364,7 @@ def run_batch(args, ws, rank, local):
             "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "fp32 + double-float trace, int64 accumulate", "data": "synthetic",
             "config": {"workload": BATCH_WORKLOAD + ("" if args.ray_scale == 1.0 else f", rays x {args.ray_scale}"),
-                       "scenes": n, "l2": "flushed between steps (512 MB write)"},
+                       "scenes": n, "l2": "flushed between steps (512 MB write)", "culling": args.culling},
             "segments_per_step": segs, "pixels_per_step": pixels,
             "e2e": {"value": e2e_value, "unit": "scenes/s", "h2d_bytes_per_step": None,
                     "d2h_bytes_per_step": host.numel() * 2, "ms_per_step": e2e_s * 1e3},
@@ -391,7 +393,7 @@ def run_csg(args, ws, rank, local):
     dev = torch.device("cuda", local)
     pk = W.csg_scene().packed()
     Wd, Hd = pk.params.width, pk.params.height
-    ctx = Context(device=local, raster_variant=args.raster_variant)
+    ctx = Context(device=local, raster_variant=args.raster_variant, culling=CULL[args.culling], grid_density=args.grid_density)
     ctx.upload(pk)
     out = torch.empty((Hd, Wd * 4), dtype=torch.int16, device=dev)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
@@ -425,6 +427,8 @@ def run_csg(args, ws, rank, local):
             "px_per_s": ws * st["pixels"] / (ms_max * 1e-3), "segments_per_step": st["segments"],
             "pixels_per_step": st["pixels"], "ray_visits_per_step": st["ray_visits"],
             "fp64_solves_per_step": st["fp64_solves"], "near_degenerate_per_step": st["near_degenerate"],
+            "bound_tests_per_step": st["bound_tests"], "object_tests_per_step": st["object_tests"],
+            "culling": args.culling,
             "stage_ms": avg, "retries_first_frame": st["retries"],
             "e2e": {"value": e2e_value, "unit": "segments/s", "h2d_bytes_per_step": None,
                     "d2h_bytes_per_step": Hd * Wd * 8, "ms_per_step": e2e_s * 1e3},
@@ -452,7 +456,7 @@ def run_serve(args, ws, rank, local):
     n = len(scenes)
     rng = np.random.default_rng(7)
     arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n))
-    ctx = Context(device=local)
+    ctx = Context(device=local, culling=CULL[args.culling], grid_density=args.grid_density)
     ctx.serve_begin(hbm_budget_bytes=int(args.budget_gb * (1 << 30)), max_slots=4096)
     # warm up the kernels on two requests
     for sc in scenes[:2]:
@@ -488,7 +492,7 @@ def run_serve(args, ws, rank, local):
     ctx.serve_end()
     ctx.close()
     # plain path: one request at a time in arrival order
-    plain = Context(device=local)
+    plain = Context(device=local, culling=CULL[args.culling], grid_density=args.grid_density)
     big = torch.empty(max(pk.params.width * pk.params.height for pk in scenes) * 4, dtype=torch.int16, device=dev)
     for pk in scenes[:2]:
         plain.upload(pk)
@@ -537,6 +541,9 @@ def main():
                     help="0: autotuned; 1: shared-memory tile atomics; 2: warp-private tiles")
     # the mixed-size batch configuration (not the default line)
     ap.add_argument("--workload", default="mid", choices=["mid", "csg", "batch", "serve"])
+    ap.add_argument("--culling", default="auto", choices=sorted(CULL),
+                    help="nearest-hit culling grid: auto (scenes of 96+ objects), off, on")
+    ap.add_argument("--grid-density", type=float, default=0.0, help="culling grid cells per object (0: 2)")
     ap.add_argument("--rate", type=float, default=1000.0, help="serve: Poisson arrival rate (requests/s)")
     ap.add_argument("--budget-gb", type=float, default=120.0, help="serve: HBM budget")
     ap.add_argument("--batch-scenes", type=int, default=512)

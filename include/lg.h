@@ -209,6 +209,8 @@ typedef struct lg_trace_stats {
   uint64_t near_degenerate;/* segments carrying LG_PATH_NEAR_DEGENERATE */
   uint64_t pixels;         /* pixel updates made by lg_accumulate */
   uint64_t tile_refs;      /* (segment, tile) pairs binned by lg_accumulate */
+  uint64_t bound_tests;    /* FP32 ray / bounding-circle tests of the nearest-hit search */
+  uint64_t object_tests;   /* FP32 ray / object classifications (bounding test passed) */
   uint32_t retries;        /* re-launches after a ring/queue overflow */
   uint32_t _pad;
   /* device time from CUDA events on the library's stream; lg_render splits accumulate
@@ -224,7 +226,19 @@ typedef struct lg_device_opts {
   uint64_t queue_capacity;    /* initial per-generation ray queue size (0 = automatic) */
   uint64_t stream_segments;   /* lg_render accumulates while tracing, with a ring of this many
                                  segments, once a frame has more (0 = 2^28) */
+  int32_t culling;            /* lg_culling: spatial culling of the nearest-hit search */
+  float grid_density;         /* culling grid cells per object (0 = 2) */
 } lg_device_opts;
+
+/* Nearest-hit culling (replaces the reference's approximate tile map, tile_map.rs:18-146).
+ * The culled search visits objects in ray order through a uniform grid and returns the
+ * same hits as the full scan. */
+typedef enum lg_culling {
+  LG_CULL_AUTO = 0,  /* grid for scenes of LG_CULL_AUTO_MIN objects or more */
+  LG_CULL_OFF = 1,   /* every ray tests every object's bounding circle */
+  LG_CULL_ON = 2     /* grid for every scene */
+} lg_culling;
+#define LG_CULL_AUTO_MIN 96
 
 typedef struct lg_ctx lg_ctx;
 

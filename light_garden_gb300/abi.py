@@ -97,6 +97,7 @@ class lg_trace_stats(C.Structure):
     _fields_ = [("primary_rays", C.c_uint64), ("ray_visits", C.c_uint64), ("segments", C.c_uint64),
                 ("fp64_solves", C.c_uint64), ("fp64_fallbacks", C.c_uint64),
                 ("near_degenerate", C.c_uint64), ("pixels", C.c_uint64), ("tile_refs", C.c_uint64),
+                ("bound_tests", C.c_uint64), ("object_tests", C.c_uint64),
                 ("retries", C.c_uint32), ("_pad", C.c_uint32),
                 ("trace_ms", C.c_float), ("accumulate_ms", C.c_float), ("resolve_ms", C.c_float),
                 ("total_ms", C.c_float), ("bin_ms", C.c_float), ("raster_ms", C.c_float)]
@@ -107,7 +108,12 @@ class lg_trace_stats(C.Structure):
 
 class lg_device_opts(C.Structure):
     _fields_ = [("device", C.c_int32), ("raster_variant", C.c_int32), ("segment_capacity", C.c_uint64),
-                ("queue_capacity", C.c_uint64), ("stream_segments", C.c_uint64)]
+                ("queue_capacity", C.c_uint64), ("stream_segments", C.c_uint64), ("culling", C.c_int32),
+                ("grid_density", C.c_float)]
+
+
+LG_CULL_AUTO, LG_CULL_OFF, LG_CULL_ON = 0, 1, 2
+LG_CULL_AUTO_MIN = 96
 
 
 # numpy dtypes with the same layout, for bulk conversion of downloads

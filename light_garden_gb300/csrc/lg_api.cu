@@ -317,6 +317,82 @@ lg_status flatten_scene(std::string& err, const lg_geo* G, uint32_t n_geo, const
 }
 
 
+// Uniform grid over the objects' FP32 bounding circles.  The margin covers the FP32 error
+// of a walk from an origin within `reach` (a few 1e-7 of the coordinates) and the
+// bounding-circle test's own slack (2e-6 of the distances), with room to spare.
+void build_grid(const std::vector<ObjScan>& scan, int culling, float density, GridH& G) {
+  const size_t n = scan.size();
+  std::memset(&G.rec, 0, sizeof G.rec);
+  G.cell_start.assign(1, 0u);
+  G.cell_obj.clear();
+  G.obj_cells.assign(n, make_ushort4(0, 0, 0, 0));
+  const bool want = culling == LG_CULL_ON || (culling != LG_CULL_OFF && n >= (size_t)LG_CULL_AUTO_MIN);
+  if (!want || n == 0) return;
+  double x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
+  for (const ObjScan& s : scan) {
+    x0 = std::min(x0, (double)s.cx - s.R); x1 = std::max(x1, (double)s.cx + s.R);
+    y0 = std::min(y0, (double)s.cy - s.R); y1 = std::max(y1, (double)s.cy + s.R);
+  }
+  const double W = x1 - x0, H = y1 - y0;
+  const double scale = 1.0 + std::max(std::fabs(x0), std::fabs(x1)) + std::max(std::fabs(y0), std::fabs(y1)) + W + H;
+  const double target = std::max(1.0, (density > 0.0f ? (double)density : 2.0) * (double)n);
+  const double ar = std::max(W, 1e-9 * scale) / std::max(H, 1e-9 * scale);
+  int nx = (int)std::lround(std::sqrt(target * ar)), ny;
+  nx = std::min(1024, std::max(1, nx));
+  ny = std::min(1024, std::max(1, (int)std::lround(target / nx)));
+  constexpr uint64_t MAX_ENTRIES = 1ull << 24;
+  for (;;) {
+    const double margin = 4e-5 * scale + 1e-3 * std::min(W / nx, H / ny);
+    const double bx0 = x0 - 2.0 * margin, by0 = y0 - 2.0 * margin;
+    const float fx0 = (float)bx0, fy0 = (float)by0;
+    const float cw = (float)((x1 + 2.0 * margin - fx0) / nx), ch = (float)((y1 + 2.0 * margin - fy0) / ny);
+    auto range = [&](const ObjScan& s) {
+      auto cell = [](double v, double org, double size, int n_) {
+        const double c = std::floor((v - org) / size);
+        return (int)std::min((double)(n_ - 1), std::max(0.0, c));
+      };
+      return make_ushort4((unsigned short)cell((double)s.cx - s.R - margin, fx0, cw, nx),
+                          (unsigned short)cell((double)s.cy - s.R - margin, fy0, ch, ny),
+                          (unsigned short)cell((double)s.cx + s.R + margin, fx0, cw, nx),
+                          (unsigned short)cell((double)s.cy + s.R + margin, fy0, ch, ny));
+    };
+    uint64_t total = 0;
+    for (size_t k = 0; k < n; ++k) {
+      G.obj_cells[k] = range(scan[k]);
+      const ushort4 r = G.obj_cells[k];
+      total += (uint64_t)(r.z - r.x + 1) * (uint64_t)(r.w - r.y + 1);
+    }
+    if (total > MAX_ENTRIES && (nx > 1 || ny > 1)) {  // huge objects: coarser cells
+      nx = std::max(1, nx / 2);
+      ny = std::max(1, ny / 2);
+      continue;
+    }
+    const size_t ncell = (size_t)nx * ny;
+    G.cell_start.assign(ncell + 1, 0u);
+    for (size_t k = 0; k < n; ++k) {
+      const ushort4 r = G.obj_cells[k];
+      for (int iy = r.y; iy <= r.w; ++iy)
+        for (int ix = r.x; ix <= r.z; ++ix) ++G.cell_start[(size_t)iy * nx + ix + 1];
+    }
+    for (size_t c = 0; c < ncell; ++c) G.cell_start[c + 1] += G.cell_start[c];
+    G.cell_obj.assign(total, 0);
+    std::vector<uint32_t> cur(G.cell_start.begin(), G.cell_start.end() - 1);
+    for (size_t k = 0; k < n; ++k) {  // ascending object order within every cell
+      const ushort4 r = G.obj_cells[k];
+      for (int iy = r.y; iy <= r.w; ++iy)
+        for (int ix = r.x; ix <= r.z; ++ix) G.cell_obj[cur[(size_t)iy * nx + ix]++] = (uint16_t)k;
+    }
+    GridRec& R = G.rec;
+    R.x0 = fx0; R.y0 = fy0; R.cw = cw; R.ch = ch;
+    R.iw = 1.0f / cw; R.ih = 1.0f / ch;
+    R.margin = (float)margin;
+    R.nx = (uint32_t)nx; R.ny = (uint32_t)ny;
+    R.cell_base = 0; R.list_base = 0;
+    R.reach = (float)scale;
+    return;
+  }
+}
+
 lg_status validate_params(std::string& err, const lg_params& p) {
   if (p.max_bounce > (uint32_t)MAX_GEN) return set_err(err, LG_ERR_INVALID_ARGUMENT, "max_bounce must be <= 64");
   if (p.width == 0 || p.height == 0 || p.width > 32768 || p.height > 32768)
@@ -408,6 +484,10 @@ SceneDev scene_dev(lg_ctx* c) {
   S.n_new = 0;
   S.light_lo = 0;
   S.light_hi = 0;
+  S.grids = (const GridRec*)c->d_grids.p;
+  S.cell_start = (const uint32_t*)c->d_cell_start.p;
+  S.cell_obj = (const uint16_t*)c->d_cell_obj.p;
+  S.obj_cells = (const ushort4*)c->d_obj_cells.p;
   return S;
 }
 
@@ -459,6 +539,20 @@ RasterArgs raster_args(lg_ctx* c) {
   return A;
 }
 
+lg_status upload_grids(lg_ctx* c, const lgh::GridTables& G) {
+  auto up = [&](DevBuf& b, const void* src, size_t bytes, const char* what) -> lg_status {
+    lg_status st = ensure(c, b, bytes + 16, what);
+    if (st) return st;
+    if (bytes) CK(cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, c->stream), what);
+    return LG_OK;
+  };
+  lg_status st;
+  if ((st = up(c->d_grids, G.recs.data(), G.recs.size() * sizeof(GridRec), "culling grids"))) return st;
+  if ((st = up(c->d_cell_start, G.cell_start.data(), G.cell_start.size() * 4, "culling grids"))) return st;
+  if ((st = up(c->d_cell_obj, G.cell_obj.data(), G.cell_obj.size() * 2, "culling grids"))) return st;
+  return up(c->d_obj_cells, G.obj_cells.data(), G.obj_cells.size() * sizeof(ushort4), "culling grids");
+}
+
 lg_status ensure_trace_buffers(lg_ctx* c) {
   lg_status st;
   if ((st = ensure(c, c->d_queue[0], c->queue_cap * sizeof(RayRec), "ray queue"))) return st;
@@ -489,6 +583,15 @@ lg_status ensure_raster_buffers(lg_ctx* c) {
   return LG_OK;
 }
 
+TraceKernel scan_kernel(bool multi, bool culled) {
+  if (multi) return culled ? k_scan<true, true> : k_scan<true, false>;
+  return culled ? k_scan<false, true> : k_scan<false, false>;
+}
+TraceKernel bounce_kernel(bool multi, bool culled) {
+  if (multi) return culled ? k_bounce<true, true> : k_bounce<true, false>;
+  return culled ? k_bounce<false, true> : k_bounce<false, false>;
+}
+
 lg_status enqueue_trace(lg_ctx* c) {
   const SceneDev S = scene_dev(c);
   const TraceBufs B = trace_bufs(c);
@@ -496,12 +599,12 @@ lg_status enqueue_trace(lg_ctx* c) {
   if (c->n_lights) k_light_setup<false><<<1, 256, 0, c->stream>>>(S);
   const size_t tsm = c->smem_fits ? c->obj_smem : 0;
   for (uint32_t g = 0; g < c->prm.max_bounce; ++g) {
-    k_scan<false><<<c->trace_grid[0], SCAN_THREADS, (size_t)scan_smem_bytes() + tsm, c->stream>>>(S, B, g,
-                                                                                                  c->smem_fits);
+    scan_kernel(false, c->culled)<<<c->trace_grid[0], SCAN_THREADS, (size_t)scan_smem_bytes() + tsm, c->stream>>>(S, B, g,
+                                                                                                   c->smem_fits);
     for (int l = LIST_REFINE_CIRCLE; l <= LIST_REFINE_CUBIC; ++l)
       k_refine<false><<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g, l);
     k_full<false><<<c->trace_grid[2], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
-    k_bounce<false><<<c->trace_grid[3], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
+    bounce_kernel(false, c->culled)<<<c->trace_grid[3], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
   }
   const uint64_t n_ov = 3ull * c->n_cubic * (c->prm.emit_control_lines ? 1 : 0) + c->prm.string_mod.modulo;
   if (n_ov) {
@@ -605,6 +708,8 @@ void fill_stats(lg_ctx* c, lg_trace_stats* s) {
   s->near_degenerate = k.near;
   s->pixels = k.pixels;
   s->tile_refs = k.tile_refs;
+  s->bound_tests = k.bound_tests;
+  s->object_tests = k.object_tests;
 }
 
 lg_status run_trace_once(lg_ctx* c, uint32_t& retries, uint64_t seg_limit = ~0ull);
@@ -714,18 +819,26 @@ lg_status lg_create(lg_ctx** out, const lg_device_opts* opts) {
   c->raster_variant = opts && (opts->raster_variant == 1 || opts->raster_variant == 2) ? opts->raster_variant : 0;
   c->queue_cap_hint = opts ? opts->queue_capacity : 0;
   if (opts && opts->stream_segments) c->stream_ring = opts->stream_segments;
+  if (opts && (opts->culling < LG_CULL_AUTO || opts->culling > LG_CULL_ON || !(opts->grid_density >= 0.0f))) {
+    delete c;
+    return LG_ERR_INVALID_ARGUMENT;
+  }
+  c->culling = opts ? opts->culling : LG_CULL_AUTO;
+  c->grid_density = opts ? opts->grid_density : 0.0f;
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, c->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_ctr, sizeof(Counters));
   if (e == cudaSuccess) e = cudaMalloc(&c->d_ctr.p, sizeof(Counters));
   for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_scan<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, scan_smem_bytes() + (int)OBJ_SMEM_MAX);
+  for (TraceKernel k : {k_scan<false, false>, k_scan<false, true>})
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, scan_smem_bytes() + (int)OBJ_SMEM_MAX);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_full<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bounce<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_scan<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, scan_smem_bytes());
+  for (TraceKernel k : {k_bounce<false, false>, k_bounce<false, true>})
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
+  for (TraceKernel k : {k_scan<true, false>, k_scan<true, true>})
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, scan_smem_bytes());
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_bin_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(MAX_SMEM_TILES * 4));
   if (e == cudaSuccess)
@@ -754,7 +867,8 @@ lg_status lg_destroy(lg_ctx* c) {
                     &c->d_list[3], &c->d_list[4], &c->d_list[5], &c->d_segs, &c->d_paths, &c->d_ctr, &c->d_tile_count, &c->d_tile_off,
                     &c->d_tile_cursor, &c->d_unit_off, &c->d_refs, &c->d_units, &c->d_accum, &c->d_stage,
                     &c->d_scenes, &c->d_canvases, &c->d_seg_scene, &c->d_cubic_scene, &c->d_part,
-                    &c->d_bounds, &c->d_order, &c->d_scene_count, &c->d_scene_off};
+                    &c->d_bounds, &c->d_order, &c->d_scene_count, &c->d_scene_off,
+                    &c->d_grids, &c->d_cell_start, &c->d_cell_obj, &c->d_obj_cells};
   for (DevBuf* b : bufs) release(*b);
   if (c->h_ctr) cudaFreeHost(c->h_ctr);
   for (int i = 0; i < 6; ++i)
@@ -798,11 +912,19 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
   if (!F.prog.empty()) CK(cudaMemcpyAsync(c->d_prog.p, F.prog.data(), F.prog.size(), cudaMemcpyHostToDevice, c->stream), "upload");
   if (!F.lights.empty()) CK(cudaMemcpyAsync(c->d_lights.p, F.lights.data(), F.lights.size() * sizeof(LightDev), cudaMemcpyHostToDevice, c->stream), "upload");
   if (!F.cubics.empty()) CK(cudaMemcpyAsync(c->d_cubics.p, F.cubics.data(), F.cubics.size() * 4, cudaMemcpyHostToDevice, c->stream), "upload");
+  build_grid(F.scan, c->culling, c->grid_density, F.grid);
+  GridTables GT;
+  GT.append(F.grid);
+  if ((st = upload_grids(c, GT))) return st;
   CK(cudaStreamSynchronize(c->stream), "upload");
   if (c->multi) {  // leaving batch mode: every captured launch and launch shape is stale
     c->multi = false;
     c->graph_valid = false;
     c->n_scenes = 0;
+  }
+  if (c->culled != (F.grid.rec.nx > 0)) {  // the captured graph holds the other kernels
+    c->culled = F.grid.rec.nx > 0;
+    c->graph_valid = false;
   }
   c->n_obj = n_objects;
   c->n_leaves = (uint32_t)F.leaves.size();
@@ -821,13 +943,13 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
   c->smem_fits = c->obj_smem <= OBJ_SMEM_MAX ? 1 : 0;
   int occ = 0;
   const size_t tsm = c->smem_fits ? c->obj_smem : 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_scan<false>, SCAN_THREADS, (size_t)scan_smem_bytes() + tsm), "occupancy");
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, scan_kernel(false, c->culled), SCAN_THREADS, (size_t)scan_smem_bytes() + tsm), "occupancy");
   c->trace_grid[0] = c->n_sm * std::max(1, occ);
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_refine<false>, 256, 0), "occupancy");
   c->trace_grid[1] = c->n_sm * std::max(1, occ);
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_full<false>, 256, tsm), "occupancy");
   c->trace_grid[2] = c->n_sm * std::max(1, occ);
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bounce<false>, 256, tsm), "occupancy");
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bounce_kernel(false, c->culled), 256, tsm), "occupancy");
   c->trace_grid[3] = c->n_sm * std::max(1, occ);
   const int mode = raster_mode(p);
   const int rsm = raster_smem_bytes(mode);
@@ -972,12 +1094,12 @@ static lg_status enqueue_stream_frame(lg_ctx* c, uint16_t* dst, size_t row, cuda
   const uint64_t n_ov = 3ull * c->n_cubic * (c->prm.emit_control_lines ? 1 : 0) + c->prm.string_mod.modulo;
   const uint32_t G = c->prm.max_bounce;
   for (uint32_t g = 0; g < G; ++g) {
-    k_scan<false><<<c->trace_grid[0], SCAN_THREADS, (size_t)scan_smem_bytes() + tsm, c->stream>>>(S, B, g,
-                                                                                                  c->smem_fits);
+    scan_kernel(false, c->culled)<<<c->trace_grid[0], SCAN_THREADS, (size_t)scan_smem_bytes() + tsm, c->stream>>>(S, B, g,
+                                                                                                   c->smem_fits);
     for (int l = LIST_REFINE_CIRCLE; l <= LIST_REFINE_CUBIC; ++l)
       k_refine<false><<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g, l);
     k_full<false><<<c->trace_grid[2], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
-    k_bounce<false><<<c->trace_grid[3], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
+    bounce_kernel(false, c->culled)<<<c->trace_grid[3], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
     if (g == 0 && n_ov) {
       const int blocks = (int)std::min<uint64_t>((n_ov + 255) / 256, 4096);
       k_overlay<<<blocks, 256, 0, c->stream>>>(S, B, (const uint32_t*)c->d_cubics.p, nullptr,

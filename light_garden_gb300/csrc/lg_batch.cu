@@ -97,11 +97,11 @@ lg_status enqueue_batch(lg_ctx* c, cudaEvent_t* ev) {
       k_scene_scatter<<<c->n_sm * 8, 256, 0, c->stream>>>(S, B, g, (unsigned*)c->d_scene_off.p,
                                                           (uint32_t*)c->d_order.p);
     }
-    k_scan<true><<<c->batch_grid_scan, SCAN_THREADS, (size_t)scan_smem_bytes(), c->stream>>>(S, B, g, 0);
+    scan_kernel(true, c->culled)<<<c->batch_grid_scan, SCAN_THREADS, (size_t)scan_smem_bytes(), c->stream>>>(S, B, g, 0);
     for (int l = LIST_REFINE_CIRCLE; l <= LIST_REFINE_CUBIC; ++l)
       k_refine<true><<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g, l);
     k_full<true><<<c->trace_grid[2], 256, 0, c->stream>>>(S, B, g, 0);
-    k_bounce<true><<<c->trace_grid[3], 256, 0, c->stream>>>(S, B, g, 0);
+    bounce_kernel(true, c->culled)<<<c->trace_grid[3], 256, 0, c->stream>>>(S, B, g, 0);
     if (g == 0 && c->n_cubic) {
       const int blocks = (int)std::min<uint64_t>((3ull * c->n_cubic + 255) / 256, 4096);
       k_overlay<<<blocks, 256, 0, c->stream>>>(S, B, (const uint32_t*)c->d_cubics.p,
@@ -205,6 +205,7 @@ lg_status lg_batch_upload(lg_ctx* c, const lg_scene_desc* scenes, uint32_t k) {
   const lg_params* p0 = scenes[0].params;
   if (!p0) return fail(c, LG_ERR_INVALID_ARGUMENT, "scene 0: null params");
   Flat F;
+  GridTables grids;
   std::vector<SceneRec> recs(k);
   std::vector<SceneCanvas> canv(k);
   std::vector<uint64_t> px_base(k);
@@ -238,6 +239,8 @@ lg_status lg_batch_upload(lg_ctx* c, const lg_scene_desc* scenes, uint32_t k) {
     F.scan.insert(F.scan.end(), Fs.scan.begin(), Fs.scan.end());
     F.leaves.insert(F.leaves.end(), Fs.leaves.begin(), Fs.leaves.end());
     F.prog.insert(F.prog.end(), Fs.prog.begin(), Fs.prog.end());
+    build_grid(Fs.scan, c->culling, c->grid_density, Fs.grid);
+    grids.append(Fs.grid);
     if (p.emit_control_lines)
       for (uint32_t cu : Fs.cubics) {
         F.cubics.push_back(obj0 + cu);
@@ -299,6 +302,9 @@ lg_status lg_batch_upload(lg_ctx* c, const lg_scene_desc* scenes, uint32_t k) {
   std::vector<float4> bounds(F.scan.size());
   for (size_t i = 0; i < F.scan.size(); ++i) std::memcpy(&bounds[i], &F.scan[i], sizeof(float4));
   if ((st = up(c->d_bounds, bounds.data(), bounds.size() * sizeof(float4), "object bounds"))) return st;
+  if ((st = upload_grids(c, grids))) return st;
+  c->culled = false;
+  for (const GridRec& g : grids.recs) c->culled = c->culled || g.nx > 0;
   if ((st = ensure(c, c->d_scene_count, (size_t)k * 4, "scene counts"))) return st;
   if ((st = ensure(c, c->d_scene_off, (size_t)k * 4, "scene offsets"))) return st;
   CK(cudaStreamSynchronize(c->stream), "upload");
@@ -333,13 +339,13 @@ lg_status lg_batch_upload(lg_ctx* c, const lg_scene_desc* scenes, uint32_t k) {
   if ((st = batch_buffers(c))) return st;
   // launch shapes: the multi-scene kernels read the object tables from global memory
   int occ = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_scan<true>, SCAN_THREADS, (size_t)scan_smem_bytes()), "occupancy");
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, scan_kernel(true, c->culled), SCAN_THREADS, (size_t)scan_smem_bytes()), "occupancy");
   c->batch_grid_scan = c->n_sm * std::max(1, occ);
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_refine<true>, 256, 0), "occupancy");
   c->trace_grid[1] = c->n_sm * std::max(1, occ);
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_full<true>, 256, 0), "occupancy");
   c->trace_grid[2] = c->n_sm * std::max(1, occ);
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bounce<true>, 256, 0), "occupancy");
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bounce_kernel(true, c->culled), 256, 0), "occupancy");
   c->trace_grid[3] = c->n_sm * std::max(1, occ);
   const int mode = raster_mode(c->prm);
   const int rsm = raster_smem_bytes(mode);
@@ -419,6 +425,8 @@ lg_status lg_batch_render(lg_ctx* c, uint16_t* dst, uint64_t dst_bytes, int32_t 
     stats->near_degenerate = k.near;
     stats->pixels = k.pixels;
     stats->tile_refs = k.refs_total;
+    stats->bound_tests = k.bound_tests;
+    stats->object_tests = k.object_tests;
     stats->retries = retries;
     float tr = 0.f, ac = 0.f;
     for (uint32_t g = 0; g < c->max_bounce_all; ++g) {

@@ -68,6 +68,11 @@ struct lg_ctx {
   std::vector<uint64_t> h_px_base;       // first pixel of each scene's image
   DevBuf d_scenes, d_canvases, d_seg_scene, d_cubic_scene, d_part;
   DevBuf d_bounds, d_order, d_scene_count, d_scene_off;
+  // culling grids (one record per scene; a single scene uses record 0)
+  DevBuf d_grids, d_cell_start, d_cell_obj, d_obj_cells;
+  int culling = LG_CULL_AUTO;
+  float grid_density = 0.0f;
+  bool culled = false;  // the uploaded scene (or some scene of the batch) has a grid
   uint64_t total_px = 0;
   uint32_t total_bins = 0;
   uint32_t max_bounce_all = 0;
@@ -87,6 +92,14 @@ void release(DevBuf& b);
 lg_status sync_counters(lg_ctx* c);
 float elapsed(cudaEvent_t a, cudaEvent_t b);
 lg_status ensure_trace_buffers(lg_ctx* c);
+// Copies concatenated culling grids to the device (asynchronous: the caller synchronizes
+// the stream before the host tables go away).
+lg_status upload_grids(lg_ctx* c, const lgh::GridTables& G);
+// The scan and bounce kernels for the context's mode (single scene or multi-scene, with or
+// without the culling walk).
+using TraceKernel = void (*)(SceneDev, TraceBufs, uint32_t, int);
+TraceKernel scan_kernel(bool multi, bool culled);
+TraceKernel bounce_kernel(bool multi, bool culled);
 SceneDev scene_dev(lg_ctx* c);
 TraceBufs trace_bufs(lg_ctx* c);
 RasterArgs raster_args(lg_ctx* c);

@@ -127,6 +127,7 @@ static_assert(sizeof(RayRec) == 80, "RayRec is 80 B");
 // endpoints may then differ from an FP64 trace by more than a tenth of the 1e-5 endpoint
 // tolerance.  Below it, decisions are checked against the bound itself (Near).
 constexpr float ILL_COND = 1e-6f;
+constexpr float FP64_SOLVE_EPS = 8.9e-16f;  // 4 ulp(1) of FP64: rounding of an FP64 discriminant
 constexpr float TOL_REACH = 5.0f;  // longest ray parameter inside a canvas (16:9 diagonal ~ 4.1)
 __device__ __forceinline__ float ray_tol(float ex, float ea) { return ex + TOL_REACH * ea; }
 constexpr float DF_ROUND = 2e-14f;  // double-float rounding per bounce, relative to the coordinates
@@ -149,6 +150,7 @@ struct Counters {
   // multi-scene streaming accumulation: the ring and the tile lists are reused every
   // generation; these keep the totals and the largest per-generation demands
   unsigned long long seg_total, seg_max, refs_total, refs_max;
+  unsigned long long bound_tests, object_tests;  // nearest-hit search: bounding tests, classifications
   unsigned int error_flags;
   unsigned int skip_raster;  // streaming accumulation: this generation's accumulation is deferred
 };
@@ -165,6 +167,28 @@ struct __align__(16) SceneRec {
   uint32_t _pad[2];
 };
 static_assert(sizeof(SceneRec) == 48, "SceneRec is 48 B");
+
+// Uniform culling grid of one scene (built on the host).  The box is the union of the
+// objects' FP32 bounding circles, each inflated by `margin` (above the FP32 error of the
+// traversal: a cell the walk reports at ray parameter t is within far less than margin of
+// the exact ray).  Cell c = iy * nx + ix lists, in ascending object order, every object
+// whose inflated box overlaps it: cell_start[cell_base + c] .. cell_start[cell_base + c + 1]
+// index cell_obj[list_base + ...] (scene-local object numbers).  obj_cells holds each
+// object's cell range (x0, y0, x1, y1), from which a walk that enters a cell knows whether
+// it already met the object in the cell before.  nx == 0: no grid, the scan is brute force.
+// Rays whose origin lies farther out than `reach` (|ox| + |oy|) carry FP32 errors above
+// the margin and test every object instead.
+struct __align__(16) GridRec {
+  float x0, y0;           // lower-left corner
+  float cw, ch;           // cell size
+  float iw, ih;           // 1 / cell size
+  float margin;           // world units: box inflation and traversal slack
+  uint32_t nx, ny;
+  uint32_t cell_base;     // first of the scene's nx * ny + 1 cell offsets
+  uint32_t list_base;     // first of the scene's object-list entries
+  float reach;
+};
+static_assert(sizeof(GridRec) == 48, "GridRec is 48 B");
 
 struct SceneDev {
   const ObjScan* scan;
@@ -187,7 +211,17 @@ struct SceneDev {
   uint32_t serve;
   uint64_t n_new;
   uint32_t light_lo, light_hi;
+  // culling grids: one per scene (index 0 for a single-scene trace)
+  const GridRec* grids;
+  const uint32_t* cell_start;
+  const uint16_t* cell_obj;
+  const ushort4* obj_cells;  // per object (absolute index): its cell range
 };
+
+template <bool MULTI>
+__device__ __forceinline__ const GridRec& grid_of(const SceneDev& S, uint32_t sid) {
+  return S.grids[MULTI ? sid : 0u];
+}
 
 // The scene a ray belongs to, as the kernels use it.  Single-scene kernels (MULTI false)
 // take everything from the kernel parameters; multi-scene kernels read the scene table.
@@ -290,13 +324,24 @@ __device__ __forceinline__ bool past_tmin(df t) { return t.hi > 1e-9f || (t.hi =
 // parametrisation (circle: t; rect: entry, exit; cubic: curve parameter).  Each kind is
 // one out-of-line function so the kernel keeps a single copy of it in the instruction
 // cache however many call sites a ray visit has.
+// Discriminant b^2 - a (|f|^2 - r^2) of the ray o + t d against the circle |p - c| = r
+// (f = o - c, a = d.d, b = f.d), computed as a (r^2 - |l|^2) with l = f - (b / a) d the
+// centre's perpendicular offset from the ray.  For an origin far from a small circle,
+// b^2 and a |f|^2 are large and nearly equal and their difference keeps only the
+// rounding of |f|^2; l is formed from f directly, so the error stays at the rounding of f.
+__device__ __forceinline__ df perp_disc(df fx, df fy, df dx, df dy, df a, df b, df r2) {
+  const df s = b / a;
+  const df lx = fx - dx * s, ly = fy - dy * s;
+  return a * (r2 - (lx * lx + ly * ly));
+}
+
 static __device__ __noinline__ int hits_circle(const Leaf64& L, df ox, df oy, df dx, df dy, Hit64* h, Near& ev) {
   int n = 0;
   (void)n;
   const df cx = L.p[0], cy = L.p[1], r = L.p[2];
   const df ocx = ox - cx, ocy = oy - cy;
   const df a = dx * dx + dy * dy, b = ocx * dx + ocy * dy, cc = ocx * ocx + ocy * ocy - r * r;
-  const df disc = b * b - a * cc;
+  const df disc = perp_disc(ocx, ocy, dx, dy, a, b, r * r);
   const float tc = -b.hi / a.hi;
   // a lateral shift tol of the ray moves disc / a = r^2 - perp^2 by at most 2 r tol
   if (fabsf(disc.hi) <= fmaxf(1e-10f * (b.hi * b.hi + fabsf(a.hi * cc.hi)), 2.0f * fabsf(r.hi) * ev.tol * a.hi) &&
@@ -512,7 +557,7 @@ static __device__ __noinline__ int hits_ellipse(const Leaf64& L, df ox, df oy, d
   const df lox = c * rx + s * ry, loy = c * ry - s * rx, ldx = c * dx + s * dy, ldy = c * dy - s * dx;
   const df sox = lox * ia, soy = loy * ib, sdx = ldx * ia, sdy = ldy * ib;
   const df a = sdx * sdx + sdy * sdy, b = sox * sdx + soy * sdy, cc = sox * sox + soy * soy - DF_ONE;
-  const df disc = b * b - a * cc;
+  const df disc = perp_disc(sox, soy, sdx, sdy, a, b, DF_ONE);
   const float tc = -b.hi / a.hi;
   const float mn = fminf(L.p[4].hi, L.p[5].hi), mx = fmaxf(L.p[4].hi, L.p[5].hi);
   // a lateral shift tol is at most tol / min(a, b) in the scaled frame
@@ -936,14 +981,22 @@ static __device__ __noinline__ bool refine_root(const SceneDev& S, uint32_t j, i
   const Leaf64 L = S.leaves[oi.leaf_begin + leaf];
   df t;
   if (L.kind == LEAF_CIRCLE) {
+    // Newton from the FP32 root until the step is below 1e-10 of t: the iterate's error is
+    // then of the order of the step times the FP32 derivative's relative error.  An FP32
+    // root far from the origin (|o - c| >> r) can be off by 1e-3 and takes several steps;
+    // no convergence in 8 hands the ray to the full solve.
     t = df{t32, 0.0f};
-    for (int it = 0; it < 2; ++it) {
+    bool conv = false;
+    for (int it = 0; it < 8 && !conv; ++it) {
       const df vx = ox + dx * t - L.p[0], vy = oy + dy * t - L.p[1];
       const df f = vx * vx + vy * vy - L.p[2] * L.p[2];
       const float fp = 2.0f * (vx.hi * dx.hi + vy.hi * dy.hi);
       if (fp == 0.0f) return false;
-      t = t - df{__fdiv_rn(f.hi, fp), 0.0f};
+      const float step = __fdiv_rn(f.hi, fp);
+      t = t - df{step, 0.0f};
+      conv = fabsf(step) <= 1e-10f * (1.0f + fabsf(t.hi));
     }
+    if (!conv) return false;
     h.px = ox + dx * t;
     h.py = oy + dy * t;
     h.nx = (h.px - L.p[0]) * L.p[3];
@@ -984,12 +1037,16 @@ static __device__ __noinline__ bool refine_root(const SceneDev& S, uint32_t j, i
     const df a0 = dx * (c0y - oy) - dy * (c0x - ox);
     const df a1 = dx * c1y - dy * c1x, a2 = dx * c2y - dy * c2x, a3 = dx * c3y - dy * c3x;
     df u{s32, 0.0f};
-    for (int it = 0; it < 2; ++it) {
+    bool conv = false;  // as for the circle: step below 1e-10, at most 8
+    for (int it = 0; it < 8 && !conv; ++it) {
       const df fu = ((a3 * u + a2) * u + a1) * u + a0;
       const float fp = (3.0f * a3.hi * u.hi + 2.0f * a2.hi) * u.hi + a1.hi;
       if (fp == 0.0f) return false;
-      u = u - df{__fdiv_rn(fu.hi, fp), 0.0f};
+      const float step = __fdiv_rn(fu.hi, fp);
+      u = u - df{step, 0.0f};
+      conv = fabsf(step) <= 1e-10f;
     }
+    if (!conv) return false;
     const df bx = ((c3x * u + c2x) * u + c1x) * u + c0x, by = ((c3y * u + c2y) * u + c1y) * u + c0y;
     t = ((bx - ox) * dx + (by - oy) * dy) / (dx * dx + dy * dy);
     h.px = ox + dx * t;

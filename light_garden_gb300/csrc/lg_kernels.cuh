@@ -48,7 +48,9 @@ struct RasterArgs {
 
 template <bool MULTI>
 __global__ void k_light_setup(SceneDev S);
-template <bool MULTI>
+// CULL: the culling-grid walk is compiled in (scenes whose grid has nx == 0 still take
+// the full scan); without it the kernels scan every object.
+template <bool MULTI, bool CULL>
 __global__ void k_scan(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
 int scan_smem_bytes();
 constexpr int SCAN_THREADS = 128;
@@ -56,7 +58,7 @@ template <bool MULTI>
 __global__ void k_refine(SceneDev S, TraceBufs B, uint32_t gen, int list);
 template <bool MULTI>
 __global__ void k_full(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
-template <bool MULTI>
+template <bool MULTI, bool CULL>
 __global__ void k_bounce(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
 __global__ void k_overlay(SceneDev S, TraceBufs B, const uint32_t* cubic_objs, const uint16_t* cubic_scene,
                           uint32_t n_cubic, lg_string_mod sm);

@@ -127,6 +127,9 @@ lg_status upload_tables(lg_ctx* c, ServeState& V, const std::vector<uint32_t>& a
   Flat F;
   std::vector<SceneRec> recs(V.max_slots);
   std::memset(recs.data(), 0, recs.size() * sizeof(SceneRec));
+  GridTables grids;  // records indexed by slot, like the scene records
+  grids.recs.resize(V.max_slots);
+  std::memset(grids.recs.data(), 0, grids.recs.size() * sizeof(GridRec));
   std::vector<uint32_t> order;
   for (uint32_t s = 0; s < V.max_slots; ++s)
     if (V.slots[s].active && std::find(admitted.begin(), admitted.end(), s) == admitted.end()) order.push_back(s);
@@ -147,6 +150,7 @@ lg_status upload_tables(lg_ctx* c, ServeState& V, const std::vector<uint32_t>& a
     F.scan.insert(F.scan.end(), Fs.scan.begin(), Fs.scan.end());
     F.leaves.insert(F.leaves.end(), Fs.leaves.begin(), Fs.leaves.end());
     F.prog.insert(F.prog.end(), Fs.prog.begin(), Fs.prog.end());
+    grids.recs[s] = grids.add(Fs.grid);
     const uint32_t light0 = (uint32_t)F.lights.size();
     for (LightDev L : Fs.lights) {
       L.scene = s;
@@ -191,6 +195,7 @@ lg_status upload_tables(lg_ctx* c, ServeState& V, const std::vector<uint32_t>& a
   if ((st = up(c->d_prog, F.prog.data(), F.prog.size(), "scene"))) return st;
   if ((st = up(c->d_lights, F.lights.data(), F.lights.size() * sizeof(LightDev), "scene"))) return st;
   if ((st = up(c->d_bounds, bounds.data(), bounds.size() * sizeof(float4), "object bounds"))) return st;
+  if ((st = upload_grids(c, grids))) return st;
   if ((st = up(c->d_scenes, recs.data(), recs.size() * sizeof(SceneRec), "scene table"))) return st;
   if ((st = up(c->d_cubics, cubic_obj.data(), cubic_obj.size() * 4, "scene"))) return st;
   if ((st = up(c->d_cubic_scene, cubic_slot.data(), cubic_slot.size() * 2, "scene"))) return st;
@@ -362,6 +367,7 @@ lg_status lg_serve_begin(lg_ctx* c, const lg_serve_opts* opts) {
   ServeState* V = new (std::nothrow) ServeState();
   if (!V) return LG_ERR_OUT_OF_MEMORY;
   c->serve = V;
+  c->culled = true;  // requests come and go: the scan takes each scene's grid or full scan as it finds it
   V->max_slots = opts->max_slots;
   V->budget = budget;
   V->slots.assign(V->max_slots, Slot());
@@ -388,13 +394,13 @@ lg_status lg_serve_begin(lg_ctx* c, const lg_serve_opts* opts) {
   std::memset(c->h_ctr, 0, sizeof(Counters));
   // launch shapes of the multi-scene kernels
   int occ = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_scan<true>, SCAN_THREADS, (size_t)scan_smem_bytes()), "occupancy");
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, scan_kernel(true, c->culled), SCAN_THREADS, (size_t)scan_smem_bytes()), "occupancy");
   c->batch_grid_scan = c->n_sm * std::max(1, occ);
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_refine<true>, 256, 0), "occupancy");
   c->trace_grid[1] = c->n_sm * std::max(1, occ);
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_full<true>, 256, 0), "occupancy");
   c->trace_grid[2] = c->n_sm * std::max(1, occ);
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bounce<true>, 256, 0), "occupancy");
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bounce_kernel(true, c->culled), 256, 0), "occupancy");
   c->trace_grid[3] = c->n_sm * std::max(1, occ);
   const int rsm = raster_smem_bytes(RM_FIXED_SPLIT_);
   CK(cudaFuncSetAttribute(k_raster<RM_FIXED_SPLIT_>, cudaFuncAttributeMaxDynamicSharedMemorySize, rsm), "smem attr");
@@ -426,6 +432,7 @@ lg_status lg_serve_submit(lg_ctx* c, const lg_scene_desc* d, uint64_t* id_out) {
   Request R;
   st = flatten_scene(c->err, d->geos, d->n_geo, d->objects, d->n_objects, d->lights, d->n_lights, R.F);
   if (st) return st;
+  build_grid(R.F.scan, c->culling, c->grid_density, R.F.grid);
   R.prm = p;
   for (uint32_t l = 0; l < d->n_lights; ++l) R.primaries += d->lights[l].num_rays;
   if (2 * R.primaries > c->queue_cap) return fail(c, LG_ERR_BUDGET, "scene has more primary rays than the budget's ray queue admits");
@@ -534,11 +541,11 @@ lg_status lg_serve_step(lg_ctx* c, lg_serve_step_stats* stats) {
     k_scene_offsets<<<1, 1024, 0, c->stream>>>((unsigned*)c->d_scene_count.p, (unsigned*)c->d_scene_off.p, V.max_slots);
     k_scene_scatter<<<c->n_sm * 8, 256, 0, c->stream>>>(SD, B, g, (unsigned*)c->d_scene_off.p, (uint32_t*)c->d_order.p);
   }
-  k_scan<true><<<c->batch_grid_scan, SCAN_THREADS, (size_t)scan_smem_bytes(), c->stream>>>(SD, B, g, 0);
+  scan_kernel(true, c->culled)<<<c->batch_grid_scan, SCAN_THREADS, (size_t)scan_smem_bytes(), c->stream>>>(SD, B, g, 0);
   for (int l = LIST_REFINE_CIRCLE; l <= LIST_REFINE_CUBIC; ++l)
     k_refine<true><<<c->trace_grid[1], 256, 0, c->stream>>>(SD, B, g, l);
   k_full<true><<<c->trace_grid[2], 256, 0, c->stream>>>(SD, B, g, 0);
-  k_bounce<true><<<c->trace_grid[3], 256, 0, c->stream>>>(SD, B, g, 0);
+  bounce_kernel(true, c->culled)<<<c->trace_grid[3], 256, 0, c->stream>>>(SD, B, g, 0);
   if (!cubic_obj.empty()) {
     lg_string_mod no_sm;
     std::memset(&no_sm, 0, sizeof no_sm);

@@ -241,15 +241,19 @@ __device__ __forceinline__ void emit_segments(const SceneDev& S, const TraceBufs
   }
 }
 
-// Warp-cooperative FP32 scan.  Objects are taken in chunks of SCAN_CHUNK: every lane
-// bounding-tests its own ray against the chunk (pruned by its running bound thr) and
-// writes the passing (ray, object) pairs to the warp's shared buffer; then all 32 lanes
-// classify the warp's pairs side by side, so the exact FP32 tests run at full SIMD width
-// instead of only in the lanes whose ray happens to cross a given object.  Each lane then
-// folds its own results in object order: thr shrinks with every certain hit and the
-// candidates (key <= thr) keep object order for the tie rule of tracer.rs:404,417.
+// Warp-cooperative FP32 scan.  Every lane bounding-tests its own ray against a run of
+// objects (pruned by its running bound thr) and writes the passing (ray, object) pairs to
+// the warp's shared buffer; then all 32 lanes classify the warp's pairs side by side, so
+// the exact FP32 tests run at full SIMD width instead of only in the lanes whose ray
+// happens to cross a given object.  Each lane then folds its own results: thr shrinks
+// with every certain hit and the candidates (key <= thr) go to the precise solve, which
+// applies the first-in-object-order tie rule of tracer.rs:404,417 itself.  The runs are
+// either the object table in chunks of SCAN_CHUNK, or (culling grid) the objects listed
+// in the grid cells the lane's ray crosses, nearest cell first.
 constexpr int SCAN_WARPS = 4;
 constexpr int SCAN_CHUNK = 16;
+constexpr int WALK_STEPS = 32;  // culled scan: cell steps and object tests between classifications
+constexpr int SCAN_CULL_BLOCKS = 3;  // culled scan: CTAs per SM the registers are sized for (no spills at 3)
 
 struct __align__(16) PairSlot {
   float key, ub, s;
@@ -267,15 +271,17 @@ struct ScanSmem {  // [slot][lane]: a warp's 32 lanes touch 32 consecutive slots
 
 int scan_smem_bytes() { return (int)sizeof(ScanSmem); }
 
-template <bool MULTI>
-__global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
+template <bool MULTI, bool CULL>
+__global__ void __launch_bounds__(SCAN_WARPS * 32, CULL ? SCAN_CULL_BLOCKS : 4)
+    k_scan(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
   ScanSmem& W = *reinterpret_cast<ScanSmem*>(smem_raw);
   ObjScan* sobj = reinterpret_cast<ObjScan*>(smem_raw + sizeof(ScanSmem));
-  __shared__ unsigned long long blk_visits, blk_near;
-  if (threadIdx.x == 0) { blk_visits = 0; blk_near = 0; }
+  __shared__ unsigned long long blk_visits, blk_near, blk_tests, blk_cls;
+  if (threadIdx.x == 0) { blk_visits = 0; blk_near = 0; blk_tests = 0; blk_cls = 0; }
   unsigned long long my_visits = 0, my_near = 0;
+  uint32_t my_tests = 0;
   bool failed;
   const ObjScan* objs = stage_objects(S, sobj, &bar, !MULTI && smem_fits != 0, B.ctr, failed);
   if (failed) return;
@@ -347,11 +353,11 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
     unsigned pending = MULTI ? live_mask : (live_mask ? 1u : 0u);
     while (pending) {
       bool mine;
-      uint32_t g_lo, g_hi;
+      uint32_t g_lo, g_hi, pass_scene = 0;
       if (MULTI) {
         const int leader = __ffs(pending) - 1;
-        const uint32_t lead_scene = __shfl_sync(0xffffffffu, my_scene, leader);
-        const unsigned grp = __ballot_sync(0xffffffffu, my_scene == lead_scene);
+        pass_scene = __shfl_sync(0xffffffffu, my_scene, leader);
+        const unsigned grp = __ballot_sync(0xffffffffu, my_scene == pass_scene);
         pending &= ~grp;
         mine = (grp >> lane) & 1u;
         g_lo = __shfl_sync(0xffffffffu, sl.base, leader);
@@ -362,22 +368,9 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
         g_lo = 0;
         g_hi = S.n_obj;
       }
-      for (uint32_t j0 = g_lo; j0 < g_hi; j0 += SCAN_CHUNK) {
-        const uint32_t jn = min((uint32_t)SCAN_CHUNK, g_hi - j0);
-        int cnt = 0;
-        for (uint32_t jj = 0; jj < jn; ++jj) {
-          const uint32_t j = j0 + jj;
-          const float4 h = MULTI ? __ldg(&S.bounds[j]) : *reinterpret_cast<const float4*>(&objs[j]);
-          float lb;
-          if (mine && bound_test(h, ox, oy, dx, dy, thr, lb)) {
-            PairSlot ps;
-            ps.key = lb;
-            ps.ub = 0.0f;
-            ps.s = 0.0f;
-            ps.m = j - g_lo;  // scene-local object index
-            W.pairs[w][cnt++][lane] = ps;
-          }
-        }
+      // Classifies the warp's cnt-per-lane pairs side by side, then folds each lane's own
+      // results: thr shrinks with every certain hit, candidates (key <= thr) are kept.
+      auto classify_fold = [&](int cnt) {
         // flatten the warp's pairs: exclusive scan of the per-lane counts
         int incl = cnt;
   #pragma unroll
@@ -386,7 +379,10 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
           if ((int)lane >= o) incl += y;
         }
         W.off[w][lane] = incl - cnt;
-        if (lane == 31) W.off[w][32] = incl;
+        if (lane == 31) {
+          W.off[w][32] = incl;
+          if (incl) atomicAdd(&blk_cls, (unsigned long long)incl);
+        }
         __syncwarp();
         const int total = W.off[w][32];
         for (int p = (int)lane; p < total; p += 32) {
@@ -410,7 +406,6 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
           ps = o;
         }
         __syncwarp();
-        // fold this lane's results in object order
         for (int k = 0; k < cnt; ++k) {
           const PairSlot ps = W.pairs[w][k][lane];
           if (ps.ub < INFINITY) thr = fminf(thr, ps.ub * (1.0f + 1e-4f) + 1e-4f);
@@ -425,8 +420,141 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
           else overflow = true;
         }
         __syncwarp();
+      };
+      const GridRec& G = grid_of<MULTI>(S, pass_scene);
+      const uint32_t gnx = CULL ? G.nx : 0u;
+      if (gnx == 0) {
+        // every object in table order
+        for (uint32_t j0 = g_lo; j0 < g_hi; j0 += SCAN_CHUNK) {
+          const uint32_t jn = min((uint32_t)SCAN_CHUNK, g_hi - j0);
+          int cnt = 0;
+          if (mine) my_tests += jn;
+          for (uint32_t jj = 0; jj < jn; ++jj) {
+            const uint32_t j = j0 + jj;
+            const float4 h = MULTI ? __ldg(&S.bounds[j]) : *reinterpret_cast<const float4*>(&objs[j]);
+            float lb;
+            if (mine && bound_test(h, ox, oy, dx, dy, thr, lb)) {
+              PairSlot ps;
+              ps.key = lb;
+              ps.ub = 0.0f;
+              ps.s = 0.0f;
+              ps.m = j - g_lo;  // scene-local object index
+              W.pairs[w][cnt++][lane] = ps;
+            }
+          }
+          classify_fold(cnt);
+        }
+      } else {
+        // Culled: every lane walks the cells its own ray crosses, nearest first, and stops
+        // at the first cell entered beyond its bound thr.  An object met again in the next
+        // cell (its cell range holds the previous cell) was tested there and is skipped, so
+        // each object is tested at most once per ray.
+        const uint32_t gny = G.ny;
+        const float gx0 = G.x0, gy0 = G.y0, cw = G.cw, ch = G.ch, margin = G.margin;
+        const uint32_t* cstart = S.cell_start + G.cell_base;
+        const uint16_t* cobj = S.cell_obj + G.list_base;
+        const ushort4* ocell = S.obj_cells + g_lo;
+        const float idx = fabsf(dx) > 1e-30f ? 1.0f / dx : 0.0f;
+        const float idy = fabsf(dy) > 1e-30f ? 1.0f / dy : 0.0f;
+        const int sx = dx > 0.0f ? 1 : -1, sy = dy > 0.0f ? 1 : -1;
+        int ix = 0, iy = 0, pix = -1, piy = -1;
+        float tx = INFINITY, ty = INFINITY;
+        uint32_t p = 0, pe = 0, steps = 0;
+        bool act = mine, linear = false;
+        if (act) {
+          if (!(fabsf(ox) + fabsf(oy) <= G.reach)) {
+            // an origin this far out carries FP32 errors above the margin: every object
+            linear = true;
+            pe = g_hi - g_lo;
+          } else {
+            const float bx1 = gx0 + (float)gnx * cw, by1 = gy0 + (float)gny * ch;
+            float t0 = 0.0f, t1 = INFINITY;
+            if (idx != 0.0f) {
+              const float a = (gx0 - ox) * idx, b = (bx1 - ox) * idx;
+              t0 = fmaxf(t0, fminf(a, b));
+              t1 = fminf(t1, fmaxf(a, b));
+            } else if (!(ox >= gx0 && ox <= bx1)) {
+              t1 = -1.0f;
+            }
+            if (idy != 0.0f) {
+              const float a = (gy0 - oy) * idy, b = (by1 - oy) * idy;
+              t0 = fmaxf(t0, fminf(a, b));
+              t1 = fminf(t1, fmaxf(a, b));
+            } else if (!(oy >= gy0 && oy <= by1)) {
+              t1 = -1.0f;
+            }
+            act = t0 <= t1 && t0 <= thr + margin;
+            if (act) {
+              const float fx = fminf(fmaxf(floorf((ox + dx * t0 - gx0) * G.iw), 0.0f), (float)(gnx - 1));
+              const float fy = fminf(fmaxf(floorf((oy + dy * t0 - gy0) * G.ih), 0.0f), (float)(gny - 1));
+              ix = (int)fx;
+              iy = (int)fy;
+              tx = idx != 0.0f ? (gx0 + (float)(ix + (dx > 0.0f ? 1 : 0)) * cw - ox) * idx : INFINITY;
+              ty = idy != 0.0f ? (gy0 + (float)(iy + (dy > 0.0f ? 1 : 0)) * ch - oy) * idy : INFINITY;
+              const uint32_t c = (uint32_t)iy * gnx + (uint32_t)ix;
+              p = __ldg(cstart + c);
+              pe = __ldg(cstart + c + 1);
+            }
+          }
+        }
+        while (__any_sync(0xffffffffu, act)) {
+          int cnt = 0;
+          for (int st = 0; st < WALK_STEPS; ++st) {
+            const bool can = act && cnt < SCAN_CHUNK;
+            if (!__any_sync(0xffffffffu, can)) break;
+            if (!can) continue;
+            if (p < pe) {
+              const uint32_t j = linear ? p : (uint32_t)__ldg(cobj + p);
+              ++p;
+              bool seen = false;
+              if (!linear) {
+                const ushort4 cr = __ldg(ocell + j);
+                seen = pix >= (int)cr.x && pix <= (int)cr.z && piy >= (int)cr.y && piy <= (int)cr.w;
+              }
+              if (!seen) {
+                ++my_tests;
+                const float4 h = MULTI ? __ldg(&S.bounds[g_lo + j]) : *reinterpret_cast<const float4*>(&objs[j]);
+                float lb;
+                if (bound_test(h, ox, oy, dx, dy, thr, lb)) {
+                  PairSlot ps;
+                  ps.key = lb;
+                  ps.ub = 0.0f;
+                  ps.s = 0.0f;
+                  ps.m = j;
+                  W.pairs[w][cnt++][lane] = ps;
+                }
+              }
+            } else if (linear || ++steps > gnx + gny + 2) {
+              act = false;
+            } else {  // the next cell along the ray
+              pix = ix;
+              piy = iy;
+              float te;
+              if (tx <= ty) {
+                ix += sx;
+                te = tx;
+                tx = (gx0 + (float)(ix + (sx > 0 ? 1 : 0)) * cw - ox) * idx;
+              } else {
+                iy += sy;
+                te = ty;
+                ty = (gy0 + (float)(iy + (sy > 0 ? 1 : 0)) * ch - oy) * idy;
+              }
+              if (ix < 0 || iy < 0 || ix >= (int)gnx || iy >= (int)gny || !(te <= thr + margin) || te == INFINITY) {
+                act = false;
+              } else {
+                const uint32_t c = (uint32_t)iy * gnx + (uint32_t)ix;
+                p = __ldg(cstart + c);
+                pe = __ldg(cstart + c + 1);
+              }
+            }
+          }
+          classify_fold(cnt);
+        }
       }
     }
+    // the ray record again (primaries were stored above): the scan does not keep it live
+    if (valid) r = q[idx];
+    const SceneLoc slp = scene_of<MULTI>(S, valid ? r.scene : 0u);
     bool emit = false;
     float x1 = 0.0f, y1 = 0.0f;
     uint8_t eflags = 0;
@@ -456,7 +584,7 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
         const int leaf = (int)((first.m >> 16) & 0xffu) - 1, face = (int)(first.m >> 24) - 1;
         if (!overflow && m == 1 && first.key == first.ub && leaf >= 0) {
           // a single candidate whose nearest root is certain: only that root is refined
-          const uint32_t oinfo = reinterpret_cast<const uint32_t*>(&objs[sl.base + sc.cand[0]])[3];
+          const uint32_t oinfo = reinterpret_cast<const uint32_t*>(&objs[slp.base + sc.cand[0]])[3];
           const int kind = leaf_kind_of(oinfo, leaf);
           sc.leaf = (int8_t)leaf;
           sc.face = (int8_t)face;
@@ -469,10 +597,10 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
         } else {
           // no object can be hit: leave through the canvas (tracer.rs:482-488)
           float L;
-          if (fast_canvas_exit(sl.aspect, r, x1, y1, L)) {
+          if (fast_canvas_exit(slp.aspect, r, x1, y1, L)) {
             emit = true;
             ++my_visits;
-            eflags = r.flags | (near_cutoff(r.c, sl.cutoff) || L > ILL_COND ? LG_PATH_NEAR_DEGENERATE : 0);
+            eflags = r.flags | (near_cutoff(r.c, slp.cutoff) || L > ILL_COND ? LG_PATH_NEAR_DEGENERATE : 0);
           } else {
             list = LIST_EXIT;
           }
@@ -485,15 +613,20 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, 4) k_scan(SceneDev S, TraceBu
   }
   atomicAdd(&blk_visits, my_visits);
   atomicAdd(&blk_near, my_near);
+  atomicAdd(&blk_tests, (unsigned long long)my_tests);
   __syncthreads();
   if (threadIdx.x == 0) {
     atomicAdd(&B.ctr->visits, blk_visits);
     atomicAdd(&B.ctr->near, blk_near);
+    atomicAdd(&B.ctr->bound_tests, blk_tests);
+    atomicAdd(&B.ctr->object_tests, blk_cls);
   }
 }
 
-template __global__ void k_scan<false>(SceneDev, TraceBufs, uint32_t, int);
-template __global__ void k_scan<true>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<false, false>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<false, true>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<true, false>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<true, true>(SceneDev, TraceBufs, uint32_t, int);
 
 __device__ __forceinline__ void store_hit(HitRec& o, int obj, const Hit64& h, float ev, uint8_t flags) {
   o.obj = obj < 0 ? HIT_NONE : (uint16_t)obj;
@@ -621,7 +754,7 @@ struct Bounce {
   RayRec child[2];
 };
 
-template <bool MULTI>
+template <bool MULTI, bool CULL>
 __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, const RayRec& r, const ScanRec& sc,
                                        const HitRec* hrec, Bounce& v) {
   v.emit = false;
@@ -647,9 +780,15 @@ __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, c
     // first-order error at the hit: lateral offset L, offset along the surface ds
     const df ddn = dx * bh.nx + dy * bh.ny;
     const float ci_abs = fabsf(ddn.hi);
-    const float L = r.ex + bh.t.hi * r.ea + DF_ROUND * (1.0f + fabsf(bh.px.hi) + fabsf(bh.py.hi));
-    const float ds = L / fmaxf(ci_abs, 1e-6f);
     const float kap = fminf(bh.k, 1e30f);
+    // The FP64 quadratic of a curved surface (b^2 - a c with |b| ~ |o - c|) moves the
+    // reference's own hit by about eps64 |o - c|^2 / (r cos) along the ray: an origin far
+    // from a small circle makes the reference's result itself uncertain, and the path is
+    // flagged once that, carried through the bounces, passes ILL_COND.
+    const float oc = bh.t.hi + (kap > 0.0f ? 1.0f / kap : 0.0f);
+    const float ref_solve = kap > 0.0f ? FP64_SOLVE_EPS * oc * oc * kap / fmaxf(ci_abs, 1e-6f) : 0.0f;
+    const float L = r.ex + bh.t.hi * r.ea + DF_ROUND * (1.0f + fabsf(bh.px.hi) + fabsf(bh.py.hi)) + ref_solve;
+    const float ds = L / fmaxf(ci_abs, 1e-6f);
     if (L > ILL_COND) fl |= LG_PATH_NEAR_DEGENERATE;
     if (oi.flags & INFO_MATERIAL) {
       // medium on the far side (tracer.rs:428-442); "origin inside obj" at the midpoint
@@ -658,18 +797,32 @@ __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, c
       bool near = false;
       if (obj_contains64(S, sl.base + (uint32_t)best, DF_HALF * (ox + bh.px), DF_HALF * (oy + bh.py), near, L)) {
         const float px32 = bh.px.hi, py32 = bh.py.hi;
-        for (uint32_t k = 0; k < sl.n; ++k) {
-          if ((int)k == best) continue;
+        // the first other material object, in table order, that contains the hit point
+        auto far_side = [&](uint32_t k) -> bool {
+          if ((int)k == best) return false;
           const float4 h = MULTI ? __ldg(&S.bounds[sl.base + k]) : *reinterpret_cast<const float4*>(&objs[sl.base + k]);
-          if (!(__float_as_uint(h.w) & INFO_MATERIAL)) continue;
+          if (!(__float_as_uint(h.w) & INFO_MATERIAL)) return false;
           const float ex = px32 - h.x, ey = py32 - h.y;
           const float tol = 2e-6f * (fabsf(px32) + fabsf(py32) + fabsf(h.x) + fabsf(h.y) + h.z) + 1e-6f;
-          if (ex * ex + ey * ey > (h.z + tol) * (h.z + tol)) continue;
-          if (obj_contains64(S, sl.base + k, bh.px, bh.py, near, L)) {
-            n2 = S.info[sl.base + k].n;
-            m2 = (uint16_t)k;
-            break;
-          }
+          if (ex * ex + ey * ey > (h.z + tol) * (h.z + tol)) return false;
+          if (!obj_contains64(S, sl.base + k, bh.px, bh.py, near, L)) return false;
+          n2 = S.info[sl.base + k].n;
+          m2 = (uint16_t)k;
+          return true;
+        };
+        const GridRec& G = grid_of<MULTI>(S, r.scene);
+        if (!CULL || G.nx == 0) {
+          for (uint32_t k = 0; k < sl.n; ++k)
+            if (far_side(k)) break;
+        } else {
+          // the hit point's cell lists, in table order, every object whose box holds it
+          const float fx = fminf(fmaxf(floorf((px32 - G.x0) * G.iw), 0.0f), (float)(G.nx - 1));
+          const float fy = fminf(fmaxf(floorf((py32 - G.y0) * G.ih), 0.0f), (float)(G.ny - 1));
+          const uint32_t c = (uint32_t)fy * G.nx + (uint32_t)fx;
+          const uint32_t* cs = S.cell_start + G.cell_base;
+          const uint16_t* co = S.cell_obj + G.list_base;
+          for (uint32_t q = __ldg(cs + c), qe = __ldg(cs + c + 1); q < qe; ++q)
+            if (far_side(__ldg(co + q))) break;
         }
       } else {
         n2 = oi.n;
@@ -782,7 +935,7 @@ __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, c
   v.nchild = w;
 }
 
-template <bool MULTI>
+template <bool MULTI, bool CULL>
 __global__ void __launch_bounds__(256, 3) k_bounce(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
@@ -822,7 +975,7 @@ __global__ void __launch_bounds__(256, 3) k_bounce(SceneDev S, TraceBufs B, uint
       if (!(l < LIST_FULL && sc.leaf == LEAF_REFINE_FAILED)) {  // those are in the full list too
         r = qin[idx];
         ++my_visits;
-        bounce<MULTI>(S, objs, r, sc, &B.hit[idx], v);
+        bounce<MULTI, CULL>(S, objs, r, sc, &B.hit[idx], v);
       }
     }
     emit_segments(S, B, v.emit, r, v.x1, v.y1, v.flags, v.hit, my_near);
@@ -851,8 +1004,10 @@ __global__ void __launch_bounds__(256, 3) k_bounce(SceneDev S, TraceBufs B, uint
     atomicAdd(&B.ctr->near, blk_near);
   }
 }
-template __global__ void k_bounce<false>(SceneDev, TraceBufs, uint32_t, int);
-template __global__ void k_bounce<true>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_bounce<false, false>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_bounce<false, true>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_bounce<true, false>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_bounce<true, true>(SceneDev, TraceBufs, uint32_t, int);
 
 // ------------------------------------------------------------------- scene order
 // Multi-scene generations > 0: a counting sort of the queue entries by scene (histogram,

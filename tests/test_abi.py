@@ -130,6 +130,16 @@ def test_null_context_is_an_argument_error(cuda_lib):
     assert L.lg_destroy(None) in (abi.LG_OK, abi.LG_ERR_INVALID_ARGUMENT)
 
 
+def test_create_rejects_bad_culling_options(cuda_lib):
+    """Option checks come before any device work (no GPU needed)."""
+    h = C.c_void_p()
+    for culling, density in ((3, 0.0), (-1, 0.0), (abi.LG_CULL_ON, -1.0), (abi.LG_CULL_AUTO, float("nan"))):
+        opts = abi.lg_device_opts()
+        opts.culling, opts.grid_density = culling, density
+        assert cuda_lib.lg_create(C.byref(h), C.byref(opts)) == abi.LG_ERR_INVALID_ARGUMENT
+        assert not h.value
+
+
 def test_noalloc_argument_checks_precede_device_work(cuda_lib):
     p = abi.params_default()
     n = C.c_uint64(123)
