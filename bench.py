@@ -391,7 +391,7 @@ def run_csg(args, ws, rank, local):
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    pk = W.csg_scene().packed()
+    pk = W.csg_scene(total_rays=max(8, int(round((1 << 22) * args.ray_scale)))).packed()
     Wd, Hd = pk.params.width, pk.params.height
     ctx = Context(device=local, raster_variant=args.raster_variant, culling=CULL[args.culling], grid_density=args.grid_density)
     ctx.upload(pk)
@@ -423,7 +423,8 @@ def run_csg(args, ws, rank, local):
             "metric": METRIC, "value": value, "unit": "segments/s", "n_gpus": ws, "steps": args.steps,
             "warmup": max(1, args.warmup), "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32 + double-float trace, int64 accumulate", "data": "synthetic",
-            "config": {"workload": CSG_WORKLOAD, "l2": "flushed between steps (512 MB write); working set > L2"},
+            "config": {"workload": CSG_WORKLOAD + ("" if args.ray_scale == 1.0 else f", rays x {args.ray_scale}"),
+                       "l2": "flushed between steps (512 MB write); working set > L2"},
             "px_per_s": ws * st["pixels"] / (ms_max * 1e-3), "segments_per_step": st["segments"],
             "pixels_per_step": st["pixels"], "ray_visits_per_step": st["ray_visits"],
             "fp64_solves_per_step": st["fp64_solves"], "near_degenerate_per_step": st["near_degenerate"],

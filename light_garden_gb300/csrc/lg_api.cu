@@ -220,6 +220,38 @@ void leaf_f32(const LeafH& L, float* a, float* b) {
   }
 }
 
+// Box holding every hit an object's membership program keeps (a hit on a leaf counts when
+// flipping that leaf's membership flips the combination) and its enclosed region:
+// And keeps hits inside both operands (box intersection), AndNot hits inside the first,
+// Or the union.  Disjoint operands of an And leave an empty object, boxed by a point.
+void csg_box(const Flat& F, uint32_t leaf0, const std::vector<uint8_t>& prog, double& x0, double& y0, double& x1,
+             double& y1) {
+  struct Box { double x0, y0, x1, y1; };
+  std::vector<Box> st;
+  for (const uint8_t op : prog) {
+    if (op < 0x40) {
+      Box b{INFINITY, INFINITY, -INFINITY, -INFINITY};
+      leaf_box(F.leaves[leaf0 + op], b.x0, b.y0, b.x1, b.y1);
+      st.push_back(b);
+      continue;
+    }
+    const Box b = st.back();
+    st.pop_back();
+    Box& a = st.back();
+    if (op == PROG_AND) {
+      Box c{std::max(a.x0, b.x0), std::max(a.y0, b.y0), std::min(a.x1, b.x1), std::min(a.y1, b.y1)};
+      if (c.x0 > c.x1 || c.y0 > c.y1) {  // empty: keep a point of the first operand
+        const double mx = 0.5 * (a.x0 + a.x1), my = 0.5 * (a.y0 + a.y1);
+        c = Box{mx, my, mx, my};
+      }
+      a = c;
+    } else if (op == PROG_OR) {
+      a = Box{std::min(a.x0, b.x0), std::min(a.y0, b.y0), std::max(a.x1, b.x1), std::max(a.y1, b.y1)};
+    }  // PROG_AND_NOT: the first operand's box
+  }
+  x0 = st.back().x0; y0 = st.back().y0; x1 = st.back().x1; y1 = st.back().y1;
+}
+
 bool blend_supported(const lg_blend_component& b) {
   if (b.op == LG_BO_MIN || b.op == LG_BO_MAX) return b.src_factor == LG_BF_ONE && b.dst_factor == LG_BF_ONE;
   if (b.op != LG_BO_ADD && b.op != LG_BO_REVERSE_SUBTRACT) return false;
@@ -267,11 +299,13 @@ lg_status flatten_scene(std::string& err, const lg_geo* G, uint32_t n_geo, const
     // FP32 scan record
     ObjScan s;
     std::memset(&s, 0, sizeof s);
-    double x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
-    for (uint32_t i = leaf0; i < F.leaves.size(); ++i) leaf_box(F.leaves[i], x0, y0, x1, y1);
+    double x0, y0, x1, y1;
+    csg_box(F, leaf0, prog, x0, y0, x1, y1);
     const double cx = 0.5 * (x0 + x1), cy = 0.5 * (y0 + y1);
+    // every hit lies in the box and on some leaf: the smaller of the two radii bounds it
     double R = 0.0;
     for (uint32_t i = leaf0; i < F.leaves.size(); ++i) R = std::max(R, leaf_extent(F.leaves[i], cx, cy));
+    R = std::min(R, 0.5 * std::hypot(x1 - x0, y1 - y0));
     if (!std::isfinite(cx) || !std::isfinite(cy) || !std::isfinite(R))
       return set_err(err, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": non-finite geometry");
     s.cx = (float)cx;

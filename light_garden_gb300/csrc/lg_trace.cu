@@ -499,8 +499,9 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, CULL ? SCAN_CULL_BLOCKS : 4)
         }
         while (__any_sync(0xffffffffu, act)) {
           int cnt = 0;
+          bool yield = false;  // a lane that finished a cell with pairs waits for the fold
           for (int st = 0; st < WALK_STEPS; ++st) {
-            const bool can = act && cnt < SCAN_CHUNK;
+            const bool can = act && !yield && cnt < SCAN_CHUNK;
             if (!__any_sync(0xffffffffu, can)) break;
             if (!can) continue;
             if (p < pe) {
@@ -524,6 +525,9 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, CULL ? SCAN_CULL_BLOCKS : 4)
                   W.pairs[w][cnt++][lane] = ps;
                 }
               }
+            } else if (cnt > 0 && !linear) {
+              // fold before the next cell: a hit in this one may end the walk here
+              yield = true;
             } else if (linear || ++steps > gnx + gny + 2) {
               act = false;
             } else {  // the next cell along the ray
