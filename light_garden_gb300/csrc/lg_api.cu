@@ -359,7 +359,6 @@ void build_grid(const std::vector<ObjScan>& scan, int culling, float density, Gr
   std::memset(&G.rec, 0, sizeof G.rec);
   G.cell_start.assign(1, 0u);
   G.cell_obj.clear();
-  G.obj_cells.assign(n, make_ushort4(0, 0, 0, 0));
   const bool want = culling == LG_CULL_ON || (culling != LG_CULL_OFF && n >= (size_t)LG_CULL_AUTO_MIN);
   if (!want || n == 0) return;
   double x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
@@ -377,24 +376,24 @@ void build_grid(const std::vector<ObjScan>& scan, int culling, float density, Gr
   constexpr uint64_t MAX_ENTRIES = 1ull << 24;
   for (;;) {
     const double margin = 4e-5 * scale + 1e-3 * std::min(W / nx, H / ny);
-    const double bx0 = x0 - 2.0 * margin, by0 = y0 - 2.0 * margin;
-    const float fx0 = (float)bx0, fy0 = (float)by0;
-    const float cw = (float)((x1 + 2.0 * margin - fx0) / nx), ch = (float)((y1 + 2.0 * margin - fy0) / ny);
-    auto range = [&](const ObjScan& s) {
-      auto cell = [](double v, double org, double size, int n_) {
-        const double c = std::floor((v - org) / size);
-        return (int)std::min((double)(n_ - 1), std::max(0.0, c));
-      };
-      return make_ushort4((unsigned short)cell((double)s.cx - s.R - margin, fx0, cw, nx),
-                          (unsigned short)cell((double)s.cy - s.R - margin, fy0, ch, ny),
-                          (unsigned short)cell((double)s.cx + s.R + margin, fx0, cw, nx),
-                          (unsigned short)cell((double)s.cy + s.R + margin, fy0, ch, ny));
-    };
+    GridRec& R = G.rec;
+    R.x0 = (float)(x0 - 2.0 * margin);
+    R.y0 = (float)(y0 - 2.0 * margin);
+    R.cw = (float)((x1 + 2.0 * margin - R.x0) / nx);
+    R.ch = (float)((y1 + 2.0 * margin - R.y0) / ny);
+    R.iw = 1.0f / R.cw;
+    R.ih = 1.0f / R.ch;
+    R.margin = (float)margin;
+    R.nx = (uint32_t)nx;
+    R.ny = (uint32_t)ny;
+    R.cell_base = 0;
+    R.list_base = 0;
+    R.reach = (float)scale;
     uint64_t total = 0;
-    for (size_t k = 0; k < n; ++k) {
-      G.obj_cells[k] = range(scan[k]);
-      const ushort4 r = G.obj_cells[k];
-      total += (uint64_t)(r.z - r.x + 1) * (uint64_t)(r.w - r.y + 1);
+    int rx0, ry0, rx1, ry1;
+    for (const ObjScan& o : scan) {
+      grid_cell_range(R, o.cx, o.cy, o.R, rx0, ry0, rx1, ry1);
+      total += (uint64_t)(rx1 - rx0 + 1) * (uint64_t)(ry1 - ry0 + 1);
     }
     if (total > MAX_ENTRIES && (nx > 1 || ny > 1)) {  // huge objects: coarser cells
       nx = std::max(1, nx / 2);
@@ -403,26 +402,19 @@ void build_grid(const std::vector<ObjScan>& scan, int culling, float density, Gr
     }
     const size_t ncell = (size_t)nx * ny;
     G.cell_start.assign(ncell + 1, 0u);
-    for (size_t k = 0; k < n; ++k) {
-      const ushort4 r = G.obj_cells[k];
-      for (int iy = r.y; iy <= r.w; ++iy)
-        for (int ix = r.x; ix <= r.z; ++ix) ++G.cell_start[(size_t)iy * nx + ix + 1];
+    for (const ObjScan& o : scan) {
+      grid_cell_range(R, o.cx, o.cy, o.R, rx0, ry0, rx1, ry1);
+      for (int iy = ry0; iy <= ry1; ++iy)
+        for (int ix = rx0; ix <= rx1; ++ix) ++G.cell_start[(size_t)iy * nx + ix + 1];
     }
     for (size_t c = 0; c < ncell; ++c) G.cell_start[c + 1] += G.cell_start[c];
     G.cell_obj.assign(total, 0);
     std::vector<uint32_t> cur(G.cell_start.begin(), G.cell_start.end() - 1);
     for (size_t k = 0; k < n; ++k) {  // ascending object order within every cell
-      const ushort4 r = G.obj_cells[k];
-      for (int iy = r.y; iy <= r.w; ++iy)
-        for (int ix = r.x; ix <= r.z; ++ix) G.cell_obj[cur[(size_t)iy * nx + ix]++] = (uint16_t)k;
+      grid_cell_range(R, scan[k].cx, scan[k].cy, scan[k].R, rx0, ry0, rx1, ry1);
+      for (int iy = ry0; iy <= ry1; ++iy)
+        for (int ix = rx0; ix <= rx1; ++ix) G.cell_obj[cur[(size_t)iy * nx + ix]++] = (uint16_t)k;
     }
-    GridRec& R = G.rec;
-    R.x0 = fx0; R.y0 = fy0; R.cw = cw; R.ch = ch;
-    R.iw = 1.0f / cw; R.ih = 1.0f / ch;
-    R.margin = (float)margin;
-    R.nx = (uint32_t)nx; R.ny = (uint32_t)ny;
-    R.cell_base = 0; R.list_base = 0;
-    R.reach = (float)scale;
     return;
   }
 }
@@ -521,7 +513,6 @@ SceneDev scene_dev(lg_ctx* c) {
   S.grids = (const GridRec*)c->d_grids.p;
   S.cell_start = (const uint32_t*)c->d_cell_start.p;
   S.cell_obj = (const uint16_t*)c->d_cell_obj.p;
-  S.obj_cells = (const ushort4*)c->d_obj_cells.p;
   return S;
 }
 
@@ -583,8 +574,7 @@ lg_status upload_grids(lg_ctx* c, const lgh::GridTables& G) {
   lg_status st;
   if ((st = up(c->d_grids, G.recs.data(), G.recs.size() * sizeof(GridRec), "culling grids"))) return st;
   if ((st = up(c->d_cell_start, G.cell_start.data(), G.cell_start.size() * 4, "culling grids"))) return st;
-  if ((st = up(c->d_cell_obj, G.cell_obj.data(), G.cell_obj.size() * 2, "culling grids"))) return st;
-  return up(c->d_obj_cells, G.obj_cells.data(), G.obj_cells.size() * sizeof(ushort4), "culling grids");
+  return up(c->d_cell_obj, G.cell_obj.data(), G.cell_obj.size() * 2, "culling grids");
 }
 
 lg_status ensure_trace_buffers(lg_ctx* c) {
@@ -902,7 +892,7 @@ lg_status lg_destroy(lg_ctx* c) {
                     &c->d_tile_cursor, &c->d_unit_off, &c->d_refs, &c->d_units, &c->d_accum, &c->d_stage,
                     &c->d_scenes, &c->d_canvases, &c->d_seg_scene, &c->d_cubic_scene, &c->d_part,
                     &c->d_bounds, &c->d_order, &c->d_scene_count, &c->d_scene_off,
-                    &c->d_grids, &c->d_cell_start, &c->d_cell_obj, &c->d_obj_cells};
+                    &c->d_grids, &c->d_cell_start, &c->d_cell_obj};
   for (DevBuf* b : bufs) release(*b);
   if (c->h_ctr) cudaFreeHost(c->h_ctr);
   for (int i = 0; i < 6; ++i)

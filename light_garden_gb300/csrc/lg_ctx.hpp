@@ -69,7 +69,7 @@ struct lg_ctx {
   DevBuf d_scenes, d_canvases, d_seg_scene, d_cubic_scene, d_part;
   DevBuf d_bounds, d_order, d_scene_count, d_scene_off;
   // culling grids (one record per scene; a single scene uses record 0)
-  DevBuf d_grids, d_cell_start, d_cell_obj, d_obj_cells;
+  DevBuf d_grids, d_cell_start, d_cell_obj;
   int culling = LG_CULL_AUTO;
   float grid_density = 0.0f;
   bool culled = false;  // the uploaded scene (or some scene of the batch) has a grid

@@ -173,9 +173,10 @@ static_assert(sizeof(SceneRec) == 48, "SceneRec is 48 B");
 // traversal: a cell the walk reports at ray parameter t is within far less than margin of
 // the exact ray).  Cell c = iy * nx + ix lists, in ascending object order, every object
 // whose inflated box overlaps it: cell_start[cell_base + c] .. cell_start[cell_base + c + 1]
-// index cell_obj[list_base + ...] (scene-local object numbers).  obj_cells holds each
-// object's cell range (x0, y0, x1, y1), from which a walk that enters a cell knows whether
-// it already met the object in the cell before.  nx == 0: no grid, the scan is brute force.
+// index cell_obj[list_base + ...] (scene-local object numbers).  An object's cell range
+// comes from grid_cell_range, the same FP32 operations on host and device, so a walk that
+// enters a cell knows whether it already met the object in the cell before.  nx == 0: no
+// grid, the scan is brute force.
 // Rays whose origin lies farther out than `reach` (|ox| + |oy|) carry FP32 errors above
 // the margin and test every object instead.
 struct __align__(16) GridRec {
@@ -215,8 +216,43 @@ struct SceneDev {
   const GridRec* grids;
   const uint32_t* cell_start;
   const uint16_t* cell_obj;
-  const ushort4* obj_cells;  // per object (absolute index): its cell range
 };
+
+// First / last cell (unclamped, as a float) of [c - R - margin, c + R + margin] on one
+// axis: round-to-nearest FP32 steps that no compiler may fuse, so the host that fills the
+// cells and the device that walks them get the same integers.
+__host__ __device__ inline float cell_lo(float c, float R, float margin, float org, float inv) {
+#ifdef __CUDA_ARCH__
+  return floorf(__fmul_rn(__fsub_rn(__fsub_rn(__fsub_rn(c, R), margin), org), inv));
+#else
+  volatile float t = c - R;
+  t = t - margin;
+  t = t - org;
+  t = t * inv;
+  return floorf(t);
+#endif
+}
+__host__ __device__ inline float cell_hi(float c, float R, float margin, float org, float inv) {
+#ifdef __CUDA_ARCH__
+  return floorf(__fmul_rn(__fsub_rn(__fadd_rn(__fadd_rn(c, R), margin), org), inv));
+#else
+  volatile float t = c + R;
+  t = t + margin;
+  t = t - org;
+  t = t * inv;
+  return floorf(t);
+#endif
+}
+// Cell range [x0, x1] x [y0, y1] of the box of a bounding circle (cx, cy, R) inflated by the
+// grid's margin.
+__host__ __device__ inline void grid_cell_range(const GridRec& G, float cx, float cy, float R, int& x0, int& y0,
+                                                int& x1, int& y1) {
+  const float fx0 = cell_lo(cx, R, G.margin, G.x0, G.iw), fx1 = cell_hi(cx, R, G.margin, G.x0, G.iw);
+  const float fy0 = cell_lo(cy, R, G.margin, G.y0, G.ih), fy1 = cell_hi(cy, R, G.margin, G.y0, G.ih);
+  const float mx = (float)(G.nx - 1), my = (float)(G.ny - 1);
+  x0 = (int)fminf(fmaxf(fx0, 0.0f), mx); x1 = (int)fminf(fmaxf(fx1, 0.0f), mx);
+  y0 = (int)fminf(fmaxf(fy0, 0.0f), my); y1 = (int)fminf(fmaxf(fy1, 0.0f), my);
+}
 
 template <bool MULTI>
 __device__ __forceinline__ const GridRec& grid_of(const SceneDev& S, uint32_t sid) {

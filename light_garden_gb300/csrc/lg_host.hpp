@@ -22,13 +22,11 @@ struct LeafH {
   double box[4];  // HALFPLANE: the world box of its polygon (the leaf itself is unbounded)
 };
 
-// Culling grid of one scene: the record (bases 0), its cell offsets and object lists, and
-// every object's cell range.
+// Culling grid of one scene: the record (bases 0), its cell offsets and object lists.
 struct GridH {
   GridRec rec;
   std::vector<uint32_t> cell_start;  // nx * ny + 1 (one entry when there is no grid)
   std::vector<uint16_t> cell_obj;
-  std::vector<ushort4> obj_cells;    // one per object
 };
 
 // One scene (or several, concatenated) in the layout of the device tables.
@@ -47,15 +45,13 @@ struct GridTables {
   std::vector<GridRec> recs;
   std::vector<uint32_t> cell_start;
   std::vector<uint16_t> cell_obj;
-  std::vector<ushort4> obj_cells;
-  // appends a scene's cells and object ranges; returns its record with the bases set
+  // appends a scene's cells and object lists; returns its record with the bases set
   GridRec add(const GridH& g) {
     GridRec r = g.rec;
     r.cell_base = (uint32_t)cell_start.size();
     r.list_base = (uint32_t)cell_obj.size();
     cell_start.insert(cell_start.end(), g.cell_start.begin(), g.cell_start.end());
     cell_obj.insert(cell_obj.end(), g.cell_obj.begin(), g.cell_obj.end());
-    obj_cells.insert(obj_cells.end(), g.obj_cells.begin(), g.obj_cells.end());
     return r;
   }
   void append(const GridH& g) { recs.push_back(add(g)); }

@@ -446,18 +446,20 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, CULL ? SCAN_CULL_BLOCKS : 4)
         }
       } else {
         // Culled: every lane walks the cells its own ray crosses, nearest first, and stops
-        // at the first cell entered beyond its bound thr.  An object met again in the next
-        // cell (its cell range holds the previous cell) was tested there and is skipped, so
-        // each object is tested at most once per ray.
+        // at the first cell entered beyond its bound thr.  The walk moves one cell in x or
+        // in y at a time, so the cells of an object's range that it visits are consecutive:
+        // an object whose range holds the previous cell was tested there and is skipped,
+        // and each object is tested at most once per ray.  Only the range's edge on the
+        // side the walk came from needs checking (step in +x: does it start left of ix?).
         const uint32_t gny = G.ny;
         const float gx0 = G.x0, gy0 = G.y0, cw = G.cw, ch = G.ch, margin = G.margin;
         const uint32_t* cstart = S.cell_start + G.cell_base;
         const uint16_t* cobj = S.cell_obj + G.list_base;
-        const ushort4* ocell = S.obj_cells + g_lo;
         const float idx = fabsf(dx) > 1e-30f ? 1.0f / dx : 0.0f;
         const float idy = fabsf(dy) > 1e-30f ? 1.0f / dy : 0.0f;
         const int sx = dx > 0.0f ? 1 : -1, sy = dy > 0.0f ? 1 : -1;
-        int ix = 0, iy = 0, pix = -1, piy = -1;
+        int ix = 0, iy = 0;
+        int came = 0;  // 0: first cell; 1: entered by an x step; 2: by a y step
         float tx = INFINITY, ty = INFINITY;
         uint32_t p = 0, pe = 0, steps = 0;
         bool act = mine, linear = false;
@@ -497,51 +499,60 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, CULL ? SCAN_CULL_BLOCKS : 4)
             }
           }
         }
+        // tests object j (scene-local) with bound h, unless met in the previous cell
+        auto test = [&](uint32_t j, const float4& h, int& cnt) {
+          if (came == 1) {
+            if (sx > 0 ? cell_lo(h.x, h.z, margin, gx0, G.iw) < (float)ix : cell_hi(h.x, h.z, margin, gx0, G.iw) > (float)ix)
+              return;
+          } else if (came == 2) {
+            if (sy > 0 ? cell_lo(h.y, h.z, margin, gy0, G.ih) < (float)iy : cell_hi(h.y, h.z, margin, gy0, G.ih) > (float)iy)
+              return;
+          }
+          ++my_tests;
+          float lb;
+          if (bound_test(h, ox, oy, dx, dy, thr, lb)) {
+            PairSlot ps;
+            ps.key = lb;
+            ps.ub = 0.0f;
+            ps.s = 0.0f;
+            ps.m = j;
+            W.pairs[w][cnt++][lane] = ps;
+          }
+        };
         while (__any_sync(0xffffffffu, act)) {
           int cnt = 0;
           bool yield = false;  // a lane that finished a cell with pairs waits for the fold
           for (int st = 0; st < WALK_STEPS; ++st) {
-            const bool can = act && !yield && cnt < SCAN_CHUNK;
+            const bool can = act && !yield && cnt + 2 <= SCAN_CHUNK;
             if (!__any_sync(0xffffffffu, can)) break;
             if (!can) continue;
             if (p < pe) {
-              const uint32_t j = linear ? p : (uint32_t)__ldg(cobj + p);
-              ++p;
-              bool seen = false;
-              if (!linear) {
-                const ushort4 cr = __ldg(ocell + j);
-                seen = pix >= (int)cr.x && pix <= (int)cr.z && piy >= (int)cr.y && piy <= (int)cr.w;
-              }
-              if (!seen) {
-                ++my_tests;
-                const float4 h = MULTI ? __ldg(&S.bounds[g_lo + j]) : *reinterpret_cast<const float4*>(&objs[j]);
-                float lb;
-                if (bound_test(h, ox, oy, dx, dy, thr, lb)) {
-                  PairSlot ps;
-                  ps.key = lb;
-                  ps.ub = 0.0f;
-                  ps.s = 0.0f;
-                  ps.m = j;
-                  W.pairs[w][cnt++][lane] = ps;
-                }
-              }
+              // two objects of the cell per step: their loads overlap
+              const bool two = p + 1 < pe;
+              const uint32_t j0 = linear ? p : (uint32_t)__ldg(cobj + p);
+              const uint32_t j1 = two ? (linear ? p + 1 : (uint32_t)__ldg(cobj + p + 1)) : j0;
+              p += two ? 2u : 1u;
+              const float4 h0 = MULTI ? __ldg(&S.bounds[g_lo + j0]) : *reinterpret_cast<const float4*>(&objs[j0]);
+              const float4 h1 = MULTI ? __ldg(&S.bounds[g_lo + j1]) : *reinterpret_cast<const float4*>(&objs[j1]);
+              test(j0, h0, cnt);
+              if (two) test(j1, h1, cnt);
             } else if (cnt > 0 && !linear) {
               // fold before the next cell: a hit in this one may end the walk here
               yield = true;
             } else if (linear || ++steps > gnx + gny + 2) {
               act = false;
             } else {  // the next cell along the ray
-              pix = ix;
-              piy = iy;
               float te;
               if (tx <= ty) {
                 ix += sx;
                 te = tx;
                 tx = (gx0 + (float)(ix + (sx > 0 ? 1 : 0)) * cw - ox) * idx;
+                came = 1;
               } else {
                 iy += sy;
                 te = ty;
                 ty = (gy0 + (float)(iy + (sy > 0 ? 1 : 0)) * ch - oy) * idy;
+                came = 2;
               }
               if (ix < 0 || iy < 0 || ix >= (int)gnx || iy >= (int)gny || !(te <= thr + margin) || te == INFINITY) {
                 act = false;
