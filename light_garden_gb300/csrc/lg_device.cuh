@@ -841,12 +841,20 @@ __device__ __forceinline__ int cubic_roots32(const float* A, const float* Bp, fl
     const float fhi = f(hi);
     if (fabsf(flo) <= err || fabsf(fhi) <= err) { unknown = true; return 0; }
     if ((flo < 0.0f) == (fhi < 0.0f)) continue;
-    for (int it = 0; it < 26; ++it) {
-      const float mid = 0.5f * (lo + hi);
-      const float fm = f(mid);
-      if ((fm < 0.0f) == (flo < 0.0f)) { lo = mid; flo = fm; } else { hi = mid; }
+    // f is monotone between knots: Newton from the secant point, kept inside the sign
+    // bracket (a step that leaves it bisects instead), until the step is below 3e-8
+    float u = (flo * hi - fhi * lo) / (flo - fhi);
+    if (!(u > lo && u < hi)) u = 0.5f * (lo + hi);
+    for (int it = 0; it < 40; ++it) {
+      const float fu = f(u);
+      if ((fu < 0.0f) == (flo < 0.0f)) { lo = u; flo = fu; } else { hi = u; }
+      const float fpu = (3.0f * a3 * u + 2.0f * a2) * u + a1;
+      float un = u - fu / fpu;
+      if (!(un > lo && un < hi)) un = 0.5f * (lo + hi);
+      const bool done = fabsf(un - u) <= 3e-8f || fu == 0.0f;
+      u = un;
+      if (done) break;
     }
-    const float u = 0.5f * (lo + hi);
     const float fp = (3.0f * a3 * u + 2.0f * a2) * u + a1;
     if (fabsf(fp) < 1e-3f * sc) { unknown = true; return 0; }
     const float bx = ((c3x * u + c2x) * u + c1x) * u + c0x, by = ((c3y * u + c2y) * u + c1y) * u + c0y;
