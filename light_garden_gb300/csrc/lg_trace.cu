@@ -677,7 +677,7 @@ template __global__ void k_refine<false>(SceneDev, TraceBufs, uint32_t, int);
 template __global__ void k_refine<true>(SceneDev, TraceBufs, uint32_t, int);
 
 template <bool MULTI>
-__global__ void __launch_bounds__(256) k_full(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
+__global__ void __launch_bounds__(256, 2) k_full(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
   __shared__ unsigned long long blk_solves;
