@@ -259,7 +259,10 @@ def run_ours(args, ws, rank, local):
                     "reads plus one flush per tile unit"}
     trace_fp32 = {"kernel": "k_scan/k_refine/k_full/k_bounce (trace, all generations)", "ms": avg["trace_ms"],
                   "ray_visits": visits, "ns_per_visit": avg["trace_ms"] * 1e6 / max(1, visits),
-                  "culling": args.culling, "bound_tests": st["bound_tests"], "object_tests": st["object_tests"]}
+                  "culling": args.culling, "bound_tests": st["bound_tests"], "object_tests": st["object_tests"],
+                  # the trace's unit of work: FP32 ray / object tests per second of trace time
+                  "bound_tests_per_s": st["bound_tests"] / (avg["trace_ms"] * 1e-3),
+                  "object_tests_per_s": st["object_tests"] / (avg["trace_ms"] * 1e-3)}
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
