@@ -126,6 +126,36 @@ __device__ __forceinline__ uint64_t n_segments(const RasterArgs& A) {
   return n < A.seg_cap ? n : A.seg_cap;
 }
 
+// Calls f(i, R, C) for every rasterisable segment i of this thread's grid-stride share.
+// The binning passes need only a segment's endpoints; the next segment's endpoints (and
+// scene) are loaded while the current one's tiles are visited, so that a thread always
+// has a load in flight.
+template <class F>
+__device__ __forceinline__ void for_each_segment(const RasterArgs& A, uint64_t n, F&& f) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  float4 nxt = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  uint32_t nsc = 0;
+  if (i < n) {
+    nxt = __ldg(reinterpret_cast<const float4*>(A.segs + i));
+    if (A.seg_scene) nsc = A.seg_scene[i];
+  }
+  for (; i < n; i += stride) {
+    const float4 g = nxt;
+    const uint32_t sc = nsc;
+    if (i + stride < n) {
+      nxt = __ldg(reinterpret_cast<const float4*>(A.segs + i + stride));
+      if (A.seg_scene) nsc = A.seg_scene[i + stride];
+    }
+    lg_segment sg;
+    sg.x0 = g.x; sg.y0 = g.y; sg.x1 = g.z; sg.y1 = g.w;
+    const CanvasLoc C = A.seg_scene ? canvas_at(A, sc) : canvas_one(A);
+    RSetup R;
+    if (!raster_setup(sg, C.W, C.H, R)) continue;
+    f(i, R, C);
+  }
+}
+
 // Per-CTA tile histogram in shared memory (native 32-bit shared atomics), one global
 // atomic per touched tile per CTA.  Falls back to warp-aggregated global atomics when the
 // tile count does not fit (smem_tiles == 0).
@@ -137,10 +167,7 @@ __global__ void __launch_bounds__(256) k_bin_count(RasterArgs A, int smem_tiles)
     for (uint32_t t = threadIdx.x; t < A.n_tiles; t += blockDim.x) hist[t] = 0;
     __syncthreads();
   }
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    RSetup R;
-    const CanvasLoc C = canvas_of_segment(A, i);
-    if (!raster_setup(A.segs[i], C.W, C.H, R)) continue;
+  for_each_segment(A, n, [&](uint64_t, const RSetup& R, const CanvasLoc& C) {
     for_each_tile(R, C, [&](uint32_t tile) {
       if (smem_tiles) {
         atomicAdd(&hist[tile], 1u);
@@ -151,7 +178,7 @@ __global__ void __launch_bounds__(256) k_bin_count(RasterArgs A, int smem_tiles)
         if ((int)lane_id() == leader) atomicAdd(&A.tile_count[tile], (unsigned)__popc(grp));
       }
     });
-  }
+  });
   if (smem_tiles) {
     __syncthreads();
     for (uint32_t t = threadIdx.x; t < A.n_tiles; t += blockDim.x)
@@ -365,27 +392,21 @@ __global__ void __launch_bounds__(SCATTER_THREADS) k_bin_scatter(RasterArgs A, i
   if (smem_tiles) {
     for (uint32_t t = threadIdx.x; t < A.n_tiles; t += blockDim.x) cur[t] = 0;
     __syncthreads();
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-      RSetup R;
-      const CanvasLoc C = canvas_of_segment(A, i);
-      if (!raster_setup(A.segs[i], C.W, C.H, R)) continue;
+    for_each_segment(A, n, [&](uint64_t, const RSetup& R, const CanvasLoc& C) {
       for_each_tile(R, C, [&](uint32_t tile) { atomicAdd(&cur[tile], 1u); });
-    }
+    });
     __syncthreads();
     for (uint32_t t = threadIdx.x; t < A.n_tiles; t += blockDim.x) {
       const unsigned c = cur[t];
       cur[t] = c ? (unsigned)atomicAdd(&A.tile_cursor[t], (unsigned long long)c) : 0u;
     }
     __syncthreads();
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-      RSetup R;
-      const CanvasLoc C = canvas_of_segment(A, i);
-      if (!raster_setup(A.segs[i], C.W, C.H, R)) continue;
+    for_each_segment(A, n, [&](uint64_t i, const RSetup& R, const CanvasLoc& C) {
       for_each_tile(R, C, [&](uint32_t tile) {
         const unsigned slot = atomicAdd(&cur[tile], 1u);
         if (slot < A.refs_cap) A.refs[slot] = (uint32_t)i;
       });
-    }
+    });
     return;
   }
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
