@@ -16,7 +16,7 @@ struct DevBuf {
   size_t bytes = 0;
 };
 
-constexpr uint32_t UNIT_REFS = 1024;       // shared-atomic raster: keeps the split sums below 2^31
+constexpr uint32_t UNIT_REFS = SPLIT_UNIT_REFS;  // shared-atomic raster: keeps the split sums within 2^31
 constexpr uint32_t UNIT_REFS_WARP = 8192;  // warp-private raster: no bound, bigger units flush less
 constexpr size_t OBJ_SMEM_MAX = 96 * 1024;
 

@@ -29,7 +29,7 @@ constexpr size_t NOALLOC_SCRATCH_BYTES = 32ull << 20;  // 32 MiB per device
 constexpr uint32_t NOALLOC_MAX_TILES = 4096;           // e.g. 2048 x 2048 pixels in 32 x 32 tiles
 constexpr uint32_t NOALLOC_MAX_BINS = 2 * NOALLOC_MAX_TILES;
 constexpr uint64_t NOALLOC_MAX_REFS = 8000000;         // (segment, tile) pairs per call
-constexpr uint32_t NOALLOC_UNIT_REFS = 1024;           // the shared-atomic raster's unit bound
+constexpr uint32_t NOALLOC_UNIT_REFS = 1024;           // units well within the shared-atomic raster's bound
 constexpr uint64_t NOALLOC_MAX_UNITS = NOALLOC_MAX_BINS + NOALLOC_MAX_REFS / NOALLOC_UNIT_REFS + 1;
 constexpr int MAX_DEVICES = 64;
 

@@ -434,11 +434,17 @@ constexpr int TILE_PX = TILE * TILE;  // cells per channel plane
 // Either way one warp's 32 accesses fall in 32 distinct banks.
 //
 // Fixed-point sums use exact split accumulation in native 32-bit shared atomics: a
-// contribution |q| < 2^42 (a colour term below 1024) is split as q = b * 2^21 + c with an
-// unsigned 21-bit c and a signed b (|b| < 2^21).  A unit holds at most 1024 segments and a
-// segment adds at most once to a pixel, so both plane sums stay below 2^31 and
-// B * 2^21 + C is exact.  A segment with a larger term (up to the clamp, 2^52) skips the
-// tile and adds its 64-bit terms to the image with global atomics, which is just as exact.
+// contribution |q| < 2^36 (a colour term below 16) is split as q = b * 2^18 + c with an
+// unsigned 18-bit c and a signed b (|b| <= 2^18).  A unit holds at most UNIT_REFS = 8192
+// segments and a segment adds at most once to a pixel, so both plane sums stay within 2^31
+// and B * 2^18 + C is exact.  (Eight times fewer units than 1024-segment units with a 21-bit
+// split: each unit ends with a flush of its 32 KB tile by global atomics.)  A segment with
+// a larger term (up to the clamp, 2^52) skips the tile and adds its 64-bit terms to the
+// image with global atomics, which is just as exact.
+constexpr int SPLIT_BITS = 18;   // c = q mod 2^18
+constexpr int SPLIT_LIMIT = 36;  // |q| < 2^36 takes the split planes
+static_assert((1ll << (SPLIT_LIMIT - SPLIT_BITS)) * SPLIT_UNIT_REFS <= (1ll << 31) &&
+                  (1ll << SPLIT_BITS) * SPLIT_UNIT_REFS <= (1ll << 31), "split plane sums must fit 32 bits");
 enum RasterMode { RM_FIXED_SPLIT = 0, RM_FIXED_MINMAX = 1, RM_F32 = 2 };
 
 template <int MODE>
@@ -530,7 +536,7 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs A) {
               long long q = to_fixed(v);
               if (B.op[ch] == LG_BO_REVERSE_SUBTRACT) q = -q;
               qv[ch] = q;
-              big = big || q >= (1ll << 42) || q < -(1ll << 42);
+              big = big || q >= (1ll << SPLIT_LIMIT) || q < -(1ll << SPLIT_LIMIT);
             } else if (MODE == RM_FIXED_MINMAX) {
               long long q = to_fixed(v);
               if (B.op[ch] == LG_BO_REVERSE_SUBTRACT) q = -q;
@@ -544,8 +550,8 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs A) {
 #pragma unroll
             for (int ch = 0; ch < 4; ++ch) {
               const long long q = qv[ch];
-              st.q[2 * ch] = big ? (unsigned)(q & 0xffffffffll) : (unsigned)(q & 0x1fffffll);
-              st.q[2 * ch + 1] = big ? (unsigned)(q >> 32) : (unsigned)(int)(q >> 21);
+              st.q[2 * ch] = big ? (unsigned)(q & 0xffffffffll) : (unsigned)(q & ((1ll << SPLIT_BITS) - 1));
+              st.q[2 * ch + 1] = big ? (unsigned)(q >> 32) : (unsigned)(int)(q >> SPLIT_BITS);
             }
             if (big) st.span |= SPAN_BIG;
           }
@@ -634,7 +640,7 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs A) {
         const int op = B.op[ch];
         if (MODE == RM_FIXED_SPLIT) {
           const unsigned* base = acc32 + 2 * ch * TILE_PX + cell;
-          const long long q = (long long)(int)base[TILE_PX] * (1ll << 21) + (long long)base[0];
+          const long long q = (long long)(int)base[TILE_PX] * (1ll << SPLIT_BITS) + (long long)base[0];
           if (q == 0) continue;
           atomicAdd(reinterpret_cast<unsigned long long*>(A.accum) + px + ch, (unsigned long long)q);
         } else if (MODE == RM_FIXED_MINMAX) {
