@@ -85,7 +85,7 @@ __global__ void k_raster_warp(RasterArgs A);
 int raster_warp_smem_bytes();
 constexpr int RM_FIXED_SPLIT_ = 0, RM_FIXED_MINMAX_ = 1, RM_F32_ = 2;
 // Segments per work unit of the shared-atomic raster: bounds the split-plane sums.
-constexpr uint32_t SPLIT_UNIT_REFS = 8192;
+constexpr uint32_t SPLIT_UNIT_REFS = 16384;
 constexpr uint32_t MAX_SMEM_TILES = 32768;  // tile bins (2 per tile) with 32-bit counters in 128 KB
 // multi-scene streaming accumulation
 __global__ void k_stream_rotate(Counters* ctr, uint64_t seg_cap);

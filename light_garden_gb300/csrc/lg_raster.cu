@@ -434,15 +434,15 @@ constexpr int TILE_PX = TILE * TILE;  // cells per channel plane
 // Either way one warp's 32 accesses fall in 32 distinct banks.
 //
 // Fixed-point sums use exact split accumulation in native 32-bit shared atomics: a
-// contribution |q| < 2^36 (a colour term below 16) is split as q = b * 2^18 + c with an
-// unsigned 18-bit c and a signed b (|b| <= 2^18).  A unit holds at most UNIT_REFS = 8192
-// segments and a segment adds at most once to a pixel, so both plane sums stay within 2^31
-// and B * 2^18 + C is exact.  (Eight times fewer units than 1024-segment units with a 21-bit
-// split: each unit ends with a flush of its 32 KB tile by global atomics.)  A segment with
-// a larger term (up to the clamp, 2^52) skips the tile and adds its 64-bit terms to the
-// image with global atomics, which is just as exact.
-constexpr int SPLIT_BITS = 18;   // c = q mod 2^18
-constexpr int SPLIT_LIMIT = 36;  // |q| < 2^36 takes the split planes
+// contribution |q| < 2^34 (a colour term below 4) is split as q = b * 2^17 + c with an
+// unsigned 17-bit c and a signed b (|b| <= 2^17).  A unit holds at most SPLIT_UNIT_REFS =
+// 16384 segments and a segment adds at most once to a pixel, so both plane sums stay within
+// 2^31 and B * 2^17 + C is exact.  (Sixteen times fewer units than 1024-segment units with
+// a 21-bit split: each unit ends with a flush of its 32 KB tile by global atomics.)  A
+// segment with a larger term (up to the clamp, 2^52) skips the tile and adds its 64-bit
+// terms to the image with global atomics, which is just as exact.
+constexpr int SPLIT_BITS = 17;   // c = q mod 2^17
+constexpr int SPLIT_LIMIT = 34;  // |q| < 2^34 takes the split planes
 static_assert((1ll << (SPLIT_LIMIT - SPLIT_BITS)) * SPLIT_UNIT_REFS <= (1ll << 31) &&
                   (1ll << SPLIT_BITS) * SPLIT_UNIT_REFS <= (1ll << 31), "split plane sums must fit 32 bits");
 enum RasterMode { RM_FIXED_SPLIT = 0, RM_FIXED_MINMAX = 1, RM_F32 = 2 };
