@@ -31,7 +31,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "traced segments/s + accumulated px/s on 1 GB300; p50/p99 scene latency vs plain"
 # DRAM bytes (read + write) per accumulated pixel of k_raster, measured with ncu on the
 # quarter-size mid scene (profiles/k_raster_mid_scene.md)
-RASTER_DRAM_BYTES_PER_PIXEL = 2.64
+RASTER_DRAM_BYTES_PER_PIXEL = 3.43
 CULL = {"auto": 0, "off": 1, "on": 2}  # lg_culling
 
 WORKLOAD = ("mid_scene: 64 objects (rect/circle/mirror/curved mirror, seed 2), 8 lights x 2^18 rays, "
