@@ -410,8 +410,6 @@ static __device__ __noinline__ int hits_circle(const Leaf64& L, df ox, df oy, df
 }
 
 static __device__ __noinline__ int hits_segment(const Leaf64& L, df ox, df oy, df dx, df dy, Hit64* h, Near& ev) {
-  int n = 0;
-  (void)n;
   const df ax = L.p[0], ay = L.p[1], ex = L.p[2] - ax, ey = L.p[3] - ay;
   const df den = dx * ey - dy * ex;
   const float le = sqrtf(ex.hi * ex.hi + ey.hi * ey.hi), ld = sqrtf(dx.hi * dx.hi + dy.hi * dy.hi);
@@ -551,7 +549,10 @@ static __device__ __noinline__ int hits_cubic(const Leaf64& L, df ox, df oy, df 
       const df dfs = (3.0f * a3 * sv + 2.0f * a2) * sv + a1;
       df sn = dfs.hi != 0.0f ? sv - fs / dfs : DF_HALF * (lo + hi);
       if (!(lo < sn && sn < hi)) sn = DF_HALF * (lo + hi);
-      if (sn == sv || (hi - lo).hi <= 1e-14f * (1.0f + fabsf(sv.hi))) { sv = sn; break; }
+      // converged: a step at the double-float resolution (the next one would be below it),
+      // or a bracket that narrow; a root approached from one side never closes the bracket
+      const float tiny = 1e-14f * (1.0f + fabsf(sv.hi));
+      if (sn == sv || fabsf((sn - sv).hi) <= 2.0f * tiny || (hi - lo).hi <= tiny) { sv = sn; break; }
       sv = sn;
     }
     roots[nr++] = sv;
