@@ -561,6 +561,7 @@ RasterArgs raster_args(lg_ctx* c) {
   A.units_cap = c->units_cap;
   A.accum = c->d_accum.p;
   A.ctr = (Counters*)c->d_ctr.p;
+  A.cta_hist = cta_hist_for(c, A.n_tiles);
   return A;
 }
 
@@ -591,6 +592,24 @@ lg_status ensure_trace_buffers(lg_ctx* c) {
   return LG_OK;
 }
 
+lg_status ensure_cta_hist(lg_ctx* c, size_t bins) {
+  if (bins > MAX_SMEM_TILES) return LG_OK;
+  return ensure(c, c->d_cta_hist, (size_t)scatter_grid(c->n_sm, 1) * bins * 4, "per-CTA bin counts");
+}
+
+uint32_t* cta_hist_for(const lg_ctx* c, size_t bins) {
+  const size_t need = (size_t)scatter_grid(c->n_sm, 1) * bins * 4;
+  return bins <= MAX_SMEM_TILES && c->d_cta_hist.p && c->d_cta_hist.bytes >= need ? (uint32_t*)c->d_cta_hist.p
+                                                                                  : nullptr;
+}
+
+void launch_bin_count(lg_ctx* c, const RasterArgs& A, int smem_tiles, size_t bsm) {
+  if (smem_tiles && A.cta_hist)
+    k_bin_count<<<scatter_grid(c->n_sm, 1), SCATTER_THREADS, bsm, c->stream>>>(A, 1);
+  else
+    k_bin_count<<<c->bin_grid, 256, bsm, c->stream>>>(A, smem_tiles);
+}
+
 lg_status ensure_raster_buffers(lg_ctx* c) {
   lg_status st;
   const uint64_t px = (uint64_t)c->prm.width * c->prm.height;
@@ -604,6 +623,7 @@ lg_status ensure_raster_buffers(lg_ctx* c) {
   if ((st = ensure(c, c->d_refs, c->refs_cap * 4, "tile refs"))) return st;
   c->units_cap = bins + c->refs_cap / UNIT_REFS + 1;
   if ((st = ensure(c, c->d_units, c->units_cap * sizeof(Unit), "raster units"))) return st;
+  if ((st = ensure_cta_hist(c, bins))) return st;
   return LG_OK;
 }
 
@@ -655,7 +675,7 @@ lg_status enqueue_accumulate(lg_ctx* c, int binned_event = -1) {
   const uint32_t bins = 2 * c->n_tiles;
   const int smem_tiles = bins <= MAX_SMEM_TILES ? 1 : 0;
   const size_t bsm = smem_tiles ? (size_t)bins * 4 : 0;
-  k_bin_count<<<c->bin_grid, 256, bsm, c->stream>>>(A, smem_tiles);
+  launch_bin_count(c, A, smem_tiles, bsm);
   k_scan_tiles<<<1, 1024, 0, c->stream>>>(A);
   k_build_units<<<std::max(1u, (2 * c->n_tiles + 255) / 256), 256, 0, c->stream>>>(A);
   k_bin_scatter<<<scatter_grid(c->n_sm, smem_tiles), SCATTER_THREADS, bsm, c->stream>>>(A, smem_tiles);
@@ -892,7 +912,7 @@ lg_status lg_destroy(lg_ctx* c) {
                     &c->d_tile_cursor, &c->d_unit_off, &c->d_refs, &c->d_units, &c->d_accum, &c->d_stage,
                     &c->d_scenes, &c->d_canvases, &c->d_seg_scene, &c->d_cubic_scene, &c->d_part,
                     &c->d_bounds, &c->d_order, &c->d_scene_count, &c->d_scene_off,
-                    &c->d_grids, &c->d_cell_start, &c->d_cell_obj};
+                    &c->d_grids, &c->d_cell_start, &c->d_cell_obj, &c->d_cta_hist};
   for (DevBuf* b : bufs) release(*b);
   if (c->h_ctr) cudaFreeHost(c->h_ctr);
   for (int i = 0; i < 6; ++i)
@@ -1132,7 +1152,7 @@ static lg_status enqueue_stream_frame(lg_ctx* c, uint16_t* dst, size_t row, cuda
     CK(cudaEventRecordWithFlags(ev[1 + 2 * g], c->stream, cudaEventRecordExternal), "stage event");
     k_stream_decide<<<1, 1, 0, c->stream>>>((Counters*)c->d_ctr.p, g, c->seg_cap, c->queue_cap, g + 1 == G ? 1 : 0);
     k_clear_counts<<<c->n_sm * 4, 256, 0, c->stream>>>(A);
-    k_bin_count<<<c->bin_grid, 256, bsm, c->stream>>>(A, smem_tiles);
+    launch_bin_count(c, A, smem_tiles, bsm);
     if (bins <= 32768) {
       k_scan_tiles<<<1, 1024, 0, c->stream>>>(A);
     } else {

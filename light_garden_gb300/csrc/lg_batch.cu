@@ -37,6 +37,7 @@ lg_status batch_buffers(lg_ctx* c) {
   if ((st = ensure(c, c->d_refs, c->refs_cap * 4, "tile refs"))) return st;
   c->units_cap = bins + c->refs_cap / UNIT_REFS + 1;
   if ((st = ensure(c, c->d_units, c->units_cap * sizeof(Unit), "raster units"))) return st;
+  if ((st = ensure_cta_hist(c, bins))) return st;
   const size_t parts = (bins + TILE_SCAN_CHUNK - 1) / TILE_SCAN_CHUNK;
   if ((st = ensure(c, c->d_part, std::max<size_t>(parts, 1) * 16, "tile scan partials"))) return st;
   if ((st = ensure(c, c->d_order, c->queue_cap * 4, "scene order"))) return st;
@@ -63,6 +64,7 @@ RasterArgs batch_raster_args(lg_ctx* c) {
   A.ntx = 0;
   A.nty = 0;
   A.n_tiles = c->total_bins;
+  A.cta_hist = cta_hist_for(c, A.n_tiles);
   return A;
 }
 
@@ -112,7 +114,7 @@ lg_status enqueue_batch(lg_ctx* c, cudaEvent_t* ev) {
     k_stream_decide<<<1, 1, 0, c->stream>>>((Counters*)c->d_ctr.p, g, c->seg_cap, c->queue_cap,
                                              g + 1 == c->max_bounce_all ? 1 : 0);
     k_clear_counts<<<c->n_sm * 4, 256, 0, c->stream>>>(A);
-    k_bin_count<<<c->bin_grid, 256, bsm, c->stream>>>(A, smem_tiles);
+    launch_bin_count(c, A, smem_tiles, bsm);
     if (bins <= SMALL_BINS) {
       k_scan_tiles<<<1, 1024, 0, c->stream>>>(A);
     } else {

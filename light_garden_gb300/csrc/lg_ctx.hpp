@@ -46,6 +46,7 @@ struct lg_ctx {
   uint64_t seg_cap_hint = 0, queue_cap_hint = 0;
   // raster
   DevBuf d_tile_count, d_tile_off, d_tile_cursor, d_unit_off, d_refs, d_units, d_accum, d_stage;
+  DevBuf d_cta_hist;  // per-CTA bin counts of the shared-memory binning (scatter launch shape)
   uint64_t refs_cap = 0, units_cap = 0;
   uint32_t n_tiles = 0, ntx = 0, nty = 0;
   // launch shapes
@@ -95,6 +96,12 @@ lg_status ensure_trace_buffers(lg_ctx* c);
 // Copies concatenated culling grids to the device (asynchronous: the caller synchronizes
 // the stream before the host tables go away).
 lg_status upload_grids(lg_ctx* c, const lgh::GridTables& G);
+// Per-CTA bin counts for `bins` bins when they fit shared memory (else nothing to do), and
+// the pointer RasterArgs should carry for them (nullptr when absent).
+lg_status ensure_cta_hist(lg_ctx* c, size_t bins);
+uint32_t* cta_hist_for(const lg_ctx* c, size_t bins);
+// k_bin_count with the scatter's launch shape when the per-CTA counts are kept.
+void launch_bin_count(lg_ctx* c, const RasterArgs& A, int smem_tiles, size_t bsm);
 // The scan and bounce kernels for the context's mode (single scene or multi-scene, with or
 // without the culling walk).
 using TraceKernel = void (*)(SceneDev, TraceBufs, uint32_t, int);

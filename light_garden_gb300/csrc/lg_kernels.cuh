@@ -42,6 +42,10 @@ struct RasterArgs {
   uint64_t refs_cap;
   Unit* units;
   uint64_t units_cap;
+  // shared-memory binning with the scatter's launch shape: k_bin_count leaves each CTA's bin
+  // counts here ([CTA][bin]) and k_bin_scatter reserves its ranges from them instead of
+  // counting its segments again (nullptr: the scatter counts)
+  uint32_t* cta_hist;
   void* accum;             // H * W * 4 of int64 (FIXED64) or float (F32)
   Counters* ctr;
 };

@@ -159,7 +159,7 @@ __device__ __forceinline__ void for_each_segment(const RasterArgs& A, uint64_t n
 // Per-CTA tile histogram in shared memory (native 32-bit shared atomics), one global
 // atomic per touched tile per CTA.  Falls back to warp-aggregated global atomics when the
 // tile count does not fit (smem_tiles == 0).
-__global__ void __launch_bounds__(256) k_bin_count(RasterArgs A, int smem_tiles) {
+__global__ void __launch_bounds__(SCATTER_THREADS) k_bin_count(RasterArgs A, int smem_tiles) {
   if (A.ctr->skip_raster) return;
   extern __shared__ unsigned hist[];
   const uint64_t n = n_segments(A);
@@ -181,8 +181,12 @@ __global__ void __launch_bounds__(256) k_bin_count(RasterArgs A, int smem_tiles)
   });
   if (smem_tiles) {
     __syncthreads();
-    for (uint32_t t = threadIdx.x; t < A.n_tiles; t += blockDim.x)
-      if (hist[t]) atomicAdd(&A.tile_count[t], hist[t]);
+    uint32_t* mine = A.cta_hist ? A.cta_hist + (uint64_t)blockIdx.x * A.n_tiles : nullptr;
+    for (uint32_t t = threadIdx.x; t < A.n_tiles; t += blockDim.x) {
+      const unsigned c = hist[t];
+      if (mine) mine[t] = c;
+      if (c) atomicAdd(&A.tile_count[t], c);
+    }
   }
 }
 
@@ -390,11 +394,16 @@ __global__ void __launch_bounds__(SCATTER_THREADS) k_bin_scatter(RasterArgs A, i
   extern __shared__ unsigned cur[];  // slots are < refs_cap < 2^32
   const uint64_t n = n_segments(A);
   if (smem_tiles) {
-    for (uint32_t t = threadIdx.x; t < A.n_tiles; t += blockDim.x) cur[t] = 0;
-    __syncthreads();
-    for_each_segment(A, n, [&](uint64_t, const RSetup& R, const CanvasLoc& C) {
-      for_each_tile(R, C, [&](uint32_t tile) { atomicAdd(&cur[tile], 1u); });
-    });
+    if (A.cta_hist) {  // this CTA's counts, left by k_bin_count with the same launch shape
+      const uint32_t* mine = A.cta_hist + (uint64_t)blockIdx.x * A.n_tiles;
+      for (uint32_t t = threadIdx.x; t < A.n_tiles; t += blockDim.x) cur[t] = mine[t];
+    } else {
+      for (uint32_t t = threadIdx.x; t < A.n_tiles; t += blockDim.x) cur[t] = 0;
+      __syncthreads();
+      for_each_segment(A, n, [&](uint64_t, const RSetup& R, const CanvasLoc& C) {
+        for_each_tile(R, C, [&](uint32_t tile) { atomicAdd(&cur[tile], 1u); });
+      });
+    }
     __syncthreads();
     for (uint32_t t = threadIdx.x; t < A.n_tiles; t += blockDim.x) {
       const unsigned c = cur[t];

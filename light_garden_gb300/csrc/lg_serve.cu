@@ -272,6 +272,7 @@ lg_status serve_raster_args(lg_ctx* c, ServeState& V, RasterArgs& A) {
   A.W = 0;
   A.H = 0;
   A.n_tiles = c->total_bins;
+  A.cta_hist = nullptr;  // serving bins in global memory (its scatter counts for itself)
   // the stream-ordered canvas copy above reads the host vector: finish it here
   CK(cudaStreamSynchronize(c->stream), "canvas table");
   return LG_OK;
