@@ -202,7 +202,7 @@ def run_ours(args, ws, rank, local):
     for _ in range(max(3, args.warmup)):
         st = ctx.render_into(out_dev.data_ptr(), pitch, True)
     torch.cuda.synchronize()
-    launches_per_step = 1 + 7 * pk.params.max_bounce + 1 + 7  # light setup, 7 per generation, overlay, raster chain
+    launches_per_step = 1 + 4 * pk.params.max_bounce + 1 + 7  # light setup, 4 per generation, overlay, raster chain
 
     barrier(ws)
     torch.cuda.synchronize()

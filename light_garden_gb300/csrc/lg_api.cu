@@ -645,8 +645,7 @@ lg_status enqueue_trace(lg_ctx* c) {
   for (uint32_t g = 0; g < c->prm.max_bounce; ++g) {
     scan_kernel(false, c->culled)<<<c->trace_grid[0], SCAN_THREADS, (size_t)scan_smem_bytes() + tsm, c->stream>>>(S, B, g,
                                                                                                    c->smem_fits);
-    for (int l = LIST_REFINE_CIRCLE; l <= LIST_REFINE_CUBIC; ++l)
-      k_refine<false><<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g, l);
+    k_refine<false><<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g);
     k_full<false><<<c->trace_grid[2], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
     bounce_kernel(false, c->culled)<<<c->trace_grid[3], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
   }
@@ -1140,8 +1139,7 @@ static lg_status enqueue_stream_frame(lg_ctx* c, uint16_t* dst, size_t row, cuda
   for (uint32_t g = 0; g < G; ++g) {
     scan_kernel(false, c->culled)<<<c->trace_grid[0], SCAN_THREADS, (size_t)scan_smem_bytes() + tsm, c->stream>>>(S, B, g,
                                                                                                    c->smem_fits);
-    for (int l = LIST_REFINE_CIRCLE; l <= LIST_REFINE_CUBIC; ++l)
-      k_refine<false><<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g, l);
+    k_refine<false><<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g);
     k_full<false><<<c->trace_grid[2], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
     bounce_kernel(false, c->culled)<<<c->trace_grid[3], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
     if (g == 0 && n_ov) {

@@ -100,8 +100,7 @@ lg_status enqueue_batch(lg_ctx* c, cudaEvent_t* ev) {
                                                           (uint32_t*)c->d_order.p);
     }
     scan_kernel(true, c->culled)<<<c->batch_grid_scan, SCAN_THREADS, (size_t)scan_smem_bytes(), c->stream>>>(S, B, g, 0);
-    for (int l = LIST_REFINE_CIRCLE; l <= LIST_REFINE_CUBIC; ++l)
-      k_refine<true><<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g, l);
+    k_refine<true><<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g);
     k_full<true><<<c->trace_grid[2], 256, 0, c->stream>>>(S, B, g, 0);
     bounce_kernel(true, c->culled)<<<c->trace_grid[3], 256, 0, c->stream>>>(S, B, g, 0);
     if (g == 0 && c->n_cubic) {

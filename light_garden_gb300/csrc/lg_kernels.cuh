@@ -59,7 +59,7 @@ __global__ void k_scan(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
 int scan_smem_bytes();
 constexpr int SCAN_THREADS = 128;
 template <bool MULTI>
-__global__ void k_refine(SceneDev S, TraceBufs B, uint32_t gen, int list);
+__global__ void k_refine(SceneDev S, TraceBufs B, uint32_t gen);
 template <bool MULTI>
 __global__ void k_full(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
 template <bool MULTI, bool CULL>

@@ -543,8 +543,7 @@ lg_status lg_serve_step(lg_ctx* c, lg_serve_step_stats* stats) {
     k_scene_scatter<<<c->n_sm * 8, 256, 0, c->stream>>>(SD, B, g, (unsigned*)c->d_scene_off.p, (uint32_t*)c->d_order.p);
   }
   scan_kernel(true, c->culled)<<<c->batch_grid_scan, SCAN_THREADS, (size_t)scan_smem_bytes(), c->stream>>>(SD, B, g, 0);
-  for (int l = LIST_REFINE_CIRCLE; l <= LIST_REFINE_CUBIC; ++l)
-    k_refine<true><<<c->trace_grid[1], 256, 0, c->stream>>>(SD, B, g, l);
+  k_refine<true><<<c->trace_grid[1], 256, 0, c->stream>>>(SD, B, g);
   k_full<true><<<c->trace_grid[2], 256, 0, c->stream>>>(SD, B, g, 0);
   bounce_kernel(true, c->culled)<<<c->trace_grid[3], 256, 0, c->stream>>>(SD, B, g, 0);
   if (!cubic_obj.empty()) {

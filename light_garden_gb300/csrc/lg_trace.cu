@@ -10,7 +10,7 @@
 //   refract / reflect with colour split (444-481) or canvas exit (482-488).
 //   Segments are appended to the segment ring and children to the next queue with one
 //   atomic per warp (ballot + popc compaction).
-// The chain per generation (k_scan, k_refine x 4 leaf kinds, k_full, k_bounce) is
+// The chain per generation (k_scan, k_refine over 4 leaf-kind lists, k_full, k_bounce) is
 // described above k_scan below.
 #include "lg_kernels.cuh"
 
@@ -131,8 +131,8 @@ template __global__ void k_light_setup<true>(SceneDev);
 // every kernel executes one compact code path on coherent work:
 //   k_scan     FP32: nearest-hit search bound and candidate list per ray; sorts the rays
 //              into work lists (refine circle / rect / segment, full solve)
-//   k_refine   double-float refinement of a winner the FP32 scan proved (one leaf kind
-//              per launch)
+//   k_refine   double-float refinement of a winner the FP32 scan proved (the leaf-kind
+//              lists one after the other)
 //   k_full     double-float solve of every candidate (near ties, uncertain roots, cubic
 //              and deep CSG objects), grouped by solve class
 //   k_bounce   medium (tracer.rs:428-442), refract / reflect with colour split
@@ -652,13 +652,21 @@ __device__ __forceinline__ void store_hit(HitRec& o, int obj, const Hit64& h, fl
   o.flags = flags;
 }
 
+// One launch refines the four leaf-kind lists one after the other (a warp's rays come from
+// one list except at the seams, so the kinds stay apart as in four launches).
 template <bool MULTI>
-__global__ void __launch_bounds__(256) k_refine(SceneDev S, TraceBufs B, uint32_t gen, int list) {
-  unsigned long long n = B.ctr->list_count[gen][list];
-  if (n > B.queue_cap) n = B.queue_cap;
+__global__ void __launch_bounds__(256) k_refine(SceneDev S, TraceBufs B, uint32_t gen) {
+  auto count = [&](int l) -> uint64_t {
+    const unsigned long long c = B.ctr->list_count[gen][l];
+    return c < B.queue_cap ? c : B.queue_cap;
+  };
+  const uint64_t o1 = count(LIST_REFINE_CIRCLE), o2 = o1 + count(LIST_REFINE_RECT);
+  const uint64_t o3 = o2 + count(LIST_REFINE_SEGMENT), n = o3 + count(LIST_REFINE_CUBIC);
   const RayRec* q = B.queue[gen & 1];
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t idx = B.list[list][i];
+    const uint32_t idx = i < o1 ? B.list[LIST_REFINE_CIRCLE][i]
+                       : i < o2 ? B.list[LIST_REFINE_RECT][i - o1]
+                       : i < o3 ? B.list[LIST_REFINE_SEGMENT][i - o2] : B.list[LIST_REFINE_CUBIC][i - o3];
     const RayRec r = q[idx];
     const ScanRec sc = B.scan[idx];
     Hit64 h;
@@ -673,8 +681,8 @@ __global__ void __launch_bounds__(256) k_refine(SceneDev S, TraceBufs B, uint32_
   }
 }
 
-template __global__ void k_refine<false>(SceneDev, TraceBufs, uint32_t, int);
-template __global__ void k_refine<true>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_refine<false>(SceneDev, TraceBufs, uint32_t);
+template __global__ void k_refine<true>(SceneDev, TraceBufs, uint32_t);
 
 template <bool MULTI>
 __global__ void __launch_bounds__(256, 2) k_full(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
