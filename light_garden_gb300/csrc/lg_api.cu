@@ -566,6 +566,9 @@ RasterArgs raster_args(lg_ctx* c) {
 }
 
 lg_status upload_grids(lg_ctx* c, const lgh::GridTables& G) {
+  // grid records address their cells and lists with 32-bit bases
+  if (G.cell_start.size() > 0xffffffffull || G.cell_obj.size() > 0xffffffffull)
+    return fail(c, LG_ERR_UNSUPPORTED, "culling grids of more than 2^32 cells or list entries in one upload");
   auto up = [&](DevBuf& b, const void* src, size_t bytes, const char* what) -> lg_status {
     lg_status st = ensure(c, b, bytes + 16, what);
     if (st) return st;
