@@ -698,8 +698,12 @@ __global__ void __launch_bounds__(256, 2) k_full(SceneDev S, TraceBufs B, uint32
   if (n > B.queue_cap) n = B.queue_cap;
   const RayRec* q = B.queue[gen & 1];
   unsigned long long my_solves = 0;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t idx = B.list[LIST_FULL][i];
+  // block-uniform loop: the CTA's warps solve one class at a time together (a barrier
+  // between classes), so that one solver's code is in flight per CTA
+  for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x; base < n; base += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = base + threadIdx.x;
+    const bool valid = i < n;
+    const uint32_t idx = B.list[LIST_FULL][valid ? i : base];  // idle lanes read a real entry, store nothing
     const RayRec r = q[idx];
     const ScanRec sc = B.scan[idx];
     const SceneLoc sl = scene_of<MULTI>(S, r.scene);
@@ -726,25 +730,27 @@ __global__ void __launch_bounds__(256, 2) k_full(SceneDev S, TraceBufs B, uint32
         }
       }
     };
-    if (!sc.overflow) {
-      uint32_t pending = (1u << sc.nc) - 1u;
+    {
+      uint32_t pending = valid && !sc.overflow ? (1u << sc.nc) - 1u : 0u;
       uint32_t cls[CAND];
       for (int k = 0; k < CAND; ++k)
         cls[k] = k < sc.nc ? solve_class(reinterpret_cast<const uint32_t*>(&sobjs[sc.cand[k]])[3]) : 7u;
-      const unsigned am = __activemask();
       for (uint32_t c = 0; c < N_SOLVE_CLASSES; ++c) {
         for (;;) {
           int k = -1;
-          for (int kk = 0; kk < sc.nc; ++kk)
+          for (int kk = 0; kk < CAND; ++kk)
             if (k < 0 && ((pending >> kk) & 1u) && cls[kk] == c) k = kk;
-          if (!__any_sync(am, k >= 0)) break;
+          if (!__any_sync(0xffffffffu, k >= 0)) break;
           if (k >= 0) {
             pending &= ~(1u << k);
             consider(sc.cand[k]);
           }
         }
+        __syncthreads();
       }
-    } else {  // list overflow (rare): every object that passes the FP32 filters, in order
+    }
+    if (!valid) continue;
+    if (sc.overflow) {  // list overflow (rare): every object that passes the FP32 filters, in order
       const float ox = r.ox.hi, oy = r.oy.hi, dx = r.dx.hi, dy = r.dy.hi;
       for (uint32_t j = 0; j < sl.n; ++j) {
         const float4 h = *reinterpret_cast<const float4*>(&sobjs[j]);
