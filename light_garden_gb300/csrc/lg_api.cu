@@ -624,7 +624,7 @@ lg_status ensure_raster_buffers(lg_ctx* c) {
   if ((st = ensure(c, c->d_tile_cursor, bins * 8, "tile cursors"))) return st;
   if ((st = ensure(c, c->d_unit_off, bins * 8, "unit offsets"))) return st;
   if ((st = ensure(c, c->d_refs, c->refs_cap * 4, "tile refs"))) return st;
-  c->units_cap = bins + c->refs_cap / UNIT_REFS + 1;
+  c->units_cap = bins + c->refs_cap / MIN_UNIT_REFS + 1;
   if ((st = ensure(c, c->d_units, c->units_cap * sizeof(Unit), "raster units"))) return st;
   if ((st = ensure_cta_hist(c, bins))) return st;
   return LG_OK;

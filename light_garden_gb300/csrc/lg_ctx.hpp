@@ -18,6 +18,8 @@ struct DevBuf {
 
 constexpr uint32_t UNIT_REFS = SPLIT_UNIT_REFS;  // shared-atomic raster: keeps the split sums within 2^31
 constexpr uint32_t UNIT_REFS_WARP = 8192;  // warp-private raster: no bound, bigger units flush less
+// the smaller of the two: the unit table is sized for whichever raster the context runs
+constexpr uint32_t MIN_UNIT_REFS = UNIT_REFS < UNIT_REFS_WARP ? UNIT_REFS : UNIT_REFS_WARP;
 constexpr size_t OBJ_SMEM_MAX = 96 * 1024;
 
 }  // namespace lgh

@@ -259,7 +259,7 @@ lg_status serve_raster_args(lg_ctx* c, ServeState& V, RasterArgs& A) {
   if ((st = ensure(c, c->d_tile_cursor, std::max<size_t>(bins, 1) * 8, "tile cursors"))) return st;
   if ((st = ensure(c, c->d_unit_off, std::max<size_t>(bins, 1) * 8, "unit offsets"))) return st;
   if ((st = ensure(c, c->d_refs, c->refs_cap * 4, "tile refs"))) return st;
-  c->units_cap = bins + c->refs_cap / UNIT_REFS + 1;
+  c->units_cap = bins + c->refs_cap / MIN_UNIT_REFS + 1;
   if ((st = ensure(c, c->d_units, c->units_cap * sizeof(Unit), "raster units"))) return st;
   const size_t parts = (bins + TILE_SCAN_CHUNK - 1) / TILE_SCAN_CHUNK;
   if ((st = ensure(c, c->d_part, std::max<size_t>(parts, 1) * 16, "tile scan partials"))) return st;

@@ -72,6 +72,24 @@ def test_raster_bit_exact_on_same_segments(gpu, oracle, variant):
     ctx.close()
 
 
+def test_raster_variants_agree_on_a_large_frame(gpu):
+    """The two tile rasters (shared-memory split planes, 16384-segment units; warp-private
+    tiles, 8192-segment units) give the same fixed-point image on a frame with far more
+    (segment, tile) references than bins, where the unit table must hold the smaller units."""
+    from light_garden_gb300.runtime import Context
+    pk = W.mid_scene(rays_per_light=1 << 15).packed()
+    accs = []
+    for variant in (1, 2):
+        ctx = Context(raster_variant=variant)
+        ctx.upload(pk)
+        ctx.trace()
+        st = ctx.accumulate()
+        assert st["tile_refs"] > 8192 * 2 * 4080
+        accs.append(ctx.accum())
+        ctx.close()
+    assert np.array_equal(accs[0], accs[1])
+
+
 def test_accumulate_segments_matches_oracle(ctx, oracle):
     pk = W.plain_small(accum=abi.LG_ACCUM_FIXED64).packed()
     o_segs, _, _, _ = oracle.trace(pk)
