@@ -37,6 +37,7 @@ class Tracer:
         self.alpha_blend = (abi.LG_BF_SRC_ALPHA, abi.LG_BF_ONE, abi.LG_BO_ADD)
         self.trace_time_vd: List[float] = []
         self.device = device
+        self._culling = abi.LG_CULL_AUTO  # the tile map is on by default (tile_map.rs:61)
         self._ctx: Optional[Context] = None  # created by the first GPU call
 
     # -- object / light list (tracer.rs:48-129) ---------------------------------------------
@@ -113,9 +114,23 @@ class Tracer:
         """The scene as the C ABI's tables (what ``lg_scene_upload`` receives)."""
         return pack(self.objects, self.lights, self.params())
 
+    # -- culling (tracer.rs:137-164: enable_tile_map / tile_map_enabled) -----------------------
+    def enable_tile_map(self, enable: bool) -> None:
+        """The reference's approximate tile map becomes the exact culling grid (``LG_CULL_AUTO``)
+        or the full scan (``LG_CULL_OFF``); the traced segments are the same either way."""
+        culling = abi.LG_CULL_AUTO if enable else abi.LG_CULL_OFF
+        if culling != self._culling:
+            self._culling = culling
+            if self._ctx is not None:  # culling is a context option: the next call makes a new one
+                self._ctx.close()
+                self._ctx = None
+
+    def tile_map_enabled(self) -> bool:
+        return self._culling != abi.LG_CULL_OFF
+
     def _sync(self) -> None:
         if self._ctx is None:
-            self._ctx = Context(self.device)
+            self._ctx = Context(self.device, culling=self._culling)
         self._ctx.upload(self.packed())
 
     def trace_all_array(self) -> np.ndarray:

@@ -137,6 +137,12 @@ def test_tracer_list_api_matches_the_reference_surface():
     t.remove_light(0)
     t.clear()
     assert t.packed().n_objects == 0 and t.packed().n_lights == 0
+    # tracer.rs:137-164: the tile map toggle maps to the culling option (on by default)
+    assert t.tile_map_enabled()
+    t.enable_tile_map(False)
+    assert not t.tile_map_enabled() and t._culling == abi.LG_CULL_OFF
+    t.enable_tile_map(True)
+    assert t.tile_map_enabled() and t._culling == abi.LG_CULL_AUTO
     assert t._ctx is None  # nothing above needed the GPU
     t.close()
 
