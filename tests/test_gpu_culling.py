@@ -139,3 +139,22 @@ def test_culled_batch_images_equal_full_scan(gpu):
         ctx.close()
     for a, b in zip(imgs[abi.LG_CULL_OFF], imgs[abi.LG_CULL_ON]):
         assert np.array_equal(a, b)
+
+
+def test_tracer_tile_map_toggle_keeps_the_image(gpu):
+    """Tracer::enable_tile_map (tracer.rs:137-160) switches the culling option; with the
+    exact grid the rendered image is the same on and off."""
+    from light_garden_gb300.tracer import Tracer
+    w = W.csg_scene(total_rays=1 << 12, width=256, height=256, string_mod=False)
+    t = Tracer(256, 256)
+    for o in w.objects:
+        t.push_object(o)
+    for l in w.lights:
+        t.push_light(l)
+    t.max_bounce = 8
+    on = t.render_to_texture()
+    t.enable_tile_map(False)
+    assert not t.tile_map_enabled()
+    off = t.render_to_texture()
+    assert np.array_equal(on, off)
+    t.close()
