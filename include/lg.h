@@ -39,7 +39,9 @@
 extern "C" {
 #endif
 
-#define LG_ABI_VERSION 1
+/* 2: lg_device_opts gained culling and grid_density, lg_trace_stats bound_tests and
+ * object_tests (both structs grew). */
+#define LG_ABI_VERSION 2
 
 typedef enum lg_status {
   LG_OK = 0,

@@ -112,6 +112,7 @@ class lg_device_opts(C.Structure):
                 ("grid_density", C.c_float)]
 
 
+LG_ABI_VERSION = 2  # include/lg.h
 LG_CULL_AUTO, LG_CULL_OFF, LG_CULL_ON = 0, 1, 2
 LG_CULL_AUTO_MIN = 96
 
@@ -220,6 +221,9 @@ def load(path: os.PathLike | str | None = None) -> C.CDLL:
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
+    version = lib.lg_abi_version()
+    if version != LG_ABI_VERSION:  # the structs below would not match the library's
+        raise RuntimeError(f"{p} has C ABI version {version}, this package expects {LG_ABI_VERSION}: rebuild it")
     if path is None:
         _lib = lib
     return lib
