@@ -30,7 +30,7 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "traced segments/s + accumulated px/s on 1 GB300; p50/p99 scene latency vs plain"
 # DRAM bytes (read + write) per accumulated pixel of k_raster, measured with ncu on the
-# quarter-size mid scene (profiles/k_raster_mid_scene.md)
+# quarter-size mid scene (a scaled constant, not a live measurement)
 RASTER_DRAM_BYTES_PER_PIXEL = 3.43
 CULL = {"auto": 0, "off": 1, "on": 2}  # lg_culling
 
@@ -246,8 +246,8 @@ def run_ours(args, ws, rank, local):
     # single kernel; the trace is 7 kernels per generation.  Algorithmic bytes per
     # accumulated pixel: an int64 RGBA read-modify-write, 32 B read + 32 B written.  The
     # launch is timed live by CUDA events recorded in the captured graph around it.
-    # DRAM traffic per accumulated pixel comes from the ncu capture summarised in
-    # profiles/k_raster_mid_scene.md (a quarter-size case; traffic scales with pixels).
+    # DRAM traffic per accumulated pixel comes from an ncu capture of a quarter-size case
+    # (traffic scales with pixels).
     hbm, peak_kind = peaks()
     alg = 64.0 * pixels
     achieved = alg / (avg["raster_ms"] * 1e-3) / 1e9

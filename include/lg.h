@@ -40,8 +40,9 @@ extern "C" {
 #endif
 
 /* 2: lg_device_opts gained culling and grid_density, lg_trace_stats bound_tests and
- * object_tests (both structs grew). */
-#define LG_ABI_VERSION 2
+ * object_tests (both structs grew).
+ * 3: lg_device_opts gained wait_polls. */
+#define LG_ABI_VERSION 3
 
 typedef enum lg_status {
   LG_OK = 0,
@@ -230,6 +231,10 @@ typedef struct lg_device_opts {
                                  segments, once a frame has more (0 = 2^28) */
   int32_t culling;            /* lg_culling: spatial culling of the nearest-hit search */
   float grid_density;         /* culling grid cells per object (0 = 2) */
+  int32_t wait_polls;         /* polls of each bounded device-side wait before it gives up with
+                                 LG_ERR_TIMEOUT: 0 = default (2^22); a negative value gives up
+                                 at once (exercises the timeout path in tests) */
+  int32_t _pad;
 } lg_device_opts;
 
 /* Nearest-hit culling (replaces the reference's approximate tile map, tile_map.rs:18-146).
@@ -366,13 +371,15 @@ lg_status lg_serve_end(lg_ctx* ctx);
  * n segments into it exactly like lg_accumulate_segments, on the calling thread's current
  * device and the given stream (NULL = default stream), without a context and without
  * allocating.  `segments` and `accum` must be device-accessible (accum: width*height*4
- * int64 for LG_ACCUM_FIXED64, float for LG_ACCUM_F32).  Binning scratch lives in one
- * 32 MiB array per device, resident until the process exits; limits per call: at most
- * 4096 tiles of 32x32 pixels (e.g. 2048x2048) and 8,000,000 (segment, tile) pairs, else
- * LG_ERR_BUDGET (and the image is not valid).  The first call on a device sets the array
- * up; make it before any stream capture.  Calls share the array, so calls that overlap on
- * the GPU race: serialise them.  Returns after the work completed; *pixels_out (optional)
- * receives the number of pixel updates. */
+ * int64 for LG_ACCUM_FIXED64, float for LG_ACCUM_F32).  Canvas sides, accumulation mode
+ * and blend state follow lg_params' rules (LG_ERR_INVALID_ARGUMENT / LG_ERR_UNSUPPORTED).
+ * Binning scratch lives in one 32 MiB array per device, resident until the process exits;
+ * limits per call: at most 4096 tiles of 32x32 pixels (e.g. 2048x2048) and 8,000,000
+ * (segment, tile) pairs, else LG_ERR_BUDGET (and the image is not valid; the next call
+ * starts afresh).  The first call on a device sets the array up; make it before any
+ * stream capture.  Calls share the array, so calls that overlap on the GPU race:
+ * serialise them.  Every call reads two counters back and waits for its stream before
+ * returning; *pixels_out (optional) receives the number of pixel updates. */
 lg_status lg_accumulate_segments_noalloc(const lg_segment* segments, uint64_t n, const lg_params* params,
                                          void* accum, void* stream, uint64_t* pixels_out);
 

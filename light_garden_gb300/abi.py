@@ -109,10 +109,10 @@ class lg_trace_stats(C.Structure):
 class lg_device_opts(C.Structure):
     _fields_ = [("device", C.c_int32), ("raster_variant", C.c_int32), ("segment_capacity", C.c_uint64),
                 ("queue_capacity", C.c_uint64), ("stream_segments", C.c_uint64), ("culling", C.c_int32),
-                ("grid_density", C.c_float)]
+                ("grid_density", C.c_float), ("wait_polls", C.c_int32), ("_pad", C.c_int32)]
 
 
-LG_ABI_VERSION = 2  # include/lg.h
+LG_ABI_VERSION = 3  # include/lg.h
 LG_CULL_AUTO, LG_CULL_OFF, LG_CULL_ON = 0, 1, 2
 LG_CULL_AUTO_MIN = 96
 

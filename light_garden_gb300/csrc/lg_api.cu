@@ -513,6 +513,7 @@ SceneDev scene_dev(lg_ctx* c) {
   S.grids = (const GridRec*)c->d_grids.p;
   S.cell_start = (const uint32_t*)c->d_cell_start.p;
   S.cell_obj = (const uint16_t*)c->d_cell_obj.p;
+  S.wait_polls = c->wait_polls;
   return S;
 }
 
@@ -871,6 +872,7 @@ lg_status lg_create(lg_ctx** out, const lg_device_opts* opts) {
   }
   c->culling = opts ? opts->culling : LG_CULL_AUTO;
   c->grid_density = opts ? opts->grid_density : 0.0f;
+  if (opts && opts->wait_polls) c->wait_polls = opts->wait_polls < 0 ? 0 : opts->wait_polls;
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, c->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);

@@ -75,6 +75,7 @@ struct lg_ctx {
   DevBuf d_grids, d_cell_start, d_cell_obj;
   int culling = LG_CULL_AUTO;
   float grid_density = 0.0f;
+  int32_t wait_polls = 1 << 22;  // bounded device waits (lg_device_opts.wait_polls)
   bool culled = false;  // the uploaded scene (or some scene of the batch) has a grid
   uint64_t total_px = 0;
   uint32_t total_bins = 0;

@@ -216,6 +216,8 @@ struct SceneDev {
   const GridRec* grids;
   const uint32_t* cell_start;
   const uint16_t* cell_obj;
+  // polls of a bounded device wait before it gives up (lg_device_opts.wait_polls; < 0: at once)
+  int32_t wait_polls;
 };
 
 // First / last cell (unclamped, as a float) of [c - R - margin, c + R + margin] on one

@@ -19,7 +19,7 @@
 #include <cstring>
 #include <mutex>
 
-#include "lg_kernels.cuh"
+#include "lg_host.hpp"
 
 using namespace lgd;
 
@@ -67,25 +67,6 @@ __global__ void k_noalloc_init(Counters* ctr, unsigned long long n_segments) {
   if (threadIdx.x == 0) ctr->seg_count = n_segments;
 }
 
-bool blend_ok(const lg_blend_component& b) {
-  if (b.op == LG_BO_MIN || b.op == LG_BO_MAX) return b.src_factor == LG_BF_ONE && b.dst_factor == LG_BF_ONE;
-  if (b.op != LG_BO_ADD && b.op != LG_BO_REVERSE_SUBTRACT) return false;
-  if (b.dst_factor != LG_BF_ONE) return false;
-  switch (b.src_factor) {
-    case LG_BF_ZERO: case LG_BF_ONE: case LG_BF_SRC: case LG_BF_ONE_MINUS_SRC: case LG_BF_SRC_ALPHA:
-    case LG_BF_ONE_MINUS_SRC_ALPHA: case LG_BF_CONSTANT: case LG_BF_ONE_MINUS_CONSTANT: return true;
-    default: return false;
-  }
-}
-
-int mode_of(const lg_params& p) {
-  if (p.accum == LG_ACCUM_F32) return RM_F32_;
-  if (p.color_blend.op == LG_BO_MIN || p.color_blend.op == LG_BO_MAX || p.alpha_blend.op == LG_BO_MIN ||
-      p.alpha_blend.op == LG_BO_MAX)
-    return RM_FIXED_MINMAX_;
-  return RM_FIXED_SPLIT_;
-}
-
 // once per device, with that device current
 lg_status setup_device(int dev, DeviceSetup*& out) {
   if (dev < 0 || dev >= MAX_DEVICES) return LG_ERR_UNSUPPORTED;
@@ -128,9 +109,11 @@ extern "C" lg_status lg_accumulate_segments_noalloc(const lg_segment* segments, 
                                                     void* accum, void* stream, uint64_t* pixels_out) {
   if (!params || !accum || (n && !segments)) return LG_ERR_INVALID_ARGUMENT;
   const lg_params& p = *params;
-  if (p.width == 0 || p.height == 0 || (p.accum != LG_ACCUM_FIXED64 && p.accum != LG_ACCUM_F32))
+  // the same canvas, accumulation and blend rules as a context's lg_params
+  if (p.width == 0 || p.height == 0 || p.width > 32768 || p.height > 32768 ||
+      (p.accum != LG_ACCUM_FIXED64 && p.accum != LG_ACCUM_F32))
     return LG_ERR_INVALID_ARGUMENT;
-  if (!blend_ok(p.color_blend) || !blend_ok(p.alpha_blend)) return LG_ERR_UNSUPPORTED;
+  if (!lgh::blend_supported(p.color_blend) || !lgh::blend_supported(p.alpha_blend)) return LG_ERR_UNSUPPORTED;
   const uint32_t ntx = (p.width + TILE - 1) / TILE, nty = (p.height + TILE - 1) / TILE;
   if ((uint64_t)ntx * nty > NOALLOC_MAX_TILES || n > 0xffffffffull) return LG_ERR_BUDGET;
   int dev = 0;
@@ -174,7 +157,7 @@ extern "C" lg_status lg_accumulate_segments_noalloc(const lg_segment* segments, 
   const uint32_t bins = A.n_tiles;
   const int smem_tiles = bins <= MAX_SMEM_TILES ? 1 : 0;
   const size_t bsm = smem_tiles ? (size_t)bins * 4 : 0;
-  const int mode = mode_of(p);
+  const int mode = lgh::raster_mode(p);
   const size_t rsm = (size_t)raster_smem_bytes(mode);
   // the previous call's contents stay in the array: counters and tile counts restart at 0
   k_noalloc_init<<<1, 256, 0, s>>>(A.ctr, (unsigned long long)n);

@@ -64,7 +64,8 @@ __device__ const ObjScan* stage_objects(const SceneDev& S, ObjScan* sobj, uint64
   }
   __syncthreads();  // barrier initialised before anyone waits on it
   bool done = false;
-  for (int it = 0; it < (1 << 22) && !done; ++it) {
+  const int polls = S.wait_polls;
+  for (int it = 0; it < polls && !done; ++it) {
     done = mbar_try_wait(bar, 0);
     if (!done && it > 64) __nanosleep(64);
   }

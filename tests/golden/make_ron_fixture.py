@@ -1,7 +1,7 @@
 """Writes tests/golden/default_scene.ron and default_scene.npz from the reference's
 shipped scene file.
 
-    python tests/golden/make_ron_fixture.py [path/to/default.ron]
+    python tests/golden/make_ron_fixture.py path/to/default.ron
 
 The reference ships one scene, ``default.ron`` (loaded by Tracer::load, tracer.rs:190-204).
 This script parses it with light_garden_gb300.ron, writes it back in the same format
@@ -25,7 +25,6 @@ from light_garden_gb300 import abi, ron  # noqa: E402
 from light_garden_gb300.scene import pack  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
-SRC = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference/default.ron")
 STRIDE = 7
 W, H = 1024, 768
 
@@ -37,7 +36,9 @@ def params():
 
 
 def main():
-    objects, lights = ron.load(SRC)
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: make_ron_fixture.py path/to/default.ron (the reference checkout's scene file)")
+    objects, lights = ron.load(Path(sys.argv[1]))
     text = ron.dumps(objects, lights)
     (HERE / "default_scene.ron").write_text(text)
     pk = pack(objects, lights, params())

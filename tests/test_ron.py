@@ -1,6 +1,7 @@
 """Scene files in the reference's RON format (light_garden_gb300.ron): the parser, the
 mapping onto the scene model, the writer, and the shipped default scene."""
 import math
+import os
 from pathlib import Path
 
 import numpy as np
@@ -11,7 +12,8 @@ from light_garden_gb300 import scene as S
 from light_garden_gb300.tracer import Tracer
 
 GOLD = Path(__file__).resolve().parent / "golden"
-REFERENCE_SCENE = Path("/root/reference/default.ron")
+# the reference checkout's own default.ron, when LG_REFERENCE_SCENE names it (optional)
+REFERENCE_SCENE = Path(os.environ["LG_REFERENCE_SCENE"]) if os.environ.get("LG_REFERENCE_SCENE") else None
 
 
 def test_parser_values():
@@ -103,7 +105,7 @@ def test_default_scene_fixture():
     assert [type(l).__name__ for l in lights] == ["PointLight", "SpotLight"]
     assert objs[0].material_opt.refractive_index == 1.05 and objs[2].material_opt.refractive_index == 1.73
     assert lights[0].num_rays == 10000 and lights[1].num_rays == 2000
-    if REFERENCE_SCENE.exists():  # the fixture is the reference's file, parsed and written back
+    if REFERENCE_SCENE is not None and REFERENCE_SCENE.exists():  # the fixture is the reference's file, parsed and written back
         o_ref, l_ref = ron.load(REFERENCE_SCENE)
         assert o_ref == objs and l_ref == lights
 

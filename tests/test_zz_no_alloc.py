@@ -5,7 +5,9 @@ whose host owns every allocation, real-time loops that must avoid the allocator,
 memory budgets): it keeps its binning scratch in a fixed device array shared by all calls.
 This checks, through the C ABI, that two calls in a row (the second reusing the array the
 first left behind) each produce exactly the fixed-point image lg_accumulate_segments makes
-from the same segments, and that a canvas over the array's limit is refused.
+from the same segments, in the additive, min/max and FP32 raster modes; that a canvas over
+the array's limit is refused; and that a call with more (segment, tile) pairs than the
+array holds returns LG_ERR_BUDGET and leaves the array fit for the next call.
 """
 import ctypes as C
 
@@ -17,32 +19,103 @@ from light_garden_gb300 import abi, workloads as W
 pytestmark = pytest.mark.gpu
 
 
-def test_noalloc_matches_context_path_twice(gpu):
-    import torch
+def _mid_segments():
     from light_garden_gb300.runtime import Context
 
-    lib = abi.load()
     pk = W.mid_scene(rays_per_light=1 << 11).packed()
     with Context() as ctx:
         ctx.upload(pk)
         ctx.trace()
         segs = ctx.segments()
+    assert len(segs) > 1000
+    return pk, segs
+
+
+def _context_image(params, segs):
+    """lg_accumulate_segments of a context: the image the allocation-free call must match."""
+    from light_garden_gb300.runtime import Context
+
+    pk = W.plain_small().packed()
+    pk.params = params
+    with Context() as ctx:
+        ctx.upload(pk)
         ctx.accumulate_segments(segs)
-        ref = ctx.accum()
-    assert len(segs) > 1000 and ref.dtype == np.int64
-    h, w = pk.params.height, pk.params.width
-    d_segs = torch.from_numpy(segs.view(np.uint8).copy()).cuda()
+        return ctx.accum()
+
+
+def _noalloc(lib, params, d_segs, n, d_acc):
+    import torch
+
+    px = C.c_uint64(0)
     stream = torch.cuda.current_stream().cuda_stream
+    st = lib.lg_accumulate_segments_noalloc(C.c_void_p(d_segs.data_ptr()) if n else None, n, C.byref(params),
+                                            C.c_void_p(d_acc.data_ptr()), C.c_void_p(stream), C.byref(px))
+    torch.cuda.synchronize()
+    return st, px.value
+
+
+def _blend(mode):
+    """params of one of the raster modes the entry point dispatches to"""
+    p = abi.params_default()
+    if mode == "f32":
+        p.accum = abi.LG_ACCUM_F32
+    elif mode == "minmax":
+        p.color_blend.src_factor, p.color_blend.dst_factor, p.color_blend.op = abi.LG_BF_ONE, abi.LG_BF_ONE, abi.LG_BO_MAX
+        p.alpha_blend.src_factor, p.alpha_blend.dst_factor, p.alpha_blend.op = abi.LG_BF_ONE, abi.LG_BF_ONE, abi.LG_BO_MIN
+    return p
+
+
+@pytest.mark.parametrize("mode", ["add", "minmax", "f32"])
+def test_noalloc_matches_context_path_twice(gpu, mode):
+    import torch
+
+    lib = abi.load()
+    pk, segs = _mid_segments()
+    p = _blend(mode)
+    p.width, p.height = pk.params.width, pk.params.height
+    ref = _context_image(p, segs)
+    h, w = p.height, p.width
+    d_segs = torch.from_numpy(segs.view(np.uint8).copy()).cuda()
+    dt = torch.float32 if mode == "f32" else torch.int64
     for call in range(2):
-        d_acc = torch.full((h * w * 4,), 12345, dtype=torch.int64, device="cuda")  # stale contents
-        px = C.c_uint64(0)
-        st = lib.lg_accumulate_segments_noalloc(C.c_void_p(d_segs.data_ptr()), len(segs), C.byref(pk.params),
-                                                C.c_void_p(d_acc.data_ptr()), C.c_void_p(stream), C.byref(px))
+        d_acc = torch.full((h * w * 4,), 12345, dtype=dt, device="cuda")  # stale contents
+        st, px = _noalloc(lib, p, d_segs, len(segs), d_acc)
         assert st == abi.LG_OK, (call, abi.STATUS_NAMES.get(st, st))
-        torch.cuda.synchronize()
         got = d_acc.cpu().numpy().reshape(h, w, 4)
-        assert np.array_equal(got, ref), f"call {call} differs from lg_accumulate_segments"
-        assert px.value > 0
+        if mode == "f32":
+            # FP32 atomics add in no fixed order: equal within a few f32 roundings per pixel
+            assert np.allclose(got, ref, rtol=1e-5, atol=1e-6), f"call {call} differs from lg_accumulate_segments"
+        else:
+            assert np.array_equal(got, ref), f"call {call} differs from lg_accumulate_segments"
+        assert px > 0
+
+
+def test_noalloc_budget_overflow_then_recovers(gpu):
+    """Diagonals across a 2048x2048 canvas cross ~127 tiles each: 70,000 of them need about
+    8.9 M (segment, tile) pairs, more than the array holds (8,000,000)."""
+    import torch
+
+    lib = abi.load()
+    rng = np.random.default_rng(5)
+    n = 70000
+    big = np.zeros(n, dtype=abi.segment_dtype())
+    j = rng.uniform(-0.02, 0.02, (n, 2)).astype(np.float32)
+    big["x0"], big["y0"] = -0.99 + j[:, 0], -0.99 + j[:, 1]
+    big["x1"], big["y1"] = 0.99 - j[:, 1], 0.99 - j[:, 0]
+    big["color"] = np.float32(0.25)
+    p = abi.params_default()
+    p.width, p.height = 2048, 2048
+    d_big = torch.from_numpy(big.view(np.uint8).copy()).cuda()
+    d_acc = torch.zeros(2048 * 2048 * 4, dtype=torch.int64, device="cuda")
+    st, _ = _noalloc(lib, p, d_big, n, d_acc)
+    assert st == abi.LG_ERR_BUDGET, abi.STATUS_NAMES.get(st, st)
+    # the next call starts from a clean array: a small frame matches the context path again
+    small = big[:500]
+    ref = _context_image(p, small)
+    d_small = torch.from_numpy(small.view(np.uint8).copy()).cuda()
+    st, _ = _noalloc(lib, p, d_small, len(small), d_acc)
+    assert st == abi.LG_OK
+    assert np.array_equal(d_acc.cpu().numpy().reshape(2048, 2048, 4), ref)
 
 
 def test_noalloc_refuses_canvas_over_limit(gpu):
@@ -54,3 +127,7 @@ def test_noalloc_refuses_canvas_over_limit(gpu):
     d_acc = torch.empty(16, dtype=torch.int64, device="cuda")
     st = lib.lg_accumulate_segments_noalloc(None, 0, C.byref(p), C.c_void_p(d_acc.data_ptr()), None, None)
     assert st == abi.LG_ERR_BUDGET
+    # within the tile limit but wider than a context accepts (32768 pixels per side)
+    p.width, p.height = 131072, 32
+    st = lib.lg_accumulate_segments_noalloc(None, 0, C.byref(p), C.c_void_p(d_acc.data_ptr()), None, None)
+    assert st == abi.LG_ERR_INVALID_ARGUMENT
