@@ -33,6 +33,7 @@ METRIC = "traced segments/s + accumulated px/s on 1 GB300; p50/p99 scene latency
 # quarter-size mid scene (a scaled constant, not a live measurement)
 RASTER_DRAM_BYTES_PER_PIXEL = 3.43
 CULL = {"auto": 0, "off": 1, "on": 2}  # lg_culling
+PRECISION = {"exact": 0, "fast": 1}  # lg_precision
 
 WORKLOAD = ("mid_scene: 64 objects (rect/circle/mirror/curved mirror, seed 2), 8 lights x 2^18 rays, "
             "16 bounces, 1920x1080, int64 Q31.32 accumulation, RGBA16F resolve")
@@ -192,6 +193,7 @@ def run_ours(args, ws, rank, local):
     dev = torch.device("cuda", local)
     w = W.mid_scene(rays_per_light=args.rays_per_light)
     pk = w.packed()
+    pk.params.precision = PRECISION[args.precision]
     Wd, Hd = pk.params.width, pk.params.height
     ctx = Context(device=local, raster_variant=args.raster_variant, culling=CULL[args.culling], grid_density=args.grid_density)
     ctx.upload(pk)
@@ -395,6 +397,7 @@ def run_csg(args, ws, rank, local):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     pk = W.csg_scene(total_rays=max(8, int(round((1 << 22) * args.ray_scale)))).packed()
+    pk.params.precision = PRECISION[args.precision]
     Wd, Hd = pk.params.width, pk.params.height
     ctx = Context(device=local, raster_variant=args.raster_variant, culling=CULL[args.culling], grid_density=args.grid_density)
     ctx.upload(pk)
@@ -548,6 +551,8 @@ def main():
     ap.add_argument("--culling", default="auto", choices=sorted(CULL),
                     help="nearest-hit culling grid: auto (scenes of 96+ objects), off, on")
     ap.add_argument("--grid-density", type=float, default=0.0, help="culling grid cells per object (0: 2)")
+    ap.add_argument("--precision", default="exact", choices=sorted(PRECISION),
+                    help="exact: FP64 bit-for-bit with the FP64 formulas; fast: double-float refinement")
     ap.add_argument("--rate", type=float, default=1000.0, help="serve: Poisson arrival rate (requests/s)")
     ap.add_argument("--budget-gb", type=float, default=120.0, help="serve: HBM budget")
     ap.add_argument("--batch-scenes", type=int, default=512)

@@ -41,7 +41,8 @@ extern "C" {
 
 /* 2: lg_device_opts gained culling and grid_density, lg_trace_stats bound_tests and
  * object_tests (both structs grew).
- * 3: lg_device_opts gained wait_polls. */
+ * 3: lg_device_opts gained wait_polls; lg_params.precision (was padding), ray_stride and
+ *    ray_offset (lg_params grew). */
 #define LG_ABI_VERSION 3
 
 typedef enum lg_status {
@@ -158,6 +159,17 @@ typedef struct lg_string_mod {
   float color[4];
 } lg_string_mod;
 
+/* ---- trace precision ----------------------------------------------------------------- *
+ * EXACT: every hit, membership test and bounce is evaluated in IEEE-754 double with each
+ * operation rounded on its own (no fused multiply-add), in the order of the restated
+ * collision2d formulas, so the trace equals the FP64 CPU trace of the same formulas bit for
+ * bit; an FP32 search only prunes the candidates.  Geometry trees may hold up to 8 levels
+ * of Logic nodes.
+ * FAST: the hit and the bounce are refined in double-float (~2^-47 relative) on the FP32
+ * pipe; decisions within the rounding of the ray's own error bound are flagged
+ * LG_PATH_NEAR_DEGENERATE and may differ from an FP64 trace. */
+enum lg_precision { LG_PRECISION_EXACT = 0, LG_PRECISION_FAST = 1 };
+
 /* ---- per-scene parameters ------------------------------------------------------------- */
 typedef struct lg_params {
   uint32_t max_bounce;          /* Tracer::max_bounce (default 5, GUI 1..=20); here 1..=64 */
@@ -170,8 +182,12 @@ typedef struct lg_params {
   int32_t accum;                /* enum lg_accum_mode */
   int32_t emit_control_lines;   /* append curved-mirror control polygons (tracer.rs:341-346) */
   int32_t record_paths;         /* also write one lg_path_record per segment (parity tooling) */
-  int32_t _pad;
+  int32_t precision;            /* enum lg_precision of the trace */
   lg_string_mod string_mod;     /* overlay segments, drawn with the same raster */
+  uint32_t ray_stride;          /* trace only the primaries i = ray_offset + k * ray_stride of each
+                                   light (0 or 1: all), as a sampled frame; the overlays are drawn
+                                   only when ray_offset == 0.  One scene only (not batches/serving) */
+  uint32_t ray_offset;
 } lg_params;
 
 /* Fills *p with the reference defaults (tracer.rs:37-39, mod.rs:57-73). */

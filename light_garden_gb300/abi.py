@@ -79,8 +79,8 @@ class lg_params(C.Structure):
                 ("blend_constant", C.c_float * 4),
                 ("color_blend", lg_blend_component), ("alpha_blend", lg_blend_component),
                 ("accum", C.c_int32), ("emit_control_lines", C.c_int32),
-                ("record_paths", C.c_int32), ("_pad", C.c_int32),
-                ("string_mod", lg_string_mod)]
+                ("record_paths", C.c_int32), ("precision", C.c_int32),
+                ("string_mod", lg_string_mod), ("ray_stride", C.c_uint32), ("ray_offset", C.c_uint32)]
 
 
 class lg_segment(C.Structure):
@@ -114,6 +114,7 @@ class lg_device_opts(C.Structure):
 
 LG_ABI_VERSION = 3  # include/lg.h
 LG_CULL_AUTO, LG_CULL_OFF, LG_CULL_ON = 0, 1, 2
+LG_PRECISION_EXACT, LG_PRECISION_FAST = 0, 1
 LG_CULL_AUTO_MIN = 96
 
 
@@ -143,7 +144,9 @@ def params_default() -> lg_params:
     p.accum = LG_ACCUM_FIXED64
     p.emit_control_lines = 1
     p.record_paths = 0
+    p.precision = LG_PRECISION_EXACT
     p.string_mod = lg_string_mod()
+    p.ray_stride, p.ray_offset = 1, 0
     return p
 
 

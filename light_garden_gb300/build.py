@@ -17,8 +17,9 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 LIB_DIR = PKG / "_lib"
 OBJ_DIR = PKG / "_build"
-SOURCES = ["lg_api.cu", "lg_trace.cu", "lg_raster.cu", "lg_noalloc.cu", "lg_batch.cu", "lg_serve.cu"]
-HEADERS = ["lg_device.cuh", "lg_kernels.cuh", "lg_df.cuh", "lg_host.hpp", "lg_ctx.hpp"]
+SOURCES = ["lg_api.cu", "lg_trace.cu", "lg_exact.cu", "lg_raster.cu", "lg_noalloc.cu", "lg_batch.cu", "lg_serve.cu"]
+HEADERS = ["lg_device.cuh", "lg_kernels.cuh", "lg_df.cuh", "lg_x64.cuh", "lg_trace_common.cuh", "lg_host.hpp",
+           "lg_ctx.hpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xptxas", "-warn-spills"]

@@ -263,8 +263,41 @@ bool blend_supported(const lg_blend_component& b) {
   }
 }
 
+// Exact mode: the tree under node gi in preorder (indices relative to the object's first
+// node), with each leaf's number in the flattened leaf table (flatten_node's order: child a
+// before child b, a polygon's edges one by one).
+void xtree(const lg_geo* G, int32_t gi, int depth, int parent, int side, std::vector<lgx::XNode>& out,
+           uint32_t& leaf_ord, int& max_depth) {
+  const lg_geo& g = G[gi];
+  lgx::XNode n;
+  std::memset(&n, 0, sizeof n);
+  n.geo = gi;
+  n.parent = (int16_t)parent;
+  n.depth = (uint8_t)std::min(depth, 255);
+  n.side = (uint8_t)side;
+  n.leaf_ord = leaf_ord;
+  const int idx = (int)out.size();
+  out.push_back(n);
+  max_depth = std::max(max_depth, depth);
+  if (g.kind == LG_GEO_LOGIC) {
+    xtree(G, g.a, depth + 1, idx, 0, out, leaf_ord, max_depth);
+    xtree(G, g.b, depth + 1, idx, 1, out, leaf_ord, max_depth);
+  } else {
+    leaf_ord += g.kind == LG_GEO_POLYGON ? (uint32_t)g.a : 1u;
+  }
+  out[idx].end = (int32_t)out.size();
+}
+
+lg_status validate_exact(std::string& err, const lg_params& p, const Flat& F) {
+  if (p.precision != LG_PRECISION_EXACT) return LG_OK;
+  if (F.xdepth > lgx::MAX_DEPTH)
+    return set_err(err, LG_ERR_UNSUPPORTED, "exact precision: geometry trees deeper than 8 Logic levels");
+  return LG_OK;
+}
+
 lg_status flatten_scene(std::string& err, const lg_geo* G, uint32_t n_geo, const lg_object* O, uint32_t n_obj,
                         const lg_light* Ls, uint32_t n_lights, Flat& F) {
+  F.xgeo.assign(G, G + n_geo);
   for (uint32_t k = 0; k < n_obj; ++k) {
     const lg_object& o = O[k];
     if (o.kind < 0 || o.kind > LG_OBJ_GEO) return set_err(err, LG_ERR_INVALID_ARGUMENT, "object " + std::to_string(k) + ": unknown kind");
@@ -293,6 +326,16 @@ lg_status flatten_scene(std::string& err, const lg_geo* G, uint32_t n_geo, const
     oi.flags = (o.has_material ? INFO_MATERIAL : 0u) |
                ((o.kind == LG_OBJ_STRAIGHT_MIRROR || o.kind == LG_OBJ_CURVED_MIRROR) ? INFO_NO_CONTAINS : 0u);
     oi.n = DF(o.has_material ? o.refractive_index : 1.0);
+    oi.n64 = o.has_material ? o.refractive_index : 1.0;
+    oi.xnode_begin = (uint32_t)F.xnode.size();
+    {
+      std::vector<lgx::XNode> nodes;
+      uint32_t ord = 0;
+      xtree(G, o.geo, 0, -1, 0, nodes, ord, F.xdepth);
+      if (nodes.size() > 32767) return set_err(err, LG_ERR_UNSUPPORTED, "object " + std::to_string(k) + ": tree too large");
+      oi.xnode_count = (uint32_t)nodes.size();
+      F.xnode.insert(F.xnode.end(), nodes.begin(), nodes.end());
+    }
     F.prog.insert(F.prog.end(), prog.begin(), prog.end());
     F.info.push_back(oi);
     if (o.kind == LG_OBJ_CURVED_MIRROR) F.cubics.push_back(k);
@@ -430,7 +473,23 @@ lg_status validate_params(std::string& err, const lg_params& p) {
   if (p.string_mod.modulo && (p.string_mod.curve != 0 || p.string_mod.mode > LG_SM_BASE))
     return set_err(err, LG_ERR_UNSUPPORTED, "string mod: only Curve::Circle with Add/Mul/Pow/Base");
   if (p.string_mod.modulo > (1ull << 30)) return set_err(err, LG_ERR_INVALID_ARGUMENT, "string mod modulo too large");
+  if (p.precision != LG_PRECISION_EXACT && p.precision != LG_PRECISION_FAST)
+    return set_err(err, LG_ERR_INVALID_ARGUMENT, "unknown precision");
+  if (p.ray_stride > 1 && p.ray_offset >= p.ray_stride)
+    return set_err(err, LG_ERR_INVALID_ARGUMENT, "ray_offset must be below ray_stride");
   return LG_OK;
+}
+
+// Overlay segments of the context's frame (none in a sampled frame with ray_offset != 0).
+uint64_t overlay_segments(const lg_ctx* c) {
+  if (c->prm.ray_stride > 1 && c->prm.ray_offset != 0) return 0;
+  return 3ull * c->n_cubic * (c->prm.emit_control_lines ? 1 : 0) + c->prm.string_mod.modulo;
+}
+
+// Primaries of a light with num_rays rays that a sampled frame traces.
+uint64_t sampled_rays(uint64_t num_rays, const lg_params& p) {
+  if (p.ray_stride <= 1) return num_rays;
+  return num_rays > p.ray_offset ? (num_rays - p.ray_offset + p.ray_stride - 1) / p.ray_stride : 0;
 }
 
 int raster_mode(const lg_params& p) {
@@ -514,6 +573,11 @@ SceneDev scene_dev(lg_ctx* c) {
   S.cell_start = (const uint32_t*)c->d_cell_start.p;
   S.cell_obj = (const uint16_t*)c->d_cell_obj.p;
   S.wait_polls = c->wait_polls;
+  S.xgeo = (const lg_geo*)c->d_xgeo.p;
+  S.xnode = (const lgx::XNode*)c->d_xnode.p;
+  S.aspect64 = c->aspect;
+  S.ray_stride = c->prm.ray_stride > 1 ? c->prm.ray_stride : 1u;
+  S.ray_offset = c->prm.ray_stride > 1 ? c->prm.ray_offset : 0u;
   return S;
 }
 
@@ -631,29 +695,88 @@ lg_status ensure_raster_buffers(lg_ctx* c) {
   return LG_OK;
 }
 
-TraceKernel scan_kernel(bool multi, bool culled) {
-  if (multi) return culled ? k_scan<true, true> : k_scan<true, false>;
-  return culled ? k_scan<false, true> : k_scan<false, false>;
+TraceKernel scan_kernel(bool multi, bool culled, bool exact) {
+  if (exact) {
+    if (multi) return culled ? k_scan<true, true, true> : k_scan<true, false, true>;
+    return culled ? k_scan<false, true, true> : k_scan<false, false, true>;
+  }
+  if (multi) return culled ? k_scan<true, true, false> : k_scan<true, false, false>;
+  return culled ? k_scan<false, true, false> : k_scan<false, false, false>;
 }
 TraceKernel bounce_kernel(bool multi, bool culled) {
   if (multi) return culled ? k_bounce<true, true> : k_bounce<true, false>;
   return culled ? k_bounce<false, true> : k_bounce<false, false>;
+}
+TraceKernel3 bounce_x_kernel(bool multi, bool culled) {
+  if (multi) return culled ? k_bounce_x<true, true> : k_bounce_x<true, false>;
+  return culled ? k_bounce_x<false, true> : k_bounce_x<false, false>;
+}
+
+lg_status trace_grids(lg_ctx* c, bool multi, size_t tsm) {
+  int occ = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, multi ? k_refine<true> : k_refine<false>, 256, 0), "occupancy");
+  c->trace_grid[1] = c->n_sm * std::max(1, occ);
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, multi ? k_full<true> : k_full<false>, 256, tsm), "occupancy");
+  c->trace_grid[2] = c->n_sm * std::max(1, occ);
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bounce_kernel(multi, c->culled), 256, tsm), "occupancy");
+  c->trace_grid[3] = c->n_sm * std::max(1, occ);
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, multi ? k_solve_x<true> : k_solve_x<false>, 256, 0), "occupancy");
+  c->trace_grid[4] = c->n_sm * std::max(1, occ);
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bounce_x_kernel(multi, c->culled), 256, 0), "occupancy");
+  c->trace_grid[5] = c->n_sm * std::max(1, occ);
+  return LG_OK;
+}
+
+void launch_light_setup(lg_ctx* c, const SceneDev& S, bool multi, int blocks) {
+  if (c->prm.precision == LG_PRECISION_EXACT) {
+    if (multi) k_light_setup_x<true><<<blocks, 256, 0, c->stream>>>(S);
+    else k_light_setup_x<false><<<blocks, 256, 0, c->stream>>>(S);
+  } else {
+    if (multi) k_light_setup<true><<<blocks, 256, 0, c->stream>>>(S);
+    else k_light_setup<false><<<blocks, 256, 0, c->stream>>>(S);
+  }
+}
+
+void launch_generation(lg_ctx* c, const SceneDev& S, const TraceBufs& B, uint32_t g, bool multi, int scan_grid,
+                       size_t scan_smem, size_t tsm, int smem_fits) {
+  const bool exact = c->prm.precision == LG_PRECISION_EXACT;
+  scan_kernel(multi, c->culled, exact)<<<scan_grid, SCAN_THREADS, scan_smem, c->stream>>>(S, B, g, smem_fits);
+  if (exact) {
+    if (multi) k_solve_x<true><<<c->trace_grid[4], 256, 0, c->stream>>>(S, B, g);
+    else k_solve_x<false><<<c->trace_grid[4], 256, 0, c->stream>>>(S, B, g);
+    bounce_x_kernel(multi, c->culled)<<<c->trace_grid[5], 256, 0, c->stream>>>(S, B, g);
+  } else {
+    if (multi) {
+      k_refine<true><<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g);
+      k_full<true><<<c->trace_grid[2], 256, tsm, c->stream>>>(S, B, g, smem_fits);
+    } else {
+      k_refine<false><<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g);
+      k_full<false><<<c->trace_grid[2], 256, tsm, c->stream>>>(S, B, g, smem_fits);
+    }
+    bounce_kernel(multi, c->culled)<<<c->trace_grid[3], 256, tsm, c->stream>>>(S, B, g, smem_fits);
+  }
+}
+
+lg_status upload_exact(lg_ctx* c, const Flat& F) {
+  lg_status st;
+  if ((st = ensure(c, c->d_xgeo, F.xgeo.size() * sizeof(lg_geo) + 16, "scene"))) return st;
+  if ((st = ensure(c, c->d_xnode, F.xnode.size() * sizeof(lgx::XNode) + 16, "scene"))) return st;
+  if (!F.xgeo.empty())
+    CK(cudaMemcpyAsync(c->d_xgeo.p, F.xgeo.data(), F.xgeo.size() * sizeof(lg_geo), cudaMemcpyHostToDevice, c->stream), "upload");
+  if (!F.xnode.empty())
+    CK(cudaMemcpyAsync(c->d_xnode.p, F.xnode.data(), F.xnode.size() * sizeof(lgx::XNode), cudaMemcpyHostToDevice, c->stream), "upload");
+  return LG_OK;
 }
 
 lg_status enqueue_trace(lg_ctx* c) {
   const SceneDev S = scene_dev(c);
   const TraceBufs B = trace_bufs(c);
   CK(cudaMemsetAsync(c->d_ctr.p, 0, sizeof(Counters), c->stream), "memset counters");
-  if (c->n_lights) k_light_setup<false><<<1, 256, 0, c->stream>>>(S);
+  if (c->n_lights) launch_light_setup(c, S, false, 1);
   const size_t tsm = c->smem_fits ? c->obj_smem : 0;
-  for (uint32_t g = 0; g < c->prm.max_bounce; ++g) {
-    scan_kernel(false, c->culled)<<<c->trace_grid[0], SCAN_THREADS, (size_t)scan_smem_bytes() + tsm, c->stream>>>(S, B, g,
-                                                                                                   c->smem_fits);
-    k_refine<false><<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g);
-    k_full<false><<<c->trace_grid[2], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
-    bounce_kernel(false, c->culled)<<<c->trace_grid[3], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
-  }
-  const uint64_t n_ov = 3ull * c->n_cubic * (c->prm.emit_control_lines ? 1 : 0) + c->prm.string_mod.modulo;
+  for (uint32_t g = 0; g < c->prm.max_bounce; ++g)
+    launch_generation(c, S, B, g, false, c->trace_grid[0], (size_t)scan_smem_bytes() + tsm, tsm, c->smem_fits);
+  const uint64_t n_ov = overlay_segments(c);
   if (n_ov) {
     const int blocks = (int)std::min<uint64_t>((n_ov + 255) / 256, 4096);
     k_overlay<<<blocks, 256, 0, c->stream>>>(S, B, (const uint32_t*)c->d_cubics.p, nullptr,
@@ -852,6 +975,8 @@ void lg_params_default(lg_params* p) {
   p->alpha_blend = {LG_BF_SRC_ALPHA, LG_BF_ONE, LG_BO_ADD}; // mod.rs:62-66
   p->accum = LG_ACCUM_FIXED64;
   p->emit_control_lines = 1;
+  p->precision = LG_PRECISION_EXACT;
+  p->ray_stride = 1;  // every primary
 }
 
 const char* lg_last_error(const lg_ctx* c) { return c ? c->err.c_str() : "null context"; }
@@ -879,13 +1004,15 @@ lg_status lg_create(lg_ctx** out, const lg_device_opts* opts) {
   if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_ctr, sizeof(Counters));
   if (e == cudaSuccess) e = cudaMalloc(&c->d_ctr.p, sizeof(Counters));
   for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
-  for (TraceKernel k : {k_scan<false, false>, k_scan<false, true>})
+  for (TraceKernel k : {k_scan<false, false, false>, k_scan<false, true, false>, k_scan<false, false, true>,
+                        k_scan<false, true, true>})
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, scan_smem_bytes() + (int)OBJ_SMEM_MAX);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_full<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
   for (TraceKernel k : {k_bounce<false, false>, k_bounce<false, true>})
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
-  for (TraceKernel k : {k_scan<true, false>, k_scan<true, true>})
+  for (TraceKernel k : {k_scan<true, false, false>, k_scan<true, true, false>, k_scan<true, false, true>,
+                        k_scan<true, true, true>})
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, scan_smem_bytes());
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_bin_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(MAX_SMEM_TILES * 4));
@@ -942,7 +1069,9 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
   Flat F;
   st = flatten_scene(c->err, geos, n_geo, objects, n_objects, lights, n_lights, F);
   if (st) return st;
+  if ((st = validate_exact(c->err, p, F))) return st;
   CK(cudaStreamSynchronize(c->stream), "synchronize");
+  if ((st = upload_exact(c, F))) return st;
   const bool same_shape = c->has_scene && c->n_obj == n_objects && c->n_leaves == F.leaves.size() &&
                           c->n_prog == F.prog.size() && c->n_lights == n_lights && c->n_cubic == F.cubics.size() &&
                           std::memcmp(&c->prm, &p, sizeof p) == 0;
@@ -958,6 +1087,13 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
   if (!F.info.empty()) CK(cudaMemcpyAsync(c->d_info.p, F.info.data(), F.info.size() * sizeof(ObjInfo), cudaMemcpyHostToDevice, c->stream), "upload");
   if (!dleaves.empty()) CK(cudaMemcpyAsync(c->d_leaves.p, dleaves.data(), dleaves.size() * sizeof(Leaf64), cudaMemcpyHostToDevice, c->stream), "upload");
   if (!F.prog.empty()) CK(cudaMemcpyAsync(c->d_prog.p, F.prog.data(), F.prog.size(), cudaMemcpyHostToDevice, c->stream), "upload");
+  if (p.ray_stride > 1) {  // a sampled frame numbers only the primaries it traces
+    uint64_t first = 0;
+    for (uint32_t l = 0; l < n_lights; ++l) {
+      F.lights[l].first = first;
+      first += sampled_rays(lights[l].num_rays, p);
+    }
+  }
   if (!F.lights.empty()) CK(cudaMemcpyAsync(c->d_lights.p, F.lights.data(), F.lights.size() * sizeof(LightDev), cudaMemcpyHostToDevice, c->stream), "upload");
   if (!F.cubics.empty()) CK(cudaMemcpyAsync(c->d_cubics.p, F.cubics.data(), F.cubics.size() * 4, cudaMemcpyHostToDevice, c->stream), "upload");
   build_grid(F.scan, c->culling, c->grid_density, F.grid);
@@ -980,7 +1116,7 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
   c->n_lights = n_lights;
   c->n_cubic = (uint32_t)F.cubics.size();
   c->n_primary = 0;
-  for (uint32_t l = 0; l < n_lights; ++l) c->n_primary += lights[l].num_rays;
+  for (uint32_t l = 0; l < n_lights; ++l) c->n_primary += sampled_rays(lights[l].num_rays, p);
   c->prm = p;
   c->aspect = (double)((float)p.width / (float)p.height);
   c->ntx = (p.width + TILE - 1) / TILE;
@@ -991,14 +1127,10 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
   c->smem_fits = c->obj_smem <= OBJ_SMEM_MAX ? 1 : 0;
   int occ = 0;
   const size_t tsm = c->smem_fits ? c->obj_smem : 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, scan_kernel(false, c->culled), SCAN_THREADS, (size_t)scan_smem_bytes() + tsm), "occupancy");
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, scan_kernel(false, c->culled, p.precision == LG_PRECISION_EXACT),
+                                                   SCAN_THREADS, (size_t)scan_smem_bytes() + tsm), "occupancy");
   c->trace_grid[0] = c->n_sm * std::max(1, occ);
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_refine<false>, 256, 0), "occupancy");
-  c->trace_grid[1] = c->n_sm * std::max(1, occ);
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_full<false>, 256, tsm), "occupancy");
-  c->trace_grid[2] = c->n_sm * std::max(1, occ);
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bounce_kernel(false, c->culled), 256, tsm), "occupancy");
-  c->trace_grid[3] = c->n_sm * std::max(1, occ);
+  if ((st = trace_grids(c, false, tsm))) return st;
   const int mode = raster_mode(p);
   const int rsm = raster_smem_bytes(mode);
   if (mode == RM_FIXED_SPLIT_) {
@@ -1131,7 +1263,7 @@ static lg_status enqueue_stream_frame(lg_ctx* c, uint16_t* dst, size_t row, cuda
   CK(cudaEventRecordWithFlags(ev[0], c->stream, cudaEventRecordExternal), "stage event");
   CK(cudaMemsetAsync(c->d_ctr.p, 0, sizeof(Counters), c->stream), "memset counters");
   k_clear_accum<<<c->n_sm * 8, 256, 0, c->stream>>>(A, fixed);
-  if (c->n_lights) k_light_setup<false><<<1, 256, 0, c->stream>>>(S);
+  if (c->n_lights) launch_light_setup(c, S, false, 1);
   const size_t tsm = c->smem_fits ? c->obj_smem : 0;
   const uint32_t bins = 2 * c->n_tiles;
   const int smem_tiles = bins <= MAX_SMEM_TILES ? 1 : 0;
@@ -1139,14 +1271,10 @@ static lg_status enqueue_stream_frame(lg_ctx* c, uint16_t* dst, size_t row, cuda
   const uint32_t n_part = (bins + TILE_SCAN_CHUNK - 1) / TILE_SCAN_CHUNK;
   const int mode = raster_mode(c->prm);
   const size_t rsm = (size_t)raster_smem_bytes(mode);
-  const uint64_t n_ov = 3ull * c->n_cubic * (c->prm.emit_control_lines ? 1 : 0) + c->prm.string_mod.modulo;
+  const uint64_t n_ov = overlay_segments(c);
   const uint32_t G = c->prm.max_bounce;
   for (uint32_t g = 0; g < G; ++g) {
-    scan_kernel(false, c->culled)<<<c->trace_grid[0], SCAN_THREADS, (size_t)scan_smem_bytes() + tsm, c->stream>>>(S, B, g,
-                                                                                                   c->smem_fits);
-    k_refine<false><<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g);
-    k_full<false><<<c->trace_grid[2], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
-    bounce_kernel(false, c->culled)<<<c->trace_grid[3], 256, tsm, c->stream>>>(S, B, g, c->smem_fits);
+    launch_generation(c, S, B, g, false, c->trace_grid[0], (size_t)scan_smem_bytes() + tsm, tsm, c->smem_fits);
     if (g == 0 && n_ov) {
       const int blocks = (int)std::min<uint64_t>((n_ov + 255) / 256, 4096);
       k_overlay<<<blocks, 256, 0, c->stream>>>(S, B, (const uint32_t*)c->d_cubics.p, nullptr,

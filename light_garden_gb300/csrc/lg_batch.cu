@@ -82,7 +82,7 @@ lg_status enqueue_batch(lg_ctx* c, cudaEvent_t* ev) {
   CK(cudaMemsetAsync(c->d_ctr.p, 0, sizeof(Counters), c->stream), "memset counters");
   CK(cudaMemsetAsync(c->d_scene_count.p, 0, (size_t)c->n_scenes * 4, c->stream), "memset scene counts");
   k_clear_accum<<<c->n_sm * 8, 256, 0, c->stream>>>(A, fixed);
-  if (c->n_lights) k_light_setup<true><<<(c->n_lights + 127) / 128, 128, 0, c->stream>>>(S);
+  if (c->n_lights) launch_light_setup(c, S, true, (int)((c->n_lights + 255) / 256));
   const uint32_t bins = c->total_bins;
   const int smem_tiles = bins <= MAX_SMEM_TILES ? 1 : 0;
   const size_t bsm = smem_tiles ? (size_t)bins * 4 : 0;
@@ -99,10 +99,7 @@ lg_status enqueue_batch(lg_ctx* c, cudaEvent_t* ev) {
       k_scene_scatter<<<c->n_sm * 8, 256, 0, c->stream>>>(S, B, g, (unsigned*)c->d_scene_off.p,
                                                           (uint32_t*)c->d_order.p);
     }
-    scan_kernel(true, c->culled)<<<c->batch_grid_scan, SCAN_THREADS, (size_t)scan_smem_bytes(), c->stream>>>(S, B, g, 0);
-    k_refine<true><<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g);
-    k_full<true><<<c->trace_grid[2], 256, 0, c->stream>>>(S, B, g, 0);
-    bounce_kernel(true, c->culled)<<<c->trace_grid[3], 256, 0, c->stream>>>(S, B, g, 0);
+    launch_generation(c, S, B, g, true, c->batch_grid_scan, (size_t)scan_smem_bytes(), 0, 0);
     if (g == 0 && c->n_cubic) {
       const int blocks = (int)std::min<uint64_t>((3ull * c->n_cubic + 255) / 256, 4096);
       k_overlay<<<blocks, 256, 0, c->stream>>>(S, B, (const uint32_t*)c->d_cubics.p,
@@ -224,17 +221,22 @@ lg_status lg_batch_upload(lg_ctx* c, const lg_scene_desc* scenes, uint32_t k) {
     if (p.accum != p0->accum || std::memcmp(&p.color_blend, &p0->color_blend, sizeof p.color_blend) ||
         std::memcmp(&p.alpha_blend, &p0->alpha_blend, sizeof p.alpha_blend) ||
         std::memcmp(p.clear_color, p0->clear_color, sizeof p.clear_color) ||
-        std::memcmp(p.blend_constant, p0->blend_constant, sizeof p.blend_constant))
-      return fail(c, LG_ERR_UNSUPPORTED, where + "the scenes of a batch must share accum mode, blend state and clear colour");
+        std::memcmp(p.blend_constant, p0->blend_constant, sizeof p.blend_constant) || p.precision != p0->precision)
+      return fail(c, LG_ERR_UNSUPPORTED,
+                  where + "the scenes of a batch must share accum mode, precision, blend state and clear colour");
     if (p.string_mod.modulo) return fail(c, LG_ERR_UNSUPPORTED, where + "the string-mod overlay is not supported in batches");
+    if (p.ray_stride > 1) return fail(c, LG_ERR_UNSUPPORTED, where + "sampled frames (ray_stride) are one-scene only");
     if (d.n_objects > 65535) return fail(c, LG_ERR_UNSUPPORTED, where + "at most 65535 objects");
     Flat Fs;
     st = flatten_scene(c->err, d.geos, d.n_geo, d.objects, d.n_objects, d.lights, d.n_lights, Fs);
+    if (!st) st = validate_exact(c->err, p, Fs);
     if (st) { c->err = where + c->err; return st; }
     const uint32_t obj0 = (uint32_t)F.scan.size(), leaf0 = (uint32_t)F.leaves.size(), prog0 = (uint32_t)F.prog.size();
+    const uint32_t xnode0 = F.append_exact(Fs);
     for (ObjInfo oi : Fs.info) {
       oi.leaf_begin += leaf0;
       oi.prog_begin += prog0;
+      oi.xnode_begin += xnode0;
       F.info.push_back(oi);
     }
     F.scan.insert(F.scan.end(), Fs.scan.begin(), Fs.scan.end());
@@ -259,6 +261,7 @@ lg_status lg_batch_upload(lg_ctx* c, const lg_scene_desc* scenes, uint32_t k) {
     R.obj_base = obj0;
     R.n_obj = d.n_objects;
     R.aspect = DF((double)((float)p.width / (float)p.height));
+    R.aspect64 = (double)((float)p.width / (float)p.height);
     for (int i = 0; i < 4; ++i) R.cutoff[i] = p.cutoff_color[i];
     R.max_bounce = p.max_bounce;
     R.light_base = light0;
@@ -297,6 +300,7 @@ lg_status lg_batch_upload(lg_ctx* c, const lg_scene_desc* scenes, uint32_t k) {
   if ((st = up(c->d_prog, F.prog.data(), F.prog.size(), "scene"))) return st;
   if ((st = up(c->d_lights, F.lights.data(), F.lights.size() * sizeof(LightDev), "scene"))) return st;
   if ((st = up(c->d_cubics, F.cubics.data(), F.cubics.size() * 4, "scene"))) return st;
+  if ((st = upload_exact(c, F))) return st;
   if ((st = up(c->d_cubic_scene, cubic_scene.data(), cubic_scene.size() * 2, "scene"))) return st;
   if ((st = up(c->d_scenes, recs.data(), recs.size() * sizeof(SceneRec), "scene table"))) return st;
   if ((st = up(c->d_canvases, canv.data(), canv.size() * sizeof(SceneCanvas), "canvas table"))) return st;
@@ -340,14 +344,10 @@ lg_status lg_batch_upload(lg_ctx* c, const lg_scene_desc* scenes, uint32_t k) {
   if ((st = batch_buffers(c))) return st;
   // launch shapes: the multi-scene kernels read the object tables from global memory
   int occ = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, scan_kernel(true, c->culled), SCAN_THREADS, (size_t)scan_smem_bytes()), "occupancy");
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, scan_kernel(true, c->culled, c->prm.precision == LG_PRECISION_EXACT),
+                                                   SCAN_THREADS, (size_t)scan_smem_bytes()), "occupancy");
   c->batch_grid_scan = c->n_sm * std::max(1, occ);
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_refine<true>, 256, 0), "occupancy");
-  c->trace_grid[1] = c->n_sm * std::max(1, occ);
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_full<true>, 256, 0), "occupancy");
-  c->trace_grid[2] = c->n_sm * std::max(1, occ);
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bounce_kernel(true, c->culled), 256, 0), "occupancy");
-  c->trace_grid[3] = c->n_sm * std::max(1, occ);
+  if ((st = trace_grids(c, true, 0))) return st;
   const int mode = raster_mode(c->prm);
   const int rsm = raster_smem_bytes(mode);
   if (mode == RM_FIXED_SPLIT_) {

@@ -33,6 +33,7 @@ struct lg_ctx {
   std::string err;
   // scene
   DevBuf d_scan, d_info, d_leaves, d_prog, d_lights, d_cubics;
+  DevBuf d_xgeo, d_xnode;  // exact mode: geometry nodes and per-object preorder trees
   uint32_t n_obj = 0, n_leaves = 0, n_prog = 0, n_lights = 0, n_cubic = 0;
   uint64_t n_primary = 0;
   lg_params prm{};
@@ -52,7 +53,8 @@ struct lg_ctx {
   uint64_t refs_cap = 0, units_cap = 0;
   uint32_t n_tiles = 0, ntx = 0, nty = 0;
   // launch shapes
-  int trace_grid[4] = {0, 0, 0, 0}, raster_grid = 0, bin_grid = 0;  // scan, refine, full, bounce
+  // scan, refine, full, bounce (fast mode), solve, bounce (exact mode)
+  int trace_grid[6] = {0, 0, 0, 0, 0, 0}, raster_grid = 0, bin_grid = 0;
   int raster_warp_grid = 0;
   int raster_variant = 0;  // 1 shared-atomic tile raster, 2 warp-private tile raster; 0 = not tuned yet
   size_t obj_smem = 0;
@@ -108,8 +110,19 @@ void launch_bin_count(lg_ctx* c, const RasterArgs& A, int smem_tiles, size_t bsm
 // The scan and bounce kernels for the context's mode (single scene or multi-scene, with or
 // without the culling walk).
 using TraceKernel = void (*)(SceneDev, TraceBufs, uint32_t, int);
-TraceKernel scan_kernel(bool multi, bool culled);
+using TraceKernel3 = void (*)(SceneDev, TraceBufs, uint32_t);
+TraceKernel scan_kernel(bool multi, bool culled, bool exact);
 TraceKernel bounce_kernel(bool multi, bool culled);
+TraceKernel3 bounce_x_kernel(bool multi, bool culled);
+// Occupancy-sized grids of the trace kernels for the context's mode (trace_grid[1..5]).
+lg_status trace_grids(lg_ctx* c, bool multi, size_t tsm);
+// The light setup and one generation's chain for the context's precision: the FP32 scan,
+// then k_refine + k_full + k_bounce (fast) or k_solve_x + k_bounce_x (exact).
+void launch_light_setup(lg_ctx* c, const SceneDev& S, bool multi, int blocks);
+void launch_generation(lg_ctx* c, const SceneDev& S, const TraceBufs& B, uint32_t g, bool multi, int scan_grid,
+                       size_t scan_smem, size_t tsm, int smem_fits);
+// Uploads a flattened scene's exact-mode tables (geometry nodes, preorder trees).
+lg_status upload_exact(lg_ctx* c, const Flat& F);
 SceneDev scene_dev(lg_ctx* c);
 TraceBufs trace_bufs(lg_ctx* c);
 RasterArgs raster_args(lg_ctx* c);

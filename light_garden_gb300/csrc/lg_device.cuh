@@ -23,6 +23,7 @@
 
 #include "../../include/lg.h"
 #include "lg_df.cuh"
+#include "lg_x64.cuh"
 
 namespace lgd {
 
@@ -73,9 +74,11 @@ struct __align__(16) ObjInfo {
   uint32_t prog_begin;
   uint32_t flags;     // INFO_MATERIAL | INFO_NO_CONTAINS
   df n;               // refractive index
+  double n64;         // the same in FP64 (exact mode)
+  uint32_t xnode_begin, xnode_count;  // exact mode: the object's geometry tree in preorder (lgx::XNode)
   uint64_t _pad;
 };
-static_assert(sizeof(ObjInfo) == 32, "ObjInfo is 32 B");
+static_assert(sizeof(ObjInfo) == 48, "ObjInfo is 48 B");
 
 struct __align__(8) Leaf64 {
   uint32_t kind;
@@ -98,6 +101,8 @@ struct __align__(16) LightDev {
   uint64_t first;      // index of this light's first primary in the virtual gen-0 queue
   uint32_t scene;      // scene of this light (multi-scene traces)
   uint32_t _pad;
+  double dir_angle;    // exact mode: spot base angle (light.rs:230-234), filled on the device
+  double n0x;          // exact mode: start medium in FP64, filled on the device
 };
 
 // Medium a ray travels in: an object index (its refractive index), or
@@ -164,7 +169,7 @@ struct __align__(16) SceneRec {
   float cutoff[4];
   uint32_t max_bounce;
   uint32_t light_base;    // the scene's first light (rays hold scene-local light indices)
-  uint32_t _pad[2];
+  double aspect64;        // exact mode: the canvas half width in FP64
 };
 static_assert(sizeof(SceneRec) == 48, "SceneRec is 48 B");
 
@@ -218,6 +223,13 @@ struct SceneDev {
   const uint16_t* cell_obj;
   // polls of a bounded device wait before it gives up (lg_device_opts.wait_polls; < 0: at once)
   int32_t wait_polls;
+  // exact mode (LG_PRECISION_EXACT): the geometry nodes as uploaded, every object's tree in
+  // preorder (ObjInfo::xnode_begin / xnode_count), the canvas half width in FP64
+  const lg_geo* xgeo;
+  const lgx::XNode* xnode;
+  double aspect64;
+  // sampled frame (one scene): queue entry v of a light is its primary ray_offset + ray_stride * v
+  uint32_t ray_stride, ray_offset;
 };
 
 // First / last cell (unclamped, as a float) of [c - R - margin, c + R + margin] on one
@@ -330,6 +342,10 @@ struct TraceBufs {
 };
 
 // ------------------------------------------------------------------------------ helpers
+// Exact mode keeps FP64 values in the 8-byte df slots of the ray and hit records (the same
+// bytes a double would occupy); these move the bits, no arithmetic.
+__device__ __forceinline__ double xd(df v) { return __hiloint2double(__float_as_int(v.lo), __float_as_int(v.hi)); }
+__device__ __forceinline__ df xdf(double x) { return df{__int_as_float(__double2loint(x)), __int_as_float(__double2hiint(x))}; }
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 __device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }
 

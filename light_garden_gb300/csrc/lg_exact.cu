@@ -1,0 +1,434 @@
+// lg_exact.cu — the solve and bounce kernels of the exact FP64 precision mode.
+//
+// In LG_PRECISION_EXACT one generation is k_scan (FP32 search, lg_trace.cu: candidates of
+// the nearest hit, in work lists) -> k_solve_x -> k_bounce_x.  Both kernels here evaluate
+// the restated collision2d formulas of lg_x64.cuh in IEEE double with every operation
+// rounded on its own, so every decision of Tracer::trace (tracer.rs:360-493: nearest hit
+// with strict < in object order, medium rule, refract / reflect, colour split, canvas exit)
+// is taken on the same FP64 values a CPU evaluation of those formulas computes, and the
+// segments and child rays come out bit for bit equal.
+//
+// Rays and hits keep their FP64 coordinates in the 8-byte df slots of RayRec / HitRec (xd /
+// xdf move the bits).
+#include "lg_kernels.cuh"
+#include "lg_trace_common.cuh"
+
+namespace lgd {
+
+using lgx::V;
+
+__device__ __forceinline__ V ray_o(const RayRec& r) { return lgx::mk(xd(r.ox), xd(r.oy)); }
+__device__ __forceinline__ V ray_d(const RayRec& r) { return lgx::mk(xd(r.dx), xd(r.dy)); }
+
+// Membership of object k (object.rs:240-253): mirrors enclose nothing.
+__device__ __forceinline__ bool obj_contains_x(const SceneDev& S, uint32_t k, V p, uint32_t* fl) {
+  const ObjInfo& oi = S.info[k];
+  if (oi.flags & INFO_NO_CONTAINS) return false;
+  return lgx::object_contains_tree(S.xgeo, S.xnode + oi.xnode_begin, (int)oi.xnode_count, p, fl);
+}
+
+// Light start media (tracer.rs:280-287: the last object with a material containing the
+// light's position) and spot base angles (light.rs:230-234), once per frame.
+template <bool MULTI>
+__global__ void k_light_setup_x(SceneDev S) {
+  const uint32_t l0 = S.serve ? S.light_lo : 0u, l1 = S.serve ? S.light_hi : S.n_lights;
+  for (uint32_t l = l0 + blockIdx.x * blockDim.x + threadIdx.x; l < l1; l += gridDim.x * blockDim.x) {
+    LightDev& L = S.lights[l];
+    const SceneLoc sl = scene_of<MULTI>(S, L.scene);
+    double n = 1.0;
+    const V p = lgx::mk(L.ox, L.oy);
+    for (uint32_t k = sl.base; k < sl.base + sl.n; ++k)
+      if (obj_contains_x(S, k, p, nullptr) && (S.info[k].flags & INFO_MATERIAL)) n = S.info[k].n64;
+    L.n0x = n;
+    L.dir_angle = lgx::spot_base_angle(L.vx, L.vy);
+  }
+}
+template __global__ void k_light_setup_x<false>(SceneDev);
+template __global__ void k_light_setup_x<true>(SceneDev);
+
+// ------------------------------------------------------------------ nearest hit
+// Exact hit record in HitRec's slots: t, p, n as FP64, the event parameter ev in (k, ev).
+__device__ __forceinline__ void store_hit_x(HitRec& o, int obj, const lgx::Hit& h, double ev, uint8_t flags) {
+  o.obj = obj < 0 ? HIT_NONE : (uint16_t)obj;
+  o.t = xdf(h.t); o.px = xdf(h.p.x); o.py = xdf(h.p.y); o.nx = xdf(h.n.x); o.ny = xdf(h.n.y);
+  const df e = xdf(ev);
+  o.k = e.hi;
+  o.ev = e.lo;
+  o.leaf = (uint8_t)h.sub;
+  o.flags = flags;
+}
+
+// Every ray with candidates (the refine lists and the full-solve list of k_scan): the
+// nearest hit over its candidates, each object solved whole as tracer.rs:412-424 does
+// (the minimum distance_squared over the object's hits, then over objects with ties kept by
+// the lower object index), and the near-degenerate flags of tracer.rs's decisions.
+template <bool MULTI>
+__global__ void __launch_bounds__(256) k_solve_x(SceneDev S, TraceBufs B, uint32_t gen) {
+  __shared__ unsigned long long blk_solves;
+  if (threadIdx.x == 0) blk_solves = 0;
+  __syncthreads();
+  uint64_t off[LIST_FULL + 2];
+  off[0] = 0;
+  for (int l = 0; l <= LIST_FULL; ++l) {
+    const unsigned long long c = B.ctr->list_count[gen][l];
+    off[l + 1] = off[l] + (c < B.queue_cap ? c : B.queue_cap);
+  }
+  const uint64_t total = off[LIST_FULL + 1];
+  const RayRec* q = B.queue[gen & 1];
+  unsigned long long my_solves = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+    int l = 0;
+    while (i >= off[l + 1]) ++l;
+    const uint32_t idx = B.list[l][i - off[l]];
+    const RayRec r = q[idx];
+    const ScanRec sc = B.scan[idx];
+    const SceneLoc sl = scene_of<MULTI>(S, r.scene);
+    const V o = ray_o(r), d = ray_d(r);
+    double best_d2 = INFINITY, second = INFINITY, ev = INFINITY;
+    int best = -1;
+    lgx::Hit bh{0.0, lgx::mk(0.0, 0.0), lgx::mk(0.0, 0.0), 0};
+    auto consider = [&](uint32_t j) {
+      const ObjInfo& oi = S.info[sl.base + j];
+      double ob = INFINITY;
+      lgx::Hit oh;
+      bool found = false;
+      ++my_solves;
+      lgx::object_hits(S.xgeo, S.xnode + oi.xnode_begin, (int)oi.xnode_count, o, d, ev, [&](const lgx::Hit& h) {
+        const V dv = lgx::vsub(h.p, o);
+        const double d2 = lgx::dot(dv, dv);
+        if (d2 < ob) {
+          ob = d2;
+          oh = h;
+          found = true;
+        }
+      });
+      if (!found) return;
+      if (ob < best_d2 || (ob == best_d2 && (int)j < best)) {
+        second = best_d2;
+        best_d2 = ob;
+        best = (int)j;
+        bh = oh;
+      } else if (ob < second) {
+        second = ob;
+      }
+    };
+    if (!sc.overflow) {
+      for (int k = 0; k < sc.nc; ++k) consider(sc.cand[k]);
+    } else {  // candidate list overflow (rare): every object that passes the FP32 filters
+      const ObjScan* sobjs = S.scan + sl.base;
+      const float ox = (float)o.x, oy = (float)o.y, dx = (float)d.x, dy = (float)d.y;
+      for (uint32_t j = 0; j < sl.n; ++j) {
+        const float4 h = *reinterpret_cast<const float4*>(&sobjs[j]);
+        float lb;
+        if (!bound_test(h, ox, oy, dx, dy, sc.thr, lb)) continue;
+        if (!(classify32(sobjs[j], ox, oy, dx, dy, lb, j == r.src_obj ? (int)r.src_leaf : -1).key <= sc.thr)) continue;
+        consider(j);
+      }
+    }
+    uint8_t fl = sc.overflow ? LG_PATH_FALLBACK : 0;
+    // tracer.rs:404,417 ties within the band, and decisions in the band before the hit
+    if (best >= 0 && second < INFINITY && lgx::sub(second, best_d2) <= lgx::mul(lgx::BAND, best_d2)) fl |= lgx::NEAR;
+    if (best >= 0 ? ev <= lgx::add(lgx::mul(bh.t, 1.0 + 1e-6), 1e-12) : ev < INFINITY) fl |= lgx::NEAR;
+    store_hit_x(B.hit[idx], best, bh, ev, fl);
+  }
+  atomicAdd(&blk_solves, my_solves);
+  __syncthreads();
+  if (threadIdx.x == 0) atomicAdd(&B.ctr->fp64_solves, blk_solves);
+}
+template __global__ void k_solve_x<false>(SceneDev, TraceBufs, uint32_t);
+template __global__ void k_solve_x<true>(SceneDev, TraceBufs, uint32_t);
+
+// ------------------------------------------------------------------ bounce
+struct BounceX {
+  bool emit;
+  float x0, y0, x1, y1;
+  int hit;
+  uint8_t flags;
+  int nchild;
+  RayRec child[2];
+};
+
+// Ray::refract restated (collision2d; called at tracer.rs:444-450): reflected direction,
+// refracted direction unless total internal reflection, unpolarised Fresnel reflectance.
+__device__ __forceinline__ bool refract_x(V d, V n, double n1, double n2, V& refl, V& refr, double& R,
+                                          uint32_t& fl) {
+  using namespace lgx;
+  double ci = -dot(d, n);
+  if (ci < 0.0) {
+    ci = -ci;
+    n = vscl(n, -1.0);
+  }
+  refl = vadd(d, vscl(n, mul(2.0, ci)));
+  const double eta = dvd(n1, n2);
+  const double k = sub(1.0, mul(mul(eta, eta), sub(1.0, mul(ci, ci))));
+  if (fabs(k) <= BAND) fl |= NEAR;
+  if (k < 0.0) {
+    R = 1.0;
+    return false;
+  }
+  const double ct = sqr(k);
+  refr = vadd(vscl(d, eta), vscl(n, sub(mul(eta, ci), ct)));
+  const double ds = add(mul(n1, ci), mul(n2, ct)), dp = add(mul(n1, ct), mul(n2, ci));
+  if (ds == 0.0 || dp == 0.0) {
+    R = 1.0;
+    return true;
+  }
+  const double rs = dvd(sub(mul(n1, ci), mul(n2, ct)), ds);
+  const double rp = dvd(sub(mul(n1, ct), mul(n2, ci)), dp);
+  R = mul(0.5, add(mul(rs, rs), mul(rp, rp)));
+  return true;
+}
+
+template <bool MULTI, bool CULL>
+__device__ __forceinline__ void bounce_x(const SceneDev& S, const RayRec& r, const ScanRec& sc, const HitRec* hrec,
+                                         BounceX& v) {
+  using namespace lgx;
+  v.emit = false;
+  v.nchild = 0;
+  const SceneLoc sl = scene_of<MULTI>(S, r.scene);
+  uint32_t fl = r.flags;
+  if (near_cutoff(r.c, sl.cutoff)) fl |= NEAR;  // tracer.rs:378-384 in the band
+  const V o = ray_o(r), d = ray_d(r);
+  v.x0 = (float)o.x;
+  v.y0 = (float)o.y;
+  int best = -1;
+  V bp = mk(0.0, 0.0), bn = mk(0.0, 0.0);
+  uint8_t leaf = 0;
+  if (sc.nc > 0 || sc.overflow) {
+    const HitRec h = *hrec;
+    fl |= h.flags;
+    if (h.obj != HIT_NONE) {
+      best = (int)h.obj;
+      bp = mk(xd(h.px), xd(h.py));
+      bn = mk(xd(h.nx), xd(h.ny));
+      leaf = h.leaf;
+    }
+  }
+  if (best >= 0) {
+    const ObjInfo& oi = S.info[sl.base + best];
+    v.emit = true;
+    v.x1 = (float)bp.x;
+    v.y1 = (float)bp.y;
+    v.hit = best;
+    if (oi.flags & INFO_MATERIAL) {
+      // the medium on the far side (tracer.rs:428-442); "origin inside obj" at the midpoint
+      double n2 = 1.0;
+      uint16_t m2 = MEDIUM_AIR;
+      const V mid = vscl(vadd(o, bp), 0.5);
+      if (obj_contains_x(S, sl.base + (uint32_t)best, mid, &fl)) {
+        // the first other object (in table order) that contains the hit point and has a material
+        const float px32 = (float)bp.x, py32 = (float)bp.y;
+        auto far_side = [&](uint32_t k) -> bool {
+          if ((int)k == best) return false;
+          const float4 h = MULTI ? __ldg(&S.bounds[sl.base + k]) : __ldg(reinterpret_cast<const float4*>(&S.scan[k]));
+          if (__float_as_uint(h.w) & INFO_NO_CONTAINS) return false;
+          const float ex = px32 - h.x, ey = py32 - h.y;
+          const float tol = 2e-6f * (fabsf(px32) + fabsf(py32) + fabsf(h.x) + fabsf(h.y) + h.z) + 1e-6f;
+          if (ex * ex + ey * ey > (h.z + tol) * (h.z + tol)) return false;  // far outside: no member, no band
+          if (!obj_contains_x(S, sl.base + k, bp, &fl)) return false;
+          if (!(__float_as_uint(h.w) & INFO_MATERIAL)) return false;
+          n2 = S.info[sl.base + k].n64;
+          m2 = (uint16_t)k;
+          return true;
+        };
+        const GridRec& G = grid_of<MULTI>(S, r.scene);
+        if (!CULL || G.nx == 0) {
+          for (uint32_t k = 0; k < sl.n; ++k)
+            if (far_side(k)) break;
+        } else {
+          // the hit point's cell lists, in table order, every object whose box holds it
+          const float fx = fminf(fmaxf(floorf((px32 - G.x0) * G.iw), 0.0f), (float)(G.nx - 1));
+          const float fy = fminf(fmaxf(floorf((py32 - G.y0) * G.ih), 0.0f), (float)(G.ny - 1));
+          const uint32_t c = (uint32_t)fy * G.nx + (uint32_t)fx;
+          const uint32_t* cs = S.cell_start + G.cell_base;
+          const uint16_t* co = S.cell_obj + G.list_base;
+          for (uint32_t q = __ldg(cs + c), qe = __ldg(cs + c + 1); q < qe; ++q)
+            if (far_side(__ldg(co + q))) break;
+        }
+      } else {
+        n2 = oi.n64;
+        m2 = (uint16_t)best;
+      }
+      const double n1 = r.medium == MEDIUM_AIR ? 1.0
+                        : r.medium == MEDIUM_LIGHT ? S.lights[sl.light_base + r.light].n0x : S.info[sl.base + r.medium].n64;
+      V rl, rr = mk(0.0, 0.0);
+      double R;
+      const bool refr = refract_x(d, bn, n1, n2, rl, rr, R, fl);
+      v.flags = (uint8_t)((fl & 0xffu) | (refr ? 0u : (uint32_t)LG_PATH_TIR));
+      const float refl = (float)R;
+      const float om = __fsub_rn(1.0f, refl);
+      RayRec& a = v.child[0];
+      a.ox = xdf(bp.x); a.oy = xdf(bp.y); a.dx = xdf(rl.x); a.dy = xdf(rl.y);
+      a.medium = r.medium;
+      a.src_obj = (uint16_t)best;
+      a.src_leaf = leaf;
+      a.c[0] = __fmul_rn(r.c[0], refl); a.c[1] = __fmul_rn(r.c[1], refl); a.c[2] = __fmul_rn(r.c[2], refl);
+      a.c[3] = r.c[3];
+      a.path = r.path;
+      a.flags = (uint8_t)fl;
+      a.ex = 0.0f;
+      a.ea = 0.0f;
+      v.nchild = 1;
+      if (refr) {
+        RayRec& t = v.child[1];
+        t.ox = xdf(bp.x); t.oy = xdf(bp.y); t.dx = xdf(rr.x); t.dy = xdf(rr.y);
+        t.medium = m2;
+        t.src_obj = (uint16_t)best;
+        t.src_leaf = leaf;
+        t.c[0] = __fmul_rn(r.c[0], om); t.c[1] = __fmul_rn(r.c[1], om); t.c[2] = __fmul_rn(r.c[2], om);
+        t.c[3] = r.c[3];
+        t.path = r.path | (1ull << r.gen);
+        t.flags = (uint8_t)fl;
+        t.ex = 0.0f;
+        t.ea = 0.0f;
+        v.nchild = 2;
+      }
+    } else {  // Ray::reflect (tracer.rs:476-480)
+      v.flags = (uint8_t)fl;
+      const double dn = dot(d, bn);
+      const V rd = vsub(d, vscl(bn, mul(2.0, dn)));
+      RayRec& a = v.child[0];
+      a.ox = xdf(bp.x); a.oy = xdf(bp.y); a.dx = xdf(rd.x); a.dy = xdf(rd.y);
+      a.medium = r.medium;
+      a.src_obj = (uint16_t)best;
+      a.src_leaf = leaf;
+      a.c[0] = r.c[0]; a.c[1] = r.c[1]; a.c[2] = r.c[2]; a.c[3] = r.c[3];
+      a.path = r.path;
+      a.flags = (uint8_t)fl;
+      a.ex = 0.0f;
+      a.ea = 0.0f;
+      v.nchild = 1;
+    }
+  } else {
+    // canvas exit (tracer.rs:482-488): nearest hit with the canvas rectangle
+    lg_geo canvas;
+    canvas.kind = LG_GEO_RECT;
+    canvas.origin[0] = 0.0; canvas.origin[1] = 0.0;
+    canvas.rot[0] = 1.0; canvas.rot[1] = 0.0;
+    const double aspect = MULTI ? S.scenes[r.scene].aspect64 : S.aspect64;
+    canvas.v[0] = mul(2.0, aspect);
+    canvas.v[1] = 2.0;
+    double cev = INFINITY;
+    int nh = 0;
+    Hit first{INFINITY, mk(0.0, 0.0), mk(0.0, 0.0), 0};
+    hits_rect(canvas, o, d, cev, [&](const Hit& h) {
+      if (nh == 0 || h.t < first.t) first = h;
+      ++nh;
+    });
+    if (nh > 0) {
+      v.emit = true;
+      v.x1 = (float)first.p.x;
+      v.y1 = (float)first.p.y;
+      v.hit = -1;
+      v.flags = (uint8_t)((fl | (cev < INFINITY ? NEAR : 0u)) & 0xffu);
+    }
+  }
+  // children: the next generation skips colours below the cutoff (tracer.rs:378-384)
+  int w = 0;
+  for (int q = 0; q < v.nchild; ++q) {
+    RayRec c = v.child[q];
+    if ((uint32_t)r.gen + 1 >= sl.max_bounce || below_cutoff(c.c, sl.cutoff)) continue;
+    c.gen = (uint8_t)(r.gen + 1);
+    c.prim = r.prim;
+    c.light = r.light;
+    c._pad = 0;
+    c.scene = r.scene;
+    v.child[w++] = c;
+  }
+  v.nchild = w;
+}
+
+// appends one segment per emitting lane with one atomic per warp (all lanes call)
+__device__ __forceinline__ void emit_segments_x(const SceneDev& S, const TraceBufs& B, const BounceX& v,
+                                                const RayRec& r, unsigned long long& my_near) {
+  const unsigned lane = lane_id();
+  const unsigned emask = __ballot_sync(0xffffffffu, v.emit);
+  if (!emask) return;
+  unsigned long long sbase = 0;
+  const int leader = __ffs(emask) - 1;
+  if ((int)lane == leader) sbase = atomicAdd(&B.ctr->seg_count, (unsigned long long)__popc(emask));
+  sbase = __shfl_sync(0xffffffffu, sbase, leader);
+  if (!v.emit) return;
+  const unsigned long long slot = sbase + __popc(emask & lanemask_lt());
+  if (v.flags & LG_PATH_NEAR_DEGENERATE) ++my_near;
+  if (slot >= B.seg_cap) return;
+  float4* dst = reinterpret_cast<float4*>(B.segs + slot);
+  dst[0] = make_float4(v.x0, v.y0, v.x1, v.y1);
+  dst[1] = make_float4(r.c[0], r.c[1], r.c[2], r.c[3]);
+  if (B.seg_scene) B.seg_scene[slot] = r.scene;
+  if (S.record_paths) {
+    lg_path_record pr;
+    pr.path = r.path; pr.primary = r.prim; pr.light = r.light; pr.gen = r.gen;
+    pr.flags = v.flags; pr.hit = v.hit; pr.source = LG_SRC_TRACE;
+    B.paths[slot] = pr;
+  }
+}
+
+template <bool MULTI, bool CULL>
+__global__ void __launch_bounds__(256) k_bounce_x(SceneDev S, TraceBufs B, uint32_t gen) {
+  __shared__ unsigned long long blk_visits, blk_near;
+  if (threadIdx.x == 0) { blk_visits = 0; blk_near = 0; }
+  __syncthreads();
+  // the rays with work: every work list of this generation, one after the other
+  uint64_t off[N_LISTS + 1];
+  off[0] = 0;
+  for (int l = 0; l < N_LISTS; ++l) {
+    const unsigned long long c = B.ctr->list_count[gen][l];
+    off[l + 1] = off[l] + (c < B.queue_cap ? c : B.queue_cap);
+  }
+  const uint64_t total = off[N_LISTS];
+  const RayRec* qin = B.queue[gen & 1];
+  RayRec* qout = B.queue[(gen + 1) & 1];
+  const unsigned lane = lane_id();
+  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+  unsigned long long my_visits = 0, my_near = 0;
+  for (uint64_t base = warp * 32; base < total; base += nwarps * 32) {
+    const uint64_t i = base + lane;
+    BounceX v;
+    v.emit = false;
+    v.nchild = 0;
+    v.flags = 0;
+    v.hit = -1;
+    RayRec r;
+    if (i < total) {
+      int l = 0;
+      while (i >= off[l + 1]) ++l;
+      const uint32_t idx = B.list[l][i - off[l]];
+      const ScanRec sc = B.scan[idx];
+      r = qin[idx];
+      ++my_visits;
+      bounce_x<MULTI, CULL>(S, r, sc, &B.hit[idx], v);
+    }
+    emit_segments_x(S, B, v, r, my_near);
+    // children: warp prefix sum of 0..2 per lane, one atomic per warp
+    int incl = v.nchild;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if ((int)lane >= o) incl += y;
+    }
+    const int tot = __shfl_sync(0xffffffffu, incl, 31);
+    if (tot > 0 && (MULTI || gen + 1 < S.max_bounce)) {
+      unsigned long long qbase = 0;
+      if (lane == 31) qbase = atomicAdd(&B.ctr->queue_count[gen + 1], (unsigned long long)tot);
+      qbase = __shfl_sync(0xffffffffu, qbase, 31);
+      const unsigned long long first = qbase + (unsigned long long)(incl - v.nchild);
+      for (int q = 0; q < v.nchild; ++q)
+        if (first + q < B.queue_cap) qout[first + q] = v.child[q];
+    }
+  }
+  atomicAdd(&blk_visits, my_visits);
+  atomicAdd(&blk_near, my_near);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    atomicAdd(&B.ctr->visits, blk_visits);
+    atomicAdd(&B.ctr->near, blk_near);
+  }
+}
+template __global__ void k_bounce_x<false, false>(SceneDev, TraceBufs, uint32_t);
+template __global__ void k_bounce_x<false, true>(SceneDev, TraceBufs, uint32_t);
+template __global__ void k_bounce_x<true, false>(SceneDev, TraceBufs, uint32_t);
+template __global__ void k_bounce_x<true, true>(SceneDev, TraceBufs, uint32_t);
+
+}  // namespace lgd

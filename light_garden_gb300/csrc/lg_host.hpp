@@ -38,6 +38,23 @@ struct Flat {
   std::vector<LightDev> lights;
   std::vector<uint32_t> cubics;
   GridH grid;
+  // exact mode: the geometry nodes as given, each object's tree in preorder (ObjInfo::
+  // xnode_begin / xnode_count index xnode; XNode::geo indexes xgeo) and the deepest node
+  std::vector<lg_geo> xgeo;
+  std::vector<lgx::XNode> xnode;
+  int xdepth = 0;
+  // appends another scene's exact-mode tables, moving its node indices past this one's;
+  // the caller adds the returned base to that scene's ObjInfo::xnode_begin
+  uint32_t append_exact(const Flat& o) {
+    const uint32_t g0 = (uint32_t)xgeo.size(), n0 = (uint32_t)xnode.size();
+    xgeo.insert(xgeo.end(), o.xgeo.begin(), o.xgeo.end());
+    for (lgx::XNode n : o.xnode) {
+      n.geo += (int32_t)g0;
+      xnode.push_back(n);
+    }
+    xdepth = xdepth > o.xdepth ? xdepth : o.xdepth;
+    return n0;
+  }
 };
 
 // Several scenes' grids, concatenated in the order of their object tables.
@@ -63,6 +80,8 @@ struct GridTables {
 lg_status flatten_scene(std::string& err, const lg_geo* G, uint32_t n_geo, const lg_object* O, uint32_t n_obj,
                         const lg_light* Ls, uint32_t n_lights, Flat& F);
 lg_status validate_params(std::string& err, const lg_params& p);
+// Exact mode's limits on a flattened scene (trees of at most lgx::MAX_DEPTH levels).
+lg_status validate_exact(std::string& err, const lg_params& p, const Flat& F);
 bool blend_supported(const lg_blend_component& b);
 int raster_mode(const lg_params& p);
 void to_device_leaves(const std::vector<LeafH>& in, std::vector<Leaf64>& out);

@@ -54,7 +54,8 @@ template <bool MULTI>
 __global__ void k_light_setup(SceneDev S);
 // CULL: the culling-grid walk is compiled in (scenes whose grid has nx == 0 still take
 // the full scan); without it the kernels scan every object.
-template <bool MULTI, bool CULL>
+// EXACT: the rays hold FP64 coordinates (exact mode); no FP32 canvas exits.
+template <bool MULTI, bool CULL, bool EXACT>
 __global__ void k_scan(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
 int scan_smem_bytes();
 constexpr int SCAN_THREADS = 128;
@@ -64,6 +65,13 @@ template <bool MULTI>
 __global__ void k_full(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
 template <bool MULTI, bool CULL>
 __global__ void k_bounce(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
+// exact FP64 mode (lg_exact.cu)
+template <bool MULTI>
+__global__ void k_light_setup_x(SceneDev S);
+template <bool MULTI>
+__global__ void k_solve_x(SceneDev S, TraceBufs B, uint32_t gen);
+template <bool MULTI, bool CULL>
+__global__ void k_bounce_x(SceneDev S, TraceBufs B, uint32_t gen);
 __global__ void k_overlay(SceneDev S, TraceBufs B, const uint32_t* cubic_objs, const uint16_t* cubic_scene,
                           uint32_t n_cubic, lg_string_mod sm);
 __global__ void k_scene_hist(SceneDev S, TraceBufs B, uint32_t gen, unsigned* count);

@@ -142,9 +142,11 @@ lg_status upload_tables(lg_ctx* c, ServeState& V, const std::vector<uint32_t>& a
     const Flat& Fs = sl.req.F;
     const uint32_t obj0 = (uint32_t)F.scan.size(), leaf0 = (uint32_t)F.leaves.size(), prog0 = (uint32_t)F.prog.size();
     if (oi == n_old) light_lo = (uint32_t)F.lights.size();
+    const uint32_t xnode0 = F.append_exact(Fs);
     for (ObjInfo o : Fs.info) {
       o.leaf_begin += leaf0;
       o.prog_begin += prog0;
+      o.xnode_begin += xnode0;
       F.info.push_back(o);
     }
     F.scan.insert(F.scan.end(), Fs.scan.begin(), Fs.scan.end());
@@ -171,6 +173,7 @@ lg_status upload_tables(lg_ctx* c, ServeState& V, const std::vector<uint32_t>& a
     R.obj_base = obj0;
     R.n_obj = (uint32_t)Fs.scan.size();
     R.aspect = DF((double)((float)sl.req.prm.width / (float)sl.req.prm.height));
+    R.aspect64 = (double)((float)sl.req.prm.width / (float)sl.req.prm.height);
     for (int i = 0; i < 4; ++i) R.cutoff[i] = sl.req.prm.cutoff_color[i];
     R.max_bounce = sl.req.prm.max_bounce;
     R.light_base = light0;
@@ -194,6 +197,7 @@ lg_status upload_tables(lg_ctx* c, ServeState& V, const std::vector<uint32_t>& a
   if ((st = up(c->d_leaves, dleaves.data(), dleaves.size() * sizeof(Leaf64), "scene"))) return st;
   if ((st = up(c->d_prog, F.prog.data(), F.prog.size(), "scene"))) return st;
   if ((st = up(c->d_lights, F.lights.data(), F.lights.size() * sizeof(LightDev), "scene"))) return st;
+  if ((st = upload_exact(c, F))) return st;
   if ((st = up(c->d_bounds, bounds.data(), bounds.size() * sizeof(float4), "object bounds"))) return st;
   if ((st = upload_grids(c, grids))) return st;
   if ((st = up(c->d_scenes, recs.data(), recs.size() * sizeof(SceneRec), "scene table"))) return st;
@@ -395,14 +399,12 @@ lg_status lg_serve_begin(lg_ctx* c, const lg_serve_opts* opts) {
   std::memset(c->h_ctr, 0, sizeof(Counters));
   // launch shapes of the multi-scene kernels
   int occ = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, scan_kernel(true, c->culled), SCAN_THREADS, (size_t)scan_smem_bytes()), "occupancy");
-  c->batch_grid_scan = c->n_sm * std::max(1, occ);
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_refine<true>, 256, 0), "occupancy");
-  c->trace_grid[1] = c->n_sm * std::max(1, occ);
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_full<true>, 256, 0), "occupancy");
-  c->trace_grid[2] = c->n_sm * std::max(1, occ);
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bounce_kernel(true, c->culled), 256, 0), "occupancy");
-  c->trace_grid[3] = c->n_sm * std::max(1, occ);
+  // the requests' precision is not known yet: the scan grid fits either kernel
+  int occ_x = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, scan_kernel(true, c->culled, false), SCAN_THREADS, (size_t)scan_smem_bytes()), "occupancy");
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_x, scan_kernel(true, c->culled, true), SCAN_THREADS, (size_t)scan_smem_bytes()), "occupancy");
+  c->batch_grid_scan = c->n_sm * std::max(1, std::min(occ, occ_x));
+  if ((st = trace_grids(c, true, 0))) { serve_free(c); return st; }
   const int rsm = raster_smem_bytes(RM_FIXED_SPLIT_);
   CK(cudaFuncSetAttribute(k_raster<RM_FIXED_SPLIT_>, cudaFuncAttributeMaxDynamicSharedMemorySize, rsm), "smem attr");
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_raster<RM_FIXED_SPLIT_>, 256, rsm), "occupancy");
@@ -426,12 +428,15 @@ lg_status lg_serve_submit(lg_ctx* c, const lg_scene_desc* d, uint64_t* id_out) {
   if (V.have_common && (std::memcmp(&p.color_blend, &V.common.color_blend, sizeof p.color_blend) ||
                         std::memcmp(&p.alpha_blend, &V.common.alpha_blend, sizeof p.alpha_blend) ||
                         std::memcmp(p.clear_color, V.common.clear_color, sizeof p.clear_color) ||
-                        std::memcmp(p.blend_constant, V.common.blend_constant, sizeof p.blend_constant)))
-    return fail(c, LG_ERR_UNSUPPORTED, "all requests of a server share blend state and clear colour");
+                        std::memcmp(p.blend_constant, V.common.blend_constant, sizeof p.blend_constant) ||
+                        p.precision != V.common.precision))
+    return fail(c, LG_ERR_UNSUPPORTED, "all requests of a server share precision, blend state and clear colour");
   if (p.string_mod.modulo) return fail(c, LG_ERR_UNSUPPORTED, "the string-mod overlay is not served");
+  if (p.ray_stride > 1) return fail(c, LG_ERR_UNSUPPORTED, "sampled frames (ray_stride) are one-scene only");
   if (d->n_objects > 65535 || d->n_lights > 65535) return fail(c, LG_ERR_UNSUPPORTED, "at most 65535 objects and lights");
   Request R;
   st = flatten_scene(c->err, d->geos, d->n_geo, d->objects, d->n_objects, d->lights, d->n_lights, R.F);
+  if (!st) st = validate_exact(c->err, p, R.F);
   if (st) return st;
   build_grid(R.F.scan, c->culling, c->grid_density, R.F.grid);
   R.prm = p;
@@ -535,17 +540,14 @@ lg_status lg_serve_step(lg_ctx* c, lg_serve_step_stats* stats) {
     SceneDev SL = SD;
     SL.light_lo = 0;
     SL.light_hi = c->n_lights;
-    k_light_setup<true><<<(c->n_lights + 127) / 128, 128, 0, c->stream>>>(SL);
+    launch_light_setup(c, SL, true, (int)((c->n_lights + 255) / 256));
   }
   if (V.live > 0) {  // queued rays in scene order
     k_scene_hist<<<c->n_sm * 8, 256, 0, c->stream>>>(SD, B, g, (unsigned*)c->d_scene_count.p);
     k_scene_offsets<<<1, 1024, 0, c->stream>>>((unsigned*)c->d_scene_count.p, (unsigned*)c->d_scene_off.p, V.max_slots);
     k_scene_scatter<<<c->n_sm * 8, 256, 0, c->stream>>>(SD, B, g, (unsigned*)c->d_scene_off.p, (uint32_t*)c->d_order.p);
   }
-  scan_kernel(true, c->culled)<<<c->batch_grid_scan, SCAN_THREADS, (size_t)scan_smem_bytes(), c->stream>>>(SD, B, g, 0);
-  k_refine<true><<<c->trace_grid[1], 256, 0, c->stream>>>(SD, B, g);
-  k_full<true><<<c->trace_grid[2], 256, 0, c->stream>>>(SD, B, g, 0);
-  bounce_kernel(true, c->culled)<<<c->trace_grid[3], 256, 0, c->stream>>>(SD, B, g, 0);
+  launch_generation(c, SD, B, g, true, c->batch_grid_scan, (size_t)scan_smem_bytes(), 0, 0);
   if (!cubic_obj.empty()) {
     lg_string_mod no_sm;
     std::memset(&no_sm, 0, sizeof no_sm);

@@ -13,6 +13,7 @@
 // The chain per generation (k_scan, k_refine over 4 leaf-kind lists, k_full, k_bounce) is
 // described above k_scan below.
 #include "lg_kernels.cuh"
+#include "lg_trace_common.cuh"
 
 namespace lgd {
 
@@ -138,43 +139,6 @@ template __global__ void k_light_setup<true>(SceneDev);
 //              and deep CSG objects), grouped by solve class
 //   k_bounce   medium (tracer.rs:428-442), refract / reflect with colour split
 //              (444-481) or canvas exit (482-488); appends segments and children
-__device__ __forceinline__ bool below_cutoff(const float* c, const float* k) {
-  return (c[0] < k[0] && c[1] < k[1] && c[2] < k[2]) || c[3] < k[3];
-}
-__device__ __forceinline__ bool near_cutoff(const float* c, const float* k) {
-  bool n = false;
-#pragma unroll
-  for (int i = 0; i < 4; ++i) n |= fabsf(c[i] - k[i]) <= 1e-6f * k[i];
-  return n;
-}
-
-// FP32 bounding-circle test shared by both scan passes: false if the object cannot hold a
-// hit at a ray parameter <= thr; lb receives a lower bound of its hit distances.
-__device__ __forceinline__ bool bound_test(const float4& h, float ox, float oy, float dx, float dy, float thr,
-                                           float& lb) {
-  const float ocx = h.x - ox, ocy = h.y - oy;
-  const float b = ocx * dx + ocy * dy, perp = ocx * dy - ocy * dx;
-  const float btol = 2e-6f * (fabsf(b) + fabsf(perp) + h.z) + 1e-6f;
-  if (fabsf(perp) > h.z + btol || b + h.z + btol < -TAU32) return false;
-  lb = b - h.z - btol;
-  return lb <= thr;
-}
-
-// Queued rays a launch takes (the children of the previous generation or step) ...
-__device__ __forceinline__ uint64_t n_real_of(const SceneDev& S, const TraceBufs& B, uint32_t gen) {
-  if (gen == 0 && !S.serve) return 0;
-  const unsigned long long n = B.ctr->queue_count[gen];
-  return n < B.queue_cap ? n : B.queue_cap;
-}
-// ... and primaries it generates (virtual queue entries after the queued ones)
-__device__ __forceinline__ uint64_t n_new_of(const SceneDev& S, uint32_t gen) {
-  return S.serve ? S.n_new : (gen == 0 ? S.n_primary : 0);
-}
-__device__ __forceinline__ uint64_t n_in_of(const SceneDev& S, const TraceBufs& B, uint32_t gen) {
-  const uint64_t n = n_real_of(S, B, gen) + n_new_of(S, gen);
-  return n < B.queue_cap ? n : B.queue_cap;
-}
-
 __device__ __forceinline__ int leaf_kind_of(uint32_t info, int leaf) {
   return (int)(leaf == 0 ? info_leaf_a(info) : info_leaf_b(info));
 }
@@ -272,7 +236,7 @@ struct ScanSmem {  // [slot][lane]: a warp's 32 lanes touch 32 consecutive slots
 
 int scan_smem_bytes() { return (int)sizeof(ScanSmem); }
 
-template <bool MULTI, bool CULL>
+template <bool MULTI, bool CULL, bool EXACT>
 __global__ void __launch_bounds__(SCAN_WARPS * 32, CULL ? SCAN_CULL_BLOCKS : 4)
     k_scan(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -312,11 +276,17 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, CULL ? SCAN_CULL_BLOCKS : 4)
           if (S.lights[mid].first <= v) l = mid; else lhi = mid;
         }
         const LightDev& L = S.lights[l];
-        const uint64_t i = v - L.first;
+        const uint64_t i = S.ray_offset + (uint64_t)S.ray_stride * (v - L.first);
         double pox, poy, pdx, pdy;
-        primary_ray(L, i, pox, poy, pdx, pdy);
-        r.ox = df_from_double(pox); r.oy = df_from_double(poy);
-        r.dx = df_from_double(pdx); r.dy = df_from_double(pdy);
+        if (EXACT) {  // exact mode: the FP64 coordinates themselves, in the df slots
+          lgx::primary_ray_x(L.kind, L.ox, L.oy, L.vx, L.vy, L.spot_angle, L.dir_angle, (double)L.num_rays, i, pox,
+                             poy, pdx, pdy);
+          r.ox = xdf(pox); r.oy = xdf(poy); r.dx = xdf(pdx); r.dy = xdf(pdy);
+        } else {
+          primary_ray(L, i, pox, poy, pdx, pdy);
+          r.ox = df_from_double(pox); r.oy = df_from_double(poy);
+          r.dx = df_from_double(pdx); r.dy = df_from_double(pdy);
+        }
         r.medium = MEDIUM_LIGHT;
         r.src_obj = SRC_NONE;
         r.src_leaf = 0;
@@ -329,8 +299,8 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, CULL ? SCAN_CULL_BLOCKS : 4)
         r._pad = 0;
         r.scene = MULTI ? (uint16_t)L.scene : (uint16_t)0;
         // rounding of the light's ray generator (sin/cos/atan) and the double-float split
-        r.ex = DF_ROUND * (1.0f + fabsf(r.ox.hi) + fabsf(r.oy.hi));
-        r.ea = DF_ROUND;
+        r.ex = EXACT ? 0.0f : DF_ROUND * (1.0f + fabsf(r.ox.hi) + fabsf(r.oy.hi));
+        r.ea = EXACT ? 0.0f : DF_ROUND;
         if (idx < B.queue_cap) q[idx] = r;
       } else {
         r = q[idx];
@@ -339,7 +309,8 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, CULL ? SCAN_CULL_BLOCKS : 4)
     const SceneLoc sl = scene_of<MULTI>(S, live ? r.scene : 0u);
     const bool dead = live && below_cutoff(r.c, sl.cutoff);
     live = live && !dead;
-    const float ox = r.ox.hi, oy = r.oy.hi, dx = r.dx.hi, dy = r.dy.hi;
+    const float ox = EXACT ? (float)xd(r.ox) : r.ox.hi, oy = EXACT ? (float)xd(r.oy) : r.oy.hi;
+    const float dx = EXACT ? (float)xd(r.dx) : r.dx.hi, dy = EXACT ? (float)xd(r.dy) : r.dy.hi;
     W.ray[w][lane] = make_float4(ox, oy, dx, dy);
     W.src[w][lane] = live ? ((uint32_t)r.src_obj << 8 | r.src_leaf) : 0xffffffffu;
     W.base[w][lane] = sl.base;
@@ -613,7 +584,7 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, CULL ? SCAN_CULL_BLOCKS : 4)
         } else {
           // no object can be hit: leave through the canvas (tracer.rs:482-488)
           float L;
-          if (fast_canvas_exit(slp.aspect, r, x1, y1, L)) {
+          if (!EXACT && fast_canvas_exit(slp.aspect, r, x1, y1, L)) {
             emit = true;
             ++my_visits;
             eflags = r.flags | (near_cutoff(r.c, slp.cutoff) || L > ILL_COND ? LG_PATH_NEAR_DEGENERATE : 0);
@@ -639,10 +610,14 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, CULL ? SCAN_CULL_BLOCKS : 4)
   }
 }
 
-template __global__ void k_scan<false, false>(SceneDev, TraceBufs, uint32_t, int);
-template __global__ void k_scan<false, true>(SceneDev, TraceBufs, uint32_t, int);
-template __global__ void k_scan<true, false>(SceneDev, TraceBufs, uint32_t, int);
-template __global__ void k_scan<true, true>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<false, false, false>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<false, true, false>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<true, false, false>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<true, true, false>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<false, false, true>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<false, true, true>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<true, false, true>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<true, true, true>(SceneDev, TraceBufs, uint32_t, int);
 
 __device__ __forceinline__ void store_hit(HitRec& o, int obj, const Hit64& h, float ev, uint8_t flags) {
   o.obj = obj < 0 ? HIT_NONE : (uint16_t)obj;
@@ -1144,11 +1119,12 @@ __global__ void k_overlay(SceneDev S, TraceBufs B, const uint32_t* cubic_objs, c
         while (e) { if (e & 1) p *= b; b *= b; e >>= 1; }
         ix = p % m;
       }
-      const double aa = (double)(sm.turns * (iix % m)) * (2.0 * 3.141592653589793) / (double)m;
-      const double ab = (double)(sm.turns * (ix % m)) * (2.0 * 3.141592653589793) / (double)m;
+      // string_mod.rs:45-55 point angles, with the ray generators' sin / cos
+      const double aa = lgx::dvd(lgx::mul((double)(sm.turns * (iix % m)), 2.0 * 3.141592653589793), (double)m);
+      const double ab = lgx::dvd(lgx::mul((double)(sm.turns * (ix % m)), 2.0 * 3.141592653589793), (double)m);
       double sa, ca, sb, cb;
-      sincos(aa, &sa, &ca);
-      sincos(ab, &sb, &cb);
+      lgx::sincos_x(aa, sa, ca);
+      lgx::sincos_x(ab, sb, cb);
       s.x0 = (float)ca; s.y0 = (float)sa; s.x1 = (float)cb; s.y1 = (float)sb;
       s.color[0] = sm.color[0]; s.color[1] = sm.color[1]; s.color[2] = sm.color[2]; s.color[3] = sm.color[3];
       pr.primary = (uint32_t)iix; pr.gen = 0; pr.source = LG_SRC_STRING_MOD;

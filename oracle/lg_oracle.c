@@ -492,24 +492,111 @@ static int validate_scene(const oscene* S) {
 }
 
 /* ------------------------------------------------------------------------ lights */
+/* sin / cos / atan of the ray generators, restated from published methods with plain
+ * IEEE-754 double operations only (every product and sum rounded on its own), so that
+ * the same operations give the same bits on every machine and on the GPU:
+ *   sincos  Cody-Waite reduction by pi/2 (pi/2 split in three parts of 33, 33 and 53
+ *           significant bits, so that k * P1 and k * P2 are exact for |k| < 2^20), then the
+ *           Taylor series of sin and cos on [-pi/4, pi/4] (terms to r^19 and r^20, the
+ *           truncation below 1e-21) in Horner form, and the quadrant from k mod 4;
+ *   atan    atan(x) = pi/2 - atan(1/x) for |x| > 1, atan(a) = pi/6 + atan((a sqrt3 - 1) /
+ *           (a + sqrt3)) for a > tan(pi/12), then the Taylor series to a^29 on |a| <= 0.268.
+ * They stay within a few ulp of the C library's functions (tests/test_oracle.py), which is
+ * what light.rs calls through Rust's f64::sin_cos / atan; the ray directions are a shared
+ * definition of this restatement and of the GPU path. */
+#define CW_P1 1.5707963267341256
+#define CW_P2 6.077100506303966e-11
+#define CW_P3 2.0222662487959506e-21
+#define TWO_OVER_PI 0.6366197723675814
+#define PI2_HI 1.5707963267948966
+#define PI2_LO 6.123233995736766e-17
+#define PI6_HI 0.5235987755982989
+#define PI6_LO (-5.360408832255455e-17)
+#define SQRT3 1.7320508075688772
+#define TAN_PI12 0.2679491924311227
+
+void lgo_sincos(double x, double* s_out, double* c_out) {
+  const double k = rint(x * TWO_OVER_PI);
+  const double r = ((x - k * CW_P1) - k * CW_P2) - k * CW_P3;
+  const double z = r * r;
+  /* sin: r + r z (-1/3! + z (1/5! - ... - z^8/19!)) */
+  double ps = -8.22063524662433e-18;        /* -1/19! */
+  ps = ps * z + 2.8114572543455206e-15;     /*  1/17! */
+  ps = ps * z - 7.647163731819816e-13;      /* -1/15! */
+  ps = ps * z + 1.6059043836821613e-10;     /*  1/13! */
+  ps = ps * z - 2.505210838544172e-08;      /* -1/11! */
+  ps = ps * z + 2.7557319223985893e-06;     /*  1/9!  */
+  ps = ps * z - 0.0001984126984126984;      /* -1/7!  */
+  ps = ps * z + 0.008333333333333333;       /*  1/5!  */
+  ps = ps * z - 0.16666666666666666;        /* -1/3!  */
+  const double sn = r + (r * z) * ps;
+  /* cos: 1 - z/2 + z^2 (1/4! - z/6! + ... + z^8/20!) */
+  double pc = 4.110317623312165e-19;        /*  1/20! */
+  pc = pc * z - 1.5619206968586225e-16;     /* -1/18! */
+  pc = pc * z + 4.779477332387385e-14;      /*  1/16! */
+  pc = pc * z - 1.1470745597729725e-11;     /* -1/14! */
+  pc = pc * z + 2.08767569878681e-09;       /*  1/12! */
+  pc = pc * z - 2.755731922398589e-07;      /* -1/10! */
+  pc = pc * z + 2.48015873015873e-05;       /*  1/8!  */
+  pc = pc * z - 0.001388888888888889;       /* -1/6!  */
+  pc = pc * z + 0.041666666666666664;       /*  1/4!  */
+  const double cs = (1.0 - 0.5 * z) + (z * z) * pc;
+  const long long q = ((long long)k % 4 + 4) % 4;
+  *s_out = q == 0 ? sn : q == 1 ? cs : q == 2 ? -sn : -cs;
+  *c_out = q == 0 ? cs : q == 1 ? -sn : q == 2 ? -cs : sn;
+}
+
+double lgo_atan(double x) {
+  if (x != x) return x;
+  const int neg = x < 0.0;
+  double a = fabs(x);
+  const int inv = a > 1.0;
+  if (inv) a = 1.0 / a;
+  const int off = a > TAN_PI12;
+  if (off) a = (a * SQRT3 - 1.0) / (a + SQRT3);
+  const double z = a * a;
+  double p = -0.034482758620689655;         /* -1/29 */
+  p = p * z + 0.037037037037037035;         /*  1/27 */
+  p = p * z - 0.04;                         /* -1/25 */
+  p = p * z + 0.043478260869565216;         /*  1/23 */
+  p = p * z - 0.047619047619047616;         /* -1/21 */
+  p = p * z + 0.05263157894736842;          /*  1/19 */
+  p = p * z - 0.058823529411764705;         /* -1/17 */
+  p = p * z + 0.06666666666666667;          /*  1/15 */
+  p = p * z - 0.07692307692307693;          /* -1/13 */
+  p = p * z + 0.09090909090909091;          /*  1/11 */
+  p = p * z - 0.1111111111111111;           /* -1/9  */
+  p = p * z + 0.14285714285714285;          /*  1/7  */
+  p = p * z - 0.2;                          /* -1/5  */
+  p = p * z + 0.3333333333333333;           /*  1/3  */
+  double r = a - (a * z) * p;
+  if (off) r = PI6_HI + (r + PI6_LO);
+  if (inv) r = PI2_HI - (r - PI2_LO);
+  return neg ? -r : r;
+}
+
 static void light_ray(const lg_light* L, uint64_t i, v2* o, v2* d) {
   double n = (double)L->num_rays;
   switch (L->kind) {
     case LG_LIGHT_POINT: { /* light.rs:163-174 */
       double f = (double)i * M_PI * 2.0 / n;
+      double sf, cf;
+      lgo_sincos(f, &sf, &cf);
       *o = mk(L->origin[0], L->origin[1]);
-      *d = mk(cos(f), sin(f));
+      *d = mk(cf, sf);
       break;
     }
     case LG_LIGHT_SPOT: { /* light.rs:225-249 */
       double sx = L->v[0], sy = L->v[1];
-      double dir_angle = fabs(sx) < SPOT_EPSILON ? (sy >= 0.0 ? M_PI * 0.5 : -M_PI * 0.5) : atan(sy / sx);
+      double dir_angle = fabs(sx) < SPOT_EPSILON ? (sy >= 0.0 ? M_PI * 0.5 : -M_PI * 0.5) : lgo_atan(sy / sx);
       double min_angle = dir_angle - 0.5 * L->spot_angle;
       double step = (double)(i + 1);
       double ang = min_angle + (step / n) * L->spot_angle;
       double sign = signbit(sx) ? -1.0 : 1.0; /* f64::signum: -0.0 -> -1 */
+      double sa, ca;
+      lgo_sincos(ang, &sa, &ca);
       *o = mk(L->origin[0], L->origin[1]);
-      *d = mk(sign * cos(ang), sign * sin(ang));
+      *d = mk(sign * ca, sign * sa);
       break;
     }
     default: { /* DIRECTIONAL, light.rs:103-115 with the definition in the header */
@@ -882,7 +969,10 @@ int lgo_trace(const lg_geo* geos, uint32_t n_geo, const lg_object* objs, uint32_
       double aa = (double)(sm->turns * ia) * (2.0 * M_PI) / (double)m;
       double ab = (double)(sm->turns * ib) * (2.0 * M_PI) / (double)m;
       lg_path_record r = {0, (uint32_t)iix, 0xffff, 0, 0, -1, LG_SRC_STRING_MOD};
-      rc = buf_push(ov, mk(cos(aa), sin(aa)), mk(cos(ab), sin(ab)), sm->color, &r);
+      double sa, ca, sb, cb;
+      lgo_sincos(aa, &sa, &ca);
+      lgo_sincos(ab, &sb, &cb);
+      rc = buf_push(ov, mk(ca, sa), mk(cb, sb), sm->color, &r);
     }
   }
   uint64_t total = 0, visits = 0, nearc = 0;

@@ -52,6 +52,11 @@ int lgo_trace(const lg_geo* geos, uint32_t n_geo, const lg_object* objs, uint32_
               lg_segment* segs, lg_path_record* paths, double* seg64, uint64_t cap,
               uint64_t* n_out, lgo_stats* stats);
 
+/* The ray generators' sin / cos / atan (see lg_oracle.c: plain IEEE double operations,
+ * within a few ulp of the C library). */
+void lgo_sincos(double x, double* s, double* c);
+double lgo_atan(double x);
+
 /* Primary rays of one light (light.rs set_num_rays): out[4*i..] = ox, oy, dx, dy. */
 int lgo_light_rays(const lg_light* light, double* out, uint64_t cap);
 

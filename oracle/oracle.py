@@ -50,6 +50,9 @@ def lib() -> C.CDLL:
                                 P(abi.lg_segment), P(abi.lg_path_record), P(C.c_double), C.c_uint64,
                                 P(C.c_uint64), P(lgo_stats)]
         L.lgo_light_rays.argtypes = [P(abi.lg_light), P(C.c_double), C.c_uint64]
+        L.lgo_sincos.argtypes = [C.c_double, P(C.c_double), P(C.c_double)]
+        L.lgo_atan.restype = C.c_double
+        L.lgo_atan.argtypes = [C.c_double]
         L.lgo_geo_hits.argtypes = [P(abi.lg_geo), C.c_uint32, C.c_int32, C.c_double, C.c_double,
                                    C.c_double, C.c_double, P(lgo_hit), C.c_int, P(C.c_uint32)]
         L.lgo_geo_contains.argtypes = [P(abi.lg_geo), C.c_uint32, C.c_int32, C.c_double, C.c_double]
@@ -181,3 +184,15 @@ def resolve_rgba8(acc: np.ndarray) -> np.ndarray:
     a = np.ascontiguousarray(acc)
     lib().lgo_resolve_rgba8(a.ctypes.data_as(C.POINTER(C.c_int64)), w, h, out.ctypes.data_as(C.POINTER(C.c_uint8)))
     return out
+
+
+def sincos(x: float):
+    """(sin x, cos x) of the ray generators (lg_oracle.c lgo_sincos)."""
+    s, c = C.c_double(), C.c_double()
+    lib().lgo_sincos(float(x), C.byref(s), C.byref(c))
+    return s.value, c.value
+
+
+def atan(x: float) -> float:
+    """atan of the spot-light generator (lg_oracle.c lgo_atan)."""
+    return lib().lgo_atan(float(x))

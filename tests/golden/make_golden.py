@@ -31,8 +31,8 @@ from oracle import oracle as O  # noqa: E402
 # name -> (workload factory, primary stride, whether the image digests are stored)
 CASES = {
     "plain_small_fixed64": (lambda: W.plain_small(accum=abi.LG_ACCUM_FIXED64), 1, True),
-    "mid_scene_subset": (lambda: W.mid_scene(), 32749, False),
-    "csg_scene_subset": (lambda: W.csg_scene(), 262139, False),
+    "mid_scene_subset": (lambda: W.mid_scene(), 8191, False),
+    "csg_scene_subset": (lambda: W.csg_scene(), 65521, False),
 }
 
 

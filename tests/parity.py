@@ -1,10 +1,16 @@
 """Path-keyed comparison of a GPU trace against the CPU oracle's trace.
 
-Both sides key every segment by (source, light, primary, generation, path bits).  The
-tolerances are the spec ones: hit-object ids and the set of segments match exactly
-outside the near-degenerate set (segments flagged LG_PATH_NEAR_DEGENERATE on either side,
-which includes every descendant of a flagged decision), and endpoints match within
-ENDPOINT_TOL relative to max(1, |p|).
+Both sides key every segment by (source, light, primary, generation, path bits).
+
+exact(): the bar of LG_PRECISION_EXACT.  The same segment set, and every segment's
+endpoints, colour, hit object and TIR flag equal bit for bit; nothing is excused.  The
+near-degenerate flag is reported, not compared: the oracle also raises it for decisions on
+objects the GPU's FP32 search proved irrelevant.
+
+compare(): the bar of LG_PRECISION_FAST (double-float).  Hit-object ids and the set of
+segments match exactly outside the near-degenerate set (segments flagged
+LG_PATH_NEAR_DEGENERATE on either side, which includes every descendant of a flagged
+decision), and endpoints match within ENDPOINT_TOL relative to max(1, |p|).
 """
 from __future__ import annotations
 
@@ -108,3 +114,51 @@ def rel_l2(a: np.ndarray, b: np.ndarray) -> float:
     d = np.linalg.norm((a - b).ravel())
     n = np.linalg.norm(b.ravel())
     return float(d / n) if n > 0 else float(d)
+
+
+@dataclass
+class ExactReport:
+    segments: int
+    gpu_only: int
+    oracle_only: int
+    endpoint_mismatch: int
+    color_mismatch: int
+    hit_mismatch: int
+    tir_mismatch: int
+    near_flag_differs: int  # informational
+
+    def ok(self) -> bool:
+        return (self.gpu_only == 0 and self.oracle_only == 0 and self.endpoint_mismatch == 0 and
+                self.color_mismatch == 0 and self.hit_mismatch == 0 and self.tir_mismatch == 0)
+
+
+def canonical(segs, paths):
+    order = np.lexsort((paths["path"], paths["gen"], paths["primary"], paths["light"], paths["source"]))
+    return segs[order], paths[order]
+
+
+def exact(g_segs, g_paths, o_segs, o_paths) -> ExactReport:
+    """Bit-for-bit comparison of two traces (any order on either side)."""
+    gs, gp = canonical(g_segs, g_paths)
+    os_, op = canonical(o_segs, o_paths)
+    gk = list(zip(_keys(gp).tolist(), gp["path"].tolist()))
+    ok = list(zip(_keys(op).tolist(), op["path"].tolist()))
+    if gk != ok:  # align on the keys both have
+        gi = {k: i for i, k in enumerate(gk)}
+        oi = {k: i for i, k in enumerate(ok)}
+        common = sorted(gi.keys() & oi.keys())
+        g_only, o_only = len(gi) - len(common), len(oi) - len(common)
+        ig = np.array([gi[k] for k in common], dtype=np.int64)
+        io = np.array([oi[k] for k in common], dtype=np.int64)
+        gs, gp, os_, op = gs[ig], gp[ig], os_[io], op[io]
+    else:
+        g_only = o_only = 0
+    ge = np.stack([gs["x0"], gs["y0"], gs["x1"], gs["y1"]], 1).view(np.uint32)
+    oe = np.stack([os_["x0"], os_["y0"], os_["x1"], os_["y1"]], 1).view(np.uint32)
+    return ExactReport(
+        segments=len(gs), gpu_only=g_only, oracle_only=o_only,
+        endpoint_mismatch=int((ge != oe).any(axis=1).sum()),
+        color_mismatch=int((gs["color"].view(np.uint32) != os_["color"].view(np.uint32)).any(axis=1).sum()),
+        hit_mismatch=int((gp["hit"] != op["hit"]).sum()),
+        tir_mismatch=int(((gp["flags"] ^ op["flags"]) & 2).astype(bool).sum()),
+        near_flag_differs=int(((gp["flags"] ^ op["flags"]) & NEAR).astype(bool).sum()))

@@ -107,6 +107,7 @@ def test_abi_version_and_defaults(cuda_lib):
     assert (p.alpha_blend.src_factor, p.alpha_blend.dst_factor, p.alpha_blend.op) == (
         abi.LG_BF_SRC_ALPHA, abi.LG_BF_ONE, abi.LG_BO_ADD)
     assert p.accum == abi.LG_ACCUM_FIXED64
+    assert p.precision == abi.LG_PRECISION_EXACT and (p.ray_stride, p.ray_offset) == (1, 0)
     # the Python mirror builds the same defaults
     q = abi.params_default()
     assert bytes(q) == bytes(p)

@@ -31,8 +31,11 @@ def _mixed_scenes():
     return out
 
 
-def test_batch_images_equal_scenes_rendered_alone(ctx):
+@pytest.mark.parametrize("precision", [abi.LG_PRECISION_EXACT, abi.LG_PRECISION_FAST])
+def test_batch_images_equal_scenes_rendered_alone(ctx, precision):
     scenes = _mixed_scenes()
+    for pk in scenes:
+        pk.params.precision = precision
     ctx.batch_upload(scenes)
     imgs, st = ctx.batch_render()
     segs = pix = 0

@@ -78,9 +78,11 @@ CASES = {
 }
 
 
+@pytest.mark.parametrize("precision", [abi.LG_PRECISION_EXACT, abi.LG_PRECISION_FAST])
 @pytest.mark.parametrize("name", sorted(CASES))
-def test_culled_trace_equals_full_scan(gpu, name):
+def test_culled_trace_equals_full_scan(gpu, name, precision):
     pk = CASES[name]()
+    pk.params.precision = precision
     st0, *full = _trace(pk, abi.LG_CULL_OFF)
     st1, *grid = _trace(pk, abi.LG_CULL_ON)
     _assert_same_trace(full, grid)

@@ -1,0 +1,149 @@
+"""The exact FP64 precision mode (LG_PRECISION_EXACT, the default) against the CPU oracle.
+
+In this mode the GPU evaluates the same FP64 formulas as the oracle, operation by operation,
+so a trace must equal the oracle's bit for bit: the same set of segments (keyed by source,
+light, primary, generation and path bits) with identical endpoints, colours, hit objects and
+TIR flags, and the fixed-point image of the frame identical to the oracle's CPU raster of its
+own segments.  Nothing is excused.  Full-size configurations are compared on sampled frames
+(every k-th primary of each light, lg_params.ray_stride) traced by both sides.
+"""
+import numpy as np
+import pytest
+
+from light_garden_gb300 import abi, workloads as W
+from light_garden_gb300.scene import (Circle, ConvexPolygon, CubicBezier, DirectionalLight, Ellipse, LineSegment,
+                                      Logic, Material, Object, PointLight, Rect, SpotLight, pack)
+from parity import exact
+
+pytestmark = pytest.mark.gpu
+
+
+def _trace_exact(ctx, oracle, pk, stride=1, offset=0, image=False):
+    pk.params.record_paths = 1
+    pk.params.precision = abi.LG_PRECISION_EXACT
+    pk.params.ray_stride, pk.params.ray_offset = stride, offset
+    ctx.upload(pk)
+    st = ctx.trace()
+    gs, gp = ctx.segments(paths=True)
+    os_, op, _, _ = oracle.trace(pk, ray_stride=stride, ray_offset=offset)
+    rep = exact(gs, gp, os_, op)
+    assert rep.ok(), rep
+    assert rep.segments == len(os_) == len(gs) == st["segments"]
+    if image:  # the frame's fixed-point image equals the oracle's raster of its own segments
+        ctx.accumulate()
+        acc = ctx.accum()
+        o_acc, _ = oracle.raster(os_, pk.params)
+        assert np.array_equal(acc, o_acc)
+        assert np.array_equal(ctx.resolve_f16(), oracle.resolve_f16(o_acc))
+    return st, rep
+
+
+def test_plain_small_exact_and_image(ctx, oracle):
+    st, rep = _trace_exact(ctx, oracle, W.plain_small(accum=abi.LG_ACCUM_FIXED64).packed(), image=True)
+    assert st["primary_rays"] == 4096 and rep.segments > 8000
+
+
+def test_mid_scene_full_size_sampled_exact(ctx, oracle):
+    """64 objects, 8 lights x 2^18 rays, 16 bounces, 1920x1080: every 97th primary."""
+    st, rep = _trace_exact(ctx, oracle, W.mid_scene().packed(), stride=97, offset=13, image=True)
+    assert st["primary_rays"] == sum((n - 13 + 96) // 97 for n in [1 << 18] * 8)
+    assert rep.segments > 1_000_000
+
+
+def test_csg_scene_full_size_sampled_exact(ctx, oracle):
+    """256 CSG objects, 2^22 rays, 32 bounces, 4096^2, string-mod overlay: every 257th
+    primary (the overlay is drawn with offset 0)."""
+    st, rep = _trace_exact(ctx, oracle, W.csg_scene().packed(), stride=257, offset=0, image=True)
+    assert rep.segments > 4_000_000
+
+
+def test_fixtures_reproduced_exactly(ctx, oracle):
+    """The committed oracle fixtures (written on another machine) are reproduced bit for bit
+    by the GPU: the trace does not depend on the host's math library."""
+    import json
+    from pathlib import Path
+    gold = Path(__file__).resolve().parent / "golden"
+    index = json.loads((gold / "golden.json").read_text())
+    for name, make in (("mid_scene_subset", W.mid_scene), ("csg_scene_subset", W.csg_scene)):
+        z = np.load(gold / f"{name}.npz")
+        pk = make().packed()
+        pk.params.record_paths = 1
+        pk.params.ray_stride = index[name]["stride"]
+        ctx.upload(pk)
+        ctx.trace()
+        gs, gp = ctx.segments(paths=True)
+        rep = exact(gs, gp, z["segs"], z["paths"])
+        assert rep.ok(), (name, rep)
+        assert rep.segments == len(z["segs"])
+
+
+def test_culling_grid_exact(gpu, oracle):
+    """A 300-object scene traced through the culling grid equals the oracle's brute-force
+    nearest-hit scan exactly."""
+    from light_garden_gb300.runtime import Context
+    w = max(W.batch_scenes(seed=21, count=64), key=lambda x: len(x.objects))
+    assert len(w.objects) >= 96
+    rays = sum(l.num_rays for l in w.lights)
+    for cull in (abi.LG_CULL_ON, abi.LG_CULL_OFF):
+        with Context(culling=cull) as ctx:
+            _trace_exact(ctx, oracle, w.packed(), stride=max(1, rays // 20000))
+
+
+def test_shapes_and_nested_csg_exact(ctx, oracle):
+    """Polygons, ellipses, lenses, straight and curved mirrors and a three-level Logic tree."""
+    nested = Logic(abi.LG_OP_OR,
+                   Logic(abi.LG_OP_AND_NOT, Circle((0.0, 0.0), 0.2), Rect((0.05, 0.0), 0.1, 0.1, (0.6, 0.8)),
+                         (0.0, 0.0), (1.0, 0.0)),
+                   Logic(abi.LG_OP_AND, Ellipse((0.15, 0.1), 0.12, 0.05, (0.8, -0.6)), Circle((0.2, 0.05), 0.1),
+                         (0.02, -0.01), (0.96, 0.28)),
+                   (0.3, -0.4), (0.6, 0.8))
+    objs = [
+        Object(abi.LG_OBJ_GEO, nested, Material(1.45)),
+        Object(abi.LG_OBJ_CONVEX_POLYGON, ConvexPolygon(((-0.1, -0.1), (0.12, -0.08), (0.15, 0.1), (-0.05, 0.14)),
+                                                        (-0.5, 0.3), (0.8, 0.6)), Material(1.6)),
+        Object(abi.LG_OBJ_ELLIPSE, Ellipse((0.5, 0.4), 0.15, 0.08, (0.6, 0.8)), Material(1.33)),
+        Object.new_lens((-0.3, -0.4), 0.25, 0.12),
+        Object.new_mirror((-0.9, 0.7), (-0.6, 0.95)),
+        Object.new_curved_mirror(CubicBezier(((0.6, -0.8), (0.8, -0.5), (0.9, -0.9), (0.95, -0.4)))),
+    ]
+    lights = [PointLight((-0.05, 0.02), 3000, (1.0, 0.8, 0.6, 1.0)),
+              SpotLight((0.9, 0.9), 1.2, (-1.0, -0.7), 2000, (0.3, 0.9, 0.4, 1.0)),
+              DirectionalLight((0.5, 0.5, 1.0, 1.0), 1500, LineSegment((-1.0, -0.95), (0.2, -0.95)))]
+    p = abi.params_default()
+    p.width, p.height, p.max_bounce = 800, 600, 24
+    _trace_exact(ctx, oracle, pack(objs, lights, p), image=True)
+
+
+def test_default_scene_from_ron_exact(ctx, oracle):
+    from pathlib import Path
+    from light_garden_gb300 import ron
+    objs, lights = ron.load(Path(__file__).resolve().parent / "golden" / "default_scene.ron")
+    p = abi.params_default()
+    p.width, p.height, p.max_bounce = 1024, 768, 12
+    _trace_exact(ctx, oracle, pack(objs, lights, p), image=True)
+
+
+def test_exact_rejects_trees_deeper_than_eight(ctx):
+    g = Circle((0.0, 0.0), 0.1)
+    for i in range(9):
+        g = Logic(abi.LG_OP_OR, g, Circle((0.01 * i, 0.0), 0.1))
+    pk = pack([Object(abi.LG_OBJ_GEO, g, Material(1.5))], [PointLight((-0.8, 0.0), 16, (1, 1, 1, 1))])
+    with pytest.raises(abi.LgError) as e:
+        ctx.upload(pk)
+    assert e.value.status == abi.LG_ERR_UNSUPPORTED
+    pk.params.precision = abi.LG_PRECISION_FAST
+    ctx.upload(pk)  # the double-float mode flattens any tree
+
+
+def test_batch_exact_images_equal_oracle(gpu, oracle):
+    """Exact mode in a multi-scene batch: every image equals the oracle's raster of the
+    oracle's trace of that scene."""
+    from light_garden_gb300.runtime import Context
+    scenes = [W.scale_rays(w, 1.0 / 64).packed() for w in W.batch_scenes(seed=9, count=6)]
+    with Context() as ctx:
+        ctx.batch_upload(scenes)
+        imgs, _ = ctx.batch_render()
+    for pk, img in zip(scenes, imgs):
+        os_, _, _, _ = oracle.trace(pk)
+        o_acc, _ = oracle.raster(os_, pk.params)
+        assert np.array_equal(img, oracle.resolve_f16(o_acc))

@@ -18,8 +18,11 @@ from parity import compare, rel_l2
 pytestmark = pytest.mark.gpu
 
 
-def _trace_both(ctx, oracle, packed, stride=1):
+def _trace_both(ctx, oracle, packed, stride=1, precision=abi.LG_PRECISION_FAST):
+    """The tolerance bar of the double-float mode (the exact mode has its own bit-for-bit
+    tests in test_gpu_exact.py and meets this bar trivially)."""
     packed.params.record_paths = 1
+    packed.params.precision = precision
     ctx.upload(packed)
     st = ctx.trace()
     g_segs, g_paths = ctx.segments(paths=True)
@@ -29,9 +32,13 @@ def _trace_both(ctx, oracle, packed, stride=1):
     return st, rep, (g_segs, g_paths), (o_segs, o_paths, o64)
 
 
-def test_plain_small_trace_parity(ctx, oracle):
+PRECISIONS = pytest.mark.parametrize("precision", [abi.LG_PRECISION_FAST, abi.LG_PRECISION_EXACT])
+
+
+@PRECISIONS
+def test_plain_small_trace_parity(ctx, oracle, precision):
     pk = W.plain_small().packed()
-    st, rep, (gs, gp), (os_, op, o64) = _trace_both(ctx, oracle, pk)
+    st, rep, (gs, gp), (os_, op, o64) = _trace_both(ctx, oracle, pk, precision=precision)
     assert rep.ok(), rep
     assert rep.matched == len(os_) - rep.oracle_only
     assert st["segments"] == len(gs)
@@ -39,16 +46,18 @@ def test_plain_small_trace_parity(ctx, oracle):
     assert st["primary_rays"] == 4096
 
 
-def test_mid_scene_trace_parity_subsampled(ctx, oracle):
+@PRECISIONS
+def test_mid_scene_trace_parity_subsampled(ctx, oracle, precision):
     pk = W.mid_scene(rays_per_light=1 << 14).packed()
-    st, rep, _, (os_, _, _) = _trace_both(ctx, oracle, pk, stride=7)
+    st, rep, _, (os_, _, _) = _trace_both(ctx, oracle, pk, stride=7, precision=precision)
     assert rep.ok(), rep
     assert rep.matched > 0.99 * len(os_)
 
 
-def test_csg_scene_trace_parity_subsampled(ctx, oracle):
+@PRECISIONS
+def test_csg_scene_trace_parity_subsampled(ctx, oracle, precision):
     pk = W.csg_scene(total_rays=1 << 16, width=1024, height=1024).packed()
-    st, rep, _, (os_, _, _) = _trace_both(ctx, oracle, pk, stride=5)
+    st, rep, _, (os_, _, _) = _trace_both(ctx, oracle, pk, stride=5, precision=precision)
     assert rep.ok(), rep
     assert rep.matched > 0.99 * len(os_)
 

@@ -62,6 +62,33 @@ def test_spot_light_fan(oracle):
         assert r[2:] == pytest.approx([math.cos(b), math.sin(b)], abs=1e-15)
 
 
+def _ulps(a: float, b: float) -> float:
+    """distance in units of the last place of b"""
+    return abs(a - b) / math.ulp(max(abs(b), 1e-300))
+
+
+def test_generator_sincos_and_atan_within_a_few_ulp_of_libm(oracle):
+    # the ray generators' own sin / cos / atan (plain IEEE double operations, so the oracle,
+    # the GPU and any machine produce the same bits) stay within a few ulp of the C library
+    rng = np.random.default_rng(11)
+    xs = np.concatenate([rng.uniform(-8.0, 8.0, 20000), 2 * math.pi * np.arange(4096) / 4096,
+                         [0.0, -0.0, math.pi / 4, math.pi / 2, math.pi, 1e-300, 5e-9]])
+    worst_s = worst_c = 0.0
+    for x in xs.tolist():
+        s, c = oracle.sincos(x)
+        # sin/cos near zero: measure against the ulp of 1 (absolute error of a unit vector)
+        worst_s = max(worst_s, abs(s - math.sin(x)) / math.ulp(max(abs(math.sin(x)), 0.5)))
+        worst_c = max(worst_c, abs(c - math.cos(x)) / math.ulp(max(abs(math.cos(x)), 0.5)))
+    assert worst_s <= 2.0 and worst_c <= 2.0, (worst_s, worst_c)
+    worst_a = max(_ulps(oracle.atan(x), math.atan(x))
+                  for x in np.concatenate([rng.uniform(-4, 4, 20000), 10.0 ** rng.uniform(-12, 12, 2000),
+                                           [0.2679491924311227, 1.0, -1.0, 1e300, -1e300, 0.0]]).tolist())
+    assert worst_a <= 4.0, worst_a
+    assert oracle.atan(float("inf")) == pytest.approx(math.pi / 2, abs=0) or abs(oracle.atan(float("inf")) - math.pi / 2) < 1e-15
+    s, c = oracle.sincos(0.0)
+    assert (s, c) == (0.0, 1.0)
+
+
 def test_directional_light_origins_and_normal(oracle):
     # origins evenly spaced along the segment from a, direction the unit left normal of b - a
     lt = S.DirectionalLight((1, 1, 1, 1), 4, S.LineSegment((-1.0, 0.0), (1.0, 0.0)))
