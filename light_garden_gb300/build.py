@@ -72,6 +72,14 @@ def build(verbose: bool = False, force: bool = False, extra_flags=(), lib_dir: P
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc link failed:\n{r.stdout}\n{r.stderr}")
+    # the benchmark's roofline ceilings (shared-memory atomics, FP32, FP64), measured live
+    peaks = lib_dir / "liblg_peaks.so"
+    if force or _stale(peaks, [CSRC / "lg_peaks.cu"]):
+        cmd = [cc, *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "-o", str(peaks),
+               str(CSRC / "lg_peaks.cu"), "-cudart", "static"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed on lg_peaks.cu:\n{r.stdout}\n{r.stderr}")
     return lib
 
 

@@ -866,11 +866,12 @@ __device__ __forceinline__ int cubic_roots32(const float* A, const float* Bp, fl
     if (!(u > lo && u < hi)) u = 0.5f * (lo + hi);
     for (int it = 0; it < 40; ++it) {
       const float fu = f(u);
+      if (fu == 0.0f) break;  // u is the root (the bracket update below would step off it)
       if ((fu < 0.0f) == (flo < 0.0f)) { lo = u; flo = fu; } else { hi = u; }
       const float fpu = (3.0f * a3 * u + 2.0f * a2) * u + a1;
       float un = u - fu / fpu;
       if (!(un > lo && un < hi)) un = 0.5f * (lo + hi);
-      const bool done = fabsf(un - u) <= 3e-8f || fu == 0.0f;
+      const bool done = fabsf(un - u) <= 3e-8f;
       u = un;
       if (done) break;
     }

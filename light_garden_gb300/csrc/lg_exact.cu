@@ -48,20 +48,42 @@ template __global__ void k_light_setup_x<true>(SceneDev);
 
 // ------------------------------------------------------------------ nearest hit
 // Exact hit record in HitRec's slots: t, p, n as FP64, the event parameter ev in (k, ev).
-__device__ __forceinline__ void store_hit_x(HitRec& o, int obj, const lgx::Hit& h, double ev, uint8_t flags) {
+__device__ __forceinline__ void store_hit_x(HitRec& o, int obj, const lgx::Hit& h, V n, int leaf, double ev,
+                                            uint8_t flags) {
   o.obj = obj < 0 ? HIT_NONE : (uint16_t)obj;
-  o.t = xdf(h.t); o.px = xdf(h.p.x); o.py = xdf(h.p.y); o.nx = xdf(h.n.x); o.ny = xdf(h.n.y);
+  o.t = xdf(h.t); o.px = xdf(h.p.x); o.py = xdf(h.p.y); o.nx = xdf(n.x); o.ny = xdf(n.y);
   const df e = xdf(ev);
   o.k = e.hi;
   o.ev = e.lo;
-  o.leaf = (uint8_t)h.sub;
+  o.leaf = (uint8_t)leaf;
   o.flags = flags;
+}
+
+// Nearest hit of object k (scene-global index) with the ray: the minimum distance_squared
+// over the object's hits, the first one on ties (tracer.rs:412-424 per object).  Returns
+// that distance (INFINITY: no hit).  Out of line, so the solve kernel keeps one copy of the
+// geometry code and its own registers for the ray state.
+static __device__ __noinline__ double obj_best_x(const SceneDev& S, uint32_t k, V o, V d, double& ev, lgx::Hit& best) {
+  const ObjInfo& oi = S.info[k];
+  double ob = INFINITY;
+  lgx::object_hits(S.xgeo, S.xnode + oi.xnode_begin, (int)oi.xnode_count, o, d, ev, [&](const lgx::Hit& h) {
+    const V dv = lgx::vsub(h.p, o);
+    const double d2 = lgx::dot(dv, dv);
+    if (lgx::plt(d2, ob)) {
+      ob = d2;
+      best = h;
+    }
+  });
+  return ob;
 }
 
 // Every ray with candidates (the refine lists and the full-solve list of k_scan): the
 // nearest hit over its candidates, each object solved whole as tracer.rs:412-424 does
 // (the minimum distance_squared over the object's hits, then over objects with ties kept by
-// the lower object index), and the near-degenerate flags of tracer.rs's decisions.
+// the lower object index), and the near-degenerate flags of tracer.rs's decisions.  The
+// CTA's warps take the candidates one solve class (circle, rect, segment, cubic / deep CSG,
+// two-leaf CSG) at a time, with a barrier between classes, so that one geometry code path
+// is in flight per CTA.
 template <bool MULTI>
 __global__ void __launch_bounds__(256) k_solve_x(SceneDev S, TraceBufs B, uint32_t gen) {
   __shared__ unsigned long long blk_solves;
@@ -76,45 +98,58 @@ __global__ void __launch_bounds__(256) k_solve_x(SceneDev S, TraceBufs B, uint32
   const uint64_t total = off[LIST_FULL + 1];
   const RayRec* q = B.queue[gen & 1];
   unsigned long long my_solves = 0;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-    int l = 0;
-    while (i >= off[l + 1]) ++l;
-    const uint32_t idx = B.list[l][i - off[l]];
+  // block-uniform loop (the class barrier needs every thread)
+  for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x; base < total; base += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = base + threadIdx.x;
+    const bool valid = i < total;
+    uint32_t idx = 0;
+    if (valid) {
+      int l = 0;
+      while (i >= off[l + 1]) ++l;
+      idx = B.list[l][i - off[l]];
+    }
     const RayRec r = q[idx];
     const ScanRec sc = B.scan[idx];
-    const SceneLoc sl = scene_of<MULTI>(S, r.scene);
+    const SceneLoc sl = scene_of<MULTI>(S, valid ? r.scene : 0u);
     const V o = ray_o(r), d = ray_d(r);
     double best_d2 = INFINITY, second = INFINITY, ev = INFINITY;
     int best = -1;
-    lgx::Hit bh{0.0, lgx::mk(0.0, 0.0), lgx::mk(0.0, 0.0), 0};
+    lgx::Hit bh{0.0, lgx::mk(0.0, 0.0), lgx::mk(0.0, 0.0), 0, 0};
     auto consider = [&](uint32_t j) {
-      const ObjInfo& oi = S.info[sl.base + j];
-      double ob = INFINITY;
       lgx::Hit oh;
-      bool found = false;
       ++my_solves;
-      lgx::object_hits(S.xgeo, S.xnode + oi.xnode_begin, (int)oi.xnode_count, o, d, ev, [&](const lgx::Hit& h) {
-        const V dv = lgx::vsub(h.p, o);
-        const double d2 = lgx::dot(dv, dv);
-        if (d2 < ob) {
-          ob = d2;
-          oh = h;
-          found = true;
-        }
-      });
-      if (!found) return;
-      if (ob < best_d2 || (ob == best_d2 && (int)j < best)) {
+      const double ob = obj_best_x(S, sl.base + j, o, d, ev, oh);
+      if (!lgx::plt(ob, INFINITY)) return;
+      if (lgx::plt(ob, best_d2) || (lgx::bits(ob) == lgx::bits(best_d2) && (int)j < best)) {
         second = best_d2;
         best_d2 = ob;
         best = (int)j;
         bh = oh;
-      } else if (ob < second) {
+      } else if (lgx::plt(ob, second)) {
         second = ob;
       }
     };
-    if (!sc.overflow) {
-      for (int k = 0; k < sc.nc; ++k) consider(sc.cand[k]);
-    } else {  // candidate list overflow (rare): every object that passes the FP32 filters
+    {
+      uint32_t pending = valid && !sc.overflow ? (1u << sc.nc) - 1u : 0u;
+      uint32_t cls[CAND];
+      for (int k = 0; k < CAND; ++k)
+        cls[k] = (pending >> k) & 1u ? solve_class(__ldg(&S.scan[sl.base + sc.cand[k]].info)) : 7u;
+      for (uint32_t c = 0; c < N_SOLVE_CLASSES; ++c) {
+        for (;;) {
+          int k = -1;
+          for (int kk = 0; kk < CAND; ++kk)
+            if (k < 0 && ((pending >> kk) & 1u) && cls[kk] == c) k = kk;
+          if (!__any_sync(0xffffffffu, k >= 0)) break;
+          if (k >= 0) {
+            pending &= ~(1u << k);
+            consider(sc.cand[k]);
+          }
+        }
+        __syncthreads();
+      }
+    }
+    if (!valid) continue;
+    if (sc.overflow) {  // candidate list overflow (rare): every object that passes the FP32 filters
       const ObjScan* sobjs = S.scan + sl.base;
       const float ox = (float)o.x, oy = (float)o.y, dx = (float)d.x, dy = (float)d.y;
       for (uint32_t j = 0; j < sl.n; ++j) {
@@ -129,7 +164,15 @@ __global__ void __launch_bounds__(256) k_solve_x(SceneDev S, TraceBufs B, uint32
     // tracer.rs:404,417 ties within the band, and decisions in the band before the hit
     if (best >= 0 && second < INFINITY && lgx::sub(second, best_d2) <= lgx::mul(lgx::BAND, best_d2)) fl |= lgx::NEAR;
     if (best >= 0 ? ev <= lgx::add(lgx::mul(bh.t, 1.0 + 1e-6), 1e-12) : ev < INFINITY) fl |= lgx::NEAR;
-    store_hit_x(B.hit[idx], best, bh, ev, fl);
+    V n = lgx::mk(0.0, 0.0);
+    int leaf = 0;
+    if (best >= 0) {  // the normal of the winning hit only
+      const ObjInfo& oi = S.info[sl.base + best];
+      const lgx::XNode* nd = S.xnode + oi.xnode_begin;
+      n = lgx::object_normal(S.xgeo, nd, d, bh);
+      leaf = lgx::hit_leaf(S.xgeo, nd, bh);
+    }
+    store_hit_x(B.hit[idx], best, bh, n, leaf, ev, fl);
   }
   atomicAdd(&blk_solves, my_solves);
   __syncthreads();
@@ -176,6 +219,38 @@ __device__ __forceinline__ bool refract_x(V d, V n, double n1, double n2, V& ref
   const double rs = dvd(sub(mul(n1, ci), mul(n2, ct)), ds);
   const double rp = dvd(sub(mul(n1, ct), mul(n2, ci)), dp);
   R = mul(0.5, add(mul(rs, rs), mul(rp, rp)));
+  return true;
+}
+
+// The canvas exit of a ray whose origin lies strictly inside the canvas [-aspect, aspect] x
+// [-1, 1] and whose exit is clear of the corners and of the origin: the same hit and flags as
+// the slab test of the canvas rectangle (hits_rect), which needs the far face of each axis
+// only: (sign(D) h - O) / D is the very quotient the slab test takes as its exit parameter.
+// Returns false (nothing decided) when any of those conditions fails.
+__device__ __forceinline__ bool canvas_exit_inside(V o, V d, double aspect, double& ev, lgx::Hit& first, int& nh) {
+  using namespace lgx;
+  const double h[2] = {aspect, 1.0};
+  const double O[2] = {o.x, o.y}, D[2] = {d.x, d.y};
+  double far[2];
+  float nr[2];
+  for (int ax = 0; ax < 2; ++ax) {
+    if (is_zero(D[ax]) || !(fabs(O[ax]) < h[ax])) return false;
+    far[ax] = dvd(sub(D[ax] > 0.0 ? h[ax] : -h[ax], O[ax]), D[ax]);
+    // the near face's parameter, roughly: only needed to rule out a corner-entry event
+    nr[ax] = ((float)(D[ax] > 0.0 ? -h[ax] : h[ax]) - (float)O[ax]) / (float)D[ax];
+  }
+  const double tf = far[1] < far[0] ? far[1] : far[0];
+  if (!(tf >= 1e-9)) return false;
+  // the slab test's events: a corner entry (the two near parameters within the band of each
+  // other) and an exit within the T_MIN band; the corner graze |tf - tn| <= 1e-10 (|tn| + tf + 1)
+  // cannot happen for tn < 0 <= 1e-9 <= tf
+  const float tn_abs = fmaxf(fabsf(nr[0]), fabsf(nr[1]));
+  if (!(fabsf(nr[0] - nr[1]) > 1e-6f * (tn_abs + (float)tf + 1.0f))) return false;
+  lgx::tmin_band(tf, ev);
+  if (gt_pos(tf, T_MIN)) {
+    first = mkhit(tf, o, d, mk(0.0, 0.0), 0);
+    nh = 1;
+  }
   return true;
 }
 
@@ -301,20 +376,22 @@ __device__ __forceinline__ void bounce_x(const SceneDev& S, const RayRec& r, con
     }
   } else {
     // canvas exit (tracer.rs:482-488): nearest hit with the canvas rectangle
-    lg_geo canvas;
-    canvas.kind = LG_GEO_RECT;
-    canvas.origin[0] = 0.0; canvas.origin[1] = 0.0;
-    canvas.rot[0] = 1.0; canvas.rot[1] = 0.0;
     const double aspect = MULTI ? S.scenes[r.scene].aspect64 : S.aspect64;
-    canvas.v[0] = mul(2.0, aspect);
-    canvas.v[1] = 2.0;
     double cev = INFINITY;
     int nh = 0;
-    Hit first{INFINITY, mk(0.0, 0.0), mk(0.0, 0.0), 0};
-    hits_rect(canvas, o, d, cev, [&](const Hit& h) {
-      if (nh == 0 || h.t < first.t) first = h;
-      ++nh;
-    });
+    Hit first{INFINITY, mk(0.0, 0.0), mk(0.0, 0.0), 0, 0};
+    if (!canvas_exit_inside(o, d, aspect, cev, first, nh)) {
+      lg_geo canvas;
+      canvas.kind = LG_GEO_RECT;
+      canvas.origin[0] = 0.0; canvas.origin[1] = 0.0;
+      canvas.rot[0] = 1.0; canvas.rot[1] = 0.0;
+      canvas.v[0] = mul(2.0, aspect);
+      canvas.v[1] = 2.0;
+      hits_rect(canvas, o, d, cev, [&](const Hit& h) {
+        if (nh == 0 || h.t < first.t) first = h;
+        ++nh;
+      });
+    }
     if (nh > 0) {
       v.emit = true;
       v.x1 = (float)first.p.x;
@@ -365,7 +442,7 @@ __device__ __forceinline__ void emit_segments_x(const SceneDev& S, const TraceBu
 }
 
 template <bool MULTI, bool CULL>
-__global__ void __launch_bounds__(256) k_bounce_x(SceneDev S, TraceBufs B, uint32_t gen) {
+__global__ void __launch_bounds__(256, 2) k_bounce_x(SceneDev S, TraceBufs B, uint32_t gen) {
   __shared__ unsigned long long blk_visits, blk_near;
   if (threadIdx.x == 0) { blk_visits = 0; blk_near = 0; }
   __syncthreads();

@@ -59,11 +59,38 @@ __device__ __forceinline__ V irot(V a, double c, double s) {
   return mk(add(mul(c, a.x), mul(s, a.y)), add(mul(-s, a.x), mul(c, a.y)));
 }
 
+// A hit as the object solve keeps it.  The normal is computed later, for the winning hit
+// only (object_normal), from what the leaf leaves here, with the same operations the
+// immediate computation would take.
 struct Hit {
   double t;
-  V p, n;
-  int sub;  // polygon: the edge that was hit (its leaf is the node's leaf_ord + sub)
+  V p;       // the hit point, o + t d of the ray in the frame the caller passed (world after
+             // object_hits lifts it through the Logic frames)
+  V aux;     // circle: the point in the circle's frame; ellipse: the point in the ellipse's
+             // own frame; cubic: (curve parameter, 0)
+  int node;  // preorder index of the leaf within its object
+  int sub;   // rect: face (axis + 2 if the outward normal points along +axis); polygon: edge
 };
+
+// Comparisons on the integer pipe (FP64 compares issue on the 1/64-rate FP64 pipe), each
+// equal to the IEEE comparison for the values it is given.
+__device__ __forceinline__ long long bits(double x) { return __double_as_longlong(x); }
+// a < b for a, b in [+0, +inf] (distances squared, curve parameters): the bit patterns of
+// non-negative doubles order like the values
+__device__ __forceinline__ bool plt(double a, double b) { return bits(a) < bits(b); }
+// t > c for a constant 0 < c < inf: false for every negative t, -0 and NaN
+__device__ __forceinline__ bool gt_pos(double t, double c) {
+  const long long b = bits(t);
+  return b > bits(c) && b <= 0x7ff0000000000000ll;
+}
+// lo < t < hi for constants 0 < lo < hi < inf
+__device__ __forceinline__ bool in_pos(double t, double lo, double hi) {
+  const long long b = bits(t);
+  return b > bits(lo) && b < bits(hi);
+}
+// x < 0.0 and x == 0.0 for finite or infinite x (not NaN)
+__device__ __forceinline__ bool is_neg(double x) { return bits(x) < 0 && (bits(x) << 1) != 0; }
+__device__ __forceinline__ bool is_zero(double x) { return (bits(x) << 1) == 0; }
 
 // Near-degenerate decision events: the smallest ray parameter at which a decision (hit or
 // no hit, which side of a boundary) fell inside the band.
@@ -72,9 +99,11 @@ __device__ __forceinline__ void event(double& ev, double t) {
   if (t < ev) ev = t;
 }
 __device__ __forceinline__ void tmin_band(double t, double& ev) {
-  if (t > 1e-2 * T_MIN && t < 1e2 * T_MIN) event(ev, t);
+  if (in_pos(t, 1e-2 * T_MIN, 1e2 * T_MIN)) event(ev, t);
 }
-__device__ __forceinline__ Hit mkhit(double t, V o, V d, V n) { return Hit{t, vadd(o, vscl(d, t)), n, 0}; }
+__device__ __forceinline__ Hit mkhit(double t, V o, V d, V aux, int sub) {
+  return Hit{t, vadd(o, vscl(d, t)), aux, 0, sub};
+}
 
 // ------------------------------------------------------------------ ray generators
 // sin / cos and atan from published methods in plain double operations (the same bits on
@@ -235,7 +264,8 @@ static __device__ __noinline__ bool leaf_contains(const lg_geo* G, const lg_geo&
 }
 
 // ------------------------------------------------------------------ leaves: hits
-// Each calls emit(Hit) for every hit with t > T_MIN, in collision2d order.
+// Each calls emit(Hit) for every hit with t > T_MIN, in collision2d order; the normals are
+// left to leaf_normal.
 template <class F>
 __device__ __forceinline__ void hits_circle(const lg_geo& g, V o, V d, double& ev, F&& emit) {
   const V c = mk(g.origin[0], g.origin[1]);
@@ -244,11 +274,11 @@ __device__ __forceinline__ void hits_circle(const lg_geo& g, V o, V d, double& e
   const double a = dot(d, d), b = dot(oc, d), cc = sub(dot(oc, oc), mul(r, r));
   const double disc = sub(mul(b, b), mul(a, cc));
   if (fabs(disc) <= mul(BAND, add(mul(b, b), fabs(mul(a, cc)))) && dvd(-b, a) > -T_MIN) event(ev, dvd(-b, a));
-  if (disc < 0.0) return;
+  if (is_neg(disc)) return;
   const double sq = sqr(disc);
   const double q = -add(b, b >= 0.0 ? sq : -sq);
   double t1, t2;
-  if (q != 0.0) {
+  if (!is_zero(q)) {
     t1 = dvd(q, a);
     t2 = dvd(cc, q);
   } else {
@@ -258,9 +288,9 @@ __device__ __forceinline__ void hits_circle(const lg_geo& g, V o, V d, double& e
   const double ts[2] = {t1, t2};
   for (int k = 0; k < 2; ++k) {
     tmin_band(ts[k], ev);
-    if (ts[k] > T_MIN) {
+    if (gt_pos(ts[k], T_MIN)) {
       const V p = vadd(o, vscl(d, ts[k]));
-      emit(mkhit(ts[k], o, d, vscl(vsub(p, c), dvd(1.0, r))));
+      emit(Hit{ts[k], p, p, 0, 0});
     }
   }
 }
@@ -269,18 +299,22 @@ template <class F>
 __device__ __forceinline__ void hits_segment(V A, V Bp, V o, V d, double& ev, F&& emit) {
   const V e = vsub(Bp, A);
   const double den = cross(d, e);
-  const double le = sqr(dot(e, e)), ld = sqr(dot(d, d));
   const V w = vsub(A, o);
-  if (fabs(den) <= mul(mul(BAND, le), ld)) event(ev, den != 0.0 ? dvd(cross(w, e), den) : 0.0);
-  if (den == 0.0) return;
+  // |den| <= BAND |e| |d| needs both lengths (square roots) only when |den| is that small:
+  // |e| <= |ex| + |ey| and |d| <= |dx| + |dy|, so a |den| above twice that bound settles it
+  const float lb = 2e-10f * ((float)fabs(e.x) + (float)fabs(e.y)) * ((float)fabs(d.x) + (float)fabs(d.y));
+  if (!(lb > 1e-30f) || !((float)fabs(den) > lb)) {
+    const double le = sqr(dot(e, e)), ld = sqr(dot(d, d));
+    if (fabs(den) <= mul(mul(BAND, le), ld)) event(ev, !is_zero(den) ? dvd(cross(w, e), den) : 0.0);
+  }
+  if (is_zero(den)) return;
   const double t = dvd(cross(w, e), den);
   const double u = dvd(cross(w, d), den);
   if (fabs(u) <= BAND || fabs(sub(u, 1.0)) <= BAND) event(ev, t);
-  if (u < 0.0 || u > 1.0) return;
+  if (is_neg(u) || u > 1.0) return;
   tmin_band(t, ev);
-  if (!(t > T_MIN)) return;
-  const V nrm = le > 0.0 ? mk(dvd(-e.y, le), dvd(e.x, le)) : mk(0.0, 0.0);
-  emit(mkhit(t, o, d, nrm));
+  if (!gt_pos(t, T_MIN)) return;
+  emit(mkhit(t, o, d, mk(0.0, 0.0), 0));
 }
 
 template <class F>
@@ -295,7 +329,7 @@ __device__ __forceinline__ void hits_rect(const lg_geo& g, V o, V d, double& ev,
   double sn = 0.0, sf = 0.0;  // outward sign of the entry / exit face
   double tn_other = -INFINITY;
   for (int ax = 0; ax < 2; ++ax) {
-    if (D[ax] == 0.0) {
+    if (is_zero(D[ax])) {
       if (fabs(sub(fabs(O[ax]), h[ax])) <= mul(BAND, h[ax])) event(ev, 0.0);
       if (fabs(O[ax]) > h[ax]) return;
       continue;
@@ -312,12 +346,10 @@ __device__ __forceinline__ void hits_rect(const lg_geo& g, V o, V d, double& ev,
   if (fabs(sub(tf, tn)) <= mul(BAND, scale)) event(ev, tn);                          // corner graze
   if (tn_other > -INFINITY && fabs(sub(tn, tn_other)) <= mul(BAND, scale)) event(ev, tn);  // corner entry
   if (tn > tf) return;
-  const V nn = an == 0 ? mk(sn, 0.0) : mk(0.0, sn);
-  const V nf = af == 0 ? mk(sf, 0.0) : mk(0.0, sf);
   tmin_band(tn, ev);
-  if (tn > T_MIN) emit(mkhit(tn, o, d, rot(nn, c, s)));
+  if (gt_pos(tn, T_MIN)) emit(mkhit(tn, o, d, mk(0.0, 0.0), an + (sn > 0.0 ? 2 : 0)));
   tmin_band(tf, ev);
-  if (tf > T_MIN) emit(mkhit(tf, o, d, rot(nf, c, s)));
+  if (gt_pos(tf, T_MIN)) emit(mkhit(tf, o, d, mk(0.0, 0.0), af + (sf > 0.0 ? 2 : 0)));
 }
 
 // cubic in power basis: B(s) = c3 s^3 + c2 s^2 + c1 s + c0
@@ -339,16 +371,23 @@ __device__ __forceinline__ double poly3(const double* a, double s) {
 __device__ __forceinline__ V cubic_point(const Cubic& k, double s) {
   return vadd(vadd(vadd(vscl(k.c3, mul(mul(s, s), s)), vscl(k.c2, mul(s, s))), vscl(k.c1, s)), k.c0);
 }
+__device__ __forceinline__ V cubic_tangent(const Cubic& k, double s) {
+  return vadd(vadd(vscl(k.c3, mul(mul(3.0, s), s)), vscl(k.c2, mul(2.0, s))), k.c1);
+}
 __device__ __forceinline__ double cubic_t(const Cubic& k, double s, V o, V d) {
   return dvd(dot(vsub(cubic_point(k, s), o), d), dot(d, d));
 }
+// Bisection to full precision between knots lo < hi in [0, 1] (f(lo) = flo != 0).  The
+// bracket and midpoints are non-negative, and the tests are on sign bits: integer work, the
+// same decisions as the FP64 comparisons.
 static __device__ __noinline__ double bisect_root(const double* a, double lo, double hi, double flo) {
+  const bool neg_lo0 = is_neg(flo);
   for (int it = 0; it < 200; ++it) {
     const double mid = mul(0.5, add(lo, hi));
-    if (mid <= lo || mid >= hi) break;
+    if (!plt(lo, mid) || !plt(mid, hi)) break;
     const double fm = poly3(a, mid);
-    if (fm == 0.0) return mid;
-    if ((fm < 0) == (flo < 0)) { lo = mid; flo = fm; } else hi = mid;
+    if (is_zero(fm)) return mid;
+    if (is_neg(fm) == neg_lo0) lo = mid; else hi = mid;
   }
   return mul(0.5, add(lo, hi));
 }
@@ -387,15 +426,15 @@ __device__ __forceinline__ void hits_cubic(const lg_geo& g, V o, V d, double& ev
     const double lo = knots[i], hi = knots[i + 1];
     const double flo = poly3(a, lo), fhi = poly3(a, hi);
     if (i > 0 && fabs(flo) <= mul(BAND, scale)) event(ev, cubic_t(k, lo, o, d));  // tangency
-    if (flo == 0.0) {
+    if (is_zero(flo)) {
       if (nr == 0 || roots[nr - 1] != lo) roots[nr++] = lo;
       continue;
     }
-    if (fhi == 0.0) {
+    if (is_zero(fhi)) {
       if (i + 2 == nk) roots[nr++] = hi;
       continue;
     }
-    if ((flo < 0) != (fhi < 0)) roots[nr++] = bisect_root(a, lo, hi, flo);
+    if (is_neg(flo) != is_neg(fhi)) roots[nr++] = bisect_root(a, lo, hi, flo);
   }
   if (fabs(a[0]) <= mul(BAND, scale)) event(ev, cubic_t(k, 0.0, o, d));  // end points
   if (fabs(poly3(a, 1.0)) <= mul(BAND, scale)) event(ev, cubic_t(k, 1.0, o, d));
@@ -405,12 +444,10 @@ __device__ __forceinline__ void hits_cubic(const lg_geo& g, V o, V d, double& ev
     const V B = cubic_point(k, s);
     const double t = dvd(dot(vsub(B, o), d), dd);
     tmin_band(t, ev);
-    if (!(t > T_MIN)) continue;
-    const V dB = vadd(vadd(vscl(k.c3, mul(mul(3.0, s), s)), vscl(k.c2, mul(2.0, s))), k.c1);
-    const double l = sqr(dot(dB, dB));
-    if (l == 0.0) event(ev, t);
-    const V nrm = l > 0.0 ? mk(dvd(-dB.y, l), dvd(dB.x, l)) : unit(mk(-d.y, d.x));
-    emit(mkhit(t, o, d, nrm));
+    if (!gt_pos(t, T_MIN)) continue;
+    const V dB = cubic_tangent(k, s);
+    if (is_zero(dot(dB, dB))) event(ev, t);  // |B'(s)| == 0: the normal falls back to the ray's
+    emit(mkhit(t, o, d, mk(s, 0.0), 0));
   }
 }
 
@@ -418,17 +455,11 @@ template <class F>
 __device__ __forceinline__ void hits_polygon(const lg_geo* G, const lg_geo& g, V o, V d, double& ev, F&& emit) {
   V P[MAX_POLY];
   const int n = poly_vertices(G, g, P);
-  const double sgn = poly_orientation(P, n);
   const double c = g.rot[0], s = g.rot[1];
   const V org = mk(g.origin[0], g.origin[1]);
   const V lo = irot(vsub(o, org), c, s), ld = irot(d, c, s);
-  for (int i = 0; i < n; ++i) {
-    hits_segment(P[i], P[(i + 1) % n], lo, ld, ev, [&](const Hit& h) {
-      const V e = vsub(P[(i + 1) % n], P[i]);
-      const V nrm = unit(vscl(mk(e.y, -e.x), sgn));  // outward
-      emit(Hit{h.t, vadd(o, vscl(d, h.t)), rot(nrm, c, s), i});
-    });
-  }
+  for (int i = 0; i < n; ++i)
+    hits_segment(P[i], P[(i + 1) % n], lo, ld, ev, [&](const Hit& h) { emit(mkhit(h.t, o, d, mk(0.0, 0.0), i)); });
 }
 
 template <class F>
@@ -440,11 +471,11 @@ __device__ __forceinline__ void hits_ellipse(const lg_geo& g, V o, V d, double& 
   const double a = dot(sd, sd), b = dot(so, sd), cc = sub(dot(so, so), 1.0);
   const double disc = sub(mul(b, b), mul(a, cc));
   if (fabs(disc) <= mul(BAND, add(mul(b, b), fabs(mul(a, cc)))) && dvd(-b, a) > -T_MIN) event(ev, dvd(-b, a));
-  if (disc < 0.0) return;
+  if (is_neg(disc)) return;
   const double sq = sqr(disc);
   const double q = -add(b, b >= 0.0 ? sq : -sq);
   double t1 = 0.0, t2 = 0.0;
-  if (q != 0.0) {
+  if (!is_zero(q)) {
     t1 = dvd(q, a);
     t2 = dvd(cc, q);
   }
@@ -452,11 +483,7 @@ __device__ __forceinline__ void hits_ellipse(const lg_geo& g, V o, V d, double& 
   const double ts[2] = {t1, t2};
   for (int k = 0; k < 2; ++k) {
     tmin_band(ts[k], ev);
-    if (ts[k] > T_MIN) {
-      const V pl = vadd(lo, vscl(ld, ts[k]));
-      const V gr = unit(mk(dvd(pl.x, mul(A, A)), dvd(pl.y, mul(Bb, Bb))));
-      emit(mkhit(ts[k], o, d, rot(gr, c, s)));
-    }
+    if (gt_pos(ts[k], T_MIN)) emit(mkhit(ts[k], o, d, vadd(lo, vscl(ld, ts[k])), 0));
   }
 }
 
@@ -470,6 +497,46 @@ __device__ __forceinline__ void leaf_hits(const lg_geo* G, const lg_geo& g, V o,
     case LG_GEO_POLYGON: hits_polygon(G, g, o, d, ev, emit); break;
     case LG_GEO_ELLIPSE: hits_ellipse(g, o, d, ev, emit); break;
     default: break;
+  }
+}
+
+// The normal of a leaf's hit (collision2d's formulas: (p - c) / r, the rect face, the unit
+// left normal of a segment, the unit left normal of B'(s), a polygon edge's outward unit
+// normal, the normalised gradient of an ellipse), in the leaf's parent frame.  d: the ray
+// direction in that frame (the cubic's fallback when B'(s) = 0).
+static __device__ __noinline__ V leaf_normal(const lg_geo* G, const lg_geo& g, const Hit& h, V d) {
+  switch (g.kind) {
+    case LG_GEO_CIRCLE:
+      return vscl(vsub(h.aux, mk(g.origin[0], g.origin[1])), dvd(1.0, g.v[0]));
+    case LG_GEO_RECT: {
+      const double sg = (h.sub & 2) ? 1.0 : -1.0;
+      const V nn = (h.sub & 1) == 0 ? mk(sg, 0.0) : mk(0.0, sg);
+      return rot(nn, g.rot[0], g.rot[1]);
+    }
+    case LG_GEO_SEGMENT: {
+      const V e = vsub(mk(g.v[2], g.v[3]), mk(g.v[0], g.v[1]));
+      const double le = sqr(dot(e, e));
+      return le > 0.0 ? mk(dvd(-e.y, le), dvd(e.x, le)) : mk(0.0, 0.0);
+    }
+    case LG_GEO_CUBIC: {
+      const V dB = cubic_tangent(cubic_of(g.v), h.aux.x);
+      const double l = sqr(dot(dB, dB));
+      return l > 0.0 ? mk(dvd(-dB.y, l), dvd(dB.x, l)) : unit(mk(-d.y, d.x));
+    }
+    case LG_GEO_POLYGON: {
+      V P[MAX_POLY];
+      const int n = poly_vertices(G, g, P);
+      const double sgn = poly_orientation(P, n);
+      const V e = vsub(P[(h.sub + 1) % n], P[h.sub]);
+      return rot(unit(vscl(mk(e.y, -e.x), sgn)), g.rot[0], g.rot[1]);
+    }
+    case LG_GEO_ELLIPSE: {
+      const double A = g.v[0], Bb = g.v[1];
+      const V gr = unit(mk(dvd(h.aux.x, mul(A, A)), dvd(h.aux.y, mul(Bb, Bb))));
+      return rot(gr, g.rot[0], g.rot[1]);
+    }
+    default:
+      return mk(0.0, 0.0);
   }
 }
 
@@ -519,19 +586,15 @@ static __device__ __noinline__ bool subtree_contains(const lg_geo* G, const XNod
 }
 
 // All hits of one object's tree with the ray (o, d) in world coordinates, in collision2d
-// order (a Logic node lists child a's kept hits, then child b's), each passed to
-// emit(Hit) in world coordinates.  A child hit survives a Logic node when the other child's
-// membership (at the hit point in the node's frame) makes it a boundary of the
-// combination; surviving points and normals move to the parent's frame.
+// order (a Logic node lists child a's kept hits, then child b's), each passed to emit(Hit)
+// with its point in world coordinates.  A child hit survives a Logic node when the other
+// child's membership (at the hit point in the node's frame) makes it a boundary of the
+// combination; surviving points move to the parent's frame.
 template <class F>
 __device__ __forceinline__ void object_hits(const lg_geo* G, const XNode* nd, int nn, V o, V d, double& ev,
                                             F&& emit) {
   if (nn == 1) {
-    const uint32_t lo = nd[0].leaf_ord;
-    leaf_hits(G, G[nd[0].geo], o, d, ev, [&](Hit h) {
-      h.sub += (int)lo;
-      emit(h);
-    });
+    leaf_hits(G, G[nd[0].geo], o, d, ev, emit);
     return;
   }
   V ro[MAX_DEPTH + 1], rd[MAX_DEPTH + 1];
@@ -546,7 +609,7 @@ __device__ __forceinline__ void object_hits(const lg_geo* G, const XNode* nd, in
       continue;
     }
     leaf_hits(G, g, ro[D], rd[D], ev, [&](Hit h) {
-      h.sub += (int)nd[i].leaf_ord;
+      h.node = i;
       int cur = i, j = nd[i].parent;
       while (j >= 0) {
         const lg_geo& L = G[nd[j].geo];
@@ -558,15 +621,30 @@ __device__ __forceinline__ void object_hits(const lg_geo* G, const XNode* nd, in
         if (cfl) event(ev, h.t);
         const bool keep = L.op == LG_OP_AND ? in_other : L.op == LG_OP_OR ? !in_other : (from_a ? !in_other : in_other);
         if (!keep) return;
-        const double c = L.rot[0], s = L.rot[1];
-        h.p = vadd(mk(L.origin[0], L.origin[1]), rot(h.p, c, s));
-        h.n = rot(h.n, c, s);
+        h.p = vadd(mk(L.origin[0], L.origin[1]), rot(h.p, L.rot[0], L.rot[1]));
         cur = j;
         j = nd[j].parent;
       }
       emit(h);
     });
   }
+}
+
+// The world normal of a hit object_hits reported: the leaf's normal, rotated out through the
+// Logic frames above it (the ray direction is taken down the same frames for the cubic's
+// fallback).
+__device__ __forceinline__ V object_normal(const lg_geo* G, const XNode* nd, V d, const Hit& h) {
+  int chain[MAX_DEPTH + 1];
+  int nc = 0;
+  for (int j = nd[h.node].parent; j >= 0 && nc <= MAX_DEPTH; j = nd[j].parent) chain[nc++] = j;
+  for (int k = nc - 1; k >= 0; --k) d = irot(d, G[nd[chain[k]].geo].rot[0], G[nd[chain[k]].geo].rot[1]);
+  V n = leaf_normal(G, G[nd[h.node].geo], h, d);
+  for (int k = 0; k < nc; ++k) n = rot(n, G[nd[chain[k]].geo].rot[0], G[nd[chain[k]].geo].rot[1]);
+  return n;
+}
+// The leaf number (in the flattened leaf table) of a hit.
+__device__ __forceinline__ int hit_leaf(const lg_geo* G, const XNode* nd, const Hit& h) {
+  return (int)nd[h.node].leaf_ord + (G[nd[h.node].geo].kind == LG_GEO_POLYGON ? h.sub : 0);
 }
 
 __device__ __forceinline__ bool object_contains_tree(const lg_geo* G, const XNode* nd, int nn, V p, uint32_t* fl) {
