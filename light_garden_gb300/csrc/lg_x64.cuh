@@ -9,8 +9,8 @@
 // collision2d's primitives as this project restates them (the geometry crate is not
 // available): circle by the cancellation-free quadratic (Numerical Recipes 5.6), rect by
 // the slab test in its frame, segment by the 2x2 parametric solve, cubic Bezier by the
-// sign changes of cross(d, B(s) - o) between the roots of its derivative, bisected to full
-// precision, ellipse through the unit circle of its scaled frame, convex polygon as its edge
+// sign changes of cross(d, B(s) - o) between the roots of its derivative, each solved by
+// safeguarded Newton, ellipse through the unit circle of its scaled frame, convex polygon as its edge
 // segments, CSG (Logic) with the children in the node's local frame.
 //
 // Native FP64 issues at 1/64 of the FP32 rate on GB300, so this mode runs only where the
@@ -377,19 +377,33 @@ __device__ __forceinline__ V cubic_tangent(const Cubic& k, double s) {
 __device__ __forceinline__ double cubic_t(const Cubic& k, double s, V o, V d) {
   return dvd(dot(vsub(cubic_point(k, s), o), d), dot(d, d));
 }
-// Bisection to full precision between knots lo < hi in [0, 1] (f(lo) = flo != 0).  The
-// bracket and midpoints are non-negative, and the tests are on sign bits: integer work, the
-// same decisions as the FP64 comparisons.
-static __device__ __noinline__ double bisect_root(const double* a, double lo, double hi, double flo) {
-  const bool neg_lo0 = is_neg(flo);
-  for (int it = 0; it < 200; ++it) {
+// The root of f between knots lo < hi in [0, 1] (f(lo) = flo != 0, f(hi) of the other sign):
+// ten bisection steps, then Newton steps from the bracket's midpoint kept inside the bracket
+// (a step that leaves it bisects instead) until a step moves it by 1e-15 or less or after
+// eight steps (Numerical Recipes 9.4, rtsafe).  The bracket and the points tried are
+// non-negative, so the comparisons run on the integer pipe with the FP64 comparisons' results.
+static __device__ __noinline__ double cubic_root(const double* a, double lo, double hi, double flo) {
+  const bool neg_lo = is_neg(flo);
+  for (int it = 0; it < 10; ++it) {
     const double mid = mul(0.5, add(lo, hi));
-    if (!plt(lo, mid) || !plt(mid, hi)) break;
+    if (!plt(lo, mid) || !plt(mid, hi)) return mid;
     const double fm = poly3(a, mid);
     if (is_zero(fm)) return mid;
-    if (is_neg(fm) == neg_lo0) lo = mid; else hi = mid;
+    if (is_neg(fm) == neg_lo) lo = mid; else hi = mid;
   }
-  return mul(0.5, add(lo, hi));
+  double s = mul(0.5, add(lo, hi));
+  for (int it = 0; it < 8; ++it) {
+    const double f = poly3(a, s);
+    if (is_zero(f)) return s;
+    if (is_neg(f) == neg_lo) lo = s; else hi = s;
+    const double fp = add(mul(add(mul(mul(3.0, a[3]), s), mul(2.0, a[2])), s), a[1]);
+    double sn = sub(s, dvd(f, fp));
+    if (!(plt(lo, sn) && plt(sn, hi))) sn = mul(0.5, add(lo, hi));
+    const double step = sub(sn, s);
+    s = sn;
+    if (fabs(step) <= 1e-15) break;
+  }
+  return s;
 }
 
 template <class F>
@@ -434,7 +448,7 @@ __device__ __forceinline__ void hits_cubic(const lg_geo& g, V o, V d, double& ev
       if (i + 2 == nk) roots[nr++] = hi;
       continue;
     }
-    if (is_neg(flo) != is_neg(fhi)) roots[nr++] = bisect_root(a, lo, hi, flo);
+    if (is_neg(flo) != is_neg(fhi)) roots[nr++] = cubic_root(a, lo, hi, flo);
   }
   if (fabs(a[0]) <= mul(BAND, scale)) event(ev, cubic_t(k, 0.0, o, d));  // end points
   if (fabs(poly3(a, 1.0)) <= mul(BAND, scale)) event(ev, cubic_t(k, 1.0, o, d));

@@ -13,7 +13,8 @@
  *   rect         slab test in the rect's local frame; entry and exit are both hits.
  *   segment      2x2 parametric solve, u in [0, 1]; normal = unit left normal of b - a.
  *   cubic        f(s) = cross(d, B(s) - o) on [0, 1], split at the roots of f', each
- *                sign change bisected to full precision; normal = perp(B'(s)).
+ *                sign change solved by safeguarded Newton (ten bisection steps, then Newton
+ *                kept inside the bracket, Numerical Recipes 9.4); normal = perp(B'(s)).
  *   logic        children hit in the node's local frame, kept when the other child's
  *                membership makes the point a boundary of the combination:
  *                And: other inside; Or: other outside; AndNot: a-hits with b outside,
@@ -271,15 +272,32 @@ static double cubic_t(const cubic* k, double s, v2 o, v2 d) {
   return dot(sub(B, o), d) / dot(d, d);
 }
 
-static double bisect_root(const double* a, double lo, double hi, double flo) {
-  for (int it = 0; it < 200; ++it) {
+/* The root of f (monotone on [lo, hi], f(lo) = flo != 0 and f(hi) of the other sign):
+ * ten bisection steps, then Newton steps from the bracket's midpoint, each kept inside the
+ * bracket (a step that leaves it bisects instead), until a step moves the root by 1e-15 or
+ * less or after eight steps (Numerical Recipes 9.4, rtsafe). */
+static double cubic_root(const double* a, double lo, double hi, double flo) {
+  const int neg_lo = flo < 0;
+  for (int it = 0; it < 10; ++it) {
     double mid = 0.5 * (lo + hi);
-    if (mid <= lo || mid >= hi) break;
+    if (mid <= lo || mid >= hi) return mid;
     double fm = poly3(a, mid);
     if (fm == 0.0) return mid;
-    if ((fm < 0) == (flo < 0)) { lo = mid; flo = fm; } else hi = mid;
+    if ((fm < 0) == neg_lo) lo = mid; else hi = mid;
   }
-  return 0.5 * (lo + hi);
+  double s = 0.5 * (lo + hi);
+  for (int it = 0; it < 8; ++it) {
+    double f = poly3(a, s);
+    if (f == 0.0) return s;
+    if ((f < 0) == neg_lo) lo = s; else hi = s;
+    double fp = (3.0 * a[3] * s + 2.0 * a[2]) * s + a[1];
+    double sn = s - f / fp;
+    if (!(sn > lo && sn < hi)) sn = 0.5 * (lo + hi);
+    double step = sn - s;
+    s = sn;
+    if (fabs(step) <= 1e-15) break;
+  }
+  return s;
 }
 
 static int hits_cubic(const lg_geo* g, v2 o, v2 d, ohit* out, int cap, double* ev) {
@@ -323,7 +341,7 @@ static int hits_cubic(const lg_geo* g, v2 o, v2 d, ohit* out, int cap, double* e
       if (i + 2 == nk) roots[nr++] = hi;
       continue;
     }
-    if ((flo < 0) != (fhi < 0)) roots[nr++] = bisect_root(a, lo, hi, flo);
+    if ((flo < 0) != (fhi < 0)) roots[nr++] = cubic_root(a, lo, hi, flo);
   }
   if (fabs(a[0]) <= BAND * scale) event(ev, cubic_t(&k, 0.0, o, d)); /* end points */
   if (fabs(poly3(a, 1.0)) <= BAND * scale) event(ev, cubic_t(&k, 1.0, o, d));
