@@ -42,7 +42,7 @@ extern "C" {
 /* 2: lg_device_opts gained culling and grid_density, lg_trace_stats bound_tests and
  * object_tests (both structs grew).
  * 3: lg_device_opts gained wait_polls; lg_params.precision (was padding), ray_stride and
- *    ray_offset (lg_params grew). */
+ *    ray_offset (lg_params grew); lg_trace_stats scan_ms, solve_ms, bounce_ms (grew). */
 #define LG_ABI_VERSION 3
 
 typedef enum lg_status {
@@ -235,6 +235,10 @@ typedef struct lg_trace_stats {
   /* device time from CUDA events on the library's stream; lg_render splits accumulate
      into bin (count, scan, scatter) and raster (tile accumulation) */
   float trace_ms, accumulate_ms, resolve_ms, total_ms, bin_ms, raster_ms;
+  /* lg_render: the trace's kernels summed over the generations: the FP32 nearest-hit search,
+     the precise solve (k_solve_x, or k_refine + k_full), the bounce */
+  float scan_ms, solve_ms, bounce_ms;
+  float _pad2;
 } lg_trace_stats;
 
 typedef struct lg_device_opts {

@@ -100,7 +100,8 @@ class lg_trace_stats(C.Structure):
                 ("bound_tests", C.c_uint64), ("object_tests", C.c_uint64),
                 ("retries", C.c_uint32), ("_pad", C.c_uint32),
                 ("trace_ms", C.c_float), ("accumulate_ms", C.c_float), ("resolve_ms", C.c_float),
-                ("total_ms", C.c_float), ("bin_ms", C.c_float), ("raster_ms", C.c_float)]
+                ("total_ms", C.c_float), ("bin_ms", C.c_float), ("raster_ms", C.c_float),
+                ("scan_ms", C.c_float), ("solve_ms", C.c_float), ("bounce_ms", C.c_float), ("_pad2", C.c_float)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_ if not name.startswith("_")}

@@ -737,13 +737,22 @@ void launch_light_setup(lg_ctx* c, const SceneDev& S, bool multi, int blocks) {
   }
 }
 
+// Events around one generation's kernels (kev_on: lg_render), k = 0 before the scan, 1
+// after it, 2 after the precise solve, 3 after the bounce.
+static void kernel_event(lg_ctx* c, uint32_t g, int k) {
+  if (c->kev_on && 4 * g + k < c->kev.size()) cudaEventRecordWithFlags(c->kev[4 * g + k], c->stream, cudaEventRecordExternal);
+}
+
 void launch_generation(lg_ctx* c, const SceneDev& S, const TraceBufs& B, uint32_t g, bool multi, int scan_grid,
                        size_t scan_smem, size_t tsm, int smem_fits) {
   const bool exact = c->prm.precision == LG_PRECISION_EXACT;
+  kernel_event(c, g, 0);
   scan_kernel(multi, c->culled, exact)<<<scan_grid, SCAN_THREADS, scan_smem, c->stream>>>(S, B, g, smem_fits);
+  kernel_event(c, g, 1);
   if (exact) {
     if (multi) k_solve_x<true><<<c->trace_grid[4], 256, 0, c->stream>>>(S, B, g);
     else k_solve_x<false><<<c->trace_grid[4], 256, 0, c->stream>>>(S, B, g);
+    kernel_event(c, g, 2);
     bounce_x_kernel(multi, c->culled)<<<c->trace_grid[5], 256, 0, c->stream>>>(S, B, g);
   } else {
     if (multi) {
@@ -753,8 +762,35 @@ void launch_generation(lg_ctx* c, const SceneDev& S, const TraceBufs& B, uint32_
       k_refine<false><<<c->trace_grid[1], 256, 0, c->stream>>>(S, B, g);
       k_full<false><<<c->trace_grid[2], 256, tsm, c->stream>>>(S, B, g, smem_fits);
     }
+    kernel_event(c, g, 2);
     bounce_kernel(multi, c->culled)<<<c->trace_grid[3], 256, tsm, c->stream>>>(S, B, g, smem_fits);
   }
+  kernel_event(c, g, 3);
+}
+
+// Per-kernel trace times of the last lg_render, from the kernel events of every generation.
+static void kernel_times(lg_ctx* c, lg_trace_stats* s) {
+  if (!s || !c->kev_on) return;
+  float a = 0.f, b = 0.f, d = 0.f;
+  for (uint32_t g = 0; g < c->prm.max_bounce && 4 * g + 3 < c->kev.size(); ++g) {
+    a += elapsed(c->kev[4 * g], c->kev[4 * g + 1]);
+    b += elapsed(c->kev[4 * g + 1], c->kev[4 * g + 2]);
+    d += elapsed(c->kev[4 * g + 2], c->kev[4 * g + 3]);
+  }
+  s->scan_ms = a;
+  s->solve_ms = b;
+  s->bounce_ms = d;
+}
+
+// lg_render's graphs record the kernel events (created once per context).
+static lg_status enable_kernel_events(lg_ctx* c) {
+  if (c->kev.empty()) {
+    c->kev.assign(4 * MAX_GEN, nullptr);
+    for (auto& e : c->kev) CK(cudaEventCreate(&e), "event");
+  }
+  if (!c->kev_on) c->graph_valid = false;  // the captured graph must record them
+  c->kev_on = true;
+  return LG_OK;
 }
 
 lg_status upload_exact(lg_ctx* c, const Flat& F) {
@@ -1049,6 +1085,8 @@ lg_status lg_destroy(lg_ctx* c) {
   for (int i = 0; i < 6; ++i)
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   for (cudaEvent_t e : c->bev)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : c->kev)
     if (e) cudaEventDestroy(e);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -1394,6 +1432,7 @@ static lg_status render_streaming(lg_ctx* c, uint16_t* dst, size_t pitch, int32_
       stats->raster_ms = ac;
       stats->resolve_ms = elapsed(ev[2 * G], ev[1 + 2 * G]);
       stats->total_ms = elapsed(ev[0], ev[1 + 2 * G]);
+      kernel_times(c, stats);
     }
     return LG_OK;
   }
@@ -1406,6 +1445,7 @@ lg_status lg_render(lg_ctx* c, uint16_t* dst, size_t pitch, int32_t dst_is_devic
   const size_t row = (size_t)c->prm.width * 8;
   if (!dst || pitch < row) return fail(c, LG_ERR_INVALID_ARGUMENT, "destination null or pitch < width * 8");
   uint32_t retries = 0;
+  if ((st = enable_kernel_events(c))) return st;
   if (c->streaming) return render_streaming(c, dst, pitch, dst_is_device, stats, retries);
   if (c->raster_variant == 0) {  // pick the raster kernel before it is baked into the graph
     st = run_trace(c, retries, c->stream_ring);
@@ -1481,6 +1521,7 @@ lg_status lg_render(lg_ctx* c, uint16_t* dst, size_t pitch, int32_t dst_is_devic
       stats->accumulate_ms = elapsed(c->ev[1], c->ev[3]);
       stats->resolve_ms = elapsed(c->ev[3], c->ev[4]);
       stats->total_ms = elapsed(c->ev[0], c->ev[4]);
+      kernel_times(c, stats);
     }
     return LG_OK;
   }

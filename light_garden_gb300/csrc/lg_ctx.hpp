@@ -85,6 +85,10 @@ struct lg_ctx {
   uint64_t n_overlay = 0;
   int batch_grid_scan = 0;
   std::vector<cudaEvent_t> bev;          // batch stage events (start, per generation x 2, resolved)
+  // lg_render: events around the trace kernels of every generation (before the scan, after
+  // the scan, after the solve, after the bounce), recorded while kev_on
+  std::vector<cudaEvent_t> kev;
+  bool kev_on = false;
   ServeState* serve = nullptr;           // serving mode (lg_serve_begin .. lg_serve_end)
 };
 
