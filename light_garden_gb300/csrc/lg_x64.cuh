@@ -379,9 +379,10 @@ __device__ __forceinline__ double cubic_t(const Cubic& k, double s, V o, V d) {
 }
 // The root of f between knots lo < hi in [0, 1] (f(lo) = flo != 0, f(hi) of the other sign):
 // ten bisection steps, then Newton steps from the bracket's midpoint kept inside the bracket
-// (a step that leaves it bisects instead) until a step moves it by 1e-15 or less or after
-// eight steps (Numerical Recipes 9.4, rtsafe).  The bracket and the points tried are
-// non-negative, so the comparisons run on the integer pipe with the FP64 comparisons' results.
+// (a step that leaves it bisects instead) until a step moves it by 1e-15 or less (Numerical
+// Recipes 9.4, rtsafe); if twelve steps do not get there, bisection of the remaining bracket
+// to full precision.  The bracket and the points tried are non-negative, so the comparisons
+// run on the integer pipe with the FP64 comparisons' results.
 static __device__ __noinline__ double cubic_root(const double* a, double lo, double hi, double flo) {
   const bool neg_lo = is_neg(flo);
   for (int it = 0; it < 10; ++it) {
@@ -392,7 +393,7 @@ static __device__ __noinline__ double cubic_root(const double* a, double lo, dou
     if (is_neg(fm) == neg_lo) lo = mid; else hi = mid;
   }
   double s = mul(0.5, add(lo, hi));
-  for (int it = 0; it < 8; ++it) {
+  for (int it = 0; it < 12; ++it) {
     const double f = poly3(a, s);
     if (is_zero(f)) return s;
     if (is_neg(f) == neg_lo) lo = s; else hi = s;
@@ -401,9 +402,16 @@ static __device__ __noinline__ double cubic_root(const double* a, double lo, dou
     if (!(plt(lo, sn) && plt(sn, hi))) sn = mul(0.5, add(lo, hi));
     const double step = sub(sn, s);
     s = sn;
-    if (fabs(step) <= 1e-15) break;
+    if (fabs(step) <= 1e-15) return s;
   }
-  return s;
+  for (int it = 0; it < 200; ++it) {
+    const double mid = mul(0.5, add(lo, hi));
+    if (!plt(lo, mid) || !plt(mid, hi)) return mid;
+    const double fm = poly3(a, mid);
+    if (is_zero(fm)) return mid;
+    if (is_neg(fm) == neg_lo) lo = mid; else hi = mid;
+  }
+  return mul(0.5, add(lo, hi));
 }
 
 template <class F>

@@ -14,7 +14,8 @@
  *   segment      2x2 parametric solve, u in [0, 1]; normal = unit left normal of b - a.
  *   cubic        f(s) = cross(d, B(s) - o) on [0, 1], split at the roots of f', each
  *                sign change solved by safeguarded Newton (ten bisection steps, then Newton
- *                kept inside the bracket, Numerical Recipes 9.4); normal = perp(B'(s)).
+ *                kept inside the bracket, Numerical Recipes 9.4, finished by bisection when
+ *                it does not converge); normal = perp(B'(s)).
  *   logic        children hit in the node's local frame, kept when the other child's
  *                membership makes the point a boundary of the combination:
  *                And: other inside; Or: other outside; AndNot: a-hits with b outside,
@@ -275,7 +276,8 @@ static double cubic_t(const cubic* k, double s, v2 o, v2 d) {
 /* The root of f (monotone on [lo, hi], f(lo) = flo != 0 and f(hi) of the other sign):
  * ten bisection steps, then Newton steps from the bracket's midpoint, each kept inside the
  * bracket (a step that leaves it bisects instead), until a step moves the root by 1e-15 or
- * less or after eight steps (Numerical Recipes 9.4, rtsafe). */
+ * less (Numerical Recipes 9.4, rtsafe); if twelve steps do not get there, bisection of the
+ * remaining bracket to full precision. */
 static double cubic_root(const double* a, double lo, double hi, double flo) {
   const int neg_lo = flo < 0;
   for (int it = 0; it < 10; ++it) {
@@ -286,7 +288,7 @@ static double cubic_root(const double* a, double lo, double hi, double flo) {
     if ((fm < 0) == neg_lo) lo = mid; else hi = mid;
   }
   double s = 0.5 * (lo + hi);
-  for (int it = 0; it < 8; ++it) {
+  for (int it = 0; it < 12; ++it) {
     double f = poly3(a, s);
     if (f == 0.0) return s;
     if ((f < 0) == neg_lo) lo = s; else hi = s;
@@ -295,9 +297,16 @@ static double cubic_root(const double* a, double lo, double hi, double flo) {
     if (!(sn > lo && sn < hi)) sn = 0.5 * (lo + hi);
     double step = sn - s;
     s = sn;
-    if (fabs(step) <= 1e-15) break;
+    if (fabs(step) <= 1e-15) return s;
   }
-  return s;
+  for (int it = 0; it < 200; ++it) {
+    double mid = 0.5 * (lo + hi);
+    if (mid <= lo || mid >= hi) return mid;
+    double fm = poly3(a, mid);
+    if (fm == 0.0) return mid;
+    if ((fm < 0) == neg_lo) lo = mid; else hi = mid;
+  }
+  return 0.5 * (lo + hi);
 }
 
 static int hits_cubic(const lg_geo* g, v2 o, v2 d, ohit* out, int cap, double* ev) {
