@@ -1,21 +1,30 @@
 """Benchmark of the trace-and-accumulate path on GB300.
 
-Workload (one step = one frame of the mid-size scene): 64 objects (rect / circle / flat
-mirror / curved mirror, seed 2), 8 lights x 2^18 primary rays, 16 bounces, 1920x1080
-canvas, int64 fixed-point accumulation, resolve to RGBA16F.
+One step is one frame of the CSG-heavy scene, the largest configuration that runs on one GPU:
+256 CSG objects (circle And / Or / AndNot rect, seed 3), 8 lights sharing 2^22 primary rays,
+32 bounces, a string-mod overlay of 4096 chords (i -> 7 i mod 4096), 4096 x 4096 int64
+fixed-point accumulation, resolve to RGBA16F, exact FP64 precision.  The frame's 1.5 G
+segments exceed one accumulation pass, so the library accumulates between generations.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload csg|mid] [--precision exact|fast] [--no-extras] [--no-cpu-baseline]
 
-``value``: traced segments per second over the whole job (all ranks), device time of the
-captured graph (trace + bin + raster + resolve) from CUDA events on the library's stream,
-L2 flushed between steps.  ``e2e``: the same metric through the public C ABI with host
-buffers (scene tables uploaded from the host and the RGBA16F image read back every step).
-``--impl reference`` times the CPU restatement of the reference tracer (the reference is
-Rust and cannot be built here) on all host cores over a bounded sample of primaries.
+``value``: traced segments per second over the whole job (all ranks), from CUDA events on
+the library's stream around the captured frame graph, with the L2 flushed (a 512 MB write)
+before every step.  ``e2e``: the same metric through the public C ABI with host buffers
+(scene tables uploaded from the host and the RGBA16F image read back into pinned host
+memory every step).  ``roofline``: the frame's longest kernel stage against the ceiling of
+the resource it uses, measured in the same process (liblg_peaks.so).  ``cpu_baseline``: the
+CPU restatement of the reference tracer (the reference is Rust and cannot be built) on all
+host cores over a sample of the primaries, and the GPU's image of the same sample compared
+with it.  The extra keys (``mid_scene``, ``fast_precision``, ``batch``, ``serve``) measure the
+other configurations on the same GPU.
+``--impl reference`` times that CPU restatement alone, one sample per step.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import statistics
@@ -29,22 +38,56 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "traced segments/s + accumulated px/s on 1 GB300; p50/p99 scene latency vs plain"
-# DRAM bytes (read + write) per accumulated pixel of k_raster, measured with ncu on the
-# quarter-size mid scene (a scaled constant, not a live measurement)
-RASTER_DRAM_BYTES_PER_PIXEL = 3.43
 CULL = {"auto": 0, "off": 1, "on": 2}  # lg_culling
 PRECISION = {"exact": 0, "fast": 1}  # lg_precision
 
-WORKLOAD = ("mid_scene: 64 objects (rect/circle/mirror/curved mirror, seed 2), 8 lights x 2^18 rays, "
-            "16 bounces, 1920x1080, int64 Q31.32 accumulation, RGBA16F resolve")
+WORKLOADS = {
+    "csg": "csg_scene: 256 CSG objects (circle op rect, ops And/Or/AndNot, seed 3), 8 lights, 2^22 rays, "
+           "32 bounces, 4096x4096, int64 Q31.32 accumulation, string-mod overlay m=4096 k=7, RGBA16F resolve",
+    "mid": "mid_scene: 64 objects (rect/circle/mirror/curved mirror, seed 2), 8 lights x 2^18 rays, "
+           "16 bounces, 1920x1080, int64 Q31.32 accumulation, RGBA16F resolve",
+}
+BATCH_WORKLOAD = ("batch: 512 seeded scenes (seed 4): objects log-uniform [4, 1024], rays log-uniform [2^12, 2^20], "
+                  "bounces U{4..32}, canvases {256, 512, 1024, 2048}^2, int64 accumulation")
+# CPU samples (primary stride per light): the baseline leg ~10-20 s, a reference-arm step ~5 s
+CPU_STRIDE = {"csg": 1024, "mid": 16}
+REF_STRIDE = {"csg": 2048, "mid": 32}
+
+# Instructions per unit of work of the trace kernels and the tile raster in the exact mode,
+# counted with ncu (smsp__sass_thread_inst_executed_op_{fadd,fmul,ffma,dadd,dmul,dfma}
+# _pred_on.sum and smsp__sass_inst_executed_op_shared_atom.sum over one frame of a small case
+# of the same workload: csg 2^18 rays at 1024^2, mid 2^14 rays per light).
+#   scan:   FP32 thread instructions per ray visit
+#   solve:  FP64 thread instructions per object solved (lg_trace_stats.fp64_solves)
+#   bounce: FP64 thread instructions per ray visit
+#   raster: shared-memory atomic warp instructions per accumulated pixel
+INST_PER_UNIT = {
+    "csg": {"scan": 694.3, "solve": 189.2, "bounce": 124.7, "raster": 0.2807},
+    "mid": {"scan": 968.7, "solve": 91.6, "bounce": 64.8, "raster": 0.3003},
+}
 
 
-def peaks():
+def measured_hbm():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
-        d = json.loads(p.read_text())
-        return float(d["hbm_gbs"]), "measured"
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+class PeaksLib(C.Structure):
+    _fields_ = [("smem_atomics_per_s", C.c_double), ("fp32_fma_per_s", C.c_double), ("fp64_op_per_s", C.c_double),
+                ("n_sm", C.c_int32), ("status", C.c_int32)]
+
+
+def live_peaks(device: int) -> dict:
+    """Throughput ceilings measured on this GPU now (light_garden_gb300/csrc/lg_peaks.cu)."""
+    lib = C.CDLL(str(ROOT / "light_garden_gb300" / "_lib" / "liblg_peaks.so"))
+    lib.lgp_measure.argtypes = [C.c_int, C.POINTER(PeaksLib)]
+    p = PeaksLib()
+    if lib.lgp_measure(device, C.byref(p)) != 0:
+        raise RuntimeError(f"lgp_measure failed: {p.status}")
+    return {"smem_atomics_per_s": p.smem_atomics_per_s, "fp32_fma_per_s": p.fp32_fma_per_s,
+            "fp64_op_per_s": p.fp64_op_per_s}
 
 
 class ClockSampler:
@@ -106,10 +149,9 @@ def dist_setup():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if ws > 1:
-        import torch.distributed as dist
         import torch
-        backend = "nccl" if torch.cuda.is_available() else "gloo"
-        dist.init_process_group(backend)
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     return ws, rank, local
 
 
@@ -130,23 +172,88 @@ def allmax(ws, v: float, device) -> float:
 
 
 def aggregate(ws: int, units: int, ms: float, device) -> tuple:
-    """Whole-job throughput of ``ws`` replicas that each processed ``units`` in ``ms``:
-    the slowest rank's time bounds the job (max over ranks)."""
+    """Whole-job throughput of ``ws`` replicas that each processed ``units`` in ``ms``: the
+    slowest rank's time bounds the job (max over ranks)."""
     ms_max = allmax(ws, ms, device)
     return ws * units / (ms_max * 1e-3), ms_max
 
 
-def cpu_sample(stride: int):
-    """Oracle (CPU restatement of tracer.rs) on a bounded sample: trace + raster."""
+def packed_workload(name: str, precision: str, ray_scale: float = 1.0):
     from light_garden_gb300 import workloads as W
+    if name == "csg":
+        pk = W.csg_scene(total_rays=max(8, int(round((1 << 22) * ray_scale)))).packed()
+    else:
+        pk = W.mid_scene(rays_per_light=max(1, int(round((1 << 18) * ray_scale)))).packed()
+    pk.params.precision = PRECISION[precision]
+    return pk
+
+
+# ------------------------------------------------------------------------ CPU restatement
+def cpu_sample(name: str, stride: int):
+    """Oracle (CPU restatement of tracer.rs) on every stride-th primary: trace + raster."""
     from oracle import oracle as O
-    pk = W.mid_scene().packed()
+    pk = packed_workload(name, "exact")
     t0 = time.perf_counter()
-    segs, _, _, st = O.trace(pk, ray_stride=stride, threads=0)
+    segs, paths, _, st = O.trace(pk, ray_stride=stride, threads=0)
     t1 = time.perf_counter()
-    _, px = O.raster(segs, pk.params, threads=0)
+    acc, px = O.raster(segs, pk.params, threads=0)
     t2 = time.perf_counter()
-    return len(segs), px, t1 - t0, t2 - t1, int(st.primary_rays)
+    return pk, segs, paths, acc, px, t1 - t0, t2 - t1, int(st.primary_rays)
+
+
+def sample_parity(pk, stride, o_segs, o_paths, o_acc, local):
+    """The GPU's trace and image of the same sampled frame against the CPU restatement's:
+    exact mode bit for bit; the FP32 accumulation and the double-float trace as errors."""
+    import numpy as np
+    from light_garden_gb300 import abi
+    from light_garden_gb300.runtime import Context
+    from oracle import oracle as O
+    sys.path.insert(0, str(ROOT / "tests"))
+    from parity import exact
+
+    def rel(a, b):
+        a = a.astype(np.float64).ravel()
+        b = b.astype(np.float64).ravel()
+        n1, n2 = np.abs(b).sum(), np.sqrt((b * b).sum())
+        return float(np.abs(a - b).sum() / n1), float(np.sqrt(((a - b) ** 2).sum()) / n2)
+
+    out = {"sample": f"every {stride}th primary of each light"}
+    orig = abi.lg_params.from_buffer_copy(pk.params)
+    with Context(device=local) as ctx:
+        pk.params.record_paths = 1
+        pk.params.ray_stride, pk.params.ray_offset = stride, 0
+        pk.params.precision = abi.LG_PRECISION_EXACT
+        ctx.upload(pk)
+        ctx.trace()
+        gs, gp = ctx.segments(paths=True)
+        rep = exact(gs, gp, o_segs, o_paths)
+        ctx.accumulate()
+        acc = ctx.accum()
+        out["exact"] = {"segments": rep.segments, "bit_exact_segments": rep.ok(),
+                        "image_bit_exact": bool(np.array_equal(acc, o_acc)),
+                        "near_flag_differs": rep.near_flag_differs}
+        del acc
+        scale = 2.0 ** -32
+        # the FP64 image of the oracle's segments: the reference for the accumulation error
+        f64, _ = O.raster_f64(o_segs, pk.params)
+        l1, l2 = rel(o_acc.astype(np.float64) * scale, f64)
+        out["fixed64_vs_fp64_raster"] = {"rel_l1": l1, "rel_l2": l2}
+        pk.params.accum = abi.LG_ACCUM_F32
+        ctx.upload(pk)
+        ctx.accumulate_segments(o_segs)
+        l1, l2 = rel(ctx.accum(), f64)
+        out["fp32_accum_vs_fp64_raster"] = {"rel_l1": l1, "rel_l2": l2}
+        # the double-float trace of the same sample, accumulated in fixed point
+        pk.params.accum = abi.LG_ACCUM_FIXED64
+        pk.params.precision = abi.LG_PRECISION_FAST
+        pk.params.record_paths = 0
+        ctx.upload(pk)
+        ctx.trace()
+        ctx.accumulate()
+        l1, l2 = rel(ctx.accum().astype(np.float64) * scale, f64)
+        out["fast_precision_image_vs_fp64"] = {"rel_l1": l1, "rel_l2": l2}
+    pk.params = orig
+    return out
 
 
 def run_reference(args, ws, rank):
@@ -154,330 +261,165 @@ def run_reference(args, ws, rank):
         return
     from oracle import oracle as O
     O.build()
-    stride = args.cpu_stride
-    cores = os.cpu_count()
-    for _ in range(args.warmup):
-        cpu_sample(stride)
+    stride = REF_STRIDE[args.workload]
     times, nseg, npx, nprim = [], 0, 0, 0
+    for _ in range(args.warmup):
+        cpu_sample(args.workload, stride)
     for _ in range(args.steps):
-        n, px, tt, tr, prim = cpu_sample(stride)
+        _, segs, _, _, px, tt, tr, prim = cpu_sample(args.workload, stride)
         times.append(tt + tr)
-        nseg, npx, nprim = n, px, prim
+        nseg, npx, nprim = len(segs), px, prim
     step_s = statistics.mean(times)
     value = nseg / step_s
-    sample = (f"every {stride}th primary ray of each light ({nprim} of {8 << 18} primaries) traced and "
-              f"rasterised per step: {nseg} segments, {npx} pixel updates")
+    sample = (f"every {stride}th primary ray of each light ({nprim} primaries) traced and rasterised per step: "
+              f"{nseg} segments, {npx} pixel updates")
     out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "segments/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample": sample},
+        "config": {"workload": WORKLOADS[args.workload], "sample": sample},
         "px_per_s": npx / step_s,
-        "cpu_baseline": {"value": value, "unit": "segments/s", "cores": cores, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "segments/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": sample},
         "e2e": {"value": value, "unit": "segments/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "the reference is Rust (no toolchain) and its geometry crate is not vendored; this is the C "
-                "restatement of tracer.rs timed on the host cores",
+        "note": "the reference is Rust (no toolchain here) and its geometry crate is not vendored; this is the C "
+                "restatement of tracer.rs (oracle/lg_oracle.c) timed on all host cores",
     }
     print(json.dumps(out), flush=True)
 
 
-def run_ours(args, ws, rank, local):
-    import ctypes as C
-
+# ------------------------------------------------------------------------ frames on the GPU
+def frame_bench(pk, local, steps, warmup, args, clocks=True):
+    """Frames of one packed scene through lg_render: device time per step (CUDA events in
+    the frame graph), L2 flushed before each step."""
     import torch
-
-    from light_garden_gb300 import abi, workloads as W
     from light_garden_gb300.runtime import Context
-
-    torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    w = W.mid_scene(rays_per_light=args.rays_per_light)
-    pk = w.packed()
-    pk.params.precision = PRECISION[args.precision]
     Wd, Hd = pk.params.width, pk.params.height
-    ctx = Context(device=local, raster_variant=args.raster_variant, culling=CULL[args.culling], grid_density=args.grid_density)
+    ctx = Context(device=local, raster_variant=args.raster_variant, culling=CULL[args.culling],
+                  grid_density=args.grid_density)
     ctx.upload(pk)
-    out_dev = torch.empty((Hd, Wd * 4), dtype=torch.int16, device=dev)
-    out_host = torch.empty((Hd, Wd * 4), dtype=torch.int16, pin_memory=True)
+    out = torch.empty((Hd, Wd * 4), dtype=torch.int16, device=dev)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
-    pitch = Wd * 8
-    for _ in range(max(3, args.warmup)):
-        st = ctx.render_into(out_dev.data_ptr(), pitch, True)
+    for _ in range(max(1, warmup)):
+        st = ctx.render_into(out.data_ptr(), Wd * 8, True)
     torch.cuda.synchronize()
-    launches_per_step = 1 + 4 * pk.params.max_bounce + 1 + 7  # light setup, 4 per generation, overlay, raster chain
-
-    barrier(ws)
-    torch.cuda.synchronize()
-    stage = {k: 0.0 for k in ("trace_ms", "bin_ms", "raster_ms", "resolve_ms", "total_ms")}
-    segs = pixels = refs = visits = solves = 0
-    with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            flush.zero_()  # write 512 MB > L2 between steps (not timed)
+    keys = ("trace_ms", "bin_ms", "raster_ms", "resolve_ms", "total_ms", "scan_ms", "solve_ms", "bounce_ms")
+    tot = {k: 0.0 for k in keys}
+    sampler = ClockSampler(local) if clocks else None
+    if sampler:
+        sampler.__enter__()
+    try:
+        for _ in range(steps):
+            flush.zero_()  # write 512 MB > L2 before every step (not timed)
             torch.cuda.synchronize()
-            st = ctx.render_into(out_dev.data_ptr(), pitch, True)
-            for k in stage:
-                stage[k] += st[k]
-            segs, pixels, refs, visits, solves = (st["segments"], st["pixels"], st["tile_refs"], st["ray_visits"],
-                                                  st["fp64_solves"])
+            st = ctx.render_into(out.data_ptr(), Wd * 8, True)
+            for k in keys:
+                tot[k] += st[k]
+    finally:
+        if sampler:
+            sampler.__exit__(None, None, None)
     torch.cuda.synchronize()
-    barrier(ws)
-    ms = stage["total_ms"] / args.steps
-    value, ms_max = aggregate(ws, segs, ms, dev)
-    px_per_s = ws * pixels / (ms_max * 1e-3)
-    avg = {k: v / args.steps for k, v in stage.items()}
-
-    # end to end through the C ABI: scene tables from the host, image back to pinned host memory
-    h2d = C.sizeof(abi.lg_geo) * pk.n_geo + C.sizeof(abi.lg_object) * pk.n_objects + \
-        C.sizeof(abi.lg_light) * pk.n_lights + C.sizeof(abi.lg_params)
-    d2h = Hd * Wd * 8
-    ctx.upload(pk)
-    ctx.render_into(out_host.data_ptr(), pitch, False)
-    barrier(ws)
-    e2e_times = []
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ctx.upload(pk)
-        st = ctx.render_into(out_host.data_ptr(), pitch, False)
-        e2e_times.append(time.perf_counter() - t0)
-    e2e_value, e2e_ms = aggregate(ws, st["segments"], statistics.mean(e2e_times) * 1e3, dev)
-    e2e_s = e2e_ms * 1e-3
-
-    # Roofline of the dominant kernel.  k_raster (one launch per frame) is the longest
-    # single kernel; the trace is 7 kernels per generation.  Algorithmic bytes per
-    # accumulated pixel: an int64 RGBA read-modify-write, 32 B read + 32 B written.  The
-    # launch is timed live by CUDA events recorded in the captured graph around it.
-    # DRAM traffic per accumulated pixel comes from an ncu capture of a quarter-size case
-    # (traffic scales with pixels).
-    hbm, peak_kind = peaks()
-    alg = 64.0 * pixels
-    achieved = alg / (avg["raster_ms"] * 1e-3) / 1e9
-    traffic = RASTER_DRAM_BYTES_PER_PIXEL * pixels
-    roof = {"bound": "hbm", "kernel": "k_raster<0> (tile accumulation, shared-memory atomics)",
-            "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
-            "peak_source": peak_kind, "algorithmic_bytes": alg,
-            "note": "the read-modify-write runs in shared memory; DRAM traffic is the segment and reference "
-                    "reads plus one flush per tile unit"}
-    trace_fp32 = {"kernel": "k_scan/k_refine/k_full/k_bounce (trace, all generations)", "ms": avg["trace_ms"],
-                  "ray_visits": visits, "ns_per_visit": avg["trace_ms"] * 1e6 / max(1, visits),
-                  "culling": args.culling, "bound_tests": st["bound_tests"], "object_tests": st["object_tests"],
-                  # the trace's unit of work: FP32 ray / object tests per second of trace time
-                  "bound_tests_per_s": st["bound_tests"] / (avg["trace_ms"] * 1e-3),
-                  "object_tests_per_s": st["object_tests"] / (avg["trace_ms"] * 1e-3)}
-
-    cpu = None
-    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        n, px, tt, tr, prim = cpu_sample(args.cpu_stride)
-        cpu = {"value": n / (tt + tr), "unit": "segments/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"every {args.cpu_stride}th primary of each light ({prim} primaries): {n} segments "
-                         f"traced in {tt:.2f} s and rasterised ({px} px) in {tr:.2f} s",
-               "trace_segments_per_s": n / tt, "raster_px_per_s": px / tr}
-    if rank == 0:
-        out = {
-            "metric": METRIC, "value": value, "unit": "segments/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": max(3, args.warmup), "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "fp64+fp32 trace, int64 accumulate", "data": "synthetic",
-            "config": {"workload": WORKLOAD if args.rays_per_light == 1 << 18 else
-                       WORKLOAD.replace("2^18 rays", f"{args.rays_per_light} rays"),
-                       "l2": "flushed between steps (512 MB write); working set > L2",
-                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
-            "px_per_s": px_per_s,
-            "segments_per_step": segs, "pixels_per_step": pixels, "tile_refs_per_step": refs,
-            "ray_visits_per_step": visits, "fp64_solves_per_step": solves,
-            "stage_ms": avg,
-            "roofline": roof,
-            "trace": trace_fp32,
-            "cpu_baseline": cpu,
-            "e2e": {"value": e2e_value, "unit": "segments/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "ms_per_step": e2e_s * 1e3},
-            "gpu_launches": launches_per_step * args.steps,
-            "clocks": clk.summary(),
-        }
-        print(json.dumps(out), flush=True)
-    ctx.close()
+    avg = {k: v / steps for k, v in tot.items()}
+    return ctx, st, avg, (sampler.summary() if sampler else None)
 
 
-BATCH_WORKLOAD = ("batch: 512 seeded scenes (seed 4): objects log-uniform [4, 1024], rays log-uniform [2^12, 2^20], "
-                  "bounces U{4..32}, canvases {256, 512, 1024, 2048}^2, int64 accumulation")
+def rooflines(name, st, avg, peaks, hbm):
+    """Each kernel stage against the ceiling of the resource it uses (exact mode)."""
+    ipu = INST_PER_UNIT[name]
+    vis, solves, px = st["ray_visits"], st["fp64_solves"], st["pixels"]
+    r = {}
+
+    def entry(kernel, bound, inst, ms, peak, unit_name, note):
+        achieved = inst / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
+        return {"kernel": kernel, "bound": bound, "achieved": achieved, "peak": peak / 1e9, "unit": unit_name,
+                "frac": achieved / (peak / 1e9) if peak else None, "traffic": None, "ms": ms, "peak_source":
+                "measured live (liblg_peaks.so)", "note": note}
+
+    r["scan"] = entry("k_scan (FP32 nearest-hit search)", "fp32_pipe", ipu["scan"] * vis, avg["scan_ms"],
+                      peaks["fp32_fma_per_s"], "G FP32 inst/s",
+                      f"{ipu['scan']} FP32 instructions per ray visit (ncu count) x {vis} visits")
+    r["solve"] = entry("k_solve_x (exact FP64 nearest hit)", "fp64_pipe", ipu["solve"] * solves, avg["solve_ms"],
+                       peaks["fp64_op_per_s"], "G FP64 inst/s",
+                       f"{ipu['solve']} FP64 instructions per object solve (ncu count) x {solves} solves")
+    r["bounce"] = entry("k_bounce_x (exact FP64 bounce and canvas exit)", "fp64_pipe", ipu["bounce"] * vis,
+                        avg["bounce_ms"], peaks["fp64_op_per_s"], "G FP64 inst/s",
+                        f"{ipu['bounce']} FP64 instructions per ray visit (ncu count) x {vis} visits")
+    ra = entry("k_raster (tile accumulation in shared memory)", "smem_atomics", ipu["raster"] * 32 * px,
+               avg["raster_ms"], peaks["smem_atomics_per_s"], "G shared atomics/s",
+               f"{ipu['raster'] * 32:.2f} shared-memory atomic lane operations per pixel (ncu count) x {px} pixels")
+    ra["hbm_equivalent"] = {"achieved_gbs": 64.0 * px / (avg["raster_ms"] * 1e-3) / 1e9, "peak_gbs": hbm[0],
+                            "note": "64 B per pixel (an int64 RGBA read-modify-write) if the update went through "
+                                    "HBM; the update runs in shared memory, so this can exceed 1 of the copy "
+                                    "bandwidth (" + hbm[1] + ")"}
+    r["raster"] = ra
+    return r
 
 
-def run_batch(args, ws, rank, local):
-    """Mixed-size batch: all scenes in one multi-scene trace (lg_batch_render, one captured
-    graph) against the plain path rendering the same scenes one after another (lg_render)."""
+def batch_bench(local, args, ray_scale=1.0 / 16):
+    """512 mixed scenes: one multi-scene trace (lg_batch_render) against the plain path
+    (lg_render of each scene in turn), at a fraction of the rays."""
     import torch
-
     from light_garden_gb300 import workloads as W
     from light_garden_gb300.runtime import Context
-
-    torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    ws_ = W.batch_scenes(count=args.batch_scenes)
-    if args.ray_scale != 1.0:
-        ws_ = [W.scale_rays(w, args.ray_scale) for w in ws_]
-    scenes = [w.packed() for w in ws_]
+    scenes = [W.scale_rays(w, ray_scale).packed() for w in W.batch_scenes(count=512)]
+    for pk in scenes:
+        pk.params.precision = PRECISION[args.precision]
     n = len(scenes)
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
-    # batched path
-    ctx = Context(device=local, raster_variant=args.raster_variant, culling=CULL[args.culling], grid_density=args.grid_density)
+    ctx = Context(device=local, culling=CULL[args.culling])
     ctx.batch_upload(scenes)
     out = torch.empty(ctx.batch_pixels() * 4, dtype=torch.int16, device=dev)
-    for _ in range(max(1, args.warmup)):
+    ctx.batch_render_into(out.data_ptr(), out.numel() * 2, True)
+    ms = []
+    for _ in range(2):
         st = ctx.batch_render_into(out.data_ptr(), out.numel() * 2, True)
-    torch.cuda.synchronize()
-    barrier(ws)
-    tot = 0.0
-    with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            st = ctx.batch_render_into(out.data_ptr(), out.numel() * 2, True)
-            tot += st["total_ms"]
-    ms = tot / args.steps
-    value, ms_max = aggregate(ws, n, ms, dev)
-    # end to end: scene tables from the host, every image back to pinned host memory
-    host = torch.empty(out.numel(), dtype=torch.int16, pin_memory=True)
-    t0 = time.perf_counter()
-    ctx.batch_upload(scenes)
-    ctx.batch_render_into(host.data_ptr(), host.numel() * 2, False)
-    e2e_s = time.perf_counter() - t0
-    e2e_value, _ = aggregate(ws, n, e2e_s * 1e3, dev)
-    segs, pixels = st["segments"], st["pixels"]
+        ms.append(st["total_ms"])
     ctx.close()
-    # plain path: the same scenes one by one through lg_render (device output)
-    plain = Context(device=local, culling=CULL[args.culling], grid_density=args.grid_density)
+    plain = Context(device=local, culling=CULL[args.culling])
     big = torch.empty(max(pk.params.width * pk.params.height for pk in scenes) * 4, dtype=torch.int16, device=dev)
-    lat = []
     for pk in scenes[:4]:
         plain.upload(pk)
         plain.render_into(big.data_ptr(), pk.params.width * 8, True)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for pk in scenes:
-        a = time.perf_counter()
         plain.upload(pk)
         plain.render_into(big.data_ptr(), pk.params.width * 8, True)
-        lat.append((time.perf_counter() - a) * 1e3)
     plain_s = time.perf_counter() - t0
     plain.close()
-    if rank == 0:
-        lat_sorted = sorted(lat)
-        pct = lambda q: lat_sorted[min(len(lat_sorted) - 1, int(q * len(lat_sorted)))]
-        out_line = {
-            "metric": "scenes/s, mixed-size batch (batched multi-scene trace vs plain one-scene path)",
-            "value": value, "unit": "scenes/s", "n_gpus": ws, "steps": args.steps, "warmup": max(1, args.warmup),
-            "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "fp32 + double-float trace, int64 accumulate", "data": "synthetic",
-            "config": {"workload": BATCH_WORKLOAD + ("" if args.ray_scale == 1.0 else f", rays x {args.ray_scale}"),
-                       "scenes": n, "l2": "flushed between steps (512 MB write)", "culling": args.culling},
-            "segments_per_step": segs, "pixels_per_step": pixels,
-            "e2e": {"value": e2e_value, "unit": "scenes/s", "h2d_bytes_per_step": None,
-                    "d2h_bytes_per_step": host.numel() * 2, "ms_per_step": e2e_s * 1e3},
-            "plain": {"scenes_per_s": n / plain_s, "wall_s": plain_s, "p50_ms": pct(0.5), "p99_ms": pct(0.99)},
-            "batched_vs_plain": value / (n / plain_s),
-            "batch_latency_ms": ms_max,
-            "gpu_launches": None,
-            "clocks": clk.summary(),
-        }
-        print(json.dumps(out_line), flush=True)
+    b = n / (min(ms) * 1e-3)
+    return {"workload": BATCH_WORKLOAD + f", rays x {ray_scale:g}", "scenes": n, "batched_scenes_per_s": b,
+            "batch_ms": min(ms), "plain_scenes_per_s": n / plain_s, "batched_vs_plain": b / (n / plain_s),
+            "note": "batched: device time of the batch graph; plain: host wall time of upload + lg_render per scene"}
 
 
-CSG_WORKLOAD = ("csg_scene: 256 CSG objects (circle op rect, ops And/Or/AndNot, seed 3), 8 lights, 2^22 rays, "
-                "32 bounces, 4096x4096, int64 accumulation, string-mod overlay m=4096 k=7")
-
-
-def run_csg(args, ws, rank, local):
-    """The CSG-heavy frame through lg_render.  Its segments exceed one accumulation pass, so
-    the library renders it with the accumulation interleaved between generations."""
-    import torch
-
-    from light_garden_gb300 import workloads as W
-    from light_garden_gb300.runtime import Context
-
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    pk = W.csg_scene(total_rays=max(8, int(round((1 << 22) * args.ray_scale)))).packed()
-    pk.params.precision = PRECISION[args.precision]
-    Wd, Hd = pk.params.width, pk.params.height
-    ctx = Context(device=local, raster_variant=args.raster_variant, culling=CULL[args.culling], grid_density=args.grid_density)
-    ctx.upload(pk)
-    out = torch.empty((Hd, Wd * 4), dtype=torch.int16, device=dev)
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
-    for _ in range(max(1, args.warmup)):
-        st = ctx.render_into(out.data_ptr(), Wd * 8, True)
-    torch.cuda.synchronize()
-    barrier(ws)
-    tot = {k: 0.0 for k in ("trace_ms", "raster_ms", "resolve_ms", "total_ms")}
-    with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            st = ctx.render_into(out.data_ptr(), Wd * 8, True)
-            for k in tot:
-                tot[k] += st[k]
-    avg = {k: v / args.steps for k, v in tot.items()}
-    value, ms_max = aggregate(ws, st["segments"], avg["total_ms"], dev)
-    host = torch.empty((Hd, Wd * 4), dtype=torch.int16, pin_memory=True)
-    t0 = time.perf_counter()
-    ctx.upload(pk)
-    ctx.render_into(host.data_ptr(), Wd * 8, False)
-    e2e_s = time.perf_counter() - t0
-    e2e_value, _ = aggregate(ws, st["segments"], e2e_s * 1e3, dev)
-    ctx.close()
-    if rank == 0:
-        line = {
-            "metric": METRIC, "value": value, "unit": "segments/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": max(1, args.warmup), "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "fp32 + double-float trace, int64 accumulate", "data": "synthetic",
-            "config": {"workload": CSG_WORKLOAD + ("" if args.ray_scale == 1.0 else f", rays x {args.ray_scale}"),
-                       "l2": "flushed between steps (512 MB write); working set > L2"},
-            "px_per_s": ws * st["pixels"] / (ms_max * 1e-3), "segments_per_step": st["segments"],
-            "pixels_per_step": st["pixels"], "ray_visits_per_step": st["ray_visits"],
-            "fp64_solves_per_step": st["fp64_solves"], "near_degenerate_per_step": st["near_degenerate"],
-            "bound_tests_per_step": st["bound_tests"], "object_tests_per_step": st["object_tests"],
-            "culling": args.culling,
-            "stage_ms": avg, "retries_first_frame": st["retries"],
-            "e2e": {"value": e2e_value, "unit": "segments/s", "h2d_bytes_per_step": None,
-                    "d2h_bytes_per_step": Hd * Wd * 8, "ms_per_step": e2e_s * 1e3},
-            "clocks": clk.summary(),
-        }
-        print(json.dumps(line), flush=True)
-
-
-def run_serve(args, ws, rank, local):
-    """Serving: requests from the mixed-size generator arrive as a Poisson stream; the server
-    (lg_serve_*, continuous batching under an HBM budget) against the plain path serving the
-    same arrivals one request at a time (lg_render, first come first served)."""
+def serve_bench(local, args, rate=100.0, count=256, ray_scale=1.0 / 16):
+    """Poisson arrivals below the server's capacity: scenes/s and p50/p99 latency of the
+    continuous-batching server against the plain path serving the same arrivals in order."""
     import numpy as np
     import torch
-
     from light_garden_gb300 import workloads as W
     from light_garden_gb300.runtime import Context
-
-    torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    ws_ = W.batch_scenes(seed=6, count=args.batch_scenes)
-    if args.ray_scale != 1.0:
-        ws_ = [W.scale_rays(w, args.ray_scale) for w in ws_]
-    scenes = [w.packed() for w in ws_]
-    n = len(scenes)
+    scenes = [W.scale_rays(w, ray_scale).packed() for w in W.batch_scenes(seed=6, count=count)]
+    for pk in scenes:
+        pk.params.precision = PRECISION[args.precision]
     rng = np.random.default_rng(7)
-    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n))
-    ctx = Context(device=local, culling=CULL[args.culling], grid_density=args.grid_density)
-    ctx.serve_begin(hbm_budget_bytes=int(args.budget_gb * (1 << 30)), max_slots=4096)
-    # warm up the kernels on two requests
-    for sc in scenes[:2]:
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, count))
+    ctx = Context(device=local, culling=CULL[args.culling])
+    ctx.serve_begin(hbm_budget_bytes=int(120 * (1 << 30)), max_slots=4096)
+    for sc in scenes[:2]:  # warm-up
         ctx.serve_submit(sc)
     while ctx.serve_step()["in_flight"] or any(ctx.serve_poll(r) is None for r in list(ctx.serve_shapes)):
         pass
-    done_at, arrive_of, ids = {}, {}, []
-    steps = restarts = 0
+    done_at, arrive_of = {}, {}
+    inflight = set()
     t0 = time.perf_counter()
     nxt = 0
-    inflight = set()
-    while len(done_at) < n:
+    while len(done_at) < count:
         now = time.perf_counter() - t0
-        while nxt < n and arrivals[nxt] <= now:
+        while nxt < count and arrivals[nxt] <= now:
             rid = ctx.serve_submit(scenes[nxt])
             arrive_of[rid] = arrivals[nxt]
             inflight.add(rid)
@@ -486,8 +428,6 @@ def run_serve(args, ws, rank, local):
             time.sleep(max(0.0, arrivals[nxt] - now))
             continue
         st = ctx.serve_step()
-        steps += 1
-        restarts += st["restarted"]
         if st["finished"] or st["in_flight"] == 0:
             t = time.perf_counter() - t0
             for rid in list(inflight):
@@ -498,8 +438,7 @@ def run_serve(args, ws, rank, local):
     lat = np.array([done_at[r] - arrive_of[r] for r in done_at]) * 1e3
     ctx.serve_end()
     ctx.close()
-    # plain path: one request at a time in arrival order
-    plain = Context(device=local, culling=CULL[args.culling], grid_density=args.grid_density)
+    plain = Context(device=local, culling=CULL[args.culling])
     big = torch.empty(max(pk.params.width * pk.params.height for pk in scenes) * 4, dtype=torch.int16, device=dev)
     for pk in scenes[:2]:
         plain.upload(pk)
@@ -516,22 +455,130 @@ def run_serve(args, ws, rank, local):
         end = max(end, a) + s
         plat.append((end - a) * 1e3)
     plat = np.array(plat)
+    return {"workload": BATCH_WORKLOAD.replace("seed 4", "seed 6") + f", rays x {ray_scale:g}",
+            "requests": count, "arrivals": f"Poisson, {rate:g} requests/s", "hbm_budget_gb": 120,
+            "scenes_per_s": count / makespan, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "makespan_s": makespan,
+            "plain": {"scenes_per_s": count / end, "p50_ms": float(np.percentile(plat, 50)),
+                      "p99_ms": float(np.percentile(plat, 99)), "mean_service_ms": float(np.mean(service) * 1e3)}}
+
+
+def run_ours(args, ws, rank, local):
+    import torch
+
+    from light_garden_gb300 import abi
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    name = args.workload
+    pk = packed_workload(name, args.precision)
+    Wd, Hd = pk.params.width, pk.params.height
+    peaks = live_peaks(local)
+    hbm = measured_hbm()
+    barrier(ws)
+    ctx, st, avg, clk = frame_bench(pk, local, args.steps, max(3, args.warmup), args)
+    barrier(ws)
+    value, ms_max = aggregate(ws, st["segments"], avg["total_ms"], dev)
+    px_per_s = ws * st["pixels"] / (ms_max * 1e-3)
+
+    # end to end through the C ABI: scene tables from the host, image back to pinned host memory
+    h2d = C.sizeof(abi.lg_geo) * pk.n_geo + C.sizeof(abi.lg_object) * pk.n_objects + \
+        C.sizeof(abi.lg_light) * pk.n_lights + C.sizeof(abi.lg_params)
+    d2h = Hd * Wd * 8
+    host = torch.empty((Hd, Wd * 4), dtype=torch.int16, pin_memory=True)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    ctx.upload(pk)
+    ctx.render_into(host.data_ptr(), Wd * 8, False)
+    barrier(ws)
+    e2e_steps = max(1, min(args.steps, 3))
+    e2e_times = []
+    for _ in range(e2e_steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.upload(pk)
+        est = ctx.render_into(host.data_ptr(), Wd * 8, False)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_value, e2e_ms = aggregate(ws, est["segments"], statistics.mean(e2e_times) * 1e3, dev)
+    ctx.close()
+    del flush
+
+    roof = rooflines(name, st, avg, peaks, hbm) if args.precision == "exact" else {}
+    dominant = max(roof.values(), key=lambda e: e["ms"]) if roof else None
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        stride = CPU_STRIDE[name]
+        spk, segs, paths, o_acc, px, tt, tr, prim = cpu_sample(name, stride)
+        cpu = {"value": len(segs) / (tt + tr), "unit": "segments/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"every {stride}th primary of each light ({prim} primaries): {len(segs)} segments traced in "
+                         f"{tt:.2f} s and rasterised ({px} px) in {tr:.2f} s",
+               "trace_segments_per_s": len(segs) / tt, "raster_px_per_s": px / tr}
+        try:
+            cpu["parity"] = sample_parity(spk, stride, segs, paths, o_acc, local)
+        except Exception as e:  # the headline line is printed either way
+            cpu["parity"] = {"error": repr(e)}
+
+    extras = {}
+    if rank == 0 and ws == 1 and not args.no_extras:
+        def extra(key, fn):
+            try:
+                extras[key] = fn()
+            except Exception as e:
+                extras[key] = {"error": repr(e)}
+
+        def mid():
+            mpk = packed_workload("mid", args.precision)
+            c2, s2, a2, _ = frame_bench(mpk, local, 5, 3, args, clocks=False)
+            c2.close()
+            d = {"workload": WORKLOADS["mid"], "value": s2["segments"] / (a2["total_ms"] * 1e-3), "unit": "segments/s",
+                 "ms_per_step": a2["total_ms"], "px_per_s": s2["pixels"] / (a2["total_ms"] * 1e-3),
+                 "segments_per_step": s2["segments"], "pixels_per_step": s2["pixels"], "stage_ms": a2}
+            if args.precision == "exact":
+                d["rooflines"] = rooflines("mid", s2, a2, peaks, hbm)
+            return d
+
+        def fast():
+            fpk = packed_workload(name, "fast")
+            c3, s3, a3, _ = frame_bench(fpk, local, 2, 1, args, clocks=False)
+            c3.close()
+            return {"workload": WORKLOADS[name] + ", double-float precision", "value": s3["segments"] / (a3["total_ms"] * 1e-3),
+                    "unit": "segments/s", "ms_per_step": a3["total_ms"], "stage_ms": a3,
+                    "near_degenerate_per_step": s3["near_degenerate"]}
+
+        if name != "mid":
+            extra("mid_scene", mid)
+        extra("fast_precision", fast)
+        extra("batch", lambda: batch_bench(local, args))
+        extra("serve", lambda: serve_bench(local, args))
+
+    launches = 1 + 3 * pk.params.max_bounce + 1 + 1  # light setup, 3 trace kernels per generation, overlay, resolve
+    if st.get("tile_refs", 0):
+        launches += 8 * pk.params.max_bounce  # streaming accumulation per generation (decide, clear, count, scan, units, scatter, raster, rotate)
     if rank == 0:
-        line = {
-            "metric": "serving: scenes/s and p50/p99 scene latency (continuous batching vs plain one-scene path)",
-            "value": n / makespan, "unit": "scenes/s", "n_gpus": ws, "steps": steps, "warmup": 2,
-            "ms_per_step": makespan * 1e3 / max(1, steps), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "fp32 + double-float trace, int64 accumulate", "data": "synthetic",
-            "config": {"workload": BATCH_WORKLOAD.replace("seed 4", "seed 6") +
-                       ("" if args.ray_scale == 1.0 else f", rays x {args.ray_scale}"),
-                       "requests": n, "arrivals": f"Poisson, {args.rate} requests/s",
-                       "hbm_budget_gb": args.budget_gb},
-            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-            "makespan_s": makespan, "restarts": restarts,
-            "plain": {"scenes_per_s": n / end, "p50_ms": float(np.percentile(plat, 50)),
-                      "p99_ms": float(np.percentile(plat, 99)), "makespan_s": end},
+        out = {
+            "metric": METRIC, "value": value, "unit": "segments/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 trace (exact), int64 accumulate" if args.precision == "exact"
+            else "double-float trace, int64 accumulate", "data": "synthetic",
+            "config": {"workload": WORKLOADS[name], "precision": args.precision,
+                       "l2": "flushed before every step (512 MB write); working set > L2",
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+            "px_per_s": px_per_s,
+            "segments_per_step": st["segments"], "pixels_per_step": st["pixels"], "tile_refs_per_step": st["tile_refs"],
+            "ray_visits_per_step": st["ray_visits"], "fp64_solves_per_step": st["fp64_solves"],
+            "stage_ms": avg,
+            "roofline": dominant,
+            "rooflines": roof,
+            "peaks": {"live": peaks, "hbm_gbs": hbm[0], "hbm_source": hbm[1]},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "segments/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": e2e_ms, "steps": e2e_steps},
+            "gpu_launches": launches * args.steps,
+            "clocks": clk,
         }
-        print(json.dumps(line), flush=True)
+        out.update(extras)
+        print(json.dumps(out), flush=True)
 
 
 def main():
@@ -540,33 +587,20 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-stride", type=int, default=4)
+    ap.add_argument("--workload", default="csg", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="exact", choices=sorted(PRECISION),
+                    help="exact: FP64 bit for bit with the FP64 formulas; fast: double-float refinement")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    # smaller cases of the same workload for profiler captures (the reported line uses the defaults)
-    ap.add_argument("--rays-per-light", type=int, default=1 << 18)
+    ap.add_argument("--no-extras", action="store_true", help="only the headline frame")
     ap.add_argument("--raster-variant", type=int, default=0, choices=[0, 1, 2],
                     help="0: autotuned; 1: shared-memory tile atomics; 2: warp-private tiles")
-    # the mixed-size batch configuration (not the default line)
-    ap.add_argument("--workload", default="mid", choices=["mid", "csg", "batch", "serve"])
     ap.add_argument("--culling", default="auto", choices=sorted(CULL),
                     help="nearest-hit culling grid: auto (scenes of 96+ objects), off, on")
     ap.add_argument("--grid-density", type=float, default=0.0, help="culling grid cells per object (0: 2)")
-    ap.add_argument("--precision", default="exact", choices=sorted(PRECISION),
-                    help="exact: FP64 bit-for-bit with the FP64 formulas; fast: double-float refinement")
-    ap.add_argument("--rate", type=float, default=1000.0, help="serve: Poisson arrival rate (requests/s)")
-    ap.add_argument("--budget-gb", type=float, default=120.0, help="serve: HBM budget")
-    ap.add_argument("--batch-scenes", type=int, default=512)
-    ap.add_argument("--ray-scale", type=float, default=1.0)
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, ws, rank)
-    elif args.workload == "batch":
-        run_batch(args, ws, rank, local)
-    elif args.workload == "serve":
-        run_serve(args, ws, rank, local)
-    elif args.workload == "csg":
-        run_csg(args, ws, rank, local)
     else:
         run_ours(args, ws, rank, local)
     if ws > 1:

@@ -737,10 +737,13 @@ void launch_light_setup(lg_ctx* c, const SceneDev& S, bool multi, int blocks) {
   }
 }
 
-// Events around one generation's kernels (kev_on: lg_render), k = 0 before the scan, 1
-// after it, 2 after the precise solve, 3 after the bounce.
+// Events around one generation's kernels while lg_render captures its frame graph (kev_on),
+// k = 0 before the scan, 1 after it, 2 after the precise solve, 3 after the bounce.
 static void kernel_event(lg_ctx* c, uint32_t g, int k) {
-  if (c->kev_on && 4 * g + k < c->kev.size()) cudaEventRecordWithFlags(c->kev[4 * g + k], c->stream, cudaEventRecordExternal);
+  if (!c->kev_on || 4 * g + k >= c->kev.size()) return;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(c->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusActive) return;
+  cudaEventRecordWithFlags(c->kev[4 * g + k], c->stream, cudaEventRecordExternal);  // only inside the frame graph
 }
 
 void launch_generation(lg_ctx* c, const SceneDev& S, const TraceBufs& B, uint32_t g, bool multi, int scan_grid,
