@@ -148,8 +148,11 @@ def test_tracer_list_api_matches_the_reference_surface():
 
 
 def test_reference_arm_sample_is_bounded(monkeypatch):
-    """bench.py's CPU sample of the mid scene: every stride-th primary of each light."""
+    """bench.py's CPU samples: every stride-th primary of each light of the mid and CSG frames."""
     import bench
-    n, px, tt, tr, prim = bench.cpu_sample(4096)
+    pk, segs, paths, acc, px, tt, tr, prim = bench.cpu_sample("mid", 4096)
     assert prim == 8 * (1 << 18) // 4096
-    assert n > prim and px > n
+    assert len(segs) > prim and px > len(segs) and acc.shape == (1080, 1920, 4)
+    pk, segs, paths, acc, px, tt, tr, prim = bench.cpu_sample("csg", 1 << 16)
+    assert prim == 8 * ((1 << 22) // 8) // (1 << 16)
+    assert len(segs) > prim and len(paths) == len(segs)
