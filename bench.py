@@ -261,7 +261,7 @@ def run_reference(args, ws, rank):
         return
     from oracle import oracle as O
     O.build()
-    stride = REF_STRIDE[args.workload]
+    stride = args.cpu_stride or REF_STRIDE[args.workload]
     times, nseg, npx, nprim = [], 0, 0, 0
     for _ in range(args.warmup):
         cpu_sample(args.workload, stride)
@@ -508,7 +508,7 @@ def run_ours(args, ws, rank, local):
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        stride = CPU_STRIDE[name]
+        stride = args.cpu_stride or CPU_STRIDE[name]
         spk, segs, paths, o_acc, px, tt, tr, prim = cpu_sample(name, stride)
         cpu = {"value": len(segs) / (tt + tr), "unit": "segments/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"every {stride}th primary of each light ({prim} primaries): {len(segs)} segments traced in "
@@ -591,6 +591,8 @@ def main():
     ap.add_argument("--precision", default="exact", choices=sorted(PRECISION),
                     help="exact: FP64 bit for bit with the FP64 formulas; fast: double-float refinement")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-stride", type=int, default=0,
+                    help="primary stride of the CPU samples (0: the workload's default)")
     ap.add_argument("--no-extras", action="store_true", help="only the headline frame")
     ap.add_argument("--raster-variant", type=int, default=0, choices=[0, 1, 2],
                     help="0: autotuned; 1: shared-memory tile atomics; 2: warp-private tiles")

@@ -70,7 +70,7 @@ REF = r"""
 import os, sys
 sys.path.insert(0, os.environ["LG_ROOT"])
 sys.argv = ["bench.py", "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0",
-            "--cpu-stride", "16384"]
+            "--workload", "mid", "--cpu-stride", "16384"]
 import bench
 bench.main()
 """
