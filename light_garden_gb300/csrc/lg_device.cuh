@@ -4,7 +4,7 @@
 //   ObjScan[n_obj]   64 B per object, FP32: inflated bounding circle + up to two leaves
 //                    inline.  This is the table every ray scans; each CTA stages it in
 //                    shared memory with one cp.async.bulk copy.
-//   ObjInfo[n_obj]   32 B per object: leaf range, membership program, material.
+//   ObjInfo[n_obj]   48 B per object: leaf range, membership program, material, FP64 tree range.
 //   Leaf64[n_leaf]   72 B per leaf, double-float world-space primitive (CSG trees flattened).
 //   prog[]           membership programs (postfix over leaf membership bits).
 //
