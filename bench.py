@@ -55,8 +55,8 @@ REF_STRIDE = {"csg": 2048, "mid": 32}
 
 # Instructions per unit of work of the trace kernels and the tile raster in the exact mode,
 # counted with ncu (smsp__sass_thread_inst_executed_op_{fadd,fmul,ffma,dadd,dmul,dfma}
-# _pred_on.sum and smsp__sass_inst_executed_op_shared_atom.sum over one frame of a small case
-# of the same workload: csg 2^18 rays at 1024^2, mid 2^14 rays per light).
+# _pred_on.sum and smsp__sass_inst_executed_op_shared_atom.sum over the frame of
+# ``bench.py --count-case``: csg 2^18 rays at 1024^2, mid 2^14 rays per light).
 #   scan:   FP32 thread instructions per ray visit
 #   solve:  FP64 thread instructions per object solved (lg_trace_stats.fp64_solves)
 #   bounce: FP64 thread instructions per ray visit
@@ -195,8 +195,9 @@ def cpu_sample(name: str, stride: int):
     pk = packed_workload(name, "exact")
     t0 = time.perf_counter()
     segs, paths, _, st = O.trace(pk, ray_stride=stride, threads=0)
+    chords = O.string_mod_chords(pk.params)  # the sample starts at primary 0: the overlay is drawn
     t1 = time.perf_counter()
-    acc, px = O.raster(segs, pk.params, threads=0)
+    acc, px = O.raster(segs, pk.params, threads=0, chords=chords)
     t2 = time.perf_counter()
     return pk, segs, paths, acc, px, t1 - t0, t2 - t1, int(st.primary_rays)
 
@@ -227,20 +228,24 @@ def sample_parity(pk, stride, o_segs, o_paths, o_acc, local):
         ctx.trace()
         gs, gp = ctx.segments(paths=True)
         rep = exact(gs, gp, o_segs, o_paths)
+        o_ch = O.string_mod_chords(pk.params)
         ctx.accumulate()
         acc = ctx.accum()
         out["exact"] = {"segments": rep.segments, "bit_exact_segments": rep.ok(),
+                        "string_mod_lines": len(o_ch), "bit_exact_lines": ctx.chords().tobytes() == o_ch.tobytes(),
                         "image_bit_exact": bool(np.array_equal(acc, o_acc)),
                         "near_flag_differs": rep.near_flag_differs}
         del acc
         scale = 2.0 ** -32
-        # the FP64 image of the oracle's segments: the reference for the accumulation error
-        f64, _ = O.raster_f64(o_segs, pk.params)
+        # the FP64 image of the oracle's segments and lines: the reference for the accumulation error
+        f64, _ = O.raster_f64(o_segs, pk.params, chords=o_ch)
         l1, l2 = rel(o_acc.astype(np.float64) * scale, f64)
         out["fixed64_vs_fp64_raster"] = {"rel_l1": l1, "rel_l2": l2}
         pk.params.accum = abi.LG_ACCUM_F32
+        pk.params.record_paths = 0
         ctx.upload(pk)
-        ctx.accumulate_segments(o_segs)
+        ctx.trace()  # the same exact trace, accumulated in FP32
+        ctx.accumulate()
         l1, l2 = rel(ctx.accum(), f64)
         out["fp32_accum_vs_fp64_raster"] = {"rel_l1": l1, "rel_l2": l2}
         # the double-float trace of the same sample, accumulated in fixed point
@@ -463,6 +468,26 @@ def serve_bench(local, args, rate=100.0, count=256, ray_scale=1.0 / 16):
                       "p99_ms": float(np.percentile(plat, 99)), "mean_service_ms": float(np.mean(service) * 1e3)}}
 
 
+def count_case(args):
+    """One frame of a small case of the workload (csg: 2^18 rays at 1024^2; mid: 2^14 rays per
+    light), no autotuning, printing the frame's units of work.  Run under ncu with instruction
+    counters, it gives the instructions per unit of INST_PER_UNIT."""
+    from light_garden_gb300 import workloads as W
+    from light_garden_gb300.runtime import Context
+    if args.workload == "csg":
+        pk = W.csg_scene(total_rays=1 << 18, width=1024, height=1024).packed()
+    else:
+        pk = W.mid_scene(rays_per_light=1 << 14).packed()
+    pk.params.precision = PRECISION[args.precision]
+    with Context(raster_variant=1, culling=CULL[args.culling]) as ctx:
+        ctx.upload(pk)
+        _, st = ctx.render()
+    keys = ("ray_visits", "fp64_solves", "pixels", "bound_tests", "object_tests", "segments", "scan_ms", "solve_ms",
+            "bounce_ms", "raster_ms", "trace_ms", "total_ms")
+    print(json.dumps({"count_case": args.workload, "precision": args.precision, **{k: st[k] for k in keys}}),
+          flush=True)
+
+
 def run_ours(args, ws, rank, local):
     import torch
 
@@ -599,7 +624,12 @@ def main():
     ap.add_argument("--culling", default="auto", choices=sorted(CULL),
                     help="nearest-hit culling grid: auto (scenes of 96+ objects), off, on")
     ap.add_argument("--grid-density", type=float, default=0.0, help="culling grid cells per object (0: 2)")
+    ap.add_argument("--count-case", action="store_true",
+                    help="render one small frame of the workload and print its units of work (for ncu counts)")
     args = ap.parse_args()
+    if args.count_case:
+        count_case(args)
+        return
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, ws, rank)

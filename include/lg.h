@@ -43,7 +43,7 @@ extern "C" {
  * object_tests (both structs grew).
  * 3: lg_device_opts gained wait_polls; lg_params.precision (was padding), ray_stride and
  *    ray_offset (lg_params grew); lg_trace_stats scan_ms, solve_ms, bounce_ms (grew). */
-#define LG_ABI_VERSION 3
+#define LG_ABI_VERSION 4
 
 typedef enum lg_status {
   LG_OK = 0,
@@ -150,13 +150,42 @@ enum lg_accum_mode {
 /* ---- string-mod overlay (src/light_garden/string_mod.rs) ------------------------------- */
 enum lg_string_mod_mode { LG_SM_ADD = 0, LG_SM_MUL = 1, LG_SM_POW = 2, LG_SM_BASE = 3 };
 
+/* StringMod::init_curve (string_mod.rs:182-188, points init_points 33-85).  With
+ * a(n) = turns * n * 2 pi / m:
+ *   CIRCLE        (cos a, sin a)
+ *   COMPLEX_EXP   c^(u32)(turns * n), c = curve_f[0] + i curve_f[1] (binary powering)
+ *   HYPOTROCHOID  r, s, d = curve_u[0..2], k = s - r:
+ *                 (k cos a + d cos(a k / r), k sin a - d sin(a k / r)) / (k + d)
+ *   LISSAJOUS     a_, b_ = curve_u[0..1], delta = curve_f[0]: (sin(a_ a + delta), sin(b_ a)) */
+enum lg_string_mod_curve {
+  LG_CURVE_CIRCLE = 0,
+  LG_CURVE_COMPLEX_EXP = 1,
+  LG_CURVE_HYPOTROCHOID = 2,
+  LG_CURVE_LISSAJOUS = 3
+};
+
+/* ModRemColor (string_mod.rs:167-172): point n takes `color` when n % modulo == rem.  A
+ * point that several entries match takes their mean (f32 sums in table order, then one
+ * division by the count); a point that none matches takes lg_string_mod.color
+ * (StringMod::get_color, string_mod.rs:124-150). */
+typedef struct lg_mod_color {
+  uint64_t modulo; /* >= 1 */
+  uint64_t rem;
+  float color[4];
+} lg_mod_color;
+
 typedef struct lg_string_mod {
   uint64_t modulo;  /* number of points m; 0 disables the overlay */
   uint64_t num;
   uint64_t turns;
   uint32_t mode;    /* enum lg_string_mod_mode */
-  uint32_t curve;   /* 0 = Curve::Circle (the only curve on this path) */
-  float color[4];
+  uint32_t curve;   /* enum lg_string_mod_curve */
+  float color[4];   /* StringMod::color */
+  double curve_f[2];    /* curve parameters, see lg_string_mod_curve */
+  uint64_t curve_u[3];
+  uint32_t n_colors;    /* entries of `colors` (StringMod::modulo_colors), 0..4096 */
+  uint32_t _pad;
+  const lg_mod_color* colors; /* host array, copied by lg_scene_upload (not kept) */
 } lg_string_mod;
 
 /* ---- trace precision ----------------------------------------------------------------- *
@@ -183,7 +212,7 @@ typedef struct lg_params {
   int32_t emit_control_lines;   /* append curved-mirror control polygons (tracer.rs:341-346) */
   int32_t record_paths;         /* also write one lg_path_record per segment (parity tooling) */
   int32_t precision;            /* enum lg_precision of the trace */
-  lg_string_mod string_mod;     /* overlay segments, drawn with the same raster */
+  lg_string_mod string_mod;     /* overlay lines (lg_chord), drawn with the same raster */
   uint32_t ray_stride;          /* trace only the primaries i = ray_offset + k * ray_stride of each
                                    light (0 or 1: all), as a sampled frame; the overlays are drawn
                                    only when ray_offset == 0.  One scene only (not batches/serving) */
@@ -201,11 +230,24 @@ typedef struct lg_segment {
   float color[4];
 } lg_segment;
 
+/* One string-mod line (StringMod::draw_init_points, string_mod.rs:104-122): the two
+ * (P2, Color) vertices of the reference's line list with their own colours.  The raster
+ * interpolates the colour along the major axis: at the sample of major-axis pixel i,
+ * f = clamp((i + 1/2 - U0) / (U1 - U0), 0, 1) with U0, U1 the vertices' major pixel
+ * coordinates, and colour = fma(f, color1 - color0, color0), each an f32 operation
+ * rounded once. */
+typedef struct lg_chord {
+  float x0, y0, x1, y1;
+  float color0[4];
+  float color1[4];
+} lg_chord;
+
 enum lg_path_flags {
   LG_PATH_NEAR_DEGENERATE = 1, /* a decision on this path fell inside the FP64 epsilon band */
   LG_PATH_TIR = 2,             /* this segment ends in total internal reflection */
   LG_PATH_FALLBACK = 4         /* candidate list overflowed: every object re-solved in FP64 */
 };
+/* LG_SRC_STRING_MOD is kept for numbering; string-mod lines are lg_chord records. */
 enum lg_path_source { LG_SRC_TRACE = 0, LG_SRC_CONTROL_LINE = 1, LG_SRC_STRING_MOD = 2 };
 
 /* Identity of a segment in the ray tree, for parity checks against a CPU trace. */
@@ -318,6 +360,12 @@ lg_status lg_segments_download(lg_ctx* ctx, lg_segment* out, lg_path_record* pat
 
 /* Copies the raw accumulation image: width*height*4 values, int64 (FIXED64) or float (F32). */
 lg_status lg_accum_download(lg_ctx* ctx, void* out, uint64_t cap_bytes);
+
+/* Copies the string-mod lines of the last lg_trace / lg_render (lg_params.string_mod.modulo
+ * of them; none in a sampled frame with ray_offset != 0, or after lg_accumulate_segments).
+ * *n_out receives the count; LG_ERR_TRUNCATED when cap is smaller.  lg_accumulate draws
+ * them together with the segments. */
+lg_status lg_chords_download(lg_ctx* ctx, lg_chord* out, uint64_t cap, uint64_t* n_out);
 
 /* ---- batches: many scenes in one trace ----------------------------------------------- *
  * No counterpart in the reference, which traces one scene per Tracer (tracer.rs:276-358).

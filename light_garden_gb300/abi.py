@@ -45,6 +45,7 @@ LG_LIGHT_POINT, LG_LIGHT_DIRECTIONAL, LG_LIGHT_SPOT = range(3)
 LG_BO_ADD, LG_BO_SUBTRACT, LG_BO_REVERSE_SUBTRACT, LG_BO_MIN, LG_BO_MAX = range(5)
 LG_ACCUM_FIXED64, LG_ACCUM_F32 = 0, 1
 LG_SM_ADD, LG_SM_MUL, LG_SM_POW, LG_SM_BASE = range(4)
+LG_CURVE_CIRCLE, LG_CURVE_COMPLEX_EXP, LG_CURVE_HYPOTROCHOID, LG_CURVE_LISSAJOUS = range(4)
 LG_PATH_NEAR_DEGENERATE, LG_PATH_TIR, LG_PATH_FALLBACK = 1, 2, 4
 LG_SRC_TRACE, LG_SRC_CONTROL_LINE, LG_SRC_STRING_MOD = 0, 1, 2
 
@@ -68,9 +69,17 @@ class lg_blend_component(C.Structure):
     _fields_ = [("src_factor", C.c_int32), ("dst_factor", C.c_int32), ("op", C.c_int32)]
 
 
+class lg_mod_color(C.Structure):
+    _fields_ = [("modulo", C.c_uint64), ("rem", C.c_uint64), ("color", C.c_float * 4)]
+
+
 class lg_string_mod(C.Structure):
+    # ``colors`` is a C pointer (const lg_mod_color*); it is declared as an integer address so
+    # that parameter blocks stay copyable, and set through set_mod_colors().
     _fields_ = [("modulo", C.c_uint64), ("num", C.c_uint64), ("turns", C.c_uint64),
-                ("mode", C.c_uint32), ("curve", C.c_uint32), ("color", C.c_float * 4)]
+                ("mode", C.c_uint32), ("curve", C.c_uint32), ("color", C.c_float * 4),
+                ("curve_f", C.c_double * 2), ("curve_u", C.c_uint64 * 3),
+                ("n_colors", C.c_uint32), ("_pad", C.c_uint32), ("colors", C.c_uint64)]
 
 
 class lg_params(C.Structure):
@@ -86,6 +95,11 @@ class lg_params(C.Structure):
 class lg_segment(C.Structure):
     _fields_ = [("x0", C.c_float), ("y0", C.c_float), ("x1", C.c_float), ("y1", C.c_float),
                 ("color", C.c_float * 4)]
+
+
+class lg_chord(C.Structure):
+    _fields_ = [("x0", C.c_float), ("y0", C.c_float), ("x1", C.c_float), ("y1", C.c_float),
+                ("color0", C.c_float * 4), ("color1", C.c_float * 4)]
 
 
 class lg_path_record(C.Structure):
@@ -113,7 +127,7 @@ class lg_device_opts(C.Structure):
                 ("grid_density", C.c_float), ("wait_polls", C.c_int32), ("_pad", C.c_int32)]
 
 
-LG_ABI_VERSION = 3  # include/lg.h
+LG_ABI_VERSION = 4  # include/lg.h
 LG_CULL_AUTO, LG_CULL_OFF, LG_CULL_ON = 0, 1, 2
 LG_PRECISION_EXACT, LG_PRECISION_FAST = 0, 1
 LG_CULL_AUTO_MIN = 96
@@ -123,6 +137,31 @@ LG_CULL_AUTO_MIN = 96
 def segment_dtype():
     import numpy as np
     return np.dtype([("x0", "<f4"), ("y0", "<f4"), ("x1", "<f4"), ("y1", "<f4"), ("color", "<f4", (4,))])
+
+
+def chord_dtype():
+    import numpy as np
+    return np.dtype([("x0", "<f4"), ("y0", "<f4"), ("x1", "<f4"), ("y1", "<f4"), ("color0", "<f4", (4,)),
+                     ("color1", "<f4", (4,))])
+
+
+# colour tables handed to the library by address; kept alive for the life of the process
+_mod_color_tables: list = []
+
+
+def set_mod_colors(params: "lg_params", entries) -> None:
+    """StringMod::modulo_colors: ``entries`` is a sequence of (modulo, rem, (r, g, b, a))."""
+    entries = list(entries)
+    sm = params.string_mod
+    if not entries:
+        sm.n_colors, sm.colors = 0, 0
+        return
+    arr = (lg_mod_color * len(entries))()
+    for e, (m, r, col) in zip(arr, entries):
+        e.modulo, e.rem = int(m), int(r)
+        e.color[:] = tuple(float(x) for x in col)
+    _mod_color_tables.append(arr)
+    sm.n_colors, sm.colors = len(entries), C.addressof(arr)
 
 
 def path_dtype():
@@ -192,6 +231,7 @@ EXPORTS = [
     ("lg_segments_download", C.c_int, [C.c_void_p, C.POINTER(lg_segment), C.POINTER(lg_path_record),
                                        C.c_uint64, C.POINTER(C.c_uint64)]),
     ("lg_accum_download", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    ("lg_chords_download", C.c_int, [C.c_void_p, C.POINTER(lg_chord), C.c_uint64, C.POINTER(C.c_uint64)]),
     ("lg_batch_upload", C.c_int, [C.c_void_p, C.POINTER(lg_scene_desc), C.c_uint32]),
     ("lg_batch_render", C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_int32, C.POINTER(lg_trace_stats)]),
     ("lg_batch_image_offset", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint64)]),

@@ -470,9 +470,16 @@ lg_status validate_params(std::string& err, const lg_params& p) {
     return set_err(err, LG_ERR_INVALID_ARGUMENT, "unknown accum mode");
   if (!blend_supported(p.color_blend) || !blend_supported(p.alpha_blend))
     return set_err(err, LG_ERR_UNSUPPORTED, "blend state reads the destination (order-dependent): not supported");
-  if (p.string_mod.modulo && (p.string_mod.curve != 0 || p.string_mod.mode > LG_SM_BASE))
-    return set_err(err, LG_ERR_UNSUPPORTED, "string mod: only Curve::Circle with Add/Mul/Pow/Base");
-  if (p.string_mod.modulo > (1ull << 30)) return set_err(err, LG_ERR_INVALID_ARGUMENT, "string mod modulo too large");
+  const lg_string_mod& sm = p.string_mod;
+  if (sm.modulo) {
+    if (sm.curve > LG_CURVE_LISSAJOUS) return set_err(err, LG_ERR_INVALID_ARGUMENT, "string mod: unknown curve");
+    if (sm.mode > LG_SM_BASE) return set_err(err, LG_ERR_INVALID_ARGUMENT, "string mod: unknown mode");
+    if (sm.modulo > (1ull << 26)) return set_err(err, LG_ERR_INVALID_ARGUMENT, "string mod: modulo above 2^26");
+    if (sm.n_colors > 4096) return set_err(err, LG_ERR_INVALID_ARGUMENT, "string mod: more than 4096 modulo colours");
+    if (sm.n_colors && !sm.colors) return set_err(err, LG_ERR_INVALID_ARGUMENT, "string mod: null modulo colours");
+    for (uint32_t k = 0; k < sm.n_colors; ++k)
+      if (sm.colors[k].modulo == 0) return set_err(err, LG_ERR_INVALID_ARGUMENT, "string mod: modulo colour with modulo 0");
+  }
   if (p.precision != LG_PRECISION_EXACT && p.precision != LG_PRECISION_FAST)
     return set_err(err, LG_ERR_INVALID_ARGUMENT, "unknown precision");
   if (p.ray_stride > 1 && p.ray_offset >= p.ray_stride)
@@ -480,10 +487,15 @@ lg_status validate_params(std::string& err, const lg_params& p) {
   return LG_OK;
 }
 
-// Overlay segments of the context's frame (none in a sampled frame with ray_offset != 0).
+// Overlay segments (curved-mirror control lines) and string-mod lines of the context's frame
+// (none in a sampled frame with ray_offset != 0).
 uint64_t overlay_segments(const lg_ctx* c) {
   if (c->prm.ray_stride > 1 && c->prm.ray_offset != 0) return 0;
-  return 3ull * c->n_cubic * (c->prm.emit_control_lines ? 1 : 0) + c->prm.string_mod.modulo;
+  return 3ull * c->n_cubic * (c->prm.emit_control_lines ? 1 : 0);
+}
+uint64_t string_mod_lines(const lg_ctx* c) {
+  if (c->prm.ray_stride > 1 && c->prm.ray_offset != 0) return 0;
+  return c->prm.string_mod.modulo;
 }
 
 // Primaries of a light with num_rays rays that a sampled frame traces.
@@ -807,6 +819,33 @@ lg_status upload_exact(lg_ctx* c, const Flat& F) {
   return LG_OK;
 }
 
+// Control lines into the segment ring, string-mod lines into their table; records how many
+// lines the accumulation draws.
+void launch_overlay(lg_ctx* c, const SceneDev& S, const TraceBufs& B) {
+  const uint64_t n_ov = overlay_segments(c), n_sm = string_mod_lines(c);
+  c->chords_ready = n_sm;
+  if (!n_ov && !n_sm) return;
+  lg_string_mod sm = c->prm.string_mod;
+  sm.modulo = n_sm;
+  ChordArgs CA;
+  CA.out = (lg_chord*)c->d_chords.p;
+  CA.colors = (const lg_mod_color*)c->d_mod_colors.p;
+  CA.n_colors = sm.n_colors;
+  const int blocks = (int)std::min<uint64_t>((n_ov + n_sm + 255) / 256, 4096);
+  k_overlay<<<blocks, 256, 0, c->stream>>>(S, B, (const uint32_t*)c->d_cubics.p, nullptr,
+                                           c->prm.emit_control_lines ? c->n_cubic : 0, sm, CA);
+}
+
+// The string-mod lines of the last trace, into the image (after its clear).
+void launch_chords(lg_ctx* c, const RasterArgs& A) {
+  if (!c->chords_ready) return;
+  const int blocks = (int)std::min<uint64_t>((c->chords_ready + 7) / 8, (uint64_t)c->n_sm * 8);
+  if (c->prm.accum == LG_ACCUM_FIXED64)
+    k_raster_chords<true><<<blocks, 256, 0, c->stream>>>(A, (const lg_chord*)c->d_chords.p, c->chords_ready);
+  else
+    k_raster_chords<false><<<blocks, 256, 0, c->stream>>>(A, (const lg_chord*)c->d_chords.p, c->chords_ready);
+}
+
 lg_status enqueue_trace(lg_ctx* c) {
   const SceneDev S = scene_dev(c);
   const TraceBufs B = trace_bufs(c);
@@ -815,12 +854,7 @@ lg_status enqueue_trace(lg_ctx* c) {
   const size_t tsm = c->smem_fits ? c->obj_smem : 0;
   for (uint32_t g = 0; g < c->prm.max_bounce; ++g)
     launch_generation(c, S, B, g, false, c->trace_grid[0], (size_t)scan_smem_bytes() + tsm, tsm, c->smem_fits);
-  const uint64_t n_ov = overlay_segments(c);
-  if (n_ov) {
-    const int blocks = (int)std::min<uint64_t>((n_ov + 255) / 256, 4096);
-    k_overlay<<<blocks, 256, 0, c->stream>>>(S, B, (const uint32_t*)c->d_cubics.p, nullptr,
-                                             c->prm.emit_control_lines ? c->n_cubic : 0, c->prm.string_mod);
-  }
+  launch_overlay(c, S, B);
   CK(cudaGetLastError(), "trace launch");
   return LG_OK;
 }
@@ -861,6 +895,7 @@ lg_status enqueue_accumulate(lg_ctx* c, int binned_event = -1) {
     k_raster<RM_FIXED_MINMAX_><<<c->raster_grid, 256, rsm, c->stream>>>(A);
   else
     k_raster<RM_F32_><<<c->raster_grid, 256, rsm, c->stream>>>(A);
+  launch_chords(c, A);
   CK(cudaGetLastError(), "accumulate launch");
   return LG_OK;
 }
@@ -1113,9 +1148,19 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
   if ((st = validate_exact(c->err, p, F))) return st;
   CK(cudaStreamSynchronize(c->stream), "synchronize");
   if ((st = upload_exact(c, F))) return st;
+  lg_params pk = p;  // kept without the caller's colour-table pointer
+  pk.string_mod.colors = nullptr;
   const bool same_shape = c->has_scene && c->n_obj == n_objects && c->n_leaves == F.leaves.size() &&
                           c->n_prog == F.prog.size() && c->n_lights == n_lights && c->n_cubic == F.cubics.size() &&
-                          std::memcmp(&c->prm, &p, sizeof p) == 0;
+                          std::memcmp(&c->prm, &pk, sizeof pk) == 0;
+  if (p.string_mod.modulo) {
+    if ((st = ensure(c, c->d_chords, p.string_mod.modulo * sizeof(lg_chord), "string-mod lines"))) return st;
+    if ((st = ensure(c, c->d_mod_colors, (size_t)std::max<uint32_t>(p.string_mod.n_colors, 1) * sizeof(lg_mod_color),
+                     "string-mod colours"))) return st;
+    if (p.string_mod.n_colors)
+      CK(cudaMemcpyAsync(c->d_mod_colors.p, p.string_mod.colors, p.string_mod.n_colors * sizeof(lg_mod_color),
+                         cudaMemcpyHostToDevice, c->stream), "upload");
+  }
   if ((st = ensure(c, c->d_scan, F.scan.size() * sizeof(ObjScan), "scene"))) return st;
   if ((st = ensure(c, c->d_info, F.info.size() * sizeof(ObjInfo), "scene"))) return st;
   std::vector<Leaf64> dleaves;
@@ -1158,7 +1203,8 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
   c->n_cubic = (uint32_t)F.cubics.size();
   c->n_primary = 0;
   for (uint32_t l = 0; l < n_lights; ++l) c->n_primary += sampled_rays(lights[l].num_rays, p);
-  c->prm = p;
+  c->prm = pk;
+  c->chords_ready = 0;
   c->aspect = (double)((float)p.width / (float)p.height);
   c->ntx = (p.width + TILE - 1) / TILE;
   c->nty = (p.height + TILE - 1) / TILE;
@@ -1190,7 +1236,7 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
   c->raster_warp_grid = c->n_sm * std::max(1, occ);
   c->bin_grid = c->n_sm * 8;
   // capacities: first guesses, grown on overflow
-  const uint64_t overlays = 3ull * F.cubics.size() + p.string_mod.modulo;
+  const uint64_t overlays = 3ull * F.cubics.size();
   // an explicit capacity from lg_device_opts is honoured as given (it still grows on overflow)
   const uint64_t want_seg = c->seg_cap_hint ? c->seg_cap_hint : 8 * c->n_primary + overlays + 1024;
   const uint64_t want_q = c->queue_cap_hint ? c->queue_cap_hint : 2 * c->n_primary + 1024;
@@ -1259,6 +1305,7 @@ lg_status lg_accumulate_segments(lg_ctx* c, const lg_segment* segs, uint64_t n, 
   CK(cudaMemcpyAsync(&d->seg_count, &nn, sizeof nn, cudaMemcpyHostToDevice, c->stream), "segment count");
   CK(cudaStreamSynchronize(c->stream), "synchronize");
   c->graph_valid = false;  // the ring no longer holds a trace
+  c->chords_ready = 0;
   return lg_accumulate(c, stats);
 }
 
@@ -1312,14 +1359,12 @@ static lg_status enqueue_stream_frame(lg_ctx* c, uint16_t* dst, size_t row, cuda
   const uint32_t n_part = (bins + TILE_SCAN_CHUNK - 1) / TILE_SCAN_CHUNK;
   const int mode = raster_mode(c->prm);
   const size_t rsm = (size_t)raster_smem_bytes(mode);
-  const uint64_t n_ov = overlay_segments(c);
   const uint32_t G = c->prm.max_bounce;
   for (uint32_t g = 0; g < G; ++g) {
     launch_generation(c, S, B, g, false, c->trace_grid[0], (size_t)scan_smem_bytes() + tsm, tsm, c->smem_fits);
-    if (g == 0 && n_ov) {
-      const int blocks = (int)std::min<uint64_t>((n_ov + 255) / 256, 4096);
-      k_overlay<<<blocks, 256, 0, c->stream>>>(S, B, (const uint32_t*)c->d_cubics.p, nullptr,
-                                               c->prm.emit_control_lines ? c->n_cubic : 0, c->prm.string_mod);
+    if (g == 0) {
+      launch_overlay(c, S, B);
+      launch_chords(c, A);
     }
     CK(cudaEventRecordWithFlags(ev[1 + 2 * g], c->stream, cudaEventRecordExternal), "stage event");
     k_stream_decide<<<1, 1, 0, c->stream>>>((Counters*)c->d_ctr.p, g, c->seg_cap, c->queue_cap, g + 1 == G ? 1 : 0);
@@ -1361,7 +1406,7 @@ static lg_status start_streaming(lg_ctx* c) {
   c->streaming = true;
   c->graph_valid = false;
   if (c->raster_variant == 0) c->raster_variant = 1;
-  const uint64_t n_ov = 3ull * c->n_cubic + c->prm.string_mod.modulo;
+  const uint64_t n_ov = 3ull * c->n_cubic;
   c->seg_cap = std::max<uint64_t>(c->stream_ring, c->queue_cap + n_ov + 1024);
   c->refs_cap = std::min<uint64_t>(4 * c->seg_cap, 0xfffffff0ull);
   if (c->bev.empty()) {
@@ -1408,7 +1453,7 @@ static lg_status render_streaming(lg_ctx* c, uint16_t* dst, size_t pitch, int32_
       ++retries;
       c->graph_valid = false;
       if (nq > c->queue_cap) c->queue_cap = nq + nq / 2 + 1024;
-      c->seg_cap = std::max<uint64_t>(c->seg_cap, c->queue_cap + 3ull * c->n_cubic + c->prm.string_mod.modulo + 1024);
+      c->seg_cap = std::max<uint64_t>(c->seg_cap, c->queue_cap + 3ull * c->n_cubic + 1024);
       if (k.refs_max > c->refs_cap) c->refs_cap = k.refs_max + k.refs_max / 4 + 4096;
       if (c->refs_cap >= 0xffffffffull) return fail(c, LG_ERR_UNSUPPORTED, "more than 2^32 (segment, tile) pairs in one pass");
       lg_status st = ensure_trace_buffers(c);
@@ -1543,6 +1588,18 @@ lg_status lg_segments_download(lg_ctx* c, lg_segment* out, lg_path_record* paths
   if (paths && !c->prm.record_paths) return fail(c, LG_ERR_INVALID_ARGUMENT, "path records need params.record_paths");
   if (n && out) CK(cudaMemcpyAsync(out, c->d_segs.p, n * sizeof(lg_segment), cudaMemcpyDeviceToHost, c->stream), "download segments");
   if (n && paths) CK(cudaMemcpyAsync(paths, c->d_paths.p, n * sizeof(lg_path_record), cudaMemcpyDeviceToHost, c->stream), "download paths");
+  CK(cudaStreamSynchronize(c->stream), "synchronize");
+  return LG_OK;
+}
+
+lg_status lg_chords_download(lg_ctx* c, lg_chord* out, uint64_t cap, uint64_t* n_out) {
+  lg_status st = need_scene(c);
+  if (st) return st;
+  if (!n_out) return fail(c, LG_ERR_INVALID_ARGUMENT, "null n_out");
+  const uint64_t n = c->chords_ready;
+  *n_out = n;
+  if (cap < n) return fail(c, LG_ERR_TRUNCATED, "buffer holds fewer lines than the frame");
+  if (n && out) CK(cudaMemcpyAsync(out, c->d_chords.p, n * sizeof(lg_chord), cudaMemcpyDeviceToHost, c->stream), "download lines");
   CK(cudaStreamSynchronize(c->stream), "synchronize");
   return LG_OK;
 }

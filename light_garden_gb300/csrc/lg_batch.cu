@@ -103,7 +103,7 @@ lg_status enqueue_batch(lg_ctx* c, cudaEvent_t* ev) {
     if (g == 0 && c->n_cubic) {
       const int blocks = (int)std::min<uint64_t>((3ull * c->n_cubic + 255) / 256, 4096);
       k_overlay<<<blocks, 256, 0, c->stream>>>(S, B, (const uint32_t*)c->d_cubics.p,
-                                               (const uint16_t*)c->d_cubic_scene.p, c->n_cubic, no_sm);
+                                               (const uint16_t*)c->d_cubic_scene.p, c->n_cubic, no_sm, ChordArgs{});
     }
     CK(cudaEventRecordWithFlags(ev[1 + 2 * g], c->stream, cudaEventRecordExternal), "stage event");
     // accumulate when the ring is full enough (every kernel below returns at once otherwise)
@@ -328,6 +328,9 @@ lg_status lg_batch_upload(lg_ctx* c, const lg_scene_desc* scenes, uint32_t k) {
   c->prm.width = 0;
   c->prm.height = 0;
   c->prm.string_mod.modulo = 0;
+  c->prm.string_mod.n_colors = 0;
+  c->prm.string_mod.colors = nullptr;
+  c->chords_ready = 0;
   c->total_px = total_px;
   c->total_bins = (uint32_t)total_bins;
   c->max_bounce_all = max_b;

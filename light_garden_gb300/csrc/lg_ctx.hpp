@@ -34,6 +34,9 @@ struct lg_ctx {
   // scene
   DevBuf d_scan, d_info, d_leaves, d_prog, d_lights, d_cubics;
   DevBuf d_xgeo, d_xnode;  // exact mode: geometry nodes and per-object preorder trees
+  DevBuf d_mod_colors;     // string mod: the modulo-colour table (lg_string_mod.colors)
+  DevBuf d_chords;         // string mod: the frame's lines (lg_string_mod.modulo of them)
+  uint64_t chords_ready = 0;  // lines the last trace left in d_chords (0: none to draw)
   uint32_t n_obj = 0, n_leaves = 0, n_prog = 0, n_lights = 0, n_cubic = 0;
   uint64_t n_primary = 0;
   lg_params prm{};

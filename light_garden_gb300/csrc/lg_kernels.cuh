@@ -72,8 +72,15 @@ template <bool MULTI>
 __global__ void k_solve_x(SceneDev S, TraceBufs B, uint32_t gen);
 template <bool MULTI, bool CULL>
 __global__ void k_bounce_x(SceneDev S, TraceBufs B, uint32_t gen);
+// The string-mod lines' table and the modulo-colour table on the device (sm.colors is the
+// caller's host pointer and is never read on the device).
+struct ChordArgs {
+  lg_chord* out;
+  const lg_mod_color* colors;
+  uint32_t n_colors;
+};
 __global__ void k_overlay(SceneDev S, TraceBufs B, const uint32_t* cubic_objs, const uint16_t* cubic_scene,
-                          uint32_t n_cubic, lg_string_mod sm);
+                          uint32_t n_cubic, lg_string_mod sm, ChordArgs CA);
 __global__ void k_scene_hist(SceneDev S, TraceBufs B, uint32_t gen, unsigned* count);
 __global__ void k_scene_offsets(unsigned* count, unsigned* off, uint32_t n_scenes);
 __global__ void k_scene_scatter(SceneDev S, TraceBufs B, uint32_t gen, unsigned* off, uint32_t* order);
@@ -94,6 +101,10 @@ __global__ void k_raster(RasterArgs A);
 int raster_smem_bytes(int mode);
 template <int MODE>
 __global__ void k_raster_warp(RasterArgs A);
+// String-mod lines straight into the image (one warp per line, global atomics), colour
+// interpolated along the major axis; FIXED: int64 Q31.32, else f32.
+template <bool FIXED>
+__global__ void k_raster_chords(RasterArgs A, const lg_chord* chords, uint64_t n);
 int raster_warp_smem_bytes();
 constexpr int RM_FIXED_SPLIT_ = 0, RM_FIXED_MINMAX_ = 1, RM_F32_ = 2;
 // Segments per work unit of the shared-atomic raster: bounds the split-plane sums.

@@ -824,6 +824,76 @@ template __global__ void k_raster_warp<RM_FIXED_SPLIT>(RasterArgs A);
 template __global__ void k_raster_warp<RM_F32>(RasterArgs A);
 int raster_warp_smem_bytes() { return 4 * TILE_PX * 8 + 32 * 48; }
 
+// ------------------------------------------------------------------ string-mod lines
+// A few thousand lines per frame: one warp per line, one lane per major-axis pixel, and
+// each pixel's terms go straight into the image with global atomics (int64 sums and
+// min / max are order-independent, so the image stays bit-reproducible in fixed point).
+template <bool FIXED>
+__global__ void __launch_bounds__(256) k_raster_chords(RasterArgs A, const lg_chord* chords, uint64_t n) {
+  const unsigned lane = lane_id();
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const BlendDev& B = A.blend;
+  const float sc = (float)A.H * 0.5f, cx = (float)A.W * 0.5f;
+  unsigned long long my_pixels = 0;
+  for (uint64_t k = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; k < n; k += nw) {
+    const lg_chord c = chords[k];
+    lg_segment sg;
+    sg.x0 = c.x0; sg.y0 = c.y0; sg.x1 = c.x1; sg.y1 = c.y1;
+    RSetup R;
+    if (!raster_setup(sg, A.W, A.H, R)) continue;
+    // the vertices' major coordinates before raster_setup orders them
+    const float U0 = R.xmajor ? __fmaf_rn(c.x0, sc, cx) : __fmaf_rn(-c.y0, sc, sc);
+    const float dU = __fsub_rn(R.xmajor ? __fmaf_rn(c.x1, sc, cx) : __fmaf_rn(-c.y1, sc, sc), U0);
+    float dc[4];
+#pragma unroll
+    for (int ch = 0; ch < 4; ++ch) dc[ch] = __fsub_rn(c.color1[ch], c.color0[ch]);
+    const int nmin = (int)(R.xmajor ? A.H : A.W);
+    for (int i = R.lo + (int)lane; i < R.hi; i += 32) {
+      const int j = raster_minor(R, i);
+      if (j < 0 || j >= nmin) continue;
+      float f = __fdiv_rn(__fsub_rn(__fadd_rn((float)i, 0.5f), U0), dU);
+      f = fminf(fmaxf(f, 0.0f), 1.0f);
+      float src[4];
+#pragma unroll
+      for (int ch = 0; ch < 4; ++ch) src[ch] = __fmaf_rn(f, dc[ch], c.color0[ch]);
+      const uint32_t x = R.xmajor ? (uint32_t)i : (uint32_t)j, y = R.xmajor ? (uint32_t)j : (uint32_t)i;
+      const uint64_t px = ((uint64_t)y * A.W + x) * 4;
+#pragma unroll
+      for (int ch = 0; ch < 4; ++ch) {
+        const int op = B.op[ch];
+        const float v = contribution(B, ch, src);
+        if (FIXED) {
+          long long q = to_fixed(v);
+          long long* g = reinterpret_cast<long long*>(A.accum) + px + ch;
+          if (op == LG_BO_MIN) atomicMin(g, q);
+          else if (op == LG_BO_MAX) atomicMax(g, q);
+          else {
+            if (op == LG_BO_REVERSE_SUBTRACT) q = -q;
+            if (q) atomicAdd(reinterpret_cast<unsigned long long*>(g), (unsigned long long)q);
+          }
+        } else {
+          float* g = reinterpret_cast<float*>(A.accum) + px + ch;
+          if (op == LG_BO_MIN || op == LG_BO_MAX) {
+            float o = *g;
+            while (op == LG_BO_MIN ? v < o : v > o) {
+              const float w = __int_as_float(atomicCAS(reinterpret_cast<int*>(g), __float_as_int(o), __float_as_int(v)));
+              if (w == o) break;
+              o = w;
+            }
+          } else {
+            atomicAdd(g, op == LG_BO_REVERSE_SUBTRACT ? -v : v);
+          }
+        }
+      }
+      ++my_pixels;
+    }
+  }
+  if (my_pixels) atomicAdd(&A.ctr->pixels, my_pixels);
+}
+
+template __global__ void k_raster_chords<true>(RasterArgs A, const lg_chord* chords, uint64_t n);
+template __global__ void k_raster_chords<false>(RasterArgs A, const lg_chord* chords, uint64_t n);
+
 template __global__ void k_raster<RM_FIXED_SPLIT>(RasterArgs A);
 template __global__ void k_raster<RM_FIXED_MINMAX>(RasterArgs A);
 template __global__ void k_raster<RM_F32>(RasterArgs A);

@@ -447,6 +447,8 @@ lg_status lg_serve_submit(lg_ctx* c, const lg_scene_desc* d, uint64_t* id_out) {
     V.common = p;
     V.have_common = true;
     c->prm = p;  // blend state for the raster
+    c->prm.string_mod.colors = nullptr;
+    c->chords_ready = 0;
   }
   R.id = V.next_id++;
   *id_out = R.id;
@@ -553,7 +555,7 @@ lg_status lg_serve_step(lg_ctx* c, lg_serve_step_stats* stats) {
     std::memset(&no_sm, 0, sizeof no_sm);
     const int blocks = (int)std::min<uint64_t>((3ull * cubic_obj.size() + 255) / 256, 4096);
     k_overlay<<<blocks, 256, 0, c->stream>>>(SD, B, (const uint32_t*)c->d_cubics.p, (const uint16_t*)c->d_cubic_scene.p,
-                                             (uint32_t)cubic_obj.size(), no_sm);
+                                             (uint32_t)cubic_obj.size(), no_sm, ChordArgs{});
   }
   // rays left per scene after this step
   CK(cudaMemsetAsync(V.d_live.p, 0, (size_t)V.max_slots * 4, c->stream), "live counts");

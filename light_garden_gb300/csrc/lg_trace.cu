@@ -1089,18 +1089,88 @@ __global__ void k_scene_scatter(SceneDev S, TraceBufs B, uint32_t gen, unsigned*
 }
 
 // ------------------------------------------------------------------- overlays
-// Curved-mirror control lines (tracer.rs:341-346) and the string-mod chords
-// (string_mod.rs:45-55, 104-122) appended after the traced segments.
+// A point of the string-mod curve (string_mod.rs:33-85), the same FP64 operations as the
+// oracle: angle (turns * n) * 2 pi / m, the library's own sine and cosine.
+__device__ void string_mod_point(const lg_string_mod& sm, uint64_t n, double& x, double& y) {
+  using namespace lgx;
+  const uint64_t k = sm.turns * n;
+  if (sm.curve == LG_CURVE_COMPLEX_EXP) {
+    // (re + i im)^(u32)k by binary powering (num-complex 0.4.6, Pow<u32> for &Complex)
+    uint32_t e = (uint32_t)k;
+    if (e == 0) { x = 1.0; y = 0.0; return; }
+    double br = sm.curve_f[0], bi = sm.curve_f[1];
+    while ((e & 1u) == 0) {
+      const double r = sub(mul(br, br), mul(bi, bi)), i = add(mul(br, bi), mul(bi, br));
+      br = r; bi = i; e >>= 1;
+    }
+    double ar = br, ai = bi;
+    while (e > 1) {
+      e >>= 1;
+      const double r = sub(mul(br, br), mul(bi, bi)), i = add(mul(br, bi), mul(bi, br));
+      br = r; bi = i;
+      if (e & 1u) {
+        const double r2 = sub(mul(ar, br), mul(ai, bi)), i2 = add(mul(ar, bi), mul(ai, br));
+        ar = r2; ai = i2;
+      }
+    }
+    x = ar; y = ai;
+    return;
+  }
+  const double angle = dvd(mul((double)k, 2.0 * 3.141592653589793), (double)sm.modulo);
+  double s, c;
+  if (sm.curve == LG_CURVE_HYPOTROCHOID) {
+    const double r = (double)sm.curve_u[0], big = (double)sm.curve_u[1], d = (double)sm.curve_u[2];
+    const double smr = sub(big, r), ratio = add(smr, d);
+    double s2, c2;
+    sincos_x(angle, s, c);
+    sincos_x(dvd(mul(angle, smr), r), s2, c2);
+    x = dvd(add(mul(smr, c), mul(d, c2)), ratio);
+    y = dvd(sub(mul(smr, s), mul(d, s2)), ratio);
+  } else if (sm.curve == LG_CURVE_LISSAJOUS) {
+    double s2, c2;
+    sincos_x(add(mul((double)sm.curve_u[0], angle), sm.curve_f[0]), s, c);
+    sincos_x(mul((double)sm.curve_u[1], angle), s2, c2);
+    x = s;
+    y = s2;
+  } else {
+    sincos_x(angle, s, c);
+    x = c;
+    y = s;
+  }
+}
+
+// StringMod::get_color (string_mod.rs:124-150): the f32 mean of the matching modulo colours,
+// summed in table order, else the base colour.
+__device__ void string_mod_color(const lg_string_mod& sm, const lg_mod_color* colors, uint32_t n_colors,
+                                 uint64_t ix, float* out) {
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  uint32_t cnt = 0;
+  for (uint32_t k = 0; k < n_colors; ++k) {
+    const lg_mod_color& e = colors[k];
+    if (ix % e.modulo == e.rem) {
+#pragma unroll
+      for (int ch = 0; ch < 4; ++ch) acc[ch] = __fadd_rn(acc[ch], e.color[ch]);
+      ++cnt;
+    }
+  }
+#pragma unroll
+  for (int ch = 0; ch < 4; ++ch) out[ch] = cnt ? __fdiv_rn(acc[ch], (float)cnt) : sm.color[ch];
+}
+
+// Overlays drawn after the trace: the control polygons of curved mirrors (tracer.rs:341-346)
+// appended to the segment ring, and the string-mod lines (string_mod.rs:104-122) written to
+// their own table, one per point: chord iix joins point iix and point ix(iix) of the mode,
+// each vertex with its own colour.
 __global__ void k_overlay(SceneDev S, TraceBufs B, const uint32_t* cubic_objs, const uint16_t* cubic_scene,
-                          uint32_t n_cubic, lg_string_mod sm) {
+                          uint32_t n_cubic, lg_string_mod sm, ChordArgs CA) {
   const uint64_t n_ctrl = 3ull * n_cubic;
   const uint64_t total = n_ctrl + sm.modulo;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-    lg_segment s;
-    lg_path_record pr;
-    pr.path = 0; pr.light = 0xffff; pr.flags = 0; pr.hit = -1;
-    uint16_t scene = 0;
     if (i < n_ctrl) {
+      lg_segment s;
+      lg_path_record pr;
+      pr.path = 0; pr.light = 0xffff; pr.flags = 0; pr.hit = -1;
+      uint16_t scene = 0;
       if (cubic_scene) scene = cubic_scene[i / 3];
       const uint32_t k = cubic_objs[i / 3];
       const int q = (int)(i % 3);
@@ -1109,6 +1179,12 @@ __global__ void k_overlay(SceneDev S, TraceBufs B, const uint32_t* cubic_objs, c
       s.x1 = L.p[2 * q + 2].hi; s.y1 = L.p[2 * q + 3].hi;
       s.color[0] = 1.f; s.color[1] = 0.f; s.color[2] = 0.f; s.color[3] = 1.f;
       pr.primary = k; pr.gen = (uint8_t)q; pr.source = LG_SRC_CONTROL_LINE;
+      const unsigned long long slot = atomicAdd(&B.ctr->seg_count, 1ull);
+      if (slot < B.seg_cap) {
+        B.segs[slot] = s;
+        if (B.seg_scene) B.seg_scene[slot] = scene;
+        if (S.record_paths) B.paths[slot] = pr;
+      }
     } else {
       const uint64_t m = sm.modulo, iix = i - n_ctrl;
       uint64_t ix;
@@ -1119,21 +1195,14 @@ __global__ void k_overlay(SceneDev S, TraceBufs B, const uint32_t* cubic_objs, c
         while (e) { if (e & 1) p *= b; b *= b; e >>= 1; }
         ix = p % m;
       }
-      // string_mod.rs:45-55 point angles, with the ray generators' sin / cos
-      const double aa = lgx::dvd(lgx::mul((double)(sm.turns * (iix % m)), 2.0 * 3.141592653589793), (double)m);
-      const double ab = lgx::dvd(lgx::mul((double)(sm.turns * (ix % m)), 2.0 * 3.141592653589793), (double)m);
-      double sa, ca, sb, cb;
-      lgx::sincos_x(aa, sa, ca);
-      lgx::sincos_x(ab, sb, cb);
-      s.x0 = (float)ca; s.y0 = (float)sa; s.x1 = (float)cb; s.y1 = (float)sb;
-      s.color[0] = sm.color[0]; s.color[1] = sm.color[1]; s.color[2] = sm.color[2]; s.color[3] = sm.color[3];
-      pr.primary = (uint32_t)iix; pr.gen = 0; pr.source = LG_SRC_STRING_MOD;
-    }
-    const unsigned long long slot = atomicAdd(&B.ctr->seg_count, 1ull);
-    if (slot < B.seg_cap) {
-      B.segs[slot] = s;
-      if (B.seg_scene) B.seg_scene[slot] = scene;
-      if (S.record_paths) B.paths[slot] = pr;
+      double xa, ya, xb, yb;
+      string_mod_point(sm, iix % m, xa, ya);
+      string_mod_point(sm, ix % m, xb, yb);
+      lg_chord c;
+      c.x0 = (float)xa; c.y0 = (float)ya; c.x1 = (float)xb; c.y1 = (float)yb;
+      string_mod_color(sm, CA.colors, CA.n_colors, iix, c.color0);
+      string_mod_color(sm, CA.colors, CA.n_colors, ix, c.color1);
+      if (CA.out) CA.out[iix] = c;
     }
   }
 }

@@ -106,6 +106,17 @@ class Context:
         self._check(st, "lg_render")
         return s.as_dict()
 
+    def chords(self):
+        """The frame's string-mod lines (lg_chord records), two colours each."""
+        n = C.c_uint64(0)
+        st = self.lib.lg_chords_download(self.h, None, 0, C.byref(n))
+        if st not in (abi.LG_OK, abi.LG_ERR_TRUNCATED):
+            self._check(st, "lg_chords_download")
+        out = np.zeros(int(n.value), abi.chord_dtype())
+        self._check(self.lib.lg_chords_download(self.h, out.ctypes.data_as(C.POINTER(abi.lg_chord)), len(out),
+                                                C.byref(n)), "lg_chords_download")
+        return out
+
     def segments(self, paths: bool = False):
         n = C.c_uint64(0)
         st = self.lib.lg_segments_download(self.h, None, None, 0, C.byref(n))

@@ -11,7 +11,8 @@ generators stand in for the configurations:
 * :func:`csg_scene`     256 CSG objects (circle op rect), 2^22 rays, 32 bounces, 4096x4096,
                         string-mod overlay (m = 4096, chords i -> 7 i mod m);
 * :func:`batch_scenes`  mixed sizes: objects log-uniform [4, 1024], rays log-uniform
-                        [2^12, 2^20], bounces U{4..32}, canvases {256, 512, 1024, 2048}^2.
+                        [2^12, 2^20], bounces U{4..32}, canvases {256, 512, 1024, 2048}^2;
+* :func:`string_mod_art` string-mod line art on each of the four curves, with modulo colours.
 
 Choices the configurations leave open (spot angle U[10, 90] degrees, directional segment
 length U[0.1, 0.5], the curved-mirror template, the CSG child placement) are made here
@@ -139,6 +140,36 @@ def csg_scene(seed: int = 3, total_rays: int = 1 << 22, n_objects: int = 256, n_
         p.string_mod.curve = 0
         p.string_mod.color[:] = (0.25, 0.25, 0.25, 1.0)
     return Workload("csg_scene", objects, lights, p)
+
+
+# string-mod line art of each curve (string_mod.rs:182-188): (curve, modulo, num, mode, turns,
+# curve_f, curve_u, modulo colours)
+_STRING_MOD_ART = {
+    abi.LG_CURVE_CIRCLE: (1500, 7, abi.LG_SM_MUL, 1, (0.0, 0.0), (0, 0, 0),
+                          [(3, 0, (1.0, 0.1, 0.1, 1.0)), (5, 2, (0.1, 1.0, 0.2, 1.0)), (7, 1, (0.2, 0.4, 1.0, 0.5))]),
+    abi.LG_CURVE_COMPLEX_EXP: (2000, 2, abi.LG_SM_POW, 1,
+                               (0.9998 * math.cos(2 * math.pi / 400), 0.9998 * math.sin(2 * math.pi / 400)), (0, 0, 0),
+                               [(2, 1, (0.9, 0.6, 0.1, 1.0)), (9, 4, (0.2, 0.2, 1.0, 0.8))]),
+    abi.LG_CURVE_HYPOTROCHOID: (1800, 13, abi.LG_SM_MUL, 3, (0.0, 0.0), (3, 5, 2),
+                                [(4, 3, (0.0, 1.0, 1.0, 1.0))]),
+    abi.LG_CURVE_LISSAJOUS: (2048, 5, abi.LG_SM_BASE, 1, (0.5, 0.0), (3, 4, 0),
+                             [(2, 0, (1.0, 1.0, 0.0, 1.0)), (3, 0, (1.0, 0.0, 1.0, 1.0)), (6, 0, (0.0, 0.0, 0.0, 1.0))]),
+}
+
+
+def string_mod_art(curve: int = abi.LG_CURVE_CIRCLE, width: int = 1024, height: int = 1024,
+                   colors: bool = True) -> Workload:
+    """String-mod line art (StringMod::draw, string_mod.rs:152-158) on one curve, with
+    modulo colours, over a small traced scene (one point light, 64 rays, no objects)."""
+    m, num, mode, turns, cf, cu, table = _STRING_MOD_ART[curve]
+    p = _params(4, width, height, abi.LG_ACCUM_FIXED64)
+    sm = p.string_mod
+    sm.modulo, sm.num, sm.mode, sm.turns, sm.curve = m, num, mode, turns, curve
+    sm.color[:] = (0.3, 0.3, 0.3, 1.0)
+    sm.curve_f[:] = cf
+    sm.curve_u[:] = cu
+    abi.set_mod_colors(p, table if colors else [])
+    return Workload(f"string_mod_art_{curve}", [], [PointLight((0.1, -0.2), 64, (1.0, 1.0, 1.0, 1.0))], p)
 
 
 def _shape_object(rng, kind: str) -> Object:

@@ -914,6 +914,104 @@ static uint64_t wrapping_pow(uint64_t b, uint64_t e) {
   return r;
 }
 
+/* ---------------------------------------------------------------- string mod
+ * string_mod.rs:33-85 (init_points), 104-122 (draw_init_points), 124-150 (get_color).
+ * The point angle is (turns * n) as f64 * TAU / m, multiplied before the division as in
+ * the reference; sine and cosine are lgo_sincos. */
+
+/* num-complex 0.4.6 (Cargo.lock), Pow<u32> for &Complex<f64>: binary powering that squares
+ * the base past the trailing zero bits of the exponent, then multiplies the accumulator by
+ * every later square whose bit is set; products (a.re b.re - a.im b.im, a.re b.im + a.im b.re). */
+static void cmul(double ar, double ai, double br, double bi, double* r, double* i) {
+  *r = ar * br - ai * bi;
+  *i = ar * bi + ai * br;
+}
+static void cpowu(double re, double im, uint32_t e, double* orr, double* oi) {
+  if (e == 0) { *orr = 1.0; *oi = 0.0; return; }
+  double br = re, bi = im;
+  while ((e & 1u) == 0) { cmul(br, bi, br, bi, &br, &bi); e >>= 1; }
+  if (e == 1) { *orr = br; *oi = bi; return; }
+  double ar = br, ai = bi;
+  while (e > 1) {
+    e >>= 1;
+    cmul(br, bi, br, bi, &br, &bi);
+    if (e & 1u) cmul(ar, ai, br, bi, &ar, &ai);
+  }
+  *orr = ar; *oi = ai;
+}
+
+static void string_mod_point(const lg_string_mod* sm, uint64_t n, double* x, double* y) {
+  const uint64_t k = sm->turns * n; /* u64, wrapping */
+  if (sm->curve == LG_CURVE_COMPLEX_EXP) {
+    cpowu(sm->curve_f[0], sm->curve_f[1], (uint32_t)k, x, y);
+    return;
+  }
+  const double angle = (double)k * (2.0 * M_PI) / (double)sm->modulo;
+  double s, c;
+  if (sm->curve == LG_CURVE_HYPOTROCHOID) {
+    const double r = (double)sm->curve_u[0], big = (double)sm->curve_u[1], d = (double)sm->curve_u[2];
+    const double smr = big - r, ratio = smr + d;
+    double s2, c2;
+    lgo_sincos(angle, &s, &c);
+    lgo_sincos(angle * smr / r, &s2, &c2);
+    *x = (smr * c + d * c2) / ratio;
+    *y = (smr * s - d * s2) / ratio;
+  } else if (sm->curve == LG_CURVE_LISSAJOUS) {
+    double s2, c2;
+    lgo_sincos((double)sm->curve_u[0] * angle + sm->curve_f[0], &s, &c);
+    lgo_sincos((double)sm->curve_u[1] * angle, &s2, &c2);
+    *x = s;
+    *y = s2;
+  } else {
+    lgo_sincos(angle, &s, &c);
+    *x = c;
+    *y = s;
+  }
+}
+
+static void string_mod_color(const lg_string_mod* sm, uint64_t ix, float* out) {
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  uint32_t cnt = 0;
+  for (uint32_t k = 0; k < sm->n_colors; ++k) {
+    const lg_mod_color* e = &sm->colors[k];
+    if (ix % e->modulo == e->rem) {
+      for (int ch = 0; ch < 4; ++ch) acc[ch] += e->color[ch];
+      ++cnt;
+    }
+  }
+  for (int ch = 0; ch < 4; ++ch) out[ch] = cnt ? acc[ch] / (float)cnt : sm->color[ch];
+}
+
+int lgo_string_mod_chords(const lg_params* prm, lg_chord* out, uint64_t cap, uint64_t* n_out) {
+  if (!prm || !n_out) return LGO_ERR_INVALID;
+  const lg_string_mod* sm = &prm->string_mod;
+  const uint64_t m = sm->modulo;
+  *n_out = m;
+  if (m == 0) return LGO_OK;
+  if (sm->curve > LG_CURVE_LISSAJOUS || sm->mode > LG_SM_BASE) return LGO_ERR_UNSUPPORTED;
+  if (sm->n_colors && !sm->colors) return LGO_ERR_INVALID;
+  for (uint32_t k = 0; k < sm->n_colors; ++k)
+    if (sm->colors[k].modulo == 0) return LGO_ERR_INVALID;
+  if (cap < m) return LGO_ERR_TRUNCATED;
+  for (uint64_t iix = 0; iix < m; ++iix) {
+    uint64_t ix;
+    switch (sm->mode) {
+      case LG_SM_ADD: ix = (iix + sm->num) % m; break;
+      case LG_SM_MUL: ix = (iix * sm->num) % m; break;
+      case LG_SM_POW: ix = wrapping_pow(iix, (uint32_t)sm->num) % m; break;
+      default: ix = wrapping_pow(sm->num, (uint32_t)iix) % m; break;
+    }
+    double xa, ya, xb, yb;
+    string_mod_point(sm, iix % m, &xa, &ya);
+    string_mod_point(sm, ix % m, &xb, &yb);
+    lg_chord* c = &out[iix];
+    c->x0 = (float)xa; c->y0 = (float)ya; c->x1 = (float)xb; c->y1 = (float)yb;
+    string_mod_color(sm, iix, c->color0);
+    string_mod_color(sm, ix, c->color1);
+  }
+  return LGO_OK;
+}
+
 int lgo_trace(const lg_geo* geos, uint32_t n_geo, const lg_object* objs, uint32_t n_obj,
               const lg_light* lights, uint32_t n_lights, const lg_params* prm,
               uint32_t ray_stride, uint32_t ray_offset, int n_threads,
@@ -977,29 +1075,6 @@ int lgo_trace(const lg_geo* geos, uint32_t n_geo, const lg_object* objs, uint32_
         lg_path_record r = {0, k, 0xffff, (uint8_t)s, 0, -1, LG_SRC_CONTROL_LINE};
         rc = buf_push(ov, mk(v[2 * s], v[2 * s + 1]), mk(v[2 * s + 2], v[2 * s + 3]), red, &r);
       }
-    }
-  }
-  /* string-mod overlay (string_mod.rs:45-55 Circle points, 104-122 draw_init_points) */
-  if (!rc && ray_offset == 0 && prm->string_mod.modulo > 0) {
-    const lg_string_mod* sm = &prm->string_mod;
-    if (sm->curve != 0 || sm->mode > LG_SM_BASE) rc = LGO_ERR_UNSUPPORTED;
-    uint64_t m = sm->modulo;
-    for (uint64_t iix = 0; iix < m && !rc; ++iix) {
-      uint64_t ix;
-      switch (sm->mode) {
-        case LG_SM_ADD: ix = (iix + sm->num) % m; break;
-        case LG_SM_MUL: ix = (iix * sm->num) % m; break;
-        case LG_SM_POW: ix = wrapping_pow(iix, (uint32_t)sm->num) % m; break;
-        default: ix = wrapping_pow(sm->num, (uint32_t)iix) % m; break;
-      }
-      uint64_t ia = iix % m, ib = ix % m;
-      double aa = (double)(sm->turns * ia) * (2.0 * M_PI) / (double)m;
-      double ab = (double)(sm->turns * ib) * (2.0 * M_PI) / (double)m;
-      lg_path_record r = {0, (uint32_t)iix, 0xffff, 0, 0, -1, LG_SRC_STRING_MOD};
-      double sa, ca, sb, cb;
-      lgo_sincos(aa, &sa, &ca);
-      lgo_sincos(ab, &sb, &cb);
-      rc = buf_push(ov, mk(ca, sa), mk(cb, sb), sm->color, &r);
     }
   }
   uint64_t total = 0, visits = 0, nearc = 0;
@@ -1236,6 +1311,89 @@ int lgo_raster(const lg_segment* segs, uint64_t n, const lg_params* P, int64_t* 
   for (int t = 0; t < nt; ++t) {
     pthread_join(th[t], NULL);
     px += J[t].pixels;
+  }
+  if (pixels) *pixels = px;
+  return LGO_OK;
+}
+
+/* String-mod lines: the raster rule of the segments, with the colour interpolated along
+ * the major axis (f from the unswapped vertex coordinates, clamped to [0, 1]). */
+static void chord_setup(const lg_chord* c, uint32_t W, uint32_t H, lg_segment* sg, float* u0, float* du) {
+  sg->x0 = c->x0; sg->y0 = c->y0; sg->x1 = c->x1; sg->y1 = c->y1;
+  for (int ch = 0; ch < 4; ++ch) sg->color[ch] = c->color0[ch];
+  float sc = (float)H * 0.5f, cx = (float)W * 0.5f, cy = sc;
+  float X0 = fmaf(c->x0, sc, cx), Y0 = fmaf(-c->y0, sc, cy);
+  float X1 = fmaf(c->x1, sc, cx), Y1 = fmaf(-c->y1, sc, cy);
+  int xmajor = fabsf(X1 - X0) >= fabsf(Y1 - Y0);
+  *u0 = xmajor ? X0 : Y0;
+  *du = (xmajor ? X1 : Y1) - *u0;
+}
+
+static void chord_color(const lg_chord* c, float u0, float du, int i, float* src) {
+  float f = (((float)i + 0.5f) - u0) / du;
+  f = f < 0.0f ? 0.0f : (f > 1.0f ? 1.0f : f);
+  for (int ch = 0; ch < 4; ++ch) src[ch] = fmaf(f, c->color1[ch] - c->color0[ch], c->color0[ch]);
+}
+
+int lgo_raster_chords(const lg_chord* chords, uint64_t n, const lg_params* P, int64_t* acc, uint64_t* pixels) {
+  if (!P || !acc || (n && !chords)) return LGO_ERR_INVALID;
+  if (!blend_ok(&P->color_blend) || !blend_ok(&P->alpha_blend)) return LGO_ERR_UNSUPPORTED;
+  uint32_t W = P->width, H = P->height;
+  uint64_t px = 0;
+  for (uint64_t k = 0; k < n; ++k) {
+    lg_segment sg;
+    float u0, du;
+    chord_setup(&chords[k], W, H, &sg, &u0, &du);
+    rsetup R;
+    if (!raster_setup(&sg, W, H, &R)) continue;
+    for (int i = R.lo; i < R.hi; ++i) {
+      int j = raster_minor(&R, i);
+      int x = R.xmajor ? i : j, y = R.xmajor ? j : i;
+      if (x < 0 || y < 0 || x >= (int)W || y >= (int)H) continue;
+      float src[4], val[4];
+      int op[4];
+      chord_color(&chords[k], u0, du, i, src);
+      contribution(P, src, val, op);
+      int64_t q[4];
+      for (int ch = 0; ch < 4; ++ch) q[ch] = lgo_fixed(val[ch]);
+      apply(&acc[4 * ((uint64_t)y * W + (uint64_t)x)], q, op);
+      ++px;
+    }
+  }
+  if (pixels) *pixels = px;
+  return LGO_OK;
+}
+
+int lgo_raster_chords_f64(const lg_chord* chords, uint64_t n, const lg_params* P, double* acc, uint64_t* pixels) {
+  if (!P || !acc || (n && !chords)) return LGO_ERR_INVALID;
+  if (!blend_ok(&P->color_blend) || !blend_ok(&P->alpha_blend)) return LGO_ERR_UNSUPPORTED;
+  uint32_t W = P->width, H = P->height;
+  uint64_t px = 0;
+  for (uint64_t k = 0; k < n; ++k) {
+    lg_segment sg;
+    float u0, du;
+    chord_setup(&chords[k], W, H, &sg, &u0, &du);
+    rsetup R;
+    if (!raster_setup(&sg, W, H, &R)) continue;
+    for (int i = R.lo; i < R.hi; ++i) {
+      int j = raster_minor(&R, i);
+      int x = R.xmajor ? i : j, y = R.xmajor ? j : i;
+      if (x < 0 || y < 0 || x >= (int)W || y >= (int)H) continue;
+      float src[4], val[4];
+      int op[4];
+      chord_color(&chords[k], u0, du, i, src);
+      contribution(P, src, val, op);
+      double* p = &acc[4 * ((uint64_t)y * W + (uint64_t)x)];
+      for (int ch = 0; ch < 4; ++ch) {
+        switch (op[ch]) {
+          case LG_BO_ADD: p[ch] += val[ch]; break;
+          case LG_BO_REVERSE_SUBTRACT: p[ch] -= val[ch]; break;
+          case LG_BO_MIN: if (val[ch] < p[ch]) p[ch] = val[ch]; break;
+          default: if (val[ch] > p[ch]) p[ch] = val[ch]; break;
+        }
+      }
+      ++px;
+    }
   }
   if (pixels) *pixels = px;
   return LGO_OK;

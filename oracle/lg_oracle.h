@@ -43,14 +43,24 @@ typedef struct lgo_hit {
 } lgo_hit;
 
 /* Trace every light (tracer.rs:276-358).  Only primaries with i % ray_stride == ray_offset
- * are traced (ray_stride = 1 traces all).  Overlays (control lines, string mod) are
- * appended when ray_offset == 0 and the params ask for them.  seg64 (optional) receives
+ * are traced (ray_stride = 1 traces all).  The curved-mirror control lines are appended
+ * when ray_offset == 0 and the params ask for them (string-mod lines: lgo_string_mod_chords).  seg64 (optional) receives
  * x0,y0,x1,y1 in FP64 per segment.  n_threads <= 0 uses all online cores. */
 int lgo_trace(const lg_geo* geos, uint32_t n_geo, const lg_object* objs, uint32_t n_obj,
               const lg_light* lights, uint32_t n_lights, const lg_params* prm,
               uint32_t ray_stride, uint32_t ray_offset, int n_threads,
               lg_segment* segs, lg_path_record* paths, double* seg64, uint64_t cap,
               uint64_t* n_out, lgo_stats* stats);
+
+/* String-mod lines of prm->string_mod (string_mod.rs:33-150): modulo of them, written to
+ * out[0..modulo).  *n_out receives the count; LGO_ERR_TRUNCATED when cap is smaller. */
+int lgo_string_mod_chords(const lg_params* prm, lg_chord* out, uint64_t cap, uint64_t* n_out);
+/* Raster of string-mod lines (the segment raster rule, colour interpolated along the major
+ * axis as include/lg.h states for lg_chord), into the same images as lgo_raster(_f64). */
+int lgo_raster_chords(const lg_chord* chords, uint64_t n, const lg_params* prm, int64_t* accum,
+                      uint64_t* pixels);
+int lgo_raster_chords_f64(const lg_chord* chords, uint64_t n, const lg_params* prm, double* accum,
+                          uint64_t* pixels);
 
 /* The ray generators' sin / cos / atan (see lg_oracle.c: plain IEEE double operations,
  * within a few ulp of the C library). */

@@ -64,6 +64,10 @@ def lib() -> C.CDLL:
                                  P(C.c_uint64)]
         L.lgo_raster_f64.argtypes = [P(abi.lg_segment), C.c_uint64, P(abi.lg_params), P(C.c_double),
                                      P(C.c_uint64)]
+        L.lgo_string_mod_chords.argtypes = [P(abi.lg_params), P(abi.lg_chord), C.c_uint64, P(C.c_uint64)]
+        L.lgo_raster_chords.argtypes = [P(abi.lg_chord), C.c_uint64, P(abi.lg_params), P(C.c_int64), P(C.c_uint64)]
+        L.lgo_raster_chords_f64.argtypes = [P(abi.lg_chord), C.c_uint64, P(abi.lg_params), P(C.c_double),
+                                            P(C.c_uint64)]
         L.lgo_resolve_f16.argtypes = [P(C.c_int64), C.c_uint32, C.c_uint32, P(C.c_uint16)]
         L.lgo_resolve_rgba8.argtypes = [P(C.c_int64), C.c_uint32, C.c_uint32, P(C.c_uint8)]
         L.lgo_f32_to_f16.restype = C.c_uint16
@@ -145,8 +149,20 @@ def clear(params) -> np.ndarray:
     return acc
 
 
-def raster(segs: np.ndarray, params, threads: int = 0, acc: np.ndarray | None = None):
-    """Fixed-point raster of segments into a cleared image.  Returns (image int64, pixels)."""
+def string_mod_chords(params) -> np.ndarray:
+    """The string-mod lines of params.string_mod (lgo_string_mod_chords)."""
+    n = C.c_uint64(0)
+    m = int(params.string_mod.modulo)
+    out = np.zeros(m, abi.chord_dtype())
+    rc = lib().lgo_string_mod_chords(C.byref(params), out.ctypes.data_as(C.POINTER(abi.lg_chord)), m, C.byref(n))
+    if rc:
+        raise OracleError(f"lgo_string_mod_chords: {rc}")
+    return out
+
+
+def raster(segs: np.ndarray, params, threads: int = 0, acc: np.ndarray | None = None, chords=None):
+    """Fixed-point raster of segments (and string-mod lines) into a cleared image.
+    Returns (image int64, pixels)."""
     if acc is None:
         acc = clear(params)
     segs = np.ascontiguousarray(segs)
@@ -155,10 +171,18 @@ def raster(segs: np.ndarray, params, threads: int = 0, acc: np.ndarray | None = 
                           acc.ctypes.data_as(C.POINTER(C.c_int64)), threads, C.byref(px))
     if rc:
         raise OracleError(f"lgo_raster: {rc}")
-    return acc, int(px.value)
+    total = int(px.value)
+    if chords is not None and len(chords):
+        ch = np.ascontiguousarray(chords, dtype=abi.chord_dtype())
+        rc = lib().lgo_raster_chords(ch.ctypes.data_as(C.POINTER(abi.lg_chord)), len(ch), C.byref(params),
+                                     acc.ctypes.data_as(C.POINTER(C.c_int64)), C.byref(px))
+        if rc:
+            raise OracleError(f"lgo_raster_chords: {rc}")
+        total += int(px.value)
+    return acc, total
 
 
-def raster_f64(segs: np.ndarray, params):
+def raster_f64(segs: np.ndarray, params, chords=None):
     acc = np.zeros((params.height, params.width, 4), np.float64)
     acc[...] = np.array(params.clear_color[:], np.float64)
     segs = np.ascontiguousarray(segs)
@@ -167,7 +191,15 @@ def raster_f64(segs: np.ndarray, params):
                               acc.ctypes.data_as(C.POINTER(C.c_double)), C.byref(px))
     if rc:
         raise OracleError(f"lgo_raster_f64: {rc}")
-    return acc, int(px.value)
+    total = int(px.value)
+    if chords is not None and len(chords):
+        ch = np.ascontiguousarray(chords, dtype=abi.chord_dtype())
+        rc = lib().lgo_raster_chords_f64(ch.ctypes.data_as(C.POINTER(abi.lg_chord)), len(ch), C.byref(params),
+                                         acc.ctypes.data_as(C.POINTER(C.c_double)), C.byref(px))
+        if rc:
+            raise OracleError(f"lgo_raster_chords_f64: {rc}")
+        total += int(px.value)
+    return acc, total
 
 
 def resolve_f16(acc: np.ndarray) -> np.ndarray:

@@ -10,8 +10,8 @@ tests a stored answer that does not depend on rebuilding the oracle.
 
 Each case stores the segments (x0, y0, x1, y1 f32 + RGBA f32), their path records and the
 FP64 endpoints in canonical order (source, light, primary, generation, path bits), for every
-``stride``-th primary ray of each light, plus SHA-256 digests of the int64 image and the
-RGBA16F resolve where the full scene is traced.
+``stride``-th primary ray of each light, the string-mod lines (two colours each), plus SHA-256
+digests of the int64 image and the RGBA16F resolve where the full scene is traced.
 """
 from __future__ import annotations
 
@@ -34,6 +34,9 @@ CASES = {
     "mid_scene_subset": (lambda: W.mid_scene(), 8191, False),
     "csg_scene_subset": (lambda: W.csg_scene(), 65521, False),
 }
+for _curve, _name in ((abi.LG_CURVE_CIRCLE, "circle"), (abi.LG_CURVE_COMPLEX_EXP, "complex_exp"),
+                      (abi.LG_CURVE_HYPOTROCHOID, "hypotrochoid"), (abi.LG_CURVE_LISSAJOUS, "lissajous")):
+    CASES[f"string_mod_{_name}"] = ((lambda c=_curve: W.string_mod_art(c)), 1, True)
 
 
 def canonical(segs, paths, s64):
@@ -50,21 +53,23 @@ def run_case(name: str):
     pk = make().packed()
     segs, paths, s64, st = O.trace(pk, ray_stride=stride, threads=0)
     segs, paths, s64 = canonical(segs, paths, s64)
+    chords = O.string_mod_chords(pk.params)  # the sample starts at primary 0: the overlay is drawn
     meta = {"stride": stride, "segments": int(len(segs)), "primary_rays": int(st.primary_rays),
-            "near_degenerate": int(st.near_degenerate), "width": pk.params.width, "height": pk.params.height}
+            "near_degenerate": int(st.near_degenerate), "width": pk.params.width, "height": pk.params.height,
+            "chords": int(len(chords))}
     if images:
-        acc, px = O.raster(segs, pk.params, threads=0)
+        acc, px = O.raster(segs, pk.params, threads=0, chords=chords)
         meta.update(pixels=px, accum_sha256=digest(acc), f16_sha256=digest(O.resolve_f16(acc)),
                     rgba8_sha256=digest(O.resolve_rgba8(acc)))
-    return segs, paths, s64, meta
+    return segs, paths, s64, chords, meta
 
 
 def main():
     O.build()
     index = {}
     for name in CASES:
-        segs, paths, s64, meta = run_case(name)
-        np.savez_compressed(HERE / f"{name}.npz", segs=segs, paths=paths, s64=s64)
+        segs, paths, s64, chords, meta = run_case(name)
+        np.savez_compressed(HERE / f"{name}.npz", segs=segs, paths=paths, s64=s64, chords=chords)
         index[name] = meta
         print(name, meta)
     (HERE / "golden.json").write_text(json.dumps(index, indent=1, sort_keys=True) + "\n")

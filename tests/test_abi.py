@@ -12,8 +12,8 @@ from light_garden_gb300 import abi
 
 HEADER = abi.LIB_DIR.parent.parent / "include" / "lg.h"
 
-STRUCTS = [abi.lg_geo, abi.lg_object, abi.lg_light, abi.lg_blend_component, abi.lg_string_mod, abi.lg_params,
-           abi.lg_segment, abi.lg_path_record, abi.lg_trace_stats, abi.lg_device_opts, abi.lg_scene_desc,
+STRUCTS = [abi.lg_geo, abi.lg_object, abi.lg_light, abi.lg_blend_component, abi.lg_mod_color, abi.lg_string_mod,
+           abi.lg_params, abi.lg_segment, abi.lg_chord, abi.lg_path_record, abi.lg_trace_stats, abi.lg_device_opts, abi.lg_scene_desc,
            abi.lg_serve_opts, abi.lg_serve_step_stats]
 
 
@@ -52,7 +52,7 @@ def c_layout(tmp_path_factory):
 def test_header_compiles_as_c_and_cxx(tmp_path):
     for cc, ext in (("gcc", "c"), ("g++", "cpp")):
         src = tmp_path / f"h.{ext}"
-        src.write_text(f'#include "{HEADER}"\nint main(void) {{ return LG_ABI_VERSION == 3 ? 0 : 1; }}\n')
+        src.write_text(f'#include "{HEADER}"\nint main(void) {{ return LG_ABI_VERSION == 4 ? 0 : 1; }}\n')
         subprocess.run([cc, "-Wall", "-Werror", "-pedantic", "-o", str(tmp_path / f"h_{ext}"), str(src)],
                        check=True)
 
@@ -70,6 +70,8 @@ def test_record_sizes_are_the_documented_ones():
     assert C.sizeof(abi.lg_segment) == 32
     assert C.sizeof(abi.lg_path_record) == 24
     assert abi.segment_dtype().itemsize == 32 and abi.path_dtype().itemsize == 24
+    # a string-mod line: two vertices with their own colours (string_mod.rs:118-119)
+    assert C.sizeof(abi.lg_chord) == 48 and abi.chord_dtype().itemsize == 48
 
 
 def test_every_declared_function_is_exported(cuda_lib):
@@ -95,7 +97,7 @@ def test_library_exports_only_the_abi(cuda_lib):
 
 
 def test_abi_version_and_defaults(cuda_lib):
-    assert cuda_lib.lg_abi_version() == 3
+    assert cuda_lib.lg_abi_version() == 4
     p = abi.lg_params()
     cuda_lib.lg_params_default(C.byref(p))
     assert p.max_bounce == 5  # Tracer::new, tracer.rs:37

@@ -24,6 +24,10 @@ def load(name):
     return z["segs"], z["paths"], z["s64"]
 
 
+def load_chords(name):
+    return np.load(GOLD / f"{name}.npz")["chords"]
+
+
 def digest(a):
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
@@ -34,12 +38,13 @@ def test_oracle_reproduces_fixture(oracle, name):
     spec = importlib.util.spec_from_file_location("make_golden", GOLD / "make_golden.py")
     mg = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mg)
-    segs, paths, s64, meta = mg.run_case(name)
+    segs, paths, s64, chords, meta = mg.run_case(name)
     gs, gp, g64 = load(name)
     assert meta == INDEX[name]
     assert segs.tobytes() == gs.tobytes()
     assert paths.tobytes() == gp.tobytes()
     assert s64.tobytes() == g64.tobytes()
+    assert chords.tobytes() == load_chords(name).tobytes()
 
 
 def test_fixture_invariants():
@@ -126,3 +131,19 @@ def test_gpu_default_scene_from_ron_matches_fixture(ctx):
     assert rep.matched > 0.99 * len(z["segs"])
     ctx.accumulate()
     assert ctx.accum().shape == (meta["height"], meta["width"], 4)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", [n for n in sorted(INDEX) if n.startswith("string_mod_")])
+def test_gpu_string_mod_art_matches_fixture(ctx, name):
+    """String-mod line art on each curve with modulo colours: the GPU's lines equal the stored
+    ones bit for bit, and its rendered frame has the stored image digests."""
+    curve = {"circle": abi.LG_CURVE_CIRCLE, "complex_exp": abi.LG_CURVE_COMPLEX_EXP,
+             "hypotrochoid": abi.LG_CURVE_HYPOTROCHOID, "lissajous": abi.LG_CURVE_LISSAJOUS}[name[len("string_mod_"):]]
+    meta = INDEX[name]
+    ctx.upload(W.string_mod_art(curve).packed())
+    img, st = ctx.render()
+    assert ctx.chords().tobytes() == load_chords(name).tobytes()
+    assert st["pixels"] == meta["pixels"]
+    assert digest(ctx.accum()) == meta["accum_sha256"]
+    assert digest(img) == meta["f16_sha256"]

@@ -29,10 +29,13 @@ def _trace_exact(ctx, oracle, pk, stride=1, offset=0, image=False):
     rep = exact(gs, gp, os_, op)
     assert rep.ok(), rep
     assert rep.segments == len(os_) == len(gs) == st["segments"]
-    if image:  # the frame's fixed-point image equals the oracle's raster of its own segments
+    # the string-mod lines (drawn when the sample starts at primary 0), bit for bit
+    o_ch = oracle.string_mod_chords(pk.params) if offset == 0 else np.zeros(0, abi.chord_dtype())
+    assert ctx.chords().tobytes() == o_ch.tobytes()
+    if image:  # the frame's fixed-point image equals the oracle's raster of its own segments and lines
         ctx.accumulate()
         acc = ctx.accum()
-        o_acc, _ = oracle.raster(os_, pk.params)
+        o_acc, _ = oracle.raster(os_, pk.params, chords=o_ch)
         assert np.array_equal(acc, o_acc)
         assert np.array_equal(ctx.resolve_f16(), oracle.resolve_f16(o_acc))
     return st, rep
@@ -75,6 +78,7 @@ def test_fixtures_reproduced_exactly(ctx, oracle):
         rep = exact(gs, gp, z["segs"], z["paths"])
         assert rep.ok(), (name, rep)
         assert rep.segments == len(z["segs"])
+        assert ctx.chords().tobytes() == z["chords"].tobytes()
 
 
 def test_culling_grid_exact(gpu, oracle):
@@ -147,3 +151,65 @@ def test_batch_exact_images_equal_oracle(gpu, oracle):
         os_, _, _, _ = oracle.trace(pk)
         o_acc, _ = oracle.raster(os_, pk.params)
         assert np.array_equal(img, oracle.resolve_f16(o_acc))
+
+
+@pytest.mark.parametrize("curve", [abi.LG_CURVE_CIRCLE, abi.LG_CURVE_COMPLEX_EXP, abi.LG_CURVE_HYPOTROCHOID,
+                                   abi.LG_CURVE_LISSAJOUS])
+def test_string_mod_lines_and_blends_exact(ctx, oracle, curve):
+    """String-mod art on every curve with modulo colours: the lines bit for bit, and the image
+    (interpolated vertex colours) bit for bit in additive and max blending; in FP32
+    accumulation within the summation bound of the FP64 raster."""
+    w = W.string_mod_art(curve, 768, 512)
+    pk = w.packed()
+    _trace_exact(ctx, oracle, pk, image=True)
+    pk.params.color_blend = abi.lg_blend_component(abi.LG_BF_ONE, abi.LG_BF_ONE, abi.LG_BO_MAX)
+    pk.params.alpha_blend = abi.lg_blend_component(abi.LG_BF_ONE, abi.LG_BF_ONE, abi.LG_BO_MIN)
+    _trace_exact(ctx, oracle, pk, image=True)
+    pk = w.packed()
+    pk.params.accum = abi.LG_ACCUM_F32
+    pk.params.record_paths = 1
+    ctx.upload(pk)
+    ctx.trace()
+    ctx.accumulate()
+    os_, _, _, _ = oracle.trace(pk)
+    o_ch = oracle.string_mod_chords(pk.params)
+    f64, _ = oracle.raster_f64(os_, pk.params, chords=o_ch)
+    acc = ctx.accum().astype(np.float64)
+    # the number of terms n of every pixel: the same lines in white, One/One added in fixed point
+    ones, ch1 = os_.copy(), o_ch.copy()
+    ones["color"], ch1["color0"], ch1["color1"] = 1.0, 1.0, 1.0
+    cp = abi.params_default()
+    cp.width, cp.height = pk.params.width, pk.params.height
+    cp.clear_color[:] = (0.0, 0.0, 0.0, 0.0)
+    cp.alpha_blend = abi.lg_blend_component(abi.LG_BF_ONE, abi.LG_BF_ONE, abi.LG_BO_ADD)
+    cnt, _ = oracle.raster(ones, cp, chords=ch1)
+    n = (cnt[..., :1] >> 32).astype(np.float64) + 1.0
+    # FP32 atomics add the same non-negative f32 terms in no fixed order: within 2 n u |sum|
+    tol = 2.0 * n * 2.0 ** -24 * np.abs(f64) + 1e-30
+    assert (np.abs(acc - f64) <= tol).all(), (np.abs(acc - f64) / tol).max()
+
+
+def test_string_mod_lines_dropped_by_accumulate_segments(ctx, oracle):
+    pk = W.string_mod_art(abi.LG_CURVE_CIRCLE, 256, 256).packed()
+    ctx.upload(pk)
+    ctx.render()
+    assert len(ctx.chords()) == pk.params.string_mod.modulo
+    segs, _, _, _ = oracle.trace(pk)
+    ctx.accumulate_segments(segs)  # the caller's segments replace the trace: no lines drawn
+    assert len(ctx.chords()) == 0
+    o_acc, _ = oracle.raster(segs, pk.params)
+    assert np.array_equal(ctx.accum(), o_acc)
+
+
+def test_string_mod_rejects_bad_parameters(ctx):
+    pk = W.string_mod_art(abi.LG_CURVE_CIRCLE, 256, 256).packed()
+    for field, value in (("curve", 4), ("mode", 4)):
+        bad = W.string_mod_art(abi.LG_CURVE_CIRCLE, 256, 256).packed()
+        setattr(bad.params.string_mod, field, value)
+        with pytest.raises(abi.LgError) as e:
+            ctx.upload(bad)
+        assert e.value.status == abi.LG_ERR_INVALID_ARGUMENT
+    abi.set_mod_colors(pk.params, [(0, 0, (1.0, 1.0, 1.0, 1.0))])  # ix % 0
+    with pytest.raises(abi.LgError) as e:
+        ctx.upload(pk)
+    assert e.value.status == abi.LG_ERR_INVALID_ARGUMENT

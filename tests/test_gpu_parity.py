@@ -192,7 +192,8 @@ def test_overlays_match_oracle(ctx, oracle):
     ctx.trace()
     gs, gp = ctx.segments(paths=True)
     os_, op, o64, _ = oracle.trace(pk)
-    for src, n in ((abi.LG_SRC_CONTROL_LINE, 3), (abi.LG_SRC_STRING_MOD, 4096)):
+    assert ctx.chords().tobytes() == oracle.string_mod_chords(pk.params).tobytes()
+    for src, n in ((abi.LG_SRC_CONTROL_LINE, 3),):
         g = gs[gp["source"] == src]
         o = os_[op["source"] == src]
         gk = gp[gp["source"] == src]

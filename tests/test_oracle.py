@@ -497,3 +497,82 @@ def test_convex_polygon(oracle):
     h, _ = hits(oracle, hept, (0.5, -3), (0, 1))
     assert len(h) == 3 and h[1][0] == pytest.approx(h[2][0], abs=1e-12)
     assert S.convex_hull([(0, 0), (1, 0), (0.5, 0.2), (1, 1), (0, 1), (0.5, 0.5)]) == ((0.0, 0.0), (1.0, 0.0), (1.0, 1.0), (0.0, 1.0))
+
+
+# ---- string mod (string_mod.rs:33-150) ------------------------------------------------------
+def sm_params(m, num, mode, curve=abi.LG_CURVE_CIRCLE, turns=1, colors=(), cf=(0.0, 0.0), cu=(0, 0, 0)):
+    p = abi.params_default()
+    sm = p.string_mod
+    sm.modulo, sm.num, sm.mode, sm.curve, sm.turns = m, num, mode, curve, turns
+    sm.color[:] = (0.3, 0.3, 0.3, 1.0)
+    sm.curve_f[:] = cf
+    sm.curve_u[:] = cu
+    abi.set_mod_colors(p, colors)
+    return p
+
+
+def test_string_mod_modes_on_the_circle(oracle):
+    m = 12
+    ang = lambda n: 2 * math.pi * n / m
+    for mode, target in ((abi.LG_SM_ADD, lambda i: (i + 5) % m), (abi.LG_SM_MUL, lambda i: (i * 5) % m),
+                         (abi.LG_SM_POW, lambda i: pow(i, 5, m)), (abi.LG_SM_BASE, lambda i: pow(5, i, m))):
+        ch = oracle.string_mod_chords(sm_params(m, 5, mode))
+        assert len(ch) == m
+        for i in range(m):
+            j = target(i)
+            assert ch[i]["x0"] == pytest.approx(math.cos(ang(i)), abs=1e-7)
+            assert ch[i]["y0"] == pytest.approx(math.sin(ang(i)), abs=1e-7)
+            assert ch[i]["x1"] == pytest.approx(math.cos(ang(j)), abs=1e-7)
+            assert ch[i]["y1"] == pytest.approx(math.sin(ang(j)), abs=1e-7)
+
+
+def test_string_mod_modulo_colours_are_averaged(oracle):
+    red, blue = (1.0, 0.0, 0.0, 1.0), (0.0, 0.0, 1.0, 0.5)
+    ch = oracle.string_mod_chords(sm_params(12, 1, abi.LG_SM_ADD, colors=[(2, 0, red), (3, 0, blue)]))
+    assert ch[1]["color0"].tolist() == pytest.approx([0.3, 0.3, 0.3, 1.0])  # no entry matches 1
+    assert ch[2]["color0"].tolist() == list(red)
+    assert ch[3]["color0"].tolist() == list(blue)
+    assert ch[6]["color0"].tolist() == [0.5, 0.0, 0.5, 0.75]  # both match: the mean
+    # the second vertex takes the colour of its own point (i + 1)
+    assert ch[5]["color1"].tolist() == [0.5, 0.0, 0.5, 0.75] and ch[1]["color1"].tolist() == list(red)
+    with pytest.raises(oracle.OracleError):  # ix % 0 is undefined in the reference
+        oracle.string_mod_chords(sm_params(12, 1, abi.LG_SM_ADD, colors=[(0, 0, red)]))
+
+
+def test_string_mod_curves(oracle):
+    m = 64
+    th = 2 * math.pi / 40
+    ch = oracle.string_mod_chords(sm_params(m, 3, abi.LG_SM_MUL, abi.LG_CURVE_COMPLEX_EXP,
+                                            cf=(math.cos(th), math.sin(th))))
+    for i in (0, 1, 7, 63):  # c^n on the unit circle = (cos n th, sin n th)
+        assert ch[i]["x0"] == pytest.approx(math.cos(i * th), abs=1e-6)
+        assert ch[i]["y0"] == pytest.approx(math.sin(i * th), abs=1e-6)
+    r, s, d = 3, 5, 2
+    ch = oracle.string_mod_chords(sm_params(m, 3, abi.LG_SM_MUL, abi.LG_CURVE_HYPOTROCHOID, turns=2, cu=(r, s, d)))
+    for i in (0, 5, 33):
+        a = 2 * i * 2 * math.pi / m
+        k = s - r
+        assert ch[i]["x0"] == pytest.approx((k * math.cos(a) + d * math.cos(a * k / r)) / (k + d), abs=1e-6)
+        assert ch[i]["y0"] == pytest.approx((k * math.sin(a) - d * math.sin(a * k / r)) / (k + d), abs=1e-6)
+    ch = oracle.string_mod_chords(sm_params(m, 3, abi.LG_SM_MUL, abi.LG_CURVE_LISSAJOUS, cf=(0.5, 0.0), cu=(3, 4, 0)))
+    for i in (0, 9, 40):
+        a = i * 2 * math.pi / m
+        assert ch[i]["x0"] == pytest.approx(math.sin(3 * a + 0.5), abs=1e-6)
+        assert ch[i]["y0"] == pytest.approx(math.sin(4 * a), abs=1e-6)
+
+
+def test_chord_colour_is_interpolated_along_the_major_axis(oracle):
+    p = raster_params()
+    ch = np.zeros(2, abi.chord_dtype())
+    ch[0]["x0"], ch[0]["y0"], ch[0]["x1"], ch[0]["y1"] = -1, 0.125, 1, 0.125  # row 3, left to right
+    ch[0]["color0"], ch[0]["color1"] = (0, 0, 0, 1), (1, 1, 1, 1)
+    ch[1]["x0"], ch[1]["y0"], ch[1]["x1"], ch[1]["y1"] = 0.125, -1, 0.125, 1  # column 4, bottom to top
+    ch[1]["color0"], ch[1]["color1"] = (1, 0, 0, 1), (0, 0, 1, 1)
+    acc, px = oracle.raster(np.zeros(0, abi.segment_dtype()), p, chords=ch[:1])
+    assert px == 8
+    # sample i sits at i + 1/2 of the 8-pixel span: f = (i + 1/2) / 8
+    assert [int(acc[3, i, 0]) for i in range(8)] == [int((i + 0.5) / 8 * 2 ** 32) for i in range(8)]
+    acc, px = oracle.raster(np.zeros(0, abi.segment_dtype()), p, chords=ch[1:])
+    # y grows downwards in pixel space: row 7 is the first vertex (y = -1), row 0 the second
+    assert [int(acc[j, 4, 2]) for j in range(8)] == [int((7 - j + 0.5) / 8 * 2 ** 32) for j in range(8)]
+    assert [int(acc[j, 4, 0]) for j in range(8)] == [int((j + 0.5) / 8 * 2 ** 32) for j in range(8)]
