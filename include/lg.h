@@ -42,7 +42,10 @@ extern "C" {
 /* 2: lg_device_opts gained culling and grid_density, lg_trace_stats bound_tests and
  * object_tests (both structs grew).
  * 3: lg_device_opts gained wait_polls; lg_params.precision (was padding), ray_stride and
- *    ray_offset (lg_params grew); lg_trace_stats scan_ms, solve_ms, bounce_ms (grew). */
+ *    ray_offset (lg_params grew); lg_trace_stats scan_ms, solve_ms, bounce_ms (grew).
+ * 4: lg_string_mod gained the curve parameters and the modulo-colour table (lg_params
+ *    grew); string-mod lines are lg_chord records (lg_chords_download), no longer
+ *    segments. */
 #define LG_ABI_VERSION 4
 
 typedef enum lg_status {
@@ -264,7 +267,7 @@ typedef struct lg_path_record {
 typedef struct lg_trace_stats {
   uint64_t primary_rays;   /* rays generated by all lights */
   uint64_t ray_visits;     /* queue entries traced (after the cutoff) */
-  uint64_t segments;       /* segments written (traced + overlays) */
+  uint64_t segments;       /* segments written (traced + control lines) */
   uint64_t fp64_solves;    /* object intersections re-solved in FP64 */
   uint64_t fp64_fallbacks; /* rays whose FP32 candidate list overflowed */
   uint64_t near_degenerate;/* segments carrying LG_PATH_NEAR_DEGENERATE */

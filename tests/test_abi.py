@@ -168,3 +168,47 @@ def test_python_context_has_no_cpu_fallback(monkeypatch, tmp_path):
     from light_garden_gb300.runtime import Context
     with pytest.raises(RuntimeError, match="missing"):
         Context()
+
+
+# ---- the Rust binding (lg-sys, written for hosts with a Rust toolchain; none is here) -------
+RUST = abi.LIB_DIR.parent.parent / "lg-sys" / "src" / "lib.rs"
+_RUST_SIZES = {"i8": 1, "u8": 1, "i16": 2, "u16": 2, "i32": 4, "u32": 4, "f32": 4, "i64": 8, "u64": 8, "f64": 8,
+               "usize": 8}
+
+
+def _rust_structs():
+    text = re.sub(r"//[^\n]*", "", RUST.read_text())
+    out = {}
+    for name, body in re.findall(r"pub struct (\w+)\s*\{(.*?)\}", text, flags=re.S):
+        out[name] = re.findall(r"pub (\w+):\s*([^,]+),", body)
+    return out
+
+
+def _rust_size(ty, structs_by_name):
+    ty = ty.strip()
+    m = re.fullmatch(r"\[(.+);\s*(\d+)\]", ty)
+    if m:
+        return _rust_size(m.group(1), structs_by_name) * int(m.group(2))
+    if ty.startswith("*"):
+        return 8
+    if ty in _RUST_SIZES:
+        return _RUST_SIZES[ty]
+    return C.sizeof(structs_by_name[ty])
+
+
+def test_rust_binding_matches_the_header():
+    """lg-sys declares every struct with the fields, order and sizes of the ctypes mirror
+    (itself checked against the C compiler above), every function of the header, and the
+    same ABI version."""
+    rs = _rust_structs()
+    by_name = {s.__name__: s for s in STRUCTS}
+    for s in STRUCTS:
+        assert s.__name__ in rs, s.__name__
+        fields = rs[s.__name__]
+        assert [f for f, _ in fields] == [f for f, *_ in s._fields_], s.__name__
+        for (f, ty), (_, cty, *_) in zip(fields, s._fields_):
+            assert _rust_size(ty, by_name) == C.sizeof(cty), (s.__name__, f, ty)
+    text = RUST.read_text()
+    fns = set(re.findall(r"pub fn (lg_\w+)\(", text))
+    assert fns == set(declared_functions())
+    assert f"pub const LG_ABI_VERSION: u32 = {abi.LG_ABI_VERSION};" in text
