@@ -62,8 +62,8 @@ REF_STRIDE = {"csg": 2048, "mid": 32}
 #   bounce: FP64 thread instructions per ray visit
 #   raster: shared-memory atomic warp instructions per accumulated pixel
 INST_PER_UNIT = {
-    "csg": {"scan": 694.3, "solve": 189.2, "bounce": 124.7, "raster": 0.2807},
-    "mid": {"scan": 968.7, "solve": 91.6, "bounce": 64.8, "raster": 0.3003},
+    "csg": {"scan": 694.3, "solve": 104.7, "bounce": 70.7, "raster": 0.2804},
+    "mid": {"scan": 968.5, "solve": 92.7, "bounce": 55.0, "raster": 0.3003},
 }
 
 

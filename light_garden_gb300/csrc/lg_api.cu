@@ -358,7 +358,7 @@ lg_status flatten_scene(std::string& err, const lg_geo* G, uint32_t n_geo, const
     // one leaf of a scanned kind (a cubic takes both inline slots), or two circle / rect /
     // segment leaves; anything else (ellipses, polygons, deeper CSG) is bounded only
     bool no_cubic = true;
-    for (uint32_t i = leaf0; i < F.leaves.size(); ++i) no_cubic = no_cubic && F.leaves[i].kind < LEAF_CUBIC;
+    for (uint32_t i = leaf0; i < leaf0 + nl && i < F.leaves.size(); ++i) no_cubic = no_cubic && F.leaves[i].kind < LEAF_CUBIC;
     uint32_t info = SCAN_BOUND;
     float scratch[6];
     if (nl == 1 && F.leaves[leaf0].kind <= LEAF_CUBIC) {

@@ -13,6 +13,14 @@
 #include "lg_kernels.cuh"
 #include "lg_trace_common.cuh"
 
+// CTAs per SM the exact kernels' registers are sized for (build-time, for sweeps)
+#ifndef LG_SOLVE_X_BLOCKS
+#define LG_SOLVE_X_BLOCKS 2
+#endif
+#ifndef LG_BOUNCE_X_BLOCKS
+#define LG_BOUNCE_X_BLOCKS 2
+#endif
+
 namespace lgd {
 
 using lgx::V;
@@ -25,6 +33,34 @@ __device__ __forceinline__ bool obj_contains_x(const SceneDev& S, uint32_t k, V 
   const ObjInfo& oi = S.info[k];
   if (oi.flags & INFO_NO_CONTAINS) return false;
   return lgx::object_contains_tree(S.xgeo, S.xnode + oi.xnode_begin, (int)oi.xnode_count, p, fl);
+}
+
+// Membership of object k at p decided in FP32 where the FP32 copy of its leaves decides it:
+// 1 inside, 0 outside, -1 undecided.  The band of leaf_member32 covers the rounding of p and
+// of the leaf parameters to FP32 (1e-6 of the coordinates against 6e-8), so a decided answer
+// is the one the FP64 tree gives; objects the scan only bounds stay undecided.
+__device__ __forceinline__ int obj_member32(const ObjScan& s, float px, float py) {
+  if (s.info & INFO_NO_CONTAINS) return 0;
+  const uint32_t sk = info_scan(s.info);
+  if (sk == SCAN_ONE) {
+    const uint32_t ka = info_leaf_a(s.info);
+    return ka == LEAF_CUBIC ? -1 : leaf_member32(ka, s.a, px, py, 1e-6f);
+  }
+  if (sk != SCAN_TWO) return -1;
+  const int a = leaf_member32(info_leaf_a(s.info), s.a, px, py, 1e-6f);
+  const int b = leaf_member32(info_leaf_b(s.info), s.b, px, py, 1e-6f);
+  switch (info_op(s.info)) {
+    case LG_OP_AND: return (a == 0 || b == 0) ? 0 : (a == 1 && b == 1 ? 1 : -1);
+    case LG_OP_OR: return (a == 1 || b == 1) ? 1 : (a == 0 && b == 0 ? 0 : -1);
+    default: return (a == 0 || b == 1) ? 0 : (a == 1 && b == 0 ? 1 : -1);  // a and not b
+  }
+}
+
+// obj_contains_x behind the FP32 pre-test (k scene-global).
+__device__ __forceinline__ bool obj_contains_f(const SceneDev& S, uint32_t k, V p, uint32_t* fl) {
+  const int m = obj_member32(S.scan[k], (float)p.x, (float)p.y);
+  if (m >= 0) return m == 1;
+  return obj_contains_x(S, k, p, fl);
 }
 
 // Light start media (tracer.rs:280-287: the last object with a material containing the
@@ -77,6 +113,36 @@ static __device__ __noinline__ double obj_best_x(const SceneDev& S, uint32_t k, 
   return ob;
 }
 
+// A two-leaf CSG object whose nearest root the FP32 scan proved (a single candidate, a
+// certain root, certain membership of its point in the other leaf): only that leaf's FP64
+// hits are computed, the one nearest the FP32 root is taken, and its point is lifted out of
+// the Logic frame with the operations object_hits uses.  The other leaf and the membership
+// tests cannot change which hit object_hits would keep, so the result is the same bits.
+static __device__ __noinline__ bool solve_proved_x(const SceneDev& S, const ObjInfo& oi, V o, V d, int side,
+                                                   float t32, double& ev, lgx::Hit& out) {
+  const lgx::XNode* nd = S.xnode + oi.xnode_begin;
+  const lg_geo& L = S.xgeo[nd[0].geo];
+  if (oi.xnode_count != 3 || L.kind != LG_GEO_LOGIC) return false;
+  const V org = lgx::mk(L.origin[0], L.origin[1]);
+  const V lo = lgx::irot(lgx::vsub(o, org), L.rot[0], L.rot[1]);
+  const V ld = lgx::irot(d, L.rot[0], L.rot[1]);
+  const int li = 1 + side;
+  double near = INFINITY;
+  bool found = false;
+  lgx::leaf_hits(S.xgeo, S.xgeo[nd[li].geo], lo, ld, ev, [&](const lgx::Hit& h) {
+    const double e = fabs(h.t - (double)t32);  // selection only
+    if (e < near) {
+      near = e;
+      out = h;
+      found = true;
+    }
+  });
+  if (!found) return false;
+  out.node = li;
+  out.p = lgx::vadd(org, lgx::rot(out.p, L.rot[0], L.rot[1]));
+  return true;
+}
+
 // Every ray with candidates (the refine lists and the full-solve list of k_scan): the
 // nearest hit over its candidates, each object solved whole as tracer.rs:412-424 does
 // (the minimum distance_squared over the object's hits, then over objects with ties kept by
@@ -85,7 +151,7 @@ static __device__ __noinline__ double obj_best_x(const SceneDev& S, uint32_t k, 
 // two-leaf CSG) at a time, with a barrier between classes, so that one geometry code path
 // is in flight per CTA.
 template <bool MULTI>
-__global__ void __launch_bounds__(256) k_solve_x(SceneDev S, TraceBufs B, uint32_t gen) {
+__global__ void __launch_bounds__(256, LG_SOLVE_X_BLOCKS) k_solve_x(SceneDev S, TraceBufs B, uint32_t gen) {
   __shared__ unsigned long long blk_solves;
   if (threadIdx.x == 0) blk_solves = 0;
   __syncthreads();
@@ -129,8 +195,19 @@ __global__ void __launch_bounds__(256) k_solve_x(SceneDev S, TraceBufs B, uint32
         second = ob;
       }
     };
+    // proved two-leaf CSG roots first, in a phase of their own
+    bool proved = false;
+    if (valid && i < off[LIST_FULL] && !sc.overflow && sc.nc == 1 && (sc.leaf == 0 || sc.leaf == 1) &&
+        solve_class(__ldg(&S.scan[sl.base + sc.cand[0]].info)) == 4u) {
+      proved = solve_proved_x(S, S.info[sl.base + sc.cand[0]], o, d, sc.leaf, sc.t32, ev, bh);
+      if (proved) {
+        best = sc.cand[0];
+        ++my_solves;
+      }
+    }
+    __syncthreads();
     {
-      uint32_t pending = valid && !sc.overflow ? (1u << sc.nc) - 1u : 0u;
+      uint32_t pending = valid && !sc.overflow && !proved ? (1u << sc.nc) - 1u : 0u;
       uint32_t cls[CAND];
       for (int k = 0; k < CAND; ++k)
         cls[k] = (pending >> k) & 1u ? solve_class(__ldg(&S.scan[sl.base + sc.cand[k]].info)) : 7u;
@@ -290,7 +367,7 @@ __device__ __forceinline__ void bounce_x(const SceneDev& S, const RayRec& r, con
       double n2 = 1.0;
       uint16_t m2 = MEDIUM_AIR;
       const V mid = vscl(vadd(o, bp), 0.5);
-      if (obj_contains_x(S, sl.base + (uint32_t)best, mid, &fl)) {
+      if (obj_contains_f(S, sl.base + (uint32_t)best, mid, &fl)) {
         // the first other object (in table order) that contains the hit point and has a material
         const float px32 = (float)bp.x, py32 = (float)bp.y;
         auto far_side = [&](uint32_t k) -> bool {
@@ -300,7 +377,7 @@ __device__ __forceinline__ void bounce_x(const SceneDev& S, const RayRec& r, con
           const float ex = px32 - h.x, ey = py32 - h.y;
           const float tol = 2e-6f * (fabsf(px32) + fabsf(py32) + fabsf(h.x) + fabsf(h.y) + h.z) + 1e-6f;
           if (ex * ex + ey * ey > (h.z + tol) * (h.z + tol)) return false;  // far outside: no member, no band
-          if (!obj_contains_x(S, sl.base + k, bp, &fl)) return false;
+          if (!obj_contains_f(S, sl.base + k, bp, &fl)) return false;
           if (!(__float_as_uint(h.w) & INFO_MATERIAL)) return false;
           n2 = S.info[sl.base + k].n64;
           m2 = (uint16_t)k;
@@ -442,7 +519,7 @@ __device__ __forceinline__ void emit_segments_x(const SceneDev& S, const TraceBu
 }
 
 template <bool MULTI, bool CULL>
-__global__ void __launch_bounds__(256, 2) k_bounce_x(SceneDev S, TraceBufs B, uint32_t gen) {
+__global__ void __launch_bounds__(256, LG_BOUNCE_X_BLOCKS) k_bounce_x(SceneDev S, TraceBufs B, uint32_t gen) {
   __shared__ unsigned long long blk_visits, blk_near;
   if (threadIdx.x == 0) { blk_visits = 0; blk_near = 0; }
   __syncthreads();

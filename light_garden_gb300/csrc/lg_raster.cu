@@ -84,9 +84,6 @@ __device__ __forceinline__ CanvasLoc canvas_at(const RasterArgs& A, uint32_t s) 
   C.W = K.W; C.H = K.H; C.ntx = K.ntx; C.bin_base = K.bin_base; C.px_base = K.px_base;
   return C;
 }
-__device__ __forceinline__ CanvasLoc canvas_of_segment(const RasterArgs& A, uint64_t i) {
-  return A.seg_scene ? canvas_at(A, A.seg_scene[i]) : canvas_one(A);
-}
 __device__ __forceinline__ CanvasLoc canvas_of_bin(const RasterArgs& A, uint64_t bin) {
   if (!A.seg_scene) return canvas_one(A);
   uint32_t lo = 0, hi = A.n_scenes;  // the last scene whose first bin is <= bin
@@ -98,27 +95,31 @@ __device__ __forceinline__ CanvasLoc canvas_of_bin(const RasterArgs& A, uint64_t
 }
 
 // ------------------------------------------------------------------ binning
-// Visits every tile that holds at least one pixel of the segment: per tile column
-// (x-major) the minor range is bounded by the samples at both ends, since v(i) is
-// monotone in i.
+// The tiles that tile column tm (major-axis tiles) of a segment touches: the minor range is
+// bounded by the samples at the column's two ends, since v(i) is monotone in i, and with
+// |slope| <= 1 it spans at most two tiles.
+template <class F>
+__device__ __forceinline__ void column_tiles(const RSetup& R, const CanvasLoc& A, int tm, F&& f) {
+  const int nmin = (int)(R.xmajor ? A.H : A.W);
+  const int a = max(R.lo, tm * TILE), b = min(R.hi, tm * TILE + TILE) - 1;
+  const int ja = raster_minor(R, a), jb = raster_minor(R, b);
+  int jlo = min(ja, jb), jhi = max(ja, jb);
+  if (jhi < 0 || jlo >= nmin) return;
+  jlo = max(jlo, 0);
+  jhi = min(jhi, nmin - 1);
+  for (int tn = jlo / TILE; tn <= jhi / TILE; ++tn) {
+    // bin id = 2 * tile + orientation: x-major and y-major segments of a tile are
+    // rasterised in separate units, each with a bank-conflict-free layout
+    const uint32_t tile = R.xmajor ? (uint32_t)tn * A.ntx + (uint32_t)tm : (uint32_t)tm * A.ntx + (uint32_t)tn;
+    f((uint32_t)(A.bin_base + 2u * tile + (R.xmajor ? 0u : 1u)));
+  }
+}
+
+// Visits every tile that holds at least one pixel of the segment.
 template <class F>
 __device__ __forceinline__ void for_each_tile(const RSetup& R, const CanvasLoc& A, F&& f) {
-  const int nmin = (int)(R.xmajor ? A.H : A.W);
   const int tlo = R.lo / TILE, thi = (R.hi - 1) / TILE;
-  for (int tm = tlo; tm <= thi; ++tm) {
-    const int a = max(R.lo, tm * TILE), b = min(R.hi, tm * TILE + TILE) - 1;
-    const int ja = raster_minor(R, a), jb = raster_minor(R, b);
-    int jlo = min(ja, jb), jhi = max(ja, jb);
-    if (jhi < 0 || jlo >= nmin) continue;
-    jlo = max(jlo, 0);
-    jhi = min(jhi, nmin - 1);
-    for (int tn = jlo / TILE; tn <= jhi / TILE; ++tn) {
-      // bin id = 2 * tile + orientation: x-major and y-major segments of a tile are
-      // rasterised in separate units, each with a bank-conflict-free layout
-      const uint32_t tile = R.xmajor ? (uint32_t)tn * A.ntx + (uint32_t)tm : (uint32_t)tm * A.ntx + (uint32_t)tn;
-      f((uint32_t)(A.bin_base + 2u * tile + (R.xmajor ? 0u : 1u)));
-    }
-  }
+  for (int tm = tlo; tm <= thi; ++tm) column_tiles(R, A, tm, f);
 }
 
 __device__ __forceinline__ uint64_t n_segments(const RasterArgs& A) {
@@ -126,33 +127,62 @@ __device__ __forceinline__ uint64_t n_segments(const RasterArgs& A) {
   return n < A.seg_cap ? n : A.seg_cap;
 }
 
-// Calls f(i, R, C) for every rasterisable segment i of this thread's grid-stride share.
-// The binning passes need only a segment's endpoints; the next segment's endpoints (and
-// scene) are loaded while the current one's tiles are visited, so that a thread always
-// has a load in flight.
+// Every (segment, bin) pair of the calling warp's share of the segments (32 consecutive
+// segments per warp step, warp-strided over the grid), with the lanes spread densely over
+// the step's tile columns: the 32 segments are set up lane-parallel, their column counts
+// prefix-summed, and lane L takes columns L, L + 32, ... of the step, finding each column's
+// segment by a binary search over the prefix sums with shuffles.  A segment that crosses
+// many tiles is shared by the warp instead of keeping 31 lanes waiting.  f(segment, bin).
+// Every lane of the warp calls it (the loops are warp-uniform).
 template <class F>
-__device__ __forceinline__ void for_each_segment(const RasterArgs& A, uint64_t n, F&& f) {
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-  float4 nxt = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  uint32_t nsc = 0;
-  if (i < n) {
-    nxt = __ldg(reinterpret_cast<const float4*>(A.segs + i));
-    if (A.seg_scene) nsc = A.seg_scene[i];
-  }
-  for (; i < n; i += stride) {
-    const float4 g = nxt;
-    const uint32_t sc = nsc;
-    if (i + stride < n) {
-      nxt = __ldg(reinterpret_cast<const float4*>(A.segs + i + stride));
-      if (A.seg_scene) nsc = A.seg_scene[i + stride];
-    }
-    lg_segment sg;
-    sg.x0 = g.x; sg.y0 = g.y; sg.x1 = g.z; sg.y1 = g.w;
-    const CanvasLoc C = A.seg_scene ? canvas_at(A, sc) : canvas_one(A);
+__device__ __forceinline__ void for_each_pair_dense(const RasterArgs& A, uint64_t n, F&& f) {
+  const unsigned lane = lane_id();
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t base = ((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5) * 32; base < n; base += nw * 32) {
+    const uint64_t i = base + lane;
     RSetup R;
-    if (!raster_setup(sg, C.W, C.H, R)) continue;
-    f(i, R, C);
+    R.xmajor = 0; R.ua = 0.0f; R.va = 0.0f; R.slope = 0.0f; R.lo = 0; R.hi = 0;
+    uint32_t sc = 0;
+    int cnt = 0;
+    if (i < n) {
+      const float4 g = __ldg(reinterpret_cast<const float4*>(A.segs + i));
+      if (A.seg_scene) sc = A.seg_scene[i];
+      const CanvasLoc C = A.seg_scene ? canvas_at(A, sc) : canvas_one(A);
+      lg_segment sg;
+      sg.x0 = g.x; sg.y0 = g.y; sg.x1 = g.z; sg.y1 = g.w;
+      if (raster_setup(sg, C.W, C.H, R)) cnt = (R.hi - 1) / TILE - R.lo / TILE + 1;
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if ((int)lane >= o) incl += y;
+    }
+    const int excl = incl - cnt;
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    for (int p0 = 0; p0 < total; p0 += 32) {
+      const int p = p0 + (int)lane;
+      // owner: the last lane whose exclusive prefix is <= p (a lane without columns shares
+      // its prefix with the next lane and loses the search to it)
+      int k = 0;
+#pragma unroll
+      for (int st = 16; st > 0; st >>= 1)
+        if (__shfl_sync(0xffffffffu, excl, k + st) <= p) k += st;
+      RSetup Q;
+      Q.xmajor = __shfl_sync(0xffffffffu, R.xmajor, k);
+      Q.ua = __shfl_sync(0xffffffffu, R.ua, k);
+      Q.va = __shfl_sync(0xffffffffu, R.va, k);
+      Q.slope = __shfl_sync(0xffffffffu, R.slope, k);
+      Q.lo = __shfl_sync(0xffffffffu, R.lo, k);
+      Q.hi = __shfl_sync(0xffffffffu, R.hi, k);
+      const uint32_t qsc = __shfl_sync(0xffffffffu, sc, k);
+      const int qexcl = __shfl_sync(0xffffffffu, excl, k);
+      if (p < total) {
+        const CanvasLoc C = A.seg_scene ? canvas_at(A, qsc) : canvas_one(A);
+        const uint64_t seg = base + (uint64_t)k;
+        column_tiles(Q, C, Q.lo / TILE + (p - qexcl), [&](uint32_t bin) { f(seg, bin); });
+      }
+    }
   }
 }
 
@@ -167,17 +197,15 @@ __global__ void __launch_bounds__(SCATTER_THREADS) k_bin_count(RasterArgs A, int
     for (uint32_t t = threadIdx.x; t < A.n_tiles; t += blockDim.x) hist[t] = 0;
     __syncthreads();
   }
-  for_each_segment(A, n, [&](uint64_t, const RSetup& R, const CanvasLoc& C) {
-    for_each_tile(R, C, [&](uint32_t tile) {
-      if (smem_tiles) {
-        atomicAdd(&hist[tile], 1u);
-      } else {
-        const unsigned act = __activemask();
-        const unsigned grp = __match_any_sync(act, tile);
-        const int leader = __ffs(grp) - 1;
-        if ((int)lane_id() == leader) atomicAdd(&A.tile_count[tile], (unsigned)__popc(grp));
-      }
-    });
+  for_each_pair_dense(A, n, [&](uint64_t, uint32_t tile) {
+    if (smem_tiles) {
+      atomicAdd(&hist[tile], 1u);
+    } else {
+      const unsigned act = __activemask();
+      const unsigned grp = __match_any_sync(act, tile);
+      const int leader = __ffs(grp) - 1;
+      if ((int)lane_id() == leader) atomicAdd(&A.tile_count[tile], (unsigned)__popc(grp));
+    }
   });
   if (smem_tiles) {
     __syncthreads();
@@ -400,9 +428,7 @@ __global__ void __launch_bounds__(SCATTER_THREADS) k_bin_scatter(RasterArgs A, i
     } else {
       for (uint32_t t = threadIdx.x; t < A.n_tiles; t += blockDim.x) cur[t] = 0;
       __syncthreads();
-      for_each_segment(A, n, [&](uint64_t, const RSetup& R, const CanvasLoc& C) {
-        for_each_tile(R, C, [&](uint32_t tile) { atomicAdd(&cur[tile], 1u); });
-      });
+      for_each_pair_dense(A, n, [&](uint64_t, uint32_t tile) { atomicAdd(&cur[tile], 1u); });
     }
     __syncthreads();
     for (uint32_t t = threadIdx.x; t < A.n_tiles; t += blockDim.x) {
@@ -410,29 +436,22 @@ __global__ void __launch_bounds__(SCATTER_THREADS) k_bin_scatter(RasterArgs A, i
       cur[t] = c ? (unsigned)atomicAdd(&A.tile_cursor[t], (unsigned long long)c) : 0u;
     }
     __syncthreads();
-    for_each_segment(A, n, [&](uint64_t i, const RSetup& R, const CanvasLoc& C) {
-      for_each_tile(R, C, [&](uint32_t tile) {
-        const unsigned slot = atomicAdd(&cur[tile], 1u);
-        if (slot < A.refs_cap) A.refs[slot] = (uint32_t)i;
-      });
+    for_each_pair_dense(A, n, [&](uint64_t i, uint32_t tile) {
+      const unsigned slot = atomicAdd(&cur[tile], 1u);
+      if (slot < A.refs_cap) A.refs[slot] = (uint32_t)i;
     });
     return;
   }
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    RSetup R;
-    const CanvasLoc C = canvas_of_segment(A, i);
-    if (!raster_setup(A.segs[i], C.W, C.H, R)) continue;
-    for_each_tile(R, C, [&](uint32_t tile) {
-      const unsigned act = __activemask();
-      const unsigned grp = __match_any_sync(act, tile);
-      const int leader = __ffs(grp) - 1;
-      unsigned long long base = 0;
-      if ((int)lane_id() == leader) base = atomicAdd(&A.tile_cursor[tile], (unsigned long long)__popc(grp));
-      base = __shfl_sync(grp, base, leader);
-      const unsigned long long slot = base + __popc(grp & lanemask_lt());
-      if (slot < A.refs_cap) A.refs[slot] = (uint32_t)i;
-    });
-  }
+  for_each_pair_dense(A, n, [&](uint64_t i, uint32_t tile) {
+    const unsigned act = __activemask();
+    const unsigned grp = __match_any_sync(act, tile);
+    const int leader = __ffs(grp) - 1;
+    unsigned long long base = 0;
+    if ((int)lane_id() == leader) base = atomicAdd(&A.tile_cursor[tile], (unsigned long long)__popc(grp));
+    base = __shfl_sync(grp, base, leader);
+    const unsigned long long slot = base + __popc(grp & lanemask_lt());
+    if (slot < A.refs_cap) A.refs[slot] = (uint32_t)i;
+  });
 }
 
 // ------------------------------------------------------------------ tile raster

@@ -215,10 +215,17 @@ __device__ __forceinline__ void emit_segments(const SceneDev& S, const TraceBufs
 // applies the first-in-object-order tie rule of tracer.rs:404,417 itself.  The runs are
 // either the object table in chunks of SCAN_CHUNK, or (culling grid) the objects listed
 // in the grid cells the lane's ray crosses, nearest cell first.
+// Launch shape (build-time, for sweeps: -DLG_SCAN_CHUNK=..., -DLG_SCAN_CULL_BLOCKS=...).
+#ifndef LG_SCAN_CHUNK
+#define LG_SCAN_CHUNK 16
+#endif
+#ifndef LG_SCAN_CULL_BLOCKS
+#define LG_SCAN_CULL_BLOCKS 3
+#endif
 constexpr int SCAN_WARPS = 4;
-constexpr int SCAN_CHUNK = 16;
+constexpr int SCAN_CHUNK = LG_SCAN_CHUNK;  // pair slots per lane between classifications
 constexpr int WALK_STEPS = 32;  // culled scan: cell steps and object tests between classifications
-constexpr int SCAN_CULL_BLOCKS = 3;  // culled scan: CTAs per SM the registers are sized for (no spills at 3)
+constexpr int SCAN_CULL_BLOCKS = LG_SCAN_CULL_BLOCKS;  // culled scan: CTAs per SM the registers are sized for
 
 struct __align__(16) PairSlot {
   float key, ub, s;
