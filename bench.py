@@ -392,11 +392,32 @@ def batch_bench(local, args, ray_scale=1.0 / 16):
         plain.upload(pk)
         plain.render_into(big.data_ptr(), pk.params.width * 8, True)
     plain_s = time.perf_counter() - t0
+    # the ceiling of batching: every 8th scene rendered alone at its reduced ray count and at
+    # full rays; batching can at best run a scene at the per-ray efficiency the same scene
+    # reaches with 1/ray_scale times the rays, where it fills far more of the GPU
+    full = [w.packed() for w in W.batch_scenes(count=512)[::8]]
+    t_small = t_full = 0.0
+    for pk_s, pk_f in zip(scenes[::8], full):
+        pk_f.params.precision = PRECISION[args.precision]
+        for pk, acc in ((pk_s, "s"), (pk_f, "f")):  # same canvases: `big` holds either
+            plain.upload(pk)
+            plain.render_into(big.data_ptr(), pk.params.width * 8, True)  # warm (graph capture)
+            torch.cuda.synchronize()
+            a = time.perf_counter()
+            plain.render_into(big.data_ptr(), pk.params.width * 8, True)
+            dt = time.perf_counter() - a
+            if acc == "s":
+                t_small += dt
+            else:
+                t_full += dt * ray_scale
     plain.close()
     b = n / (min(ms) * 1e-3)
+    ceiling = t_small / t_full if t_full > 0 else None
     return {"workload": BATCH_WORKLOAD + f", rays x {ray_scale:g}", "scenes": n, "batched_scenes_per_s": b,
             "batch_ms": min(ms), "plain_scenes_per_s": n / plain_s, "batched_vs_plain": b / (n / plain_s),
-            "note": "batched: device time of the batch graph; plain: host wall time of upload + lg_render per scene"}
+            "ceiling_vs_plain": ceiling,
+            "note": "batched: device time of the batch graph; plain: host wall time of upload + lg_render per scene; "
+                    "ceiling: 64 scenes (every 8th) alone, time at these rays over time at full rays x ray scale"}
 
 
 def serve_bench(local, args, rate=100.0, count=256, ray_scale=1.0 / 16):

@@ -217,7 +217,7 @@ __device__ __forceinline__ void emit_segments(const SceneDev& S, const TraceBufs
 // in the grid cells the lane's ray crosses, nearest cell first.
 // Launch shape (build-time, for sweeps: -DLG_SCAN_CHUNK=..., -DLG_SCAN_CULL_BLOCKS=...).
 #ifndef LG_SCAN_CHUNK
-#define LG_SCAN_CHUNK 16
+#define LG_SCAN_CHUNK 8
 #endif
 #ifndef LG_SCAN_CULL_BLOCKS
 #define LG_SCAN_CULL_BLOCKS 3
