@@ -853,7 +853,7 @@ lg_status enqueue_trace(lg_ctx* c) {
   if (c->n_lights) launch_light_setup(c, S, false, 1);
   const size_t tsm = c->smem_fits ? c->obj_smem : 0;
   for (uint32_t g = 0; g < c->prm.max_bounce; ++g)
-    launch_generation(c, S, B, g, false, c->trace_grid[0], (size_t)scan_smem_bytes() + tsm, tsm, c->smem_fits);
+    launch_generation(c, S, B, g, false, c->trace_grid[0], (size_t)scan_smem_bytes(c->culled) + tsm, tsm, c->smem_fits);
   launch_overlay(c, S, B);
   CK(cudaGetLastError(), "trace launch");
   return LG_OK;
@@ -1081,13 +1081,13 @@ lg_status lg_create(lg_ctx** out, const lg_device_opts* opts) {
   for (TraceKernel k : {k_scan<false, false, false>, k_scan<false, true, false>, k_scan<false, false, true>,
                         k_scan<false, true, true>})
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, scan_smem_bytes() + (int)OBJ_SMEM_MAX);
+      e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, scan_smem_bytes(false) + (int)OBJ_SMEM_MAX);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_full<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
   for (TraceKernel k : {k_bounce<false, false>, k_bounce<false, true>})
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
   for (TraceKernel k : {k_scan<true, false, false>, k_scan<true, true, false>, k_scan<true, false, true>,
                         k_scan<true, true, true>})
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, scan_smem_bytes());
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, scan_smem_bytes(false));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_bin_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(MAX_SMEM_TILES * 4));
   if (e == cudaSuccess)
@@ -1215,7 +1215,7 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
   int occ = 0;
   const size_t tsm = c->smem_fits ? c->obj_smem : 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, scan_kernel(false, c->culled, p.precision == LG_PRECISION_EXACT),
-                                                   SCAN_THREADS, (size_t)scan_smem_bytes() + tsm), "occupancy");
+                                                   SCAN_THREADS, (size_t)scan_smem_bytes(c->culled) + tsm), "occupancy");
   c->trace_grid[0] = c->n_sm * std::max(1, occ);
   if ((st = trace_grids(c, false, tsm))) return st;
   const int mode = raster_mode(p);
@@ -1361,7 +1361,7 @@ static lg_status enqueue_stream_frame(lg_ctx* c, uint16_t* dst, size_t row, cuda
   const size_t rsm = (size_t)raster_smem_bytes(mode);
   const uint32_t G = c->prm.max_bounce;
   for (uint32_t g = 0; g < G; ++g) {
-    launch_generation(c, S, B, g, false, c->trace_grid[0], (size_t)scan_smem_bytes() + tsm, tsm, c->smem_fits);
+    launch_generation(c, S, B, g, false, c->trace_grid[0], (size_t)scan_smem_bytes(c->culled) + tsm, tsm, c->smem_fits);
     if (g == 0) {
       launch_overlay(c, S, B);
       launch_chords(c, A);

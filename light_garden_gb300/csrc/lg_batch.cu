@@ -99,7 +99,7 @@ lg_status enqueue_batch(lg_ctx* c, cudaEvent_t* ev) {
       k_scene_scatter<<<c->n_sm * 8, 256, 0, c->stream>>>(S, B, g, (unsigned*)c->d_scene_off.p,
                                                           (uint32_t*)c->d_order.p);
     }
-    launch_generation(c, S, B, g, true, c->batch_grid_scan, (size_t)scan_smem_bytes(), 0, 0);
+    launch_generation(c, S, B, g, true, c->batch_grid_scan, (size_t)scan_smem_bytes(c->culled), 0, 0);
     if (g == 0 && c->n_cubic) {
       const int blocks = (int)std::min<uint64_t>((3ull * c->n_cubic + 255) / 256, 4096);
       k_overlay<<<blocks, 256, 0, c->stream>>>(S, B, (const uint32_t*)c->d_cubics.p,
@@ -348,7 +348,7 @@ lg_status lg_batch_upload(lg_ctx* c, const lg_scene_desc* scenes, uint32_t k) {
   // launch shapes: the multi-scene kernels read the object tables from global memory
   int occ = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, scan_kernel(true, c->culled, c->prm.precision == LG_PRECISION_EXACT),
-                                                   SCAN_THREADS, (size_t)scan_smem_bytes()), "occupancy");
+                                                   SCAN_THREADS, (size_t)scan_smem_bytes(c->culled)), "occupancy");
   c->batch_grid_scan = c->n_sm * std::max(1, occ);
   if ((st = trace_grids(c, true, 0))) return st;
   const int mode = raster_mode(c->prm);

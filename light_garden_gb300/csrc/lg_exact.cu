@@ -18,7 +18,7 @@
 #define LG_SOLVE_X_BLOCKS 2
 #endif
 #ifndef LG_BOUNCE_X_BLOCKS
-#define LG_BOUNCE_X_BLOCKS 2
+#define LG_BOUNCE_X_BLOCKS 3
 #endif
 
 namespace lgd {
@@ -113,23 +113,48 @@ static __device__ __noinline__ double obj_best_x(const SceneDev& S, uint32_t k, 
   return ob;
 }
 
-// A two-leaf CSG object whose nearest root the FP32 scan proved (a single candidate, a
-// certain root, certain membership of its point in the other leaf): only that leaf's FP64
-// hits are computed, the one nearest the FP32 root is taken, and its point is lifted out of
-// the Logic frame with the operations object_hits uses.  The other leaf and the membership
-// tests cannot change which hit object_hits would keep, so the result is the same bits.
-static __device__ __noinline__ bool solve_proved_x(const SceneDev& S, const ObjInfo& oi, V o, V d, int side,
-                                                   float t32, double& ev, lgx::Hit& out) {
-  const lgx::XNode* nd = S.xnode + oi.xnode_begin;
-  const lg_geo& L = S.xgeo[nd[0].geo];
-  if (oi.xnode_count != 3 || L.kind != LG_GEO_LOGIC) return false;
-  const V org = lgx::mk(L.origin[0], L.origin[1]);
-  const V lo = lgx::irot(lgx::vsub(o, org), L.rot[0], L.rot[1]);
-  const V ld = lgx::irot(d, L.rot[0], L.rot[1]);
-  const int li = 1 + side;
+// The FP64 hit of one leaf at the root the FP32 scan proved (t32; face32: the rect face as
+// 2 axis + (outward sign > 0)): the very operations of leaf_hits for that root only.  A
+// circle computes the quotient of its proved root (q / a or c / q, told apart by their FP32
+// values) and not the other; a rect computes the slab quotient of its proved face and not the
+// other three.  Other leaves take leaf_hits and the root nearest t32.  False: no such hit
+// (the caller solves the object whole).
+__device__ __forceinline__ bool leaf_proved_hit(const lg_geo* G, const lg_geo& g, V o, V d, float t32, int face32,
+                                                double& ev, lgx::Hit& out) {
+  using namespace lgx;
+  if (g.kind == LG_GEO_CIRCLE) {
+    const V oc = vsub(o, mk(g.origin[0], g.origin[1]));
+    const double r = g.v[0];
+    const double a = dot(d, d), b = dot(oc, d), cc = sub(dot(oc, oc), mul(r, r));
+    const double disc = sub(mul(b, b), mul(a, cc));
+    if (is_neg(disc)) return false;
+    const double sq = sqr(disc);
+    const double q = -add(b, b >= 0.0 ? sq : -sq);
+    if (is_zero(q)) return false;
+    const float ra = (float)q / (float)a, rc = (float)cc / (float)q;  // selection only
+    const double t = fabsf(ra - t32) <= fabsf(rc - t32) ? dvd(q, a) : dvd(cc, q);
+    if (!gt_pos(t, T_MIN)) return false;
+    const V p = vadd(o, vscl(d, t));
+    out = Hit{t, p, p, 0, 0};
+    return true;
+  }
+  if (g.kind == LG_GEO_RECT) {
+    if (face32 < 0) return false;
+    const int ax = face32 >> 1;
+    const bool pos = (face32 & 1) != 0;
+    const V lo = irot(vsub(o, mk(g.origin[0], g.origin[1])), g.rot[0], g.rot[1]);
+    const V ld = irot(d, g.rot[0], g.rot[1]);
+    const double h = mul(0.5, g.v[ax]);
+    const double O = ax ? lo.y : lo.x, D = ax ? ld.y : ld.x;
+    if (is_zero(D)) return false;
+    const double t = dvd(sub(pos ? h : -h, O), D);
+    if (!gt_pos(t, T_MIN)) return false;
+    out = mkhit(t, o, d, mk(0.0, 0.0), ax + (pos ? 2 : 0));
+    return true;
+  }
   double near = INFINITY;
   bool found = false;
-  lgx::leaf_hits(S.xgeo, S.xgeo[nd[li].geo], lo, ld, ev, [&](const lgx::Hit& h) {
+  leaf_hits(G, g, o, d, ev, [&](const Hit& h) {
     const double e = fabs(h.t - (double)t32);  // selection only
     if (e < near) {
       near = e;
@@ -137,7 +162,30 @@ static __device__ __noinline__ bool solve_proved_x(const SceneDev& S, const ObjI
       found = true;
     }
   });
-  if (!found) return false;
+  return found;
+}
+
+// An object whose nearest root the FP32 scan proved (a single candidate with a certain root
+// and, for a two-leaf CSG object, certain membership of that root's point in the other
+// leaf): only the proved leaf's root is computed in FP64, and a CSG hit point is lifted out
+// of the Logic frame with the operations object_hits uses.  The other roots, the other leaf
+// and the membership tests cannot change which hit object_hits keeps, so the result is the
+// same bits.
+static __device__ __noinline__ bool solve_proved_x(const SceneDev& S, const ObjInfo& oi, V o, V d, int side, int face,
+                                                   float t32, double& ev, lgx::Hit& out) {
+  const lgx::XNode* nd = S.xnode + oi.xnode_begin;
+  const lg_geo& L = S.xgeo[nd[0].geo];
+  if (oi.xnode_count == 1) {
+    if (side != 0 || !leaf_proved_hit(S.xgeo, L, o, d, t32, face, ev, out)) return false;
+    out.node = 0;
+    return true;
+  }
+  if (oi.xnode_count != 3 || L.kind != LG_GEO_LOGIC) return false;
+  const V org = lgx::mk(L.origin[0], L.origin[1]);
+  const V lo = lgx::irot(lgx::vsub(o, org), L.rot[0], L.rot[1]);
+  const V ld = lgx::irot(d, L.rot[0], L.rot[1]);
+  const int li = 1 + side;
+  if (!leaf_proved_hit(S.xgeo, S.xgeo[nd[li].geo], lo, ld, t32, face, ev, out)) return false;
   out.node = li;
   out.p = lgx::vadd(org, lgx::rot(out.p, L.rot[0], L.rot[1]));
   return true;
@@ -195,11 +243,13 @@ __global__ void __launch_bounds__(256, LG_SOLVE_X_BLOCKS) k_solve_x(SceneDev S, 
         second = ob;
       }
     };
-    // proved two-leaf CSG roots first, in a phase of their own
+    // proved roots (single circle and rect leaves, two-leaf CSG) first, in a phase of their own
     bool proved = false;
-    if (valid && i < off[LIST_FULL] && !sc.overflow && sc.nc == 1 && (sc.leaf == 0 || sc.leaf == 1) &&
-        solve_class(__ldg(&S.scan[sl.base + sc.cand[0]].info)) == 4u) {
-      proved = solve_proved_x(S, S.info[sl.base + sc.cand[0]], o, d, sc.leaf, sc.t32, ev, bh);
+    uint32_t pcls = 7u;
+    if (valid && i < off[LIST_FULL] && !sc.overflow && sc.nc == 1 && (sc.leaf == 0 || sc.leaf == 1))
+      pcls = solve_class(__ldg(&S.scan[sl.base + sc.cand[0]].info));
+    if (pcls == 0u || pcls == 1u || pcls == 4u) {
+      proved = solve_proved_x(S, S.info[sl.base + sc.cand[0]], o, d, sc.leaf, sc.face, sc.t32, ev, bh);
       if (proved) {
         best = sc.cand[0];
         ++my_solves;

@@ -57,7 +57,7 @@ __global__ void k_light_setup(SceneDev S);
 // EXACT: the rays hold FP64 coordinates (exact mode); no FP32 canvas exits.
 template <bool MULTI, bool CULL, bool EXACT>
 __global__ void k_scan(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
-int scan_smem_bytes();
+int scan_smem_bytes(bool culled);  // dynamic shared memory of k_scan<_, culled, _> before the object table
 constexpr int SCAN_THREADS = 128;
 template <bool MULTI>
 __global__ void k_refine(SceneDev S, TraceBufs B, uint32_t gen);

@@ -215,15 +215,20 @@ __device__ __forceinline__ void emit_segments(const SceneDev& S, const TraceBufs
 // applies the first-in-object-order tie rule of tracer.rs:404,417 itself.  The runs are
 // either the object table in chunks of SCAN_CHUNK, or (culling grid) the objects listed
 // in the grid cells the lane's ray crosses, nearest cell first.
-// Launch shape (build-time, for sweeps: -DLG_SCAN_CHUNK=..., -DLG_SCAN_CULL_BLOCKS=...).
-#ifndef LG_SCAN_CHUNK
-#define LG_SCAN_CHUNK 8
+// Launch shape (build-time, for sweeps: -DLG_SCAN_CHUNK_CULL=..., -DLG_SCAN_CULL_BLOCKS=...).
+// Pair slots per lane between classifications: the culled walk does best with 8 (a smaller
+// shared-memory buffer leaves more of the SM's L1 to the grid and queue loads), the table scan
+// with 16 (CSG frame: 8 slots 1217 ms of scan, 16 slots 1469; mid frame: 16 slots 68 ms, 8 slots 73).
+#ifndef LG_SCAN_CHUNK_CULL
+#define LG_SCAN_CHUNK_CULL 8
+#endif
+#ifndef LG_SCAN_CHUNK_FULL
+#define LG_SCAN_CHUNK_FULL 16
 #endif
 #ifndef LG_SCAN_CULL_BLOCKS
 #define LG_SCAN_CULL_BLOCKS 3
 #endif
 constexpr int SCAN_WARPS = 4;
-constexpr int SCAN_CHUNK = LG_SCAN_CHUNK;  // pair slots per lane between classifications
 constexpr int WALK_STEPS = 32;  // culled scan: cell steps and object tests between classifications
 constexpr int SCAN_CULL_BLOCKS = LG_SCAN_CULL_BLOCKS;  // culled scan: CTAs per SM the registers are sized for
 
@@ -232,8 +237,9 @@ struct __align__(16) PairSlot {
   uint32_t m;  // object | (leaf + 1) << 16 | (face + 1) << 24; before classification key holds lb
 };
 
-struct ScanSmem {  // [slot][lane]: a warp's 32 lanes touch 32 consecutive slots
-  PairSlot pairs[SCAN_WARPS][SCAN_CHUNK][32];
+template <int CHUNK>
+struct ScanSmemT {  // [slot][lane]: a warp's 32 lanes touch 32 consecutive slots
+  PairSlot pairs[SCAN_WARPS][CHUNK][32];
   PairSlot cand[SCAN_WARPS][CAND][32];
   float4 ray[SCAN_WARPS][32];
   uint32_t src[SCAN_WARPS][32];
@@ -241,11 +247,15 @@ struct ScanSmem {  // [slot][lane]: a warp's 32 lanes touch 32 consecutive slots
   int off[SCAN_WARPS][33];
 };
 
-int scan_smem_bytes() { return (int)sizeof(ScanSmem); }
+int scan_smem_bytes(bool culled) {
+  return culled ? (int)sizeof(ScanSmemT<LG_SCAN_CHUNK_CULL>) : (int)sizeof(ScanSmemT<LG_SCAN_CHUNK_FULL>);
+}
 
 template <bool MULTI, bool CULL, bool EXACT>
 __global__ void __launch_bounds__(SCAN_WARPS * 32, CULL ? SCAN_CULL_BLOCKS : 4)
     k_scan(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
+  constexpr int SCAN_CHUNK = CULL ? LG_SCAN_CHUNK_CULL : LG_SCAN_CHUNK_FULL;
+  using ScanSmem = ScanSmemT<SCAN_CHUNK>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
   ScanSmem& W = *reinterpret_cast<ScanSmem*>(smem_raw);
