@@ -45,7 +45,7 @@ extern "C" {
  *    ray_offset (lg_params grew); lg_trace_stats scan_ms, solve_ms, bounce_ms (grew).
  * 4: lg_string_mod gained the curve parameters and the modulo-colour table (lg_params
  *    grew); string-mod lines are lg_chord records (lg_chords_download), no longer
- *    segments. */
+ *    segments; lg_device_opts.scan_pairs (was padding). */
 #define LG_ABI_VERSION 4
 
 typedef enum lg_status {
@@ -299,7 +299,10 @@ typedef struct lg_device_opts {
   int32_t wait_polls;         /* polls of each bounded device-side wait before it gives up with
                                  LG_ERR_TIMEOUT: 0 = default (2^22); a negative value gives up
                                  at once (exercises the timeout path in tests) */
-  int32_t _pad;
+  int32_t scan_pairs;         /* pair slots per lane of the FP32 nearest-hit scan, 8 or 16; 0 =
+                                 autotune: the first lg_render / lg_batch_render of each scene or
+                                 batch renders with both and keeps the faster (results are
+                                 identical either way) */
 } lg_device_opts;
 
 /* Nearest-hit culling (replaces the reference's approximate tile map, tile_map.rs:18-146).

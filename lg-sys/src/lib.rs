@@ -267,7 +267,7 @@ pub struct lg_device_opts {
     pub culling: i32,
     pub grid_density: f32,
     pub wait_polls: i32,
-    pub _pad: i32,
+    pub scan_pairs: i32,
 }
 
 #[repr(C)]

@@ -124,7 +124,7 @@ class lg_trace_stats(C.Structure):
 class lg_device_opts(C.Structure):
     _fields_ = [("device", C.c_int32), ("raster_variant", C.c_int32), ("segment_capacity", C.c_uint64),
                 ("queue_capacity", C.c_uint64), ("stream_segments", C.c_uint64), ("culling", C.c_int32),
-                ("grid_density", C.c_float), ("wait_polls", C.c_int32), ("_pad", C.c_int32)]
+                ("grid_density", C.c_float), ("wait_polls", C.c_int32), ("scan_pairs", C.c_int32)]
 
 
 LG_ABI_VERSION = 4  # include/lg.h

@@ -707,13 +707,51 @@ lg_status ensure_raster_buffers(lg_ctx* c) {
   return LG_OK;
 }
 
-TraceKernel scan_kernel(bool multi, bool culled, bool exact) {
+template <int CH>
+static TraceKernel scan_kernel_ch(bool multi, bool culled, bool exact) {
   if (exact) {
-    if (multi) return culled ? k_scan<true, true, true> : k_scan<true, false, true>;
-    return culled ? k_scan<false, true, true> : k_scan<false, false, true>;
+    if (multi) return culled ? k_scan<true, true, true, CH> : k_scan<true, false, true, CH>;
+    return culled ? k_scan<false, true, true, CH> : k_scan<false, false, true, CH>;
   }
-  if (multi) return culled ? k_scan<true, true, false> : k_scan<true, false, false>;
-  return culled ? k_scan<false, true, false> : k_scan<false, false, false>;
+  if (multi) return culled ? k_scan<true, true, false, CH> : k_scan<true, false, false, CH>;
+  return culled ? k_scan<false, true, false, CH> : k_scan<false, false, false, CH>;
+}
+
+TraceKernel scan_kernel(bool multi, bool culled, bool exact, int pairs) {
+  return pairs <= 8 ? scan_kernel_ch<8>(multi, culled, exact) : scan_kernel_ch<16>(multi, culled, exact);
+}
+
+// The scan's pair slots per lane: the tuned or requested value, else 8 with a culling grid
+// and 16 without.
+int scan_pairs_of(const lg_ctx* c) { return c->scan_pairs ? c->scan_pairs : (c->culled ? 8 : 16); }
+
+// Occupancy-sized grid of the scan for the context's mode and pair slots.
+lg_status scan_grid(lg_ctx* c, bool multi) {
+  const bool exact = c->prm.precision == LG_PRECISION_EXACT;
+  const int pairs = scan_pairs_of(c);
+  int occ = 0;
+  if (multi) {
+    // serving: the requests' precision is not known yet, the grid fits either kernel
+    int occ_x = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, scan_kernel(true, c->culled, c->serve ? false : exact, pairs),
+                                                     SCAN_THREADS, (size_t)scan_smem_bytes(pairs)), "occupancy");
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_x, scan_kernel(true, c->culled, c->serve ? true : exact, pairs),
+                                                     SCAN_THREADS, (size_t)scan_smem_bytes(pairs)), "occupancy");
+    c->batch_grid_scan = c->n_sm * std::max(1, std::min(occ, occ_x));
+  } else {
+    const size_t tsm = c->smem_fits ? c->obj_smem : 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, scan_kernel(false, c->culled, exact, pairs), SCAN_THREADS,
+                                                     (size_t)scan_smem_bytes(pairs) + tsm), "occupancy");
+    c->trace_grid[0] = c->n_sm * std::max(1, occ);
+  }
+  return LG_OK;
+}
+
+// Switches the scan to `pairs` slots per lane: new grid, new graph.
+lg_status set_scan_pairs(lg_ctx* c, int pairs, bool multi) {
+  c->scan_pairs = pairs;
+  c->graph_valid = false;
+  return scan_grid(c, multi);
 }
 TraceKernel bounce_kernel(bool multi, bool culled) {
   if (multi) return culled ? k_bounce<true, true> : k_bounce<true, false>;
@@ -762,7 +800,8 @@ void launch_generation(lg_ctx* c, const SceneDev& S, const TraceBufs& B, uint32_
                        size_t scan_smem, size_t tsm, int smem_fits) {
   const bool exact = c->prm.precision == LG_PRECISION_EXACT;
   kernel_event(c, g, 0);
-  scan_kernel(multi, c->culled, exact)<<<scan_grid, SCAN_THREADS, scan_smem, c->stream>>>(S, B, g, smem_fits);
+  scan_kernel(multi, c->culled, exact, scan_pairs_of(c))<<<scan_grid, SCAN_THREADS, scan_smem, c->stream>>>(S, B, g,
+                                                                                                   smem_fits);
   kernel_event(c, g, 1);
   if (exact) {
     if (multi) k_solve_x<true><<<c->trace_grid[4], 256, 0, c->stream>>>(S, B, g);
@@ -853,7 +892,7 @@ lg_status enqueue_trace(lg_ctx* c) {
   if (c->n_lights) launch_light_setup(c, S, false, 1);
   const size_t tsm = c->smem_fits ? c->obj_smem : 0;
   for (uint32_t g = 0; g < c->prm.max_bounce; ++g)
-    launch_generation(c, S, B, g, false, c->trace_grid[0], (size_t)scan_smem_bytes(c->culled) + tsm, tsm, c->smem_fits);
+    launch_generation(c, S, B, g, false, c->trace_grid[0], (size_t)scan_smem_bytes(scan_pairs_of(c)) + tsm, tsm, c->smem_fits);
   launch_overlay(c, S, B);
   CK(cudaGetLastError(), "trace launch");
   return LG_OK;
@@ -1072,22 +1111,27 @@ lg_status lg_create(lg_ctx** out, const lg_device_opts* opts) {
   c->culling = opts ? opts->culling : LG_CULL_AUTO;
   c->grid_density = opts ? opts->grid_density : 0.0f;
   if (opts && opts->wait_polls) c->wait_polls = opts->wait_polls < 0 ? 0 : opts->wait_polls;
+  if (opts && opts->scan_pairs != 0 && opts->scan_pairs != 8 && opts->scan_pairs != 16) {
+    delete c;
+    return LG_ERR_INVALID_ARGUMENT;
+  }
+  c->scan_pairs_opt = opts ? opts->scan_pairs : 0;
   cudaError_t e = cudaSetDevice(c->device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, c->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_ctr, sizeof(Counters));
   if (e == cudaSuccess) e = cudaMalloc(&c->d_ctr.p, sizeof(Counters));
   for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
-  for (TraceKernel k : {k_scan<false, false, false>, k_scan<false, true, false>, k_scan<false, false, true>,
-                        k_scan<false, true, true>})
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, scan_smem_bytes(false) + (int)OBJ_SMEM_MAX);
+  for (int pairs : {8, 16})
+    for (int m = 0; m < 2; ++m)
+      for (int cu = 0; cu < 2; ++cu)
+        for (int ex = 0; ex < 2; ++ex)
+          if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(scan_kernel(m != 0, cu != 0, ex != 0, pairs), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     scan_smem_bytes(pairs) + (m ? 0 : (int)OBJ_SMEM_MAX));
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_full<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
   for (TraceKernel k : {k_bounce<false, false>, k_bounce<false, true>})
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OBJ_SMEM_MAX);
-  for (TraceKernel k : {k_scan<true, false, false>, k_scan<true, true, false>, k_scan<true, false, true>,
-                        k_scan<true, true, true>})
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, scan_smem_bytes(false));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_bin_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(MAX_SMEM_TILES * 4));
   if (e == cudaSuccess)
@@ -1214,9 +1258,11 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
   c->smem_fits = c->obj_smem <= OBJ_SMEM_MAX ? 1 : 0;
   int occ = 0;
   const size_t tsm = c->smem_fits ? c->obj_smem : 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, scan_kernel(false, c->culled, p.precision == LG_PRECISION_EXACT),
-                                                   SCAN_THREADS, (size_t)scan_smem_bytes(c->culled) + tsm), "occupancy");
-  c->trace_grid[0] = c->n_sm * std::max(1, occ);
+  if (!same_shape) {  // a new scene: its first lg_render times both scan pair-buffer sizes
+    c->scan_pairs = c->scan_pairs_opt;
+    c->scan_tune = c->scan_pairs_opt == 0;
+  }
+  if ((st = scan_grid(c, false))) return st;
   if ((st = trace_grids(c, false, tsm))) return st;
   const int mode = raster_mode(p);
   const int rsm = raster_smem_bytes(mode);
@@ -1361,7 +1407,7 @@ static lg_status enqueue_stream_frame(lg_ctx* c, uint16_t* dst, size_t row, cuda
   const size_t rsm = (size_t)raster_smem_bytes(mode);
   const uint32_t G = c->prm.max_bounce;
   for (uint32_t g = 0; g < G; ++g) {
-    launch_generation(c, S, B, g, false, c->trace_grid[0], (size_t)scan_smem_bytes(c->culled) + tsm, tsm, c->smem_fits);
+    launch_generation(c, S, B, g, false, c->trace_grid[0], (size_t)scan_smem_bytes(scan_pairs_of(c)) + tsm, tsm, c->smem_fits);
     if (g == 0) {
       launch_overlay(c, S, B);
       launch_chords(c, A);
@@ -1487,9 +1533,32 @@ static lg_status render_streaming(lg_ctx* c, uint16_t* dst, size_t pitch, int32_
   return fail(c, LG_ERR_OUT_OF_MEMORY, "render buffers kept overflowing");
 }
 
+static lg_status render_frame(lg_ctx* c, uint16_t* dst, size_t pitch, int32_t dst_is_device, lg_trace_stats* stats);
+
+// The first frame of a scene (unless lg_device_opts.scan_pairs fixes it) renders with each
+// scan pair-buffer size and keeps the one whose scan kernels ran faster; the frames are
+// identical, so the caller's image is simply the last one.
 lg_status lg_render(lg_ctx* c, uint16_t* dst, size_t pitch, int32_t dst_is_device, lg_trace_stats* stats) {
   lg_status st = need_scene(c);
   if (st) return st;
+  if (c->scan_tune) {
+    c->scan_tune = false;
+    float best = INFINITY;
+    int pick = scan_pairs_of(c);
+    for (int pairs : {8, 16}) {
+      if ((st = set_scan_pairs(c, pairs, false))) return st;
+      lg_trace_stats s;
+      if ((st = render_frame(c, dst, pitch, dst_is_device, &s))) return st;
+      const float ms = s.scan_ms > 0.0f ? s.scan_ms : s.total_ms;
+      if (ms < best) { best = ms; pick = pairs; }
+    }
+    if ((st = set_scan_pairs(c, pick, false))) return st;
+  }
+  return render_frame(c, dst, pitch, dst_is_device, stats);
+}
+
+static lg_status render_frame(lg_ctx* c, uint16_t* dst, size_t pitch, int32_t dst_is_device, lg_trace_stats* stats) {
+  lg_status st = LG_OK;
   const size_t row = (size_t)c->prm.width * 8;
   if (!dst || pitch < row) return fail(c, LG_ERR_INVALID_ARGUMENT, "destination null or pitch < width * 8");
   uint32_t retries = 0;

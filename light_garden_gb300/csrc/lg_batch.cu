@@ -99,7 +99,7 @@ lg_status enqueue_batch(lg_ctx* c, cudaEvent_t* ev) {
       k_scene_scatter<<<c->n_sm * 8, 256, 0, c->stream>>>(S, B, g, (unsigned*)c->d_scene_off.p,
                                                           (uint32_t*)c->d_order.p);
     }
-    launch_generation(c, S, B, g, true, c->batch_grid_scan, (size_t)scan_smem_bytes(c->culled), 0, 0);
+    launch_generation(c, S, B, g, true, c->batch_grid_scan, (size_t)scan_smem_bytes(scan_pairs_of(c)), 0, 0);
     if (g == 0 && c->n_cubic) {
       const int blocks = (int)std::min<uint64_t>((3ull * c->n_cubic + 255) / 256, 4096);
       k_overlay<<<blocks, 256, 0, c->stream>>>(S, B, (const uint32_t*)c->d_cubics.p,
@@ -347,9 +347,9 @@ lg_status lg_batch_upload(lg_ctx* c, const lg_scene_desc* scenes, uint32_t k) {
   if ((st = batch_buffers(c))) return st;
   // launch shapes: the multi-scene kernels read the object tables from global memory
   int occ = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, scan_kernel(true, c->culled, c->prm.precision == LG_PRECISION_EXACT),
-                                                   SCAN_THREADS, (size_t)scan_smem_bytes(c->culled)), "occupancy");
-  c->batch_grid_scan = c->n_sm * std::max(1, occ);
+  c->scan_pairs = c->scan_pairs_opt;  // a new batch: its first lg_batch_render times both scan sizes
+  c->scan_tune = c->scan_pairs_opt == 0;
+  if ((st = scan_grid(c, true))) return st;
   if ((st = trace_grids(c, true, 0))) return st;
   const int mode = raster_mode(c->prm);
   const int rsm = raster_smem_bytes(mode);
@@ -395,6 +395,21 @@ lg_status lg_batch_render(lg_ctx* c, uint16_t* dst, uint64_t dst_bytes, int32_t 
   std::vector<cudaEvent_t>& ev = c->bev;
   uint32_t retries = 0;
   lg_status st;
+  if (c->scan_tune) {
+    // autotune of the scan's pair slots per lane: the whole batch with each size (identical
+    // images), keep the one whose generations trace faster
+    c->scan_tune = false;
+    float best = INFINITY;
+    int pick = scan_pairs_of(c);
+    for (int pairs : {8, 16}) {
+      if ((st = set_scan_pairs(c, pairs, true))) return st;
+      if ((st = run_batch(c, ev, retries))) return st;
+      float ms = 0.f;
+      for (uint32_t g = 0; g < c->max_bounce_all; ++g) ms += elapsed(g == 0 ? ev[0] : ev[2 * g], ev[1 + 2 * g]);
+      if (ms < best) { best = ms; pick = pairs; }
+    }
+    if ((st = set_scan_pairs(c, pick, true))) return st;
+  }
   if (c->raster_variant == 0) {
     // autotune: the whole batch with each tile-raster kernel (identical images), keep the faster
     float best = INFINITY;

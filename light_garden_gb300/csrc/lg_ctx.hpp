@@ -60,6 +60,9 @@ struct lg_ctx {
   int trace_grid[6] = {0, 0, 0, 0, 0, 0}, raster_grid = 0, bin_grid = 0;
   int raster_warp_grid = 0;
   int raster_variant = 0;  // 1 shared-atomic tile raster, 2 warp-private tile raster; 0 = not tuned yet
+  int scan_pairs = 0;      // pair slots per lane of the scan (8 / 16; 0: by the culling grid)
+  int scan_pairs_opt = 0;  // lg_device_opts.scan_pairs (0: tune on a scene's first render)
+  bool scan_tune = false;  // the next lg_render / lg_batch_render times both sizes first
   size_t obj_smem = 0;
   int smem_fits = 0;
   // graph
@@ -118,7 +121,12 @@ void launch_bin_count(lg_ctx* c, const RasterArgs& A, int smem_tiles, size_t bsm
 // without the culling walk).
 using TraceKernel = void (*)(SceneDev, TraceBufs, uint32_t, int);
 using TraceKernel3 = void (*)(SceneDev, TraceBufs, uint32_t);
-TraceKernel scan_kernel(bool multi, bool culled, bool exact);
+TraceKernel scan_kernel(bool multi, bool culled, bool exact, int pairs);
+// The scan's pair slots per lane for the context, its occupancy-sized grid (trace_grid[0], or
+// batch_grid_scan when multi), and a switch to another size (new grid, graph invalidated).
+int scan_pairs_of(const lg_ctx* c);
+lg_status scan_grid(lg_ctx* c, bool multi);
+lg_status set_scan_pairs(lg_ctx* c, int pairs, bool multi);
 TraceKernel bounce_kernel(bool multi, bool culled);
 TraceKernel3 bounce_x_kernel(bool multi, bool culled);
 // Occupancy-sized grids of the trace kernels for the context's mode (trace_grid[1..5]).

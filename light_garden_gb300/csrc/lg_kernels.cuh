@@ -55,9 +55,10 @@ __global__ void k_light_setup(SceneDev S);
 // CULL: the culling-grid walk is compiled in (scenes whose grid has nx == 0 still take
 // the full scan); without it the kernels scan every object.
 // EXACT: the rays hold FP64 coordinates (exact mode); no FP32 canvas exits.
-template <bool MULTI, bool CULL, bool EXACT>
+// CHUNK: pair slots per lane between classifications (8 or 16).
+template <bool MULTI, bool CULL, bool EXACT, int CHUNK>
 __global__ void k_scan(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits);
-int scan_smem_bytes(bool culled);  // dynamic shared memory of k_scan<_, culled, _> before the object table
+int scan_smem_bytes(int pairs);  // dynamic shared memory of k_scan<.., pairs> before the object table
 constexpr int SCAN_THREADS = 128;
 template <bool MULTI>
 __global__ void k_refine(SceneDev S, TraceBufs B, uint32_t gen);

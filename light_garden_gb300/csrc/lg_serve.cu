@@ -399,11 +399,9 @@ lg_status lg_serve_begin(lg_ctx* c, const lg_serve_opts* opts) {
   std::memset(c->h_ctr, 0, sizeof(Counters));
   // launch shapes of the multi-scene kernels
   int occ = 0;
-  // the requests' precision is not known yet: the scan grid fits either kernel
-  int occ_x = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, scan_kernel(true, c->culled, false), SCAN_THREADS, (size_t)scan_smem_bytes(c->culled)), "occupancy");
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_x, scan_kernel(true, c->culled, true), SCAN_THREADS, (size_t)scan_smem_bytes(c->culled)), "occupancy");
-  c->batch_grid_scan = c->n_sm * std::max(1, std::min(occ, occ_x));
+  c->scan_pairs = c->scan_pairs_opt;  // served requests keep the untuned rule (or the requested size)
+  c->scan_tune = false;
+  if ((st = scan_grid(c, true))) { serve_free(c); return st; }
   if ((st = trace_grids(c, true, 0))) { serve_free(c); return st; }
   const int rsm = raster_smem_bytes(RM_FIXED_SPLIT_);
   CK(cudaFuncSetAttribute(k_raster<RM_FIXED_SPLIT_>, cudaFuncAttributeMaxDynamicSharedMemorySize, rsm), "smem attr");
@@ -549,7 +547,7 @@ lg_status lg_serve_step(lg_ctx* c, lg_serve_step_stats* stats) {
     k_scene_offsets<<<1, 1024, 0, c->stream>>>((unsigned*)c->d_scene_count.p, (unsigned*)c->d_scene_off.p, V.max_slots);
     k_scene_scatter<<<c->n_sm * 8, 256, 0, c->stream>>>(SD, B, g, (unsigned*)c->d_scene_off.p, (uint32_t*)c->d_order.p);
   }
-  launch_generation(c, SD, B, g, true, c->batch_grid_scan, (size_t)scan_smem_bytes(c->culled), 0, 0);
+  launch_generation(c, SD, B, g, true, c->batch_grid_scan, (size_t)scan_smem_bytes(scan_pairs_of(c)), 0, 0);
   if (!cubic_obj.empty()) {
     lg_string_mod no_sm;
     std::memset(&no_sm, 0, sizeof no_sm);

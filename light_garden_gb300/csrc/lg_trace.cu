@@ -215,16 +215,12 @@ __device__ __forceinline__ void emit_segments(const SceneDev& S, const TraceBufs
 // applies the first-in-object-order tie rule of tracer.rs:404,417 itself.  The runs are
 // either the object table in chunks of SCAN_CHUNK, or (culling grid) the objects listed
 // in the grid cells the lane's ray crosses, nearest cell first.
-// Launch shape (build-time, for sweeps: -DLG_SCAN_CHUNK_CULL=..., -DLG_SCAN_CULL_BLOCKS=...).
-// Pair slots per lane between classifications: the culled walk does best with 8 (a smaller
-// shared-memory buffer leaves more of the SM's L1 to the grid and queue loads), the table scan
-// with 16 (CSG frame: 8 slots 1217 ms of scan, 16 slots 1469; mid frame: 16 slots 68 ms, 8 slots 73).
-#ifndef LG_SCAN_CHUNK_CULL
-#define LG_SCAN_CHUNK_CULL 8
-#endif
-#ifndef LG_SCAN_CHUNK_FULL
-#define LG_SCAN_CHUNK_FULL 16
-#endif
+// Launch shape.  The pair slots per lane between classifications (CHUNK, 8 or 16) are a
+// template parameter that each context tunes on its first frame (lg_device_opts.scan_pairs):
+// the culled walk tends to do best with 8 (a smaller shared-memory buffer leaves more of the
+// SM's L1 to the grid and queue loads), the table scan with 16 (CSG frame: 8 slots 1217 ms of
+// scan, 16 slots 1469; mid frame: 16 slots 68 ms, 8 slots 73).  CTAs per SM of the culled scan
+// are build-time (-DLG_SCAN_CULL_BLOCKS=..., for sweeps).
 #ifndef LG_SCAN_CULL_BLOCKS
 #define LG_SCAN_CULL_BLOCKS 3
 #endif
@@ -247,14 +243,12 @@ struct ScanSmemT {  // [slot][lane]: a warp's 32 lanes touch 32 consecutive slot
   int off[SCAN_WARPS][33];
 };
 
-int scan_smem_bytes(bool culled) {
-  return culled ? (int)sizeof(ScanSmemT<LG_SCAN_CHUNK_CULL>) : (int)sizeof(ScanSmemT<LG_SCAN_CHUNK_FULL>);
-}
+int scan_smem_bytes(int pairs) { return pairs <= 8 ? (int)sizeof(ScanSmemT<8>) : (int)sizeof(ScanSmemT<16>); }
 
-template <bool MULTI, bool CULL, bool EXACT>
+template <bool MULTI, bool CULL, bool EXACT, int CHUNK>
 __global__ void __launch_bounds__(SCAN_WARPS * 32, CULL ? SCAN_CULL_BLOCKS : 4)
     k_scan(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
-  constexpr int SCAN_CHUNK = CULL ? LG_SCAN_CHUNK_CULL : LG_SCAN_CHUNK_FULL;
+  constexpr int SCAN_CHUNK = CHUNK;
   using ScanSmem = ScanSmemT<SCAN_CHUNK>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
@@ -627,14 +621,22 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, CULL ? SCAN_CULL_BLOCKS : 4)
   }
 }
 
-template __global__ void k_scan<false, false, false>(SceneDev, TraceBufs, uint32_t, int);
-template __global__ void k_scan<false, true, false>(SceneDev, TraceBufs, uint32_t, int);
-template __global__ void k_scan<true, false, false>(SceneDev, TraceBufs, uint32_t, int);
-template __global__ void k_scan<true, true, false>(SceneDev, TraceBufs, uint32_t, int);
-template __global__ void k_scan<false, false, true>(SceneDev, TraceBufs, uint32_t, int);
-template __global__ void k_scan<false, true, true>(SceneDev, TraceBufs, uint32_t, int);
-template __global__ void k_scan<true, false, true>(SceneDev, TraceBufs, uint32_t, int);
-template __global__ void k_scan<true, true, true>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<false, false, false, 8>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<false, false, true, 8>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<false, true, false, 8>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<false, true, true, 8>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<true, false, false, 8>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<true, false, true, 8>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<true, true, false, 8>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<true, true, true, 8>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<false, false, false, 16>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<false, false, true, 16>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<false, true, false, 16>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<false, true, true, 16>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<true, false, false, 16>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<true, false, true, 16>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<true, true, false, 16>(SceneDev, TraceBufs, uint32_t, int);
+template __global__ void k_scan<true, true, true, 16>(SceneDev, TraceBufs, uint32_t, int);
 
 __device__ __forceinline__ void store_hit(HitRec& o, int obj, const Hit64& h, float ev, uint8_t flags) {
   o.obj = obj < 0 ? HIT_NONE : (uint16_t)obj;

@@ -18,10 +18,10 @@ from .scene import PackedScene
 class Context:
     def __init__(self, device: int = 0, segment_capacity: int = 0, queue_capacity: int = 0, raster_variant: int = 0,
                  stream_segments: int = 0, culling: int = abi.LG_CULL_AUTO, grid_density: float = 0.0,
-                 wait_polls: int = 0):
+                 wait_polls: int = 0, scan_pairs: int = 0):
         self.lib = abi.load()
         opts = abi.lg_device_opts(device, raster_variant, segment_capacity, queue_capacity, stream_segments, culling,
-                                  grid_density, wait_polls)
+                                  grid_density, wait_polls, scan_pairs)
         h = C.c_void_p()
         st = self.lib.lg_create(C.byref(h), C.byref(opts))
         if st != abi.LG_OK:
