@@ -590,7 +590,8 @@ def run_ours(args, ws, rank, local):
             c3.close()
             return {"workload": WORKLOADS[name] + ", double-float precision", "value": s3["segments"] / (a3["total_ms"] * 1e-3),
                     "unit": "segments/s", "ms_per_step": a3["total_ms"], "stage_ms": a3,
-                    "near_degenerate_per_step": s3["near_degenerate"]}
+                    "flagged_per_step": {"decision_band": s3["near_degenerate"], "ill_conditioned": s3["ill_conditioned"],
+                                         "segments": s3["segments"]}}
 
         if name != "mid":
             extra("mid_scene", mid)

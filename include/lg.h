@@ -45,7 +45,8 @@ extern "C" {
  *    ray_offset (lg_params grew); lg_trace_stats scan_ms, solve_ms, bounce_ms (grew).
  * 4: lg_string_mod gained the curve parameters and the modulo-colour table (lg_params
  *    grew); string-mod lines are lg_chord records (lg_chords_download), no longer
- *    segments; lg_device_opts.scan_pairs (was padding). */
+ *    segments; lg_device_opts.scan_pairs (was padding); LG_PATH_ILL_CONDITIONED split from
+ *    LG_PATH_NEAR_DEGENERATE, lg_trace_stats.ill_conditioned (grew). */
 #define LG_ABI_VERSION 4
 
 typedef enum lg_status {
@@ -248,7 +249,10 @@ typedef struct lg_chord {
 enum lg_path_flags {
   LG_PATH_NEAR_DEGENERATE = 1, /* a decision on this path fell inside the FP64 epsilon band */
   LG_PATH_TIR = 2,             /* this segment ends in total internal reflection */
-  LG_PATH_FALLBACK = 4         /* candidate list overflowed: every object re-solved in FP64 */
+  LG_PATH_FALLBACK = 4,        /* candidate list overflowed: every object re-solved in FP64 */
+  LG_PATH_ILL_CONDITIONED = 8  /* double-float mode: the ray's rounding bound passed 1e-6 (chaotic
+                                  amplification along the path), so the path may part from an
+                                  FP64 trace although no decision fell in a band */
 };
 /* LG_SRC_STRING_MOD is kept for numbering; string-mod lines are lg_chord records. */
 enum lg_path_source { LG_SRC_TRACE = 0, LG_SRC_CONTROL_LINE = 1, LG_SRC_STRING_MOD = 2 };
@@ -270,7 +274,7 @@ typedef struct lg_trace_stats {
   uint64_t segments;       /* segments written (traced + control lines) */
   uint64_t fp64_solves;    /* object intersections re-solved in FP64 */
   uint64_t fp64_fallbacks; /* rays whose FP32 candidate list overflowed */
-  uint64_t near_degenerate;/* segments carrying LG_PATH_NEAR_DEGENERATE */
+  uint64_t near_degenerate;/* segments carrying LG_PATH_NEAR_DEGENERATE (a decision in its band) */
   uint64_t pixels;         /* pixel updates made by lg_accumulate */
   uint64_t tile_refs;      /* (segment, tile) pairs binned by lg_accumulate */
   uint64_t bound_tests;    /* FP32 ray / bounding-circle tests of the nearest-hit search */
@@ -284,6 +288,7 @@ typedef struct lg_trace_stats {
      the precise solve (k_solve_x, or k_refine + k_full), the bounce */
   float scan_ms, solve_ms, bounce_ms;
   float _pad2;
+  uint64_t ill_conditioned; /* segments carrying LG_PATH_ILL_CONDITIONED (double-float mode) */
 } lg_trace_stats;
 
 typedef struct lg_device_opts {

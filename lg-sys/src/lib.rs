@@ -93,6 +93,7 @@ pub const LG_PRECISION_FAST: i32 = 1;
 pub const LG_PATH_NEAR_DEGENERATE: u8 = 1;
 pub const LG_PATH_TIR: u8 = 2;
 pub const LG_PATH_FALLBACK: u8 = 4;
+pub const LG_PATH_ILL_CONDITIONED: u8 = 8;
 // lg_path_source
 pub const LG_SRC_TRACE: u32 = 0;
 pub const LG_SRC_CONTROL_LINE: u32 = 1;
@@ -254,6 +255,7 @@ pub struct lg_trace_stats {
     pub solve_ms: f32,
     pub bounce_ms: f32,
     pub _pad2: f32,
+    pub ill_conditioned: u64,
 }
 
 #[repr(C)]

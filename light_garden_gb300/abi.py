@@ -46,7 +46,7 @@ LG_BO_ADD, LG_BO_SUBTRACT, LG_BO_REVERSE_SUBTRACT, LG_BO_MIN, LG_BO_MAX = range(
 LG_ACCUM_FIXED64, LG_ACCUM_F32 = 0, 1
 LG_SM_ADD, LG_SM_MUL, LG_SM_POW, LG_SM_BASE = range(4)
 LG_CURVE_CIRCLE, LG_CURVE_COMPLEX_EXP, LG_CURVE_HYPOTROCHOID, LG_CURVE_LISSAJOUS = range(4)
-LG_PATH_NEAR_DEGENERATE, LG_PATH_TIR, LG_PATH_FALLBACK = 1, 2, 4
+LG_PATH_NEAR_DEGENERATE, LG_PATH_TIR, LG_PATH_FALLBACK, LG_PATH_ILL_CONDITIONED = 1, 2, 4, 8
 LG_SRC_TRACE, LG_SRC_CONTROL_LINE, LG_SRC_STRING_MOD = 0, 1, 2
 
 
@@ -115,7 +115,8 @@ class lg_trace_stats(C.Structure):
                 ("retries", C.c_uint32), ("_pad", C.c_uint32),
                 ("trace_ms", C.c_float), ("accumulate_ms", C.c_float), ("resolve_ms", C.c_float),
                 ("total_ms", C.c_float), ("bin_ms", C.c_float), ("raster_ms", C.c_float),
-                ("scan_ms", C.c_float), ("solve_ms", C.c_float), ("bounce_ms", C.c_float), ("_pad2", C.c_float)]
+                ("scan_ms", C.c_float), ("solve_ms", C.c_float), ("bounce_ms", C.c_float), ("_pad2", C.c_float),
+                ("ill_conditioned", C.c_uint64)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_ if not name.startswith("_")}

@@ -989,6 +989,7 @@ void fill_stats(lg_ctx* c, lg_trace_stats* s) {
   s->fp64_solves = k.fp64_solves;
   s->fp64_fallbacks = k.fallbacks;
   s->near_degenerate = k.near;
+  s->ill_conditioned = k.ill;
   s->pixels = k.pixels;
   s->tile_refs = k.tile_refs;
   s->bound_tests = k.bound_tests;

@@ -149,7 +149,7 @@ struct Counters {
   unsigned long long seg_count;               // ring cursor (= segments demanded)
   unsigned long long queue_count[MAX_GEN + 1]; // entries demanded per generation
   unsigned long long list_count[MAX_GEN][N_LISTS];
-  unsigned long long visits, fp64_solves, fallbacks, near;
+  unsigned long long visits, fp64_solves, fallbacks, near, ill;
   unsigned long long pixels, tile_refs, units;
   unsigned long long unit_cursor;
   // multi-scene streaming accumulation: the ring and the tile lists are reused every
@@ -924,9 +924,11 @@ __device__ __forceinline__ int leaf_roots32(uint32_t kind, const float* L, const
     const float le = fabsf(ex) + fabsf(ey);
     const float wn = fabsf(wx) + fabsf(wy);
     if (fabsf(den) <= 1e-4f * le) { unknown = true; return 0; }
-    const float t0 = (wx * ey - wy * ex) / den, u = (wx * dy - wy * dx) / den;
-    tol = 4e-6f * (wn + le) * (1.0f + le / fabsf(den)) + 1e-6f;
-    const float ub = 1e-5f * (1.0f + (wn + le) / le) * (1.0f + le / fabsf(den));
+    // one approximate reciprocal (2 ulp) for both quotients: far inside the 4e-6 tolerance
+    const float inv = __fdividef(1.0f, den);
+    const float t0 = (wx * ey - wy * ex) * inv, u = (wx * dy - wy * dx) * inv;
+    tol = 4e-6f * (wn + le) * (1.0f + le * fabsf(inv)) + 1e-6f;
+    const float ub = 1e-5f * (1.0f + (wn + le) / le) * (1.0f + le * fabsf(inv));
     if (u < -ub || u > 1.0f + ub) return 0;
     t[0] = t0;
     cert[0] = !(u < ub || u > 1.0f - ub);
@@ -947,7 +949,8 @@ __device__ __forceinline__ int leaf_roots32(uint32_t kind, const float* L, const
       if (fabsf(O[ax]) >= H[ax] - band) { unknown = true; return 0; }
       continue;
     }
-    float t1 = (-H[ax] - O[ax]) / D[ax], t2 = (H[ax] - O[ax]) / D[ax];
+    const float inv = __fdividef(1.0f, D[ax]);  // approximate reciprocal (2 ulp): far inside tol
+    float t1 = (-H[ax] - O[ax]) * inv, t2 = (H[ax] - O[ax]) * inv;
     // entering through the -H face when D > 0 (outward normal -1), else the +H face
     int f1 = 2 * ax + (D[ax] > 0.0f ? 0 : 1), f2 = 2 * ax + (D[ax] > 0.0f ? 1 : 0);
     if (t1 > t2) { const float x = t1; t1 = t2; t2 = x; }

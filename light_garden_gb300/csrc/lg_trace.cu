@@ -182,7 +182,7 @@ __device__ __forceinline__ bool fast_canvas_exit(const df aspect, const RayRec& 
 // appends one segment per emitting lane with one atomic per warp (all lanes call)
 __device__ __forceinline__ void emit_segments(const SceneDev& S, const TraceBufs& B, bool emit, const RayRec& r,
                                               float x1, float y1, uint8_t flags, int hit,
-                                              unsigned long long& my_near) {
+                                              unsigned long long& my_near, unsigned long long& my_ill) {
   const unsigned lane = lane_id();
   const unsigned emask = __ballot_sync(0xffffffffu, emit);
   if (!emask) return;
@@ -193,6 +193,7 @@ __device__ __forceinline__ void emit_segments(const SceneDev& S, const TraceBufs
   if (!emit) return;
   const unsigned long long slot = sbase + __popc(emask & lanemask_lt());
   if (flags & LG_PATH_NEAR_DEGENERATE) ++my_near;
+  if (flags & LG_PATH_ILL_CONDITIONED) ++my_ill;
   if (slot >= B.seg_cap) return;
   float4* dst = reinterpret_cast<float4*>(B.segs + slot);
   dst[0] = make_float4(r.ox.hi, r.oy.hi, x1, y1);
@@ -254,9 +255,9 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, CULL ? SCAN_CULL_BLOCKS : 4)
   __shared__ __align__(8) uint64_t bar;
   ScanSmem& W = *reinterpret_cast<ScanSmem*>(smem_raw);
   ObjScan* sobj = reinterpret_cast<ObjScan*>(smem_raw + sizeof(ScanSmem));
-  __shared__ unsigned long long blk_visits, blk_near, blk_tests, blk_cls;
-  if (threadIdx.x == 0) { blk_visits = 0; blk_near = 0; blk_tests = 0; blk_cls = 0; }
-  unsigned long long my_visits = 0, my_near = 0;
+  __shared__ unsigned long long blk_visits, blk_near, blk_ill, blk_tests, blk_cls;
+  if (threadIdx.x == 0) { blk_visits = 0; blk_near = 0; blk_ill = 0; blk_tests = 0; blk_cls = 0; }
+  unsigned long long my_visits = 0, my_near = 0, my_ill = 0;
   uint32_t my_tests = 0;
   bool failed;
   const ObjScan* objs = stage_objects(S, sobj, &bar, !MULTI && smem_fits != 0, B.ctr, failed);
@@ -598,7 +599,8 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, CULL ? SCAN_CULL_BLOCKS : 4)
           if (!EXACT && fast_canvas_exit(slp.aspect, r, x1, y1, L)) {
             emit = true;
             ++my_visits;
-            eflags = r.flags | (near_cutoff(r.c, slp.cutoff) || L > ILL_COND ? LG_PATH_NEAR_DEGENERATE : 0);
+            eflags = r.flags | (near_cutoff(r.c, slp.cutoff) ? LG_PATH_NEAR_DEGENERATE : 0) |
+                     (L > ILL_COND ? LG_PATH_ILL_CONDITIONED : 0);
           } else {
             list = LIST_EXIT;
           }
@@ -607,15 +609,17 @@ __global__ void __launch_bounds__(SCAN_WARPS * 32, CULL ? SCAN_CULL_BLOCKS : 4)
       B.scan[idx] = sc;
       list_append(B, gen, list, (uint32_t)idx);
     }
-    emit_segments(S, B, emit, r, x1, y1, eflags, -1, my_near);
+    emit_segments(S, B, emit, r, x1, y1, eflags, -1, my_near, my_ill);
   }
   atomicAdd(&blk_visits, my_visits);
   atomicAdd(&blk_near, my_near);
+  atomicAdd(&blk_ill, my_ill);
   atomicAdd(&blk_tests, (unsigned long long)my_tests);
   __syncthreads();
   if (threadIdx.x == 0) {
     atomicAdd(&B.ctr->visits, blk_visits);
     atomicAdd(&B.ctr->near, blk_near);
+    atomicAdd(&B.ctr->ill, blk_ill);
     atomicAdd(&B.ctr->bound_tests, blk_tests);
     atomicAdd(&B.ctr->object_tests, blk_cls);
   }
@@ -813,7 +817,7 @@ __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, c
     const float ref_solve = kap > 0.0f ? FP64_SOLVE_EPS * oc * oc * kap / fmaxf(ci_abs, 1e-6f) : 0.0f;
     const float L = r.ex + bh.t.hi * r.ea + DF_ROUND * (1.0f + fabsf(bh.px.hi) + fabsf(bh.py.hi)) + ref_solve;
     const float ds = L / fmaxf(ci_abs, 1e-6f);
-    if (L > ILL_COND) fl |= LG_PATH_NEAR_DEGENERATE;
+    if (L > ILL_COND) fl |= LG_PATH_ILL_CONDITIONED;
     if (oi.flags & INFO_MATERIAL) {
       // medium on the far side (tracer.rs:428-442); "origin inside obj" at the midpoint
       df n2 = DF_ONE;
@@ -940,7 +944,7 @@ __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, c
       v.x1 = ch[bi].px.hi; v.y1 = ch[bi].py.hi;
       v.hit = -1;
       const float L = r.ex + ch[bi].t.hi * r.ea;
-      v.flags = fl | (cev.ev < INFINITY || L > ILL_COND ? LG_PATH_NEAR_DEGENERATE : 0);
+      v.flags = fl | (cev.ev < INFINITY ? LG_PATH_NEAR_DEGENERATE : 0) | (L > ILL_COND ? LG_PATH_ILL_CONDITIONED : 0);
     }
   }
   // children: the next generation skips colours below the cutoff (tracer.rs:378-384)
@@ -953,7 +957,8 @@ __device__ __forceinline__ void bounce(const SceneDev& S, const ObjScan* objs, c
     c.light = r.light;
     c._pad = 0;
     c.scene = r.scene;
-    if (near_cutoff(c.c, sl.cutoff) || !(c.ex <= ILL_COND && c.ea <= ILL_COND)) c.flags |= LG_PATH_NEAR_DEGENERATE;
+    if (near_cutoff(c.c, sl.cutoff)) c.flags |= LG_PATH_NEAR_DEGENERATE;
+    if (!(c.ex <= ILL_COND && c.ea <= ILL_COND)) c.flags |= LG_PATH_ILL_CONDITIONED;
     v.child[w++] = c;
   }
   v.nchild = w;
@@ -963,8 +968,8 @@ template <bool MULTI, bool CULL>
 __global__ void __launch_bounds__(256, 3) k_bounce(SceneDev S, TraceBufs B, uint32_t gen, int smem_fits) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
-  __shared__ unsigned long long blk_visits, blk_near;
-  if (threadIdx.x == 0) { blk_visits = 0; blk_near = 0; }
+  __shared__ unsigned long long blk_visits, blk_near, blk_ill;
+  if (threadIdx.x == 0) { blk_visits = 0; blk_near = 0; blk_ill = 0; }
   bool failed;
   const ObjScan* objs = stage_objects(S, reinterpret_cast<ObjScan*>(smem_raw), &bar, !MULTI && smem_fits != 0, B.ctr,
                                       failed);
@@ -982,7 +987,7 @@ __global__ void __launch_bounds__(256, 3) k_bounce(SceneDev S, TraceBufs B, uint
   const unsigned lane = lane_id();
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
-  unsigned long long my_visits = 0, my_near = 0;
+  unsigned long long my_visits = 0, my_near = 0, my_ill = 0;
   for (uint64_t base = warp * 32; base < total; base += nwarps * 32) {
     const uint64_t i = base + lane;
     Bounce v;
@@ -1002,7 +1007,7 @@ __global__ void __launch_bounds__(256, 3) k_bounce(SceneDev S, TraceBufs B, uint
         bounce<MULTI, CULL>(S, objs, r, sc, &B.hit[idx], v);
       }
     }
-    emit_segments(S, B, v.emit, r, v.x1, v.y1, v.flags, v.hit, my_near);
+    emit_segments(S, B, v.emit, r, v.x1, v.y1, v.flags, v.hit, my_near, my_ill);
     // children: warp prefix sum of 0..2 per lane, one atomic per warp
     int incl = v.nchild;
 #pragma unroll
@@ -1022,10 +1027,12 @@ __global__ void __launch_bounds__(256, 3) k_bounce(SceneDev S, TraceBufs B, uint
   }
   atomicAdd(&blk_visits, my_visits);
   atomicAdd(&blk_near, my_near);
+  atomicAdd(&blk_ill, my_ill);
   __syncthreads();
   if (threadIdx.x == 0) {
     atomicAdd(&B.ctr->visits, blk_visits);
     atomicAdd(&B.ctr->near, blk_near);
+    atomicAdd(&B.ctr->ill, blk_ill);
   }
 }
 template __global__ void k_bounce<false, false>(SceneDev, TraceBufs, uint32_t, int);

@@ -8,9 +8,12 @@ near-degenerate flag is reported, not compared: the oracle also raises it for de
 objects the GPU's FP32 search proved irrelevant.
 
 compare(): the bar of LG_PRECISION_FAST (double-float).  Hit-object ids and the set of
-segments match exactly outside the near-degenerate set (segments flagged
-LG_PATH_NEAR_DEGENERATE on either side, which includes every descendant of a flagged
-decision), and endpoints match within ENDPOINT_TOL relative to max(1, |p|).
+segments match exactly outside the flagged set, and endpoints match within ENDPOINT_TOL
+relative to max(1, |p|).  Flagged means LG_PATH_NEAR_DEGENERATE (a decision in the oracle's
+1e-10 band, on either side) or LG_PATH_ILL_CONDITIONED (GPU side: the double-float ray's
+rounding bound passed 1e-6, so chaotic amplification may have parted it from the FP64 path),
+and includes every descendant of a flagged decision.  The report counts the pairs excused
+only as ill-conditioned separately (`flagged_ill`).
 """
 from __future__ import annotations
 
@@ -21,6 +24,7 @@ import numpy as np
 ENDPOINT_TOL = 1e-5
 COLOR_TOL = 1e-6   # relative: a few f32 ulps from the f64 -> f32 rounding of the reflectance
 NEAR = 1
+ILL = 8  # LG_PATH_ILL_CONDITIONED
 
 
 def _keys(paths: np.ndarray) -> np.ndarray:
@@ -43,6 +47,7 @@ class ParityReport:
     flagged_matched: int = 0
     flagged_hit_mismatch: int = 0
     flagged_max_endpoint_err: float = 0.0
+    flagged_ill: int = 0  # pairs flagged only as ill-conditioned (no decision in a band)
 
     def ok(self) -> bool:
         return (self.gpu_only_unflagged == 0 and self.oracle_only_unflagged == 0 and
@@ -63,8 +68,9 @@ def compare(g_segs, g_paths, o_segs, o_paths, o_s64, primary_filter=None) -> Par
     common = gi.keys() & oi.keys()
     g_only = gi.keys() - oi.keys()
     o_only = oi.keys() - gi.keys()
-    gflag = (g_paths["flags"] & NEAR) != 0
-    oflag = (o_paths["flags"] & NEAR) != 0
+    gflag = (g_paths["flags"] & (NEAR | ILL)) != 0
+    oflag = (o_paths["flags"] & (NEAR | ILL)) != 0
+    g_band = (g_paths["flags"] & NEAR) != 0
     ig = np.array([gi[k] for k in common], dtype=np.int64)
     io = np.array([oi[k] for k in common], dtype=np.int64)
     flagged = gflag[ig] | oflag[io] if len(ig) else np.zeros(0, bool)
@@ -103,9 +109,10 @@ def compare(g_segs, g_paths, o_segs, o_paths, o_s64, primary_filter=None) -> Par
 
     g_only_unf = sum(1 for k in g_only if not excused(k, gflag[gi[k]], oi, oflag))
     o_only_unf = sum(1 for k in o_only if not excused(k, oflag[oi[k]], gi, gflag))
+    ill_only = int((flagged & ~g_band[ig] & ~((o_paths["flags"][io] & NEAR) != 0)).sum()) if len(ig) else 0
     return ParityReport(len(common), len(g_only), len(o_only), g_only_unf, o_only_unf, hit_mm, col_mm, max_err,
                         int(flagged.sum()) + len(g_only) + len(o_only) - g_only_unf - o_only_unf,
-                        int(len(fg)), f_hit, f_err)
+                        int(len(fg)), f_hit, f_err, ill_only)
 
 
 def rel_l2(a: np.ndarray, b: np.ndarray) -> float:
