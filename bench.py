@@ -648,9 +648,17 @@ def main():
     ap.add_argument("--grid-density", type=float, default=0.0, help="culling grid cells per object (0: 2)")
     ap.add_argument("--count-case", action="store_true",
                     help="render one small frame of the workload and print its units of work (for ncu counts)")
+    ap.add_argument("--only", choices=["batch", "serve"], default=None,
+                    help="run only that extra leg and print its JSON (for profiling)")
     args = ap.parse_args()
     if args.count_case:
         count_case(args)
+        return
+    if args.only:
+        import torch
+        torch.cuda.set_device(0)
+        fn = batch_bench if args.only == "batch" else serve_bench
+        print(json.dumps({args.only: fn(0, args)}), flush=True)
         return
     ws, rank, local = dist_setup()
     if args.impl == "reference":
