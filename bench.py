@@ -62,8 +62,8 @@ REF_STRIDE = {"csg": 2048, "mid": 32}
 #   bounce: FP64 thread instructions per ray visit
 #   raster: shared-memory atomic warp instructions per accumulated pixel
 INST_PER_UNIT = {
-    "csg": {"scan": 694.3, "solve": 104.7, "bounce": 70.7, "raster": 0.2804},
-    "mid": {"scan": 968.5, "solve": 92.7, "bounce": 55.0, "raster": 0.3003},
+    "csg": {"scan": 627.2, "solve": 80.2, "bounce": 70.7, "raster": 0.2805},
+    "mid": {"scan": 943.7, "solve": 71.4, "bounce": 55.0, "raster": 0.3005},
 }
 
 
@@ -179,8 +179,10 @@ def aggregate(ws: int, units: int, ms: float, device) -> tuple:
 
 
 def packed_workload(name: str, precision: str, ray_scale: float = 1.0):
-    from light_garden_gb300 import workloads as W
-    if name == "csg":
+    from light_garden_gb300 import abi, workloads as W
+    if name == "plain":  # 1 point light (4096 rays), circle + mirror, 8 bounces, 512x512
+        pk = W.plain_small(accum=abi.LG_ACCUM_FIXED64).packed()
+    elif name == "csg":
         pk = W.csg_scene(total_rays=max(8, int(round((1 << 22) * ray_scale)))).packed()
     else:
         pk = W.mid_scene(rays_per_light=max(1, int(round((1 << 18) * ray_scale)))).packed()
@@ -376,10 +378,13 @@ def batch_bench(local, args, ray_scale=1.0 / 16):
     ctx.batch_upload(scenes)
     out = torch.empty(ctx.batch_pixels() * 4, dtype=torch.int16, device=dev)
     ctx.batch_render_into(out.data_ptr(), out.numel() * 2, True)
-    ms = []
+    ms, stages = [], None
     for _ in range(2):
         st = ctx.batch_render_into(out.data_ptr(), out.numel() * 2, True)
         ms.append(st["total_ms"])
+        if st["total_ms"] == min(ms):
+            stages = {k: st[k] for k in ("trace_ms", "accumulate_ms", "resolve_ms", "segments", "pixels", "ray_visits",
+                                         "primary_rays")}
     ctx.close()
     plain = Context(device=local, culling=CULL[args.culling])
     big = torch.empty(max(pk.params.width * pk.params.height for pk in scenes) * 4, dtype=torch.int16, device=dev)
@@ -415,7 +420,7 @@ def batch_bench(local, args, ray_scale=1.0 / 16):
     ceiling = t_small / t_full if t_full > 0 else None
     return {"workload": BATCH_WORKLOAD + f", rays x {ray_scale:g}", "scenes": n, "batched_scenes_per_s": b,
             "batch_ms": min(ms), "plain_scenes_per_s": n / plain_s, "batched_vs_plain": b / (n / plain_s),
-            "ceiling_vs_plain": ceiling,
+            "ceiling_vs_plain": ceiling, "batch_stages": stages,
             "note": "batched: device time of the batch graph; plain: host wall time of upload + lg_render per scene; "
                     "ceiling: 64 scenes (every 8th) alone, time at these rays over time at full rays x ray scale"}
 
@@ -593,8 +598,18 @@ def run_ours(args, ws, rank, local):
                     "flagged_per_step": {"decision_band": s3["near_degenerate"], "ill_conditioned": s3["ill_conditioned"],
                                          "segments": s3["segments"]}}
 
+        def image_errors():
+            # the other configurations' images against the FP64 raster of the oracle's own trace
+            out = {}
+            for wname, stride in (("plain", 1), ("mid", 64)):
+                spk, segs, paths, o_acc, _, _, _, prim = cpu_sample(wname, stride)
+                out["plain_small" if wname == "plain" else "mid_scene"] = {
+                    "primaries": prim, **sample_parity(spk, stride, segs, paths, o_acc, local)}
+            return out
+
         if name != "mid":
             extra("mid_scene", mid)
+        extra("image_errors", image_errors)
         extra("fast_precision", fast)
         extra("batch", lambda: batch_bench(local, args))
         extra("serve", lambda: serve_bench(local, args))

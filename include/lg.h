@@ -305,9 +305,9 @@ typedef struct lg_device_opts {
                                  LG_ERR_TIMEOUT: 0 = default (2^22); a negative value gives up
                                  at once (exercises the timeout path in tests) */
   int32_t scan_pairs;         /* pair slots per lane of the FP32 nearest-hit scan, 8 or 16; 0 =
-                                 autotune: the first lg_render / lg_batch_render of each scene or
+                                 autotune: the second lg_render / lg_batch_render of each scene or
                                  batch renders with both and keeps the faster (results are
-                                 identical either way) */
+                                 identical either way; a scene rendered once is not tuned) */
 } lg_device_opts;
 
 /* Nearest-hit culling (replaces the reference's approximate tile map, tile_map.rs:18-146).

@@ -1259,9 +1259,10 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
   c->smem_fits = c->obj_smem <= OBJ_SMEM_MAX ? 1 : 0;
   int occ = 0;
   const size_t tsm = c->smem_fits ? c->obj_smem : 0;
-  if (!same_shape) {  // a new scene: its first lg_render times both scan pair-buffer sizes
+  if (!same_shape) {  // a new scene: its second lg_render times both scan pair-buffer sizes
     c->scan_pairs = c->scan_pairs_opt;
     c->scan_tune = c->scan_pairs_opt == 0;
+    c->renders = 0;
   }
   if ((st = scan_grid(c, false))) return st;
   if ((st = trace_grids(c, false, tsm))) return st;
@@ -1536,13 +1537,15 @@ static lg_status render_streaming(lg_ctx* c, uint16_t* dst, size_t pitch, int32_
 
 static lg_status render_frame(lg_ctx* c, uint16_t* dst, size_t pitch, int32_t dst_is_device, lg_trace_stats* stats);
 
-// The first frame of a scene (unless lg_device_opts.scan_pairs fixes it) renders with each
-// scan pair-buffer size and keeps the one whose scan kernels ran faster; the frames are
-// identical, so the caller's image is simply the last one.
+// The second frame of a scene (unless lg_device_opts.scan_pairs fixes the size) renders with
+// each scan pair-buffer size and keeps the one whose scan kernels ran faster; the frames are
+// identical, so the caller's image is simply the last one.  A scene rendered once keeps the
+// default (8 slots with a culling grid, 16 without) and pays no tuning.
 lg_status lg_render(lg_ctx* c, uint16_t* dst, size_t pitch, int32_t dst_is_device, lg_trace_stats* stats) {
   lg_status st = need_scene(c);
   if (st) return st;
-  if (c->scan_tune) {
+  if (c->renders < 0xffffffffu) ++c->renders;
+  if (c->scan_tune && c->renders >= 2) {
     c->scan_tune = false;
     float best = INFINITY;
     int pick = scan_pairs_of(c);

@@ -347,8 +347,9 @@ lg_status lg_batch_upload(lg_ctx* c, const lg_scene_desc* scenes, uint32_t k) {
   if ((st = batch_buffers(c))) return st;
   // launch shapes: the multi-scene kernels read the object tables from global memory
   int occ = 0;
-  c->scan_pairs = c->scan_pairs_opt;  // a new batch: its first lg_batch_render times both scan sizes
+  c->scan_pairs = c->scan_pairs_opt;  // a new batch: its second lg_batch_render times both scan sizes
   c->scan_tune = c->scan_pairs_opt == 0;
+  c->renders = 0;
   if ((st = scan_grid(c, true))) return st;
   if ((st = trace_grids(c, true, 0))) return st;
   const int mode = raster_mode(c->prm);
@@ -395,9 +396,10 @@ lg_status lg_batch_render(lg_ctx* c, uint16_t* dst, uint64_t dst_bytes, int32_t 
   std::vector<cudaEvent_t>& ev = c->bev;
   uint32_t retries = 0;
   lg_status st;
-  if (c->scan_tune) {
-    // autotune of the scan's pair slots per lane: the whole batch with each size (identical
-    // images), keep the one whose generations trace faster
+  if (c->renders < 0xffffffffu) ++c->renders;
+  if (c->scan_tune && c->renders >= 2) {
+    // autotune of the scan's pair slots per lane on the batch's second render: the whole
+    // batch with each size (identical images), keep the one whose generations trace faster
     c->scan_tune = false;
     float best = INFINITY;
     int pick = scan_pairs_of(c);

@@ -62,7 +62,9 @@ struct lg_ctx {
   int raster_variant = 0;  // 1 shared-atomic tile raster, 2 warp-private tile raster; 0 = not tuned yet
   int scan_pairs = 0;      // pair slots per lane of the scan (8 / 16; 0: by the culling grid)
   int scan_pairs_opt = 0;  // lg_device_opts.scan_pairs (0: tune on a scene's first render)
-  bool scan_tune = false;  // the next lg_render / lg_batch_render times both sizes first
+  bool scan_tune = false;  // armed by a new scene: its second lg_render (lg_batch_render) times
+                           // both sizes first; a scene rendered once is never tuned
+  uint32_t renders = 0;    // lg_render / lg_batch_render calls since the scene or batch changed
   size_t obj_smem = 0;
   int smem_fits = 0;
   // graph
