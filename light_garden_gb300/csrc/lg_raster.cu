@@ -461,32 +461,18 @@ constexpr int TILE_PX = TILE * TILE;  // cells per channel plane
 // 32 lanes own 32 columns; y-major units index [col][row] and their lanes own 32 rows.
 // Either way one warp's 32 accesses fall in 32 distinct banks.
 //
-// Fixed-point sums are exact in two native 32-bit shared planes per channel.
-//
-// Carry planes (LG_RASTER_CARRY, the default): a term q = h * 2^32 + l (l its low 32 bits,
-// unsigned; h = q >> 32) adds l to the low plane with an atomic that returns the old value;
-// the add wrapped iff the new value is below the old one, and then h + 1 (else h, when
-// nonzero) goes to the high plane.  At the end the high plane holds sum(h) + carries and the
-// low plane sum(l) mod 2^32, so H * 2^32 + L is the int64 sum.  A colour term below 1.0 has
-// h = 0 and costs one atomic per channel, plus one for the rare carry (about 4.4 per pixel
-// against 8 for split planes).  A unit holds at most SPLIT_UNIT_REFS = 16384 segments and a
-// segment adds at most once to a pixel, so with |q| < 2^48 the high plane stays within 2^31.
-//
-// Split planes (LG_RASTER_CARRY=0): |q| < 2^34 is split as q = b * 2^17 + c with an unsigned
-// 17-bit c and a signed b; both plane sums stay within 2^31 and B * 2^17 + C is exact; every
-// channel costs two atomics.
-//
-// Either way a segment with a larger term (up to the clamp, 2^52) skips the tile and adds its
-// 64-bit terms to the image with global atomics, which is just as exact.
-#ifndef LG_RASTER_CARRY
-#define LG_RASTER_CARRY 1
-#endif
-constexpr int SPLIT_BITS = LG_RASTER_CARRY ? 32 : 17;    // low plane: q mod 2^SPLIT_BITS
-constexpr int SPLIT_LIMIT = LG_RASTER_CARRY ? 48 : 34;   // |q| < 2^SPLIT_LIMIT takes the planes
-static_assert(LG_RASTER_CARRY ? ((1ll << (SPLIT_LIMIT - 32)) + 1) * SPLIT_UNIT_REFS <= (1ll << 31)
-                              : (1ll << (SPLIT_LIMIT - SPLIT_BITS)) * SPLIT_UNIT_REFS <= (1ll << 31) &&
-                                    (1ll << SPLIT_BITS) * SPLIT_UNIT_REFS <= (1ll << 31),
-              "plane sums must fit 32 bits");
+// Fixed-point sums use exact split accumulation in native 32-bit shared atomics: a
+// contribution |q| < 2^34 (a colour term below 4) is split as q = b * 2^17 + c with an
+// unsigned 17-bit c and a signed b (|b| <= 2^17).  A unit holds at most SPLIT_UNIT_REFS =
+// 16384 segments and a segment adds at most once to a pixel, so both plane sums stay within
+// 2^31 and B * 2^17 + C is exact.  (Sixteen times fewer units than 1024-segment units with
+// a 21-bit split: each unit ends with a flush of its 32 KB tile by global atomics.)  A
+// segment with a larger term (up to the clamp, 2^52) skips the tile and adds its 64-bit
+// terms to the image with global atomics, which is just as exact.
+constexpr int SPLIT_BITS = 17;   // c = q mod 2^17
+constexpr int SPLIT_LIMIT = 34;  // |q| < 2^34 takes the split planes
+static_assert((1ll << (SPLIT_LIMIT - SPLIT_BITS)) * SPLIT_UNIT_REFS <= (1ll << 31) &&
+                  (1ll << SPLIT_BITS) * SPLIT_UNIT_REFS <= (1ll << 31), "split plane sums must fit 32 bits");
 enum RasterMode { RM_FIXED_SPLIT = 0, RM_FIXED_MINMAX = 1, RM_F32 = 2 };
 
 template <int MODE>
@@ -592,13 +578,8 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs A) {
 #pragma unroll
             for (int ch = 0; ch < 4; ++ch) {
               const long long q = qv[ch];
-              if (LG_RASTER_CARRY || big) {  // (low 32 bits, high 32 bits)
-                st.q[2 * ch] = (unsigned)(q & 0xffffffffll);
-                st.q[2 * ch + 1] = (unsigned)(q >> 32);
-              } else {
-                st.q[2 * ch] = (unsigned)(q & ((1ll << SPLIT_BITS) - 1));
-                st.q[2 * ch + 1] = (unsigned)(int)(q >> SPLIT_BITS);
-              }
+              st.q[2 * ch] = big ? (unsigned)(q & 0xffffffffll) : (unsigned)(q & ((1ll << SPLIT_BITS) - 1));
+              st.q[2 * ch + 1] = big ? (unsigned)(q >> 32) : (unsigned)(int)(q >> SPLIT_BITS);
             }
             if (big) st.span |= SPAN_BIG;
           }
@@ -637,16 +618,6 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs A) {
             for (int ch = 0; ch < 4; ++ch) {
               const unsigned long long q = ((unsigned long long)qs[2 * ch + 1] << 32) | qs[2 * ch];
               if (q) atomicAdd(g + ch, q);
-            }
-          } else if (LG_RASTER_CARRY) {
-            unsigned old[4];
-#pragma unroll
-            for (int ch = 0; ch < 4; ++ch) old[ch] = qs[2 * ch] ? atomicAdd(acc32 + 2 * ch * TILE_PX + cell, qs[2 * ch]) : 0u;
-#pragma unroll
-            for (int ch = 0; ch < 4; ++ch) {
-              const unsigned lo = qs[2 * ch];
-              const unsigned h = qs[2 * ch + 1] + ((lo && old[ch] + lo < old[ch]) ? 1u : 0u);  // carry out of the low plane
-              if (h) atomicAdd(acc32 + (2 * ch + 1) * TILE_PX + cell, h);
             }
           } else {
 #pragma unroll
@@ -697,7 +668,7 @@ __global__ void __launch_bounds__(256, 4) k_raster(RasterArgs A) {
         const int op = B.op[ch];
         if (MODE == RM_FIXED_SPLIT) {
           const unsigned* base = acc32 + 2 * ch * TILE_PX + cell;
-          const long long q = (long long)(int)base[TILE_PX] * (1ll << SPLIT_BITS) + (long long)base[0];  // base[0] unsigned
+          const long long q = (long long)(int)base[TILE_PX] * (1ll << SPLIT_BITS) + (long long)base[0];
           if (q == 0) continue;
           atomicAdd(reinterpret_cast<unsigned long long*>(A.accum) + px + ch, (unsigned long long)q);
         } else if (MODE == RM_FIXED_MINMAX) {
