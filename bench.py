@@ -63,7 +63,7 @@ REF_STRIDE = {"csg": 2048, "mid": 32}
 #   raster: shared-memory atomic warp instructions per accumulated pixel
 INST_PER_UNIT = {
     "csg": {"scan": 627.2, "solve": 80.2, "bounce": 70.7, "raster": 0.2805},
-    "mid": {"scan": 943.7, "solve": 71.4, "bounce": 55.0, "raster": 0.3005},
+    "mid": {"scan": 951.0, "solve": 71.4, "bounce": 55.0, "raster": 0.3005},
 }
 
 
@@ -425,6 +425,24 @@ def batch_bench(local, args, ray_scale=1.0 / 16):
                     "ceiling: 64 scenes (every 8th) alone, time at these rays over time at full rays x ray scale"}
 
 
+def batch_graph(local, args, ray_scale=1.0 / 16):
+    """The 512-scene batch alone: upload, three lg_batch_render calls, the last one's stages."""
+    import torch
+    from light_garden_gb300 import workloads as W
+    from light_garden_gb300.runtime import Context
+    scenes = [W.scale_rays(w, ray_scale).packed() for w in W.batch_scenes(count=512)]
+    for pk in scenes:
+        pk.params.precision = PRECISION[args.precision]
+    ctx = Context(device=local, culling=CULL[args.culling])
+    ctx.batch_upload(scenes)
+    out = torch.empty(ctx.batch_pixels() * 4, dtype=torch.int16, device=torch.device("cuda", local))
+    for _ in range(3):
+        st = ctx.batch_render_into(out.data_ptr(), out.numel() * 2, True)
+    ctx.close()
+    return {k: st[k] for k in ("total_ms", "trace_ms", "accumulate_ms", "resolve_ms", "segments", "pixels", "ray_visits",
+                               "primary_rays", "fp64_solves", "bound_tests", "object_tests")}
+
+
 def serve_bench(local, args, rate=100.0, count=256, ray_scale=1.0 / 16):
     """Poisson arrivals below the server's capacity: scenes/s and p50/p99 latency of the
     continuous-batching server against the plain path serving the same arrivals in order."""
@@ -663,8 +681,9 @@ def main():
     ap.add_argument("--grid-density", type=float, default=0.0, help="culling grid cells per object (0: 2)")
     ap.add_argument("--count-case", action="store_true",
                     help="render one small frame of the workload and print its units of work (for ncu counts)")
-    ap.add_argument("--only", choices=["batch", "serve"], default=None,
-                    help="run only that extra leg and print its JSON (for profiling)")
+    ap.add_argument("--only", choices=["batch", "serve", "batch-graph"], default=None,
+                    help="run only that extra leg and print its JSON (for profiling); batch-graph: the 512-scene "
+                         "batch at 1/16 of the rays rendered three times, nothing else")
     args = ap.parse_args()
     if args.count_case:
         count_case(args)
@@ -672,7 +691,7 @@ def main():
     if args.only:
         import torch
         torch.cuda.set_device(0)
-        fn = batch_bench if args.only == "batch" else serve_bench
+        fn = {"batch": batch_bench, "serve": serve_bench, "batch-graph": batch_graph}[args.only]
         print(json.dumps({args.only: fn(0, args)}), flush=True)
         return
     ws, rank, local = dist_setup()

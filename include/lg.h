@@ -314,11 +314,15 @@ typedef struct lg_device_opts {
  * The culled search visits objects in ray order through a uniform grid and returns the
  * same hits as the full scan. */
 typedef enum lg_culling {
-  LG_CULL_AUTO = 0,  /* grid for scenes of LG_CULL_AUTO_MIN objects or more */
+  LG_CULL_AUTO = 0,  /* grid for scenes of LG_CULL_AUTO_MIN objects or more; the bounce's medium
+                        test uses it, and the nearest-hit scan walks it from LG_CULL_WALK_MIN
+                        objects (batches: always) or as the scene's second lg_render measured
+                        faster (lg_device_opts.scan_pairs = 0) */
   LG_CULL_OFF = 1,   /* every ray tests every object's bounding circle */
-  LG_CULL_ON = 2     /* grid for every scene */
+  LG_CULL_ON = 2     /* grid for every scene, walked by the scan */
 } lg_culling;
-#define LG_CULL_AUTO_MIN 96
+#define LG_CULL_AUTO_MIN 16
+#define LG_CULL_WALK_MIN 96
 
 typedef struct lg_ctx lg_ctx;
 

@@ -102,6 +102,8 @@ pub const LG_SRC_STRING_MOD: u32 = 2;
 pub const LG_CULL_AUTO: i32 = 0;
 pub const LG_CULL_OFF: i32 = 1;
 pub const LG_CULL_ON: i32 = 2;
+pub const LG_CULL_AUTO_MIN: u32 = 16;
+pub const LG_CULL_WALK_MIN: u32 = 96;
 
 #[repr(C)]
 pub struct lg_ctx {

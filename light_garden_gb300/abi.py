@@ -131,7 +131,8 @@ class lg_device_opts(C.Structure):
 LG_ABI_VERSION = 4  # include/lg.h
 LG_CULL_AUTO, LG_CULL_OFF, LG_CULL_ON = 0, 1, 2
 LG_PRECISION_EXACT, LG_PRECISION_FAST = 0, 1
-LG_CULL_AUTO_MIN = 96
+LG_CULL_AUTO_MIN = 16
+LG_CULL_WALK_MIN = 96
 
 
 # numpy dtypes with the same layout, for bulk conversion of downloads

@@ -723,7 +723,7 @@ TraceKernel scan_kernel(bool multi, bool culled, bool exact, int pairs) {
 
 // The scan's pair slots per lane: the tuned or requested value, else 8 with a culling grid
 // and 16 without.
-int scan_pairs_of(const lg_ctx* c) { return c->scan_pairs ? c->scan_pairs : (c->culled ? 8 : 16); }
+int scan_pairs_of(const lg_ctx* c) { return c->scan_pairs ? c->scan_pairs : (c->scan_walk ? 8 : 16); }
 
 // Occupancy-sized grid of the scan for the context's mode and pair slots.
 lg_status scan_grid(lg_ctx* c, bool multi) {
@@ -733,14 +733,14 @@ lg_status scan_grid(lg_ctx* c, bool multi) {
   if (multi) {
     // serving: the requests' precision is not known yet, the grid fits either kernel
     int occ_x = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, scan_kernel(true, c->culled, c->serve ? false : exact, pairs),
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, scan_kernel(true, c->scan_walk, c->serve ? false : exact, pairs),
                                                      SCAN_THREADS, (size_t)scan_smem_bytes(pairs)), "occupancy");
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_x, scan_kernel(true, c->culled, c->serve ? true : exact, pairs),
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_x, scan_kernel(true, c->scan_walk, c->serve ? true : exact, pairs),
                                                      SCAN_THREADS, (size_t)scan_smem_bytes(pairs)), "occupancy");
     c->batch_grid_scan = c->n_sm * std::max(1, std::min(occ, occ_x));
   } else {
     const size_t tsm = c->smem_fits ? c->obj_smem : 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, scan_kernel(false, c->culled, exact, pairs), SCAN_THREADS,
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, scan_kernel(false, c->scan_walk, exact, pairs), SCAN_THREADS,
                                                      (size_t)scan_smem_bytes(pairs) + tsm), "occupancy");
     c->trace_grid[0] = c->n_sm * std::max(1, occ);
   }
@@ -800,7 +800,7 @@ void launch_generation(lg_ctx* c, const SceneDev& S, const TraceBufs& B, uint32_
                        size_t scan_smem, size_t tsm, int smem_fits) {
   const bool exact = c->prm.precision == LG_PRECISION_EXACT;
   kernel_event(c, g, 0);
-  scan_kernel(multi, c->culled, exact, scan_pairs_of(c))<<<scan_grid, SCAN_THREADS, scan_smem, c->stream>>>(S, B, g,
+  scan_kernel(multi, c->scan_walk, exact, scan_pairs_of(c))<<<scan_grid, SCAN_THREADS, scan_smem, c->stream>>>(S, B, g,
                                                                                                    smem_fits);
   kernel_event(c, g, 1);
   if (exact) {
@@ -1241,6 +1241,14 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
     c->culled = F.grid.rec.nx > 0;
     c->graph_valid = false;
   }
+  // a new scene's scan walks the grid from LG_CULL_WALK_MIN objects until the autotuner measures
+  // it (the bounce's medium test takes the grid whenever there is one); the same scene again keeps
+  // what was tuned
+  const bool walk = c->culled && (n_objects >= LG_CULL_WALK_MIN || c->culling == LG_CULL_ON);
+  if ((!same_shape || !c->culled) && c->scan_walk != walk) {
+    c->scan_walk = walk;
+    c->graph_valid = false;
+  }
   c->n_obj = n_objects;
   c->n_leaves = (uint32_t)F.leaves.size();
   c->n_prog = (uint32_t)F.prog.size();
@@ -1546,16 +1554,22 @@ lg_status lg_render(lg_ctx* c, uint16_t* dst, size_t pitch, int32_t dst_is_devic
   if (st) return st;
   if (c->renders < 0xffffffffu) ++c->renders;
   if (c->scan_tune && c->renders >= 2) {
+    // with a culling grid: the grid walk with 8 pair slots against the table scan with 16; without
+    // one: the table scan with 8 against 16
     c->scan_tune = false;
     float best = INFINITY;
     int pick = scan_pairs_of(c);
-    for (int pairs : {8, 16}) {
-      if ((st = set_scan_pairs(c, pairs, false))) return st;
+    bool pick_walk = c->scan_walk;
+    const int opts[2][2] = {{c->culled ? 1 : 0, 8}, {0, 16}};
+    for (const auto& o : opts) {
+      c->scan_walk = o[0] != 0;
+      if ((st = set_scan_pairs(c, o[1], false))) return st;
       lg_trace_stats s;
       if ((st = render_frame(c, dst, pitch, dst_is_device, &s))) return st;
-      const float ms = s.scan_ms > 0.0f ? s.scan_ms : s.total_ms;
-      if (ms < best) { best = ms; pick = pairs; }
+      const float ms = s.trace_ms > 0.0f ? s.trace_ms : s.total_ms;  // the walk also moves work to the solve
+      if (ms < best) { best = ms; pick = o[1]; pick_walk = o[0] != 0; }
     }
+    c->scan_walk = pick_walk;
     if ((st = set_scan_pairs(c, pick, false))) return st;
   }
   return render_frame(c, dst, pitch, dst_is_device, stats);

@@ -310,6 +310,7 @@ lg_status lg_batch_upload(lg_ctx* c, const lg_scene_desc* scenes, uint32_t k) {
   if ((st = upload_grids(c, grids))) return st;
   c->culled = false;
   for (const GridRec& g : grids.recs) c->culled = c->culled || g.nx > 0;
+  c->scan_walk = c->culled;  // scenes without a grid take the table scan inside the walking kernel
   if ((st = ensure(c, c->d_scene_count, (size_t)k * 4, "scene counts"))) return st;
   if ((st = ensure(c, c->d_scene_off, (size_t)k * 4, "scene offsets"))) return st;
   CK(cudaStreamSynchronize(c->stream), "upload");

@@ -87,6 +87,7 @@ struct lg_ctx {
   float grid_density = 0.0f;
   int32_t wait_polls = 1 << 22;  // bounded device waits (lg_device_opts.wait_polls)
   bool culled = false;  // the uploaded scene (or some scene of the batch) has a grid
+  bool scan_walk = false;  // the nearest-hit scan walks the grid (else it scans the object table)
   uint64_t total_px = 0;
   uint32_t total_bins = 0;
   uint32_t max_bounce_all = 0;

@@ -879,9 +879,12 @@ __device__ __forceinline__ int cubic_roots32(const float* A, const float* Bp, fl
     if (fabsf(fp) < 1e-3f * sc) { unknown = true; return 0; }
     const float bx = ((c3x * u + c2x) * u + c1x) * u + c0x, by = ((c3y * u + c2y) * u + c1y) * u + c0y;
     const float dbx = (3.0f * c3x * u + 2.0f * c2x) * u + c1x, dby = (3.0f * c3y * u + 2.0f * c2y) * u + c1y;
-    t[n] = ((bx - ox) * dx + (by - oy) * dy) / dd;
-    sv[n] = u;
-    cert[n] = u > 1e-4f && u < 1.0f - 1e-4f;
+    // constant indices only, so that t, sv and cert stay in registers (n <= 2 here)
+    const float tn = ((bx - ox) * dx + (by - oy) * dy) / dd;
+    const bool cn = u > 1e-4f && u < 1.0f - 1e-4f;
+    if (n == 0) { t[0] = tn; sv[0] = u; cert[0] = cn; }
+    else if (n == 1) { t[1] = tn; sv[1] = u; cert[1] = cn; }
+    else { t[2] = tn; sv[2] = u; cert[2] = cn; }
     const float tl = fabsf(dbx * dx + dby * dy) * (err / fabsf(fp) + 1e-6f) +
                      2e-6f * (fabsf(bx) + fabsf(by) + fabsf(ox) + fabsf(oy)) + 1e-6f;
     tol = fmaxf(tol, tl);
@@ -996,8 +999,8 @@ __device__ __noinline__ Class32 classify32(const ObjScan& r, float ox, float oy,
   for (int side = 0; side < nleaf; ++side) {
     const float* L = side == 0 ? r.a : r.b;
     const uint32_t kind = side == 0 ? info_leaf_a(r.info) : info_leaf_b(r.info);
-    float t[3];
-    bool cert[3];
+    float t[3] = {0.0f, 0.0f, 0.0f};
+    bool cert[3] = {false, false, false};
     int face[3];
     float sv[3];
     float tol = 1e-5f;
@@ -1007,31 +1010,44 @@ __device__ __noinline__ Class32 classify32(const ObjScan& r, float ox, float oy,
       c.key = fminf(c.key, fmaxf(lb, 0.0f));
       continue;
     }
+    // the root at the surface the ray leaves (source leaf) is skipped; the arrays are only
+    // read at constant indices, so they stay in registers
+    int skip = -1;
     if (side == src_leaf && n > 0) {
       int ks = 0;
-      for (int k = 1; k < n; ++k)
-        if (fabsf(t[k]) < fabsf(t[ks])) ks = k;
+      float tks = t[0];
+      bool cks = cert[0];
+#pragma unroll
+      for (int k = 1; k < 3; ++k)
+        if (k < n && fabsf(t[k]) < fabsf(tks)) { ks = k; tks = t[k]; cks = cert[k]; }
       bool other_near = false;
-      for (int k = 0; k < n; ++k)
-        if (k != ks && fabsf(t[k]) < 4.0f * TAU32) other_near = true;
-      if (fabsf(t[ks]) < TAU32 && cert[ks] && !other_near) {
-        for (int k = ks; k + 1 < n; ++k) { t[k] = t[k + 1]; cert[k] = cert[k + 1]; face[k] = face[k + 1]; sv[k] = sv[k + 1]; }
-        n -= 1;
-      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        if (k < n && k != ks && fabsf(t[k]) < 4.0f * TAU32) other_near = true;
+      if (fabsf(tks) < TAU32 && cks && !other_near) skip = ks;
     }
+    // the roots move through three registers (no dynamically indexed array)
+    float ta = t[0], tb = t[1], tc = t[2], sa = sv[0], sb = sv[1], sc2 = sv[2];
+    bool ca = cert[0], cb = cert[1], cc = cert[2];
+    int fa = face[0], fb = face[1], fc = face[2];
     for (int k = 0; k < n; ++k) {
-      bool certain = cert[k];
+      const float tk = ta, svk = sa;
+      const bool ck = ca;
+      const int fk = fa;
+      ta = tb; tb = tc; sa = sb; sb = sc2; ca = cb; cb = cc; fa = fb; fb = fc;
+      if (k == skip) continue;
+      bool certain = ck;
       if (nleaf == 2 && certain) {
         // CSG filter at a well-located hit point; an uncertain root stays a candidate
-        if (t[k] < -TAU32) continue;
-        const float px = ox + dx * t[k], py = oy + dy * t[k];
+        if (tk < -TAU32) continue;
+        const float px = ox + dx * tk, py = oy + dy * tk;
         const float* Lo = side == 0 ? r.b : r.a;
         const uint32_t ko = side == 0 ? info_leaf_b(r.info) : info_leaf_a(r.info);
         const int m = leaf_member32(ko, Lo, px, py, 4.0f * tol);
         if (m < 0) certain = false;
         else if (!op_keep(info_op(r.info), side == 0, m == 1)) continue;
       }
-      root32(t[k], tol, c, certain, side, face[k], sv[k]);
+      root32(tk, tol, c, certain, side, fk, svk);
     }
   }
   return c;

@@ -373,6 +373,7 @@ lg_status lg_serve_begin(lg_ctx* c, const lg_serve_opts* opts) {
   if (!V) return LG_ERR_OUT_OF_MEMORY;
   c->serve = V;
   c->culled = true;  // requests come and go: the scan takes each scene's grid or full scan as it finds it
+  c->scan_walk = true;
   V->max_slots = opts->max_slots;
   V->budget = budget;
   V->slots.assign(V->max_slots, Slot());
