@@ -62,8 +62,8 @@ REF_STRIDE = {"csg": 2048, "mid": 32}
 #   bounce: FP64 thread instructions per ray visit
 #   raster: shared-memory atomic warp instructions per accumulated pixel
 INST_PER_UNIT = {
-    "csg": {"scan": 627.2, "solve": 80.2, "bounce": 70.7, "raster": 0.2805},
-    "mid": {"scan": 951.0, "solve": 71.4, "bounce": 55.0, "raster": 0.3005},
+    "csg": {"scan": 631.1, "solve": 80.2, "bounce": 70.7, "raster": 0.2805},
+    "mid": {"scan": 952.3, "solve": 71.4, "bounce": 55.0, "raster": 0.3005},
 }
 
 
@@ -363,10 +363,11 @@ def rooflines(name, st, avg, peaks, hbm):
     return r
 
 
-def batch_bench(local, args, ray_scale=1.0 / 16):
+def batch_bench(local, args, ray_scale=None):
     """512 mixed scenes: one multi-scene trace (lg_batch_render) against the plain path
     (lg_render of each scene in turn), at a fraction of the rays."""
     import torch
+    ray_scale = args.batch_scale if ray_scale is None else ray_scale
     from light_garden_gb300 import workloads as W
     from light_garden_gb300.runtime import Context
     dev = torch.device("cuda", local)
@@ -406,7 +407,8 @@ def batch_bench(local, args, ray_scale=1.0 / 16):
         pk_f.params.precision = PRECISION[args.precision]
         for pk, acc in ((pk_s, "s"), (pk_f, "f")):  # same canvases: `big` holds either
             plain.upload(pk)
-            plain.render_into(big.data_ptr(), pk.params.width * 8, True)  # warm (graph capture)
+            for _ in range(2):  # graph capture, then the scan autotune of the scene's second render
+                plain.render_into(big.data_ptr(), pk.params.width * 8, True)
             torch.cuda.synchronize()
             a = time.perf_counter()
             plain.render_into(big.data_ptr(), pk.params.width * 8, True)
@@ -425,9 +427,10 @@ def batch_bench(local, args, ray_scale=1.0 / 16):
                     "ceiling: 64 scenes (every 8th) alone, time at these rays over time at full rays x ray scale"}
 
 
-def batch_graph(local, args, ray_scale=1.0 / 16):
+def batch_graph(local, args, ray_scale=None):
     """The 512-scene batch alone: upload, three lg_batch_render calls, the last one's stages."""
     import torch
+    ray_scale = args.batch_scale if ray_scale is None else ray_scale
     from light_garden_gb300 import workloads as W
     from light_garden_gb300.runtime import Context
     scenes = [W.scale_rays(w, ray_scale).packed() for w in W.batch_scenes(count=512)]
@@ -632,9 +635,13 @@ def run_ours(args, ws, rank, local):
         extra("batch", lambda: batch_bench(local, args))
         extra("serve", lambda: serve_bench(local, args))
 
-    launches = 1 + 3 * pk.params.max_bounce + 1 + 1  # light setup, 3 trace kernels per generation, overlay, resolve
-    if st.get("tile_refs", 0):
-        launches += 8 * pk.params.max_bounce  # streaming accumulation per generation (decide, clear, count, scan, units, scatter, raster, rotate)
+    # light setup, 3 trace kernels per generation, overlay, accumulation clear, resolve, string-mod lines
+    G = pk.params.max_bounce
+    launches = 1 + 3 * G + 1 + 1 + 1 + (1 if pk.params.string_mod.modulo else 0)
+    if st["segments"] > (1 << 28):  # the frame streams: per generation decide, clear, count, scan, units, scatter, raster, rotate
+        launches += 8 * G
+    else:  # one accumulation: count, tile scan, units, scatter, raster
+        launches += 5
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": "segments/s", "n_gpus": ws, "steps": args.steps,
@@ -681,6 +688,8 @@ def main():
     ap.add_argument("--grid-density", type=float, default=0.0, help="culling grid cells per object (0: 2)")
     ap.add_argument("--count-case", action="store_true",
                     help="render one small frame of the workload and print its units of work (for ncu counts)")
+    ap.add_argument("--batch-scale", type=float, default=1.0 / 16,
+                    help="ray-count scale of the batch legs' scenes (default 1/16)")
     ap.add_argument("--only", choices=["batch", "serve", "batch-graph"], default=None,
                     help="run only that extra leg and print its JSON (for profiling); batch-graph: the 512-scene "
                          "batch at 1/16 of the rays rendered three times, nothing else")
