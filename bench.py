@@ -62,8 +62,8 @@ REF_STRIDE = {"csg": 2048, "mid": 32}
 #   bounce: FP64 thread instructions per ray visit
 #   raster: shared-memory atomic warp instructions per accumulated pixel
 INST_PER_UNIT = {
-    "csg": {"scan": 631.1, "solve": 80.2, "bounce": 70.7, "raster": 0.2805},
-    "mid": {"scan": 952.3, "solve": 71.4, "bounce": 55.0, "raster": 0.3005},
+    "csg": {"scan": 631.1, "solve": 80.2, "bounce": 71.7, "raster": 0.2805},
+    "mid": {"scan": 952.3, "solve": 67.4, "bounce": 55.9, "raster": 0.3005},
 }
 
 

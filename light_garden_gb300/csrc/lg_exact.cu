@@ -15,10 +15,10 @@
 
 // CTAs per SM the exact kernels' registers are sized for (build-time, for sweeps)
 #ifndef LG_SOLVE_X_BLOCKS
-#define LG_SOLVE_X_BLOCKS 2
+#define LG_SOLVE_X_BLOCKS 3
 #endif
 #ifndef LG_BOUNCE_X_BLOCKS
-#define LG_BOUNCE_X_BLOCKS 3
+#define LG_BOUNCE_X_BLOCKS 4
 #endif
 
 namespace lgd {
@@ -114,13 +114,14 @@ static __device__ __noinline__ double obj_best_x(const SceneDev& S, uint32_t k, 
 }
 
 // The FP64 hit of one leaf at the root the FP32 scan proved (t32; face32: the rect face as
-// 2 axis + (outward sign > 0)): the very operations of leaf_hits for that root only.  A
-// circle computes the quotient of its proved root (q / a or c / q, told apart by their FP32
-// values) and not the other; a rect computes the slab quotient of its proved face and not the
-// other three.  Other leaves take leaf_hits and the root nearest t32.  False: no such hit
-// (the caller solves the object whole).
+// 2 axis + (outward sign > 0); s32: a cubic's curve parameter): the very operations of
+// leaf_hits for that root only.  A circle computes the quotient of its proved root (q / a or
+// c / q, told apart by their FP32 values) and not the other; a rect computes the slab quotient
+// of its proved face and not the other three; a cubic searches only the bracket that holds
+// s32.  Other leaves take leaf_hits and the root nearest t32.  False: no such hit (the caller
+// solves the object whole).
 __device__ __forceinline__ bool leaf_proved_hit(const lg_geo* G, const lg_geo& g, V o, V d, float t32, int face32,
-                                                double& ev, lgx::Hit& out) {
+                                                float s32, double& ev, lgx::Hit& out) {
   using namespace lgx;
   if (g.kind == LG_GEO_CIRCLE) {
     const V oc = vsub(o, mk(g.origin[0], g.origin[1]));
@@ -152,6 +153,45 @@ __device__ __forceinline__ bool leaf_proved_hit(const lg_geo* G, const lg_geo& g
     out = mkhit(t, o, d, mk(0.0, 0.0), ax + (pos ? 2 : 0));
     return true;
   }
+  if (g.kind == LG_GEO_CUBIC && s32 > 0.0f) {
+    // the bracket between the derivative's roots that holds the proved curve parameter s32:
+    // hits_cubic's operations for that bracket only (a parameter within 1e-4 of a knot, or
+    // a knot or bracket end that is itself a root, takes the whole leaf below)
+    const Cubic k = cubic_of(g.v);
+    const double a[4] = {cross(d, vsub(k.c0, o)), cross(d, k.c1), cross(d, k.c2), cross(d, k.c3)};
+    double kn[4];
+    int nk = 0;
+    kn[nk++] = 0.0;
+    const double qa = mul(3.0, a[3]), qb = mul(2.0, a[2]), qc = a[1];
+    if (qa != 0.0) {
+      const double disc = sub(mul(qb, qb), mul(mul(4.0, qa), qc));
+      if (disc >= 0.0) {
+        const double sq = sqr(disc);
+        const double q = mul(-0.5, add(qb, qb >= 0 ? sq : -sq));
+        double r1 = dvd(q, qa), r2 = q != 0.0 ? dvd(qc, q) : r1;
+        if (r1 > r2) { const double x = r1; r1 = r2; r2 = x; }
+        if (r1 > 0.0 && r1 < 1.0) kn[nk++] = r1;
+        if (r2 > 0.0 && r2 < 1.0 && (nk == 1 || r2 != kn[1])) kn[nk++] = r2;
+      }
+    } else if (qb != 0.0) {
+      const double r = dvd(-qc, qb);
+      if (r > 0.0 && r < 1.0) kn[nk++] = r;
+    }
+    kn[nk++] = 1.0;
+    double lo = -1.0, hi = -1.0;
+    for (int i = 0; i + 1 < nk; ++i)
+      if ((double)s32 > kn[i] + 1e-4 && (double)s32 < kn[i + 1] - 1e-4) { lo = kn[i]; hi = kn[i + 1]; }
+    if (lo >= 0.0) {
+      const double flo = poly3(a, lo), fhi = poly3(a, hi);
+      if (!is_zero(flo) && !is_zero(fhi) && is_neg(flo) != is_neg(fhi)) {
+        const double sr = cubic_root(a, lo, hi, flo);
+        const double t = dvd(dot(vsub(cubic_point(k, sr), o), d), dot(d, d));
+        if (!gt_pos(t, T_MIN)) return false;
+        out = mkhit(t, o, d, mk(sr, 0.0), 0);
+        return true;
+      }
+    }
+  }
   double near = INFINITY;
   bool found = false;
   leaf_hits(G, g, o, d, ev, [&](const Hit& h) {
@@ -172,11 +212,11 @@ __device__ __forceinline__ bool leaf_proved_hit(const lg_geo* G, const lg_geo& g
 // and the membership tests cannot change which hit object_hits keeps, so the result is the
 // same bits.
 static __device__ __noinline__ bool solve_proved_x(const SceneDev& S, const ObjInfo& oi, V o, V d, int side, int face,
-                                                   float t32, double& ev, lgx::Hit& out) {
+                                                   float t32, float s32, double& ev, lgx::Hit& out) {
   const lgx::XNode* nd = S.xnode + oi.xnode_begin;
   const lg_geo& L = S.xgeo[nd[0].geo];
   if (oi.xnode_count == 1) {
-    if (side != 0 || !leaf_proved_hit(S.xgeo, L, o, d, t32, face, ev, out)) return false;
+    if (side != 0 || !leaf_proved_hit(S.xgeo, L, o, d, t32, face, s32, ev, out)) return false;
     out.node = 0;
     return true;
   }
@@ -185,7 +225,7 @@ static __device__ __noinline__ bool solve_proved_x(const SceneDev& S, const ObjI
   const V lo = lgx::irot(lgx::vsub(o, org), L.rot[0], L.rot[1]);
   const V ld = lgx::irot(d, L.rot[0], L.rot[1]);
   const int li = 1 + side;
-  if (!leaf_proved_hit(S.xgeo, S.xgeo[nd[li].geo], lo, ld, t32, face, ev, out)) return false;
+  if (!leaf_proved_hit(S.xgeo, S.xgeo[nd[li].geo], lo, ld, t32, face, 0.0f, ev, out)) return false;
   out.node = li;
   out.p = lgx::vadd(org, lgx::rot(out.p, L.rot[0], L.rot[1]));
   return true;
@@ -248,8 +288,9 @@ __global__ void __launch_bounds__(256, LG_SOLVE_X_BLOCKS) k_solve_x(SceneDev S, 
     uint32_t pcls = 7u;
     if (valid && i < off[LIST_FULL] && !sc.overflow && sc.nc == 1 && (sc.leaf == 0 || sc.leaf == 1))
       pcls = solve_class(__ldg(&S.scan[sl.base + sc.cand[0]].info));
-    if (pcls == 0u || pcls == 1u || pcls == 4u) {
-      proved = solve_proved_x(S, S.info[sl.base + sc.cand[0]], o, d, sc.leaf, sc.face, sc.t32, ev, bh);
+    // class 3 holds single cubic leaves and deep CSG trees; only a cubic reaches a refine list
+    if (pcls == 0u || pcls == 1u || pcls == 4u || (pcls == 3u && sc.leaf == 0)) {
+      proved = solve_proved_x(S, S.info[sl.base + sc.cand[0]], o, d, sc.leaf, sc.face, sc.t32, sc.s32, ev, bh);
       if (proved) {
         best = sc.cand[0];
         ++my_solves;

@@ -223,7 +223,7 @@ __device__ __forceinline__ void emit_segments(const SceneDev& S, const TraceBufs
 // scan, 16 slots 1469; mid frame: 16 slots 68 ms, 8 slots 73).  CTAs per SM of the culled scan
 // are build-time (-DLG_SCAN_CULL_BLOCKS=..., for sweeps).
 #ifndef LG_SCAN_CULL_BLOCKS
-#define LG_SCAN_CULL_BLOCKS 3
+#define LG_SCAN_CULL_BLOCKS 4
 #endif
 constexpr int SCAN_WARPS = 4;
 constexpr int WALK_STEPS = 32;  // culled scan: cell steps and object tests between classifications
