@@ -15,7 +15,7 @@
 
 // CTAs per SM the exact kernels' registers are sized for (build-time, for sweeps)
 #ifndef LG_SOLVE_X_BLOCKS
-#define LG_SOLVE_X_BLOCKS 3
+#define LG_SOLVE_X_BLOCKS 4
 #endif
 #ifndef LG_BOUNCE_X_BLOCKS
 #define LG_BOUNCE_X_BLOCKS 4

@@ -221,12 +221,16 @@ __device__ __forceinline__ void emit_segments(const SceneDev& S, const TraceBufs
 // the culled walk tends to do best with 8 (a smaller shared-memory buffer leaves more of the
 // SM's L1 to the grid and queue loads), the table scan with 16 (CSG frame: 8 slots 1217 ms of
 // scan, 16 slots 1469; mid frame: 16 slots 68 ms, 8 slots 73).  CTAs per SM of the culled scan
-// are build-time (-DLG_SCAN_CULL_BLOCKS=..., for sweeps).
+// and its walk steps between classifications are build-time (-DLG_SCAN_CULL_BLOCKS=...,
+// -DLG_SCAN_WALK_STEPS=..., for sweeps).
 #ifndef LG_SCAN_CULL_BLOCKS
 #define LG_SCAN_CULL_BLOCKS 4
 #endif
+#ifndef LG_SCAN_WALK_STEPS
+#define LG_SCAN_WALK_STEPS 32
+#endif
 constexpr int SCAN_WARPS = 4;
-constexpr int WALK_STEPS = 32;  // culled scan: cell steps and object tests between classifications
+constexpr int WALK_STEPS = LG_SCAN_WALK_STEPS;  // culled scan: cell steps and object tests between classifications
 constexpr int SCAN_CULL_BLOCKS = LG_SCAN_CULL_BLOCKS;  // culled scan: CTAs per SM the registers are sized for
 
 struct __align__(16) PairSlot {

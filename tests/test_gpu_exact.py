@@ -118,6 +118,34 @@ def test_shapes_and_nested_csg_exact(ctx, oracle):
     _trace_exact(ctx, oracle, pack(objs, lights, p), image=True)
 
 
+def test_cubic_mirrors_exact(ctx, oracle):
+    """24 seeded cubic-Bezier mirrors (every third an S-curve that a line can cross three
+    times) around a glass disc, 32,000 rays, 16 bounces: the cubic hits whose root the FP32
+    scan proved are solved in their own bracket alone, and must still equal the oracle's
+    full three-bracket solve bit for bit."""
+    rng = np.random.default_rng(1234)
+    objs = []
+    for k in range(24):
+        c = rng.uniform(-0.8, 0.8, 2)
+        r = rng.uniform(0.08, 0.25)
+        a = rng.uniform(0, 2 * np.pi)
+        u = np.array([np.cos(a), np.sin(a)])
+        n = np.array([-u[1], u[0]])
+        if k % 3 == 0:
+            h = r * 1.5
+            pts = [c - r * u - h * n, c - r / 3 * u + 3 * h * n, c + r / 3 * u - 3 * h * n, c + r * u + h * n]
+        else:
+            pts = [c + r * rng.uniform(-1, 1, 2) for _ in range(4)]
+        objs.append(Object.new_curved_mirror(CubicBezier(tuple(tuple(map(float, q)) for q in pts))))
+    objs.append(Object(abi.LG_OBJ_GEO, Circle((0.05, -0.1), 0.12), Material(1.5)))
+    lights = [PointLight((0.0, 0.0), 20000, (1.0, 0.9, 0.7, 1.0)),
+              SpotLight((-0.95, 0.9), 0.9, (1.0, -0.8), 12000, (0.4, 0.8, 1.0, 1.0))]
+    p = abi.params_default()
+    p.width, p.height, p.max_bounce = 1024, 1024, 16
+    st, rep = _trace_exact(ctx, oracle, pack(objs, lights, p), image=True)
+    assert rep.segments > 900_000
+
+
 def test_default_scene_from_ron_exact(ctx, oracle):
     from pathlib import Path
     from light_garden_gb300 import ron
