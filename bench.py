@@ -65,6 +65,12 @@ INST_PER_UNIT = {
     "csg": {"scan": 631.1, "solve": 80.2, "bounce": 71.7, "raster": 0.2805},
     "mid": {"scan": 952.3, "solve": 67.4, "bounce": 55.9, "raster": 0.3005},
 }
+# Warp instructions issued (smsp__inst_executed.sum) per unit of the same frames: the trace
+# stages against the SM's issue ceiling (4 schedulers x 1 warp instruction per cycle per SM).
+WARP_INST_PER_UNIT = {
+    "csg": {"scan": 323.2, "solve": 52.0, "bounce": 75.2},
+    "mid": {"scan": 270.3, "solve": 66.2, "bounce": 49.8},
+}
 
 
 def measured_hbm():
@@ -331,8 +337,21 @@ def frame_bench(pk, local, steps, warmup, args, clocks=True):
     return ctx, st, avg, (sampler.summary() if sampler else None)
 
 
-def rooflines(name, st, avg, peaks, hbm):
-    """Each kernel stage against the ceiling of the resource it uses (exact mode)."""
+def issue_ceiling(local, clk):
+    """Warp instructions per second the GPU can issue: SMs x 4 schedulers x the median SM clock
+    sampled during the timed region (or the maximum clock when unsampled)."""
+    import torch
+    mhz = (clk or {}).get("sm_mhz") or (clk or {}).get("sm_max_mhz")
+    if not mhz:
+        return None
+    n_sm = torch.cuda.get_device_properties(local).multi_processor_count
+    return n_sm * 4 * mhz * 1e6, f"{n_sm} SMs x 4 schedulers x {mhz:g} MHz (sampled)"
+
+
+def rooflines(name, st, avg, peaks, hbm, issue=None):
+    """Each kernel stage against the ceiling of the resource it uses (exact mode); with
+    ``issue`` = (warp instructions per second the SMs can issue, how it was found), the trace
+    stages also carry their share of the issue slots."""
     ipu = INST_PER_UNIT[name]
     vis, solves, px = st["ray_visits"], st["fp64_solves"], st["pixels"]
     r = {}
@@ -352,6 +371,15 @@ def rooflines(name, st, avg, peaks, hbm):
     r["bounce"] = entry("k_bounce_x (exact FP64 bounce and canvas exit)", "fp64_pipe", ipu["bounce"] * vis,
                         avg["bounce_ms"], peaks["fp64_op_per_s"], "G FP64 inst/s",
                         f"{ipu['bounce']} FP64 instructions per ray visit (ncu count) x {vis} visits")
+    if issue and issue[0]:
+        wpu = WARP_INST_PER_UNIT[name]
+        for stage, units, uname in (("scan", vis, "ray visit"), ("solve", solves, "object solve"),
+                                    ("bounce", vis, "ray visit")):
+            ms = avg[stage + "_ms"]
+            achieved = wpu[stage] * units / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
+            r[stage]["issue"] = {"achieved": achieved, "peak": issue[0] / 1e9, "unit": "G warp inst/s",
+                                 "frac": achieved / (issue[0] / 1e9),
+                                 "note": f"{wpu[stage]} warp instructions per {uname} (ncu count); peak {issue[1]}"}
     ra = entry("k_raster (tile accumulation in shared memory)", "smem_atomics", ipu["raster"] * 32 * px,
                avg["raster_ms"], peaks["smem_atomics_per_s"], "G shared atomics/s",
                f"{ipu['raster'] * 32:.2f} shared-memory atomic lane operations per pixel (ncu count) x {px} pixels")
@@ -575,7 +603,8 @@ def run_ours(args, ws, rank, local):
     ctx.close()
     del flush
 
-    roof = rooflines(name, st, avg, peaks, hbm) if args.precision == "exact" else {}
+    issue = issue_ceiling(local, clk)
+    roof = rooflines(name, st, avg, peaks, hbm, issue) if args.precision == "exact" else {}
     dominant = max(roof.values(), key=lambda e: e["ms"]) if roof else None
 
     cpu = None
@@ -607,7 +636,7 @@ def run_ours(args, ws, rank, local):
                  "ms_per_step": a2["total_ms"], "px_per_s": s2["pixels"] / (a2["total_ms"] * 1e-3),
                  "segments_per_step": s2["segments"], "pixels_per_step": s2["pixels"], "stage_ms": a2}
             if args.precision == "exact":
-                d["rooflines"] = rooflines("mid", s2, a2, peaks, hbm)
+                d["rooflines"] = rooflines("mid", s2, a2, peaks, hbm, issue)
             return d
 
         def fast():
