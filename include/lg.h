@@ -46,8 +46,9 @@ extern "C" {
  * 4: lg_string_mod gained the curve parameters and the modulo-colour table (lg_params
  *    grew); string-mod lines are lg_chord records (lg_chords_download), no longer
  *    segments; lg_device_opts.scan_pairs (was padding); LG_PATH_ILL_CONDITIONED split from
- *    LG_PATH_NEAR_DEGENERATE, lg_trace_stats.ill_conditioned (grew). */
-#define LG_ABI_VERSION 4
+ *    LG_PATH_NEAR_DEGENERATE, lg_trace_stats.ill_conditioned (grew).
+ * 5: lg_string_mod.nested (lg_string_mod and lg_params grew). */
+#define LG_ABI_VERSION 5
 
 typedef enum lg_status {
   LG_OK = 0,
@@ -178,6 +179,18 @@ typedef struct lg_mod_color {
   float color[4];
 } lg_mod_color;
 
+/* StringMod::nested (string_mod.rs:14, 87-102, 152-158).  When `nested` is not NULL the
+ * lines drawn are the nested mod's, and its points are the crossings of this mod's m lines:
+ * for diff = 1 .. m-1, for a = 0 .. m-1, the crossing of line a with line (a + diff) % m,
+ * if they cross, in that order (so every crossing appears twice).  Two lines cross when the
+ * 2x2 parametric solve of the segments, in FP64 with each operation rounded on its own, has
+ * a non-zero determinant and both parameters in [0, 1]; the point is a + t (b - a) on the
+ * first.  Nested line k joins crossing k % n and crossing ix(k) % n of the nested mode,
+ * with the nested mod's colours; no crossings, no lines.  The nested mod's curve, turns,
+ * curve parameters and its own `nested` are not used.  This mod's modulo is then at most
+ * LG_STRING_MOD_NESTED_MAX. */
+#define LG_STRING_MOD_NESTED_MAX 4096u
+
 typedef struct lg_string_mod {
   uint64_t modulo;  /* number of points m; 0 disables the overlay */
   uint64_t num;
@@ -190,6 +203,8 @@ typedef struct lg_string_mod {
   uint32_t n_colors;    /* entries of `colors` (StringMod::modulo_colors), 0..4096 */
   uint32_t _pad;
   const lg_mod_color* colors; /* host array, copied by lg_scene_upload (not kept) */
+  const struct lg_string_mod* nested; /* NULL, or the mod drawn between this one's line
+                                         crossings; copied by lg_scene_upload (not kept) */
 } lg_string_mod;
 
 /* ---- trace precision ----------------------------------------------------------------- *
@@ -377,7 +392,8 @@ lg_status lg_segments_download(lg_ctx* ctx, lg_segment* out, lg_path_record* pat
 lg_status lg_accum_download(lg_ctx* ctx, void* out, uint64_t cap_bytes);
 
 /* Copies the string-mod lines of the last lg_trace / lg_render (lg_params.string_mod.modulo
- * of them; none in a sampled frame with ray_offset != 0, or after lg_accumulate_segments).
+ * of them, or with a nested mod its modulo, or none when the lines do not cross; none in a
+ * sampled frame with ray_offset != 0, or after lg_accumulate_segments).
  * *n_out receives the count; LG_ERR_TRUNCATED when cap is smaller.  lg_accumulate draws
  * them together with the segments. */
 lg_status lg_chords_download(lg_ctx* ctx, lg_chord* out, uint64_t cap, uint64_t* n_out);

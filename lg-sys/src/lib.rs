@@ -1,5 +1,5 @@
 //! Raw bindings to `liblightgarden_cuda.so`, the GB300 trace-and-accumulate path of
-//! light_garden (`include/lg.h`, C ABI version 4).
+//! light_garden (`include/lg.h`, C ABI version 5).
 //!
 //! The reference crate calls this in place of `Tracer::trace_all` (src/light_garden/tracer.rs:276)
 //! and the wgpu line pass (src/sub_render_pass.rs:43-101): flatten the objects and lights into
@@ -12,7 +12,7 @@
 
 use core::ffi::{c_char, c_void};
 
-pub const LG_ABI_VERSION: u32 = 4;
+pub const LG_ABI_VERSION: u32 = 5;
 
 pub type lg_status = i32;
 pub const LG_OK: lg_status = 0;
@@ -86,6 +86,7 @@ pub const LG_CURVE_CIRCLE: u32 = 0;
 pub const LG_CURVE_COMPLEX_EXP: u32 = 1;
 pub const LG_CURVE_HYPOTROCHOID: u32 = 2;
 pub const LG_CURVE_LISSAJOUS: u32 = 3;
+pub const LG_STRING_MOD_NESTED_MAX: u32 = 4096;
 // lg_precision
 pub const LG_PRECISION_EXACT: i32 = 0;
 pub const LG_PRECISION_FAST: i32 = 1;
@@ -175,6 +176,8 @@ pub struct lg_string_mod {
     pub n_colors: u32,
     pub _pad: u32,
     pub colors: *const lg_mod_color,
+    /// StringMod::nested: NULL, or the mod drawn between the crossings of this one's lines.
+    pub nested: *const lg_string_mod,
 }
 
 #[repr(C)]

@@ -74,12 +74,14 @@ class lg_mod_color(C.Structure):
 
 
 class lg_string_mod(C.Structure):
-    # ``colors`` is a C pointer (const lg_mod_color*); it is declared as an integer address so
-    # that parameter blocks stay copyable, and set through set_mod_colors().
+    # ``colors`` (const lg_mod_color*) and ``nested`` (const lg_string_mod*) are C pointers;
+    # they are declared as integer addresses so that parameter blocks stay copyable, and set
+    # through set_mod_colors() and set_nested().
     _fields_ = [("modulo", C.c_uint64), ("num", C.c_uint64), ("turns", C.c_uint64),
                 ("mode", C.c_uint32), ("curve", C.c_uint32), ("color", C.c_float * 4),
                 ("curve_f", C.c_double * 2), ("curve_u", C.c_uint64 * 3),
-                ("n_colors", C.c_uint32), ("_pad", C.c_uint32), ("colors", C.c_uint64)]
+                ("n_colors", C.c_uint32), ("_pad", C.c_uint32), ("colors", C.c_uint64),
+                ("nested", C.c_uint64)]
 
 
 class lg_params(C.Structure):
@@ -128,7 +130,8 @@ class lg_device_opts(C.Structure):
                 ("grid_density", C.c_float), ("wait_polls", C.c_int32), ("scan_pairs", C.c_int32)]
 
 
-LG_ABI_VERSION = 4  # include/lg.h
+LG_ABI_VERSION = 5  # include/lg.h
+LG_STRING_MOD_NESTED_MAX = 4096  # include/lg.h
 LG_CULL_AUTO, LG_CULL_OFF, LG_CULL_ON = 0, 1, 2
 LG_PRECISION_EXACT, LG_PRECISION_FAST = 0, 1
 LG_CULL_AUTO_MIN = 16
@@ -164,6 +167,19 @@ def set_mod_colors(params: "lg_params", entries) -> None:
         e.color[:] = tuple(float(x) for x in col)
     _mod_color_tables.append(arr)
     sm.n_colors, sm.colors = len(entries), C.addressof(arr)
+
+
+def set_nested(params: "lg_params", nested: "lg_string_mod | None") -> None:
+    """StringMod::nested: the mod drawn between the crossings of params.string_mod's lines
+    (a copy of ``nested`` is kept alive and handed to the library by address; None clears)."""
+    if nested is None:
+        params.string_mod.nested = 0
+        return
+    keep = lg_string_mod()
+    C.memmove(C.addressof(keep), C.addressof(nested), C.sizeof(lg_string_mod))
+    keep.nested = 0
+    _mod_color_tables.append(keep)
+    params.string_mod.nested = C.addressof(keep)
 
 
 def path_dtype():

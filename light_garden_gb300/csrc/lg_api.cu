@@ -479,6 +479,18 @@ lg_status validate_params(std::string& err, const lg_params& p) {
     if (sm.n_colors && !sm.colors) return set_err(err, LG_ERR_INVALID_ARGUMENT, "string mod: null modulo colours");
     for (uint32_t k = 0; k < sm.n_colors; ++k)
       if (sm.colors[k].modulo == 0) return set_err(err, LG_ERR_INVALID_ARGUMENT, "string mod: modulo colour with modulo 0");
+    if (sm.nested) {
+      const lg_string_mod& ns = *sm.nested;
+      if (sm.modulo > LG_STRING_MOD_NESTED_MAX)
+        return set_err(err, LG_ERR_UNSUPPORTED, "string mod: a nested mod needs modulo <= LG_STRING_MOD_NESTED_MAX");
+      if (ns.mode > LG_SM_BASE) return set_err(err, LG_ERR_INVALID_ARGUMENT, "nested string mod: unknown mode");
+      if (ns.modulo > (1ull << 26)) return set_err(err, LG_ERR_INVALID_ARGUMENT, "nested string mod: modulo above 2^26");
+      if (ns.n_colors > 4096) return set_err(err, LG_ERR_INVALID_ARGUMENT, "nested string mod: more than 4096 modulo colours");
+      if (ns.n_colors && !ns.colors) return set_err(err, LG_ERR_INVALID_ARGUMENT, "nested string mod: null modulo colours");
+      for (uint32_t k = 0; k < ns.n_colors; ++k)
+        if (ns.colors[k].modulo == 0)
+          return set_err(err, LG_ERR_INVALID_ARGUMENT, "nested string mod: modulo colour with modulo 0");
+    }
   }
   if (p.precision != LG_PRECISION_EXACT && p.precision != LG_PRECISION_FAST)
     return set_err(err, LG_ERR_INVALID_ARGUMENT, "unknown precision");
@@ -495,6 +507,7 @@ uint64_t overlay_segments(const lg_ctx* c) {
 }
 uint64_t string_mod_lines(const lg_ctx* c) {
   if (c->prm.ray_stride > 1 && c->prm.ray_offset != 0) return 0;
+  if (c->has_nested) return c->n_cross ? c->nested.modulo : 0;  // no crossings, no lines
   return c->prm.string_mod.modulo;
 }
 
@@ -864,12 +877,14 @@ void launch_overlay(lg_ctx* c, const SceneDev& S, const TraceBufs& B) {
   const uint64_t n_ov = overlay_segments(c), n_sm = string_mod_lines(c);
   c->chords_ready = n_sm;
   if (!n_ov && !n_sm) return;
-  lg_string_mod sm = c->prm.string_mod;
+  lg_string_mod sm = c->has_nested ? c->nested : c->prm.string_mod;
   sm.modulo = n_sm;
   ChordArgs CA;
   CA.out = (lg_chord*)c->d_chords.p;
   CA.colors = (const lg_mod_color*)c->d_mod_colors.p;
   CA.n_colors = sm.n_colors;
+  CA.pts = c->has_nested ? (const double2*)c->d_cross.p : nullptr;
+  CA.n_pts = c->n_cross;
   const int blocks = (int)std::min<uint64_t>((n_ov + n_sm + 255) / 256, 4096);
   k_overlay<<<blocks, 256, 0, c->stream>>>(S, B, (const uint32_t*)c->d_cubics.p, nullptr,
                                            c->prm.emit_control_lines ? c->n_cubic : 0, sm, CA);
@@ -883,6 +898,39 @@ void launch_chords(lg_ctx* c, const RasterArgs& A) {
     k_raster_chords<true><<<blocks, 256, 0, c->stream>>>(A, (const lg_chord*)c->d_chords.p, c->chords_ready);
   else
     k_raster_chords<false><<<blocks, 256, 0, c->stream>>>(A, (const lg_chord*)c->d_chords.p, c->chords_ready);
+}
+
+// The crossing points of a string mod's lines, for its nested mod (StringMod::
+// line_crossings_as_points, string_mod.rs:87-102), computed once per upload: the lines, the
+// crossings per block of (diff, line) pairs, their scan, then the points in pair order.
+lg_status upload_crossings(lg_ctx* c, const lg_string_mod& outer) {
+  const uint64_t m = outer.modulo;
+  c->n_cross = 0;
+  if (m < 2) return LG_OK;
+  lg_string_mod sm = outer;
+  sm.colors = nullptr;
+  sm.nested = nullptr;
+  const uint64_t n_pairs = m * (m - 1);
+  const uint32_t n_blk = (uint32_t)((n_pairs + CROSS_PAIRS_PER_BLOCK - 1) / CROSS_PAIRS_PER_BLOCK);
+  lg_status st;
+  if ((st = ensure(c, c->d_sm_lines, 2 * m * sizeof(double2), "string-mod crossings"))) return st;
+  if ((st = ensure(c, c->d_cross_blk, (size_t)n_blk * 4 + 16, "string-mod crossings"))) return st;
+  double2* lines = (double2*)c->d_sm_lines.p;
+  uint32_t* blk = (uint32_t*)c->d_cross_blk.p;
+  unsigned long long* d_total = (unsigned long long*)((char*)c->d_cross_blk.p + (((size_t)n_blk * 4 + 7) & ~(size_t)7));
+  k_sm_lines<<<(int)((m + 255) / 256), 256, 0, c->stream>>>(sm, lines);
+  k_cross_count<<<n_blk, CROSS_THREADS, 0, c->stream>>>(lines, m, blk);
+  k_cross_scan<<<1, 1024, 0, c->stream>>>(blk, n_blk, d_total);
+  unsigned long long total = 0;
+  CK(cudaMemcpyAsync(&total, d_total, sizeof total, cudaMemcpyDeviceToHost, c->stream), "string-mod crossings");
+  CK(cudaStreamSynchronize(c->stream), "string-mod crossings");
+  if (total) {
+    if ((st = ensure(c, c->d_cross, total * sizeof(double2), "string-mod crossings"))) return st;
+    k_cross_write<<<n_blk, CROSS_THREADS, 0, c->stream>>>(lines, m, blk, (double2*)c->d_cross.p);
+    CK(cudaGetLastError(), "string-mod crossings");
+  }
+  c->n_cross = total;
+  return LG_OK;
 }
 
 lg_status enqueue_trace(lg_ctx* c) {
@@ -1193,19 +1241,36 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
   if ((st = validate_exact(c->err, p, F))) return st;
   CK(cudaStreamSynchronize(c->stream), "synchronize");
   if ((st = upload_exact(c, F))) return st;
-  lg_params pk = p;  // kept without the caller's colour-table pointer
+  lg_params pk = p;  // kept without the caller's colour-table and nested-mod pointers
   pk.string_mod.colors = nullptr;
+  pk.string_mod.nested = nullptr;
+  const bool nested = p.string_mod.modulo && p.string_mod.nested;
+  lg_string_mod nk{};  // the nested mod, kept without its pointers
+  if (nested) {
+    nk = *p.string_mod.nested;
+    nk.colors = nullptr;
+    nk.nested = nullptr;
+  }
   const bool same_shape = c->has_scene && c->n_obj == n_objects && c->n_leaves == F.leaves.size() &&
                           c->n_prog == F.prog.size() && c->n_lights == n_lights && c->n_cubic == F.cubics.size() &&
-                          std::memcmp(&c->prm, &pk, sizeof pk) == 0;
+                          std::memcmp(&c->prm, &pk, sizeof pk) == 0 && c->has_nested == nested &&
+                          std::memcmp(&c->nested, &nk, sizeof nk) == 0;
   if (p.string_mod.modulo) {
-    if ((st = ensure(c, c->d_chords, p.string_mod.modulo * sizeof(lg_chord), "string-mod lines"))) return st;
-    if ((st = ensure(c, c->d_mod_colors, (size_t)std::max<uint32_t>(p.string_mod.n_colors, 1) * sizeof(lg_mod_color),
+    // the mod drawn: the nested one (between the crossings of this mod's lines), else this one
+    const lg_string_mod& drawn = nested ? *p.string_mod.nested : p.string_mod;
+    if ((st = ensure(c, c->d_chords, std::max<uint64_t>(drawn.modulo, 1) * sizeof(lg_chord), "string-mod lines")))
+      return st;
+    if ((st = ensure(c, c->d_mod_colors, (size_t)std::max<uint32_t>(drawn.n_colors, 1) * sizeof(lg_mod_color),
                      "string-mod colours"))) return st;
-    if (p.string_mod.n_colors)
-      CK(cudaMemcpyAsync(c->d_mod_colors.p, p.string_mod.colors, p.string_mod.n_colors * sizeof(lg_mod_color),
+    if (drawn.n_colors)
+      CK(cudaMemcpyAsync(c->d_mod_colors.p, drawn.colors, drawn.n_colors * sizeof(lg_mod_color),
                          cudaMemcpyHostToDevice, c->stream), "upload");
   }
+  c->has_nested = false;  // set again below once the crossings are in place
+  c->n_cross = 0;
+  if (nested && (st = upload_crossings(c, p.string_mod))) return st;
+  c->has_nested = nested;
+  c->nested = nk;
   if ((st = ensure(c, c->d_scan, F.scan.size() * sizeof(ObjScan), "scene"))) return st;
   if ((st = ensure(c, c->d_info, F.info.size() * sizeof(ObjInfo), "scene"))) return st;
   std::vector<Leaf64> dleaves;

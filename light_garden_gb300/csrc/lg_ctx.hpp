@@ -34,9 +34,15 @@ struct lg_ctx {
   // scene
   DevBuf d_scan, d_info, d_leaves, d_prog, d_lights, d_cubics;
   DevBuf d_xgeo, d_xnode;  // exact mode: geometry nodes and per-object preorder trees
-  DevBuf d_mod_colors;     // string mod: the modulo-colour table (lg_string_mod.colors)
+  DevBuf d_mod_colors;     // string mod: the modulo-colour table of the mod drawn (the nested one if any)
   DevBuf d_chords;         // string mod: the frame's lines (lg_string_mod.modulo of them)
   uint64_t chords_ready = 0;  // lines the last trace left in d_chords (0: none to draw)
+  // nested string mod: its parameters (pointers cleared), the crossing points of the outer
+  // mod's lines (double2, computed at upload) and their count
+  bool has_nested = false;
+  lg_string_mod nested{};
+  DevBuf d_sm_lines, d_cross_blk, d_cross;
+  uint64_t n_cross = 0;
   uint32_t n_obj = 0, n_leaves = 0, n_prog = 0, n_lights = 0, n_cubic = 0;
   uint64_t n_primary = 0;
   lg_params prm{};

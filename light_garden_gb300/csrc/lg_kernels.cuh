@@ -79,7 +79,19 @@ struct ChordArgs {
   lg_chord* out;
   const lg_mod_color* colors;
   uint32_t n_colors;
+  const double2* pts;  // nested mod: its points (the outer mod's line crossings), else null
+  uint64_t n_pts;
 };
+// Crossings of a string mod's lines (lg_string_mod.nested): the lines' endpoints, then the
+// (diff, line) pairs in blocks of CROSS_PAIRS_PER_BLOCK: counts per block, their exclusive
+// scan (one CTA), and the crossing points written in pair order.
+constexpr int CROSS_THREADS = 256;
+constexpr int CROSS_PER_THREAD = 16;
+constexpr uint64_t CROSS_PAIRS_PER_BLOCK = (uint64_t)CROSS_THREADS * CROSS_PER_THREAD;
+__global__ void k_sm_lines(lg_string_mod sm, double2* lines);
+__global__ void k_cross_count(const double2* lines, uint64_t m, uint32_t* blk);
+__global__ void k_cross_scan(uint32_t* blk, uint32_t n_blk, unsigned long long* total);
+__global__ void k_cross_write(const double2* lines, uint64_t m, const uint32_t* blk_off, double2* pts);
 __global__ void k_overlay(SceneDev S, TraceBufs B, const uint32_t* cubic_objs, const uint16_t* cubic_scene,
                           uint32_t n_cubic, lg_string_mod sm, ChordArgs CA);
 __global__ void k_scene_hist(SceneDev S, TraceBufs B, uint32_t gen, unsigned* count);

@@ -1169,6 +1169,21 @@ __device__ void string_mod_point(const lg_string_mod& sm, uint64_t n, double& x,
   }
 }
 
+// The point that line iix of a string mod joins to point iix, by the mod's mode
+// (string_mod.rs:110-115; u64 arithmetic wrapping like Rust's release build).
+__device__ __forceinline__ uint64_t string_mod_target(const lg_string_mod& sm, uint64_t iix) {
+  const uint64_t m = sm.modulo;
+  if (sm.mode == LG_SM_ADD) return (iix + sm.num) % m;
+  if (sm.mode == LG_SM_MUL) return (iix * sm.num) % m;
+  uint64_t b = sm.mode == LG_SM_POW ? iix : sm.num, e = sm.mode == LG_SM_POW ? (uint32_t)sm.num : (uint32_t)iix, p = 1;
+  while (e) {
+    if (e & 1) p *= b;
+    b *= b;
+    e >>= 1;
+  }
+  return p % m;
+}
+
 // StringMod::get_color (string_mod.rs:124-150): the f32 mean of the matching modulo colours,
 // summed in table order, else the base colour.
 __device__ void string_mod_color(const lg_string_mod& sm, const lg_mod_color* colors, uint32_t n_colors,
@@ -1217,23 +1232,145 @@ __global__ void k_overlay(SceneDev S, TraceBufs B, const uint32_t* cubic_objs, c
       }
     } else {
       const uint64_t m = sm.modulo, iix = i - n_ctrl;
-      uint64_t ix;
-      if (sm.mode == LG_SM_ADD) ix = (iix + sm.num) % m;
-      else if (sm.mode == LG_SM_MUL) ix = (iix * sm.num) % m;
-      else {
-        uint64_t b = sm.mode == LG_SM_POW ? iix : sm.num, e = sm.mode == LG_SM_POW ? (uint32_t)sm.num : (uint32_t)iix, p = 1;
-        while (e) { if (e & 1) p *= b; b *= b; e >>= 1; }
-        ix = p % m;
-      }
+      const uint64_t ix = string_mod_target(sm, iix);
       double xa, ya, xb, yb;
-      string_mod_point(sm, iix % m, xa, ya);
-      string_mod_point(sm, ix % m, xb, yb);
+      if (CA.pts) {  // nested: points iix and ix of the outer mod's crossings (string_mod.rs:116-117)
+        const double2 pa = CA.pts[iix % CA.n_pts], pb = CA.pts[ix % CA.n_pts];
+        xa = pa.x; ya = pa.y; xb = pb.x; yb = pb.y;
+      } else {
+        string_mod_point(sm, iix % m, xa, ya);
+        string_mod_point(sm, ix % m, xb, yb);
+      }
       lg_chord c;
       c.x0 = (float)xa; c.y0 = (float)ya; c.x1 = (float)xb; c.y1 = (float)yb;
       string_mod_color(sm, CA.colors, CA.n_colors, iix, c.color0);
       string_mod_color(sm, CA.colors, CA.n_colors, ix, c.color1);
       if (CA.out) CA.out[iix] = c;
     }
+  }
+}
+
+// ---------------------------------------------------------- nested string mods
+// StringMod::line_crossings_as_points (string_mod.rs:87-102): line k of the outer mod joins
+// point k and point ix(k) of its curve, in FP64 (lines[2k], lines[2k + 1]).
+__global__ void k_sm_lines(lg_string_mod sm, double2* lines) {
+  const uint64_t m = sm.modulo;
+  for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < m; k += (uint64_t)gridDim.x * blockDim.x) {
+    double x, y;
+    string_mod_point(sm, k % m, x, y);
+    lines[2 * k] = make_double2(x, y);
+    string_mod_point(sm, string_mod_target(sm, k) % m, x, y);
+    lines[2 * k + 1] = make_double2(x, y);
+  }
+}
+
+// Crossing of segments ab and cd (collision2d's LineSegment::intersect is not vendored; this
+// is the definition include/lg.h states): the 2x2 parametric solve a + t (b - a) =
+// c + u (d - c), each FP64 operation rounded on its own, a crossing when the determinant is
+// not zero and t, u lie in [0, 1]; the point is a + t (b - a).
+__device__ __forceinline__ bool seg_cross_x(double2 a, double2 b, double2 c, double2 d, double2& p) {
+  using namespace lgx;
+  const double rx = sub(b.x, a.x), ry = sub(b.y, a.y), sx = sub(d.x, c.x), sy = sub(d.y, c.y);
+  const double den = sub(mul(rx, sy), mul(ry, sx));
+  if (den == 0.0) return false;
+  const double wx = sub(c.x, a.x), wy = sub(c.y, a.y);
+  const double t = dvd(sub(mul(wx, sy), mul(wy, sx)), den);
+  const double u = dvd(sub(mul(wx, ry), mul(wy, rx)), den);
+  if (!(t >= 0.0 && t <= 1.0 && u >= 0.0 && u <= 1.0)) return false;
+  p.x = add(a.x, mul(rx, t));
+  p.y = add(a.y, mul(ry, t));
+  return true;
+}
+
+// pair q of m (m - 1), in the reference's order: diff = q / m + 1 (outer loop), line a = q % m
+__device__ __forceinline__ bool pair_cross(const double2* lines, uint64_t m, uint64_t q, double2& p) {
+  const uint64_t diff = q / m + 1, a = q % m, b = (a + diff) % m;
+  return seg_cross_x(lines[2 * a], lines[2 * a + 1], lines[2 * b], lines[2 * b + 1], p);
+}
+
+// A thread's run of CROSS_PER_THREAD consecutive pairs: how many of them cross.
+__device__ __forceinline__ uint32_t run_crossings(const double2* lines, uint64_t m, uint64_t q0, uint64_t n_pairs) {
+  uint32_t c = 0;
+  for (int k = 0; k < CROSS_PER_THREAD; ++k) {
+    double2 p;
+    if (q0 + k < n_pairs && pair_cross(lines, m, q0 + k, p)) ++c;
+  }
+  return c;
+}
+
+// exclusive sum over the CTA's threads (CROSS_THREADS of them); *total receives the sum
+__device__ __forceinline__ uint32_t cta_exclusive(uint32_t v, uint32_t* warp_sums, uint32_t* total) {
+  const unsigned lane = lane_id(), w = threadIdx.x >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if ((int)lane >= o) incl += y;
+  }
+  if (lane == 31) warp_sums[w] = incl;
+  __syncthreads();
+  uint32_t before = 0, all = 0;
+  for (unsigned k = 0; k < CROSS_THREADS / 32; ++k) {
+    if (k < w) before += warp_sums[k];
+    all += warp_sums[k];
+  }
+  if (total) *total = all;
+  return before + incl - v;
+}
+
+__global__ void __launch_bounds__(CROSS_THREADS) k_cross_count(const double2* lines, uint64_t m, uint32_t* blk) {
+  __shared__ uint32_t warp_sums[CROSS_THREADS / 32];
+  const uint64_t n_pairs = m * (m - 1);
+  const uint64_t q0 = blockIdx.x * CROSS_PAIRS_PER_BLOCK + (uint64_t)threadIdx.x * CROSS_PER_THREAD;
+  const uint32_t c = run_crossings(lines, m, q0, n_pairs);
+  uint32_t total = 0;
+  cta_exclusive(c, warp_sums, &total);
+  if (threadIdx.x == 0) blk[blockIdx.x] = total;
+}
+
+// one CTA of 1024 threads: exclusive scan of the per-block counts in place
+__global__ void __launch_bounds__(1024) k_cross_scan(uint32_t* blk, uint32_t n_blk, unsigned long long* total) {
+  __shared__ unsigned long long carry;
+  __shared__ uint32_t warp_sums[32];
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const unsigned lane = lane_id(), w = threadIdx.x >> 5;
+  for (uint32_t base = 0; base < n_blk; base += blockDim.x) {
+    const uint32_t i = base + threadIdx.x;
+    const uint32_t v = i < n_blk ? blk[i] : 0u;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if ((int)lane >= o) incl += y;
+    }
+    if (lane == 31) warp_sums[w] = incl;
+    __syncthreads();
+    uint32_t before = 0, all = 0;
+    for (unsigned k = 0; k < blockDim.x / 32; ++k) {
+      if (k < w) before += warp_sums[k];
+      all += warp_sums[k];
+    }
+    const unsigned long long c0 = carry;
+    if (i < n_blk) blk[i] = (uint32_t)(c0 + before + incl - v);
+    __syncthreads();
+    if (threadIdx.x == 0) carry = c0 + all;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+// the crossing points in pair order: block offset + the thread's place in the block + its run
+__global__ void __launch_bounds__(CROSS_THREADS) k_cross_write(const double2* lines, uint64_t m,
+                                                                const uint32_t* blk_off, double2* pts) {
+  __shared__ uint32_t warp_sums[CROSS_THREADS / 32];
+  const uint64_t n_pairs = m * (m - 1);
+  const uint64_t q0 = blockIdx.x * CROSS_PAIRS_PER_BLOCK + (uint64_t)threadIdx.x * CROSS_PER_THREAD;
+  const uint32_t c = run_crossings(lines, m, q0, n_pairs);
+  uint64_t slot = (uint64_t)blk_off[blockIdx.x] + cta_exclusive(c, warp_sums, nullptr);
+  for (int k = 0; k < CROSS_PER_THREAD; ++k) {
+    double2 p;
+    if (q0 + k < n_pairs && pair_cross(lines, m, q0 + k, p)) pts[slot++] = p;
   }
 }
 

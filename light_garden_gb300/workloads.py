@@ -13,6 +13,7 @@ generators stand in for the configurations:
 * :func:`batch_scenes`  mixed sizes: objects log-uniform [4, 1024], rays log-uniform
                         [2^12, 2^20], bounces U{4..32}, canvases {256, 512, 1024, 2048}^2;
 * :func:`string_mod_art` string-mod line art on each of the four curves, with modulo colours.
+* :func:`nested_string_mod_art` a nested string mod over the crossings of one of those.
 
 Choices the configurations leave open (spot angle U[10, 90] degrees, directional segment
 length U[0.1, 0.5], the curved-mirror template, the CSG child placement) are made here
@@ -170,6 +171,28 @@ def string_mod_art(curve: int = abi.LG_CURVE_CIRCLE, width: int = 1024, height: 
     sm.curve_u[:] = cu
     abi.set_mod_colors(p, table if colors else [])
     return Workload(f"string_mod_art_{curve}", [], [PointLight((0.1, -0.2), 64, (1.0, 1.0, 1.0, 1.0))], p)
+
+
+# nested string-mod art (StringMod::nested, string_mod.rs:152-158): the nested mod's lines join
+# crossings of the outer mod's lines; (nested modulo, num, mode, modulo colours)
+_NESTED_ART = (6000, 17, abi.LG_SM_ADD, [(5, 1, (0.1, 0.8, 1.0, 1.0)), (7, 3, (1.0, 0.5, 0.0, 0.7))])
+
+
+def nested_string_mod_art(curve: int = abi.LG_CURVE_CIRCLE, width: int = 1024, height: int = 1024,
+                          outer_modulo: int = 400) -> Workload:
+    """Nested string-mod art: the outer mod of :func:`string_mod_art` on one curve with
+    ``outer_modulo`` lines (at most 4096), whose crossings are the points of a nested mod."""
+    w = string_mod_art(curve, width, height)
+    w.params.string_mod.modulo = outer_modulo
+    m, num, mode, table = _NESTED_ART
+    ns = abi.lg_string_mod()
+    ns.modulo, ns.num, ns.mode = m, num, mode
+    ns.color[:] = (0.9, 0.9, 0.2, 1.0)
+    holder = abi.params_default()
+    abi.set_mod_colors(holder, table)
+    ns.n_colors, ns.colors = holder.string_mod.n_colors, holder.string_mod.colors
+    abi.set_nested(w.params, ns)
+    return Workload(f"nested_string_mod_art_{curve}", w.objects, w.lights, w.params)
 
 
 def _shape_object(rng, kind: str) -> Object:

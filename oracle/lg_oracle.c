@@ -982,25 +982,113 @@ static void string_mod_color(const lg_string_mod* sm, uint64_t ix, float* out) {
   for (int ch = 0; ch < 4; ++ch) out[ch] = cnt ? acc[ch] / (float)cnt : sm->color[ch];
 }
 
-int lgo_string_mod_chords(const lg_params* prm, lg_chord* out, uint64_t cap, uint64_t* n_out) {
-  if (!prm || !n_out) return LGO_ERR_INVALID;
-  const lg_string_mod* sm = &prm->string_mod;
+/* StringMod::draw_init_points (string_mod.rs:104-122): the point that line iix joins to
+ * point iix, by the mod's mode (u64 arithmetic wrapping like Rust's release build). */
+static uint64_t string_mod_target(const lg_string_mod* sm, uint64_t iix) {
   const uint64_t m = sm->modulo;
-  *n_out = m;
-  if (m == 0) return LGO_OK;
-  if (sm->curve > LG_CURVE_LISSAJOUS || sm->mode > LG_SM_BASE) return LGO_ERR_UNSUPPORTED;
+  switch (sm->mode) {
+    case LG_SM_ADD: return (iix + sm->num) % m;
+    case LG_SM_MUL: return (iix * sm->num) % m;
+    case LG_SM_POW: return wrapping_pow(iix, (uint32_t)sm->num) % m;
+    default: return wrapping_pow(sm->num, (uint32_t)iix) % m;
+  }
+}
+
+static int string_mod_check(const lg_string_mod* sm, int nested) {
+  if ((!nested && sm->curve > LG_CURVE_LISSAJOUS) || sm->mode > LG_SM_BASE) return LGO_ERR_UNSUPPORTED;
   if (sm->n_colors && !sm->colors) return LGO_ERR_INVALID;
   for (uint32_t k = 0; k < sm->n_colors; ++k)
     if (sm->colors[k].modulo == 0) return LGO_ERR_INVALID;
+  return LGO_OK;
+}
+
+/* Crossing of segments ab and cd, the definition the library states for lg_string_mod.nested
+ * (collision2d's LineSegment::intersect is not vendored): the 2x2 parametric solve
+ * a + t (b - a) = c + u (d - c), each FP64 operation rounded on its own; a crossing needs a
+ * non-zero determinant and t, u in [0, 1]. */
+static int seg_cross(double ax, double ay, double bx, double by, double cx, double cy, double dx, double dy,
+                     double* px, double* py) {
+  const double rx = bx - ax, ry = by - ay, sx = dx - cx, sy = dy - cy;
+  const double den = rx * sy - ry * sx;
+  if (den == 0.0) return 0;
+  const double wx = cx - ax, wy = cy - ay;
+  const double t = (wx * sy - wy * sx) / den;
+  const double u = (wx * ry - wy * rx) / den;
+  if (!(t >= 0.0 && t <= 1.0 && u >= 0.0 && u <= 1.0)) return 0;
+  *px = ax + rx * t;
+  *py = ay + ry * t;
+  return 1;
+}
+
+/* StringMod::line_crossings_as_points (string_mod.rs:87-102): the lines of the mod's own
+ * draw, then for diff = 1 .. m-1 and a = 0 .. m-1 the crossing of line a with line
+ * (a + diff) % m.  Writes up to cap points (x, y) to xy; *n_out = all crossings. */
+int lgo_string_mod_crossings(const lg_string_mod* sm, double* xy, uint64_t cap, uint64_t* n_out) {
+  if (!sm || !n_out) return LGO_ERR_INVALID;
+  *n_out = 0;
+  const uint64_t m = sm->modulo;
+  if (m < 2) return LGO_OK;
+  if (m > LG_STRING_MOD_NESTED_MAX) return LGO_ERR_UNSUPPORTED;
+  int rc = string_mod_check(sm, 0);
+  if (rc) return rc;
+  double* L = malloc(4 * m * sizeof(double));
+  if (!L) return LGO_ERR_OOM;
+  for (uint64_t i = 0; i < m; ++i) {
+    string_mod_point(sm, i % m, &L[4 * i], &L[4 * i + 1]);
+    string_mod_point(sm, string_mod_target(sm, i) % m, &L[4 * i + 2], &L[4 * i + 3]);
+  }
+  uint64_t n = 0;
+  for (uint64_t diff = 1; diff < m; ++diff)
+    for (uint64_t a = 0; a < m; ++a) {
+      const double* p = &L[4 * a];
+      const double* q = &L[4 * ((a + diff) % m)];
+      double x, y;
+      if (seg_cross(p[0], p[1], p[2], p[3], q[0], q[1], q[2], q[3], &x, &y)) {
+        if (xy && n < cap) { xy[2 * n] = x; xy[2 * n + 1] = y; }
+        ++n;
+      }
+    }
+  free(L);
+  *n_out = n;
+  return xy && n > cap ? LGO_ERR_TRUNCATED : LGO_OK;
+}
+
+int lgo_string_mod_chords(const lg_params* prm, lg_chord* out, uint64_t cap, uint64_t* n_out) {
+  if (!prm || !n_out) return LGO_ERR_INVALID;
+  const lg_string_mod* sm = &prm->string_mod;
+  *n_out = 0;
+  if (sm->modulo == 0) return LGO_OK;
+  int rc = string_mod_check(sm, 0);
+  if (rc) return rc;
+  if (sm->nested) {  /* StringMod::draw with a nested mod (string_mod.rs:152-155) */
+    const lg_string_mod* ns = sm->nested;
+    if ((rc = string_mod_check(ns, 1))) return rc;
+    uint64_t np = 0;
+    if ((rc = lgo_string_mod_crossings(sm, NULL, 0, &np))) return rc;
+    const uint64_t n = np ? ns->modulo : 0;
+    *n_out = n;
+    if (n == 0) return LGO_OK;
+    if (cap < n) return LGO_ERR_TRUNCATED;
+    double* pts = malloc(2 * np * sizeof(double));
+    if (!pts) return LGO_ERR_OOM;
+    if ((rc = lgo_string_mod_crossings(sm, pts, np, &np))) { free(pts); return rc; }
+    for (uint64_t iix = 0; iix < n; ++iix) {
+      const uint64_t ix = string_mod_target(ns, iix);
+      const double* a = &pts[2 * (iix % np)];
+      const double* b = &pts[2 * (ix % np)];
+      lg_chord* c = &out[iix];
+      c->x0 = (float)a[0]; c->y0 = (float)a[1]; c->x1 = (float)b[0]; c->y1 = (float)b[1];
+      string_mod_color(ns, iix, c->color0);
+      string_mod_color(ns, ix, c->color1);
+    }
+    free(pts);
+    return LGO_OK;
+  }
+  const uint64_t m = sm->modulo;
+  *n_out = m;
   if (cap < m) return LGO_ERR_TRUNCATED;
   for (uint64_t iix = 0; iix < m; ++iix) {
-    uint64_t ix;
-    switch (sm->mode) {
-      case LG_SM_ADD: ix = (iix + sm->num) % m; break;
-      case LG_SM_MUL: ix = (iix * sm->num) % m; break;
-      case LG_SM_POW: ix = wrapping_pow(iix, (uint32_t)sm->num) % m; break;
-      default: ix = wrapping_pow(sm->num, (uint32_t)iix) % m; break;
-    }
+    const uint64_t ix = string_mod_target(sm, iix);
     double xa, ya, xb, yb;
     string_mod_point(sm, iix % m, &xa, &ya);
     string_mod_point(sm, ix % m, &xb, &yb);

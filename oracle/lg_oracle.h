@@ -52,9 +52,14 @@ int lgo_trace(const lg_geo* geos, uint32_t n_geo, const lg_object* objs, uint32_
               lg_segment* segs, lg_path_record* paths, double* seg64, uint64_t cap,
               uint64_t* n_out, lgo_stats* stats);
 
-/* String-mod lines of prm->string_mod (string_mod.rs:33-150): modulo of them, written to
- * out[0..modulo).  *n_out receives the count; LGO_ERR_TRUNCATED when cap is smaller. */
+/* String-mod lines of prm->string_mod (string_mod.rs:33-158): modulo of them, or with a
+ * nested mod the nested modulo (none when the lines do not cross), written to out[0..n).
+ * *n_out receives the count; LGO_ERR_TRUNCATED when cap is smaller. */
 int lgo_string_mod_chords(const lg_params* prm, lg_chord* out, uint64_t cap, uint64_t* n_out);
+/* Crossing points of the mod's lines in the order of StringMod::line_crossings_as_points
+ * (string_mod.rs:87-102), as (x, y) pairs: up to cap of them to xy (NULL: count only);
+ * *n_out receives the count, LGO_ERR_TRUNCATED when cap is smaller. */
+int lgo_string_mod_crossings(const lg_string_mod* sm, double* xy, uint64_t cap, uint64_t* n_out);
 /* Raster of string-mod lines (the segment raster rule, colour interpolated along the major
  * axis as include/lg.h states for lg_chord), into the same images as lgo_raster(_f64). */
 int lgo_raster_chords(const lg_chord* chords, uint64_t n, const lg_params* prm, int64_t* accum,

@@ -19,6 +19,9 @@ HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liblg_oracle.so"
 
 
+LGO_ERR_TRUNCATED = -6  # lg_oracle.h
+
+
 class lgo_stats(C.Structure):
     _fields_ = [("primary_rays", C.c_uint64), ("ray_visits", C.c_uint64), ("segments", C.c_uint64),
                 ("near_degenerate", C.c_uint64), ("pixels", C.c_uint64), ("seconds", C.c_double)]
@@ -65,6 +68,7 @@ def lib() -> C.CDLL:
         L.lgo_raster_f64.argtypes = [P(abi.lg_segment), C.c_uint64, P(abi.lg_params), P(C.c_double),
                                      P(C.c_uint64)]
         L.lgo_string_mod_chords.argtypes = [P(abi.lg_params), P(abi.lg_chord), C.c_uint64, P(C.c_uint64)]
+        L.lgo_string_mod_crossings.argtypes = [P(abi.lg_string_mod), P(C.c_double), C.c_uint64, P(C.c_uint64)]
         L.lgo_raster_chords.argtypes = [P(abi.lg_chord), C.c_uint64, P(abi.lg_params), P(C.c_int64), P(C.c_uint64)]
         L.lgo_raster_chords_f64.argtypes = [P(abi.lg_chord), C.c_uint64, P(abi.lg_params), P(C.c_double),
                                             P(C.c_uint64)]
@@ -152,11 +156,28 @@ def clear(params) -> np.ndarray:
 def string_mod_chords(params) -> np.ndarray:
     """The string-mod lines of params.string_mod (lgo_string_mod_chords)."""
     n = C.c_uint64(0)
-    m = int(params.string_mod.modulo)
-    out = np.zeros(m, abi.chord_dtype())
-    rc = lib().lgo_string_mod_chords(C.byref(params), out.ctypes.data_as(C.POINTER(abi.lg_chord)), m, C.byref(n))
+    rc = lib().lgo_string_mod_chords(C.byref(params), None, 0, C.byref(n))
+    if rc not in (0, LGO_ERR_TRUNCATED):
+        raise OracleError(f"lgo_string_mod_chords: {rc}")
+    out = np.zeros(int(n.value), abi.chord_dtype())
+    rc = lib().lgo_string_mod_chords(C.byref(params), out.ctypes.data_as(C.POINTER(abi.lg_chord)), len(out),
+                                     C.byref(n))
     if rc:
         raise OracleError(f"lgo_string_mod_chords: {rc}")
+    return out
+
+
+def string_mod_crossings(sm) -> np.ndarray:
+    """Crossing points of the lines of an lg_string_mod, (n, 2) FP64 (lgo_string_mod_crossings)."""
+    n = C.c_uint64(0)
+    rc = lib().lgo_string_mod_crossings(C.byref(sm), None, 0, C.byref(n))
+    if rc:
+        raise OracleError(f"lgo_string_mod_crossings: {rc}")
+    out = np.zeros((int(n.value), 2), np.float64)
+    rc = lib().lgo_string_mod_crossings(C.byref(sm), out.ctypes.data_as(C.POINTER(C.c_double)), len(out),
+                                        C.byref(n))
+    if rc:
+        raise OracleError(f"lgo_string_mod_crossings: {rc}")
     return out
 
 

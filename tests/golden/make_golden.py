@@ -37,6 +37,8 @@ CASES = {
 for _curve, _name in ((abi.LG_CURVE_CIRCLE, "circle"), (abi.LG_CURVE_COMPLEX_EXP, "complex_exp"),
                       (abi.LG_CURVE_HYPOTROCHOID, "hypotrochoid"), (abi.LG_CURVE_LISSAJOUS, "lissajous")):
     CASES[f"string_mod_{_name}"] = ((lambda c=_curve: W.string_mod_art(c)), 1, True)
+# a nested mod over the crossings of a hypotrochoid mod's lines (StringMod::nested)
+CASES["nested_string_mod_hypotrochoid"] = ((lambda: W.nested_string_mod_art(abi.LG_CURVE_HYPOTROCHOID)), 1, True)
 
 
 def canonical(segs, paths, s64):
@@ -64,16 +66,19 @@ def run_case(name: str):
     return segs, paths, s64, chords, meta
 
 
-def main():
+def main(names=None):
+    """Writes the fixtures of ``names`` (every case when none are given) and their entries in
+    golden.json, keeping the other entries."""
     O.build()
-    index = {}
-    for name in CASES:
+    path = HERE / "golden.json"
+    index = json.loads(path.read_text()) if names and path.exists() else {}
+    for name in names or CASES:
         segs, paths, s64, chords, meta = run_case(name)
         np.savez_compressed(HERE / f"{name}.npz", segs=segs, paths=paths, s64=s64, chords=chords)
         index[name] = meta
         print(name, meta)
-    (HERE / "golden.json").write_text(json.dumps(index, indent=1, sort_keys=True) + "\n")
+    path.write_text(json.dumps(index, indent=1, sort_keys=True) + "\n")
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -52,7 +52,7 @@ def c_layout(tmp_path_factory):
 def test_header_compiles_as_c_and_cxx(tmp_path):
     for cc, ext in (("gcc", "c"), ("g++", "cpp")):
         src = tmp_path / f"h.{ext}"
-        src.write_text(f'#include "{HEADER}"\nint main(void) {{ return LG_ABI_VERSION == 4 ? 0 : 1; }}\n')
+        src.write_text(f'#include "{HEADER}"\nint main(void) {{ return LG_ABI_VERSION == 5 ? 0 : 1; }}\n')
         subprocess.run([cc, "-Wall", "-Werror", "-pedantic", "-o", str(tmp_path / f"h_{ext}"), str(src)],
                        check=True)
 
@@ -97,7 +97,7 @@ def test_library_exports_only_the_abi(cuda_lib):
 
 
 def test_abi_version_and_defaults(cuda_lib):
-    assert cuda_lib.lg_abi_version() == 4
+    assert cuda_lib.lg_abi_version() == 5
     p = abi.lg_params()
     cuda_lib.lg_params_default(C.byref(p))
     assert p.max_bounce == 5  # Tracer::new, tracer.rs:37

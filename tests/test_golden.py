@@ -134,6 +134,20 @@ def test_gpu_default_scene_from_ron_matches_fixture(ctx):
 
 
 @pytest.mark.gpu
+def test_gpu_nested_string_mod_matches_fixture(ctx):
+    """A nested mod over the crossings of a hypotrochoid mod's lines: the GPU's lines equal
+    the stored ones bit for bit, and its rendered frame has the stored image digests."""
+    name = "nested_string_mod_hypotrochoid"
+    meta = INDEX[name]
+    ctx.upload(W.nested_string_mod_art(abi.LG_CURVE_HYPOTROCHOID).packed())
+    img, st = ctx.render()
+    assert ctx.chords().tobytes() == load_chords(name).tobytes()
+    assert st["pixels"] == meta["pixels"]
+    assert digest(ctx.accum()) == meta["accum_sha256"]
+    assert digest(img) == meta["f16_sha256"]
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("name", [n for n in sorted(INDEX) if n.startswith("string_mod_")])
 def test_gpu_string_mod_art_matches_fixture(ctx, name):
     """String-mod line art on each curve with modulo colours: the GPU's lines equal the stored

@@ -217,6 +217,56 @@ def test_string_mod_lines_and_blends_exact(ctx, oracle, curve):
     assert (np.abs(acc - f64) <= tol).all(), (np.abs(acc - f64) / tol).max()
 
 
+@pytest.mark.parametrize("curve", [abi.LG_CURVE_CIRCLE, abi.LG_CURVE_COMPLEX_EXP, abi.LG_CURVE_HYPOTROCHOID,
+                                   abi.LG_CURVE_LISSAJOUS])
+def test_nested_string_mod_exact(ctx, oracle, curve):
+    """A nested mod over the crossings of 400 lines of each curve: the crossings (computed on
+    the GPU at upload), the nested lines and the image equal the oracle's bit for bit."""
+    w = W.nested_string_mod_art(curve, 768, 512)
+    _trace_exact(ctx, oracle, w.packed(), image=True)
+    assert len(ctx.chords()) == 6000
+
+
+def test_nested_string_mod_at_the_limit_and_edge_cases(ctx, oracle):
+    # 4096 outer lines: 16.8 M line pairs in 4096 blocks, about 6 M crossings
+    pk = W.nested_string_mod_art(abi.LG_CURVE_CIRCLE, 1024, 1024, outer_modulo=4096).packed()
+    _trace_exact(ctx, oracle, pk, image=True)
+    # the same scene with another nested mod: the new lines, not the old ones
+    ns = abi.lg_string_mod()
+    ns.modulo, ns.num, ns.mode = 2500, 3, abi.LG_SM_POW
+    ns.color[:] = (0.2, 1.0, 0.4, 1.0)
+    abi.set_nested(pk.params, ns)
+    _trace_exact(ctx, oracle, pk, image=True)
+    assert len(ctx.chords()) == 2500
+    # lines that never cross (each from a point to itself): no nested lines, and the image is
+    # the trace's alone
+    pk = W.nested_string_mod_art(abi.LG_CURVE_CIRCLE, 256, 256, outer_modulo=64).packed()
+    pk.params.string_mod.mode, pk.params.string_mod.num = abi.LG_SM_ADD, 0
+    _trace_exact(ctx, oracle, pk, image=True)
+    assert len(ctx.chords()) == 0
+    # one outer line: no pairs at all
+    pk = W.nested_string_mod_art(abi.LG_CURVE_CIRCLE, 256, 256, outer_modulo=1).packed()
+    _trace_exact(ctx, oracle, pk, image=True)
+    assert len(ctx.chords()) == 0
+
+
+def test_nested_string_mod_rejects_bad_parameters(ctx):
+    pk = W.nested_string_mod_art(abi.LG_CURVE_CIRCLE, 256, 256,
+                                 outer_modulo=abi.LG_STRING_MOD_NESTED_MAX + 1).packed()
+    with pytest.raises(abi.LgError) as e:
+        ctx.upload(pk)
+    assert e.value.status == abi.LG_ERR_UNSUPPORTED
+    for field, value in (("mode", 4), ("modulo", (1 << 26) + 1)):
+        pk = W.nested_string_mod_art(abi.LG_CURVE_CIRCLE, 256, 256).packed()
+        ns = abi.lg_string_mod()
+        ns.modulo, ns.num, ns.mode = 100, 3, abi.LG_SM_ADD
+        setattr(ns, field, value)
+        abi.set_nested(pk.params, ns)
+        with pytest.raises(abi.LgError) as e:
+            ctx.upload(pk)
+        assert e.value.status == abi.LG_ERR_INVALID_ARGUMENT
+
+
 def test_string_mod_lines_dropped_by_accumulate_segments(ctx, oracle):
     pk = W.string_mod_art(abi.LG_CURVE_CIRCLE, 256, 256).packed()
     ctx.upload(pk)

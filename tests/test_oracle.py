@@ -561,6 +561,140 @@ def test_string_mod_curves(oracle):
         assert ch[i]["y0"] == pytest.approx(math.sin(4 * a), abs=1e-6)
 
 
+# ---- nested string mods (StringMod::line_crossings_as_points, string_mod.rs:87-102, 152-158) ---
+def nested_mod(m, num, mode, colors=(), color=(0.6, 0.2, 0.1, 1.0)):
+    ns = abi.lg_string_mod()
+    ns.modulo, ns.num, ns.mode = m, num, mode
+    ns.color[:] = color
+    holder = abi.params_default()
+    abi.set_mod_colors(holder, colors)
+    ns.n_colors, ns.colors = holder.string_mod.n_colors, holder.string_mod.colors
+    return ns
+
+
+def _target(m, num, mode, i):
+    if mode == abi.LG_SM_ADD:
+        return (i + num) % m
+    if mode == abi.LG_SM_MUL:
+        return (i * num) % (1 << 64) % m
+    if mode == abi.LG_SM_POW:
+        return pow(i, num & 0xffffffff, 1 << 64) % m
+    return pow(num, i & 0xffffffff, 1 << 64) % m
+
+
+def _cpow(re, im, e):
+    # binary powering with each product rounded on its own (Python floats are IEEE doubles)
+    if e == 0:
+        return 1.0, 0.0
+    br, bi = re, im
+    while e & 1 == 0:
+        br, bi = br * br - bi * bi, br * bi + bi * br
+        e >>= 1
+    if e == 1:
+        return br, bi
+    ar, ai = br, bi
+    while e > 1:
+        e >>= 1
+        br, bi = br * br - bi * bi, br * bi + bi * br
+        if e & 1:
+            ar, ai = ar * br - ai * bi, ar * bi + ai * br
+    return ar, ai
+
+
+def _cross(a, b, c, d):
+    rx, ry, sx, sy = b[0] - a[0], b[1] - a[1], d[0] - c[0], d[1] - c[1]
+    den = rx * sy - ry * sx
+    if den == 0.0:
+        return None
+    wx, wy = c[0] - a[0], c[1] - a[1]
+    t = (wx * sy - wy * sx) / den
+    u = (wx * ry - wy * rx) / den
+    if not (0.0 <= t <= 1.0 and 0.0 <= u <= 1.0):
+        return None
+    return a[0] + rx * t, a[1] + ry * t
+
+
+def test_nested_string_mod_restated_bit_for_bit(oracle):
+    """The crossings and the nested lines restated in Python on the complex-power curve (whose
+    points are products only, so the restatement is exact): the oracle's FP64 crossing points,
+    their order (diff outer, line inner, every crossing twice) and the nested lines' f32
+    endpoints and averaged colours equal it bit for bit."""
+    m, num, mode = 48, 5, abi.LG_SM_MUL
+    th = 2 * math.pi / 48
+    c = (0.999 * math.cos(th), 0.999 * math.sin(th))
+    p = sm_params(m, num, mode, abi.LG_CURVE_COMPLEX_EXP, turns=1, cf=c)
+    pts = [_cpow(c[0], c[1], (1 * n) & 0xffffffff) for n in range(m)]
+    lines = [(pts[i % m], pts[_target(m, num, mode, i) % m]) for i in range(m)]
+    want = []
+    for diff in range(1, m):
+        for a in range(m):
+            q = _cross(*lines[a], *lines[(a + diff) % m])
+            if q is not None:
+                want.append(q)
+    got = oracle.string_mod_crossings(p.string_mod)
+    assert len(want) > 500
+    assert got.tolist() == [list(q) for q in want]
+    red, blue = (1.0, 0.0, 0.0, 1.0), (0.0, 0.2, 1.0, 0.5)
+    table = [(3, 1, red), (4, 0, blue)]
+    ns = nested_mod(700, 11, abi.LG_SM_ADD, table)
+    abi.set_nested(p, ns)
+    ch = oracle.string_mod_chords(p)
+    assert len(ch) == 700
+
+    def colour(ix):
+        hit = [col for (mo, r, col) in table if ix % mo == r]
+        if not hit:
+            return [np.float32(v) for v in (0.6, 0.2, 0.1, 1.0)]
+        acc = [np.float32(0.0)] * 4
+        for col in hit:
+            acc = [np.float32(a + np.float32(v)) for a, v in zip(acc, col)]
+        return [np.float32(a / np.float32(len(hit))) for a in acc]
+
+    n = len(want)
+    for i in range(700):
+        j = (i + 11) % 700
+        a, b = want[i % n], want[j % n]
+        assert (ch[i]["x0"], ch[i]["y0"], ch[i]["x1"], ch[i]["y1"]) == \
+            tuple(np.float32(v) for v in (a[0], a[1], b[0], b[1]))
+        assert ch[i]["color0"].tolist() == [float(v) for v in colour(i)]
+        assert ch[i]["color1"].tolist() == [float(v) for v in colour(j)]
+
+
+def test_nested_string_mod_known_answers(oracle):
+    # two diameters, each drawn both ways (ADD 2 on 4 circle points): a horizontal and a vertical
+    # line cross at the centre, a line and its reverse are parallel (determinant exactly 0):
+    # 8 crossings, all at the origin up to the rounding of cos(pi / 2)
+    p = sm_params(4, 2, abi.LG_SM_ADD)
+    got = oracle.string_mod_crossings(p.string_mod)
+    assert got.shape == (8, 2) and np.abs(got).max() < 1e-15
+    abi.set_nested(p, nested_mod(5, 1, abi.LG_SM_ADD))
+    assert len(oracle.string_mod_chords(p)) == 5
+    # every line from a point to itself (ADD 0): no crossings, so no nested lines
+    p = sm_params(16, 0, abi.LG_SM_ADD)
+    assert len(oracle.string_mod_crossings(p.string_mod)) == 0
+    abi.set_nested(p, nested_mod(9, 1, abi.LG_SM_ADD))
+    assert len(oracle.string_mod_chords(p)) == 0
+    # a nested mod of modulo 0 draws nothing; an outer mod of modulo 0 disables the overlay
+    p = sm_params(12, 5, abi.LG_SM_MUL)
+    abi.set_nested(p, nested_mod(0, 1, abi.LG_SM_ADD))
+    assert len(oracle.string_mod_chords(p)) == 0
+    p = sm_params(0, 5, abi.LG_SM_MUL)
+    abi.set_nested(p, nested_mod(9, 1, abi.LG_SM_ADD))
+    assert len(oracle.string_mod_chords(p)) == 0
+    # limits: the outer modulo of a nested mod, the nested mode and colour table
+    p = sm_params(abi.LG_STRING_MOD_NESTED_MAX + 1, 5, abi.LG_SM_MUL)
+    abi.set_nested(p, nested_mod(9, 1, abi.LG_SM_ADD))
+    with pytest.raises(oracle.OracleError):
+        oracle.string_mod_chords(p)
+    p = sm_params(12, 5, abi.LG_SM_MUL)
+    abi.set_nested(p, nested_mod(9, 1, 7))
+    with pytest.raises(oracle.OracleError):
+        oracle.string_mod_chords(p)
+    abi.set_nested(p, nested_mod(9, 1, abi.LG_SM_ADD, [(0, 0, (1, 1, 1, 1))]))
+    with pytest.raises(oracle.OracleError):
+        oracle.string_mod_chords(p)
+
+
 def test_chord_colour_is_interpolated_along_the_major_axis(oracle):
     p = raster_params()
     ch = np.zeros(2, abi.chord_dtype())
