@@ -17,8 +17,8 @@ memory every step).  ``roofline``: the frame's longest kernel stage against the 
 the resource it uses, measured in the same process (liblg_peaks.so).  ``cpu_baseline``: the
 CPU restatement of the reference tracer (the reference is Rust and cannot be built) on all
 host cores over a sample of the primaries, and the GPU's image of the same sample compared
-with it.  The extra keys (``mid_scene``, ``fast_precision``, ``batch``, ``serve``) measure the
-other configurations on the same GPU.
+with it.  The extra keys (``mid_scene``, ``image_errors``, ``fast_precision``, ``batch``,
+``serve``, ``serve_load``) measure the other configurations on the same GPU.
 ``--impl reference`` times that CPU restatement alone, one sample per step.
 """
 from __future__ import annotations
@@ -475,8 +475,10 @@ def batch_graph(local, args, ray_scale=None):
 
 
 def serve_bench(local, args, rate=100.0, count=256, ray_scale=1.0 / 16):
-    """Poisson arrivals below the server's capacity: scenes/s and p50/p99 latency of the
-    continuous-batching server against the plain path serving the same arrivals in order."""
+    """Poisson arrivals: scenes/s and p50/p99 latency of the continuous-batching server against
+    the plain path serving the same arrivals in order.  At 100 requests/s the load is below
+    either path's capacity (the latencies are service times); at 200 requests/s, the bottom of
+    the serving configuration's range, it is above it and the latencies include queueing."""
     import numpy as np
     import torch
     from light_garden_gb300 import workloads as W
@@ -663,6 +665,7 @@ def run_ours(args, ws, rank, local):
         extra("fast_precision", fast)
         extra("batch", lambda: batch_bench(local, args))
         extra("serve", lambda: serve_bench(local, args))
+        extra("serve_load", lambda: serve_bench(local, args, rate=200.0))
 
     # light setup, 3 trace kernels per generation, overlay, accumulation clear, resolve, string-mod lines
     G = pk.params.max_bounce
