@@ -2,7 +2,7 @@
 
 The reference ships no tests and its geometry crate is not on disk, so these analytic cases
 (plus the committed golden fixtures of ``test_golden.py``) are what pins the oracle before
-it is used to judge the CUDA path.  Each case states the mathematics it checks.
+it is used to check the CUDA path.  Each case states the mathematics it checks.
 """
 import math
 
