@@ -9,7 +9,9 @@ Mirrors light_garden's scene types:
   :class:`Object` with the constructors ``new_mirror``, ``new_curved_mirror``,
   ``new_circle``, ``new_rect``, ``new_lens``, ``new_geo`` and ``material_opt``;
 * lights    (``Light``, src/light_garden/light.rs:10-14): :class:`PointLight`,
-  :class:`SpotLight`, :class:`DirectionalLight`.
+  :class:`SpotLight`, :class:`DirectionalLight`;
+* string mods (src/light_garden/string_mod.rs): :class:`StringMod`, :class:`Curve`,
+  :class:`ModRemColor`, :class:`StringModMode`, filling ``lg_params.string_mod``.
 
 :func:`pack` flattens a list of objects and lights into ``lg_geo``/``lg_object``/
 ``lg_light`` arrays: one node array holding every geometry tree, objects naming their
@@ -347,3 +349,78 @@ def canvas_bounds(width: int, height: int) -> Rect:
 def rotation(angle: float) -> Tuple[float, float]:
     """A Rot2 as (cos, sin)."""
     return _rot(angle)
+
+
+# ---- string mods (src/light_garden/string_mod.rs) ------------------------------------------------
+class StringModMode:
+    """StringModMode (string_mod.rs:174-180)."""
+    Add, Mul, Pow, Base = abi.LG_SM_ADD, abi.LG_SM_MUL, abi.LG_SM_POW, abi.LG_SM_BASE
+
+
+@dataclass
+class Curve:
+    """Curve (string_mod.rs:182-188): ``Curve.circle()``, ``Curve.complex_exp(c)``,
+    ``Curve.hypotrochoid(r, s, d)``, ``Curve.lissajous(a, b, delta)``."""
+    kind: int = abi.LG_CURVE_CIRCLE
+    f: Tuple[float, float] = (0.0, 0.0)
+    u: Tuple[int, int, int] = (0, 0, 0)
+
+    @staticmethod
+    def circle() -> "Curve":
+        return Curve()
+
+    @staticmethod
+    def complex_exp(c: complex) -> "Curve":
+        return Curve(abi.LG_CURVE_COMPLEX_EXP, (float(c.real), float(c.imag)))
+
+    @staticmethod
+    def hypotrochoid(r: int, s: int, d: int) -> "Curve":
+        return Curve(abi.LG_CURVE_HYPOTROCHOID, u=(int(r), int(s), int(d)))
+
+    @staticmethod
+    def lissajous(a: int, b: int, delta: float) -> "Curve":
+        return Curve(abi.LG_CURVE_LISSAJOUS, (float(delta), 0.0), (int(a), int(b), 0))
+
+
+@dataclass
+class ModRemColor:
+    """ModRemColor (string_mod.rs:167-172): point n takes ``color`` when n % modulo == rem."""
+    modulo: int
+    rem: int
+    color: Color
+
+
+@dataclass
+class StringMod:
+    """StringMod (string_mod.rs:3-31) with the reference's defaults (``StringMod::new``).
+    ``pow`` and ``modulo_color_index`` are GUI state of the reference and do not change what
+    is drawn."""
+    modulo: int = 5
+    num: int = 1
+    pow: int = 0
+    color: Color = (1.0, 1.0, 1.0, 1.0)
+    turns: int = 1
+    init_curve: Curve = field(default_factory=Curve)
+    mode: int = StringModMode.Mul
+    modulo_colors: List[ModRemColor] = field(default_factory=list)
+    modulo_color_index: int = 0
+    nested: Optional["StringMod"] = None
+
+    def to_abi(self) -> abi.lg_string_mod:
+        """The lg_string_mod of this mod (its colour table and nested mod kept alive by abi)."""
+        holder = abi.params_default()
+        sm = holder.string_mod
+        sm.modulo, sm.num, sm.turns, sm.mode, sm.curve = self.modulo, self.num, self.turns, self.mode, \
+            self.init_curve.kind
+        sm.color[:] = tuple(float(x) for x in self.color)
+        sm.curve_f[:] = self.init_curve.f
+        sm.curve_u[:] = self.init_curve.u
+        abi.set_mod_colors(holder, [(c.modulo, c.rem, c.color) for c in self.modulo_colors])
+        if self.nested is not None:
+            abi.set_nested(holder, self.nested.to_abi())
+        return holder.string_mod
+
+    def apply(self, params: abi.lg_params) -> abi.lg_params:
+        """Draw this mod over the frame of ``params`` (StringMod::draw, string_mod.rs:152-158)."""
+        params.string_mod = self.to_abi()
+        return params

@@ -111,6 +111,40 @@ def test_scale_rays():
     assert w2.primary_rays == 8 << 12 and w.primary_rays == 8 << 18
 
 
+def test_string_mod_types_mirror_the_reference():
+    """StringMod / Curve / ModRemColor / StringModMode with the reference's names and defaults
+    (StringMod::new, string_mod.rs:18-31) fill lg_params.string_mod, nested mod included, exactly
+    as the nested workload sets it field by field."""
+    d = S.StringMod()
+    assert (d.modulo, d.num, d.pow, d.color, d.turns, d.init_curve, d.mode, d.modulo_colors, d.modulo_color_index,
+            d.nested) == (5, 1, 0, (1.0, 1.0, 1.0, 1.0), 1, S.Curve.circle(), S.StringModMode.Mul, [], 0, None)
+    sm = S.StringMod(modulo=400, num=13, color=(0.3, 0.3, 0.3, 1.0), turns=3, init_curve=S.Curve.hypotrochoid(3, 5, 2),
+                     modulo_colors=[S.ModRemColor(4, 3, (0.0, 1.0, 1.0, 1.0))],
+                     nested=S.StringMod(modulo=6000, num=17, color=(0.9, 0.9, 0.2, 1.0), mode=S.StringModMode.Add,
+                                        modulo_colors=[S.ModRemColor(5, 1, (0.1, 0.8, 1.0, 1.0)),
+                                                       S.ModRemColor(7, 3, (1.0, 0.5, 0.0, 0.7))]))
+    mine = sm.apply(abi.params_default()).string_mod
+    ref = W.nested_string_mod_art(abi.LG_CURVE_HYPOTROCHOID).params.string_mod
+
+    def fields(x, skip=()):
+        return {f: (list(getattr(x, f)) if hasattr(getattr(x, f), "__len__") else getattr(x, f))
+                for f, *_ in x._fields_ if f not in ("colors", "nested") + skip}
+
+    def table(x):
+        return [(e.modulo, e.rem, list(e.color)) for e in (abi.lg_mod_color * x.n_colors).from_address(x.colors)] \
+            if x.n_colors else []
+
+    assert fields(mine) == fields(ref) and table(mine) == table(ref)
+    nm = abi.lg_string_mod.from_address(mine.nested)
+    nr = abi.lg_string_mod.from_address(ref.nested)
+    unused = ("turns", "curve", "curve_f", "curve_u")  # a nested mod's points are the crossings
+    assert fields(nm, unused) == fields(nr, unused) and table(nm) == table(nr)
+    c = S.Curve.complex_exp(complex(0.6, 0.8))
+    assert (c.kind, c.f) == (abi.LG_CURVE_COMPLEX_EXP, (0.6, 0.8))
+    c = S.Curve.lissajous(3, 4, 0.5)
+    assert (c.kind, c.f, c.u) == (abi.LG_CURVE_LISSAJOUS, (0.5, 0.0), (3, 4, 0))
+
+
 def test_tracer_list_api_matches_the_reference_surface():
     """tracer.rs:48-129: push / index / replace / remove / clear, without touching the GPU."""
     t = Tracer(1920, 1080)
