@@ -350,7 +350,9 @@ uint32_t lg_abi_version(void);
 /* ---- one scene ------------------------------------------------------------------------ */
 /* Copies a scene (geometry trees, objects, lights, parameters) to the device.  Replaces
  * the whole object/light list, like Tracer::clear + push_object/push_light
- * (tracer.rs:54-94) followed by Light::set_num_rays (light.rs:45-51). */
+ * (tracer.rs:54-94) followed by Light::set_num_rays (light.rs:45-51).  A call rejected by
+ * its argument checks keeps the previous scene; one that fails later (device memory) leaves
+ * no scene (LG_ERR_NO_SCENE until the next successful upload). */
 lg_status lg_scene_upload(lg_ctx* ctx, const lg_geo* geos, uint32_t n_geo,
                           const lg_object* objects, uint32_t n_objects,
                           const lg_light* lights, uint32_t n_lights, const lg_params* params);

@@ -1239,8 +1239,6 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
   st = flatten_scene(c->err, geos, n_geo, objects, n_objects, lights, n_lights, F);
   if (st) return st;
   if ((st = validate_exact(c->err, p, F))) return st;
-  CK(cudaStreamSynchronize(c->stream), "synchronize");
-  if ((st = upload_exact(c, F))) return st;
   lg_params pk = p;  // kept without the caller's colour-table and nested-mod pointers
   pk.string_mod.colors = nullptr;
   pk.string_mod.nested = nullptr;
@@ -1255,6 +1253,12 @@ lg_status lg_scene_upload(lg_ctx* c, const lg_geo* geos, uint32_t n_geo, const l
                           c->n_prog == F.prog.size() && c->n_lights == n_lights && c->n_cubic == F.cubics.size() &&
                           std::memcmp(&c->prm, &pk, sizeof pk) == 0 && c->has_nested == nested &&
                           std::memcmp(&c->nested, &nk, sizeof nk) == 0;
+  // From here on the device tables are replaced: until this upload completes there is no scene
+  // to trace, so a failure below leaves LG_ERR_NO_SCENE rather than a mix of two scenes (whose
+  // line counts could exceed the line table).
+  c->has_scene = false;
+  CK(cudaStreamSynchronize(c->stream), "synchronize");
+  if ((st = upload_exact(c, F))) return st;
   if (p.string_mod.modulo) {
     // the mod drawn: the nested one (between the crossings of this mod's lines), else this one
     const lg_string_mod& drawn = nested ? *p.string_mod.nested : p.string_mod;
