@@ -331,6 +331,9 @@ lg_status lg_batch_upload(lg_ctx* c, const lg_scene_desc* scenes, uint32_t k) {
   c->prm.string_mod.modulo = 0;
   c->prm.string_mod.n_colors = 0;
   c->prm.string_mod.colors = nullptr;
+  c->prm.string_mod.nested = nullptr;
+  c->has_nested = false;
+  c->n_cross = 0;
   c->chords_ready = 0;
   c->total_px = total_px;
   c->total_bins = (uint32_t)total_bins;

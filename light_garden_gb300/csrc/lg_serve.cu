@@ -447,6 +447,9 @@ lg_status lg_serve_submit(lg_ctx* c, const lg_scene_desc* d, uint64_t* id_out) {
     V.have_common = true;
     c->prm = p;  // blend state for the raster
     c->prm.string_mod.colors = nullptr;
+    c->prm.string_mod.nested = nullptr;
+    c->has_nested = false;
+    c->n_cross = 0;
     c->chords_ready = 0;
   }
   R.id = V.next_id++;
