@@ -1020,6 +1020,11 @@ static int seg_cross(double ax, double ay, double bx, double by, double cx, doub
   return 1;
 }
 
+int lgo_seg_cross(double ax, double ay, double bx, double by, double cx, double cy, double dx, double dy,
+                  double* px, double* py) {
+  return seg_cross(ax, ay, bx, by, cx, cy, dx, dy, px, py);
+}
+
 /* StringMod::line_crossings_as_points (string_mod.rs:87-102): the lines of the mod's own
  * draw, then for diff = 1 .. m-1 and a = 0 .. m-1 the crossing of line a with line
  * (a + diff) % m.  Writes up to cap points (x, y) to xy; *n_out = all crossings. */

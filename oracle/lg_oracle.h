@@ -60,6 +60,10 @@ int lgo_string_mod_chords(const lg_params* prm, lg_chord* out, uint64_t cap, uin
  * (string_mod.rs:87-102), as (x, y) pairs: up to cap of them to xy (NULL: count only);
  * *n_out receives the count, LGO_ERR_TRUNCATED when cap is smaller. */
 int lgo_string_mod_crossings(const lg_string_mod* sm, double* xy, uint64_t cap, uint64_t* n_out);
+/* The crossing of segments ab and cd that lgo_string_mod_crossings uses (include/lg.h states it
+ * for lg_string_mod.nested): 1 and the point when they cross, else 0. */
+int lgo_seg_cross(double ax, double ay, double bx, double by, double cx, double cy, double dx, double dy,
+                  double* px, double* py);
 /* Raster of string-mod lines (the segment raster rule, colour interpolated along the major
  * axis as include/lg.h states for lg_chord), into the same images as lgo_raster(_f64). */
 int lgo_raster_chords(const lg_chord* chords, uint64_t n, const lg_params* prm, int64_t* accum,

@@ -69,6 +69,7 @@ def lib() -> C.CDLL:
                                      P(C.c_uint64)]
         L.lgo_string_mod_chords.argtypes = [P(abi.lg_params), P(abi.lg_chord), C.c_uint64, P(C.c_uint64)]
         L.lgo_string_mod_crossings.argtypes = [P(abi.lg_string_mod), P(C.c_double), C.c_uint64, P(C.c_uint64)]
+        L.lgo_seg_cross.argtypes = [C.c_double] * 8 + [P(C.c_double), P(C.c_double)]
         L.lgo_raster_chords.argtypes = [P(abi.lg_chord), C.c_uint64, P(abi.lg_params), P(C.c_int64), P(C.c_uint64)]
         L.lgo_raster_chords_f64.argtypes = [P(abi.lg_chord), C.c_uint64, P(abi.lg_params), P(C.c_double),
                                             P(C.c_uint64)]
@@ -165,6 +166,14 @@ def string_mod_chords(params) -> np.ndarray:
     if rc:
         raise OracleError(f"lgo_string_mod_chords: {rc}")
     return out
+
+
+def seg_cross(a, b, c, d):
+    """The crossing point of segments ab and cd, or None (lgo_seg_cross)."""
+    x, y = C.c_double(0.0), C.c_double(0.0)
+    if lib().lgo_seg_cross(a[0], a[1], b[0], b[1], c[0], c[1], d[0], d[1], C.byref(x), C.byref(y)):
+        return x.value, y.value
+    return None
 
 
 def string_mod_crossings(sm) -> np.ndarray:

@@ -614,6 +614,27 @@ def _cross(a, b, c, d):
     return a[0] + rx * t, a[1] + ry * t
 
 
+def test_segment_crossing_known_answers(oracle):
+    """The crossing definition of nested string mods: a + t (b - a) = c + u (d - c) with a
+    non-zero determinant and t, u in [0, 1] (both ends included)."""
+    # an X: the diagonals of the unit square cross at its centre, t = u = 1/2 exactly
+    assert oracle.seg_cross((0, 0), (1, 1), (0, 1), (1, 0)) == (0.5, 0.5)
+    # a T: c d passes through b, t = 1 exactly, u = 1/2
+    assert oracle.seg_cross((0, 0), (1, 0), (1, -1), (1, 1)) == (1.0, 0.0)
+    # sharing an end point: w = c - a = 0, so t = u = 0
+    assert oracle.seg_cross((0.25, 0.5), (1, 2), (0.25, 0.5), (-3, 1)) == (0.25, 0.5)
+    # stopping short of the other line (t > 1), and missing its extent (u > 1)
+    assert oracle.seg_cross((0, 0), (0.9, 0), (1, -1), (1, 1)) is None
+    assert oracle.seg_cross((0, 0), (2, 0), (1, 0.5), (1, 2)) is None
+    # parallel, collinear and overlapping, and a zero-length line: the determinant is 0
+    assert oracle.seg_cross((0, 0), (1, 0), (0, 1), (1, 1)) is None
+    assert oracle.seg_cross((0, 0), (2, 0), (1, 0), (3, 0)) is None
+    assert oracle.seg_cross((0.5, 0.5), (0.5, 0.5), (0, 0), (1, 1)) is None
+    # the point is taken on the first line: a + t (b - a)
+    p = oracle.seg_cross((0, 0), (3, 1), (0, 1), (3, 0))
+    assert p == (0 + 3 * 0.5, 0 + 1 * 0.5)
+
+
 def test_nested_string_mod_restated_bit_for_bit(oracle):
     """The crossings and the nested lines restated in Python on the complex-power curve (whose
     points are products only, so the restatement is exact): the oracle's FP64 crossing points,
