@@ -1170,7 +1170,7 @@ __device__ void string_mod_point(const lg_string_mod& sm, uint64_t n, double& x,
 }
 
 // The point that line iix of a string mod joins to point iix, by the mod's mode
-// (string_mod.rs:110-115; u64 arithmetic wrapping like Rust's release build).
+// (string_mod.rs:112-117; u64 arithmetic wrapping like Rust's release build).
 __device__ __forceinline__ uint64_t string_mod_target(const lg_string_mod& sm, uint64_t iix) {
   const uint64_t m = sm.modulo;
   if (sm.mode == LG_SM_ADD) return (iix + sm.num) % m;
@@ -1234,7 +1234,7 @@ __global__ void k_overlay(SceneDev S, TraceBufs B, const uint32_t* cubic_objs, c
       const uint64_t m = sm.modulo, iix = i - n_ctrl;
       const uint64_t ix = string_mod_target(sm, iix);
       double xa, ya, xb, yb;
-      if (CA.pts) {  // nested: points iix and ix of the outer mod's crossings (string_mod.rs:116-117)
+      if (CA.pts) {  // nested: points iix and ix of the outer mod's crossings (string_mod.rs:118-119)
         const double2 pa = CA.pts[iix % CA.n_pts], pb = CA.pts[ix % CA.n_pts];
         xa = pa.x; ya = pa.y; xb = pb.x; yb = pb.y;
       } else {
